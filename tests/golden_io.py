@@ -1,0 +1,44 @@
+"""Loader for tests/golden/tg_predicates.npz (made by tests/golden/gen_golden.py)."""
+import os
+
+import numpy as np
+
+from sedona_gpuspatial.wkb import WkbColumn
+
+PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tg_predicates.npz")
+
+
+def load():
+    z = np.load(PATH)
+    cols = {}
+    for name in ("polys", "holed", "pts"):
+        cols[name] = WkbColumn(z[name + "_offsets"].astype(np.int32), z[name + "_data"])
+    return z, cols
+
+
+def table(z, name):
+    """Yields (pred_code, build_rows, probe_rows, expected[nb, np]) per predicate."""
+    preds = z[name + "_preds"]
+    sb, sp = (int(v) for v in z[name + "_stride"])
+    count = int(z[name + "_count"][0])
+    res = np.unpackbits(z[name + "_res"], bitorder="little")[:count]
+    return preds, sb, sp, res
+
+
+SHAPES = {
+    # table name: (build column, probe column)
+    "poly_point": ("polys", "pts"),
+    "holed_point": ("holed", "pts"),
+    "poly_poly": ("polys", "polys"),
+    "point_poly": ("pts", "polys"),
+    "point_point": ("pts", "pts"),
+}
+
+
+def cube(z, cols, name):
+    preds, sb, sp, res = table(z, name)
+    bname, pname = SHAPES[name]
+    nb = len(range(0, len(cols[bname]), sb))
+    np_ = len(range(0, len(cols[pname]), sp))
+    return preds, np.arange(0, len(cols[bname]), sb), np.arange(0, len(cols[pname]), sp), \
+        res.reshape(len(preds), nb, np_)
