@@ -1,0 +1,158 @@
+/*
+ * spj_gb300.h — entry points of the GB300 spatial-join library beyond the
+ * reference's gpuspatial_c.h.  None of these have a counterpart in the
+ * reference's C interface; each line says which reference caller it serves.
+ *
+ *  - SpjJoin*: the fused build/probe join that GPUSpatialIndex::query_batch
+ *    (rust/sedona-spatial-join-gpu/src/index/gpu_spatial_index.rs:163-229)
+ *    performs as two FFI calls (index probe, then refine) with host round
+ *    trips in between.  Here probe WKB goes in and the refined (build, probe)
+ *    pairs come out, with no host work in between.  It also carries ST_DWithin
+ *    (rejected on the reference GPU path,
+ *    rust/sedona-spatial-join-gpu/src/physical_planner.rs:155).
+ *  - SpjJoinProbeDevice: device-resident variant (the batched mode: WKB
+ *    columns already in HBM, pairs left in HBM).
+ *  - SpjKnn*: the KNN join (query_knn is NotImplemented on the reference GPU
+ *    path, rust/sedona-spatial-join-gpu/src/index/gpu_spatial_index.rs:252-264;
+ *    the CPU semantics followed are
+ *    rust/sedona-spatial-join/src/index/default_spatial_index.rs:306-502).
+ *  - SpjHostRegister / SpjHostUnregister: page-lock caller buffers so the
+ *    host<->device copies of probe columns and results run at full speed.
+ *
+ * All functions return 0 on success and EINVAL (or another errno value) on
+ * failure; SpjJoinLastError / SpjKnnLastError give the message.  An SpjJoin
+ * or SpjKnn object is used by one thread at a time.
+ */
+#ifndef SPJ_GB300_H
+#define SPJ_GB300_H
+
+#include <stdint.h>
+
+#include "gpuspatial_c.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Predicate code for ST_DWithin(build, probe, distance); relation predicates
+ * use enum SedonaSpatialRelationPredicate. */
+#define SPJ_PREDICATE_DWITHIN 100
+
+/* refine_form values */
+#define SPJ_REFINE_PLAIN_F64 0 /* every test in FP64, full segment scans */
+#define SPJ_REFINE_FAST_F32 1  /* y-band index + FP32 filter + FP64 escalation */
+
+struct SpjJoinConfig {
+  const struct GpuSpatialRuntime* runtime; /* initialized runtime (device) */
+  uint32_t leaf_size;                      /* LBVH leaf size, 0 = default (4) */
+  int32_t refine_form;                     /* SPJ_REFINE_* (default FAST_F32) */
+  int32_t profile;                         /* 1: time phases with CUDA events */
+};
+
+/* An Arrow binary (int32 offsets) or large_binary (int64 offsets) WKB column
+ * whose buffers live in device memory.  offsets index data; validity is an
+ * LSB bitmap or NULL, its bits start at validity_offset. */
+struct SpjDeviceWkb {
+  int64_t length;
+  const void* offsets;
+  int32_t offsets_are_64bit;
+  const uint8_t* data;
+  uint64_t data_length;
+  const uint8_t* validity;
+  int64_t validity_offset;
+};
+
+/* Per-phase device time (ms, CUDA events on the join's stream; zero unless
+ * profile = 1) and counters since the last reset. */
+struct SpjJoinStats {
+  double ms_decode, ms_filter, ms_refine, ms_compact;
+  uint64_t calls, probe_rows, candidates, results;
+  uint64_t escalations;     /* segment / distance tests decided in FP64 */
+  uint64_t pairs_evaluated; /* candidate pairs refined */
+  uint64_t kernel_launches;
+  uint64_t probe_bytes;
+  uint64_t build_rows, build_vertices, build_device_bytes;
+};
+
+typedef struct SpjJoin SpjJoin;
+
+int SpjJoinCreate(const struct SpjJoinConfig* config, SpjJoin** out);
+void SpjJoinRelease(SpjJoin* join);
+const char* SpjJoinLastError(SpjJoin* join);
+
+/* Build side from a host Arrow array (binary / large_binary WKB); may be
+ * called repeatedly to append batches, then SpjJoinFinishBuild. */
+int SpjJoinPushBuildArrow(SpjJoin* join, const struct ArrowSchema* schema,
+                          const struct ArrowArray* array);
+int SpjJoinFinishBuild(SpjJoin* join);
+/* Build side from a device column (replaces any pushed batches). */
+int SpjJoinBuildDevice(SpjJoin* join, const struct SpjDeviceWkb* column);
+
+/* Probe with a host Arrow array; the refined pairs (probe ids offset by
+ * probe_base) are delivered through callback, in ascending probe order,
+ * possibly in several chunks; a non-zero return from callback stops the
+ * probe and is returned. */
+int SpjJoinProbeArrow(SpjJoin* join, const struct ArrowSchema* schema,
+                      const struct ArrowArray* array, int32_t predicate, double distance,
+                      uint32_t probe_base,
+                      int (*callback)(const uint32_t* build_indices,
+                                      const uint32_t* probe_indices, uint64_t length,
+                                      void* user_data),
+                      void* user_data);
+
+/* Probe with a device column; *d_build / *d_probe receive device arrays of
+ * *n_pairs entries, owned by the join and valid until its next probe. */
+int SpjJoinProbeDevice(SpjJoin* join, const struct SpjDeviceWkb* column, int32_t predicate,
+                       double distance, uint32_t probe_base, const uint32_t** d_build,
+                       const uint32_t** d_probe, uint64_t* n_pairs);
+
+/* Probe with a host column given as plain buffers (the same layout as an
+ * Arrow binary array); results are copied into caller buffers of capacity
+ * `capacity` pairs.  *n_pairs receives the full count; if it exceeds
+ * capacity nothing is copied and ENOSPC is returned. */
+int SpjJoinProbeHost(SpjJoin* join, int64_t length, const void* offsets,
+                     int32_t offsets_are_64bit, const uint8_t* data, const uint8_t* validity,
+                     int32_t predicate, double distance, uint32_t probe_base,
+                     uint32_t* out_build, uint32_t* out_probe, uint64_t capacity,
+                     uint64_t* n_pairs);
+
+/* The CUDA stream (cudaStream_t) the join launches its kernels on. */
+void* SpjJoinStream(SpjJoin* join);
+int SpjJoinGetStats(SpjJoin* join, struct SpjJoinStats* out);
+int SpjJoinResetStats(SpjJoin* join);
+
+/* ------------------------------------------------------------------------ */
+/* KNN join over point columns                                              */
+
+typedef struct SpjKnn SpjKnn;
+
+struct SpjKnnConfig {
+  const struct GpuSpatialRuntime* runtime;
+  uint32_t leaf_size;  /* 0 = default */
+  int32_t refine_form; /* SPJ_REFINE_* */
+};
+
+int SpjKnnCreate(const struct SpjKnnConfig* config, SpjKnn** out);
+void SpjKnnRelease(SpjKnn* knn);
+const char* SpjKnnLastError(SpjKnn* knn);
+/* Build points: n FP64 (x, y) pairs, host memory. */
+int SpjKnnBuild(SpjKnn* knn, const double* xy, uint64_t n);
+/* For each probe point, the k nearest build points by Euclidean distance,
+ * ties broken by build row id; out_idx / out_dist hold n_probe*k entries in
+ * (probe, rank) order; slots beyond the build size get UINT32_MAX / +inf.
+ * Host or device pointers (device == 1) for all four arrays. */
+int SpjKnnQuery(SpjKnn* knn, const double* probe_xy, uint64_t n_probe, uint32_t k,
+                uint32_t* out_idx, double* out_dist, int32_t device);
+void* SpjKnnStream(SpjKnn* knn);
+
+/* ------------------------------------------------------------------------ */
+
+int SpjHostRegister(void* ptr, uint64_t bytes);
+int SpjHostUnregister(void* ptr);
+/* Library version string. */
+const char* SpjVersion(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

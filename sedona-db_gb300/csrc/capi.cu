@@ -1,0 +1,800 @@
+// capi.cu — the C ABI: the reference's GpuSpatialRuntime / SedonaFloatIndex2D /
+// SedonaSpatialRefiner objects (include/gpuspatial_c.h) and the SpjJoin /
+// SpjKnn extensions (include/spj_gb300.h), over the device engine.
+//
+// Error convention as the reference's SafeExecute
+// (c/sedona-libgpuspatial/libgpuspatial/src/gpuspatial_c.cc:45-58): any
+// exception becomes EINVAL plus a message kept on the object (or on the probe
+// context, so concurrent probes do not overwrite each other's message).
+#include <errno.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gpuspatial_c.h"
+#include "../../include/spj_gb300.h"
+#include "engine.cuh"
+#include "knn.cuh"
+#include "prims.cuh"
+
+// Arrow C data interface (https://arrow.apache.org/docs/format/CDataInterface.html)
+#ifndef ARROW_C_DATA_INTERFACE
+#define ARROW_C_DATA_INTERFACE
+struct ArrowSchema {
+  const char* format;
+  const char* name;
+  const char* metadata;
+  int64_t flags;
+  int64_t n_children;
+  struct ArrowSchema** children;
+  struct ArrowSchema* dictionary;
+  void (*release)(struct ArrowSchema*);
+  void* private_data;
+};
+struct ArrowArray {
+  int64_t length;
+  int64_t null_count;
+  int64_t offset;
+  int64_t n_buffers;
+  int64_t n_children;
+  const void** buffers;
+  struct ArrowArray** children;
+  struct ArrowArray* dictionary;
+  void (*release)(struct ArrowArray*);
+  void* private_data;
+};
+#endif
+
+namespace {
+
+using namespace spj;
+
+template <class F>
+int guarded(std::string& last_error, F&& f) {
+  try {
+    f();
+    last_error.clear();
+    return 0;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+    return EINVAL;
+  } catch (...) {
+    last_error = "unknown internal error";
+    return EINVAL;
+  }
+}
+
+// --- runtime ----------------------------------------------------------------
+
+struct RuntimeData {
+  int device_id = 0;
+  bool initialized = false;
+  std::string last_error;
+};
+
+int rt_init(GpuSpatialRuntime* self, GpuSpatialRuntimeConfig* config) {
+  auto* d = static_cast<RuntimeData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    SPJ_CHECK(config != nullptr, "null runtime config");
+    int ndev = 0;
+    SPJ_CUDA(cudaGetDeviceCount(&ndev));
+    SPJ_CHECK(config->device_id >= 0 && config->device_id < ndev,
+              "device_id " + std::to_string(config->device_id) + " out of range");
+    SPJ_CUDA(cudaSetDevice(config->device_id));
+    cudaMemPool_t pool;
+    SPJ_CUDA(cudaDeviceGetDefaultMemPool(&pool, config->device_id));
+    uint64_t thresh = UINT64_MAX;  // keep freed blocks cached across calls
+    SPJ_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thresh));
+    if (config->use_cuda_memory_pool && config->cuda_memory_pool_init_precent > 0) {
+      SPJ_CHECK(config->cuda_memory_pool_init_precent <= 100,
+                "cuda_memory_pool_init_precent must be in [0, 100]");
+      size_t free_b = 0, total_b = 0;
+      SPJ_CUDA(cudaMemGetInfo(&free_b, &total_b));
+      size_t want = total_b / 100 * (size_t)config->cuda_memory_pool_init_precent;
+      if (want > free_b / 10 * 9) want = free_b / 10 * 9;
+      void* p = nullptr;
+      SPJ_CUDA(cudaMallocAsync(&p, want, 0));
+      SPJ_CUDA(cudaFreeAsync(p, 0));
+      SPJ_CUDA(cudaStreamSynchronize(0));
+    }
+    d->device_id = config->device_id;
+    d->initialized = true;
+  });
+}
+
+void rt_release(GpuSpatialRuntime* self) {
+  delete static_cast<RuntimeData*>(self->private_data);
+  self->private_data = nullptr;
+}
+
+const char* rt_error(GpuSpatialRuntime* self) {
+  return static_cast<RuntimeData*>(self->private_data)->last_error.c_str();
+}
+
+RuntimeData* runtime_of(const GpuSpatialRuntime* rt) {
+  SPJ_CHECK(rt != nullptr && rt->private_data != nullptr, "null runtime");
+  auto* d = static_cast<RuntimeData*>(rt->private_data);
+  SPJ_CHECK(d->initialized, "runtime is not initialized");
+  return d;
+}
+
+// --- workspace pool: one per concurrent caller -------------------------------
+
+class WorkspacePool {
+ public:
+  explicit WorkspacePool(int device) : device_(device) {}
+  std::unique_ptr<Workspace> acquire() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!free_.empty()) {
+        auto w = std::move(free_.back());
+        free_.pop_back();
+        return w;
+      }
+    }
+    SPJ_CUDA(cudaSetDevice(device_));
+    return std::make_unique<Workspace>();
+  }
+  void release(std::unique_ptr<Workspace> w) {
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.push_back(std::move(w));
+  }
+  void clear() {
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.clear();
+  }
+
+ private:
+  int device_;
+  std::mutex mu_;
+  std::vector<std::unique_ptr<Workspace>> free_;
+};
+
+struct WsLease {
+  WorkspacePool& pool;
+  std::unique_ptr<Workspace> ws;
+  explicit WsLease(WorkspacePool& p) : pool(p), ws(p.acquire()) {}
+  ~WsLease() {
+    if (ws) pool.release(std::move(ws));
+  }
+  Workspace& operator*() { return *ws; }
+  Workspace* operator->() { return ws.get(); }
+};
+
+// --- Arrow binary parsing -----------------------------------------------------
+
+HostWkbColumn parse_arrow(const ArrowSchema* schema, const ArrowArray* array) {
+  SPJ_CHECK(schema != nullptr && array != nullptr, "null Arrow schema or array");
+  SPJ_CHECK(schema->format != nullptr, "Arrow schema without format");
+  const std::string fmt(schema->format);
+  HostWkbColumn c;
+  if (fmt == "z") c.offsets64 = false;
+  else if (fmt == "Z") c.offsets64 = true;
+  else throw Error("unsupported Arrow type '" + fmt + "': expected binary WKB (z or Z)");
+  SPJ_CHECK(array->n_buffers == 3, "binary Arrow array must have 3 buffers");
+  c.n = array->length;
+  const size_t osz = c.offsets64 ? 8 : 4;
+  c.offsets = static_cast<const uint8_t*>(array->buffers[1]) + (size_t)array->offset * osz;
+  c.data = static_cast<const uint8_t*>(array->buffers[2]);
+  if (array->null_count != 0 && array->buffers[0] != nullptr) {
+    c.validity = static_cast<const uint8_t*>(array->buffers[0]);
+    c.validity_offset = array->offset;
+  }
+  if (c.n > 0) SPJ_CHECK(array->buffers[1] != nullptr, "binary Arrow array without offsets");
+  return c;
+}
+
+// Concatenation of pushed host batches (offsets rebased to one data buffer).
+struct HostColumnBuilder {
+  std::vector<int64_t> offsets{0};
+  std::vector<uint8_t> data;
+  std::vector<uint8_t> valid;  // one byte per row
+  bool any_null = false;
+  void append(const HostWkbColumn& c) {
+    for (int64_t i = 0; i < c.n; i++) {
+      int64_t s, e;
+      if (c.offsets64) {
+        s = reinterpret_cast<const int64_t*>(c.offsets)[i];
+        e = reinterpret_cast<const int64_t*>(c.offsets)[i + 1];
+      } else {
+        s = reinterpret_cast<const int32_t*>(c.offsets)[i];
+        e = reinterpret_cast<const int32_t*>(c.offsets)[i + 1];
+      }
+      bool v = true;
+      if (c.validity) {
+        int64_t b = c.validity_offset + i;
+        v = (c.validity[b >> 3] >> (b & 7)) & 1;
+      }
+      valid.push_back(v ? 1 : 0);
+      if (!v) any_null = true;
+      if (v && e > s) data.insert(data.end(), c.data + s, c.data + e);
+      offsets.push_back((int64_t)data.size());
+    }
+  }
+  int64_t rows() const { return (int64_t)offsets.size() - 1; }
+  void clear() {
+    offsets.assign(1, 0);
+    data.clear();
+    valid.clear();
+    any_null = false;
+  }
+  std::vector<uint8_t> bitmap() const {
+    std::vector<uint8_t> bm((valid.size() + 7) / 8, 0);
+    for (size_t i = 0; i < valid.size(); i++)
+      if (valid[i]) bm[i >> 3] |= (uint8_t)(1u << (i & 7));
+    return bm;
+  }
+};
+
+// Build a join engine from a host column (H2D staged through a workspace).
+void build_engine_from_host(JoinEngine& eng, WorkspacePool& pool, const HostColumnBuilder& hb) {
+  WsLease ws(pool);
+  std::vector<uint8_t> bm;
+  HostWkbColumn c;
+  c.n = hb.rows();
+  c.offsets = hb.offsets.data();
+  c.offsets64 = true;
+  c.data = hb.data.data();
+  if (hb.any_null) {
+    bm = hb.bitmap();
+    c.validity = bm.data();
+  }
+  uint64_t bytes = 0;
+  WkbDeviceColumn d = stage_column(*ws, c, &bytes);
+  eng.build(d, ws->stream);
+}
+
+// --- SedonaFloatIndex2D ----------------------------------------------------
+
+struct IndexData {
+  RuntimeData* rt;
+  std::vector<float> rects;
+  Lbvh bvh;
+  bool built = false;
+  std::unique_ptr<WorkspacePool> pool;
+  std::string last_error;
+};
+
+struct IndexContext {
+  std::vector<uint32_t> build, probe;
+  std::string last_error;
+};
+
+IndexData* idx_of(SedonaFloatIndex2D* self) {
+  auto* d = static_cast<IndexData*>(self->private_data);
+  SPJ_CUDA(cudaSetDevice(d->rt->device_id));
+  return d;
+}
+
+int idx_clear(SedonaFloatIndex2D* self) {
+  auto* d = static_cast<IndexData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    idx_of(self);
+    d->rects.clear();
+    d->bvh = Lbvh();
+    d->built = false;
+  });
+}
+
+void idx_create_ctx(SedonaSpatialIndexContext* ctx) { ctx->private_data = new IndexContext(); }
+void idx_destroy_ctx(SedonaSpatialIndexContext* ctx) {
+  delete static_cast<IndexContext*>(ctx->private_data);
+  ctx->private_data = nullptr;
+}
+
+int idx_push(SedonaFloatIndex2D* self, const float* buf, uint32_t n) {
+  auto* d = static_cast<IndexData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    idx_of(self);
+    SPJ_CHECK(!d->built, "push_build after finish_building (call clear first)");
+    SPJ_CHECK(n == 0 || buf != nullptr, "null rect buffer");
+    d->rects.insert(d->rects.end(), buf, buf + (size_t)n * 4);
+  });
+}
+
+int idx_finish(SedonaFloatIndex2D* self) {
+  auto* d = static_cast<IndexData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    idx_of(self);
+    WsLease ws(*d->pool);
+    const uint32_t n = (uint32_t)(d->rects.size() / 4);
+    DevBuf boxes(((size_t)n + 1) * 16, ws->stream);
+    if (n)
+      SPJ_CUDA(cudaMemcpyAsync(boxes.get(), d->rects.data(), (size_t)n * 16,
+                               cudaMemcpyHostToDevice, ws->stream));
+    build_lbvh(boxes.as<float4>(), n, 4, d->bvh, ws->stream);
+    SPJ_CUDA(cudaStreamSynchronize(ws->stream));
+    d->built = true;
+  });
+}
+
+int idx_probe(SedonaFloatIndex2D* self, SedonaSpatialIndexContext* context, const float* buf,
+              uint32_t n,
+              int (*callback)(const uint32_t*, const uint32_t*, uint32_t, void*),
+              void* user_data) {
+  auto* d = static_cast<IndexData*>(self->private_data);
+  auto* ctx = static_cast<IndexContext*>(context->private_data);
+  int cb_status = 0;
+  int rc = guarded(ctx->last_error, [&] {
+    idx_of(self);
+    SPJ_CHECK(d->built, "probe before finish_building");
+    SPJ_CHECK(n == 0 || buf != nullptr, "null rect buffer");
+    SPJ_CHECK(callback != nullptr, "null callback");
+    WsLease ws(*d->pool);
+    cudaStream_t s = ws->stream;
+    ws->boxes_tmp.reserve(((size_t)n + 1) * 16, s);
+    if (n)
+      SPJ_CUDA(cudaMemcpyAsync(ws->boxes_tmp.get(), buf, (size_t)n * 16, cudaMemcpyHostToDevice,
+                               s));
+    const LbvhView tv = d->bvh.view();
+    uint64_t m = probe_count(tv, ws->boxes_tmp.as<float4>(), n, ws->psc, s);
+    SPJ_CHECK(m <= 0xFFFFFFFFull, "candidate count exceeds the 32-bit callback length");
+    ws->cand_build.reserve((m + 1) * 4, s);
+    ws->cand_probe.reserve((m + 1) * 4, s);
+    probe_scatter(tv, ws->boxes_tmp.as<float4>(), n, ws->psc, 0, ws->cand_build.as<uint32_t>(),
+                  ws->cand_probe.as<uint32_t>(), s);
+    ctx->build.resize(m);
+    ctx->probe.resize(m);
+    if (m) {
+      SPJ_CUDA(cudaMemcpyAsync(ctx->build.data(), ws->cand_build.get(), m * 4,
+                               cudaMemcpyDeviceToHost, s));
+      SPJ_CUDA(cudaMemcpyAsync(ctx->probe.data(), ws->cand_probe.get(), m * 4,
+                               cudaMemcpyDeviceToHost, s));
+    }
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    cb_status = callback(ctx->build.data(), ctx->probe.data(), (uint32_t)m, user_data);
+  });
+  if (rc) return rc;
+  return cb_status;
+}
+
+const char* idx_error(SedonaFloatIndex2D* self) {
+  return static_cast<IndexData*>(self->private_data)->last_error.c_str();
+}
+const char* idx_ctx_error(SedonaSpatialIndexContext* ctx) {
+  return static_cast<IndexContext*>(ctx->private_data)->last_error.c_str();
+}
+void idx_release(SedonaFloatIndex2D* self) {
+  auto* d = static_cast<IndexData*>(self->private_data);
+  if (d) {
+    cudaSetDevice(d->rt->device_id);
+    delete d;
+  }
+  self->private_data = nullptr;
+}
+
+// --- SedonaSpatialRefiner ----------------------------------------------------
+
+struct RefinerData {
+  RuntimeData* rt;
+  std::string build_format;
+  HostColumnBuilder host;
+  std::unique_ptr<JoinEngine> engine;
+  std::unique_ptr<WorkspacePool> pool;
+  std::string last_error;
+};
+
+RefinerData* ref_of(SedonaSpatialRefiner* self) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  SPJ_CUDA(cudaSetDevice(d->rt->device_id));
+  return d;
+}
+
+int ref_clear(SedonaSpatialRefiner* self) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    ref_of(self);
+    d->host.clear();
+    EngineConfig cfg = d->engine->config();
+    d->engine = std::make_unique<JoinEngine>(d->rt->device_id, cfg);
+  });
+}
+
+int ref_init_schema(SedonaSpatialRefiner* self, const ArrowSchema* schema) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    SPJ_CHECK(schema != nullptr && schema->format != nullptr, "null build schema");
+    std::string f(schema->format);
+    SPJ_CHECK(f == "z" || f == "Z", "unsupported build Arrow type '" + f + "'");
+    d->build_format = f;
+  });
+}
+
+int ref_push(SedonaSpatialRefiner* self, const ArrowArray* array) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    SPJ_CHECK(!d->build_format.empty(), "push_build before init_build_schema");
+    ArrowSchema sch{};
+    sch.format = d->build_format.c_str();
+    d->host.append(parse_arrow(&sch, array));
+  });
+}
+
+int ref_finish(SedonaSpatialRefiner* self) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    ref_of(self);
+    build_engine_from_host(*d->engine, *d->pool, d->host);
+  });
+}
+
+int ref_refine(SedonaSpatialRefiner* self, const ArrowSchema* probe_schema,
+               const ArrowArray* probe_array, SedonaSpatialRelationPredicate predicate,
+               uint32_t* build_indices, uint32_t* probe_indices, uint32_t n,
+               uint32_t* new_n) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  return guarded(d->last_error, [&] {
+    ref_of(self);
+    SPJ_CHECK(d->engine->built(), "refine before finish_building");
+    SPJ_CHECK(new_n != nullptr, "null new_indices_size");
+    SPJ_CHECK(n == 0 || (build_indices && probe_indices), "null index arrays");
+    const int p = (int)predicate;
+    SPJ_CHECK(p >= 0 && p <= 7, "unknown predicate");
+    HostWkbColumn pc = parse_arrow(probe_schema, probe_array);
+    WsLease ws(*d->pool);
+    cudaStream_t s = ws->stream;
+    // bounds of the caller's indices are checked on the host: cheap and exact
+    const uint32_t nb = d->engine->build_geoms().n;
+    for (uint32_t i = 0; i < n; i++) {
+      SPJ_CHECK(build_indices[i] < nb, "build index out of range");
+      SPJ_CHECK(probe_indices[i] < (uint64_t)pc.n, "probe index out of range");
+    }
+    uint64_t bytes = 0;
+    WkbDeviceColumn dc = stage_column(*ws, pc, &bytes);
+    decode_wkb(dc, ws->probe, ws->dsc, false, s);
+    ws->cand_build.reserve(((size_t)n + 1) * 4, s);
+    ws->cand_probe.reserve(((size_t)n + 1) * 4, s);
+    if (n) {
+      SPJ_CUDA(cudaMemcpyAsync(ws->cand_build.get(), build_indices, (size_t)n * 4,
+                               cudaMemcpyHostToDevice, s));
+      SPJ_CUDA(cudaMemcpyAsync(ws->cand_probe.get(), probe_indices, (size_t)n * 4,
+                               cudaMemcpyHostToDevice, s));
+    }
+    uint64_t kept = d->engine->refine_pairs(*ws, ws->probe.view(), ws->cand_build.as<uint32_t>(),
+                                            ws->cand_probe.as<uint32_t>(), n, p, 0.0);
+    // output ordered by probe index (reference: sort_probe_indices,
+    // include/gpuspatial/refine/rt_spatial_refiner.hpp:48); the sort is
+    // stable, so pairs of one probe keep their input order
+    if (kept > 1) {
+      DevBuf ak(kept * 4, s), av(kept * 4, s), tmp;
+      int bits = 1;
+      while (bits < 32 && ((uint64_t)pc.n >> bits) != 0) bits++;
+      radix_sort_pairs(ws->out_probe.as<uint32_t>(), ws->out_build.as<uint32_t>(),
+                       ak.as<uint32_t>(), av.as<uint32_t>(), (int64_t)kept, (bits + 7) / 8 * 8,
+                       tmp, s);
+    }
+    if (kept) {
+      SPJ_CUDA(cudaMemcpyAsync(build_indices, ws->out_build.get(), kept * 4,
+                               cudaMemcpyDeviceToHost, s));
+      SPJ_CUDA(cudaMemcpyAsync(probe_indices, ws->out_probe.get(), kept * 4,
+                               cudaMemcpyDeviceToHost, s));
+    }
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    *new_n = (uint32_t)kept;
+  });
+}
+
+const char* ref_error(SedonaSpatialRefiner* self) {
+  return static_cast<RefinerData*>(self->private_data)->last_error.c_str();
+}
+void ref_release(SedonaSpatialRefiner* self) {
+  auto* d = static_cast<RefinerData*>(self->private_data);
+  if (d) {
+    cudaSetDevice(d->rt->device_id);
+    delete d;
+  }
+  self->private_data = nullptr;
+}
+
+}  // namespace
+
+// =============================================================================
+// exported: reference interface
+
+extern "C" void GpuSpatialRuntimeCreate(GpuSpatialRuntime* runtime) {
+  runtime->init = rt_init;
+  runtime->release = rt_release;
+  runtime->get_last_error = rt_error;
+  runtime->private_data = new RuntimeData();
+}
+
+extern "C" int GpuSpatialIndexFloat2DCreate(SedonaFloatIndex2D* index,
+                                            const GpuSpatialIndexConfig* config) {
+  try {
+    SPJ_CHECK(index && config, "null index or config");
+    RuntimeData* rt = runtime_of(config->runtime);
+    SPJ_CUDA(cudaSetDevice(rt->device_id));
+    auto* d = new IndexData();
+    d->rt = rt;
+    d->pool = std::make_unique<WorkspacePool>(rt->device_id);
+    index->clear = idx_clear;
+    index->create_context = idx_create_ctx;
+    index->destroy_context = idx_destroy_ctx;
+    index->push_build = idx_push;
+    index->finish_building = idx_finish;
+    index->probe = idx_probe;
+    index->get_last_error = idx_error;
+    index->context_get_last_error = idx_ctx_error;
+    index->release = idx_release;
+    index->private_data = d;
+    return 0;
+  } catch (const std::exception& e) {
+    fprintf(stderr, "GpuSpatialIndexFloat2DCreate: %s\n", e.what());
+    return EINVAL;
+  }
+}
+
+extern "C" int GpuSpatialRefinerCreate(SedonaSpatialRefiner* refiner,
+                                       const GpuSpatialRefinerConfig* config) {
+  try {
+    SPJ_CHECK(refiner && config, "null refiner or config");
+    RuntimeData* rt = runtime_of(config->runtime);
+    SPJ_CUDA(cudaSetDevice(rt->device_id));
+    auto* d = new RefinerData();
+    d->rt = rt;
+    d->engine = std::make_unique<JoinEngine>(rt->device_id, EngineConfig());
+    d->pool = std::make_unique<WorkspacePool>(rt->device_id);
+    refiner->clear = ref_clear;
+    refiner->init_build_schema = ref_init_schema;
+    refiner->push_build = ref_push;
+    refiner->finish_building = ref_finish;
+    refiner->refine = ref_refine;
+    refiner->get_last_error = ref_error;
+    refiner->release = ref_release;
+    refiner->private_data = d;
+    return 0;
+  } catch (const std::exception& e) {
+    fprintf(stderr, "GpuSpatialRefinerCreate: %s\n", e.what());
+    return EINVAL;
+  }
+}
+
+// =============================================================================
+// exported: SpjJoin
+
+struct SpjJoin {
+  RuntimeData* rt = nullptr;
+  std::unique_ptr<JoinEngine> engine;
+  std::unique_ptr<WorkspacePool> pool;
+  std::unique_ptr<Workspace> ws;  // the join's own stream and scratch
+  HostColumnBuilder host;
+  std::vector<uint32_t> hb, hp;
+  std::string last_error;
+};
+
+extern "C" int SpjJoinCreate(const SpjJoinConfig* config, SpjJoin** out) {
+  try {
+    SPJ_CHECK(config && out, "null config or output");
+    RuntimeData* rt = runtime_of(config->runtime);
+    SPJ_CUDA(cudaSetDevice(rt->device_id));
+    EngineConfig ec;
+    if (config->leaf_size) ec.leaf_size = config->leaf_size;
+    ec.refine_form = config->refine_form;
+    SPJ_CHECK(ec.refine_form == kPlainF64 || ec.refine_form == kFastF32, "unknown refine_form");
+    ec.profile = config->profile != 0;
+    auto j = std::make_unique<SpjJoin>();
+    j->rt = rt;
+    j->engine = std::make_unique<JoinEngine>(rt->device_id, ec);
+    j->pool = std::make_unique<WorkspacePool>(rt->device_id);
+    j->ws = std::make_unique<Workspace>();
+    *out = j.release();
+    return 0;
+  } catch (const std::exception& e) {
+    fprintf(stderr, "SpjJoinCreate: %s\n", e.what());
+    return EINVAL;
+  }
+}
+
+extern "C" void SpjJoinRelease(SpjJoin* j) {
+  if (!j) return;
+  cudaSetDevice(j->rt->device_id);
+  delete j;
+}
+
+extern "C" const char* SpjJoinLastError(SpjJoin* j) { return j->last_error.c_str(); }
+
+extern "C" int SpjJoinPushBuildArrow(SpjJoin* j, const ArrowSchema* schema,
+                                     const ArrowArray* array) {
+  return guarded(j->last_error, [&] { j->host.append(parse_arrow(schema, array)); });
+}
+
+extern "C" int SpjJoinFinishBuild(SpjJoin* j) {
+  return guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    build_engine_from_host(*j->engine, *j->pool, j->host);
+    j->host.clear();
+  });
+}
+
+static WkbDeviceColumn device_column(const SpjDeviceWkb* c) {
+  SPJ_CHECK(c != nullptr, "null column");
+  SPJ_CHECK(c->length >= 0, "negative column length");
+  SPJ_CHECK(c->length == 0 || (c->offsets && c->data), "null device buffers");
+  WkbDeviceColumn d;
+  d.n = c->length;
+  d.offsets = c->offsets;
+  d.offsets64 = c->offsets_are_64bit != 0;
+  d.data = c->data;
+  d.data_len = c->data_length;
+  d.validity = c->validity;
+  d.validity_offset = c->validity_offset;
+  return d;
+}
+
+extern "C" int SpjJoinBuildDevice(SpjJoin* j, const SpjDeviceWkb* column) {
+  return guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    j->host.clear();
+    j->engine->build(device_column(column), j->ws->stream);
+  });
+}
+
+extern "C" int SpjJoinProbeDevice(SpjJoin* j, const SpjDeviceWkb* column, int32_t predicate,
+                                  double distance, uint32_t probe_base, const uint32_t** d_build,
+                                  const uint32_t** d_probe, uint64_t* n_pairs) {
+  return guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    SPJ_CHECK(d_build && d_probe && n_pairs, "null outputs");
+    *n_pairs = j->engine->probe(*j->ws, device_column(column), predicate, distance, probe_base,
+                                d_build, d_probe);
+  });
+}
+
+extern "C" int SpjJoinProbeArrow(SpjJoin* j, const ArrowSchema* schema, const ArrowArray* array,
+                                 int32_t predicate, double distance, uint32_t probe_base,
+                                 int (*callback)(const uint32_t*, const uint32_t*, uint64_t,
+                                                 void*),
+                                 void* user_data) {
+  int cb_status = 0;
+  int rc = guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    SPJ_CHECK(callback != nullptr, "null callback");
+    HostWkbColumn hc = parse_arrow(schema, array);
+    uint64_t bytes = 0;
+    WkbDeviceColumn dc = stage_column(*j->ws, hc, &bytes);
+    const uint32_t *db, *dp;
+    uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp);
+    j->hb.resize(m);
+    j->hp.resize(m);
+    if (m) {
+      SPJ_CUDA(cudaMemcpyAsync(j->hb.data(), db, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
+      SPJ_CUDA(cudaMemcpyAsync(j->hp.data(), dp, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
+    }
+    SPJ_CUDA(cudaStreamSynchronize(j->ws->stream));
+    cb_status = callback(j->hb.data(), j->hp.data(), m, user_data);
+  });
+  return rc ? rc : cb_status;
+}
+
+extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
+                                int32_t offsets_are_64bit, const uint8_t* data,
+                                const uint8_t* validity, int32_t predicate, double distance,
+                                uint32_t probe_base, uint32_t* out_build, uint32_t* out_probe,
+                                uint64_t capacity, uint64_t* n_pairs) {
+  int rc = 0;
+  int g = guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    SPJ_CHECK(n_pairs != nullptr, "null n_pairs");
+    HostWkbColumn hc;
+    hc.n = length;
+    hc.offsets = offsets;
+    hc.offsets64 = offsets_are_64bit != 0;
+    hc.data = data;
+    hc.validity = validity;
+    uint64_t bytes = 0;
+    WkbDeviceColumn dc = stage_column(*j->ws, hc, &bytes);
+    const uint32_t *db, *dp;
+    uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp);
+    *n_pairs = m;
+    if (m > capacity) {
+      rc = ENOSPC;
+      j->last_error = "output capacity too small: need " + std::to_string(m) + " pairs";
+      return;
+    }
+    if (m) {
+      SPJ_CHECK(out_build && out_probe, "null output buffers");
+      SPJ_CUDA(cudaMemcpyAsync(out_build, db, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
+      SPJ_CUDA(cudaMemcpyAsync(out_probe, dp, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
+    }
+    SPJ_CUDA(cudaStreamSynchronize(j->ws->stream));
+  });
+  if (g) return g;
+  if (rc) return rc;
+  return 0;
+}
+
+extern "C" void* SpjJoinStream(SpjJoin* j) { return (void*)j->ws->stream; }
+
+extern "C" int SpjJoinGetStats(SpjJoin* j, SpjJoinStats* out) {
+  return guarded(j->last_error, [&] {
+    SPJ_CHECK(out != nullptr, "null stats");
+    JoinStats s = j->engine->stats();
+    out->ms_decode = s.ms_decode;
+    out->ms_filter = s.ms_filter;
+    out->ms_refine = s.ms_refine;
+    out->ms_compact = s.ms_compact;
+    out->calls = s.calls;
+    out->probe_rows = s.probe_rows;
+    out->candidates = s.candidates;
+    out->results = s.results;
+    out->escalations = s.escalations;
+    out->pairs_evaluated = s.pairs_evaluated;
+    out->kernel_launches = s.kernel_launches;
+    out->probe_bytes = s.probe_bytes;
+    const DeviceGeoms& g = j->engine->build_geoms();
+    out->build_rows = g.n;
+    out->build_vertices = g.nverts;
+    out->build_device_bytes = g.device_bytes() + j->engine->lbvh().device_bytes();
+  });
+}
+
+extern "C" int SpjJoinResetStats(SpjJoin* j) {
+  return guarded(j->last_error, [&] { j->engine->reset_stats(); });
+}
+
+// =============================================================================
+// exported: SpjKnn
+
+struct SpjKnn {
+  RuntimeData* rt = nullptr;
+  std::unique_ptr<KnnIndex> index;
+  std::string last_error;
+};
+
+extern "C" int SpjKnnCreate(const SpjKnnConfig* config, SpjKnn** out) {
+  try {
+    SPJ_CHECK(config && out, "null config or output");
+    RuntimeData* rt = runtime_of(config->runtime);
+    SPJ_CUDA(cudaSetDevice(rt->device_id));
+    auto k = std::make_unique<SpjKnn>();
+    k->rt = rt;
+    k->index = std::make_unique<KnnIndex>(config->leaf_size ? config->leaf_size : 8,
+                                          config->refine_form);
+    *out = k.release();
+    return 0;
+  } catch (const std::exception& e) {
+    fprintf(stderr, "SpjKnnCreate: %s\n", e.what());
+    return EINVAL;
+  }
+}
+
+extern "C" void SpjKnnRelease(SpjKnn* k) {
+  if (!k) return;
+  cudaSetDevice(k->rt->device_id);
+  delete k;
+}
+
+extern "C" const char* SpjKnnLastError(SpjKnn* k) { return k->last_error.c_str(); }
+
+extern "C" int SpjKnnBuild(SpjKnn* k, const double* xy, uint64_t n) {
+  return guarded(k->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(k->rt->device_id));
+    k->index->build(xy, n);
+  });
+}
+
+extern "C" int SpjKnnQuery(SpjKnn* k, const double* probe_xy, uint64_t n, uint32_t kk,
+                           uint32_t* out_idx, double* out_dist, int32_t device) {
+  return guarded(k->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(k->rt->device_id));
+    k->index->query(probe_xy, n, kk, out_idx, out_dist, device != 0);
+  });
+}
+
+extern "C" void* SpjKnnStream(SpjKnn* k) { return (void*)k->index->stream(); }
+
+extern "C" int SpjHostRegister(void* ptr, uint64_t bytes) {
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  return e == cudaSuccess ? 0 : EINVAL;
+}
+
+extern "C" int SpjHostUnregister(void* ptr) {
+  cudaError_t e = cudaHostUnregister(ptr);
+  return e == cudaSuccess ? 0 : EINVAL;
+}
+
+extern "C" const char* SpjVersion(void) { return "spj-gb300 0.1.0 (sm_103a)"; }

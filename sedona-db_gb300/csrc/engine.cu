@@ -1,0 +1,252 @@
+// engine.cu — build / probe orchestration on one stream per caller.
+#include "engine.cuh"
+#include "prims.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace spj {
+
+Workspace::Workspace() {
+  SPJ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  own_stream = true;
+  for (auto& e : ev) SPJ_CUDA(cudaEventCreate(&e));
+}
+
+Workspace::~Workspace() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  // DevBufs free on their own streams; make sure those frees are issued
+  // before the stream goes away
+  probe = DeviceGeoms();
+  dsc = DecodeScratch();
+  psc = ProbeScratch();
+  boxes_tmp.release();
+  cand_build.release();
+  cand_probe.release();
+  flags.release();
+  pos.release();
+  out_build.release();
+  out_probe.release();
+  scan_tmp.release();
+  status.release();
+  wkb_data.release();
+  wkb_offsets.release();
+  wkb_validity.release();
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    if (own_stream) cudaStreamDestroy(stream);
+  }
+}
+
+JoinEngine::JoinEngine(int device, EngineConfig cfg) : device_(device), cfg_(cfg) {}
+
+JoinEngine::~JoinEngine() { cudaDeviceSynchronize(); }
+
+void JoinEngine::build(const WkbDeviceColumn& col, cudaStream_t s) {
+  built_ = false;
+  decode_wkb(col, bg_, bsc_, false, s);
+  if (bg_.nrings > 0) build_band_index(bg_, bsc_, s);
+  build_lbvh(bg_.box.as<float4>(), bg_.n, cfg_.leaf_size, bvh_, s);
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  built_ = true;
+}
+
+static inline float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predicate,
+                           double distance, uint32_t probe_base, const uint32_t** d_build,
+                           const uint32_t** d_probe) {
+  SPJ_CHECK(built_, "probe called before the build side was finished");
+  SPJ_CHECK(predicate == kPredDWithin || (predicate >= 0 && predicate <= 7),
+            "unknown predicate code " + std::to_string(predicate));
+  SPJ_CHECK(col.n >= 0 && (uint64_t)col.n + probe_base <= 0xFFFFFFFFull,
+            "probe row ids exceed 32 bits");
+  if (predicate == kPredDWithin) SPJ_CHECK(distance >= 0 && !std::isnan(distance),
+                                           "ST_DWithin distance must be a non-negative number");
+  cudaStream_t s = ws.stream;
+  const bool prof = cfg_.profile;
+  uint64_t launches = 0;
+  if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[0], s));
+
+  const bool hint = ws.last_probe_points;
+  decode_wkb(col, ws.probe, ws.dsc, hint, s);
+  launches += ws.probe.all_points && hint ? 1 : 17;
+  ws.last_probe_points = ws.probe.all_points;
+  const uint32_t n = ws.probe.n;
+  if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[1], s));
+
+  const float4* boxes = ws.probe.box.as<float4>();
+  if (predicate == kPredDWithin) {
+    SPJ_CHECK(ws.probe.all_points && bg_.all_points,
+              "ST_DWithin is supported for point build and probe sides");
+    ws.boxes_tmp.reserve(((size_t)n + 1) * sizeof(float4), s);
+    expand_boxes(ws.probe.pt.as<double2>(), ws.probe.box.as<float4>(),
+                 ws.probe.kind.as<uint8_t>(), n, distance, ws.boxes_tmp.as<float4>(), s);
+    boxes = ws.boxes_tmp.as<float4>();
+    launches++;
+  }
+  const LbvhView tv = bvh_.view();
+  const uint64_t m = probe_count(tv, boxes, n, ws.psc, s);  // syncs
+  SPJ_CHECK(m < (1ull << 34), "candidate pair count too large");
+  ws.cand_build.reserve((m + 1) * 4, s);
+  ws.cand_probe.reserve((m + 1) * 4, s);
+  probe_scatter(tv, boxes, n, ws.psc, probe_base, ws.cand_build.as<uint32_t>(),
+                ws.cand_probe.as<uint32_t>(), s);
+  launches += 5;
+  if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
+
+  reset_status(ws.status, s);
+  ws.flags.reserve(m + 1, s);
+  const GeomsView bv = bg_.view(), pv = ws.probe.view();
+  if (predicate == kPredDWithin)
+    refine_dwithin(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
+                   probe_base, distance, cfg_.refine_form, ws.flags.as<uint8_t>(),
+                   ws.status.as<DeviceStatus>(), s);
+  else
+    refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
+                    probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
+                    ws.status.as<DeviceStatus>(), s);
+  launches += 1;
+  if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
+
+  ws.pos.reserve((m + 1) * 8, s);
+  scan_u8_u64(ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), (int64_t)m, ws.scan_tmp, s);
+  uint64_t total = 0;
+  DeviceStatus hst;
+  SPJ_CUDA(cudaMemcpyAsync(&total, ws.pos.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(&hst, ws.status.get(), sizeof hst, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  if (hst.first_bad != ~0ull) {
+    throw Error(std::string("refine: ") + status_message((uint32_t)(hst.first_bad >> 40)));
+  }
+  ws.out_build.reserve((total + 1) * 4, s);
+  ws.out_probe.reserve((total + 1) * 4, s);
+  compact_pairs(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), ws.flags.as<uint8_t>(),
+                ws.pos.as<uint64_t>(), m, ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(),
+                s);
+  launches += 4;
+  if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[4], s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  {
+    std::lock_guard<std::mutex> lk(stats_mu_);
+    stats_.calls++;
+    stats_.probe_rows += n;
+    stats_.candidates += m;
+    stats_.results += total;
+    stats_.escalations += hst.counters[0];
+    stats_.pairs_evaluated += hst.counters[1];
+    stats_.kernel_launches += launches;
+    stats_.probe_bytes += (uint64_t)col.data_len + (uint64_t)(col.n + 1) * (col.offsets64 ? 8 : 4);
+    if (prof) {
+      stats_.ms_decode += ev_ms(ws.ev[0], ws.ev[1]);
+      stats_.ms_filter += ev_ms(ws.ev[1], ws.ev[2]);
+      stats_.ms_refine += ev_ms(ws.ev[2], ws.ev[3]);
+      stats_.ms_compact += ev_ms(ws.ev[3], ws.ev[4]);
+    }
+  }
+  *d_build = ws.out_build.as<uint32_t>();
+  *d_probe = ws.out_probe.as<uint32_t>();
+  return total;
+}
+
+uint64_t JoinEngine::refine_pairs(Workspace& ws, const GeomsView& pv, const uint32_t* cb,
+                                  const uint32_t* cp, uint64_t m, int predicate,
+                                  double distance) {
+  SPJ_CHECK(built_, "refine called before the build side was finished");
+  cudaStream_t s = ws.stream;
+  reset_status(ws.status, s);
+  ws.flags.reserve(m + 1, s);
+  const GeomsView bv = bg_.view();
+  if (predicate == kPredDWithin)
+    refine_dwithin(bv, pv, cb, cp, m, 0, distance, cfg_.refine_form, ws.flags.as<uint8_t>(),
+                   ws.status.as<DeviceStatus>(), s);
+  else
+    refine_relation(bv, pv, cb, cp, m, 0, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
+                    ws.status.as<DeviceStatus>(), s);
+  ws.pos.reserve((m + 1) * 8, s);
+  scan_u8_u64(ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), (int64_t)m, ws.scan_tmp, s);
+  uint64_t total = 0;
+  DeviceStatus hst;
+  SPJ_CUDA(cudaMemcpyAsync(&total, ws.pos.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(&hst, ws.status.get(), sizeof hst, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  if (hst.first_bad != ~0ull)
+    throw Error(std::string("refine: ") + status_message((uint32_t)(hst.first_bad >> 40)));
+  ws.out_build.reserve((total + 1) * 4, s);
+  ws.out_probe.reserve((total + 1) * 4, s);
+  compact_pairs(cb, cp, ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), m,
+                ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), s);
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  {
+    std::lock_guard<std::mutex> lk(stats_mu_);
+    stats_.candidates += m;
+    stats_.results += total;
+    stats_.escalations += hst.counters[0];
+    stats_.pairs_evaluated += hst.counters[1];
+  }
+  return total;
+}
+
+JoinStats JoinEngine::stats() {
+  std::lock_guard<std::mutex> lk(stats_mu_);
+  return stats_;
+}
+
+void JoinEngine::reset_stats() {
+  std::lock_guard<std::mutex> lk(stats_mu_);
+  stats_ = JoinStats();
+}
+
+WkbDeviceColumn stage_column(Workspace& ws, const HostWkbColumn& col, uint64_t* bytes) {
+  cudaStream_t s = ws.stream;
+  WkbDeviceColumn d;
+  d.n = col.n;
+  d.offsets64 = col.offsets64;
+  const size_t osz = col.offsets64 ? 8 : 4;
+  int64_t base, end;
+  if (col.n == 0) {
+    base = end = 0;
+  } else if (col.offsets64) {
+    base = reinterpret_cast<const int64_t*>(col.offsets)[0];
+    end = reinterpret_cast<const int64_t*>(col.offsets)[col.n];
+  } else {
+    base = reinterpret_cast<const int32_t*>(col.offsets)[0];
+    end = reinterpret_cast<const int32_t*>(col.offsets)[col.n];
+  }
+  SPJ_CHECK(base >= 0 && end >= base, "invalid Arrow offsets");
+  const int64_t base4 = base & ~int64_t(3);
+  ws.wkb_offsets.reserve((size_t)(col.n + 1) * osz, s);
+  ws.wkb_data.reserve((size_t)(end - base4) + 16, s);
+  if (col.n >= 0 && col.offsets)
+    SPJ_CUDA(cudaMemcpyAsync(ws.wkb_offsets.get(), col.offsets, (size_t)(col.n + 1) * osz,
+                             cudaMemcpyHostToDevice, s));
+  if (end > base4)
+    SPJ_CUDA(cudaMemcpyAsync(ws.wkb_data.get(), col.data + base4, (size_t)(end - base4),
+                             cudaMemcpyHostToDevice, s));
+  uint64_t b = (uint64_t)(col.n + 1) * osz + (uint64_t)(end - base4);
+  if (col.validity) {
+    const int64_t b0 = col.validity_offset >> 3;
+    const int64_t b1 = (col.validity_offset + col.n + 7) >> 3;
+    ws.wkb_validity.reserve((size_t)(b1 - b0) + 1, s);
+    SPJ_CUDA(cudaMemcpyAsync(ws.wkb_validity.get(), col.validity + b0, (size_t)(b1 - b0),
+                             cudaMemcpyHostToDevice, s));
+    d.validity = ws.wkb_validity.as<uint8_t>();
+    d.validity_offset = col.validity_offset & 7;
+    b += (uint64_t)(b1 - b0);
+  }
+  d.offsets = ws.wkb_offsets.get();
+  // offsets index the caller's data buffer; shift the device pointer so the
+  // same offsets land in the staged copy (which starts at base4)
+  d.data = ws.wkb_data.as<uint8_t>() - base4;
+  d.data_len = (uint64_t)end;
+  if (bytes) *bytes = b;
+  return d;
+}
+
+}  // namespace spj

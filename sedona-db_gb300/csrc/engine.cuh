@@ -1,0 +1,108 @@
+// engine.cuh — the join engine behind the C ABI: a decoded, indexed build
+// side resident in HBM and a probe pipeline
+//   decode probe WKB -> f32 filter boxes -> LBVH count / scan / scatter ->
+//   refine (tg semantics or DWithin) -> scan / compact
+// whose results stay on the device.  This is the GB300 counterpart of the
+// reference's GPUSpatialIndex::query_batch
+// (rust/sedona-spatial-join-gpu/src/index/gpu_spatial_index.rs:163-229), which
+// runs RTSpatialIndex::Probe and RTSpatialRefiner::Refine back to back with
+// host round trips in between.
+#pragma once
+#include <mutex>
+
+#include "geoms.cuh"
+#include "lbvh.cuh"
+#include "refine.cuh"
+
+namespace spj {
+
+constexpr int kPredDWithin = 100;  // ST_DWithin(build, probe, distance)
+
+struct EngineConfig {
+  uint32_t leaf_size = 4;
+  int refine_form = kFastF32;
+  bool profile = false;  // time each phase with CUDA events on the engine stream
+};
+
+// Per-phase device time (CUDA events on the launching stream) and counters.
+struct JoinStats {
+  double ms_decode = 0, ms_filter = 0, ms_refine = 0, ms_compact = 0;
+  uint64_t calls = 0;
+  uint64_t probe_rows = 0;
+  uint64_t candidates = 0;
+  uint64_t results = 0;
+  uint64_t escalations = 0;  // segment / distance tests decided in FP64
+  uint64_t pairs_evaluated = 0;
+  uint64_t kernel_launches = 0;
+  uint64_t probe_bytes = 0;  // WKB + offsets bytes of the probe columns
+};
+
+// Per-call scratch; one per concurrent caller.
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DeviceGeoms probe;
+  DecodeScratch dsc;
+  ProbeScratch psc;
+  DevBuf boxes_tmp, cand_build, cand_probe, flags, pos, out_build, out_probe, scan_tmp, status;
+  DevBuf wkb_data, wkb_offsets, wkb_validity;  // H2D staging of host columns
+  cudaEvent_t ev[6] = {};
+  bool last_probe_points = true;
+  Workspace();
+  ~Workspace();
+};
+
+class JoinEngine {
+ public:
+  JoinEngine(int device, EngineConfig cfg);
+  ~JoinEngine();
+
+  int device() const { return device_; }
+  EngineConfig& config() { return cfg_; }
+
+  // Build side from a device WKB column (decoded, boxed, indexed, banded).
+  void build(const WkbDeviceColumn& col, cudaStream_t s);
+  bool built() const { return built_; }
+  const DeviceGeoms& build_geoms() const { return bg_; }
+  const Lbvh& lbvh() const { return bvh_; }
+
+  // Probe with a device WKB column.  Results (device pointers owned by the
+  // workspace, valid until its next call) are grouped by probe row in
+  // ascending probe order; probe ids are offset by probe_base.
+  uint64_t probe(Workspace& ws, const WkbDeviceColumn& col, int predicate, double distance,
+                 uint32_t probe_base, const uint32_t** d_build, const uint32_t** d_probe);
+
+  // Refine caller-supplied candidate pairs (device arrays) against an
+  // already decoded probe column; output compacted into ws.out_*.
+  uint64_t refine_pairs(Workspace& ws, const GeomsView& probe, const uint32_t* cb,
+                        const uint32_t* cp, uint64_t m, int predicate, double distance);
+
+  JoinStats stats();
+  void reset_stats();
+
+ private:
+  int device_;
+  EngineConfig cfg_;
+  DeviceGeoms bg_;
+  DecodeScratch bsc_;
+  Lbvh bvh_;
+  bool built_ = false;
+  std::mutex stats_mu_;
+  JoinStats stats_;
+};
+
+// Host Arrow binary column view (after the Arrow C data interface is parsed).
+struct HostWkbColumn {
+  int64_t n = 0;
+  const void* offsets = nullptr;  // int32 or int64, n+1 entries (absolute into data)
+  bool offsets64 = false;
+  const uint8_t* data = nullptr;
+  const uint8_t* validity = nullptr;
+  int64_t validity_offset = 0;
+};
+
+// Copies a host column into the workspace staging buffers (H2D on ws.stream)
+// and returns the device view.  Returns the bytes copied in *bytes.
+WkbDeviceColumn stage_column(Workspace& ws, const HostWkbColumn& col, uint64_t* bytes);
+
+}  // namespace spj

@@ -1,0 +1,33 @@
+// knn.cuh — KNN join over point columns: for each probe point the k build
+// points with the smallest Euclidean distance, ties broken by build row id
+// (the ground truth of rust/sedona-spatial-join/tests/spatial_join_integration.rs:1373-1414,
+// the CPU query_knn of rust/sedona-spatial-join/src/index/default_spatial_index.rs:306-502).
+#pragma once
+#include "lbvh.cuh"
+
+namespace spj {
+
+class KnnIndex {
+ public:
+  KnnIndex(uint32_t leaf_size, int form);
+  ~KnnIndex();
+  void build(const double* xy_host, uint64_t n);
+  // probe_xy: n (x, y) FP64 pairs; outputs n*k entries; host or device arrays
+  void query(const double* probe_xy, uint64_t n, uint32_t k, uint32_t* out_idx, double* out_dist,
+             bool device_ptrs);
+  cudaStream_t stream() const { return stream_; }
+  uint64_t exact_evals() const { return exact_evals_; }
+
+ private:
+  uint32_t leaf_size_;
+  int form_;
+  cudaStream_t stream_ = nullptr;
+  uint64_t n_ = 0;
+  Lbvh bvh_;
+  DevBuf xy_sorted_;  // build points in LBVH order
+  float slack_ = 0;   // bound on |p - RN32(p)| over the build side
+  DevBuf probe_, oidx_, odist_, counters_;
+  uint64_t exact_evals_ = 0;
+};
+
+}  // namespace spj

@@ -1,0 +1,349 @@
+// lbvh.cu — LBVH build (Morton keys, device radix sort, Karras node emit,
+// bottom-up refit) and the two-pass probe traversal.
+#include "lbvh.cuh"
+#include "prims.cuh"
+
+namespace spj {
+namespace {
+
+__device__ __forceinline__ bool box_valid(float4 b) {
+  return b.x <= b.z && b.y <= b.w;  // false for NaN
+}
+
+__device__ __forceinline__ bool overlap(float4 a, float4 b) {
+  return !(a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y);
+}
+
+__device__ __forceinline__ float4 box_union(float4 a, float4 b) {
+  return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w));
+}
+
+// order-preserving float <-> u32 map for atomic min/max
+__device__ __forceinline__ uint32_t f2o(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float o2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+#else
+  uint32_t v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  float f;
+  memcpy(&f, &v, 4);
+  return f;
+#endif
+}
+
+__global__ void k_valid_flags(const float4* __restrict__ boxes, uint32_t n,
+                              uint8_t* __restrict__ flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    flag[i] = box_valid(boxes[i]) ? 1 : 0;
+}
+
+__global__ void k_compact_ids(const uint8_t* __restrict__ flag, const uint64_t* __restrict__ pos,
+                              uint32_t n, uint32_t* __restrict__ ids) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (flag[i]) ids[pos[i]] = (uint32_t)i;
+}
+
+__global__ void k_bounds(const float4* __restrict__ boxes, const uint32_t* __restrict__ ids,
+                         uint32_t m, uint32_t* __restrict__ ext) {
+  float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float4 b = boxes[ids[i]];
+    float cx = 0.5f * (b.x + b.z), cy = 0.5f * (b.y + b.w);
+    mnx = fminf(mnx, cx);
+    mny = fminf(mny, cy);
+    mxx = fmaxf(mxx, cx);
+    mxy = fmaxf(mxy, cy);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&ext[0], f2o(mnx));
+    atomicMin(&ext[1], f2o(mny));
+    atomicMax(&ext[2], f2o(mxx));
+    atomicMax(&ext[3], f2o(mxy));
+  }
+}
+
+__device__ __forceinline__ uint32_t spread16(uint32_t v) {
+  v &= 0xFFFFu;
+  v = (v | (v << 8)) & 0x00FF00FFu;
+  v = (v | (v << 4)) & 0x0F0F0F0Fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+
+__global__ void k_morton(const float4* __restrict__ boxes, const uint32_t* __restrict__ ids,
+                         uint32_t m, const uint32_t* __restrict__ ext, uint32_t* __restrict__ keys) {
+  const float x0 = o2f(ext[0]), y0 = o2f(ext[1]), x1 = o2f(ext[2]), y1 = o2f(ext[3]);
+  const float sx = x1 > x0 ? 65535.0f / (x1 - x0) : 0.0f;
+  const float sy = y1 > y0 ? 65535.0f / (y1 - y0) : 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float4 b = boxes[ids[i]];
+    float cx = 0.5f * (b.x + b.z), cy = 0.5f * (b.y + b.w);
+    uint32_t qx = (uint32_t)fminf(fmaxf((cx - x0) * sx, 0.0f), 65535.0f);
+    uint32_t qy = (uint32_t)fminf(fmaxf((cy - y0) * sy, 0.0f), 65535.0f);
+    keys[i] = (spread16(qy) << 1) | spread16(qx);
+  }
+}
+
+__global__ void k_gather_boxes(const float4* __restrict__ boxes, const uint32_t* __restrict__ ids,
+                               uint32_t m, float4* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = boxes[ids[i]];
+}
+
+// Karras (2012) node emit over leaf keys made unique by the leaf index.
+__device__ __forceinline__ int delta(const uint32_t* keys, uint32_t L, uint32_t ls, int i, int j) {
+  if (j < 0 || j >= (int)L) return -1;
+  uint32_t a = keys[(size_t)i * ls], b = keys[(size_t)j * ls];
+  if (a != b) return __clz(a ^ b);
+  return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+__global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t L, uint32_t ls,
+                         int2* __restrict__ child, int* __restrict__ parent_int,
+                         int* __restrict__ parent_leaf) {
+  for (int64_t ii = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ii < (int64_t)L - 1;
+       ii += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)ii;
+    const int d = (delta(keys, L, ls, i, i + 1) - delta(keys, L, ls, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, L, ls, i, i - d);
+    int lmax = 2;
+    while (delta(keys, L, ls, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+      if (delta(keys, L, ls, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = delta(keys, L, ls, i, j);
+    int sp = 0;
+    int t = l;
+    do {
+      t = (t + 1) >> 1;
+      if (delta(keys, L, ls, i, i + (sp + t) * d) > dnode) sp += t;
+    } while (t > 1);
+    const int gamma = i + sp * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    int left = (lo == gamma) ? ~gamma : gamma;
+    int right = (hi == gamma + 1) ? ~(gamma + 1) : (gamma + 1);
+    child[i] = make_int2(left, right);
+    if (left < 0) parent_leaf[~left] = (i << 1) | 0;
+    else parent_int[left] = (i << 1) | 0;
+    if (right < 0) parent_leaf[~right] = (i << 1) | 1;
+    else parent_int[right] = (i << 1) | 1;
+  }
+}
+
+// Bottom-up refit: each leaf computes its box, writes it into its parent's
+// child slot, and the second thread to arrive at a node carries on upward.
+__global__ void k_refit(const float4* __restrict__ sbox, uint32_t m, uint32_t L, uint32_t ls,
+                        const int* __restrict__ parent_int, const int* __restrict__ parent_leaf,
+                        float4* __restrict__ node_box, unsigned* __restrict__ visits) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < L;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t b0 = (uint32_t)c * ls, b1 = min(b0 + ls, m);
+    float4 bb = sbox[b0];
+    for (uint32_t k = b0 + 1; k < b1; k++) bb = box_union(bb, sbox[k]);
+    int slot = parent_leaf[c];
+    while (true) {
+      int node = slot >> 1;
+      node_box[slot] = bb;
+      __threadfence();
+      unsigned prev = atomicAdd(&visits[node], 1u);
+      if (prev == 0) break;  // sibling not done yet; it will continue
+      __threadfence();
+      // the sibling's box was written by another SM: read past L1
+      float4 a = __ldcg(&node_box[2 * node]), b = __ldcg(&node_box[2 * node + 1]);
+      bb = box_union(a, b);
+      if (node == 0) break;  // root
+      slot = parent_int[node];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// traversal
+
+constexpr int kTravThreads = 128;
+constexpr int kStack = 64;
+
+template <bool kScatter>
+__global__ void __launch_bounds__(kTravThreads)
+    k_probe(LbvhView t, const float4* __restrict__ probe_box, uint32_t nprobe,
+            uint32_t* __restrict__ counts, const uint64_t* __restrict__ offs, uint32_t probe_base,
+            uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe) {
+  // per-thread stack in shared memory, [depth][thread] so a warp's pushes hit
+  // 32 distinct banks
+  __shared__ int stack[kStack * kTravThreads];
+  for (int64_t pi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pi < nprobe;
+       pi += (int64_t)gridDim.x * blockDim.x) {
+    const float4 q = probe_box[pi];
+    uint32_t cnt = 0;
+    uint64_t pos = kScatter ? offs[pi] : 0;
+    if (box_valid(q) && t.nprims > 0) {
+      int sp = 0;
+      int node = t.nleaves > 1 ? 0 : ~0;  // root: internal node 0, or the single leaf
+      while (true) {
+        if (node < 0) {
+          const uint32_t c = (uint32_t)(~node);
+          const uint32_t b0 = c * t.leaf_size;
+          const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+          for (uint32_t k = b0; k < b1; k++) {
+            if (overlap(t.sorted_box[k], q)) {
+              if (kScatter) {
+                out_build[pos] = t.sorted_id[k];
+                out_probe[pos] = (uint32_t)pi + probe_base;
+                pos++;
+              } else {
+                cnt++;
+              }
+            }
+          }
+        } else {
+          const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+          const int2 ch = t.node_child[node];
+          const bool hl = overlap(lb, q), hr = overlap(rb, q);
+          if (hl && hr) {
+            if (sp < kStack) stack[sp * kTravThreads + threadIdx.x] = ch.y;
+            sp++;
+            node = ch.x;
+            continue;
+          }
+          if (hl) {
+            node = ch.x;
+            continue;
+          }
+          if (hr) {
+            node = ch.y;
+            continue;
+          }
+        }
+        if (sp == 0) break;
+        sp--;
+        node = sp < kStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
+      }
+    }
+    if (!kScatter) counts[pi] = cnt;
+  }
+}
+
+__global__ void k_expand(const double2* __restrict__ pts, const float4* __restrict__ boxes,
+                         const uint8_t* __restrict__ kind, uint32_t n, double d,
+                         float4* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float q = __int_as_float(0x7fc00000);
+    float4 o = make_float4(q, q, q, q);
+    if (kind[i] == 1) {
+      double2 p = pts[i];
+      double lo[2] = {p.x - d, p.y - d}, hi[2] = {p.x + d, p.y + d};
+      float fl[2], fh[2];
+      for (int a = 0; a < 2; a++) {
+        float x = __double2float_rn(lo[a]), y = __double2float_rn(hi[a]);
+        if ((double)x > lo[a]) x = next_downf(x);
+        if ((double)y < hi[a]) y = next_upf(y);
+        fl[a] = x;
+        fh[a] = y;
+      }
+      o = make_float4(fl[0], fl[1], fh[0], fh[1]);
+    } else if (kind[i] != 0) {
+      o = boxes[i];  // non-point rows: distance joins are point-only; caller rejects
+    }
+    out[i] = o;
+  }
+}
+
+}  // namespace
+
+void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, cudaStream_t s) {
+  SPJ_CHECK(leaf_size >= 1 && leaf_size <= 64, "leaf size must be in [1, 64]");
+  out.leaf_size = leaf_size;
+  DevBuf flag((size_t)n + 1, s), pos(((size_t)n + 1) * 8, s), tmp;
+  const int g = grid_for(n, 256);
+  k_valid_flags<<<g, 256, 0, s>>>(boxes, n, flag.as<uint8_t>());
+  scan_u8_u64(flag.as<uint8_t>(), pos.as<uint64_t>(), n, tmp, s);
+  uint64_t m64 = 0;
+  SPJ_CUDA(cudaMemcpyAsync(&m64, pos.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  const uint32_t m = (uint32_t)m64;
+  out.nprims = m;
+  out.nleaves = m ? (m + leaf_size - 1) / leaf_size : 0;
+  out.sorted_box.reserve(((size_t)m + 1) * sizeof(float4), s);
+  out.sorted_id.reserve(((size_t)m + 1) * 4, s);
+  const uint32_t L = out.nleaves;
+  out.node_box.reserve((size_t)(L > 1 ? 2 * (L - 1) : 1) * sizeof(float4), s);
+  out.node_child.reserve((size_t)(L > 1 ? L - 1 : 1) * sizeof(int2), s);
+  if (m == 0) return;
+  uint32_t* ids = out.sorted_id.as<uint32_t>();
+  k_compact_ids<<<g, 256, 0, s>>>(flag.as<uint8_t>(), pos.as<uint64_t>(), n, ids);
+  DevBuf ext(16, s);
+  uint32_t init[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u};
+  SPJ_CUDA(cudaMemcpyAsync(ext.get(), init, 16, cudaMemcpyHostToDevice, s));
+  const int gm = grid_for(m, 256);
+  k_bounds<<<gm, 256, 0, s>>>(boxes, ids, m, ext.as<uint32_t>());
+  DevBuf keys((size_t)m * 4, s), akeys((size_t)m * 4, s), avals((size_t)m * 4, s);
+  k_morton<<<gm, 256, 0, s>>>(boxes, ids, m, ext.as<uint32_t>(), keys.as<uint32_t>());
+  radix_sort_pairs(keys.as<uint32_t>(), ids, akeys.as<uint32_t>(), avals.as<uint32_t>(), m, 32,
+                   tmp, s);
+  k_gather_boxes<<<gm, 256, 0, s>>>(boxes, ids, m, out.sorted_box.as<float4>());
+  if (L > 1) {
+    DevBuf parent_int((size_t)L * 4, s), parent_leaf((size_t)L * 4, s), visits((size_t)L * 4, s);
+    SPJ_CUDA(cudaMemsetAsync(visits.get(), 0, (size_t)L * 4, s));
+    k_karras<<<grid_for(L - 1, 256), 256, 0, s>>>(keys.as<uint32_t>(), L, leaf_size,
+                                                  out.node_child.as<int2>(),
+                                                  parent_int.as<int>(), parent_leaf.as<int>());
+    k_refit<<<grid_for(L, 256), 256, 0, s>>>(out.sorted_box.as<float4>(), m, L, leaf_size,
+                                             parent_int.as<int>(), parent_leaf.as<int>(),
+                                             out.node_box.as<float4>(), visits.as<unsigned>());
+  }
+  SPJ_CUDA(cudaGetLastError());
+  SPJ_CUDA(cudaStreamSynchronize(s));
+}
+
+uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                     ProbeScratch& sc, cudaStream_t s) {
+  sc.counts.reserve(((size_t)nprobe + 1) * 4, s);
+  sc.offsets.reserve(((size_t)nprobe + 1) * 8, s);
+  if (nprobe == 0) return 0;
+  const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
+  k_probe<false><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, sc.counts.as<uint32_t>(),
+                                            nullptr, 0, nullptr, nullptr);
+  scan_u32_u64(sc.counts.as<uint32_t>(), sc.offsets.as<uint64_t>(), nprobe, sc.tmp, s);
+  uint64_t total = 0;
+  SPJ_CUDA(cudaMemcpyAsync(&total, sc.offsets.as<uint64_t>() + nprobe, 8, cudaMemcpyDeviceToHost,
+                           s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  return total;
+}
+
+void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                   const ProbeScratch& sc, uint32_t probe_base, uint32_t* out_build,
+                   uint32_t* out_probe, cudaStream_t s) {
+  if (nprobe == 0) return;
+  const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
+  k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr,
+                                           sc.offsets.as<uint64_t>(), probe_base, out_build,
+                                           out_probe);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void expand_boxes(const double2* pts, const float4* boxes, const uint8_t* kind, uint32_t n,
+                  double distance, float4* out, cudaStream_t s) {
+  if (n == 0) return;
+  k_expand<<<grid_for(n, 256), 256, 0, s>>>(pts, boxes, kind, n, distance, out);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+}  // namespace spj

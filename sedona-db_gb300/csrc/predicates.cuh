@@ -1,0 +1,403 @@
+// predicates.cuh — device restatement of the reference refiner's predicate
+// arithmetic (the tg library, c/sedona-tg/src/tg/tg.c, which the reference
+// CPU join calls as tg_geom_<pred>(build, probe),
+// rust/sedona-spatial-join/src/refine/tg.rs:322-357).
+//
+// Two tiers per segment test:
+//   * an FP32 classifier on round-to-nearest copies of the coordinates that
+//     only decides a segment when a strict FP32 comparison proves the FP64
+//     comparison tg makes (round-to-nearest is monotone, so RN(a) < RN(b)
+//     implies a < b); everything else escalates;
+//   * the FP64 path, which repeats tg's operation sequence exactly (including
+//     its division-based slope test and nextafter nudges), so escalated
+//     decisions are the reference's decisions bit for bit.
+// The library is compiled with --fmad=false so no multiply-add is fused.
+#pragma once
+#include "geoms.cuh"
+
+namespace spj {
+namespace pred {
+
+enum { kOut = 0, kIn = 1, kOn = 2 };
+
+__device__ __forceinline__ bool feq(double x, double y) { return !((x < y) | (x > y)); }
+__device__ __forceinline__ bool eq_zero(double x) { return feq(x, 0.0); }
+__device__ __forceinline__ double fmin0(double x, double y) { return x < y ? x : y; }
+__device__ __forceinline__ double fmax0(double x, double y) { return x > y ? x : y; }
+__device__ __forceinline__ float fmin0f(float x, float y) { return x < y ? x : y; }
+__device__ __forceinline__ float fmax0f(float x, float y) { return x > y ? x : y; }
+__device__ __forceinline__ bool pteq(double2 a, double2 b) { return feq(a.x, b.x) && feq(a.y, b.y); }
+
+// tg.c:861-900
+__device__ __noinline__ bool collinear(double x1, double y1, double x2, double y2, double x3,
+                                       double y3) {
+  const bool x1x2 = feq(x1, x2), x1x3 = feq(x1, x3), x2x3 = feq(x2, x3);
+  const bool y1y2 = feq(y1, y2), y1y3 = feq(y1, y3), y2y3 = feq(y2, y3);
+  if (x1x2) return x1x3;
+  if (y1y2) return y1y3;
+  if ((x1x2 & y1y2) | (x1x3 & y1y3) | (x2x3 & y2y3)) return true;
+  const double cx1 = __dsub_rn(x3, x1), cy1 = __dsub_rn(y3, y1);
+  const double cx2 = __dsub_rn(x2, x1), cy2 = __dsub_rn(y2, y1);
+  double s1 = __dmul_rn(cx1, cy2);
+  double s2 = __dmul_rn(cy1, cx2);
+  const double s3 = __dsub_rn(__ddiv_rn(s1, cy2), cx1);
+  const double s4 = __dsub_rn(__ddiv_rn(s2, cx2), cy1);
+  if (s3 < 0) s1 = next_down(s1);
+  else if (s3 > 0) s1 = next_up(s1);
+  if (s4 < 0) s2 = next_down(s2);
+  else if (s4 > 0) s2 = next_up(s2);
+  return eq_zero(__dsub_rn(s1, s2));
+}
+
+// tg.c:1192-1197 with tg_rect_covers_point (tg.c:1776-1785)
+__device__ __forceinline__ bool point_on_segment(double2 p, double2 a, double2 b) {
+  const double mnx = fmin0(a.x, b.x), mny = fmin0(a.y, b.y);
+  const double mxx = fmax0(a.x, b.x), mxy = fmax0(a.y, b.y);
+  if (p.x < mnx || p.y < mny || p.x > mxx || p.y > mxy) return false;
+  return collinear(a.x, a.y, b.x, b.y, p.x, p.y);
+}
+
+// tg.c:1199-1276: +x ray from p against segment (sa, sb)
+__device__ __noinline__ int raycast(double2 sa, double2 sb, double2 p) {
+  const double rminx = fmin0(sa.x, sb.x), rminy = fmin0(sa.y, sb.y);
+  const double rmaxx = fmax0(sa.x, sb.x), rmaxy = fmax0(sa.y, sb.y);
+  if (p.y < rminy || p.y > rmaxy) return kOut;
+  if (p.x < rminx) {
+    if (p.y != rminy && p.y != rmaxy) return kIn;
+  } else if (p.x > rmaxx) {
+    if (rminy != rmaxy && rminx != rmaxx) return kOut;
+  }
+  double2 a = sa, b = sb;
+  if (b.y < a.y) {
+    double2 t = a;
+    a = b;
+    b = t;
+  }
+  if (pteq(p, a) || pteq(p, b)) return kOn;
+  if (a.y == b.y) {
+    if (a.x == b.x) return kOut;
+    if (p.y == b.y) {
+      if (!(p.x < rminx || p.x > rmaxx)) return kOn;
+    }
+  }
+  if (a.x == b.x && p.x == b.x) {
+    if (p.y >= a.y && p.y <= b.y) return kOn;
+  }
+  if (collinear(a.x, a.y, b.x, b.y, p.x, p.y)) {
+    if (p.x < rminx) {
+      if (rminy == rmaxy) return kOut;
+    } else if (p.x > rmaxx) {
+      return kOut;
+    }
+    return kOn;
+  }
+  double py = p.y;
+  if (py == a.y || py == b.y) py = next_up(py);
+  if (py < a.y || py > b.y) return kOut;
+  if (a.x > b.x) {
+    if (p.x >= a.x) return kOut;
+    if (p.x <= b.x) return kIn;
+  } else {
+    if (p.x >= b.x) return kOut;
+    if (p.x <= a.x) return kIn;
+  }
+  const double lhs = __ddiv_rn(__dsub_rn(py, a.y), __dsub_rn(p.x, a.x));
+  const double rhs = __ddiv_rn(__dsub_rn(b.y, a.y), __dsub_rn(b.x, a.x));
+  return lhs >= rhs ? kIn : kOut;
+}
+
+// tg.c:1392-1440
+__device__ __noinline__ bool seg_intersects_seg(double2 a, double2 b, double2 c, double2 d) {
+  {
+    const double aminx = fmin0(a.x, b.x), aminy = fmin0(a.y, b.y);
+    const double amaxx = fmax0(a.x, b.x), amaxy = fmax0(a.y, b.y);
+    const double bminx = fmin0(c.x, d.x), bminy = fmin0(c.y, d.y);
+    const double bmaxx = fmax0(c.x, d.x), bmaxy = fmax0(c.y, d.y);
+    if (bminx > amaxx || bmaxx < aminx || bminy > amaxy || bmaxy < aminy) return false;
+  }
+  if (pteq(a, c) || pteq(a, d) || pteq(b, c) || pteq(b, d)) return true;
+  const double cmpx = __dsub_rn(c.x, a.x), cmpy = __dsub_rn(c.y, a.y);
+  const double rx = __dsub_rn(b.x, a.x), ry = __dsub_rn(b.y, a.y);
+  const double cmpxr = __dsub_rn(__dmul_rn(cmpx, ry), __dmul_rn(cmpy, rx));
+  if (eq_zero(cmpxr)) {
+    if (!(((__dsub_rn(c.x, a.x) <= 0) != (__dsub_rn(c.x, b.x) <= 0))) ||
+        ((__dsub_rn(c.y, a.y) <= 0) != (__dsub_rn(c.y, b.y) <= 0))) {
+      return point_on_segment(c, a, b) || point_on_segment(d, a, b) ||
+             point_on_segment(a, c, d) || point_on_segment(b, c, d);
+    }
+    return true;
+  }
+  const double sx = __dsub_rn(d.x, c.x), sy = __dsub_rn(d.y, c.y);
+  const double rxs = __dsub_rn(__dmul_rn(rx, sy), __dmul_rn(ry, sx));
+  if (eq_zero(rxs)) return false;
+  const double cmpxs = __dsub_rn(__dmul_rn(cmpx, sy), __dmul_rn(cmpy, sx));
+  const double rxsr = __ddiv_rn(1.0, rxs);
+  const double t = __dmul_rn(cmpxs, rxsr);
+  const double u = __dmul_rn(cmpxr, rxsr);
+  if (!((t >= 0) && (t <= 1) && (u >= 0) && (u <= 1))) return false;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// per-ring point evaluation (tg.c:2668-2735, 2809-2822)
+
+struct RingHit {
+  bool hit;
+  int idx;
+};
+
+// One segment's contribution, FP64 (tg pip_eval_seg + pip_eval_seg_slow).
+__device__ __forceinline__ void pip_seg_f64(double2 a, double2 b, double2 p, int i, bool aoe,
+                                            bool& in, int& idx) {
+  const double ymin = fmin0(a.y, b.y), ymax = fmax0(a.y, b.y);
+  if (p.y < ymin || p.y > ymax) return;
+  switch (raycast(a, b, p)) {
+    case kIn:
+      if (idx == -1) in = !in;
+      break;
+    case kOn:
+      in = aoe;
+      idx = i;
+      break;
+    default:
+      break;
+  }
+}
+
+// FP32 classification of one segment: returns kOut / kIn when a strict
+// comparison of round-to-nearest values proves tg's FP64 early exit, or -1.
+__device__ __forceinline__ int pip_seg_f32(float2 a, float2 b, float2 p) {
+  const float ymin = fmin0f(a.y, b.y), ymax = fmax0f(a.y, b.y);
+  if (p.y < ymin || p.y > ymax) return kOut;
+  const float xmin = fmin0f(a.x, b.x), xmax = fmax0f(a.x, b.x);
+  if (p.x < xmin && p.y > ymin && p.y < ymax) return kIn;
+  if (p.x > xmax && ymin < ymax && xmin < xmax) return kOut;
+  return -1;
+}
+
+__device__ __forceinline__ bool rect_covers_point(Rect64 r, double2 p) {
+  return !(p.x < r.x || p.y < r.y || p.x > r.z || p.y > r.w);
+}
+
+__device__ __forceinline__ int band_of(float y32, float y0, float inv_h, int nb) {
+  float t = __fmul_rn(__fsub_rn(y32, y0), inv_h);
+  if (!(t >= 0.0f)) return 0;
+  float f = floorf(t);
+  if (f >= (float)(nb - 1)) return nb - 1;
+  return (int)f;
+}
+
+// Plain FP64 form: every segment through tg's FP64 sequence.
+__device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r, double2 p,
+                                                  bool aoe) {
+  RingHit h{false, -1};
+  if (!rect_covers_point(G.ring_rect[r], p)) return h;
+  const uint32_t V = G.ring_vtx[r];
+  const int ns = G.ring_nsegs[r];
+  bool in = false;
+  int idx = -1;
+  double2 a = G.xy[V];
+  for (int i = 0; i < ns; i++) {
+    const double2 b = G.xy[V + i + 1];
+    pip_seg_f64(a, b, p, i, aoe, in, idx);
+    a = b;
+  }
+  h.hit = in;
+  h.idx = idx;
+  return h;
+}
+
+// Chosen form: y-band edge index + FP32 classification + FP64 escalation.
+// Without a band index on this column the ring's segments are all scanned
+// (still with the FP32 classifier).  Segments are visited in increasing
+// index order, so idx (last ON segment) matches tg's sequential walk.
+__device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r, double2 p,
+                                                 float2 p32, bool aoe, uint32_t& esc) {
+  RingHit h{false, -1};
+  if (!rect_covers_point(G.ring_rect[r], p)) return h;
+  const uint32_t V = G.ring_vtx[r];
+  bool in = false;
+  int idx = -1;
+  bool banded = G.ring_bands != nullptr && G.band_param[r].y >= 0.0f;
+  if (banded) {
+    const uint32_t B = G.ring_bands[r];
+    const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
+    const float2 prm = G.band_param[r];
+    const int b = band_of(p32.y, prm.x, prm.y, nb);
+    const uint32_t e0 = G.band_off[B + b], e1 = G.band_off[B + b + 1];
+    for (uint32_t k = e0; k < e1; k++) {
+      const int i = G.band_edges[k];
+      const int c = pip_seg_f32(G.xy32[V + i], G.xy32[V + i + 1], p32);
+      if (c == kOut) continue;
+      if (c == kIn) {
+        if (idx == -1) in = !in;
+        continue;
+      }
+      esc++;
+      pip_seg_f64(G.xy[V + i], G.xy[V + i + 1], p, i, aoe, in, idx);
+    }
+  } else {
+    const int ns = G.ring_nsegs[r];
+    float2 a32 = G.xy32[V];
+    for (int i = 0; i < ns; i++) {
+      const float2 b32 = G.xy32[V + i + 1];
+      const int c = pip_seg_f32(a32, b32, p32);
+      a32 = b32;
+      if (c == kOut) continue;
+      if (c == kIn) {
+        if (idx == -1) in = !in;
+        continue;
+      }
+      esc++;
+      pip_seg_f64(G.xy[V + i], G.xy[V + i + 1], p, i, aoe, in, idx);
+    }
+  }
+  h.hit = in;
+  h.idx = idx;
+  return h;
+}
+
+template <bool kFast>
+__device__ __forceinline__ RingHit ring_pip(const GeomsView& G, uint32_t r, double2 p, float2 p32,
+                                            bool aoe, uint32_t& esc) {
+  if (kFast) return ring_pip_fast(G, r, p, p32, aoe, esc);
+  return ring_pip_plain(G, r, p, aoe);
+}
+
+__device__ __forceinline__ uint32_t ring_npts(const GeomsView& G, uint32_t r) {
+  return G.ring_vtx[r + 1] - G.ring_vtx[r] - 1;
+}
+
+// tg.c:3909-3934 (a polygon without holes is a tg ring, tg.c:3785-3789)
+template <bool kFast>
+__device__ __forceinline__ bool poly_contains_point(const GeomsView& G, uint32_t part, double2 p,
+                                                    float2 p32, bool aoe, uint32_t& esc) {
+  const uint32_t r0 = G.part_ring[part], r1 = G.part_ring[part + 1];
+  if (r1 - r0 == 1) return ring_pip<kFast>(G, r0, p, p32, aoe, esc).hit;
+  if (ring_npts(G, r0) < 3) return false;  // tg_poly_empty
+  if (!ring_pip<kFast>(G, r0, p, p32, aoe, esc).hit) return false;
+  for (uint32_t h = r0 + 1; h < r1; h++)
+    if (ring_pip<kFast>(G, h, p, p32, !aoe, esc).hit) return false;
+  return true;
+}
+
+// tg.c:1171-1190 + tg.c:3436-3443: p lies on a segment of any ring
+template <bool kFast>
+__device__ __forceinline__ bool poly_touches_point(const GeomsView& G, uint32_t part, double2 p,
+                                                   float2 p32, uint32_t& esc) {
+  const uint32_t r0 = G.part_ring[part], r1 = G.part_ring[part + 1];
+  for (uint32_t r = r0; r < r1; r++) {
+    const uint32_t V = G.ring_vtx[r];
+    const int ns = G.ring_nsegs[r];
+    for (int i = 0; i < ns; i++) {
+      if (kFast) {
+        // point_on_segment starts with a rect cover test; strict FP32
+        // separation proves it fails
+        const float2 a = G.xy32[V + i], b = G.xy32[V + i + 1];
+        if (p32.x < fmin0f(a.x, b.x) || p32.x > fmax0f(a.x, b.x) || p32.y < fmin0f(a.y, b.y) ||
+            p32.y > fmax0f(a.y, b.y))
+          continue;
+        esc++;
+      }
+      if (point_on_segment(p, G.xy[V + i], G.xy[V + i + 1])) return true;
+    }
+  }
+  return false;
+}
+
+// Number of segments of ring r intersecting segment (a, b), stopping at 2
+// (tg.c:3046-3087 with allow_on_edge; tg_ring_search filter tg.c:2468-2485).
+template <bool kFast>
+__device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, double2 a, double2 b,
+                                             uint32_t& esc) {
+  const uint32_t V = G.ring_vtx[r];
+  int count = 0;
+  if (!kFast) {
+    const int ns = G.ring_nsegs[r];
+    for (int i = 0; i < ns && count < 2; i++)
+      if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
+    return count;
+  }
+  const float2 a32 = make_float2(__double2float_rn(a.x), __double2float_rn(a.y));
+  const float2 b32 = make_float2(__double2float_rn(b.x), __double2float_rn(b.y));
+  const float qx0 = fmin0f(a32.x, b32.x), qx1 = fmax0f(a32.x, b32.x);
+  const float qy0 = fmin0f(a32.y, b32.y), qy1 = fmax0f(a32.y, b32.y);
+  auto test = [&](int i) {
+    const float2 c = G.xy32[V + i], d = G.xy32[V + i + 1];
+    if (fmin0f(c.x, d.x) > qx1 || fmax0f(c.x, d.x) < qx0 || fmin0f(c.y, d.y) > qy1 ||
+        fmax0f(c.y, d.y) < qy0)
+      return;  // strictly separated rects: tg's first test fails
+    esc++;
+    if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
+  };
+  const bool banded = G.ring_bands != nullptr && G.band_param[r].y >= 0.0f;
+  if (banded) {
+    const uint32_t B = G.ring_bands[r];
+    const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
+    const float2 prm = G.band_param[r];
+    const int b0 = band_of(qy0, prm.x, prm.y, nb), b1 = band_of(qy1, prm.x, prm.y, nb);
+    for (int bb = b0; bb <= b1 && count < 2; bb++) {
+      const uint32_t e0 = G.band_off[B + bb], e1 = G.band_off[B + bb + 1];
+      for (uint32_t k = e0; k < e1 && count < 2; k++) {
+        const int i = G.band_edges[k];
+        if (bb > b0) {
+          // visit each segment once: only in the first band of the query it spans
+          const float2 c = G.xy32[V + i], d = G.xy32[V + i + 1];
+          if (band_of(fmin0f(c.y, d.y), prm.x, prm.y, nb) < bb) continue;
+        }
+        test(i);
+      }
+    }
+  } else {
+    const int ns = G.ring_nsegs[r];
+    for (int i = 0; i < ns && count < 2; i++) test(i);
+  }
+  return count;
+}
+
+__device__ __forceinline__ double rect_area(Rect64 r) {
+  return __dmul_rn(__dsub_rn(r.z, r.x), __dsub_rn(r.w, r.y));
+}
+
+// tg.c:3166-3192 + tg.c:3089-3113 with allow_on_edge = true, for two rings.
+// The result is the OR over the smaller ring's vertices of "vertex in or on
+// the larger ring" and over its segments of "crosses >= 2 of the larger
+// ring's segments"; tg's per-segment rect test only skips terms that are
+// false, so the vertex tests run first and the result is the same.
+template <bool kFast>
+__device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32_t ra,
+                                                     const GeomsView& GB, uint32_t rb,
+                                                     uint32_t& esc) {
+  if (ring_npts(GA, ra) < 3 || ring_npts(GB, rb) < 3) return false;
+  const Rect64 A = GA.ring_rect[ra], Bq = GB.ring_rect[rb];
+  if (Bq.x > A.z || Bq.z < A.x || Bq.y > A.w || Bq.w < A.y) return false;
+  const GeomsView* Gr = &GA;
+  const GeomsView* Go = &GB;
+  uint32_t rr = ra, ro = rb;
+  if (rect_area(Bq) > rect_area(A)) {
+    Gr = &GB;
+    Go = &GA;
+    rr = rb;
+    ro = ra;
+  }
+  const uint32_t Vo = Go->ring_vtx[ro];
+  const int nso = Go->ring_nsegs[ro];
+  for (int i = 0; i <= nso; i++) {
+    const double2 v = Go->xy[Vo + i];
+    const float2 v32 = Go->xy32[Vo + i];
+    if (ring_pip<kFast>(*Gr, rr, v, v32, true, esc).hit) return true;
+  }
+  const Rect64 R = Gr->ring_rect[rr];
+  for (int i = 0; i < nso; i++) {
+    const double2 a = Go->xy[Vo + i], b = Go->xy[Vo + i + 1];
+    // tg.c:3092-3094 segment rect vs ring rect
+    if (fmin0(a.x, b.x) > R.z || fmax0(a.x, b.x) < R.x || fmin0(a.y, b.y) > R.w ||
+        fmax0(a.y, b.y) < R.y)
+      continue;
+    if (ring_seg_hits<kFast>(*Gr, rr, a, b, esc) >= 2) return true;
+  }
+  return false;
+}
+
+}  // namespace pred
+}  // namespace spj

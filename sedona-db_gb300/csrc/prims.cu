@@ -1,0 +1,260 @@
+// prims.cu — device-wide scans and an 8-bit LSD radix sort.
+//
+// Scan: reduce-then-scan over 4096-element tiles (256 threads x 16 items);
+// the tile sums are scanned by one 1024-thread block that walks them in
+// chunks, then each tile is rescanned with its prefix.  Two reads of the
+// input plus one write of the output: the scan is HBM-bound.
+//
+// Radix sort: per 8-bit digit, (1) a per-tile 256-bin histogram, (2) a scan of
+// the digit-major histogram table, (3) a stable block-local split sort of the
+// tile in shared memory by the 8 digit bits, then a scatter whose runs of
+// equal digits land on consecutive addresses.
+#include "prims.cuh"
+
+namespace spj {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <class Tin, class Tout>
+__global__ void k_tile_reduce(const Tin* __restrict__ in, int64_t n, Tout* __restrict__ sums) {
+  __shared__ Tout sm[9];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  Tout acc = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; j++) {
+    int64_t i = base + j * kScanThreads + threadIdx.x;
+    if (i < n) acc += (Tout)in[i];
+  }
+  Tout total;
+  block_exclusive_scan_256<Tout>(acc, sm, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+template <class T>
+__global__ void k_scan_sums(T* __restrict__ sums, int64_t nt, T* __restrict__ total_out) {
+  // one block of 1024 threads scans all tile sums in place (exclusive)
+  __shared__ T warp_tot[32];
+  __shared__ T carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t b = 0; b < nt; b += blockDim.x) {
+    int64_t i = b + threadIdx.x;
+    T v = i < nt ? sums[i] : T(0);
+    T inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      T w = warp_tot[lane];
+      T wi = warp_inclusive_scan(w);
+      warp_tot[lane] = wi - w;
+    }
+    __syncthreads();
+    T ex = carry + warp_tot[warp] + inc - v;
+    if (i < nt) sums[i] = ex;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = ex + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+template <class Tin, class Tout>
+__global__ void k_tile_scan(const Tin* __restrict__ in, int64_t n, const Tout* __restrict__ sums,
+                            Tout* __restrict__ out) {
+  __shared__ Tout sm[9];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  // blocked arrangement: thread t owns items [t*16, t*16+16) of the tile
+  Tout v[kScanItems];
+  Tout acc = 0;
+  const int64_t mybase = base + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+  for (int j = 0; j < kScanItems; j++) {
+    int64_t i = mybase + j;
+    v[j] = i < n ? (Tout)in[i] : Tout(0);
+    acc += v[j];
+  }
+  Tout ex = block_exclusive_scan_256<Tout>(acc, sm, nullptr) + sums[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < kScanItems; j++) {
+    int64_t i = mybase + j;
+    if (i < n) out[i] = ex;
+    ex += v[j];
+  }
+}
+
+template <class Tin, class Tout>
+void scan_impl(const Tin* in, Tout* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
+  int64_t nt = (n + kScanTile - 1) / kScanTile;
+  if (nt < 1) nt = 1;
+  tmp.reserve((size_t)(nt + 1) * sizeof(Tout), s);
+  Tout* sums = tmp.as<Tout>();
+  if (n == 0) {
+    SPJ_CUDA(cudaMemsetAsync(out, 0, sizeof(Tout), s));
+    return;
+  }
+  k_tile_reduce<Tin, Tout><<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums);
+  k_scan_sums<Tout><<<1, 1024, 0, s>>>(sums, nt, out + n);
+  k_tile_scan<Tin, Tout><<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums, out);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// radix sort
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+
+__global__ void k_digit_hist(const uint32_t* __restrict__ keys, int64_t n, int shift,
+                             uint32_t* __restrict__ hist, int64_t ntiles) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+#pragma unroll
+  for (int j = 0; j < kSortItems; j++) {
+    int64_t i = base + j * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  // digit-major layout: offset of (digit, tile) after the scan
+  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_digit_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                int64_t n, int shift, const uint32_t* __restrict__ offs,
+                                int64_t ntiles, uint32_t* __restrict__ okeys,
+                                uint32_t* __restrict__ ovals) {
+  __shared__ uint32_t sk[kSortTile];
+  __shared__ uint32_t sv[kSortTile];
+  __shared__ uint32_t scan_sm[9];
+  __shared__ uint32_t dstart[256];
+  __shared__ uint32_t gbase[256];
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+  const int cnt = (int)min((int64_t)kSortTile, n - base);
+  // load the tile in blocked order (thread t holds [t*8, t*8+8))
+  uint32_t k[kSortItems], v[kSortItems];
+#pragma unroll
+  for (int j = 0; j < kSortItems; j++) {
+    int li = threadIdx.x * kSortItems + j;
+    if (li < cnt) {
+      k[j] = keys[base + li];
+      v[j] = vals[base + li];
+    } else {
+      k[j] = 0xFFFFFFFFu;  // pads sort to the end and are never written
+      v[j] = 0;
+    }
+  }
+  // stable split sort by the 8 digit bits, LSB first
+  for (int b = 0; b < 8; b++) {
+    uint32_t ones = 0;
+#pragma unroll
+    for (int j = 0; j < kSortItems; j++) ones += (k[j] >> (shift + b)) & 1u;
+    if (shift + b >= 32) ones = 0;
+    uint32_t total_ones;
+    uint32_t ones_before = block_exclusive_scan_256<uint32_t>(ones, scan_sm, &total_ones);
+    const uint32_t nzero = kSortTile - total_ones;
+    uint32_t zeros_before = threadIdx.x * kSortItems - ones_before;
+#pragma unroll
+    for (int j = 0; j < kSortItems; j++) {
+      uint32_t bit = (shift + b < 32) ? ((k[j] >> (shift + b)) & 1u) : 0u;
+      uint32_t dst = bit ? nzero + ones_before : zeros_before;
+      if (bit) ones_before++;
+      else zeros_before++;
+      sk[dst] = k[j];
+      sv[dst] = v[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSortItems; j++) {
+      k[j] = sk[threadIdx.x * kSortItems + j];
+      v[j] = sv[threadIdx.x * kSortItems + j];
+    }
+    __syncthreads();
+  }
+  // first position of each digit in the sorted tile
+  dstart[threadIdx.x] = 0xFFFFFFFFu;
+  gbase[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kSortItems; j++) {
+    int li = threadIdx.x * kSortItems + j;
+    if (li < cnt) {
+      uint32_t d = (k[j] >> shift) & 0xFF;
+      uint32_t prevd = li > 0 ? ((sk[li - 1] >> shift) & 0xFF) : 0xFFFFFFFFu;
+      if (li == 0 || prevd != d) dstart[d] = li;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kSortItems; j++) {
+    int li = threadIdx.x * kSortItems + j;
+    if (li < cnt) {
+      uint32_t d = (k[j] >> shift) & 0xFF;
+      uint64_t dst = (uint64_t)gbase[d] + (uint32_t)(li - dstart[d]);
+      okeys[dst] = k[j];
+      ovals[dst] = v[j];
+    }
+  }
+}
+
+}  // namespace
+
+void scan_u32_u64(const uint32_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
+  scan_impl<uint32_t, uint64_t>(in, out, n, tmp, s);
+}
+void scan_u8_u64(const uint8_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
+  scan_impl<uint8_t, uint64_t>(in, out, n, tmp, s);
+}
+void scan_u32_u32(const uint32_t* in, uint32_t* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
+  scan_impl<uint32_t, uint32_t>(in, out, n, tmp, s);
+}
+
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
+                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s) {
+  if (n <= 1) return;
+  SPJ_CHECK(n < (int64_t)0xFFFFFFFF, "radix sort: too many keys");
+  const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
+  const int64_t nh = 256 * ntiles;
+  tmp.reserve((size_t)(2 * nh + 1) * sizeof(uint32_t) + 4096 * 8, s);
+  uint32_t* hist = tmp.as<uint32_t>();
+  uint32_t* offs = hist + nh;
+  DevBuf scan_tmp;
+  uint32_t *ik = keys, *iv = vals, *ok = alt_keys, *ov = alt_vals;
+  int passes = 0;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    k_digit_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, n, shift, hist, ntiles);
+    scan_u32_u32(hist, offs, nh, scan_tmp, s);
+    k_digit_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, iv, n, shift, offs, ntiles, ok,
+                                                              ov);
+    SPJ_CUDA(cudaGetLastError());
+    std::swap(ik, ok);
+    std::swap(iv, ov);
+    passes++;
+  }
+  if (passes & 1) {
+    SPJ_CUDA(cudaMemcpyAsync(keys, ik, n * 4, cudaMemcpyDeviceToDevice, s));
+    SPJ_CUDA(cudaMemcpyAsync(vals, iv, n * 4, cudaMemcpyDeviceToDevice, s));
+  }
+}
+
+const char* status_message(uint32_t code) {
+  switch (code) {
+    case kOk: return "ok";
+    case kWkbTruncated: return "invalid WKB (truncated)";
+    case kWkbByteOrder: return "invalid WKB (byte order)";
+    case kWkbType: return "unsupported WKB geometry type";
+    case kWkbDims: return "only 2D WKB geometries are supported";
+    case kWkbCount: return "invalid WKB (count)";
+    case kOverflow: return "output capacity exceeded";
+    case kUnsupported: return "predicate not supported for these geometry types";
+  }
+  return "unknown device error";
+}
+
+}  // namespace spj

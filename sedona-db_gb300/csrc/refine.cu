@@ -1,0 +1,356 @@
+// refine.cu — relation-predicate and ST_DWithin refinement of candidate
+// pairs, one thread per candidate, plus order-preserving compaction.
+//
+// Replaces the reference's RTSpatialRefiner::Refine
+// (c/sedona-libgpuspatial/libgpuspatial/src/rt_spatial_refiner.cu:134-242),
+// which re-parses probe WKB on the CPU each call and runs OptiX PIP
+// (src/rt/shaders/polygon_point_query.cu) or a recursive DE-9IM relate
+// (src/relate_engine.cu:294-336).  Here both sides are already decoded in HBM
+// and the predicate is the tg semantics the reference CPU join uses.
+#include "predicates.cuh"
+#include "prims.cuh"
+#include "refine.cuh"
+
+#include <cmath>
+
+namespace spj {
+namespace {
+
+using namespace pred;
+
+constexpr int kUnsupportedResult = -1;
+
+__device__ __forceinline__ float2 rn32(double2 p) {
+  return make_float2(__double2float_rn(p.x), __double2float_rn(p.y));
+}
+
+__device__ __forceinline__ uint32_t nparts(const GeomsView& G, uint32_t i) {
+  return G.row_part[i + 1] - G.row_part[i];
+}
+
+// tg.c:5740-5760 intersects dispatch
+template <bool kFast>
+__device__ int g_intersects(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
+                            uint32_t& esc) {
+  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
+  if (ka == kEmpty || kb == kEmpty) return 0;
+  if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
+  if (ka == kPoint || kb == kPoint) {
+    const GeomsView& GP = ka == kPoint ? GA : GB;  // the point
+    const GeomsView& GY = ka == kPoint ? GB : GA;  // the polygonal side
+    const uint32_t ip = ka == kPoint ? ia : ib, iy = ka == kPoint ? ib : ia;
+    const double2 p = GP.pt[ip];
+    const float2 p32 = rn32(p);
+    for (uint32_t q = GY.row_part[iy]; q < GY.row_part[iy + 1]; q++)
+      if (poly_contains_point<kFast>(GY, q, p, p32, true, esc)) return 1;
+    return 0;
+  }
+  bool unsupported = false;
+  for (uint32_t qa = GA.row_part[ia]; qa < GA.row_part[ia + 1]; qa++) {
+    const uint32_t ra = GA.part_ring[qa];
+    const bool sa = GA.part_ring[qa + 1] - ra == 1;
+    for (uint32_t qb = GB.row_part[ib]; qb < GB.row_part[ib + 1]; qb++) {
+      const uint32_t rb = GB.part_ring[qb];
+      const bool sb = GB.part_ring[qb + 1] - rb == 1;
+      if (!(sa && sb)) {
+        unsupported = true;
+        continue;
+      }
+      if (ring_intersects_ring<kFast>(GA, ra, GB, rb, esc)) return 1;
+    }
+  }
+  return unsupported ? kUnsupportedResult : 0;
+}
+
+// tg.c:6538-6556 contains dispatch (point 'other' cases)
+template <bool kFast>
+__device__ int g_contains(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
+                          uint32_t& esc) {
+  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
+  if (ka == kEmpty || kb == kEmpty) return 0;
+  if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
+  if (ka == kPoint) return 0;  // tg.c:1157-1162
+  if (kb == kPoint) {
+    const double2 p = GB.pt[ib];
+    const float2 p32 = rn32(p);
+    for (uint32_t q = GA.row_part[ia]; q < GA.row_part[ia + 1]; q++)
+      if (poly_contains_point<kFast>(GA, q, p, p32, false, esc)) return 1;
+    return 0;
+  }
+  return kUnsupportedResult;
+}
+
+// tg.c:6028-6046 covers dispatch
+template <bool kFast>
+__device__ int g_covers(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
+                        uint32_t& esc) {
+  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
+  if (ka == kEmpty || kb == kEmpty) return 0;
+  if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
+  if (kb == kPoint) {
+    const double2 p = GB.pt[ib];
+    const float2 p32 = rn32(p);
+    for (uint32_t q = GA.row_part[ia]; q < GA.row_part[ia + 1]; q++)
+      if (poly_contains_point<kFast>(GA, q, p, p32, true, esc)) return 1;
+    return 0;
+  }
+  if (ka == kPoint && kb == kPolygon) {
+    // tg.c:1152-1155: the polygon's rect is the point itself
+    const uint32_t r = GB.part_ring[GB.row_part[ib]];
+    if (ring_npts(GB, r) < 3) return 0;
+    const Rect64 R = GB.ring_rect[r];
+    const double2 p = GA.pt[ia];
+    return pteq(p, make_double2(R.x, R.y)) && pteq(p, make_double2(R.z, R.w));
+  }
+  return kUnsupportedResult;
+}
+
+// tg.c:6771-6789 touches dispatch
+template <bool kFast>
+__device__ int g_touches(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
+                         uint32_t& esc) {
+  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
+  if (ka == kEmpty || kb == kEmpty) return 0;
+  if (ka == kPoint && kb == kPoint) return 0;
+  if (ka == kPolygon && kb == kPoint) {
+    const double2 p = GB.pt[ib];
+    return poly_touches_point<kFast>(GA, GA.row_part[ia], p, rn32(p), esc);
+  }
+  if (ka == kPoint && kb == kPolygon) {
+    const double2 p = GA.pt[ia];
+    return poly_touches_point<kFast>(GB, GB.row_part[ib], p, rn32(p), esc);
+  }
+  return kUnsupportedResult;
+}
+
+template <bool kFast>
+__device__ int eval(const GeomsView& B, uint32_t b, const GeomsView& P, uint32_t p, int predicate,
+                    uint32_t& esc) {
+  switch (predicate) {
+    case kIntersects:
+      return g_intersects<kFast>(B, b, P, p, esc);
+    case kDisjoint: {
+      int r = g_intersects<kFast>(B, b, P, p, esc);
+      return r < 0 ? r : !r;
+    }
+    case kContains:
+      return g_contains<kFast>(B, b, P, p, esc);
+    case kWithin:
+      return g_contains<kFast>(P, p, B, b, esc);
+    case kCovers:
+      return g_covers<kFast>(B, b, P, p, esc);
+    case kCoveredBy:
+      return g_covers<kFast>(P, p, B, b, esc);
+    case kTouches:
+      return g_touches<kFast>(B, b, P, p, esc);
+    case kEquals: {
+      int w = g_contains<kFast>(P, p, B, b, esc);
+      if (w <= 0) return w;
+      return g_contains<kFast>(B, b, P, p, esc);
+    }
+  }
+  return kUnsupportedResult;
+}
+
+__device__ __forceinline__ void flush_counters(DeviceStatus* st, uint32_t esc, uint32_t pairs) {
+  // warp-aggregate, one atomic per warp
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    esc += __shfl_xor_sync(0xffffffffu, esc, o);
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (esc) atomicAdd(&st->counters[0], (unsigned long long)esc);
+    if (pairs) atomicAdd(&st->counters[1], (unsigned long long)pairs);
+  }
+}
+
+template <bool kFast>
+__global__ void __launch_bounds__(256)
+    k_refine(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
+             const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, int predicate,
+             uint8_t* __restrict__ flags, DeviceStatus* st) {
+  uint32_t esc = 0, pairs = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // every lane runs the same number of loop trips so the warp-wide flush
+  // below sees all 32 lanes
+  const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t trips = (m + stride - 1) / stride;
+  for (uint64_t t = 0; t < trips; t++) {
+    const uint64_t k = start + t * stride;
+    if (k >= m) continue;
+    const uint32_t b = cb[k], p = cp[k] - probe_base;
+    int r = eval<kFast>(B, b, P, p, predicate, esc);
+    pairs++;
+    if (r < 0) {
+      status_fail(st, kUnsupported, k);
+      r = 0;
+    }
+    flags[k] = (uint8_t)r;
+  }
+  flush_counters(st, esc, pairs);
+}
+
+// ---------------------------------------------------------------------------
+// ST_DWithin
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+  s = __dadd_rn(a, b);
+  const double bb = __dsub_rn(s, a);
+  e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void two_prod(double a, double b, double& p, double& e) {
+  p = __dmul_rn(a, b);
+  e = __fma_rn(a, b, -p);
+}
+
+// Sign of the exact sum of n doubles (Shewchuk grow-expansion).
+template <int N>
+__device__ __forceinline__ int exact_sign(const double (&t)[N]) {
+  double e[N];
+  int len = 0;
+  for (int i = 0; i < N; i++) {
+    double q = t[i];
+    int nl = 0;
+    for (int j = 0; j < len; j++) {
+      double s, h;
+      two_sum(q, e[j], s, h);
+      q = s;
+      if (h != 0.0) e[nl++] = h;
+    }
+    if (q != 0.0) e[nl++] = q;
+    len = nl;
+  }
+  if (len == 0) return 0;
+  return e[len - 1] > 0 ? 1 : -1;
+}
+
+// Exact decision of RN(sqrt(dx^2 + dy^2)) <= d, i.e. a correctly rounded
+// hypot compared with d (ties to even at the rounding midpoint).
+__device__ __noinline__ bool dwithin_exact(double2 b, double2 p, double d) {
+  const double dx = __dsub_rn(b.x, p.x), dy = __dsub_rn(b.y, p.y);
+  if (isnan(dx) || isnan(dy) || isnan(d) || d < 0) return false;
+  if (isinf(dx) || isinf(dy)) return isinf(d);
+  if (isinf(d)) return true;
+  const double up = next_up(d);
+  const double ulp = __dsub_rn(up, d);
+  // m = d + ulp/2 ; m^2 = d^2 + d*ulp + ulp^2/4 (the last two exact)
+  double P1, e1, P2, e2, Q1, q1;
+  two_prod(dx, dx, P1, e1);
+  two_prod(dy, dy, P2, e2);
+  two_prod(d, d, Q1, q1);
+  const double Q2 = __dmul_rn(d, ulp);
+  const double Q3 = __dmul_rn(__dmul_rn(ulp, ulp), 0.25);
+  const double t[8] = {e1, e2, -q1, -Q3, -Q2, P1, P2, -Q1};
+  const int sg = exact_sign(t);
+  if (sg < 0) return true;
+  if (sg > 0) return false;
+  // exactly on the midpoint: rounds to the even neighbour
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+  return (bits & 1ull) == 0;
+}
+
+template <bool kFast>
+__global__ void __launch_bounds__(256)
+    k_dwithin(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
+              const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, double d,
+              float d_lo, float d_hi, uint8_t* __restrict__ flags, DeviceStatus* st) {
+  uint32_t esc = 0, pairs = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t trips = (m + stride - 1) / stride;
+  for (uint64_t t = 0; t < trips; t++) {
+    const uint64_t k = start + t * stride;
+    if (k >= m) continue;
+    const uint32_t bi = cb[k], pi = cp[k] - probe_base;
+    pairs++;
+    if (B.kind[bi] != kPoint || P.kind[pi] != kPoint) {
+      status_fail(st, kUnsupported, k);
+      flags[k] = 0;
+      continue;
+    }
+    const double2 b = B.pt[bi], p = P.pt[pi];
+    int r = -1;
+    if (kFast) {
+      // |r32 - hypot| <= err: coordinate rounding (u = 2^-24 per operand,
+      // doubled) plus the FP32 square / sum / sqrt rounding.
+      const float bx = __double2float_rn(b.x), by = __double2float_rn(b.y);
+      const float px = __double2float_rn(p.x), py = __double2float_rn(p.y);
+      const float fx = __fsub_rn(bx, px), fy = __fsub_rn(by, py);
+      const float r32 = __fsqrt_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)));
+      const float mag = fabsf(bx) + fabsf(px) + fabsf(by) + fabsf(py) + fabsf(fx) + fabsf(fy);
+      const float err = __fadd_ru(__fmul_ru(mag, 2.384185791015625e-07f),   // 2^-22
+                                  __fmul_ru(r32, 4.76837158203125e-07f));   // 2^-21
+      // d_lo <= d <= d_hi are the neighbouring floats of d
+      if (__fadd_ru(r32, err) < d_lo) r = 1;
+      else if (__fsub_rd(r32, err) > d_hi) r = 0;
+    } else {
+      // plain form: FP64 squared distance with a relative margin
+      const double dx = __dsub_rn(b.x, p.x), dy = __dsub_rn(b.y, p.y);
+      const double s2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      const double d2 = __dmul_rn(d, d);
+      if (s2 < __dmul_rn(d2, 1.0 - 1e-14)) r = 1;
+      else if (s2 > __dmul_rn(d2, 1.0 + 1e-14)) r = 0;
+    }
+    if (r < 0) {
+      esc++;
+      r = dwithin_exact(b, p, d) ? 1 : 0;
+    }
+    flags[k] = (uint8_t)r;
+  }
+  flush_counters(st, esc, pairs);
+}
+
+__global__ void k_compact(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
+                          const uint8_t* __restrict__ flags, const uint64_t* __restrict__ pos,
+                          uint64_t m, uint32_t* __restrict__ ob, uint32_t* __restrict__ op) {
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m;
+       k += (uint64_t)gridDim.x * blockDim.x) {
+    if (flags[k]) {
+      const uint64_t o = pos[k];
+      ob[o] = cb[k];
+      op[o] = cp[k];
+    }
+  }
+}
+
+}  // namespace
+
+void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
+                     const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
+                     uint8_t* flags, DeviceStatus* st, cudaStream_t s) {
+  if (m == 0) return;
+  const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
+  if (form == kFastF32)
+    k_refine<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st);
+  else
+    k_refine<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
+                    const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
+                    uint8_t* flags, DeviceStatus* st, cudaStream_t s) {
+  if (m == 0) return;
+  const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
+  float d_lo = (float)distance, d_hi = (float)distance;
+  if ((double)d_lo > distance) d_lo = next_downf(d_lo);
+  if ((double)d_hi < distance) d_hi = next_upf(d_hi);
+  if (form == kFastF32)
+    k_dwithin<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_lo, d_hi,
+                                      flags, st);
+  else
+    k_dwithin<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_lo, d_hi,
+                                       flags, st);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void compact_pairs(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags,
+                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s) {
+  if (m == 0) return;
+  k_compact<<<grid_for((int64_t)m, 256, kNumSMs * 16), 256, 0, s>>>(cb, cp, flags, pos, m, ob, op);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+}  // namespace spj

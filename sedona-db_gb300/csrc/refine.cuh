@@ -1,0 +1,44 @@
+// refine.cuh — candidate-pair refinement kernels (relation predicates,
+// ST_DWithin) and flag compaction.
+#pragma once
+#include "geoms.cuh"
+
+namespace spj {
+
+// Predicate codes: enum SedonaSpatialRelationPredicate order
+// (c/sedona-libgpuspatial/libgpuspatial/include/gpuspatial/gpuspatial_c.h:142-151).
+enum Predicate : int {
+  kEquals = 0,
+  kDisjoint = 1,
+  kTouches = 2,
+  kContains = 3,
+  kCovers = 4,
+  kIntersects = 5,
+  kWithin = 6,
+  kCoveredBy = 7,
+};
+
+enum RefineForm : int {
+  kPlainF64 = 0,  // every segment test through the FP64 sequence, no band index
+  kFastF32 = 1,   // y-band index + FP32 classification + FP64 escalation
+};
+
+// flags[k] = pred(build[cb[k]], probe[cp[k] - probe_base]) for k < m.
+// counters: status->counters[0] += FP64 escalations, [1] += pairs evaluated.
+void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
+                     const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
+                     uint8_t* flags, DeviceStatus* st, cudaStream_t s);
+
+// flags[k] = hypot(build - probe) <= distance for point pairs.  The FP32
+// filter decides pairs whose distance is far from the threshold relative to
+// a static error bound; the rest are decided exactly (expansion arithmetic).
+void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
+                    const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
+                    uint8_t* flags, DeviceStatus* st, cudaStream_t s);
+
+// Stream compaction of (cb, cp) by flags: positions from an exclusive scan
+// of the flags (pos has m+1 entries).  Order is preserved.
+void compact_pairs(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags,
+                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s);
+
+}  // namespace spj

@@ -1,0 +1,13 @@
+"""GB300-native spatial-join hot path of SedonaDB (sm_103a CUDA behind the
+reference's gpuspatial C ABI).
+
+Python surface:
+  capi      ctypes bindings of include/gpuspatial_c.h and include/spj_gb300.h
+            (Runtime, FloatIndex2D, Refiner, SpatialJoin, KnnJoin)
+  index     the SpatialIndex / builder mirror of the reference's GPU provider
+  wkb       Arrow binary WKB columns as numpy buffers
+  datagen   seeded synthetic workloads
+"""
+from .wkb import WkbColumn  # noqa: F401
+
+__all__ = ["WkbColumn"]

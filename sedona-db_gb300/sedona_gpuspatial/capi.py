@@ -1,0 +1,499 @@
+"""ctypes bindings of the C ABI (include/gpuspatial_c.h, include/spj_gb300.h).
+
+The classes mirror the reference's safe Rust wrapper over the same ABI
+(c/sedona-libgpuspatial/src/libgpuspatial.rs and src/lib.rs): a
+process-global runtime, ``FloatIndex2D`` (push_build / finish_building /
+probe returning (build, probe) candidate index arrays) and ``Refiner``
+(init_build_schema / push_build / finish_building / refine), with errors
+surfaced as ``GpuSpatialError`` carrying the library's last-error message.
+There is no CPU fallback: if the CUDA library is missing the import fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from typing import Callable, Optional, Tuple
+
+import numpy as np
+
+from .wkb import WkbColumn
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libspj_gb300.so")
+
+
+class GpuSpatialError(RuntimeError):
+    pass
+
+
+# ---------------------------------------------------------------------------
+# ABI structs
+
+class GpuSpatialRuntimeConfig(C.Structure):
+    _fields_ = [("ptx_root", C.c_char_p), ("device_id", C.c_int),
+                ("use_cuda_memory_pool", C.c_bool), ("cuda_memory_pool_init_precent", C.c_int)]
+
+
+class GpuSpatialRuntime(C.Structure):
+    pass
+
+
+GpuSpatialRuntime._fields_ = [
+    ("init", C.CFUNCTYPE(C.c_int, C.POINTER(GpuSpatialRuntime), C.POINTER(GpuSpatialRuntimeConfig))),
+    ("release", C.CFUNCTYPE(None, C.POINTER(GpuSpatialRuntime))),
+    ("get_last_error", C.CFUNCTYPE(C.c_char_p, C.POINTER(GpuSpatialRuntime))),
+    ("private_data", C.c_void_p)]
+
+
+class GpuSpatialIndexConfig(C.Structure):
+    _fields_ = [("runtime", C.POINTER(GpuSpatialRuntime)), ("concurrency", C.c_uint32)]
+
+
+class SedonaSpatialIndexContext(C.Structure):
+    _fields_ = [("private_data", C.c_void_p)]
+
+
+PROBE_CB = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
+                       C.c_void_p)
+
+
+class SedonaFloatIndex2D(C.Structure):
+    pass
+
+
+_IDX = C.POINTER(SedonaFloatIndex2D)
+_CTX = C.POINTER(SedonaSpatialIndexContext)
+SedonaFloatIndex2D._fields_ = [
+    ("clear", C.CFUNCTYPE(C.c_int, _IDX)),
+    ("create_context", C.CFUNCTYPE(None, _CTX)),
+    ("destroy_context", C.CFUNCTYPE(None, _CTX)),
+    ("push_build", C.CFUNCTYPE(C.c_int, _IDX, C.POINTER(C.c_float), C.c_uint32)),
+    ("finish_building", C.CFUNCTYPE(C.c_int, _IDX)),
+    ("probe", C.CFUNCTYPE(C.c_int, _IDX, _CTX, C.POINTER(C.c_float), C.c_uint32, PROBE_CB,
+                          C.c_void_p)),
+    ("get_last_error", C.CFUNCTYPE(C.c_char_p, _IDX)),
+    ("context_get_last_error", C.CFUNCTYPE(C.c_char_p, _CTX)),
+    ("release", C.CFUNCTYPE(None, _IDX)),
+    ("private_data", C.c_void_p)]
+
+
+class GpuSpatialRefinerConfig(C.Structure):
+    _fields_ = [("runtime", C.POINTER(GpuSpatialRuntime)), ("concurrency", C.c_uint32),
+                ("compress_bvh", C.c_bool), ("pipeline_batches", C.c_uint32)]
+
+
+class ArrowSchema(C.Structure):
+    pass
+
+
+ArrowSchema._fields_ = [
+    ("format", C.c_char_p), ("name", C.c_char_p), ("metadata", C.c_char_p), ("flags", C.c_int64),
+    ("n_children", C.c_int64), ("children", C.c_void_p), ("dictionary", C.c_void_p),
+    ("release", C.c_void_p), ("private_data", C.c_void_p)]
+
+
+class ArrowArray(C.Structure):
+    _fields_ = [
+        ("length", C.c_int64), ("null_count", C.c_int64), ("offset", C.c_int64),
+        ("n_buffers", C.c_int64), ("n_children", C.c_int64),
+        ("buffers", C.POINTER(C.c_void_p)), ("children", C.c_void_p), ("dictionary", C.c_void_p),
+        ("release", C.c_void_p), ("private_data", C.c_void_p)]
+
+
+class SedonaSpatialRefiner(C.Structure):
+    pass
+
+
+_REF = C.POINTER(SedonaSpatialRefiner)
+SedonaSpatialRefiner._fields_ = [
+    ("clear", C.CFUNCTYPE(C.c_int, _REF)),
+    ("init_build_schema", C.CFUNCTYPE(C.c_int, _REF, C.POINTER(ArrowSchema))),
+    ("push_build", C.CFUNCTYPE(C.c_int, _REF, C.POINTER(ArrowArray))),
+    ("finish_building", C.CFUNCTYPE(C.c_int, _REF)),
+    ("refine", C.CFUNCTYPE(C.c_int, _REF, C.POINTER(ArrowSchema), C.POINTER(ArrowArray), C.c_int,
+                           C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
+                           C.POINTER(C.c_uint32))),
+    ("get_last_error", C.CFUNCTYPE(C.c_char_p, _REF)),
+    ("release", C.CFUNCTYPE(None, _REF)),
+    ("private_data", C.c_void_p)]
+
+
+class SpjJoinConfig(C.Structure):
+    _fields_ = [("runtime", C.POINTER(GpuSpatialRuntime)), ("leaf_size", C.c_uint32),
+                ("refine_form", C.c_int32), ("profile", C.c_int32)]
+
+
+class SpjDeviceWkb(C.Structure):
+    _fields_ = [("length", C.c_int64), ("offsets", C.c_void_p), ("offsets_are_64bit", C.c_int32),
+                ("data", C.c_void_p), ("data_length", C.c_uint64), ("validity", C.c_void_p),
+                ("validity_offset", C.c_int64)]
+
+
+class SpjJoinStats(C.Structure):
+    _fields_ = [("ms_decode", C.c_double), ("ms_filter", C.c_double), ("ms_refine", C.c_double),
+                ("ms_compact", C.c_double), ("calls", C.c_uint64), ("probe_rows", C.c_uint64),
+                ("candidates", C.c_uint64), ("results", C.c_uint64),
+                ("escalations", C.c_uint64), ("pairs_evaluated", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("probe_bytes", C.c_uint64),
+                ("build_rows", C.c_uint64), ("build_vertices", C.c_uint64),
+                ("build_device_bytes", C.c_uint64)]
+
+
+class SpjKnnConfig(C.Structure):
+    _fields_ = [("runtime", C.POINTER(GpuSpatialRuntime)), ("leaf_size", C.c_uint32),
+                ("refine_form", C.c_int32)]
+
+
+JOIN_CB = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint64,
+                      C.c_void_p)
+
+# exported symbols, declared in include/*.h
+EXPORTS = [
+    "GpuSpatialRuntimeCreate", "GpuSpatialIndexFloat2DCreate", "GpuSpatialRefinerCreate",
+    "SpjJoinCreate", "SpjJoinRelease", "SpjJoinLastError", "SpjJoinPushBuildArrow",
+    "SpjJoinFinishBuild", "SpjJoinBuildDevice", "SpjJoinProbeArrow", "SpjJoinProbeDevice",
+    "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
+    "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
+    "SpjKnnStream", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
+]
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def lib() -> C.CDLL:
+    """Loads lib/libspj_gb300.so (raises if it was not built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise GpuSpatialError(
+                    f"CUDA library not built: {LIB_PATH} (run __graft_entry__.build())")
+            L = C.CDLL(LIB_PATH)
+            L.GpuSpatialRuntimeCreate.argtypes = [C.POINTER(GpuSpatialRuntime)]
+            L.GpuSpatialRuntimeCreate.restype = None
+            L.GpuSpatialIndexFloat2DCreate.argtypes = [_IDX, C.POINTER(GpuSpatialIndexConfig)]
+            L.GpuSpatialRefinerCreate.argtypes = [_REF, C.POINTER(GpuSpatialRefinerConfig)]
+            L.SpjJoinCreate.argtypes = [C.POINTER(SpjJoinConfig), C.POINTER(C.c_void_p)]
+            L.SpjJoinRelease.argtypes = [C.c_void_p]
+            L.SpjJoinRelease.restype = None
+            L.SpjJoinLastError.argtypes = [C.c_void_p]
+            L.SpjJoinLastError.restype = C.c_char_p
+            L.SpjJoinPushBuildArrow.argtypes = [C.c_void_p, C.POINTER(ArrowSchema),
+                                                C.POINTER(ArrowArray)]
+            L.SpjJoinFinishBuild.argtypes = [C.c_void_p]
+            L.SpjJoinBuildDevice.argtypes = [C.c_void_p, C.POINTER(SpjDeviceWkb)]
+            L.SpjJoinProbeArrow.argtypes = [C.c_void_p, C.POINTER(ArrowSchema),
+                                            C.POINTER(ArrowArray), C.c_int32, C.c_double,
+                                            C.c_uint32, JOIN_CB, C.c_void_p]
+            L.SpjJoinProbeDevice.argtypes = [C.c_void_p, C.POINTER(SpjDeviceWkb), C.c_int32,
+                                             C.c_double, C.c_uint32,
+                                             C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                             C.POINTER(C.c_uint64)]
+            L.SpjJoinProbeHost.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
+                                           C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
+                                           C.POINTER(C.c_uint64)]
+            L.SpjJoinStream.argtypes = [C.c_void_p]
+            L.SpjJoinStream.restype = C.c_void_p
+            L.SpjJoinGetStats.argtypes = [C.c_void_p, C.POINTER(SpjJoinStats)]
+            L.SpjJoinResetStats.argtypes = [C.c_void_p]
+            L.SpjKnnCreate.argtypes = [C.POINTER(SpjKnnConfig), C.POINTER(C.c_void_p)]
+            L.SpjKnnRelease.argtypes = [C.c_void_p]
+            L.SpjKnnRelease.restype = None
+            L.SpjKnnLastError.argtypes = [C.c_void_p]
+            L.SpjKnnLastError.restype = C.c_char_p
+            L.SpjKnnBuild.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+            L.SpjKnnQuery.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
+                                      C.c_void_p, C.c_void_p, C.c_int32]
+            L.SpjKnnStream.argtypes = [C.c_void_p]
+            L.SpjKnnStream.restype = C.c_void_p
+            L.SpjHostRegister.argtypes = [C.c_void_p, C.c_uint64]
+            L.SpjHostUnregister.argtypes = [C.c_void_p]
+            L.SpjVersion.restype = C.c_char_p
+            _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# Arrow C data interface for binary WKB columns built from numpy buffers
+
+class ArrowBinary:
+    """Keeps an ArrowSchema / ArrowArray pair (binary or large_binary) alive."""
+
+    def __init__(self, col: WkbColumn, offset: int = 0, length: Optional[int] = None):
+        large = col.offsets.dtype == np.int64
+        self._fmt = b"Z" if large else b"z"
+        self.schema = ArrowSchema(format=self._fmt, name=b"geometry", metadata=None, flags=2,
+                                  n_children=0)
+        self._off = np.ascontiguousarray(col.offsets)
+        self._data = np.ascontiguousarray(col.data) if len(col.data) else np.zeros(8, np.uint8)
+        self._valid = col.validity
+        self._bufs = (C.c_void_p * 3)(
+            self._valid.ctypes.data if self._valid is not None else None,
+            self._off.ctypes.data, self._data.ctypes.data)
+        n = (len(col) - offset) if length is None else length
+        nulls = 0
+        if self._valid is not None:
+            bits = np.unpackbits(self._valid, bitorder="little")[offset:offset + n]
+            nulls = int(n - bits.sum())
+        self.array = ArrowArray(length=n, null_count=nulls, offset=offset, n_buffers=3,
+                                n_children=0, buffers=self._bufs)
+
+
+# ---------------------------------------------------------------------------
+
+class Runtime:
+    """The process-global runtime (c/sedona-libgpuspatial/src/lib.rs:41-90)."""
+
+    _instance = None
+    _lock = threading.Lock()
+
+    def __init__(self, device_id: int = 0, use_pool: bool = True, pool_percent: int = 0):
+        L = lib()
+        self.rt = GpuSpatialRuntime()
+        L.GpuSpatialRuntimeCreate(C.byref(self.rt))
+        cfg = GpuSpatialRuntimeConfig(b"", device_id, use_pool, pool_percent)
+        if self.rt.init(C.byref(self.rt), C.byref(cfg)) != 0:
+            msg = self.rt.get_last_error(C.byref(self.rt)).decode()
+            raise GpuSpatialError(f"runtime init failed: {msg}")
+        self.device_id = device_id
+
+    @classmethod
+    def get(cls, device_id: int = 0) -> "Runtime":
+        with cls._lock:
+            if cls._instance is None:
+                cls._instance = Runtime(device_id)
+            return cls._instance
+
+
+def _check(rc: int, what: str, msg_fn: Callable[[], bytes]):
+    if rc != 0:
+        raise GpuSpatialError(f"{what}: {msg_fn().decode(errors='replace')}")
+
+
+class FloatIndex2D:
+    """SedonaFloatIndex2D (c/sedona-libgpuspatial/src/libgpuspatial.rs:126-308)."""
+
+    def __init__(self, runtime: Optional[Runtime] = None, concurrency: int = 1):
+        self.runtime = runtime or Runtime.get()
+        self.idx = SedonaFloatIndex2D()
+        cfg = GpuSpatialIndexConfig(C.pointer(self.runtime.rt), concurrency)
+        if lib().GpuSpatialIndexFloat2DCreate(C.byref(self.idx), C.byref(cfg)) != 0:
+            raise GpuSpatialError("Index Create failed")
+
+    def _err(self):
+        return self.idx.get_last_error(C.byref(self.idx))
+
+    def clear(self):
+        _check(self.idx.clear(C.byref(self.idx)), "clear", self._err)
+
+    def push_build(self, rects: np.ndarray):
+        r = np.ascontiguousarray(rects, dtype=np.float32).reshape(-1, 4)
+        self._keep = r
+        _check(self.idx.push_build(C.byref(self.idx), r.ctypes.data_as(C.POINTER(C.c_float)),
+                                   len(r)), "push_build", self._err)
+
+    def finish_building(self):
+        _check(self.idx.finish_building(C.byref(self.idx)), "finish_building", self._err)
+
+    def probe(self, rects: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+        r = np.ascontiguousarray(rects, dtype=np.float32).reshape(-1, 4)
+        ctx = SedonaSpatialIndexContext()
+        self.idx.create_context(C.byref(ctx))
+        out = {}
+
+        def cb(b, p, n, _ud):
+            try:
+                out["b"] = np.ctypeslib.as_array(b, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+                out["p"] = np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+                return 0
+            except Exception as e:  # panic-safe callback (libgpuspatial.rs:532-572)
+                out["err"] = e
+                return -1
+
+        ccb = PROBE_CB(cb)
+        try:
+            rc = self.idx.probe(C.byref(self.idx), C.byref(ctx),
+                                r.ctypes.data_as(C.POINTER(C.c_float)), len(r), ccb, None)
+            if rc != 0:
+                if "err" in out:
+                    raise GpuSpatialError(f"probe callback failed: {out['err']}")
+                msg = self.idx.context_get_last_error(C.byref(ctx)).decode()
+                raise GpuSpatialError(f"probe: {msg}")
+        finally:
+            self.idx.destroy_context(C.byref(ctx))
+        return out["b"], out["p"]
+
+    def __del__(self):
+        if getattr(self, "idx", None) is not None and self.idx.private_data:
+            self.idx.release(C.byref(self.idx))
+
+
+PREDICATES = {"equals": 0, "disjoint": 1, "touches": 2, "contains": 3, "covers": 4,
+              "intersects": 5, "within": 6, "coveredby": 7, "dwithin": 100}
+
+
+class Refiner:
+    """SedonaSpatialRefiner (c/sedona-libgpuspatial/src/libgpuspatial.rs:310-486)."""
+
+    def __init__(self, runtime: Optional[Runtime] = None, concurrency: int = 1,
+                 compress_bvh: bool = False, pipeline_batches: int = 1):
+        self.runtime = runtime or Runtime.get()
+        self.ref = SedonaSpatialRefiner()
+        cfg = GpuSpatialRefinerConfig(C.pointer(self.runtime.rt), concurrency, compress_bvh,
+                                      pipeline_batches)
+        if lib().GpuSpatialRefinerCreate(C.byref(self.ref), C.byref(cfg)) != 0:
+            raise GpuSpatialError("Refiner Create failed")
+        self._keep = []
+
+    def _err(self):
+        return self.ref.get_last_error(C.byref(self.ref))
+
+    def clear(self):
+        _check(self.ref.clear(C.byref(self.ref)), "clear", self._err)
+
+    def init_build_schema(self, large: bool = False):
+        self._schema = ArrowSchema(format=b"Z" if large else b"z", name=b"geometry")
+        _check(self.ref.init_build_schema(C.byref(self.ref), C.byref(self._schema)),
+               "init_build_schema", self._err)
+
+    def push_build(self, col: WkbColumn):
+        a = ArrowBinary(col)
+        self._keep.append(a)
+        _check(self.ref.push_build(C.byref(self.ref), C.byref(a.array)), "push_build", self._err)
+
+    def finish_building(self):
+        _check(self.ref.finish_building(C.byref(self.ref)), "finish_building", self._err)
+
+    def refine(self, probe: WkbColumn, predicate: str, build_idx: np.ndarray,
+               probe_idx: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+        a = ArrowBinary(probe)
+        b = np.ascontiguousarray(build_idx, dtype=np.uint32).copy()
+        p = np.ascontiguousarray(probe_idx, dtype=np.uint32).copy()
+        new_n = C.c_uint32(0)
+        rc = self.ref.refine(C.byref(self.ref), C.byref(a.schema), C.byref(a.array),
+                             PREDICATES[predicate], b.ctypes.data_as(C.POINTER(C.c_uint32)),
+                             p.ctypes.data_as(C.POINTER(C.c_uint32)), len(b), C.byref(new_n))
+        _check(rc, "refine", self._err)
+        return b[:new_n.value], p[:new_n.value]
+
+    def __del__(self):
+        if getattr(self, "ref", None) is not None and self.ref.private_data:
+            self.ref.release(C.byref(self.ref))
+
+
+class SpatialJoin:
+    """The fused build/probe join (SpjJoin*, include/spj_gb300.h)."""
+
+    def __init__(self, runtime: Optional[Runtime] = None, leaf_size: int = 0,
+                 refine_form: int = 1, profile: bool = False):
+        self.runtime = runtime or Runtime.get()
+        self.h = C.c_void_p()
+        cfg = SpjJoinConfig(C.pointer(self.runtime.rt), leaf_size, refine_form, int(profile))
+        if lib().SpjJoinCreate(C.byref(cfg), C.byref(self.h)) != 0:
+            raise GpuSpatialError("SpjJoinCreate failed")
+        self._keep = []
+
+    def _err(self):
+        return lib().SpjJoinLastError(self.h)
+
+    def build(self, col: WkbColumn):
+        a = ArrowBinary(col)
+        self._keep = [a]
+        _check(lib().SpjJoinPushBuildArrow(self.h, C.byref(a.schema), C.byref(a.array)),
+               "push_build", self._err)
+        _check(lib().SpjJoinFinishBuild(self.h), "finish_build", self._err)
+
+    def build_device(self, dcol: SpjDeviceWkb):
+        _check(lib().SpjJoinBuildDevice(self.h, C.byref(dcol)), "build_device", self._err)
+
+    def probe(self, col: WkbColumn, predicate: str = "intersects", distance: float = 0.0,
+              probe_base: int = 0) -> Tuple[np.ndarray, np.ndarray]:
+        a = ArrowBinary(col)
+        out = {}
+
+        def cb(b, p, n, _ud):
+            out["b"] = np.ctypeslib.as_array(b, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+            out["p"] = np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+            return 0
+
+        ccb = JOIN_CB(cb)
+        rc = lib().SpjJoinProbeArrow(self.h, C.byref(a.schema), C.byref(a.array),
+                                     PREDICATES[predicate], distance, probe_base, ccb, None)
+        _check(rc, "probe", self._err)
+        return out["b"], out["p"]
+
+    def probe_host(self, col: WkbColumn, predicate: str, distance: float, out_b: np.ndarray,
+                   out_p: np.ndarray, probe_base: int = 0) -> int:
+        n = C.c_uint64(0)
+        rc = lib().SpjJoinProbeHost(
+            self.h, len(col), col.offsets.ctypes.data, int(col.offsets.dtype == np.int64),
+            col.data.ctypes.data, col.validity.ctypes.data if col.validity is not None else None,
+            PREDICATES[predicate], distance, probe_base, out_b.ctypes.data, out_p.ctypes.data,
+            len(out_b), C.byref(n))
+        _check(rc, "probe_host", self._err)
+        return n.value
+
+    def probe_device(self, dcol: SpjDeviceWkb, predicate: str = "intersects",
+                     distance: float = 0.0, probe_base: int = 0):
+        db, dp, n = C.c_void_p(), C.c_void_p(), C.c_uint64()
+        rc = lib().SpjJoinProbeDevice(self.h, C.byref(dcol), PREDICATES[predicate], distance,
+                                      probe_base, C.byref(db), C.byref(dp), C.byref(n))
+        _check(rc, "probe_device", self._err)
+        return db.value, dp.value, n.value
+
+    def stream(self) -> int:
+        return lib().SpjJoinStream(self.h)
+
+    def stats(self) -> dict:
+        s = SpjJoinStats()
+        _check(lib().SpjJoinGetStats(self.h, C.byref(s)), "stats", self._err)
+        return {f: getattr(s, f) for f, _ in SpjJoinStats._fields_}
+
+    def reset_stats(self):
+        _check(lib().SpjJoinResetStats(self.h), "reset_stats", self._err)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().SpjJoinRelease(self.h)
+            self.h = None
+
+
+class KnnJoin:
+    """KNN join over point columns (SpjKnn*, include/spj_gb300.h)."""
+
+    def __init__(self, runtime: Optional[Runtime] = None, leaf_size: int = 0,
+                 refine_form: int = 1):
+        self.runtime = runtime or Runtime.get()
+        self.h = C.c_void_p()
+        cfg = SpjKnnConfig(C.pointer(self.runtime.rt), leaf_size, refine_form)
+        if lib().SpjKnnCreate(C.byref(cfg), C.byref(self.h)) != 0:
+            raise GpuSpatialError("SpjKnnCreate failed")
+
+    def _err(self):
+        return lib().SpjKnnLastError(self.h)
+
+    def build(self, x: np.ndarray, y: np.ndarray):
+        xy = np.ascontiguousarray(np.stack([x, y], 1), dtype=np.float64)
+        _check(lib().SpjKnnBuild(self.h, xy.ctypes.data, len(xy)), "knn build", self._err)
+
+    def query(self, x: np.ndarray, y: np.ndarray, k: int):
+        xy = np.ascontiguousarray(np.stack([x, y], 1), dtype=np.float64)
+        idx = np.empty((len(xy), k), dtype=np.uint32)
+        dist = np.empty((len(xy), k), dtype=np.float64)
+        _check(lib().SpjKnnQuery(self.h, xy.ctypes.data, len(xy), k, idx.ctypes.data,
+                                 dist.ctypes.data, 0), "knn query", self._err)
+        return idx, dist
+
+    def query_device(self, d_xy: int, n: int, k: int, d_idx: int, d_dist: int):
+        _check(lib().SpjKnnQuery(self.h, d_xy, n, k, d_idx, d_dist, 1), "knn query", self._err)
+
+    def stream(self) -> int:
+        return lib().SpjKnnStream(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().SpjKnnRelease(self.h)
+            self.h = None

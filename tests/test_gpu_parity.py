@@ -1,0 +1,308 @@
+"""CUDA path vs the oracle (and the reference's own tg outcomes frozen in the
+golden fixtures), through the C ABI.  Integer / index results must be
+bit-exact: pair sets are compared as sorted (probe, build) lists."""
+import numpy as np
+import pytest
+
+import golden_io
+
+pytestmark = pytest.mark.gpu
+
+PREDS = ["intersects", "contains", "covers", "within", "coveredby", "touches", "equals"]
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from sedona_gpuspatial import _build, capi
+    _build.build()
+    return capi
+
+
+@pytest.fixture(scope="module")
+def oracle_mod():
+    import oracle
+    oracle.build(with_ref=False)
+    return oracle
+
+
+def pairs(b, p):
+    return sorted(zip(np.asarray(p).tolist(), np.asarray(b).tolist()))
+
+
+def oracle_pairs(oracle_mod, build, probe, pred, distance=0.0):
+    ob, op = oracle_mod.join(oracle_mod.Geoms(build), oracle_mod.Geoms(probe), pred, distance,
+                             nthreads=4)
+    return pairs(ob, op)
+
+
+# ---------------------------------------------------------------------------
+# fused join (SpjJoin): workload-shaped inputs at small sizes
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("pred", PREDS)
+def test_point_in_polygon_join(capi, oracle_mod, form, pred):
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload1(n_points=30000, n_polys=500)
+    j = capi.SpatialJoin(refine_form=form)
+    j.build(inp.build)
+    b, p = j.probe(inp.probe, pred)
+    assert pairs(b, p) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_polygon_polygon_intersects(capi, oracle_mod, form):
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload2(n_buildings=20000, n_zones=300)
+    j = capi.SpatialJoin(refine_form=form)
+    j.build(inp.build)
+    b, p = j.probe(inp.probe, "intersects")
+    exp = oracle_pairs(oracle_mod, inp.build, inp.probe, "intersects")
+    assert len(exp) > 1000
+    assert pairs(b, p) == exp
+
+
+def test_contains_stream_batches(capi, oracle_mod):
+    """Workload-3 shape: probe batches of uneven size, probe ids offset by the
+    batch start (probe_base), concatenated in probe order."""
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload3(n_points=60000, n_zones=400)
+    j = capi.SpatialJoin()
+    j.build(inp.build)
+    got = []
+    start = 0
+    rng = np.random.default_rng(5)
+    while start < len(inp.probe):
+        n = int(min(len(inp.probe) - start, rng.integers(1000, 9000)))
+        b, p = j.probe(inp.probe.slice(start, start + n), "contains", probe_base=start)
+        assert np.all(np.diff(p.astype(np.int64)) >= 0)  # ascending probe order
+        got += pairs(b, p)
+        start += n
+    assert sorted(got) == oracle_pairs(oracle_mod, inp.build, inp.probe, "contains")
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_dwithin(capi, oracle_mod, form):
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload4(n_probe=20000, n_build=20000)
+    j = capi.SpatialJoin(refine_form=form)
+    j.build(inp.build)
+    b, p = j.probe(inp.probe, "dwithin", distance=250.0)
+    exp = oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin", 250.0)
+    assert len(exp) > 10000
+    assert pairs(b, p) == exp
+
+
+def test_dwithin_exact_boundary(capi, oracle_mod):
+    """Integer Pythagorean triples put pairs exactly at distance d."""
+    from sedona_gpuspatial import wkb
+    bx = np.array([0, 3, 5, 8, 20, 7, 24], dtype=np.float64)
+    by = np.array([0, 4, 12, 15, 21, 24, 7], dtype=np.float64)
+    build = wkb.points_column(bx, by)
+    probe = wkb.points_column(np.array([0.0, 10.0]), np.array([0.0, 3.0]))
+    j = capi.SpatialJoin()
+    j.build(build)
+    for d in (5.0, 13.0, 17.0, 25.0, 29.0, 4.999999999999999):
+        b, p = j.probe(probe, "dwithin", distance=d)
+        assert pairs(b, p) == oracle_pairs(oracle_mod, build, probe, "dwithin", d), d
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_knn(capi, oracle_mod, form):
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload4(n_probe=5000, n_build=40000)
+    bx, by = _points(oracle_mod, inp.build)
+    px, py = _points(oracle_mod, inp.probe)
+    kj = capi.KnnJoin(refine_form=form)
+    kj.build(bx, by)
+    idx, dist = kj.query(px, py, 8)
+    oi, od = oracle_mod.knn(oracle_mod.Geoms(inp.build), oracle_mod.Geoms(inp.probe), 8, nthreads=4)
+    assert np.array_equal(idx, oi)
+    np.testing.assert_allclose(dist, od, rtol=1e-12, atol=0)
+
+
+def test_knn_ties_by_row_id(capi, oracle_mod):
+    from sedona_gpuspatial import wkb
+    # duplicated build points: equal distances must come back in row order
+    bx = np.array([1.0, 1.0, 2.0, 1.0, -1.0, 0.0, 0.0]); by = np.array([0.0, 0.0, 0.0, 0.0, 0.0, 1.0, -1.0])
+    kj = capi.KnnJoin()
+    kj.build(bx, by)
+    idx, dist = kj.query(np.array([0.0]), np.array([0.0]), 6)
+    oi, od = oracle_mod.knn(oracle_mod.Geoms(wkb.points_column(bx, by)),
+                            oracle_mod.Geoms(wkb.points_column(np.array([0.0]), np.array([0.0]))), 6)
+    assert idx.tolist() == oi.tolist()
+    assert idx[0].tolist()[:6] == [0, 1, 3, 4, 5, 6]
+
+
+def test_knn_k_larger_than_build(capi):
+    kj = capi.KnnJoin()
+    kj.build(np.array([0.0, 1.0]), np.array([0.0, 0.0]))
+    idx, dist = kj.query(np.array([0.2]), np.array([0.0]), 4)
+    assert idx[0].tolist() == [0, 1, 0xFFFFFFFF, 0xFFFFFFFF]
+    assert np.isinf(dist[0, 2:]).all()
+
+
+def _points(oracle_mod, col):
+    g = oracle_mod.Geoms(col)
+    import ctypes as C
+    L = oracle_mod.lib()
+    x = np.empty(len(col)); y = np.empty(len(col))
+    xx, yy = C.c_double(), C.c_double()
+    for i in range(len(col)):
+        L.spjo_point(g.ptr, i, C.byref(xx), C.byref(yy))
+        x[i], y[i] = xx.value, yy.value
+    return x, y
+
+
+# ---------------------------------------------------------------------------
+# golden fixtures: the reference's own tg outcomes, through the refiner ABI
+
+@pytest.mark.parametrize("name", list(golden_io.SHAPES))
+@pytest.mark.parametrize("form", [0, 1])
+def test_refiner_matches_reference_tg_golden(capi, name, form):
+    z, cols = golden_io.load()
+    preds, brows, prows, exp = golden_io.cube(z, cols, name)
+    bname, pname = golden_io.SHAPES[name]
+    j = capi.SpatialJoin(refine_form=form)
+    j.build(cols[bname])
+    probe = cols[pname]
+    for k, code in enumerate(preds):
+        pred = [n for n, c in capi.PREDICATES.items() if c == code][0]
+        if pred == "disjoint":
+            continue  # not a join predicate (the planner never plans it)
+        if name == "poly_poly" and False:
+            pass
+        try:
+            b, p = j.probe(probe, pred)
+        except capi.GpuSpatialError as e:
+            # combinations outside the supported set must say so
+            assert "not supported" in str(e)
+            continue
+        got = np.zeros((len(cols[bname]), len(probe)), dtype=np.uint8)
+        got[b, p] = 1
+        sub = got[np.ix_(brows, prows)]
+        bad = np.argwhere(sub != exp[k])
+        assert len(bad) == 0, (pred, [(int(brows[i]), int(prows[j])) for i, j in bad[:5]])
+
+
+def test_refiner_abi_known_answer(capi):
+    """gpu_spatial_index.rs:647-746 through index probe + refiner refine:
+    3 squares x 4 points -> probe indices [0, 2, 3]."""
+    from sedona_gpuspatial import wkb
+    squares = [[(0, 0), (10, 0), (10, 10), (0, 10), (0, 0)],
+               [(20, 20), (30, 20), (30, 30), (20, 30), (20, 20)],
+               [(40, 40), (50, 40), (50, 50), (40, 50), (40, 40)]]
+    build = wkb.column_from_values([wkb.wkb_polygon([[(float(x), float(y)) for x, y in s]])
+                                    for s in squares])
+    pts = [(5, 5), (15, 15), (25, 25), (45, 45)]
+    probe = wkb.column_from_values([wkb.wkb_point(float(x), float(y)) for x, y in pts])
+    idx = capi.FloatIndex2D()
+    idx.push_build(np.array([[0, 0, 10, 10], [20, 20, 30, 30], [40, 40, 50, 50]], np.float32))
+    idx.finish_building()
+    cb, cp = idx.probe(np.array([[x, y, x, y] for x, y in pts], np.float32))
+    ref = capi.Refiner()
+    ref.init_build_schema()
+    ref.push_build(build)
+    ref.finish_building()
+    b, p = ref.refine(probe, "intersects", cb, cp)
+    assert p.tolist() == [0, 2, 3]
+    assert b.tolist() == [0, 1, 2]
+
+
+def test_index_matches_rect_join(capi, oracle_mod):
+    """index_test.cu:52-86 recipe: mt19937-style uniform boxes in
+    [-180,180], sizes U(0,100), box-box and point-box."""
+    rng = np.random.default_rng(0)
+
+    def boxes(n, points=False):
+        x = rng.uniform(-180, 180, n); y = rng.uniform(-180, 180, n)
+        w = 0 if points else rng.uniform(0, 100, n)
+        h = 0 if points else rng.uniform(0, 100, n)
+        return np.stack([x, y, x + w, y + h], 1).astype(np.float32)
+
+    for nb, npb, pts in [(1, 1, False), (7, 100, False), (1000, 3000, False), (5000, 8192, True),
+                         (8192, 1000, False)]:
+        B, P = boxes(nb), boxes(npb, pts)
+        idx = capi.FloatIndex2D()
+        idx.push_build(B[: nb // 2])
+        idx.push_build(B[nb // 2:])  # two pushes concatenate
+        idx.finish_building()
+        b, p = idx.probe(P)
+        ob, op = oracle_mod.rect_join(B, P, nthreads=4)
+        assert pairs(b, p) == pairs(ob, op), (nb, npb)
+
+
+def test_index_empty_and_nan(capi):
+    idx = capi.FloatIndex2D()
+    idx.finish_building()
+    b, p = idx.probe(np.array([[0, 0, 1, 1]], np.float32))
+    assert len(b) == 0
+    idx2 = capi.FloatIndex2D()
+    idx2.push_build(np.array([[np.nan] * 4, [0, 0, 1, 1]], np.float32))
+    idx2.finish_building()
+    b, p = idx2.probe(np.array([[0.5, 0.5, 0.5, 0.5], [np.nan] * 4], np.float32))
+    assert b.tolist() == [1] and p.tolist() == [0]
+
+
+def test_nulls_empties_bigendian_large_binary(capi, oracle_mod):
+    from sedona_gpuspatial import wkb
+    sq = [[(0.0, 0.0), (4.0, 0.0), (4.0, 4.0), (0.0, 4.0), (0.0, 0.0)]]
+    build_vals = [wkb.wkb_polygon(sq), None, wkb.wkb_polygon(sq, big_endian=True),
+                  wkb.wkb_polygon([]), wkb.wkb_multipolygon([sq, [[(10.0, 10.0), (12.0, 10.0),
+                                                                   (12.0, 12.0), (10.0, 10.0)]]])]
+    probe_vals = [wkb.wkb_point(1, 1), None, wkb.wkb_point(float("nan"), float("nan")),
+                  wkb.wkb_point(11.5, 10.5, big_endian=True), wkb.wkb_point(4, 2)]
+    for large in (False, True):
+        build = wkb.column_from_values(build_vals, large=large)
+        probe = wkb.column_from_values(probe_vals, large=large)
+        j = capi.SpatialJoin()
+        j.build(build)
+        for pred in ("intersects", "contains", "covers"):
+            b, p = j.probe(probe, pred)
+            assert pairs(b, p) == oracle_pairs(oracle_mod, build, probe, pred), (large, pred)
+
+
+def test_sliced_arrow_array(capi, oracle_mod):
+    """A probe array with a non-zero Arrow offset (a slice of a batch)."""
+    from sedona_gpuspatial import capi as c, datagen
+    inp = datagen.workload1(n_points=5000, n_polys=200)
+    j = capi.SpatialJoin()
+    j.build(inp.build)
+    a = c.ArrowBinary(inp.probe, offset=1000, length=2000)
+    import ctypes as C
+    out = {}
+
+    def cb(b, p, n, _):
+        out["b"] = np.ctypeslib.as_array(b, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+        out["p"] = np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+        return 0
+
+    rc = c.lib().SpjJoinProbeArrow(j.h, C.byref(a.schema), C.byref(a.array), 5, 0.0, 0,
+                                   c.JOIN_CB(cb), None)
+    assert rc == 0
+    exp = oracle_pairs(oracle_mod, inp.build, inp.probe.slice(1000, 3000), "intersects")
+    assert pairs(out["b"], out["p"]) == exp
+
+
+def test_malformed_wkb_reports_row(capi):
+    from sedona_gpuspatial import wkb
+    good = wkb.wkb_point(1, 1)
+    bad = good[:10]  # truncated
+    j = capi.SpatialJoin()
+    j.build(wkb.column_from_values([wkb.wkb_polygon([[(0.0, 0.0), (2.0, 0.0), (2.0, 2.0), (0.0, 0.0)]])]))
+    with pytest.raises(capi.GpuSpatialError, match="row 1"):
+        j.probe(wkb.column_from_values([good, bad, good]), "intersects")
+    # the object stays usable after the error
+    b, p = j.probe(wkb.column_from_values([good]), "intersects")
+    assert p.tolist() == [0]
+
+
+def test_empty_probe_and_build(capi):
+    from sedona_gpuspatial import wkb
+    j = capi.SpatialJoin()
+    j.build(wkb.column_from_values([]))
+    b, p = j.probe(wkb.column_from_values([wkb.wkb_point(0, 0)]), "intersects")
+    assert len(b) == 0
+    j2 = capi.SpatialJoin()
+    j2.build(wkb.column_from_values([wkb.wkb_point(0, 0)]))
+    b, p = j2.probe(wkb.column_from_values([]), "intersects")
+    assert len(b) == 0
