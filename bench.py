@@ -1,0 +1,399 @@
+"""Spatial-join benchmark: join pairs/s and probe rows/s on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 2] [--impl ours|reference]
+
+Workload (default 2): 2M building polygons (4-12 vertices, GMM-clustered)
+probing 50k star zones (32-256 vertices) with ST_Intersects; both sides FP64
+WKB in Arrow binary layout, seeded synthetic data.  A step is one pass of the
+probe phase over the whole probe column: WKB decode -> f32 filter boxes ->
+LBVH count / scan / scatter -> refine -> compaction, with the probe column
+resident in HBM at the start of the timed region (value) or staged from
+pinned host memory through the C ABI with the pairs copied back (e2e).
+The probe column (>300 MB) exceeds the 129 MB L2, so no flush is needed
+between steps.  The chosen form (banded FP32 filter + FP64 escalation) is the
+headline; the plain FP64 form is timed beside it.
+
+--impl reference times the reference CPU join restated in C (oracle/, the
+reference's Rust binary cannot be built here) on the host cores, on a
+bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "sedona-db_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "join pairs/s & probe rows/s on 1 GB300 (exact pair set): chosen vs plain GPU form"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def make_inputs(workload: int, scale: float):
+    from sedona_gpuspatial import datagen
+    if workload == 1:
+        return datagen.workload1(n_points=int(1_000_000 * scale), n_polys=int(10_000 * scale))
+    if workload == 2:
+        return datagen.workload2(n_buildings=int(2_000_000 * scale), n_zones=int(50_000 * scale))
+    if workload == 3:
+        return datagen.workload3(n_points=int(10_000_000 * scale), n_zones=int(50_000 * scale))
+    if workload == 4:
+        return datagen.workload4(n_probe=int(20_000_000 * scale), n_build=int(1_000_000 * scale))
+    raise SystemExit(f"unknown workload {workload}")
+
+
+WORKLOAD_NAMES = {
+    1: "pip_uniform_1m_points_x_10k_star_polygons_st_intersects",
+    2: "polygon_polygon_2m_buildings_x_50k_zones_st_intersects",
+    3: "contains_10m_gmm_points_x_50k_zones_st_contains",
+    4: "dwithin25_20m_x_1m_gmm_points",
+}
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock + throttle reasons)."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier_max(pg, value: float, device) -> float:
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def to_device(col):
+    """Uploads a WKB column into torch-owned device buffers; returns the
+    SpjDeviceWkb view and the tensors keeping it alive."""
+    import torch
+    from sedona_gpuspatial import capi
+    off = torch.from_numpy(np.ascontiguousarray(col.offsets)).cuda()
+    data = torch.from_numpy(np.ascontiguousarray(col.data)).cuda()
+    d = capi.SpjDeviceWkb(length=len(col), offsets=off.data_ptr(),
+                          offsets_are_64bit=int(col.offsets.dtype == np.int64),
+                          data=data.data_ptr(), data_length=len(col.data), validity=None,
+                          validity_offset=0)
+    return d, (off, data)
+
+
+def probe_vertices_per_row(col) -> float:
+    """Average stored vertices per probe row: 1 for a point column; for the
+    single-ring polygon columns the generators make, (bytes - 13 per row) / 16."""
+    if len(col) == 0:
+        return 0.0
+    if int(col.data[1]) == 1:  # WKB type of row 0 (little endian): Point
+        return 1.0
+    return (len(col.data) - 13 * len(col)) / 16.0 / len(col)
+
+
+def algorithmic_refine_bytes(stats, probe_vertices_per_row: float, build_vertex_bytes: int):
+    """8 B per candidate (ids) + the probe geometry's FP64 vertices per
+    candidate + the build side's FP64 vertices once + 1 B flag per candidate."""
+    m = stats["candidates"]
+    return m * (8 + 16 * probe_vertices_per_row + 1) + build_vertex_bytes
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    from sedona_gpuspatial import capi
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inp = make_inputs(args.workload, args.scale)
+    pred = {"knn": "dwithin"}.get(inp.predicate, inp.predicate)
+    distance = float(inp.params.get("distance", 0.0))
+    rt = capi.Runtime.get(local)
+
+    def make_join(form):
+        j = capi.SpatialJoin(rt, refine_form=form, profile=True)
+        j.build(inp.build)
+        return j
+
+    dcol, keep = to_device(inp.probe)
+    n_rows = len(inp.probe)
+    results = {}
+    for form, name, steps in ((1, "chosen", args.steps), (0, "plain", max(1, args.plain_steps))):
+        j = make_join(form)
+        stream = torch.cuda.ExternalStream(j.stream())
+        for _ in range(args.warmup):
+            j.probe_device(dcol, pred, distance)
+        j.reset_stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        sampler = ClockSampler(local) if name == "chosen" else None
+        if sampler:
+            sampler.__enter__()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        npairs = 0
+        for _ in range(steps):
+            _, _, npairs = j.probe_device(dcol, pred, distance)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__()
+        ms = e0.elapsed_time(e1) / steps
+        ms = barrier_max(pg, ms, dev)
+        st = j.stats()
+        results[name] = {"ms": ms, "pairs": npairs, "stats": st,
+                         "clocks": sampler.summary() if sampler else None, "join": j}
+    chosen = results["chosen"]
+    st = chosen["stats"]
+    steps = args.steps
+
+    # e2e: host (pinned) WKB -> C ABI -> host pairs, copies inside the timed region
+    j = chosen["join"]
+    off = np.ascontiguousarray(inp.probe.offsets)
+    data = np.ascontiguousarray(inp.probe.data)
+    cap = int(chosen["pairs"] * 1.01) + 16
+    ob = np.empty(cap, np.uint32)
+    op = np.empty(cap, np.uint32)
+    L = capi.lib()
+    for arr in (off, data, ob, op):
+        L.SpjHostRegister(arr.ctypes.data, arr.nbytes)
+    for _ in range(args.warmup):
+        j.probe_host(inp.probe, pred, distance, ob, op)
+    stream = torch.cuda.ExternalStream(j.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    n_e2e = 0
+    for _ in range(steps):
+        n_e2e = j.probe_host(inp.probe, pred, distance, ob, op)
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = barrier_max(pg, e0.elapsed_time(e1) / steps, dev)
+    for arr in (off, data, ob, op):
+        L.SpjHostUnregister(arr.ctypes.data)
+    assert n_e2e == chosen["pairs"], (n_e2e, chosen["pairs"])
+
+    # roofline of the dominant kernel (refine) over the timed steps
+    hbm_peak, peak_kind = load_peaks()
+    probe_vpr = probe_vertices_per_row(inp.probe)
+    build_vbytes = int(st["build_vertices"]) * 16
+    ref_bytes = algorithmic_refine_bytes({"candidates": st["candidates"] / steps}, probe_vpr,
+                                         build_vbytes)
+    ref_ms = st["ms_refine"] / steps
+    achieved = ref_bytes / (ref_ms * 1e-3) / 1e9 if ref_ms > 0 else 0.0
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", f"refine_traffic_workload{args.workload}.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+
+    pairs_total = chosen["pairs"] * world
+    value = pairs_total / (chosen["ms"] * 1e-3)
+    plain = results["plain"]
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "pairs/s",
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": chosen["ms"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 (f32 filter)",
+        "data": "synthetic (seeded; SpatialBench data not available)",
+        "config": {"workload": WORKLOAD_NAMES[args.workload], "probe_rows": n_rows,
+                   "build_rows": len(inp.build), "predicate": pred, "scale": args.scale,
+                   "pairs_per_step": chosen["pairs"], "l2": "probe column > L2, no flush",
+                   "parallelism": f"replicas x{world}"},
+        "probe_rows_per_s": n_rows * world / (chosen["ms"] * 1e-3),
+        "plain_f64_form": {"pairs_per_s": plain["pairs"] * world / (plain["ms"] * 1e-3),
+                           "ms_per_step": plain["ms"], "pairs": plain["pairs"],
+                           "steps": max(1, args.plain_steps),
+                           "speedup_chosen_vs_plain": plain["ms"] / chosen["ms"]},
+        "phases_ms_per_step": {k: st[k] / steps for k in
+                               ("ms_decode", "ms_filter", "ms_refine", "ms_compact")},
+        "fp64_escalated_fraction": st["escalations"] / max(1, st["pairs_evaluated"]),
+        "candidates_per_step": st["candidates"] / steps,
+        "gpu_launches": int(st["kernel_launches"]),
+        "e2e": {"value": pairs_total / (e2e_ms * 1e-3), "unit": "pairs/s",
+                "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(off.nbytes + data.nbytes),
+                "d2h_bytes_per_step": int(8 * n_e2e)},
+        "roofline": {"bound": "hbm", "kernel": "k_refine<fast>", "achieved": achieved,
+                     "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": ref_bytes},
+        "clocks": chosen["clocks"],
+    }
+    return out, inp
+
+
+def cpu_baseline(inp, seconds_budget: float = 15.0):
+    """The oracle (C restatement of the reference CPU join) on a bounded
+    sample of the probe side with all host threads."""
+    import oracle
+    oracle.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    B = oracle.Geoms(inp.build)
+    pred = {"knn": "dwithin"}.get(inp.predicate, inp.predicate)
+    distance = float(inp.params.get("distance", 0.0))
+    n = len(inp.probe)
+    rows = min(n, 20000)
+    t0 = time.perf_counter()
+    npairs = 0
+    done = 0
+    while True:
+        P = oracle.Geoms(inp.probe.slice(done % n, min(n, done % n + rows)))
+        b, p = oracle.join(B, P, pred, distance, nthreads=threads)
+        npairs += len(b)
+        done += len(P._keep)
+        el = time.perf_counter() - t0
+        if el > seconds_budget or done >= n:
+            break
+        rows = min(n, int(rows * 2))
+    return {"value": npairs / el, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "probe_rows_per_s": done / el,
+            "sample": f"first {done} probe rows of the workload against the full build side"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    inp = make_inputs(args.workload, args.scale)
+    vals = []
+    for _ in range(args.warmup):
+        pass  # the CPU join has no warm-up state worth priming beyond the first sample
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(inp, seconds_budget=args.ref_seconds))
+    v = float(np.median([x["value"] for x in vals]))
+    base = vals[-1]
+    return {
+        "impl": "reference",
+        "metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD_NAMES[args.workload], "probe_rows": len(inp.probe),
+                   "build_rows": len(inp.build), "scale": args.scale},
+        "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": base["cores"],
+                         "kind": "port", "sample": base["sample"]},
+        "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "restatement of the reference CPU SpatialJoinExec (tg predicates) in C; "
+                "the reference's Rust binary cannot be built here",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--workload", type=int, default=2)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, pg = (1, 0, 0, None)
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    world, rank, local, pg = dist_setup()
+    out, inp = run_ours(args, world, rank, local, pg)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(inp, seconds_budget=args.ref_seconds)
+        out.pop("_", None)
+        print(json.dumps(out))
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

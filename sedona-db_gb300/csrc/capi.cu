@@ -245,17 +245,20 @@ void build_engine_from_host(JoinEngine& eng, WorkspacePool& pool, const HostColu
   }
   uint64_t bytes = 0;
   WkbDeviceColumn d = stage_column(*ws, c, &bytes);
-  eng.build(d, ws->stream);
+  SPJ_CUDA(cudaStreamSynchronize(ws->stream));  // staged column complete
+  eng.build(d);
 }
 
 // --- SedonaFloatIndex2D ----------------------------------------------------
 
 struct IndexData {
   RuntimeData* rt;
+  // declared before bvh: members are destroyed in reverse order, and bvh's
+  // buffers free on a pool workspace's stream
+  std::unique_ptr<WorkspacePool> pool;
   std::vector<float> rects;
   Lbvh bvh;
   bool built = false;
-  std::unique_ptr<WorkspacePool> pool;
   std::string last_error;
 };
 
@@ -629,7 +632,8 @@ extern "C" int SpjJoinBuildDevice(SpjJoin* j, const SpjDeviceWkb* column) {
   return guarded(j->last_error, [&] {
     SPJ_CUDA(cudaSetDevice(j->rt->device_id));
     j->host.clear();
-    j->engine->build(device_column(column), j->ws->stream);
+    SPJ_CUDA(cudaDeviceSynchronize());  // the caller's column is complete
+    j->engine->build(device_column(column));
   });
 }
 

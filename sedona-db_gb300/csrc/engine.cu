@@ -40,12 +40,23 @@ Workspace::~Workspace() {
   }
 }
 
-JoinEngine::JoinEngine(int device, EngineConfig cfg) : device_(device), cfg_(cfg) {}
+JoinEngine::JoinEngine(int device, EngineConfig cfg) : device_(device), cfg_(cfg) {
+  SPJ_CUDA(cudaStreamCreateWithFlags(&bs_, cudaStreamNonBlocking));
+}
 
-JoinEngine::~JoinEngine() { cudaDeviceSynchronize(); }
+JoinEngine::~JoinEngine() {
+  // the build-side buffers free on bs_: release them before bs_ goes away
+  cudaStreamSynchronize(bs_);
+  bg_ = DeviceGeoms();
+  bsc_ = DecodeScratch();
+  bvh_ = Lbvh();
+  cudaStreamSynchronize(bs_);
+  cudaStreamDestroy(bs_);
+}
 
-void JoinEngine::build(const WkbDeviceColumn& col, cudaStream_t s) {
+void JoinEngine::build(const WkbDeviceColumn& col) {
   built_ = false;
+  cudaStream_t s = bs_;
   decode_wkb(col, bg_, bsc_, false, s);
   if (bg_.nrings > 0) build_band_index(bg_, bsc_, s);
   build_lbvh(bg_.box.as<float4>(), bg_.n, cfg_.leaf_size, bvh_, s);

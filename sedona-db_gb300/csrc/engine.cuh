@@ -60,8 +60,10 @@ class JoinEngine {
   int device() const { return device_; }
   EngineConfig& config() { return cfg_; }
 
-  // Build side from a device WKB column (decoded, boxed, indexed, banded).
-  void build(const WkbDeviceColumn& col, cudaStream_t s);
+  // Build side from a device WKB column (decoded, boxed, indexed, banded),
+  // on the engine's own stream; the column must be complete on the device
+  // (the caller has synchronized whatever stream wrote it).
+  void build(const WkbDeviceColumn& col);
   bool built() const { return built_; }
   const DeviceGeoms& build_geoms() const { return bg_; }
   const Lbvh& lbvh() const { return bvh_; }
@@ -86,6 +88,7 @@ class JoinEngine {
   DeviceGeoms bg_;
   DecodeScratch bsc_;
   Lbvh bvh_;
+  cudaStream_t bs_ = nullptr;  // build stream; owns the frees of bg_/bsc_/bvh_
   bool built_ = false;
   std::mutex stats_mu_;
   JoinStats stats_;
