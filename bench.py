@@ -121,26 +121,34 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_setup():
+def dist_setup(backend: str = "nccl"):
+    """Replicas only: every rank runs the whole workload on its own GPU; the
+    process group is used for the barrier around the timed region and the
+    max-over-ranks time, never on the data path."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl"
         dist.init_process_group(backend=backend)
         pg = dist
     return world, rank, local, pg
 
 
 def barrier_max(pg, value: float, device) -> float:
+    """Max of a per-rank time over all ranks (the job's time)."""
     if pg is None:
         return value
     import torch
     t = torch.tensor([value], dtype=torch.float64, device=device)
     pg.all_reduce(t, op=pg.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_value(pairs_per_rank: int, world: int, ms_max: float) -> float:
+    """Whole-job pairs/s: every replica processes the same workload."""
+    return pairs_per_rank * world / (ms_max * 1e-3)
 
 
 def to_device(col):

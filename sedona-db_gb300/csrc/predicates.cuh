@@ -382,6 +382,39 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
   }
   const uint32_t Vo = Go->ring_vtx[ro];
   const int nso = Go->ring_nsegs[ro];
+  if (kFast && nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
+    // Isolation exit.  If every segment of the larger ring has a bbox
+    // strictly separated from the smaller ring's bbox (a strict f32
+    // comparison of round-to-nearest values proves the f64 one), then
+    //  - no segment test can succeed (tg's first test is the bbox test), and
+    //  - for every vertex v of the smaller ring, each ray-cast decision is one
+    //    of tg's comparison-only exits (v lies outside every segment's closed
+    //    bbox), i.e. the exact half-open crossing rule; no segment crosses the
+    //    smaller ring's bbox, so that parity is the same for all its vertices.
+    // The result is therefore the point-in-ring test of the first vertex.
+    const Rect64 ob = Go->ring_rect[ro];
+    const float bx0 = __double2float_rn(ob.x), by0 = __double2float_rn(ob.y);
+    const float bx1 = __double2float_rn(ob.z), by1 = __double2float_rn(ob.w);
+    const uint32_t Vr = Gr->ring_vtx[rr];
+    const uint32_t B = Gr->ring_bands[rr];
+    const int nb = (int)(Gr->ring_bands[rr + 1] - B) - 1;
+    const float2 prm = Gr->band_param[rr];
+    const int b0 = band_of(by0, prm.x, prm.y, nb), b1 = band_of(by1, prm.x, prm.y, nb);
+    bool near = false;
+    for (int bb = b0; bb <= b1 && !near; bb++) {
+      const uint32_t e0 = Gr->band_off[B + bb], e1 = Gr->band_off[B + bb + 1];
+      for (uint32_t k = e0; k < e1; k++) {
+        const int i = Gr->band_edges[k];
+        const float2 c = Gr->xy32[Vr + i], d = Gr->xy32[Vr + i + 1];
+        if (!(fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
+              fmin0f(c.y, d.y) > by1)) {
+          near = true;
+          break;
+        }
+      }
+    }
+    if (!near) return ring_pip<kFast>(*Gr, rr, Go->xy[Vo], Go->xy32[Vo], true, esc).hit;
+  }
   for (int i = 0; i <= nso; i++) {
     const double2 v = Go->xy[Vo + i];
     const float2 v32 = Go->xy32[Vo + i];
