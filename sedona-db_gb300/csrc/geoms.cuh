@@ -38,6 +38,7 @@ struct GeomsView {
   const uint32_t* ring_vtx = nullptr;
   const int32_t* ring_nsegs = nullptr;
   const Rect64* ring_rect = nullptr;
+  const float4* ring_rect32 = nullptr;  // the same rect rounded to nearest
   const double2* xy = nullptr;
   const float2* xy32 = nullptr;
   // y-band edge index (nullptr when not built)
@@ -52,7 +53,8 @@ struct DeviceGeoms {
   bool all_points = false;  // every non-empty row is a point
   bool any_points = false;
   bool any_polys = false;
-  DevBuf kind, pt, box, row_part, part_ring, ring_vtx, ring_nsegs, ring_rect, xy, xy32;
+  DevBuf kind, pt, box, row_part, part_ring, ring_vtx, ring_nsegs, ring_rect, ring_rect32, xy,
+      xy32;
   DevBuf ring_bands, band_off, band_edges, band_param;
   bool has_bands = false;
 
@@ -70,6 +72,7 @@ struct DeviceGeoms {
     v.ring_vtx = ring_vtx.as<uint32_t>();
     v.ring_nsegs = ring_nsegs.as<int32_t>();
     v.ring_rect = ring_rect.as<Rect64>();
+    v.ring_rect32 = ring_rect32.as<float4>();
     v.xy = xy.as<double2>();
     v.xy32 = xy32.as<float2>();
     if (has_bands) {
@@ -82,7 +85,8 @@ struct DeviceGeoms {
   }
   size_t device_bytes() const {
     return kind.size() + pt.size() + box.size() + row_part.size() + part_ring.size() +
-           ring_vtx.size() + ring_nsegs.size() + ring_rect.size() + xy.size() + xy32.size() +
+           ring_vtx.size() + ring_nsegs.size() + ring_rect.size() + ring_rect32.size() +
+           xy.size() + xy32.size() +
            ring_bands.size() + band_off.size() + band_edges.size() + band_param.size();
   }
 };

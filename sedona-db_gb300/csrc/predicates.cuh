@@ -179,6 +179,16 @@ __device__ __forceinline__ bool rect_covers_point(Rect64 r, double2 p) {
   return !(p.x < r.x || p.y < r.y || p.x > r.z || p.y > r.w);
 }
 
+// tg_rect_covers_point(ring rect, p), decided on the RN32 copies when a strict
+// comparison settles it (strictly outside, or strictly inside), else in FP64.
+__device__ __forceinline__ bool ring_rect_covers(const GeomsView& G, uint32_t r, double2 p,
+                                                 float2 p32) {
+  const float4 q = G.ring_rect32[r];
+  if (p32.x < q.x || p32.y < q.y || p32.x > q.z || p32.y > q.w) return false;
+  if (p32.x > q.x && p32.y > q.y && p32.x < q.z && p32.y < q.w) return true;
+  return rect_covers_point(G.ring_rect[r], p);
+}
+
 __device__ __forceinline__ int band_of(float y32, float y0, float inv_h, int nb) {
   float t = __fmul_rn(__fsub_rn(y32, y0), inv_h);
   if (!(t >= 0.0f)) return 0;
@@ -214,7 +224,7 @@ __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r
 __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r, double2 p,
                                                  float2 p32, bool aoe, uint32_t& esc) {
   RingHit h{false, -1};
-  if (!rect_covers_point(G.ring_rect[r], p)) return h;
+  if (!ring_rect_covers(G, r, p, p32)) return h;
   const uint32_t V = G.ring_vtx[r];
   bool in = false;
   int idx = -1;
@@ -309,7 +319,7 @@ __device__ __forceinline__ bool poly_touches_point(const GeomsView& G, uint32_t 
 // (tg.c:3046-3087 with allow_on_edge; tg_ring_search filter tg.c:2468-2485).
 template <bool kFast>
 __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, double2 a, double2 b,
-                                             uint32_t& esc) {
+                                             float2 a32, float2 b32, uint32_t& esc) {
   const uint32_t V = G.ring_vtx[r];
   int count = 0;
   if (!kFast) {
@@ -318,8 +328,6 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
       if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
     return count;
   }
-  const float2 a32 = make_float2(__double2float_rn(a.x), __double2float_rn(a.y));
-  const float2 b32 = make_float2(__double2float_rn(b.x), __double2float_rn(b.y));
   const float qx0 = fmin0f(a32.x, b32.x), qx1 = fmax0f(a32.x, b32.x);
   const float qy0 = fmin0f(a32.y, b32.y), qy1 = fmax0f(a32.y, b32.y);
   auto test = [&](int i) {
@@ -359,6 +367,46 @@ __device__ __forceinline__ double rect_area(Rect64 r) {
   return __dmul_rn(__dsub_rn(r.z, r.x), __dsub_rn(r.w, r.y));
 }
 
+// Interval [lo, hi] containing the exact area of a rect known only through
+// its RN32 corners (each exact coordinate is within one f32 ulp of its RN).
+__device__ __forceinline__ void rect_area_bounds(float4 q, float& lo, float& hi) {
+  const float wl = fmaxf(__fsub_rd(next_downf(q.z), next_upf(q.x)), 0.0f);
+  const float wh = __fsub_ru(next_upf(q.z), next_downf(q.x));
+  const float hl = fmaxf(__fsub_rd(next_downf(q.w), next_upf(q.y)), 0.0f);
+  const float hh = __fsub_ru(next_upf(q.w), next_downf(q.y));
+  lo = __fmul_rd(wl, hl);
+  hi = __fmul_ru(wh, hh);
+}
+
+// tg swaps the rings when rect_area(other) > rect_area(ring) in FP64
+// (tg.c:3176-3183).  Decided from f32 area bounds when they are separated by
+// far more than FP64 rounding can move the two products; else in FP64.
+template <bool kFast>
+__device__ __forceinline__ bool swap_rings(const GeomsView& GA, uint32_t ra, const GeomsView& GB,
+                                           uint32_t rb) {
+  if (kFast) {
+    float a_lo, a_hi, b_lo, b_hi;
+    rect_area_bounds(GA.ring_rect32[ra], a_lo, a_hi);
+    rect_area_bounds(GB.ring_rect32[rb], b_lo, b_hi);
+    if (b_lo > __fmul_ru(a_hi, 1.0000010f)) return true;
+    if (__fmul_ru(b_hi, 1.0000010f) < a_lo) return false;
+  }
+  return rect_area(GB.ring_rect[rb]) > rect_area(GA.ring_rect[ra]);
+}
+
+// tg_rect_intersects_rect of two ring rects, f32 first when strict.
+template <bool kFast>
+__device__ __forceinline__ bool ring_rects_intersect(const GeomsView& GA, uint32_t ra,
+                                                     const GeomsView& GB, uint32_t rb) {
+  if (kFast) {
+    const float4 a = GA.ring_rect32[ra], b = GB.ring_rect32[rb];
+    if (b.x > a.z || b.z < a.x || b.y > a.w || b.w < a.y) return false;
+    if (b.x < a.z && b.z > a.x && b.y < a.w && b.w > a.y) return true;
+  }
+  const Rect64 A = GA.ring_rect[ra], Bq = GB.ring_rect[rb];
+  return !(Bq.x > A.z || Bq.z < A.x || Bq.y > A.w || Bq.w < A.y);
+}
+
 // tg.c:3166-3192 + tg.c:3089-3113 with allow_on_edge = true, for two rings.
 // The result is the OR over the smaller ring's vertices of "vertex in or on
 // the larger ring" and over its segments of "crosses >= 2 of the larger
@@ -369,12 +417,11 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
                                                      const GeomsView& GB, uint32_t rb,
                                                      uint32_t& esc) {
   if (ring_npts(GA, ra) < 3 || ring_npts(GB, rb) < 3) return false;
-  const Rect64 A = GA.ring_rect[ra], Bq = GB.ring_rect[rb];
-  if (Bq.x > A.z || Bq.z < A.x || Bq.y > A.w || Bq.w < A.y) return false;
+  if (!ring_rects_intersect<kFast>(GA, ra, GB, rb)) return false;
   const GeomsView* Gr = &GA;
   const GeomsView* Go = &GB;
   uint32_t rr = ra, ro = rb;
-  if (rect_area(Bq) > rect_area(A)) {
+  if (swap_rings<kFast>(GA, ra, GB, rb)) {
     Gr = &GB;
     Go = &GA;
     rr = rb;
@@ -392,9 +439,8 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
     //    bbox), i.e. the exact half-open crossing rule; no segment crosses the
     //    smaller ring's bbox, so that parity is the same for all its vertices.
     // The result is therefore the point-in-ring test of the first vertex.
-    const Rect64 ob = Go->ring_rect[ro];
-    const float bx0 = __double2float_rn(ob.x), by0 = __double2float_rn(ob.y);
-    const float bx1 = __double2float_rn(ob.z), by1 = __double2float_rn(ob.w);
+    const float4 ob = Go->ring_rect32[ro];
+    const float bx0 = ob.x, by0 = ob.y, bx1 = ob.z, by1 = ob.w;
     const uint32_t Vr = Gr->ring_vtx[rr];
     const uint32_t B = Gr->ring_bands[rr];
     const int nb = (int)(Gr->ring_bands[rr + 1] - B) - 1;
@@ -420,14 +466,22 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
     const float2 v32 = Go->xy32[Vo + i];
     if (ring_pip<kFast>(*Gr, rr, v, v32, true, esc).hit) return true;
   }
-  const Rect64 R = Gr->ring_rect[rr];
+  const float4 R32 = Gr->ring_rect32[rr];
   for (int i = 0; i < nso; i++) {
     const double2 a = Go->xy[Vo + i], b = Go->xy[Vo + i + 1];
-    // tg.c:3092-3094 segment rect vs ring rect
-    if (fmin0(a.x, b.x) > R.z || fmax0(a.x, b.x) < R.x || fmin0(a.y, b.y) > R.w ||
-        fmax0(a.y, b.y) < R.y)
+    const float2 a32 = Go->xy32[Vo + i], b32 = Go->xy32[Vo + i + 1];
+    // tg.c:3092-3094 segment rect vs ring rect: a separated segment has no
+    // hits anyway, so only the strict f32 separation is used to skip it
+    if (kFast && (fmin0f(a32.x, b32.x) > R32.z || fmax0f(a32.x, b32.x) < R32.x ||
+                  fmin0f(a32.y, b32.y) > R32.w || fmax0f(a32.y, b32.y) < R32.y))
       continue;
-    if (ring_seg_hits<kFast>(*Gr, rr, a, b, esc) >= 2) return true;
+    if (!kFast) {
+      const Rect64 R = Gr->ring_rect[rr];
+      if (fmin0(a.x, b.x) > R.z || fmax0(a.x, b.x) < R.x || fmin0(a.y, b.y) > R.w ||
+          fmax0(a.y, b.y) < R.y)
+        continue;
+    }
+    if (ring_seg_hits<kFast>(*Gr, rr, a, b, a32, b32, esc) >= 2) return true;
   }
   return false;
 }

@@ -20,8 +20,11 @@ using namespace pred;
 
 constexpr int kUnsupportedResult = -1;
 
-__device__ __forceinline__ float2 rn32(double2 p) {
-  return make_float2(__double2float_rn(p.x), __double2float_rn(p.y));
+// RN32 coordinates of a point row: the decoder stores them as its degenerate
+// filter box (x, y, x, y), so no f64 -> f32 conversion is needed here.
+__device__ __forceinline__ float2 pt32(const GeomsView& G, uint32_t i) {
+  const float4 b = G.box[i];
+  return make_float2(b.x, b.y);
 }
 
 __device__ __forceinline__ uint32_t nparts(const GeomsView& G, uint32_t i) {
@@ -40,7 +43,7 @@ __device__ int g_intersects(const GeomsView& GA, uint32_t ia, const GeomsView& G
     const GeomsView& GY = ka == kPoint ? GB : GA;  // the polygonal side
     const uint32_t ip = ka == kPoint ? ia : ib, iy = ka == kPoint ? ib : ia;
     const double2 p = GP.pt[ip];
-    const float2 p32 = rn32(p);
+    const float2 p32 = pt32(GP, ip);
     for (uint32_t q = GY.row_part[iy]; q < GY.row_part[iy + 1]; q++)
       if (poly_contains_point<kFast>(GY, q, p, p32, true, esc)) return 1;
     return 0;
@@ -72,7 +75,7 @@ __device__ int g_contains(const GeomsView& GA, uint32_t ia, const GeomsView& GB,
   if (ka == kPoint) return 0;  // tg.c:1157-1162
   if (kb == kPoint) {
     const double2 p = GB.pt[ib];
-    const float2 p32 = rn32(p);
+    const float2 p32 = pt32(GB, ib);
     for (uint32_t q = GA.row_part[ia]; q < GA.row_part[ia + 1]; q++)
       if (poly_contains_point<kFast>(GA, q, p, p32, false, esc)) return 1;
     return 0;
@@ -89,7 +92,7 @@ __device__ int g_covers(const GeomsView& GA, uint32_t ia, const GeomsView& GB, u
   if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
   if (kb == kPoint) {
     const double2 p = GB.pt[ib];
-    const float2 p32 = rn32(p);
+    const float2 p32 = pt32(GB, ib);
     for (uint32_t q = GA.row_part[ia]; q < GA.row_part[ia + 1]; q++)
       if (poly_contains_point<kFast>(GA, q, p, p32, true, esc)) return 1;
     return 0;
@@ -114,11 +117,11 @@ __device__ int g_touches(const GeomsView& GA, uint32_t ia, const GeomsView& GB, 
   if (ka == kPoint && kb == kPoint) return 0;
   if (ka == kPolygon && kb == kPoint) {
     const double2 p = GB.pt[ib];
-    return poly_touches_point<kFast>(GA, GA.row_part[ia], p, rn32(p), esc);
+    return poly_touches_point<kFast>(GA, GA.row_part[ia], p, pt32(GB, ib), esc);
   }
   if (ka == kPoint && kb == kPolygon) {
     const double2 p = GA.pt[ia];
-    return poly_touches_point<kFast>(GB, GB.row_part[ib], p, rn32(p), esc);
+    return poly_touches_point<kFast>(GB, GB.row_part[ib], p, pt32(GA, ia), esc);
   }
   return kUnsupportedResult;
 }
@@ -275,8 +278,9 @@ __global__ void __launch_bounds__(256)
     if (kFast) {
       // |r32 - hypot| <= err: coordinate rounding (u = 2^-24 per operand,
       // doubled) plus the FP32 square / sum / sqrt rounding.
-      const float bx = __double2float_rn(b.x), by = __double2float_rn(b.y);
-      const float px = __double2float_rn(p.x), py = __double2float_rn(p.y);
+      const float2 b32 = pt32(B, bi), p32 = pt32(P, pi);
+      const float bx = b32.x, by = b32.y;
+      const float px = p32.x, py = p32.y;
       const float fx = __fsub_rn(bx, px), fy = __fsub_rn(by, py);
       const float r32 = __fsqrt_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)));
       const float mag = fabsf(bx) + fabsf(px) + fabsf(by) + fabsf(py) + fabsf(fx) + fabsf(fy);

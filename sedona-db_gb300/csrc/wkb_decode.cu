@@ -284,7 +284,7 @@ __global__ void k_wkb_coords(const uint8_t* __restrict__ d, uint64_t len, bool a
                              const uint32_t* __restrict__ ring_npts,
                              const uint32_t* __restrict__ ring_vtx, double2* __restrict__ xy,
                              float2* __restrict__ xy32, Rect64* __restrict__ ring_rect,
-                             int32_t* __restrict__ ring_nsegs) {
+                             float4* __restrict__ ring_rect32, int32_t* __restrict__ ring_nsegs) {
   const int lane = threadIdx.x & 31;
   const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -321,6 +321,8 @@ __global__ void k_wkb_coords(const uint8_t* __restrict__ d, uint64_t len, bool a
     __syncwarp();
     if (lane == 0) {
       ring_rect[r] = make_rect64(mnx, mny, mxx, mxy);
+      ring_rect32[r] = make_float4(__double2float_rn(mnx), __double2float_rn(mny),
+                                   __double2float_rn(mxx), __double2float_rn(mxy));
       int32_t ns = 0;
       if (npts >= 3) {
         double2 f = xy[V], l = xy[V + npts - 1];
@@ -568,6 +570,7 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
   out.ring_vtx.reserve(((size_t)out.nrings + 1) * 4, s);
   out.ring_nsegs.reserve(((size_t)out.nrings + 1) * 4, s);
   out.ring_rect.reserve(((size_t)out.nrings + 1) * sizeof(Rect64), s);
+  out.ring_rect32.reserve(((size_t)out.nrings + 1) * sizeof(float4), s);
   out.xy.reserve(((size_t)out.nverts + 1) * sizeof(double2), s);
   out.xy32.reserve(((size_t)out.nverts + 1) * sizeof(float2), s);
   sc.ring_src.reserve(((size_t)out.nrings + 1) * 12, s);
@@ -587,7 +590,7 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
     k_wkb_coords<<<grid_for((int64_t)out.nrings * 32, 256, kNumSMs * 32), 256, 0, s>>>(
         col.data, col.data_len, al, out.nrings, ring_src, ring_npts, out.ring_vtx.as<uint32_t>(),
         out.xy.as<double2>(), out.xy32.as<float2>(), out.ring_rect.as<Rect64>(),
-        out.ring_nsegs.as<int32_t>());
+        out.ring_rect32.as<float4>(), out.ring_nsegs.as<int32_t>());
     k_row_box<<<grid, block, 0, s>>>(out.n, out.kind.as<uint8_t>(), out.row_part.as<uint32_t>(),
                                      out.part_ring.as<uint32_t>(), out.ring_rect.as<Rect64>(),
                                      out.box.as<float4>());
