@@ -146,6 +146,33 @@ int SpjKnnQuery(SpjKnn* knn, const double* probe_xy, uint64_t n_probe, uint32_t 
 void* SpjKnnStream(SpjKnn* knn);
 
 /* ------------------------------------------------------------------------ */
+/* Probe without allocating.  No counterpart in the reference interface.     */
+
+/* Largest n_rects one SpjIndexProbeNoAlloc call accepts. */
+#define SPJ_NOALLOC_MAX_PROBES (1u << 18)
+
+/* The candidate filter of a built SedonaFloatIndex2D (the same pairs its
+ * probe reports: every intersecting (build, probe) rect pair, in ascending
+ * probe order) for callers that cannot allocate device memory at probe time,
+ * e.g. an executor whose own arena holds the device memory budget, or a
+ * latency-critical loop that must not touch the CUDA allocator.  Makes no
+ * cudaMalloc / cudaFree and calls no allocating library routine: its scratch
+ * is a 4 MiB static device array that every GPU loading the library keeps
+ * until exit, which limits a call to SPJ_NOALLOC_MAX_PROBES rects (larger
+ * n_rects is rejected with EINVAL and a message from get_last_error).
+ * d_rects (n_rects x [min_x, min_y, max_x, max_y] float32), d_out_build and
+ * d_out_probe (capacity entries each) are device pointers; *n_pairs (host)
+ * receives the pair count, and if it exceeds capacity nothing is written and
+ * ENOSPC is returned.  stream is a cudaStream_t (NULL = default stream); the
+ * call synchronizes it.  The first call on a device looks up the static
+ * array's device address (no allocation), so make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialized by the caller. */
+int SpjIndexProbeNoAlloc(struct SedonaFloatIndex2D* index, const float* d_rects,
+                         uint32_t n_rects, uint32_t* d_out_build, uint32_t* d_out_probe,
+                         uint64_t capacity, uint64_t* n_pairs, void* stream);
+
+/* ------------------------------------------------------------------------ */
 
 int SpjHostRegister(void* ptr, uint64_t bytes);
 int SpjHostUnregister(void* ptr);

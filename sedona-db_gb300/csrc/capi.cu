@@ -495,6 +495,17 @@ void ref_release(SedonaSpatialRefiner* self) {
 
 }  // namespace
 
+namespace spj {
+// The LBVH of a built SedonaFloatIndex2D (nullptr before finish_building), its
+// runtime's device and its last-error slot; used by SpjIndexProbeNoAlloc.
+const Lbvh* index_lbvh(SedonaFloatIndex2D* index, int* device, std::string** last_error) {
+  auto* d = static_cast<IndexData*>(index->private_data);
+  *device = d->rt->device_id;
+  *last_error = &d->last_error;
+  return d->built ? &d->bvh : nullptr;
+}
+}  // namespace spj
+
 // =============================================================================
 // exported: reference interface
 

@@ -339,6 +339,25 @@ void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
   SPJ_CUDA(cudaGetLastError());
 }
 
+void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                      uint32_t* counts, cudaStream_t s) {
+  if (nprobe == 0) return;
+  const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
+  k_probe<false><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, counts, nullptr, 0, nullptr,
+                                            nullptr);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                        const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
+                        uint32_t* out_probe, cudaStream_t s) {
+  if (nprobe == 0) return;
+  const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
+  k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr, offs, probe_base,
+                                           out_build, out_probe);
+  SPJ_CUDA(cudaGetLastError());
+}
+
 void expand_boxes(const double2* pts, const float4* boxes, const uint8_t* kind, uint32_t n,
                   double distance, float4* out, cudaStream_t s) {
   if (n == 0) return;

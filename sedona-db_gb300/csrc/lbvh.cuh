@@ -63,6 +63,15 @@ void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                    const ProbeScratch& sc, uint32_t probe_base, uint32_t* out_build,
                    uint32_t* out_probe, cudaStream_t s);
 
+// The two traversal passes with caller-owned count / offset arrays (no
+// allocation): counts[nprobe] written by the first, offs[nprobe] read by the
+// second.
+void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                      uint32_t* counts, cudaStream_t s);
+void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                        const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
+                        uint32_t* out_probe, cudaStream_t s);
+
 // Expand point/box probes by a distance (f64), then round outward to f32
 // (rust/sedona-spatial-join/src/operand_evaluator.rs:605-607).
 void expand_boxes(const double2* pts, const float4* boxes, const uint8_t* kind, uint32_t n,

@@ -211,6 +211,24 @@ void scan_u32_u64(const uint32_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cud
 void scan_u8_u64(const uint8_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
   scan_impl<uint8_t, uint64_t>(in, out, n, tmp, s);
 }
+size_t scan_tile_sums_bytes(int64_t n) {
+  int64_t nt = (n + kScanTile - 1) / kScanTile;
+  return (size_t)((nt < 1 ? 1 : nt) + 1) * sizeof(uint64_t);
+}
+
+void scan_u32_u64_into(const uint32_t* in, uint64_t* out, int64_t n, uint64_t* sums,
+                       cudaStream_t s) {
+  if (n == 0) {
+    SPJ_CUDA(cudaMemsetAsync(out, 0, sizeof(uint64_t), s));
+    return;
+  }
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  k_tile_reduce<uint32_t, uint64_t><<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums);
+  k_scan_sums<uint64_t><<<1, 1024, 0, s>>>(sums, nt, out + n);
+  k_tile_scan<uint32_t, uint64_t><<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums, out);
+  SPJ_CUDA(cudaGetLastError());
+}
+
 void scan_u32_u32(const uint32_t* in, uint32_t* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
   scan_impl<uint32_t, uint32_t>(in, out, n, tmp, s);
 }

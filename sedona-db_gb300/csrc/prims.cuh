@@ -11,6 +11,10 @@ namespace spj {
 void scan_u32_u64(const uint32_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t s);
 void scan_u8_u64(const uint8_t* in, uint64_t* out, int64_t n, DevBuf& tmp, cudaStream_t s);
 void scan_u32_u32(const uint32_t* in, uint32_t* out, int64_t n, DevBuf& tmp, cudaStream_t s);
+// Same scan with caller-owned tile-sum scratch of scan_tile_sums_bytes(n) bytes.
+size_t scan_tile_sums_bytes(int64_t n);
+void scan_u32_u64_into(const uint32_t* in, uint64_t* out, int64_t n, uint64_t* tile_sums,
+                       cudaStream_t s);
 
 // Stable LSD sort of (keys, vals) by key bits [0, key_bits).  keys/vals are
 // replaced by the sorted sequences; alt_keys/alt_vals are scratch of size n.

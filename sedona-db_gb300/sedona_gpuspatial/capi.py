@@ -156,6 +156,7 @@ EXPORTS = [
     "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
     "SpjKnnStream", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
+    "SpjIndexProbeNoAlloc",
 ]
 
 _lib = None
