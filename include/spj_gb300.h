@@ -122,6 +122,41 @@ int SpjJoinGetStats(SpjJoin* join, struct SpjJoinStats* out);
 int SpjJoinResetStats(SpjJoin* join);
 
 /* ------------------------------------------------------------------------ */
+/* Batched probe stream: many uneven record batches of point WKB probed in
+ * one CUDA-graph replay (a persistent work-queue kernel counts, a scan
+ * places, the same kernel emits).  Serves SpatialJoinStream's per-batch
+ * query_batch loop (rust/sedona-spatial-join/src/stream.rs:1166-1200) without
+ * a host round trip per batch.  The SpjJoin it is created from must outlive
+ * it.  Relation predicates only; batch rows must be points. */
+
+typedef struct SpjStream SpjStream;
+
+int SpjStreamCreate(SpjJoin* join, SpjStream** out);
+void SpjStreamRelease(SpjStream* stream);
+const char* SpjStreamLastError(SpjStream* stream);
+/* Device columns, one per batch; probe ids are global over the batches in
+ * order (batch i starts after the rows of batches 0..i-1). */
+int SpjStreamSetBatches(SpjStream* stream, const struct SpjDeviceWkb* batches,
+                        int32_t n_batches);
+/* One replay over all batches; pairs (device arrays owned by the stream,
+ * valid until the next run) grouped by probe row in ascending order. */
+int SpjStreamRun(SpjStream* stream, int32_t predicate, const uint32_t** d_build,
+                 const uint32_t** d_probe, uint64_t* n_pairs);
+/* block: 64, 128 or 256 threads; chunk_rows: rows per work item; leaf_size:
+ * LBVH leaf size (rebuilds the index). */
+int SpjStreamSetParams(SpjStream* stream, int32_t block, uint32_t chunk_rows, uint32_t leaf_size);
+/* Times block x chunk_rows x leaf_size candidates on the current batches,
+ * keeps the fastest and returns it; cache_path (may be NULL) stores results
+ * per device and workload signature and is consulted first. */
+int SpjStreamAutotune(SpjStream* stream, int32_t predicate, const char* cache_path,
+                      int32_t* block, uint32_t* chunk_rows, uint32_t* leaf_size);
+/* Device time of the last replay (CUDA events around the graph launch),
+ * FP64-escalated tests so far and kernel launches per replay. */
+int SpjStreamGetStats(SpjStream* stream, double* ms_last, uint64_t* escalations,
+                      uint64_t* launches_per_replay);
+void* SpjStreamCudaStream(SpjStream* stream);
+
+/* ------------------------------------------------------------------------ */
 /* KNN join over point columns                                              */
 
 typedef struct SpjKnn SpjKnn;

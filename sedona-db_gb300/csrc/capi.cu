@@ -19,6 +19,7 @@
 #include "../../include/spj_gb300.h"
 #include "engine.cuh"
 #include "knn.cuh"
+#include "stream.cuh"
 #include "prims.cuh"
 
 // Arrow C data interface (https://arrow.apache.org/docs/format/CDataInterface.html)
@@ -750,6 +751,85 @@ extern "C" int SpjJoinGetStats(SpjJoin* j, SpjJoinStats* out) {
 extern "C" int SpjJoinResetStats(SpjJoin* j) {
   return guarded(j->last_error, [&] { j->engine->reset_stats(); });
 }
+
+// =============================================================================
+// exported: SpjStream
+
+struct SpjStream {
+  SpjJoin* join = nullptr;
+  std::unique_ptr<StreamJoin> s;
+  std::string last_error;
+};
+
+extern "C" int SpjStreamCreate(SpjJoin* j, SpjStream** out) {
+  if (!j || !out) return EINVAL;
+  return guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    SPJ_CHECK(j->engine->built(), "stream on a join whose build side is not finished");
+    auto st = std::make_unique<SpjStream>();
+    st->join = j;
+    st->s = std::make_unique<StreamJoin>(*j->engine);
+    *out = st.release();
+  });
+}
+
+extern "C" void SpjStreamRelease(SpjStream* st) {
+  if (!st) return;
+  cudaSetDevice(st->join->rt->device_id);
+  delete st;
+}
+
+extern "C" const char* SpjStreamLastError(SpjStream* st) { return st->last_error.c_str(); }
+
+extern "C" int SpjStreamSetBatches(SpjStream* st, const SpjDeviceWkb* batches, int32_t n) {
+  return guarded(st->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(st->join->rt->device_id));
+    SPJ_CHECK(n >= 0 && (n == 0 || batches != nullptr), "bad batch list");
+    std::vector<WkbDeviceColumn> cols;
+    for (int32_t i = 0; i < n; i++) cols.push_back(device_column(&batches[i]));
+    st->s->set_batches(cols);
+  });
+}
+
+extern "C" int SpjStreamRun(SpjStream* st, int32_t predicate, const uint32_t** d_build,
+                            const uint32_t** d_probe, uint64_t* n_pairs) {
+  return guarded(st->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(st->join->rt->device_id));
+    SPJ_CHECK(d_build && d_probe && n_pairs, "null outputs");
+    *n_pairs = st->s->run(predicate, d_build, d_probe);
+  });
+}
+
+extern "C" int SpjStreamSetParams(SpjStream* st, int32_t block, uint32_t chunk_rows,
+                                  uint32_t leaf_size) {
+  return guarded(st->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(st->join->rt->device_id));
+    st->s->set_params(StreamParams{block, chunk_rows, leaf_size});
+  });
+}
+
+extern "C" int SpjStreamAutotune(SpjStream* st, int32_t predicate, const char* cache_path,
+                                 int32_t* block, uint32_t* chunk_rows, uint32_t* leaf_size) {
+  return guarded(st->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(st->join->rt->device_id));
+    StreamParams p = st->s->autotune(predicate, cache_path ? std::string(cache_path) : "");
+    if (block) *block = p.block;
+    if (chunk_rows) *chunk_rows = p.chunk_rows;
+    if (leaf_size) *leaf_size = p.leaf_size;
+  });
+}
+
+extern "C" int SpjStreamGetStats(SpjStream* st, double* ms_last, uint64_t* escalations,
+                                 uint64_t* launches) {
+  return guarded(st->last_error, [&] {
+    const StreamStats& s = st->s->stats();
+    if (ms_last) *ms_last = s.ms_last;
+    if (escalations) *escalations = s.escalations;
+    if (launches) *launches = s.launches_per_replay;
+  });
+}
+
+extern "C" void* SpjStreamCudaStream(SpjStream* st) { return (void*)st->s->stream(); }
 
 // =============================================================================
 // exported: SpjKnn

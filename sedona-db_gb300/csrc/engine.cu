@@ -64,6 +64,13 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
   built_ = true;
 }
 
+void JoinEngine::reindex(uint32_t leaf_size) {
+  SPJ_CHECK(built_, "reindex before the build side was finished");
+  cfg_.leaf_size = leaf_size;
+  build_lbvh(bg_.box.as<float4>(), bg_.n, leaf_size, bvh_, bs_);
+  SPJ_CUDA(cudaStreamSynchronize(bs_));
+}
+
 static inline float ev_ms(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0;
   cudaEventElapsedTime(&ms, a, b);

@@ -65,6 +65,8 @@ class JoinEngine {
   // (the caller has synchronized whatever stream wrote it).
   void build(const WkbDeviceColumn& col);
   bool built() const { return built_; }
+  // Rebuild the LBVH over the decoded build boxes with another leaf size.
+  void reindex(uint32_t leaf_size);
   const DeviceGeoms& build_geoms() const { return bg_; }
   const Lbvh& lbvh() const { return bvh_; }
 

@@ -17,6 +17,7 @@
 
 namespace spj {
 namespace pred {
+namespace {  // internal linkage: included by several translation units
 
 enum { kOut = 0, kIn = 1, kOn = 2 };
 
@@ -164,14 +165,61 @@ __device__ __forceinline__ void pip_seg_f64(double2 a, double2 b, double2 p, int
   }
 }
 
-// FP32 classification of one segment: returns kOut / kIn when a strict
-// comparison of round-to-nearest values proves tg's FP64 early exit, or -1.
+// Sign of the exact orientation (b - a) x (p - a) of three FP64 points known
+// through their round-to-nearest f32 copies a, b, p: +1 / -1 when the f32
+// evaluation clears twice a static bound E on its error, else 0.
+// E covers the coordinate rounding (|c - RN32(c)| <= 2^-24 |RN32(c)|, doubled,
+// plus 2^-150 absolute for the subnormal range), the rounding of the two
+// differences, the two products and the final difference.  A decided sign
+// therefore leaves |exact| >= E, some 2^28 times the FP64 rounding of tg's
+// own orientation / slope / intersection arithmetic on the same points, so
+// tg's FP64 decisions follow the exact sign.
+__device__ __forceinline__ int orient32(float2 a, float2 b, float2 p) {
+  const float dx = __fsub_rn(b.x, a.x), dy = __fsub_rn(b.y, a.y);
+  const float ex = __fsub_rn(p.x, a.x), ey = __fsub_rn(p.y, a.y);
+  const float t1 = __fmul_rn(dx, ey), t2 = __fmul_rn(dy, ex);
+  const float o = __fsub_rn(t1, t2);
+  const float u = 5.9604645e-08f;   // 2^-24
+  const float c2 = 1.1920929e-07f;  // 2^-23
+  const float tiny = 1.4012985e-45f;
+  const float Edx = __fadd_ru(__fmul_ru(c2, __fadd_ru(fabsf(b.x), fabsf(a.x))),
+                              __fadd_ru(__fmul_ru(u, fabsf(dx)), tiny));
+  const float Edy = __fadd_ru(__fmul_ru(c2, __fadd_ru(fabsf(b.y), fabsf(a.y))),
+                              __fadd_ru(__fmul_ru(u, fabsf(dy)), tiny));
+  const float Eex = __fadd_ru(__fmul_ru(c2, __fadd_ru(fabsf(p.x), fabsf(a.x))),
+                              __fadd_ru(__fmul_ru(u, fabsf(ex)), tiny));
+  const float Eey = __fadd_ru(__fmul_ru(c2, __fadd_ru(fabsf(p.y), fabsf(a.y))),
+                              __fadd_ru(__fmul_ru(u, fabsf(ey)), tiny));
+  const float E1 = __fadd_ru(__fadd_ru(__fmul_ru(fabsf(dx), Eey), __fmul_ru(fabsf(ey), Edx)),
+                             __fadd_ru(__fmul_ru(Edx, Eey), __fmul_ru(u, fabsf(t1))));
+  const float E2 = __fadd_ru(__fadd_ru(__fmul_ru(fabsf(dy), Eex), __fmul_ru(fabsf(ex), Edy)),
+                             __fadd_ru(__fmul_ru(Edy, Eex), __fmul_ru(u, fabsf(t2))));
+  const float E = __fmul_ru(__fadd_ru(__fadd_ru(E1, E2), __fadd_ru(__fmul_ru(u, fabsf(o)), tiny)),
+                            2.0000019f);  // x2 margin, x(1 + 2^-20) slack
+  if (o > E) return 1;
+  if (o < -E) return -1;
+  return 0;  // undecided (also for NaN / inf)
+}
+
+// FP32 classification of one segment: returns kOut / kIn when it provably
+// equals tg's FP64 ray-cast result, or -1.  Strict comparisons of
+// round-to-nearest values prove tg's early exits; a point strictly inside
+// the segment's y-range gets tg's slope-test answer, which for such a point
+// is the side of p relative to the upward segment (IN when p is left of it),
+// from orient32 when that sign is decided.
 __device__ __forceinline__ int pip_seg_f32(float2 a, float2 b, float2 p) {
   const float ymin = fmin0f(a.y, b.y), ymax = fmax0f(a.y, b.y);
   if (p.y < ymin || p.y > ymax) return kOut;
   const float xmin = fmin0f(a.x, b.x), xmax = fmax0f(a.x, b.x);
-  if (p.x < xmin && p.y > ymin && p.y < ymax) return kIn;
+  const bool inner_y = p.y > ymin && p.y < ymax;
+  if (p.x < xmin && inner_y) return kIn;
   if (p.x > xmax && ymin < ymax && xmin < xmax) return kOut;
+  if (inner_y) {
+    const bool up = a.y < b.y;
+    const int o = orient32(up ? a : b, up ? b : a, p);
+    if (o > 0) return kIn;
+    if (o < 0) return kOut;
+  }
   return -1;
 }
 
@@ -335,6 +383,18 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
     if (fmin0f(c.x, d.x) > qx1 || fmax0f(c.x, d.x) < qx0 || fmin0f(c.y, d.y) > qy1 ||
         fmax0f(c.y, d.y) < qy0)
       return;  // strictly separated rects: tg's first test fails
+    // Decided orientations: c, d strictly on one side of line ab (or a, b of
+    // line cd) means tg's parameter u (or t) = o1 / (o1 - o2) lies outside
+    // [0, 1] by far more than its FP64 rounding -> no intersection; strictly
+    // opposite sides on both lines means t, u are inside (0, 1) -> crossing.
+    const int o1 = orient32(a32, b32, c), o2 = orient32(a32, b32, d);
+    if (o1 != 0 && o1 == o2) return;
+    const int o3 = orient32(c, d, a32), o4 = orient32(c, d, b32);
+    if (o3 != 0 && o3 == o4) return;
+    if (o1 != 0 && o2 != 0 && o3 != 0 && o4 != 0) {
+      count++;
+      return;
+    }
     esc++;
     if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
   };
@@ -452,11 +512,20 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
       for (uint32_t k = e0; k < e1; k++) {
         const int i = Gr->band_edges[k];
         const float2 c = Gr->xy32[Vr + i], d = Gr->xy32[Vr + i + 1];
-        if (!(fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
-              fmin0f(c.y, d.y) > by1)) {
-          near = true;
-          break;
-        }
+        if (fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
+            fmin0f(c.y, d.y) > by1)
+          continue;  // bboxes strictly separated
+        // the smaller ring's box strictly on one side of the segment's line
+        // (all four corners, decided orientations): the segment misses the
+        // box, every segment test against it fails in tg, and its ray-cast
+        // decision for any vertex in the box is the exact side test
+        const int s0 = orient32(c, d, make_float2(bx0, by0));
+        if (s0 != 0 && orient32(c, d, make_float2(bx1, by0)) == s0 &&
+            orient32(c, d, make_float2(bx1, by1)) == s0 &&
+            orient32(c, d, make_float2(bx0, by1)) == s0)
+          continue;
+        near = true;
+        break;
       }
     }
     if (!near) return ring_pip<kFast>(*Gr, rr, Go->xy[Vo], Go->xy32[Vo], true, esc).hit;
@@ -486,5 +555,6 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
   return false;
 }
 
+}  // namespace
 }  // namespace pred
 }  // namespace spj

@@ -157,6 +157,9 @@ EXPORTS = [
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
     "SpjKnnStream", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
     "SpjIndexProbeNoAlloc",
+    "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
+    "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
+    "SpjStreamCudaStream",
 ]
 
 _lib = None
@@ -213,6 +216,22 @@ def lib() -> C.CDLL:
             L.SpjHostRegister.argtypes = [C.c_void_p, C.c_uint64]
             L.SpjHostUnregister.argtypes = [C.c_void_p]
             L.SpjVersion.restype = C.c_char_p
+            L.SpjStreamCreate.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+            L.SpjStreamRelease.argtypes = [C.c_void_p]
+            L.SpjStreamRelease.restype = None
+            L.SpjStreamLastError.argtypes = [C.c_void_p]
+            L.SpjStreamLastError.restype = C.c_char_p
+            L.SpjStreamSetBatches.argtypes = [C.c_void_p, C.POINTER(SpjDeviceWkb), C.c_int32]
+            L.SpjStreamRun.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
+                                       C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)]
+            L.SpjStreamSetParams.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32]
+            L.SpjStreamAutotune.argtypes = [C.c_void_p, C.c_int32, C.c_char_p,
+                                            C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
+                                            C.POINTER(C.c_uint32)]
+            L.SpjStreamGetStats.argtypes = [C.c_void_p, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+            L.SpjStreamCudaStream.argtypes = [C.c_void_p]
+            L.SpjStreamCudaStream.restype = C.c_void_p
             _lib = L
     return _lib
 
@@ -459,6 +478,56 @@ class SpatialJoin:
     def __del__(self):
         if getattr(self, "h", None):
             lib().SpjJoinRelease(self.h)
+            self.h = None
+
+
+class StreamProbe:
+    """Batched probe stream over device point batches (SpjStream*,
+    include/spj_gb300.h): one CUDA-graph replay per run."""
+
+    def __init__(self, join: "SpatialJoin"):
+        self.join = join  # must outlive the stream
+        self.h = C.c_void_p()
+        if lib().SpjStreamCreate(join.h, C.byref(self.h)) != 0:
+            raise GpuSpatialError(f"SpjStreamCreate: {lib().SpjJoinLastError(join.h).decode()}")
+
+    def _err(self):
+        return lib().SpjStreamLastError(self.h)
+
+    def set_batches(self, dcols):
+        arr = (SpjDeviceWkb * max(len(dcols), 1))(*dcols)
+        self._cols = arr
+        _check(lib().SpjStreamSetBatches(self.h, arr, len(dcols)), "set_batches", self._err)
+
+    def run(self, predicate: str = "contains"):
+        db, dp, n = C.c_void_p(), C.c_void_p(), C.c_uint64()
+        _check(lib().SpjStreamRun(self.h, PREDICATES[predicate], C.byref(db), C.byref(dp),
+                                  C.byref(n)), "run", self._err)
+        return db.value, dp.value, n.value
+
+    def set_params(self, block: int, chunk_rows: int, leaf_size: int):
+        _check(lib().SpjStreamSetParams(self.h, block, chunk_rows, leaf_size), "set_params",
+               self._err)
+
+    def autotune(self, predicate: str, cache_path: Optional[str] = None):
+        b, c, l = C.c_int32(), C.c_uint32(), C.c_uint32()
+        _check(lib().SpjStreamAutotune(self.h, PREDICATES[predicate],
+                                       cache_path.encode() if cache_path else None, C.byref(b),
+                                       C.byref(c), C.byref(l)), "autotune", self._err)
+        return b.value, c.value, l.value
+
+    def stats(self):
+        ms, esc, la = C.c_double(), C.c_uint64(), C.c_uint64()
+        _check(lib().SpjStreamGetStats(self.h, C.byref(ms), C.byref(esc), C.byref(la)), "stats",
+               self._err)
+        return {"ms_last": ms.value, "escalations": esc.value, "launches_per_replay": la.value}
+
+    def stream(self) -> int:
+        return lib().SpjStreamCudaStream(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().SpjStreamRelease(self.h)
             self.h = None
 
 

@@ -306,3 +306,83 @@ def test_empty_probe_and_build(capi):
     j2.build(wkb.column_from_values([wkb.wkb_point(0, 0)]))
     b, p = j2.probe(wkb.column_from_values([]), "intersects")
     assert len(b) == 0
+
+
+# ---------------------------------------------------------------------------
+# batched probe stream (one CUDA-graph replay over uneven record batches)
+
+def _device_batches(capi, col, sizes):
+    import torch
+    keep, dcols = [], []
+    start = 0
+    for n in sizes:
+        part = col.slice(start, start + n)
+        off = torch.from_numpy(np.ascontiguousarray(part.offsets)).cuda()
+        data = torch.from_numpy(np.ascontiguousarray(part.data)).cuda()
+        keep.append((off, data))
+        dcols.append(capi.SpjDeviceWkb(length=n, offsets=off.data_ptr(),
+                                       offsets_are_64bit=int(part.offsets.dtype == np.int64),
+                                       data=data.data_ptr(), data_length=len(part.data),
+                                       validity=None, validity_offset=0))
+        start += n
+    return dcols, keep
+
+
+class _DevArray:
+    """A raw device pointer exposed through __cuda_array_interface__."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def _device_pairs(db, dp, n):
+    import torch
+    if n == 0:
+        return np.zeros(0, np.uint32), np.zeros(0, np.uint32)
+    torch.cuda.synchronize()
+    b = torch.as_tensor(_DevArray(db, n), device="cuda").cpu().numpy().view(np.uint32)
+    p = torch.as_tensor(_DevArray(dp, n), device="cuda").cpu().numpy().view(np.uint32)
+    return b, p
+
+
+@pytest.mark.parametrize("params", [None, (64, 256, 2), (256, 4096, 8)])
+def test_stream_matches_oracle(capi, oracle_mod, params):
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload3(n_points=80000, n_zones=400)
+    j = capi.SpatialJoin()
+    j.build(inp.build)
+    rng = np.random.default_rng(9)
+    sizes, left = [], len(inp.probe)
+    while left:
+        s = int(min(left, np.floor(np.exp(rng.uniform(np.log(64), np.log(20000))))))
+        sizes.append(s)
+        left -= s
+    dcols, keep = _device_batches(capi, inp.probe, sizes)
+    st = capi.StreamProbe(j)
+    if params:
+        st.set_params(*params)
+    st.set_batches(dcols)
+    exp = oracle_pairs(oracle_mod, inp.build, inp.probe, "contains")
+    for _ in range(2):  # two replays of the same graph
+        db, dp, n = st.run("contains")
+        b, p = _device_pairs(db, dp, n)
+        assert np.all(np.diff(p.astype(np.int64)) >= 0)
+        assert pairs(b, p) == exp
+
+
+def test_stream_autotune_and_cache(capi, oracle_mod, tmp_path):
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload3(n_points=20000, n_zones=200)
+    j = capi.SpatialJoin()
+    j.build(inp.build)
+    dcols, keep = _device_batches(capi, inp.probe, [5000, 7000, 8000])
+    st = capi.StreamProbe(j)
+    st.set_batches(dcols)
+    cache = str(tmp_path / "tune.txt")
+    best = st.autotune("intersects", cache)
+    assert best[0] in (64, 128, 256) and best[2] in (2, 4, 8)
+    assert best == st.autotune("intersects", cache)  # served from the cache
+    db, dp, n = st.run("intersects")
+    b, p = _device_pairs(db, dp, n)
+    assert pairs(b, p) == oracle_pairs(oracle_mod, inp.build, inp.probe, "intersects")
