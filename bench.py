@@ -428,6 +428,121 @@ def run_stream(args, world, rank, local, pg):
     return out, inp
 
 
+def run_learned(args, world, rank, local, pg):
+    """Workload 5: 100M GMM build points, 10M range boxes + 10M exact-point
+    lookups (ST_Intersects).  Chosen form: the learned index (trained on the
+    GPU).  Plain form: the LBVH join with the FP64 refine on the same inputs,
+    which is also the judge of the pair set."""
+    import torch
+    from sedona_gpuspatial import capi, datagen
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    s = args.scale
+    build, boxes, lookups, _ = datagen.workload5(n_build=int(100_000_000 * s),
+                                                 n_boxes=int(10_000_000 * s),
+                                                 n_lookups=int(10_000_000 * s))
+    rt = capi.Runtime.get(local)
+    db_, kb = to_device(build)
+    dbox, kbox = to_device(boxes)
+    dlk, klk = to_device(lookups)
+    li = capi.LearnedIndex(rt, leaves=4096)
+    li.build_device(db_)
+    st_build = li.stats()
+
+    def step(obj, method):
+        n = 0
+        for d in (dbox, dlk):
+            _, _, m = getattr(obj, method)(d, "intersects")
+            n += m
+        return n
+
+    stream = torch.cuda.ExternalStream(li.stream())
+    for _ in range(args.warmup):
+        step(li, "query_device")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.__enter__()
+    before = li.stats()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    npairs = 0
+    for _ in range(args.steps):
+        npairs = step(li, "query_device")
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    sampler.__exit__()
+    after = li.stats()
+    ms = barrier_max(pg, e0.elapsed_time(e1) / args.steps, dev)
+    lookups_n = after["lookups"] - before["lookups"]
+    steps_per_lookup = (after["search_steps"] - before["search_steps"]) / max(1, lookups_n)
+
+    # ablation: the untrained model (line through each leaf's end keys)
+    li.set_trained(False)
+    st_untrained = li.stats()
+    step(li, "query_device")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b0 = li.stats()
+    n_untrained = step(li, "query_device")
+    torch.cuda.synchronize()
+    untrained_ms = (time.perf_counter() - t0) * 1e3
+    b1 = li.stats()
+    untrained_steps = (b1["search_steps"] - b0["search_steps"]) / max(1, b1["lookups"] - b0["lookups"])
+    li.set_trained(True)
+    assert n_untrained == npairs
+
+    # plain form / judge: the LBVH join, FP64 refine, same inputs
+    jp = capi.SpatialJoin(rt, refine_form=0)
+    jp.build_device(db_)
+    step(jp, "probe_device")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n_plain = step(jp, "probe_device")
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    assert n_plain == npairs, (n_plain, npairs)
+    n_rows = len(boxes) + len(lookups)
+    hbm_peak, peak_kind = load_peaks()
+    # algorithmic bytes per step: probe WKB + offsets once, per lookup the
+    # key / point reads (4 B key + 16 B point per scanned build point are
+    # not counted: re-reads), 8 B per pair out
+    alg = len(boxes.data) + len(lookups.data) + 4 * (n_rows + 2) + 8 * npairs
+    achieved = alg / (ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": aggregate_value(npairs, world, ms), "unit": "pairs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (f32 filter)", "data": "synthetic (seeded; SpatialBench data not available)",
+        "config": {"workload": "learned_index_100m_points_10m_boxes_10m_lookups_st_intersects",
+                   "build_rows": len(build), "probe_rows": n_rows, "scale": s,
+                   "pairs_per_step": npairs, "leaves": 4096,
+                   "l2": "probe columns > L2, no flush", "parallelism": f"replicas x{world}"},
+        "probe_rows_per_s": n_rows * world / (ms * 1e-3),
+        "learned_index": {"build_ms": st_build["ms_build"], "max_err": st_build["max_err"],
+                          "mean_err": st_build["mean_err"],
+                          "leaves_over_window": st_build["leaves_over_window"],
+                          "lbvh_fallbacks": after["lbvh_fallbacks"] - before["lbvh_fallbacks"],
+                          "window_misses": after["window_misses"] - before["window_misses"],
+                          "search_steps_per_lookup": steps_per_lookup,
+                          "untrained": {"ms_per_step": untrained_ms,
+                                        "max_err": st_untrained["max_err"],
+                                        "mean_err": st_untrained["mean_err"],
+                                        "search_steps_per_lookup": untrained_steps}},
+        "plain_f64_form": {"pairs_per_s": npairs / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                           "form": "LBVH join, FP64 refine (also the pair-set judge)",
+                           "speedup_chosen_vs_plain": plain_ms / ms},
+        "roofline": {"bound": "hbm", "kernel": "k_learned_query (both passes)",
+                     "achieved": achieved, "peak": hbm_peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg},
+        "clocks": sampler.summary(),
+    }
+    return out, None
+
+
 def cpu_baseline(inp, seconds_budget: float = 15.0):
     """The oracle (C restatement of the reference CPU join) on a bounded
     sample of the probe side with all host threads."""
@@ -505,6 +620,9 @@ def main():
     world, rank, local, pg = dist_setup()
     if args.workload == 3:
         out, inp = run_stream(args, world, rank, local, pg)
+    elif args.workload == 5:
+        out, inp = run_learned(args, world, rank, local, pg)
+        args.no_cpu_baseline = True
     else:
         out, inp = run_ours(args, world, rank, local, pg)
     if rank == 0:

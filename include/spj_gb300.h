@@ -123,8 +123,9 @@ int SpjJoinResetStats(SpjJoin* join);
 
 /* ------------------------------------------------------------------------ */
 /* Batched probe stream: many uneven record batches of point WKB probed in
- * one CUDA-graph replay (a persistent work-queue kernel counts, a scan
- * places, the same kernel emits).  Serves SpatialJoinStream's per-batch
+ * one CUDA-graph replay (a persistent work-queue kernel decodes every batch,
+ * then filter, refine and compaction run once over the whole stream, with no
+ * host round trip in between).  Serves SpatialJoinStream's per-batch
  * query_batch loop (rust/sedona-spatial-join/src/stream.rs:1166-1200) without
  * a host round trip per batch.  The SpjJoin it is created from must outlive
  * it.  Relation predicates only; batch rows must be points. */
@@ -142,7 +143,7 @@ int SpjStreamSetBatches(SpjStream* stream, const struct SpjDeviceWkb* batches,
  * valid until the next run) grouped by probe row in ascending order. */
 int SpjStreamRun(SpjStream* stream, int32_t predicate, const uint32_t** d_build,
                  const uint32_t** d_probe, uint64_t* n_pairs);
-/* block: 64, 128 or 256 threads; chunk_rows: rows per work item; leaf_size:
+/* block: 128 or 256 threads (decode kernel); chunk_rows: rows per work item; leaf_size:
  * LBVH leaf size (rebuilds the index). */
 int SpjStreamSetParams(SpjStream* stream, int32_t block, uint32_t chunk_rows, uint32_t leaf_size);
 /* Times block x chunk_rows x leaf_size candidates on the current batches,
@@ -155,6 +156,56 @@ int SpjStreamAutotune(SpjStream* stream, int32_t predicate, const char* cache_pa
 int SpjStreamGetStats(SpjStream* stream, double* ms_last, uint64_t* escalations,
                       uint64_t* launches_per_replay);
 void* SpjStreamCudaStream(SpjStream* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Learned point index: the build points sorted by a 32-bit Hilbert key on a
+ * 2^16 x 2^16 grid over their extent, a two-stage piecewise-linear model of
+ * key -> rank (a root line picks one of `leaves` per-leaf lines) trained on
+ * the GPU, lookups searched within each leaf's measured error and verified
+ * exactly; the LBVH over the same points is the fallback (leaves over the
+ * window) and the judge.  No counterpart in the reference (which has no
+ * learned index); it serves point build sides of the join (probe points:
+ * exact-point lookups; probe polygons such as range boxes: ST_Intersects /
+ * ST_Within / ST_CoveredBy(build point, probe polygon)). */
+
+typedef struct SpjLearned SpjLearned;
+
+struct SpjLearnedConfig {
+  const struct GpuSpatialRuntime* runtime;
+  uint32_t leaves; /* 0 = 4096 */
+  uint32_t window; /* max per-leaf error served by the model, 0 = 4096 */
+};
+
+struct SpjLearnedStats {
+  uint64_t points, lookups, window_misses, lbvh_fallbacks, search_steps;
+  uint32_t leaves, max_err, leaves_over_window, trained;
+  double root_a, root_b, mean_err, grad_norm_after, ms_build;
+};
+
+int SpjLearnedCreate(const struct SpjLearnedConfig* config, SpjLearned** out);
+void SpjLearnedRelease(SpjLearned* li);
+const char* SpjLearnedLastError(SpjLearned* li);
+/* Build from a device WKB column of points (non-point rows are skipped). */
+int SpjLearnedBuildDevice(SpjLearned* li, const struct SpjDeviceWkb* points);
+/* trained = 0 replaces the trained per-leaf lines with the untrained start
+ * (the line through each leaf's first and last key), 1 retrains. */
+int SpjLearnedSetTrained(SpjLearned* li, int32_t trained);
+/* Probe with a device WKB column; pairs (device arrays owned by the index,
+ * valid until its next query) grouped by probe row; probe ids offset by
+ * probe_base. */
+int SpjLearnedQueryDevice(SpjLearned* li, const struct SpjDeviceWkb* probe, int32_t predicate,
+                          uint32_t probe_base, const uint32_t** d_build,
+                          const uint32_t** d_probe, uint64_t* n_pairs);
+/* Per-leaf squared loss and gradient at host parameters a[L], b[L]
+ * (evaluated by the training kernels; for checks against a CPU oracle). */
+int SpjLearnedLossAndGrad(SpjLearned* li, const double* a, const double* b, double* loss,
+                          double* grad_a, double* grad_b);
+/* Host copies of the sorted keys (points entries), leaf starts (L+1), leaf
+ * key origins, per-leaf lines and errors (L each). */
+int SpjLearnedExport(SpjLearned* li, uint32_t* keys, uint32_t* leaf_start, uint32_t* leaf_kc,
+                     double* a, double* b, uint32_t* err);
+int SpjLearnedGetStats(SpjLearned* li, struct SpjLearnedStats* out);
+void* SpjLearnedStream(SpjLearned* li);
 
 /* ------------------------------------------------------------------------ */
 /* KNN join over point columns                                              */

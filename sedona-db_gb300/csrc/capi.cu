@@ -19,6 +19,7 @@
 #include "../../include/spj_gb300.h"
 #include "engine.cuh"
 #include "knn.cuh"
+#include "learned.cuh"
 #include "stream.cuh"
 #include "prims.cuh"
 
@@ -830,6 +831,158 @@ extern "C" int SpjStreamGetStats(SpjStream* st, double* ms_last, uint64_t* escal
 }
 
 extern "C" void* SpjStreamCudaStream(SpjStream* st) { return (void*)st->s->stream(); }
+
+// =============================================================================
+// exported: SpjLearned
+
+struct SpjLearned {
+  RuntimeData* rt = nullptr;
+  uint32_t leaves = 4096, window = 4096;
+  bool trained = true;
+  double ms_build = 0;
+  std::unique_ptr<JoinEngine> engine;  // decodes the build points, owns the LBVH
+  std::unique_ptr<Workspace> ws;
+  std::unique_ptr<LearnedIndex> index;
+  DevBuf out_b, out_p;
+  std::string last_error;
+  ~SpjLearned() {
+    if (ws) cudaStreamSynchronize(ws->stream);
+    out_b.release();
+    out_p.release();
+    index.reset();
+  }
+};
+
+extern "C" int SpjLearnedCreate(const SpjLearnedConfig* config, SpjLearned** out) {
+  try {
+    SPJ_CHECK(config && out, "null config or output");
+    RuntimeData* rt = runtime_of(config->runtime);
+    SPJ_CUDA(cudaSetDevice(rt->device_id));
+    auto li = std::make_unique<SpjLearned>();
+    li->rt = rt;
+    if (config->leaves) li->leaves = config->leaves;
+    if (config->window) li->window = config->window;
+    SPJ_CHECK(li->leaves <= 65535, "leaves must be at most 65535");
+    li->engine = std::make_unique<JoinEngine>(rt->device_id, EngineConfig());
+    li->ws = std::make_unique<Workspace>();
+    *out = li.release();
+    return 0;
+  } catch (const std::exception& e) {
+    fprintf(stderr, "SpjLearnedCreate: %s\n", e.what());
+    return EINVAL;
+  }
+}
+
+extern "C" void SpjLearnedRelease(SpjLearned* li) {
+  if (!li) return;
+  cudaSetDevice(li->rt->device_id);
+  delete li;
+}
+
+extern "C" const char* SpjLearnedLastError(SpjLearned* li) { return li->last_error.c_str(); }
+
+extern "C" int SpjLearnedBuildDevice(SpjLearned* li, const SpjDeviceWkb* points) {
+  return guarded(li->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(li->rt->device_id));
+    SPJ_CUDA(cudaDeviceSynchronize());  // the caller's column is complete
+    cudaEvent_t e0, e1;
+    SPJ_CUDA(cudaEventCreate(&e0));
+    SPJ_CUDA(cudaEventCreate(&e1));
+    SPJ_CUDA(cudaEventRecord(e0, li->ws->stream));
+    li->engine->build(device_column(points));
+    li->index = std::make_unique<LearnedIndex>(li->leaves, li->window);
+    li->index->build(li->engine->build_geoms(), li->engine->lbvh(), li->ws->stream);
+    SPJ_CUDA(cudaEventRecord(e1, li->ws->stream));
+    SPJ_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    li->ms_build = ms;
+    li->trained = true;
+  });
+}
+
+extern "C" int SpjLearnedSetTrained(SpjLearned* li, int32_t trained) {
+  return guarded(li->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(li->rt->device_id));
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    li->index->train(trained != 0, li->ws->stream);
+    li->trained = trained != 0;
+  });
+}
+
+extern "C" int SpjLearnedQueryDevice(SpjLearned* li, const SpjDeviceWkb* probe, int32_t predicate,
+                                     uint32_t probe_base, const uint32_t** d_build,
+                                     const uint32_t** d_probe, uint64_t* n_pairs) {
+  return guarded(li->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(li->rt->device_id));
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    SPJ_CHECK(d_build && d_probe && n_pairs, "null outputs");
+    SPJ_CHECK(predicate >= 0 && predicate <= 7, "relation predicates only");
+    Workspace& ws = *li->ws;
+    decode_wkb(device_column(probe), ws.probe, ws.dsc, ws.last_probe_points, ws.stream);
+    ws.last_probe_points = ws.probe.all_points;
+    *n_pairs = li->index->query(ws.probe.view(), probe_base, predicate, li->out_b, li->out_p,
+                                ws.stream);
+    *d_build = li->out_b.as<uint32_t>();
+    *d_probe = li->out_p.as<uint32_t>();
+  });
+}
+
+extern "C" int SpjLearnedLossAndGrad(SpjLearned* li, const double* a, const double* b,
+                                     double* loss, double* grad_a, double* grad_b) {
+  return guarded(li->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(li->rt->device_id));
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    std::vector<double> va(a, a + li->leaves), vb(b, b + li->leaves), l, ga, gb;
+    li->index->loss_and_grad(va, vb, l, ga, gb, li->ws->stream);
+    std::copy(l.begin(), l.end(), loss);
+    std::copy(ga.begin(), ga.end(), grad_a);
+    std::copy(gb.begin(), gb.end(), grad_b);
+  });
+}
+
+extern "C" int SpjLearnedExport(SpjLearned* li, uint32_t* keys, uint32_t* leaf_start,
+                                uint32_t* leaf_kc, double* a, double* b, uint32_t* err) {
+  return guarded(li->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(li->rt->device_id));
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    std::vector<uint32_t> k, s, kc, e;
+    std::vector<double> va, vb;
+    li->index->export_model(k, s, kc, va, vb, e, li->ws->stream);
+    if (keys) std::copy(k.begin(), k.end(), keys);
+    if (leaf_start) std::copy(s.begin(), s.end(), leaf_start);
+    if (leaf_kc) std::copy(kc.begin(), kc.end(), leaf_kc);
+    if (a) std::copy(va.begin(), va.end(), a);
+    if (b) std::copy(vb.begin(), vb.end(), b);
+    if (err) std::copy(e.begin(), e.end(), err);
+  });
+}
+
+extern "C" int SpjLearnedGetStats(SpjLearned* li, SpjLearnedStats* out) {
+  return guarded(li->last_error, [&] {
+    SPJ_CHECK(out != nullptr, "null stats");
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    const LearnedStats& s = li->index->stats();
+    out->points = s.points;
+    out->lookups = s.lookups;
+    out->window_misses = s.window_misses;
+    out->lbvh_fallbacks = s.lbvh_fallbacks;
+    out->search_steps = s.search_steps;
+    out->leaves = s.leaves;
+    out->max_err = s.max_err;
+    out->leaves_over_window = s.leaves_over_window;
+    out->trained = li->trained ? 1 : 0;
+    out->root_a = s.root_a;
+    out->root_b = s.root_b;
+    out->mean_err = s.mean_err;
+    out->grad_norm_after = s.grad_norm_after;
+    out->ms_build = li->ms_build;
+  });
+}
+
+extern "C" void* SpjLearnedStream(SpjLearned* li) { return (void*)li->ws->stream; }
 
 // =============================================================================
 // exported: SpjKnn

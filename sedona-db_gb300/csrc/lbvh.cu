@@ -183,7 +183,8 @@ template <bool kScatter>
 __global__ void __launch_bounds__(kTravThreads)
     k_probe(LbvhView t, const float4* __restrict__ probe_box, uint32_t nprobe,
             uint32_t* __restrict__ counts, const uint64_t* __restrict__ offs, uint32_t probe_base,
-            uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe) {
+            uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
+            uint64_t cap = ~0ull) {
   // per-thread stack in shared memory, [depth][thread] so a warp's pushes hit
   // 32 distinct banks
   __shared__ int stack[kStack * kTravThreads];
@@ -203,8 +204,10 @@ __global__ void __launch_bounds__(kTravThreads)
           for (uint32_t k = b0; k < b1; k++) {
             if (overlap(t.sorted_box[k], q)) {
               if (kScatter) {
-                out_build[pos] = t.sorted_id[k];
-                out_probe[pos] = (uint32_t)pi + probe_base;
+                if (pos < cap) {  // writes bounded by the output capacity
+                  out_build[pos] = t.sorted_id[k];
+                  out_probe[pos] = (uint32_t)pi + probe_base;
+                }
                 pos++;
               } else {
                 cnt++;
@@ -350,11 +353,11 @@ void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprob
 
 void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                         const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
-                        uint32_t* out_probe, cudaStream_t s) {
+                        uint32_t* out_probe, cudaStream_t s, uint64_t capacity) {
   if (nprobe == 0) return;
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr, offs, probe_base,
-                                           out_build, out_probe);
+                                           out_build, out_probe, capacity);
   SPJ_CUDA(cudaGetLastError());
 }
 

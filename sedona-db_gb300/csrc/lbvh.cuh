@@ -70,7 +70,7 @@ void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprob
                       uint32_t* counts, cudaStream_t s);
 void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                         const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
-                        uint32_t* out_probe, cudaStream_t s);
+                        uint32_t* out_probe, cudaStream_t s, uint64_t capacity = ~0ull);
 
 // Expand point/box probes by a distance (f64), then round outward to f32
 // (rust/sedona-spatial-join/src/operand_evaluator.rs:605-607).

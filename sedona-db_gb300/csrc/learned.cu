@@ -1,0 +1,801 @@
+// learned.cu — learned point index (see learned.cuh): Hilbert keys, device
+// radix sort, GPU training of the two-stage piecewise-linear model, and the
+// lookup / range kernels with LBVH fallback.
+#include <cmath>
+
+#include "learned.cuh"
+#include "predicates.cuh"
+#include "prims.cuh"
+#include "refine.cuh"
+
+namespace spj {
+
+struct LearnedView {
+  uint32_t n, L, window;
+  const uint32_t* keys;
+  const uint32_t* ids;
+  const double2* xy;
+  const float2* xy32;
+  const uint32_t* start;  // L + 1
+  const double* a;
+  const double* b;
+  const uint32_t* kc;
+  const uint32_t* err;
+  double ra, rb;
+  uint32_t k0;
+  float x0, y0, sx, sy;
+};
+
+namespace {
+
+using namespace pred;
+
+constexpr int kLeafThreads = 256;
+constexpr uint32_t kMaxCells = 256;
+
+// Hilbert index of cell (x, y) on a 2^16 x 2^16 grid (the classic
+// rotate-and-reflect walk from the top quadrant level down).
+__device__ __forceinline__ uint32_t hilbert16(uint32_t x, uint32_t y) {
+  const uint32_t n = 1u << 16;
+  uint32_t d = 0;
+  for (uint32_t s = n >> 1; s > 0; s >>= 1) {
+    const uint32_t rx = (x & s) ? 1u : 0u, ry = (y & s) ? 1u : 0u;
+    d += s * s * ((3u * rx) ^ ry);
+    if (ry == 0) {
+      if (rx == 1) {
+        x = n - 1 - x;
+        y = n - 1 - y;
+      }
+      const uint32_t t = x;
+      x = y;
+      y = t;
+    }
+  }
+  return d;
+}
+
+// grid cell of an RN32 coordinate: monotone, so every point inside a box
+// falls in the box's cell range
+__device__ __forceinline__ uint32_t cell_of(float v, float v0, float s) {
+  const float t = __fmul_rn(__fsub_rn(v, v0), s);
+  if (!(t >= 0.0f)) return 0;
+  if (t >= 65535.0f) return 65535;
+  return (uint32_t)t;
+}
+
+__device__ __forceinline__ uint32_t key_of(const LearnedView& v, float2 p) {
+  return hilbert16(cell_of(p.x, v.x0, v.sx), cell_of(p.y, v.y0, v.sy));
+}
+
+__device__ __forceinline__ uint32_t root_leaf(const LearnedView& v, uint32_t q) {
+  const double t = (v.ra * ((double)q - (double)v.k0) + v.rb) * ((double)v.L / (double)v.n);
+  if (!(t >= 0.0)) return 0;
+  if (t >= (double)(v.L - 1)) return v.L - 1;
+  return (uint32_t)t;
+}
+
+__device__ __forceinline__ uint32_t bsearch_first_ge(const uint32_t* keys, uint32_t lo,
+                                                     uint32_t hi, uint32_t q, uint32_t& steps) {
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    steps++;
+    if (keys[mid] < q) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// lower_bound(q) over the sorted keys; exact (verified); `bad` is set when
+// the leaf's error exceeds the window (the caller takes the LBVH instead)
+__device__ __forceinline__ uint32_t learned_lower_bound(const LearnedView& v, uint32_t q,
+                                                        uint32_t& steps, uint32_t& misses,
+                                                        bool& bad) {
+  const uint32_t l = root_leaf(v, q);
+  const uint32_t e = v.err[l];
+  bad = e > v.window;
+  if (bad) return 0;
+  const double pred = __fma_rn(v.a[l], (double)q - (double)v.kc[l], v.b[l]);
+  double lo_d = floor(pred) - (double)e - 1.0, hi_d = ceil(pred) + (double)e + 2.0;
+  lo_d = fmax(lo_d, 0.0);
+  hi_d = fmin(hi_d, (double)v.n);
+  uint32_t lo = (uint32_t)lo_d, hi = (uint32_t)fmax(hi_d, lo_d);
+  uint32_t p = bsearch_first_ge(v.keys, lo, hi, q, steps);
+  const bool ok_lo = p == 0 || v.keys[p - 1] < q;
+  const bool ok_hi = p == v.n || v.keys[p] >= q;
+  if (!(ok_lo && ok_hi)) {
+    misses++;
+    p = bsearch_first_ge(v.keys, 0, v.n, q, steps);
+  }
+  return p;
+}
+
+// --- build ------------------------------------------------------------------
+
+__global__ void k_point_flags(const uint8_t* __restrict__ kind, uint32_t n, uint8_t* flag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    flag[i] = kind[i] == kPoint ? 1 : 0;
+}
+
+__global__ void k_compact(const uint8_t* __restrict__ flag, const uint64_t* __restrict__ pos,
+                          uint32_t n, uint32_t* __restrict__ ids) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (flag[i]) ids[pos[i]] = i;
+}
+
+__device__ __forceinline__ uint32_t f2o(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_extent(const float4* __restrict__ box, const uint32_t* __restrict__ ids,
+                         uint32_t m, uint32_t* ext) {
+  float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const float4 b = box[ids[i]];
+    mnx = fminf(mnx, b.x);
+    mny = fminf(mny, b.y);
+    mxx = fmaxf(mxx, b.x);
+    mxy = fmaxf(mxy, b.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&ext[0], f2o(mnx));
+    atomicMin(&ext[1], f2o(mny));
+    atomicMax(&ext[2], f2o(mxx));
+    atomicMax(&ext[3], f2o(mxy));
+  }
+}
+
+__global__ void k_keys(LearnedView v, const float4* __restrict__ box,
+                       const uint32_t* __restrict__ ids, uint32_t m, uint32_t* __restrict__ keys) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const float4 b = box[ids[i]];
+    keys[i] = key_of(v, make_float2(b.x, b.y));
+  }
+}
+
+__global__ void k_gather(const double2* __restrict__ pt, const float4* __restrict__ box,
+                         const uint32_t* __restrict__ ids, uint32_t m, double2* __restrict__ xy,
+                         float2* __restrict__ xy32) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const uint32_t id = ids[i];
+    xy[i] = pt[id];
+    const float4 b = box[id];
+    xy32[i] = make_float2(b.x, b.y);
+  }
+}
+
+// per-block partial sums of (x, x^2, r, x r) with x = key - k0 (FP64)
+__global__ void k_root_partials(const uint32_t* __restrict__ keys, uint32_t n, uint32_t k0,
+                                double4* __restrict__ part) {
+  __shared__ double sm[4][32];
+  double s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = (double)(keys[i] - k0), r = (double)i;
+    s1 += x;
+    s2 = __fma_rn(x, x, s2);
+    s3 += r;
+    s4 = __fma_rn(x, r, s4);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+    s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    sm[0][w] = s1;
+    sm[1][w] = s2;
+    sm[2][w] = s3;
+    sm[3][w] = s4;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[4] = {0, 0, 0, 0};
+    for (int j = 0; j < (int)(blockDim.x >> 5); j++)
+      for (int c = 0; c < 4; c++) t[c] += sm[c][j];
+    part[blockIdx.x] = make_double4(t[0], t[1], t[2], t[3]);
+  }
+}
+
+__global__ void k_leaf_ids(LearnedView v, uint16_t* __restrict__ leaf) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x)
+    leaf[i] = (uint16_t)root_leaf(v, v.keys[i]);
+}
+
+__global__ void k_leaf_bounds(const uint16_t* __restrict__ leaf, uint32_t n, uint32_t L,
+                              uint32_t* __restrict__ start) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int li = leaf[i];
+    const int lp = i ? (int)leaf[i - 1] : -1;
+    for (int l = lp + 1; l <= li; l++) start[l] = i;
+    if (i == n - 1)
+      for (uint32_t l = (uint32_t)li + 1; l <= L; l++) start[l] = n;
+  }
+}
+
+// block reduction of 6 doubles (blockDim == kLeafThreads)
+__device__ __forceinline__ void block_sum6(double (&v)[6], double (*sm)[kLeafThreads / 32]) {
+  for (int o = 16; o > 0; o >>= 1)
+    for (int c = 0; c < 6; c++) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int c = 0; c < 6; c++) sm[c][w] = v[c];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < 6; c++) {
+      double t = 0;
+      for (int j = 0; j < kLeafThreads / 32; j++) t += sm[c][j];
+      v[c] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Untrained start: the line through the leaf's first and last (key, rank).
+__global__ void k_leaf_init(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
+                            uint32_t L, double* a, double* b, uint32_t* kc) {
+  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+    const uint32_t s = start[l], e = start[l + 1];
+    if (s >= e) {
+      a[l] = 0;
+      b[l] = (double)s;
+      kc[l] = s ? keys[s - 1] : 0;
+      continue;
+    }
+    kc[l] = keys[s];
+    const double dx = (double)(keys[e - 1] - keys[s]);
+    a[l] = dx > 0 ? (double)(e - 1 - s) / dx : 0.0;
+    b[l] = (double)s;
+  }
+}
+
+// Forward + backward over one leaf per CTA: residual e = a x + b - r,
+// loss = sum e^2, grad = (sum 2 e x, sum 2 e), Hessian = 2 (sum x^2, sum x, n).
+__global__ void __launch_bounds__(kLeafThreads)
+    k_leaf_fwd_bwd(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
+                   const uint32_t* __restrict__ kc, const double* __restrict__ a,
+                   const double* __restrict__ b, double* __restrict__ out /* L x 6 */) {
+  __shared__ double sm[6][kLeafThreads / 32];
+  const uint32_t l = blockIdx.x;
+  const uint32_t s = start[l], e = start[l + 1];
+  const double al = a[l], bl = b[l];
+  const uint32_t k = kc[l];
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (uint32_t i = s + threadIdx.x; i < e; i += kLeafThreads) {
+    const double x = (double)(keys[i] - k), r = (double)i;
+    const double res = __fma_rn(al, x, bl) - r;  // forward
+    v[0] = __fma_rn(res, res, v[0]);            // loss
+    v[1] = __fma_rn(2.0 * res, x, v[1]);        // d/da
+    v[2] += 2.0 * res;                          // d/db
+    v[3] = __fma_rn(2.0 * x, x, v[3]);          // H_aa
+    v[4] += 2.0 * x;                            // H_ab
+    v[5] += 2.0;                                // H_bb
+  }
+  block_sum6(v, sm);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 6; c++) out[(size_t)l * 6 + c] = v[c];
+}
+
+// One Newton step per leaf: (a, b) -= H^-1 g (exact for the quadratic loss).
+__global__ void k_leaf_newton(const double* __restrict__ fb, uint32_t L, double* a, double* b) {
+  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+    const double* f = fb + (size_t)l * 6;
+    const double ga = f[1], gb = f[2], haa = f[3], hab = f[4], hbb = f[5];
+    if (hbb <= 0) continue;  // empty leaf
+    const double det = haa * hbb - hab * hab;
+    if (!(fabs(det) > 1e-12 * fabs(haa * hbb))) {
+      b[l] -= gb / hbb;  // single distinct key: constant model
+      continue;
+    }
+    a[l] -= (hbb * ga - hab * gb) / det;
+    b[l] -= (haa * gb - hab * ga) / det;
+  }
+}
+
+__global__ void __launch_bounds__(kLeafThreads)
+    k_leaf_err(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
+               const uint32_t* __restrict__ kc, const double* __restrict__ a,
+               const double* __restrict__ b, uint32_t* __restrict__ err) {
+  __shared__ double sm[kLeafThreads / 32];
+  const uint32_t l = blockIdx.x;
+  const uint32_t s = start[l], e = start[l + 1];
+  double m = 0;
+  for (uint32_t i = s + threadIdx.x; i < e; i += kLeafThreads) {
+    const double pred = __fma_rn(a[l], (double)(keys[i] - kc[l]), b[l]);
+    m = fmax(m, fabs(pred - (double)i));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 1; j < kLeafThreads / 32; j++) m = fmax(m, sm[j]);
+    m = fmax(m, sm[0]);
+    err[l] = m > 4.0e9 ? 0xFFFFFFFFu : (uint32_t)ceil(m);
+  }
+}
+
+// --- queries --------------------------------------------------------------
+
+__device__ __forceinline__ bool in_box(float2 p, float4 b) {
+  return !(p.x < b.x || p.x > b.z || p.y < b.y || p.y > b.w);
+}
+
+// pred(build point, probe polygon row) for range rows
+__device__ __forceinline__ bool range_pred(const GeomsView& P, uint32_t pr, double2 pt,
+                                           float2 pt32, bool aoe, uint32_t& esc) {
+  for (uint32_t q = P.row_part[pr]; q < P.row_part[pr + 1]; q++)
+    if (poly_contains_point<true>(P, q, pt, pt32, aoe, esc)) return true;
+  return false;
+}
+
+template <int kPass>
+__global__ void __launch_bounds__(128)
+    k_learned_query(LearnedView v, LbvhView t, GeomsView B, GeomsView P, uint32_t probe_base,
+                    int predicate, uint32_t* __restrict__ counts,
+                    const uint64_t* __restrict__ offs, uint32_t* __restrict__ ob,
+                    uint32_t* __restrict__ op, unsigned long long* __restrict__ ctr,
+                    DeviceStatus* st) {
+  __shared__ int stack[64 * 128];
+  uint32_t steps = 0, misses = 0, fallbacks = 0, lookups = 0, esc = 0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t trips = (P.n + stride - 1) / stride;
+  for (uint32_t tr = 0; tr < trips; tr++) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + tr * stride;
+    if (i >= P.n) continue;
+    const uint8_t kind = P.kind[i];
+    uint32_t cnt = 0;
+    uint64_t pos = kPass ? offs[i] : 0;
+    auto emit = [&](uint32_t build_row) {
+      if (kPass) {
+        ob[pos] = build_row;
+        op[pos] = i + probe_base;
+        pos++;
+      } else {
+        cnt++;
+      }
+    };
+    const bool is_point = kind == kPoint;
+    const bool is_poly = kind == kPolygon || kind == kMultiPolygon;
+    bool aoe = true;
+    bool ok = true;
+    if (is_point) {
+      // point-point: every predicate is equality except touches (always
+      // false, tg.c:1102-1106); disjoint is not a join predicate here
+      if (predicate == kTouches) ok = false;
+      if (predicate == kDisjoint) {
+        ok = false;
+        status_fail(st, kUnsupported, i);
+      }
+    } else if (is_poly) {
+      // pred(build point, probe polygon): within -> polygon contains point,
+      // intersects / coveredby -> polygon covers point; contains / equals
+      // are always false for a point (tg.c:1157-1162); the rest unsupported
+      if (predicate == kWithin) {
+        aoe = false;
+      } else if (predicate == kContains || predicate == kEquals) {
+        ok = false;
+      } else if (predicate != kIntersects && predicate != kCoveredBy) {
+        ok = false;
+        status_fail(st, kUnsupported, i);
+      }
+    }
+    if (!ok) {
+      if (!kPass) counts[i] = 0;
+      continue;
+    }
+    if (is_point) {
+      const double2 p = P.pt[i];
+      const float4 pb = P.box[i];
+      const float2 p32 = make_float2(pb.x, pb.y);
+      const uint32_t q = key_of(v, p32);
+      bool bad = false;
+      lookups++;
+      uint32_t j = learned_lower_bound(v, q, steps, misses, bad);
+      if (!bad) {
+        for (; j < v.n && v.keys[j] == q; j++)
+          if (pteq(v.xy[j], p)) emit(v.ids[j]);
+      } else {
+        fallbacks++;
+        // LBVH: build rows whose RN32 point equals the probe's RN32 point
+        int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
+        while (t.nprims > 0) {
+          if (node < 0) {
+            const uint32_t c = (uint32_t)(~node), b0 = c * t.leaf_size;
+            const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+            for (uint32_t k = b0; k < b1; k++)
+              if (in_box(make_float2(t.sorted_box[k].x, t.sorted_box[k].y), pb)) {
+                const uint32_t id = t.sorted_id[k];
+                if (pteq(B.pt[id], p)) emit(id);
+              }
+          } else {
+            const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+            const int2 ch = t.node_child[node];
+            const bool hl = !(lb.x > pb.z || lb.z < pb.x || lb.y > pb.w || lb.w < pb.y);
+            const bool hr = !(rb.x > pb.z || rb.z < pb.x || rb.y > pb.w || rb.w < pb.y);
+            if (hl && hr) {
+              if (sp < 64) stack[sp * 128 + threadIdx.x] = ch.y;
+              sp++;
+              node = ch.x;
+              continue;
+            }
+            if (hl || hr) {
+              node = hl ? ch.x : ch.y;
+              continue;
+            }
+          }
+          if (sp == 0) break;
+          sp--;
+          node = sp < 64 ? stack[sp * 128 + threadIdx.x] : 0;
+        }
+      }
+    } else if (is_poly) {
+      const float4 bx = P.box[i];  // outward f32 box of the probe polygon
+      const uint32_t cx0 = cell_of(bx.x, v.x0, v.sx), cx1 = cell_of(bx.z, v.x0, v.sx);
+      const uint32_t cy0 = cell_of(bx.y, v.y0, v.sy), cy1 = cell_of(bx.w, v.y0, v.sy);
+      const uint64_t ncell = (uint64_t)(cx1 - cx0 + 1) * (cy1 - cy0 + 1);
+      bool use_tree = ncell > kMaxCells;
+      if (!use_tree) {
+        // a leaf over the window anywhere in the box sends the row to the LBVH
+        for (uint32_t cy = cy0; cy <= cy1 && !use_tree; cy++)
+          for (uint32_t cx = cx0; cx <= cx1 && !use_tree; cx++)
+            use_tree = v.err[root_leaf(v, hilbert16(cx, cy))] > v.window;
+      }
+      if (!use_tree) {
+        for (uint32_t cy = cy0; cy <= cy1; cy++) {
+          for (uint32_t cx = cx0; cx <= cx1; cx++) {
+            const uint32_t q = hilbert16(cx, cy);
+            bool bad = false;
+            lookups++;
+            uint32_t j = learned_lower_bound(v, q, steps, misses, bad);
+            for (; j < v.n && v.keys[j] == q; j++) {
+              const float2 p32 = v.xy32[j];
+              if (!in_box(p32, bx)) continue;
+              if (range_pred(P, i, v.xy[j], p32, aoe, esc)) emit(v.ids[j]);
+            }
+          }
+        }
+      } else {
+        fallbacks++;
+        int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
+        while (t.nprims > 0) {
+          if (node < 0) {
+            const uint32_t c = (uint32_t)(~node), b0 = c * t.leaf_size;
+            const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+            for (uint32_t k = b0; k < b1; k++) {
+              const float4 sb = t.sorted_box[k];
+              if (!in_box(make_float2(sb.x, sb.y), bx)) continue;
+              const uint32_t id = t.sorted_id[k];
+              if (range_pred(P, i, B.pt[id], make_float2(sb.x, sb.y), aoe, esc)) emit(id);
+            }
+          } else {
+            const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+            const int2 ch = t.node_child[node];
+            const bool hl = !(lb.x > bx.z || lb.z < bx.x || lb.y > bx.w || lb.w < bx.y);
+            const bool hr = !(rb.x > bx.z || rb.z < bx.x || rb.y > bx.w || rb.w < bx.y);
+            if (hl && hr) {
+              if (sp < 64) stack[sp * 128 + threadIdx.x] = ch.y;
+              sp++;
+              node = ch.x;
+              continue;
+            }
+            if (hl || hr) {
+              node = hl ? ch.x : ch.y;
+              continue;
+            }
+          }
+          if (sp == 0) break;
+          sp--;
+          node = sp < 64 ? stack[sp * 128 + threadIdx.x] : 0;
+        }
+      }
+    }
+    if (!kPass) counts[i] = cnt;
+  }
+  if (kPass == 0) {
+    for (int o = 16; o > 0; o >>= 1) {
+      steps += __shfl_xor_sync(0xffffffffu, steps, o);
+      misses += __shfl_xor_sync(0xffffffffu, misses, o);
+      fallbacks += __shfl_xor_sync(0xffffffffu, fallbacks, o);
+      lookups += __shfl_xor_sync(0xffffffffu, lookups, o);
+      esc += __shfl_xor_sync(0xffffffffu, esc, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&ctr[0], (unsigned long long)lookups);
+      atomicAdd(&ctr[1], (unsigned long long)misses);
+      atomicAdd(&ctr[2], (unsigned long long)fallbacks);
+      atomicAdd(&ctr[3], (unsigned long long)steps);
+      atomicAdd(&ctr[4], (unsigned long long)esc);
+    }
+  }
+}
+
+float o2f_host(uint32_t u) {
+  uint32_t v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  float f;
+  memcpy(&f, &v, 4);
+  return f;
+}
+
+}  // namespace
+
+LearnedIndex::LearnedIndex(uint32_t leaves, uint32_t window) : L_(leaves), window_(window) {
+  SPJ_CHECK(leaves >= 1 && leaves <= 65535, "leaves must be in [1, 65535]");
+}
+
+LearnedIndex::~LearnedIndex() { cudaDeviceSynchronize(); }
+
+static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevBuf& keys,
+                             const DevBuf& ids, const DevBuf& xy, const DevBuf& xy32,
+                             const DevBuf& start, const DevBuf& a, const DevBuf& b,
+                             const DevBuf& kc, const DevBuf& err, double ra, double rb,
+                             uint32_t k0, float x0, float y0, float sx, float sy) {
+  LearnedView v;
+  v.n = n;
+  v.L = L;
+  v.window = window;
+  v.keys = keys.as<uint32_t>();
+  v.ids = ids.as<uint32_t>();
+  v.xy = xy.as<double2>();
+  v.xy32 = xy32.as<float2>();
+  v.start = start.as<uint32_t>();
+  v.a = a.as<double>();
+  v.b = b.as<double>();
+  v.kc = kc.as<uint32_t>();
+  v.err = err.as<uint32_t>();
+  v.ra = ra;
+  v.rb = rb;
+  v.k0 = k0;
+  v.x0 = x0;
+  v.y0 = y0;
+  v.sx = sx;
+  v.sy = sy;
+  return v;
+}
+
+#define SPJ_LVIEW()                                                                           \
+  make_view(n_, L_, window_, keys_, ids_, xy_, xy32_, leaf_start_, leaf_a_, leaf_b_, leaf_kc_, \
+            leaf_err_, root_a_, root_b_, k0_, x0_, y0_, sx_, sy_)
+
+void LearnedIndex::build(const DeviceGeoms& pts, const Lbvh& bvh, cudaStream_t s) {
+  bv_ = pts.view();
+  tv_ = bvh.view();
+  const uint32_t N = pts.n;
+  DevBuf flag((size_t)N + 1, s), pos(((size_t)N + 1) * 8, s);
+  k_point_flags<<<grid_for(N, 256), 256, 0, s>>>(pts.kind.as<uint8_t>(), N, flag.as<uint8_t>());
+  scan_u8_u64(flag.as<uint8_t>(), pos.as<uint64_t>(), N, tmp_, s);
+  uint64_t m64 = 0;
+  SPJ_CUDA(cudaMemcpyAsync(&m64, pos.as<uint64_t>() + N, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  n_ = (uint32_t)m64;
+  const uint32_t m = n_;
+  keys_.reserve(((size_t)m + 1) * 4, s);
+  ids_.reserve(((size_t)m + 1) * 4, s);
+  k_compact<<<grid_for(N, 256), 256, 0, s>>>(flag.as<uint8_t>(), pos.as<uint64_t>(), N,
+                                              ids_.as<uint32_t>());
+  DevBuf ext(16, s);
+  const uint32_t init[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u};
+  SPJ_CUDA(cudaMemcpyAsync(ext.get(), init, 16, cudaMemcpyHostToDevice, s));
+  if (m) k_extent<<<grid_for(m, 256), 256, 0, s>>>(pts.box.as<float4>(), ids_.as<uint32_t>(), m,
+                                                    ext.as<uint32_t>());
+  uint32_t he[4];
+  SPJ_CUDA(cudaMemcpyAsync(he, ext.get(), 16, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  if (m) {
+    x0_ = o2f_host(he[0]);
+    y0_ = o2f_host(he[1]);
+    const float x1 = o2f_host(he[2]), y1 = o2f_host(he[3]);
+    sx_ = x1 > x0_ ? 65536.0f / (x1 - x0_) : 0.0f;
+    sy_ = y1 > y0_ ? 65536.0f / (y1 - y0_) : 0.0f;
+  }
+  LearnedView v = SPJ_LVIEW();
+  if (m) k_keys<<<grid_for(m, 256), 256, 0, s>>>(v, pts.box.as<float4>(), ids_.as<uint32_t>(),
+                                                  m, keys_.as<uint32_t>());
+  {
+    DevBuf ak(((size_t)m + 1) * 4, s), av(((size_t)m + 1) * 4, s);
+    radix_sort_pairs(keys_.as<uint32_t>(), ids_.as<uint32_t>(), ak.as<uint32_t>(),
+                     av.as<uint32_t>(), m, 32, tmp_, s);
+  }
+  xy_.reserve(((size_t)m + 1) * 16, s);
+  xy32_.reserve(((size_t)m + 1) * 8, s);
+  if (m) k_gather<<<grid_for(m, 256), 256, 0, s>>>(pts.pt.as<double2>(), pts.box.as<float4>(),
+                                                    ids_.as<uint32_t>(), m, xy_.as<double2>(),
+                                                    xy32_.as<float2>());
+  leaf_start_.reserve(((size_t)L_ + 1) * 4, s);
+  leaf_a_.reserve(((size_t)L_ + 1) * 8, s);
+  leaf_b_.reserve(((size_t)L_ + 1) * 8, s);
+  leaf_kc_.reserve(((size_t)L_ + 1) * 4, s);
+  leaf_err_.reserve(((size_t)L_ + 1) * 4, s);
+  counters_.reserve(64, s);
+  fit_root(s);
+  train(true, s);
+}
+
+void LearnedIndex::fit_root(cudaStream_t s) {
+  const uint32_t m = n_;
+  k0_ = 0;
+  if (m) SPJ_CUDA(cudaMemcpyAsync(&k0_, keys_.get(), 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  const int nb = m ? std::min<int>(grid_for(m, 256), 1024) : 1;
+  DevBuf part((size_t)nb * sizeof(double4), s);
+  std::vector<double4> hp(nb);
+  if (m) {
+    k_root_partials<<<nb, 256, 0, s>>>(keys_.as<uint32_t>(), m, k0_, part.as<double4>());
+    SPJ_CUDA(cudaMemcpyAsync(hp.data(), part.get(), nb * sizeof(double4), cudaMemcpyDeviceToHost,
+                             s));
+  }
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  double sx = 0, sxx = 0, sr = 0, sxr = 0;
+  for (int i = 0; i < (m ? nb : 0); i++) {
+    sx += hp[i].x;
+    sxx += hp[i].y;
+    sr += hp[i].z;
+    sxr += hp[i].w;
+  }
+  const double nn = (double)m;
+  const double var = m ? sxx / nn - (sx / nn) * (sx / nn) : 0;
+  if (m && var > 0) {
+    root_a_ = (sxr / nn - (sx / nn) * (sr / nn)) / var;
+    root_b_ = sr / nn - root_a_ * sx / nn;
+  } else {
+    root_a_ = 0;
+    root_b_ = nn / 2;
+  }
+  if (root_a_ < 0) root_a_ = 0;  // keys are sorted: the leaf map must be monotone
+  // leaf ranges
+  DevBuf leaf(((size_t)m + 1) * 2, s);
+  LearnedView v = SPJ_LVIEW();
+  if (m) {
+    k_leaf_ids<<<grid_for(m, 256), 256, 0, s>>>(v, leaf.as<uint16_t>());
+    k_leaf_bounds<<<grid_for(m, 256), 256, 0, s>>>(leaf.as<uint16_t>(), m, L_,
+                                                   leaf_start_.as<uint32_t>());
+  } else {
+    SPJ_CUDA(cudaMemsetAsync(leaf_start_.get(), 0, ((size_t)L_ + 1) * 4, s));
+  }
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  stats_.root_a = root_a_;
+  stats_.root_b = root_b_;
+  stats_.leaves = L_;
+  stats_.points = m;
+}
+
+void LearnedIndex::train(bool trained, cudaStream_t s) {
+  k_leaf_init<<<grid_for(L_, 256), 256, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
+                                                L_, leaf_a_.as<double>(), leaf_b_.as<double>(),
+                                                leaf_kc_.as<uint32_t>());
+  DevBuf fb((size_t)L_ * 6 * 8, s);
+  if (trained) {
+    k_leaf_fwd_bwd<<<L_, kLeafThreads, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
+                                               leaf_kc_.as<uint32_t>(), leaf_a_.as<double>(),
+                                               leaf_b_.as<double>(), fb.as<double>());
+    k_leaf_newton<<<grid_for(L_, 256), 256, 0, s>>>(fb.as<double>(), L_, leaf_a_.as<double>(),
+                                                    leaf_b_.as<double>());
+    // gradient after the step (~0 up to rounding): reported as a check
+    k_leaf_fwd_bwd<<<L_, kLeafThreads, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
+                                               leaf_kc_.as<uint32_t>(), leaf_a_.as<double>(),
+                                               leaf_b_.as<double>(), fb.as<double>());
+    std::vector<double> h((size_t)L_ * 6);
+    SPJ_CUDA(cudaMemcpyAsync(h.data(), fb.get(), h.size() * 8, cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    double g = 0;
+    for (uint32_t l = 0; l < L_; l++) {
+      // relative to the gradient scale of the leaf
+      const double scale = std::sqrt(h[l * 6 + 3] * h[l * 6 + 5]) + 1.0;
+      g = std::max(g, std::fabs(h[l * 6 + 2]) / std::sqrt(h[l * 6 + 5] + 1.0) / scale);
+    }
+    stats_.grad_norm_after = g;
+  }
+  measure_errors(s);
+}
+
+void LearnedIndex::measure_errors(cudaStream_t s) {
+  k_leaf_err<<<L_, kLeafThreads, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
+                                         leaf_kc_.as<uint32_t>(), leaf_a_.as<double>(),
+                                         leaf_b_.as<double>(), leaf_err_.as<uint32_t>());
+  std::vector<uint32_t> e(L_), st(L_ + 1);
+  SPJ_CUDA(cudaMemcpyAsync(e.data(), leaf_err_.get(), (size_t)L_ * 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(st.data(), leaf_start_.get(), ((size_t)L_ + 1) * 4,
+                           cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  uint32_t mx = 0, over = 0, nonempty = 0;
+  double sum = 0;
+  for (uint32_t l = 0; l < L_; l++) {
+    if (st[l + 1] == st[l]) continue;
+    nonempty++;
+    mx = std::max(mx, e[l]);
+    sum += e[l];
+    if (e[l] > window_) over++;
+  }
+  stats_.max_err = mx;
+  stats_.mean_err = nonempty ? sum / nonempty : 0;
+  stats_.leaves_over_window = over;
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void LearnedIndex::loss_and_grad(const std::vector<double>& a, const std::vector<double>& b,
+                                 std::vector<double>& loss, std::vector<double>& ga,
+                                 std::vector<double>& gb, cudaStream_t s) {
+  SPJ_CHECK(a.size() == L_ && b.size() == L_, "parameter arrays must have one entry per leaf");
+  DevBuf da((size_t)L_ * 8, s), db((size_t)L_ * 8, s), fb((size_t)L_ * 6 * 8, s);
+  SPJ_CUDA(cudaMemcpyAsync(da.get(), a.data(), (size_t)L_ * 8, cudaMemcpyHostToDevice, s));
+  SPJ_CUDA(cudaMemcpyAsync(db.get(), b.data(), (size_t)L_ * 8, cudaMemcpyHostToDevice, s));
+  k_leaf_fwd_bwd<<<L_, kLeafThreads, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
+                                             leaf_kc_.as<uint32_t>(), da.as<double>(),
+                                             db.as<double>(), fb.as<double>());
+  std::vector<double> h((size_t)L_ * 6);
+  SPJ_CUDA(cudaMemcpyAsync(h.data(), fb.get(), h.size() * 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  loss.resize(L_);
+  ga.resize(L_);
+  gb.resize(L_);
+  for (uint32_t l = 0; l < L_; l++) {
+    loss[l] = h[l * 6];
+    ga[l] = h[l * 6 + 1];
+    gb[l] = h[l * 6 + 2];
+  }
+}
+
+uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int predicate,
+                             DevBuf& out_build, DevBuf& out_probe, cudaStream_t s) {
+  const uint32_t np = probe.n;
+  counts_.reserve(((size_t)np + 1) * 4, s);
+  offs_.reserve(((size_t)np + 1) * 8, s);
+  scratch_.reserve(sizeof(DeviceStatus), s);
+  reset_status(scratch_, s);
+  SPJ_CUDA(cudaMemsetAsync(counters_.get(), 0, 64, s));
+  const LearnedView v = SPJ_LVIEW();
+  DeviceStatus* st = scratch_.as<DeviceStatus>();
+  auto* ctr = counters_.as<unsigned long long>();
+  const int g = grid_for(np, 128, kNumSMs * 16);
+  if (np)
+    k_learned_query<0><<<g, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate,
+                                         counts_.as<uint32_t>(), nullptr, nullptr, nullptr, ctr,
+                                         st);
+  scan_u32_u64(counts_.as<uint32_t>(), offs_.as<uint64_t>(), np, tmp_, s);
+  uint64_t total = 0;
+  SPJ_CUDA(cudaMemcpyAsync(&total, offs_.as<uint64_t>() + np, 8, cudaMemcpyDeviceToHost, s));
+  check_status(scratch_, s, "learned query");  // syncs
+  out_build.reserve((total + 1) * 4, s);
+  out_probe.reserve((total + 1) * 4, s);
+  if (np)
+    k_learned_query<1><<<g, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate, nullptr,
+                                         offs_.as<uint64_t>(), out_build.as<uint32_t>(),
+                                         out_probe.as<uint32_t>(), ctr, st);
+  unsigned long long h[8];
+  SPJ_CUDA(cudaMemcpyAsync(h, counters_.get(), 64, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  SPJ_CUDA(cudaGetLastError());
+  stats_.lookups += h[0];
+  stats_.window_misses += h[1];
+  stats_.lbvh_fallbacks += h[2];
+  stats_.search_steps += h[3];
+  return total;
+}
+
+void LearnedIndex::export_model(std::vector<uint32_t>& keys, std::vector<uint32_t>& leaf_start,
+                                std::vector<uint32_t>& leaf_kc, std::vector<double>& a,
+                                std::vector<double>& b, std::vector<uint32_t>& err,
+                                cudaStream_t s) {
+  keys.resize(n_);
+  leaf_start.resize(L_ + 1);
+  leaf_kc.resize(L_);
+  a.resize(L_);
+  b.resize(L_);
+  err.resize(L_);
+  if (n_) SPJ_CUDA(cudaMemcpyAsync(keys.data(), keys_.get(), (size_t)n_ * 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(leaf_start.data(), leaf_start_.get(), ((size_t)L_ + 1) * 4,
+                           cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(leaf_kc.data(), leaf_kc_.get(), (size_t)L_ * 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(a.data(), leaf_a_.get(), (size_t)L_ * 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(b.data(), leaf_b_.get(), (size_t)L_ * 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(err.data(), leaf_err_.get(), (size_t)L_ * 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace spj

@@ -172,9 +172,13 @@ template <bool kFast>
 __global__ void __launch_bounds__(256)
     k_refine(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
              const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, int predicate,
-             uint8_t* __restrict__ flags, DeviceStatus* st) {
+             uint8_t* __restrict__ flags, DeviceStatus* st,
+             const uint64_t* __restrict__ m_dev = nullptr) {
   uint32_t esc = 0, pairs = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // with m_dev the pair count lives on the device (graph replays) and m is
+  // the buffer capacity: flags past the count are cleared
+  const uint64_t mm = m_dev ? min(*m_dev, m) : m;
   // every lane runs the same number of loop trips so the warp-wide flush
   // below sees all 32 lanes
   const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -182,6 +186,10 @@ __global__ void __launch_bounds__(256)
   for (uint64_t t = 0; t < trips; t++) {
     const uint64_t k = start + t * stride;
     if (k >= m) continue;
+    if (k >= mm) {
+      flags[k] = 0;
+      continue;
+    }
     const uint32_t b = cb[k], p = cp[k] - probe_base;
     int r = eval<kFast>(B, b, P, p, predicate, esc);
     pairs++;
@@ -308,11 +316,13 @@ __global__ void __launch_bounds__(256)
 
 __global__ void k_compact(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
                           const uint8_t* __restrict__ flags, const uint64_t* __restrict__ pos,
-                          uint64_t m, uint32_t* __restrict__ ob, uint32_t* __restrict__ op) {
+                          uint64_t m, uint32_t* __restrict__ ob, uint32_t* __restrict__ op,
+                          uint64_t out_cap) {
   for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m;
        k += (uint64_t)gridDim.x * blockDim.x) {
     if (flags[k]) {
       const uint64_t o = pos[k];
+      if (o >= out_cap) continue;  // bounded by the output capacity
       ob[o] = cb[k];
       op[o] = cp[k];
     }
@@ -323,13 +333,15 @@ __global__ void k_compact(const uint32_t* __restrict__ cb, const uint32_t* __res
 
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
-                     uint8_t* flags, DeviceStatus* st, cudaStream_t s) {
+                     uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint64_t* m_dev) {
   if (m == 0) return;
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
   if (form == kFastF32)
-    k_refine<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st);
+    k_refine<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                     m_dev);
   else
-    k_refine<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st);
+    k_refine<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                      m_dev);
   SPJ_CUDA(cudaGetLastError());
 }
 
@@ -351,9 +363,11 @@ void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32
 }
 
 void compact_pairs(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags,
-                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s) {
+                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s,
+                   uint64_t out_cap) {
   if (m == 0) return;
-  k_compact<<<grid_for((int64_t)m, 256, kNumSMs * 16), 256, 0, s>>>(cb, cp, flags, pos, m, ob, op);
+  k_compact<<<grid_for((int64_t)m, 256, kNumSMs * 16), 256, 0, s>>>(cb, cp, flags, pos, m, ob, op,
+                                                                     out_cap);
   SPJ_CUDA(cudaGetLastError());
 }
 

@@ -25,9 +25,12 @@ enum RefineForm : int {
 
 // flags[k] = pred(build[cb[k]], probe[cp[k] - probe_base]) for k < m.
 // counters: status->counters[0] += FP64 escalations, [1] += pairs evaluated.
+// With m_dev the pair count is read on the device (CUDA-graph replays) and m
+// is the capacity of cb/cp/flags; flags past the count are cleared.
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
-                     uint8_t* flags, DeviceStatus* st, cudaStream_t s);
+                     uint8_t* flags, DeviceStatus* st, cudaStream_t s,
+                     const uint64_t* m_dev = nullptr);
 
 // flags[k] = hypot(build - probe) <= distance for point pairs.  The FP32
 // filter decides pairs whose distance is far from the threshold relative to
@@ -39,6 +42,7 @@ void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32
 // Stream compaction of (cb, cp) by flags: positions from an exclusive scan
 // of the flags (pos has m+1 entries).  Order is preserved.
 void compact_pairs(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags,
-                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s);
+                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s,
+                   uint64_t out_cap = ~0ull);
 
 }  // namespace spj

@@ -4,13 +4,20 @@
 // The reference probes one DataFusion batch per FFI call
 // (rust/sedona-spatial-join/src/stream.rs:1166-1200 -> query_batch), each call
 // paying host round trips.  Here the batches of a stream are described in a
-// device table and cut into fixed-size row chunks; a persistent kernel pulls
-// chunks from a work queue (one atomic per chunk) and, per probe row, decodes
-// the point from its WKB, walks the LBVH and refines each candidate inline.
-// It runs twice — pass 0 counts each row's pairs, an exclusive scan turns the
-// counts into offsets, pass 1 writes the pairs — so the output is grouped by
-// probe row in ascending order and no candidate buffer exists.  Queue reset,
-// both passes, the scan and the copy-out of the total are one CUDA graph.
+// device table and cut into fixed-size row chunks.  One replay of a CUDA graph
+// runs:
+//   1. a persistent decode kernel pulling chunks from a work queue (one atomic
+//      per chunk) and decoding every row's point into one stream-wide column;
+//   2. the LBVH count pass, a scan, and the scatter pass over that column
+//      (candidate pairs, bounded by the candidate capacity);
+//   3. the refine kernel over the candidates (the pair count is read on the
+//      device), a scan of its flags, and the compaction (bounded by the output
+//      capacity);
+//   4. the copy-out of the two totals.
+// The host checks the totals after the replay; when a capacity was too small
+// it grows the buffers, re-captures and replays (the buffers then stay large
+// enough for later replays of the same stream).  Pairs come out grouped by
+// probe row in ascending order.
 #pragma once
 #include <string>
 #include <vector>
@@ -20,8 +27,8 @@
 namespace spj {
 
 struct StreamParams {
-  int block = 128;            // threads per CTA: 64, 128 or 256
-  uint32_t chunk_rows = 1024;  // rows per work-queue item
+  int block = 256;             // threads per CTA of the decode kernel: 128 or 256
+  uint32_t chunk_rows = 4096;  // rows per work-queue item
   uint32_t leaf_size = 4;      // LBVH leaf size
   bool operator==(const StreamParams& o) const {
     return block == o.block && chunk_rows == o.chunk_rows && leaf_size == o.leaf_size;
@@ -29,8 +36,9 @@ struct StreamParams {
 };
 
 struct StreamStats {
-  double ms_last = 0;         // device time of the last replay (CUDA events)
-  uint64_t rows = 0, pairs = 0, replays = 0, escalations = 0, launches_per_replay = 0;
+  double ms_last = 0;  // device time of the last replay (CUDA events)
+  uint64_t rows = 0, pairs = 0, candidates = 0, replays = 0, escalations = 0;
+  uint64_t launches_per_replay = 0;
 };
 
 class StreamJoin {
@@ -45,8 +53,9 @@ class StreamJoin {
   uint64_t run(int predicate, const uint32_t** d_build, const uint32_t** d_probe);
   void set_params(const StreamParams& p);
   const StreamParams& params() const { return params_; }
-  // Times each candidate parameter set on the current batches and keeps the
-  // fastest; results are cached in `cache_path` (JSON lines) when non-empty.
+  // Times the candidate parameter sets on (a prefix of) the current batches
+  // and keeps the fastest; results are cached in `cache_path` (one line per
+  // device / workload signature / predicate) when it is non-empty.
   StreamParams autotune(int predicate, const std::string& cache_path);
   cudaStream_t stream() const { return s_; }
   const StreamStats& stats() const { return stats_; }
@@ -57,9 +66,11 @@ class StreamJoin {
   JoinEngine& eng_;
   cudaStream_t s_ = nullptr;
   StreamParams params_;
-  DevBuf batches_, chunks_, counts_, offs_, sums_, out_b_, out_p_, ctrl_;
-  uint64_t* h_total_ = nullptr;  // pinned: total pairs + status word
-  uint64_t capacity_ = 0;
+  DevBuf batches_, chunks_, ctrl_;
+  DevBuf kind_, pt_, box_, counts_, offs_, sums_;  // stream-wide decoded column
+  DevBuf cand_b_, cand_p_, flags_, pos_, sums2_, out_b_, out_p_;
+  uint64_t* h_tot_ = nullptr;  // pinned: candidates, pairs, status, escalations
+  uint64_t ccap_ = 0, ocap_ = 0;
   uint32_t nrows_ = 0, nchunks_ = 0, nbatches_ = 0;
   std::vector<WkbDeviceColumn> cols_;
   cudaGraphExec_t exec_ = nullptr;

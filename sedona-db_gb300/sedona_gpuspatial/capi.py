@@ -160,7 +160,24 @@ EXPORTS = [
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
     "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
     "SpjStreamCudaStream",
+    "SpjLearnedCreate", "SpjLearnedRelease", "SpjLearnedLastError", "SpjLearnedBuildDevice",
+    "SpjLearnedSetTrained", "SpjLearnedQueryDevice", "SpjLearnedLossAndGrad", "SpjLearnedExport",
+    "SpjLearnedGetStats", "SpjLearnedStream",
 ]
+
+
+class SpjLearnedConfig(C.Structure):
+    _fields_ = [("runtime", C.POINTER(GpuSpatialRuntime)), ("leaves", C.c_uint32),
+                ("window", C.c_uint32)]
+
+
+class SpjLearnedStats(C.Structure):
+    _fields_ = [("points", C.c_uint64), ("lookups", C.c_uint64), ("window_misses", C.c_uint64),
+                ("lbvh_fallbacks", C.c_uint64), ("search_steps", C.c_uint64),
+                ("leaves", C.c_uint32), ("max_err", C.c_uint32),
+                ("leaves_over_window", C.c_uint32), ("trained", C.c_uint32),
+                ("root_a", C.c_double), ("root_b", C.c_double), ("mean_err", C.c_double),
+                ("grad_norm_after", C.c_double), ("ms_build", C.c_double)]
 
 _lib = None
 _lib_lock = threading.Lock()
@@ -232,6 +249,21 @@ def lib() -> C.CDLL:
                                             C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
             L.SpjStreamCudaStream.argtypes = [C.c_void_p]
             L.SpjStreamCudaStream.restype = C.c_void_p
+            L.SpjLearnedCreate.argtypes = [C.POINTER(SpjLearnedConfig), C.POINTER(C.c_void_p)]
+            L.SpjLearnedRelease.argtypes = [C.c_void_p]
+            L.SpjLearnedRelease.restype = None
+            L.SpjLearnedLastError.argtypes = [C.c_void_p]
+            L.SpjLearnedLastError.restype = C.c_char_p
+            L.SpjLearnedBuildDevice.argtypes = [C.c_void_p, C.POINTER(SpjDeviceWkb)]
+            L.SpjLearnedSetTrained.argtypes = [C.c_void_p, C.c_int32]
+            L.SpjLearnedQueryDevice.argtypes = [C.c_void_p, C.POINTER(SpjDeviceWkb), C.c_int32,
+                                                C.c_uint32, C.POINTER(C.c_void_p),
+                                                C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)]
+            L.SpjLearnedLossAndGrad.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+            L.SpjLearnedExport.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+            L.SpjLearnedGetStats.argtypes = [C.c_void_p, C.POINTER(SpjLearnedStats)]
+            L.SpjLearnedStream.argtypes = [C.c_void_p]
+            L.SpjLearnedStream.restype = C.c_void_p
             _lib = L
     return _lib
 
@@ -528,6 +560,73 @@ class StreamProbe:
     def __del__(self):
         if getattr(self, "h", None):
             lib().SpjStreamRelease(self.h)
+            self.h = None
+
+
+class LearnedIndex:
+    """Learned point index over a device point column (SpjLearned*,
+    include/spj_gb300.h)."""
+
+    def __init__(self, runtime: Optional[Runtime] = None, leaves: int = 4096, window: int = 4096):
+        self.runtime = runtime or Runtime.get()
+        self.h = C.c_void_p()
+        cfg = SpjLearnedConfig(C.pointer(self.runtime.rt), leaves, window)
+        if lib().SpjLearnedCreate(C.byref(cfg), C.byref(self.h)) != 0:
+            raise GpuSpatialError("SpjLearnedCreate failed")
+        self.leaves = leaves
+
+    def _err(self):
+        return lib().SpjLearnedLastError(self.h)
+
+    def build_device(self, dcol: SpjDeviceWkb):
+        _check(lib().SpjLearnedBuildDevice(self.h, C.byref(dcol)), "build", self._err)
+
+    def set_trained(self, trained: bool):
+        _check(lib().SpjLearnedSetTrained(self.h, int(trained)), "set_trained", self._err)
+
+    def query_device(self, dcol: SpjDeviceWkb, predicate: str = "intersects", probe_base: int = 0):
+        db, dp, n = C.c_void_p(), C.c_void_p(), C.c_uint64()
+        _check(lib().SpjLearnedQueryDevice(self.h, C.byref(dcol), PREDICATES[predicate],
+                                           probe_base, C.byref(db), C.byref(dp), C.byref(n)),
+               "query", self._err)
+        return db.value, dp.value, n.value
+
+    def loss_and_grad(self, a: np.ndarray, b: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        loss = np.empty(self.leaves)
+        ga = np.empty(self.leaves)
+        gb = np.empty(self.leaves)
+        _check(lib().SpjLearnedLossAndGrad(self.h, a.ctypes.data, b.ctypes.data, loss.ctypes.data,
+                                           ga.ctypes.data, gb.ctypes.data), "loss_and_grad",
+               self._err)
+        return loss, ga, gb
+
+    def export(self):
+        st = self.stats()
+        n, L = st["points"], self.leaves
+        keys = np.empty(n, np.uint32)
+        start = np.empty(L + 1, np.uint32)
+        kc = np.empty(L, np.uint32)
+        a = np.empty(L)
+        b = np.empty(L)
+        err = np.empty(L, np.uint32)
+        _check(lib().SpjLearnedExport(self.h, keys.ctypes.data, start.ctypes.data, kc.ctypes.data,
+                                      a.ctypes.data, b.ctypes.data, err.ctypes.data), "export",
+               self._err)
+        return {"keys": keys, "leaf_start": start, "leaf_kc": kc, "a": a, "b": b, "err": err}
+
+    def stats(self) -> dict:
+        s = SpjLearnedStats()
+        _check(lib().SpjLearnedGetStats(self.h, C.byref(s)), "stats", self._err)
+        return {f: getattr(s, f) for f, _ in SpjLearnedStats._fields_}
+
+    def stream(self) -> int:
+        return lib().SpjLearnedStream(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().SpjLearnedRelease(self.h)
             self.h = None
 
 

@@ -346,7 +346,7 @@ def _device_pairs(db, dp, n):
     return b, p
 
 
-@pytest.mark.parametrize("params", [None, (64, 256, 2), (256, 4096, 8)])
+@pytest.mark.parametrize("params", [None, (128, 256, 2), (256, 8192, 8)])
 def test_stream_matches_oracle(capi, oracle_mod, params):
     from sedona_gpuspatial import datagen
     inp = datagen.workload3(n_points=80000, n_zones=400)
