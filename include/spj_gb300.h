@@ -179,7 +179,9 @@ struct SpjLearnedConfig {
 struct SpjLearnedStats {
   uint64_t points, lookups, window_misses, lbvh_fallbacks, search_steps;
   uint32_t leaves, max_err, leaves_over_window, trained;
-  double root_a, root_b, mean_err, grad_norm_after, ms_build;
+  /* stage one: radix table of root_entries prefixes of (key - first key)
+   * >> root_shift; mean_err: mean over leaves of the max |rank error| */
+  double root_shift, root_entries, mean_err, grad_norm_after, ms_build;
 };
 
 int SpjLearnedCreate(const struct SpjLearnedConfig* config, SpjLearned** out);

@@ -974,8 +974,8 @@ extern "C" int SpjLearnedGetStats(SpjLearned* li, SpjLearnedStats* out) {
     out->max_err = s.max_err;
     out->leaves_over_window = s.leaves_over_window;
     out->trained = li->trained ? 1 : 0;
-    out->root_a = s.root_a;
-    out->root_b = s.root_b;
+    out->root_shift = s.root_shift;
+    out->root_entries = s.root_entries;
     out->mean_err = s.mean_err;
     out->grad_norm_after = s.grad_norm_after;
     out->ms_build = li->ms_build;

@@ -21,7 +21,8 @@ struct LearnedView {
   const double* b;
   const uint32_t* kc;
   const uint32_t* err;
-  double ra, rb;
+  const uint16_t* root_tab;  // root_p + 1 entries: leaves whose first key's prefix < p
+  uint32_t root_shift, root_p;
   uint32_t k0;
   float x0, y0, sx, sy;
 };
@@ -67,11 +68,24 @@ __device__ __forceinline__ uint32_t key_of(const LearnedView& v, float2 p) {
   return hilbert16(cell_of(p.x, v.x0, v.sx), cell_of(p.y, v.y0, v.sy));
 }
 
+// Stage one: the leaf holding lower_bound(q).  Leaves are equal-count rank
+// ranges; the answer is the last leaf whose first key is < q (leaf 0 when
+// none is).  A radix table over key prefixes narrows the leaves to the few
+// whose first key shares q's prefix, then a short binary search over those
+// first keys (kc) finishes.
 __device__ __forceinline__ uint32_t root_leaf(const LearnedView& v, uint32_t q) {
-  const double t = (v.ra * ((double)q - (double)v.k0) + v.rb) * ((double)v.L / (double)v.n);
-  if (!(t >= 0.0)) return 0;
-  if (t >= (double)(v.L - 1)) return v.L - 1;
-  return (uint32_t)t;
+  if (v.n == 0 || q <= v.k0) return 0;
+  uint32_t p = (q - v.k0) >> v.root_shift;
+  if (p > v.root_p - 1) p = v.root_p - 1;
+  uint32_t lo = v.root_tab[p], hi = v.root_tab[p + 1];
+  // leaves < lo: first key's prefix < p (first key < q); leaves >= hi:
+  // prefix > p (first key > q); find the first leaf in [lo, hi) with key >= q
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (v.kc[mid] < q) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo ? lo - 1 : 0;
 }
 
 __device__ __forceinline__ uint32_t bsearch_first_ge(const uint32_t* keys, uint32_t lo,
@@ -94,17 +108,25 @@ __device__ __forceinline__ uint32_t learned_lower_bound(const LearnedView& v, ui
   const uint32_t e = v.err[l];
   bad = e > v.window;
   if (bad) return 0;
+  // the answer lies in [start_l, start_{l+1}] (the first key of leaf l is
+  // < q unless l == 0, and leaf l+1's first key is >= q)
+  const double s_lo = (double)v.start[l];
+  const double s_hi = fmin((double)v.start[l + 1] + 1.0, (double)v.n);
   const double pred = __fma_rn(v.a[l], (double)q - (double)v.kc[l], v.b[l]);
-  double lo_d = floor(pred) - (double)e - 1.0, hi_d = ceil(pred) + (double)e + 2.0;
-  lo_d = fmax(lo_d, 0.0);
-  hi_d = fmin(hi_d, (double)v.n);
-  uint32_t lo = (uint32_t)lo_d, hi = (uint32_t)fmax(hi_d, lo_d);
+  double lo_d = fmax(floor(pred) - (double)e - 1.0, s_lo);
+  double hi_d = fmin(ceil(pred) + (double)e + 2.0, s_hi);
+  if (!(hi_d >= lo_d)) hi_d = lo_d;  // also catches NaN
+  uint32_t lo = (uint32_t)lo_d, hi = (uint32_t)hi_d;
   uint32_t p = bsearch_first_ge(v.keys, lo, hi, q, steps);
   const bool ok_lo = p == 0 || v.keys[p - 1] < q;
   const bool ok_hi = p == v.n || v.keys[p] >= q;
   if (!(ok_lo && ok_hi)) {
+    // outside the measured error (q between keys at a leaf edge): the
+    // leaf's whole range, then (never needed by construction) everything
     misses++;
-    p = bsearch_first_ge(v.keys, 0, v.n, q, steps);
+    p = bsearch_first_ge(v.keys, (uint32_t)s_lo, (uint32_t)s_hi, q, steps);
+    if (!((p == 0 || v.keys[p - 1] < q) && (p == v.n || v.keys[p] >= q)))
+      p = bsearch_first_ge(v.keys, 0, v.n, q, steps);
   }
   return p;
 }
@@ -170,56 +192,6 @@ __global__ void k_gather(const double2* __restrict__ pt, const float4* __restric
   }
 }
 
-// per-block partial sums of (x, x^2, r, x r) with x = key - k0 (FP64)
-__global__ void k_root_partials(const uint32_t* __restrict__ keys, uint32_t n, uint32_t k0,
-                                double4* __restrict__ part) {
-  __shared__ double sm[4][32];
-  double s1 = 0, s2 = 0, s3 = 0, s4 = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double x = (double)(keys[i] - k0), r = (double)i;
-    s1 += x;
-    s2 = __fma_rn(x, x, s2);
-    s3 += r;
-    s4 = __fma_rn(x, r, s4);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    s3 += __shfl_xor_sync(0xffffffffu, s3, o);
-    s4 += __shfl_xor_sync(0xffffffffu, s4, o);
-  }
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) {
-    sm[0][w] = s1;
-    sm[1][w] = s2;
-    sm[2][w] = s3;
-    sm[3][w] = s4;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t[4] = {0, 0, 0, 0};
-    for (int j = 0; j < (int)(blockDim.x >> 5); j++)
-      for (int c = 0; c < 4; c++) t[c] += sm[c][j];
-    part[blockIdx.x] = make_double4(t[0], t[1], t[2], t[3]);
-  }
-}
-
-__global__ void k_leaf_ids(LearnedView v, uint16_t* __restrict__ leaf) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x)
-    leaf[i] = (uint16_t)root_leaf(v, v.keys[i]);
-}
-
-__global__ void k_leaf_bounds(const uint16_t* __restrict__ leaf, uint32_t n, uint32_t L,
-                              uint32_t* __restrict__ start) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int li = leaf[i];
-    const int lp = i ? (int)leaf[i - 1] : -1;
-    for (int l = lp + 1; l <= li; l++) start[l] = i;
-    if (i == n - 1)
-      for (uint32_t l = (uint32_t)li + 1; l <= L; l++) start[l] = n;
-  }
-}
-
 // block reduction of 6 doubles (blockDim == kLeafThreads)
 __device__ __forceinline__ void block_sum6(double (&v)[6], double (*sm)[kLeafThreads / 32]) {
   for (int o = 16; o > 0; o >>= 1)
@@ -240,13 +212,13 @@ __device__ __forceinline__ void block_sum6(double (&v)[6], double (*sm)[kLeafThr
 
 // Untrained start: the line through the leaf's first and last (key, rank).
 __global__ void k_leaf_init(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
-                            uint32_t L, double* a, double* b, uint32_t* kc) {
+                            uint32_t L, uint32_t n, double* a, double* b, uint32_t* kc) {
   for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
     const uint32_t s = start[l], e = start[l + 1];
     if (s >= e) {
       a[l] = 0;
       b[l] = (double)s;
-      kc[l] = s ? keys[s - 1] : 0;
+      kc[l] = s < n ? keys[s] : 0xFFFFFFFFu;  // keeps first keys non-decreasing
       continue;
     }
     kc[l] = keys[s];
@@ -534,8 +506,9 @@ LearnedIndex::~LearnedIndex() { cudaDeviceSynchronize(); }
 static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevBuf& keys,
                              const DevBuf& ids, const DevBuf& xy, const DevBuf& xy32,
                              const DevBuf& start, const DevBuf& a, const DevBuf& b,
-                             const DevBuf& kc, const DevBuf& err, double ra, double rb,
-                             uint32_t k0, float x0, float y0, float sx, float sy) {
+                             const DevBuf& kc, const DevBuf& err, const DevBuf& root_tab,
+                             uint32_t root_shift, uint32_t root_p, uint32_t k0, float x0,
+                             float y0, float sx, float sy) {
   LearnedView v;
   v.n = n;
   v.L = L;
@@ -549,8 +522,9 @@ static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevB
   v.b = b.as<double>();
   v.kc = kc.as<uint32_t>();
   v.err = err.as<uint32_t>();
-  v.ra = ra;
-  v.rb = rb;
+  v.root_tab = root_tab.as<uint16_t>();
+  v.root_shift = root_shift;
+  v.root_p = root_p;
   v.k0 = k0;
   v.x0 = x0;
   v.y0 = y0;
@@ -561,7 +535,7 @@ static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevB
 
 #define SPJ_LVIEW()                                                                           \
   make_view(n_, L_, window_, keys_, ids_, xy_, xy32_, leaf_start_, leaf_a_, leaf_b_, leaf_kc_, \
-            leaf_err_, root_a_, root_b_, k0_, x0_, y0_, sx_, sy_)
+            leaf_err_, root_tab_, root_shift_, root_p_, k0_, x0_, y0_, sx_, sy_)
 
 void LearnedIndex::build(const DeviceGeoms& pts, const Lbvh& bvh, cudaStream_t s) {
   bv_ = pts.view();
@@ -619,55 +593,45 @@ void LearnedIndex::build(const DeviceGeoms& pts, const Lbvh& bvh, cudaStream_t s
 
 void LearnedIndex::fit_root(cudaStream_t s) {
   const uint32_t m = n_;
-  k0_ = 0;
-  if (m) SPJ_CUDA(cudaMemcpyAsync(&k0_, keys_.get(), 4, cudaMemcpyDeviceToHost, s));
+  // equal-count leaves: leaf l covers ranks [l*m/L, (l+1)*m/L)
+  std::vector<uint32_t> st(L_ + 1);
+  for (uint32_t l = 0; l <= L_; l++) st[l] = (uint32_t)((uint64_t)l * m / L_);
+  SPJ_CUDA(cudaMemcpyAsync(leaf_start_.get(), st.data(), st.size() * 4, cudaMemcpyHostToDevice, s));
+  k_leaf_init<<<grid_for(L_, 256), 256, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
+                                                L_, m, leaf_a_.as<double>(), leaf_b_.as<double>(),
+                                                leaf_kc_.as<uint32_t>());
+  std::vector<uint32_t> kc(L_);
+  uint32_t kend = 0;
+  SPJ_CUDA(cudaMemcpyAsync(kc.data(), leaf_kc_.get(), (size_t)L_ * 4, cudaMemcpyDeviceToHost, s));
+  if (m)
+    SPJ_CUDA(cudaMemcpyAsync(&kend, keys_.as<uint32_t>() + (m - 1), 4, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
-  const int nb = m ? std::min<int>(grid_for(m, 256), 1024) : 1;
-  DevBuf part((size_t)nb * sizeof(double4), s);
-  std::vector<double4> hp(nb);
-  if (m) {
-    k_root_partials<<<nb, 256, 0, s>>>(keys_.as<uint32_t>(), m, k0_, part.as<double4>());
-    SPJ_CUDA(cudaMemcpyAsync(hp.data(), part.get(), nb * sizeof(double4), cudaMemcpyDeviceToHost,
-                             s));
+  // stage-one radix table over key prefixes: entry p counts the leaves whose
+  // first key has a prefix below p
+  k0_ = m ? kc[0] : 0;
+  const uint32_t span = m ? kend - k0_ : 0;
+  int bits = 0;
+  while (bits < 32 && (span >> bits) != 0) bits++;
+  root_shift_ = bits > 16 ? (uint32_t)(bits - 16) : 0u;
+  root_p_ = (span >> root_shift_) + 1;
+  std::vector<uint16_t> tab(root_p_ + 1);
+  uint32_t l = 0;
+  for (uint32_t p = 0; p <= root_p_; p++) {
+    while (l < L_ && kc[l] != 0xFFFFFFFFu && ((kc[l] - k0_) >> root_shift_) < p) l++;
+    tab[p] = (uint16_t)l;
   }
+  root_tab_.reserve(tab.size() * 2, s);
+  SPJ_CUDA(cudaMemcpyAsync(root_tab_.get(), tab.data(), tab.size() * 2, cudaMemcpyHostToDevice, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
-  double sx = 0, sxx = 0, sr = 0, sxr = 0;
-  for (int i = 0; i < (m ? nb : 0); i++) {
-    sx += hp[i].x;
-    sxx += hp[i].y;
-    sr += hp[i].z;
-    sxr += hp[i].w;
-  }
-  const double nn = (double)m;
-  const double var = m ? sxx / nn - (sx / nn) * (sx / nn) : 0;
-  if (m && var > 0) {
-    root_a_ = (sxr / nn - (sx / nn) * (sr / nn)) / var;
-    root_b_ = sr / nn - root_a_ * sx / nn;
-  } else {
-    root_a_ = 0;
-    root_b_ = nn / 2;
-  }
-  if (root_a_ < 0) root_a_ = 0;  // keys are sorted: the leaf map must be monotone
-  // leaf ranges
-  DevBuf leaf(((size_t)m + 1) * 2, s);
-  LearnedView v = SPJ_LVIEW();
-  if (m) {
-    k_leaf_ids<<<grid_for(m, 256), 256, 0, s>>>(v, leaf.as<uint16_t>());
-    k_leaf_bounds<<<grid_for(m, 256), 256, 0, s>>>(leaf.as<uint16_t>(), m, L_,
-                                                   leaf_start_.as<uint32_t>());
-  } else {
-    SPJ_CUDA(cudaMemsetAsync(leaf_start_.get(), 0, ((size_t)L_ + 1) * 4, s));
-  }
-  SPJ_CUDA(cudaStreamSynchronize(s));
-  stats_.root_a = root_a_;
-  stats_.root_b = root_b_;
+  stats_.root_shift = root_shift_;
+  stats_.root_entries = root_p_;
   stats_.leaves = L_;
   stats_.points = m;
 }
 
 void LearnedIndex::train(bool trained, cudaStream_t s) {
   k_leaf_init<<<grid_for(L_, 256), 256, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
-                                                L_, leaf_a_.as<double>(), leaf_b_.as<double>(),
+                                                L_, n_, leaf_a_.as<double>(), leaf_b_.as<double>(),
                                                 leaf_kc_.as<uint32_t>());
   DevBuf fb((size_t)L_ * 6 * 8, s);
   if (trained) {

@@ -1,7 +1,8 @@
 // learned.cuh — learned point index: the build points sorted by a 32-bit
 // Hilbert key on a 2^16 x 2^16 grid over their extent, and a two-stage
-// piecewise-linear model (a root line choosing one of L leaves, one line per
-// leaf) that maps a key to its rank in the sorted order.  A lookup evaluates
+// piecewise-linear model of key -> rank: stage one picks one of L
+// equal-count leaves through a radix table over key prefixes (a radix spline
+// over the leaves' first keys), stage two is one line per leaf.  A lookup evaluates
 // the model and binary-searches only within the leaf's measured maximum
 // error; the result is verified against the neighbouring keys, so a lookup
 // is exact whatever the model's quality.  The LBVH over the same points is
@@ -25,7 +26,7 @@ namespace spj {
 struct LearnedStats {
   uint32_t leaves = 0;
   uint64_t points = 0;
-  double root_a = 0, root_b = 0;
+  uint32_t root_shift = 0, root_entries = 0;  // stage-one radix table
   uint32_t max_err = 0;   // over leaves
   double mean_err = 0;    // mean per-leaf max error (non-empty leaves)
   uint32_t leaves_over_window = 0;
@@ -72,7 +73,8 @@ class LearnedIndex {
   DevBuf keys_, ids_, xy_, xy32_;  // sorted by key
   DevBuf leaf_start_, leaf_a_, leaf_b_, leaf_kc_, leaf_err_, counters_, counts_, offs_, tmp_,
       scratch_;
-  double root_a_ = 0, root_b_ = 0;
+  DevBuf root_tab_;
+  uint32_t root_shift_ = 0, root_p_ = 1;
   uint32_t k0_ = 0;
   LearnedStats stats_;
 };

@@ -176,7 +176,8 @@ class SpjLearnedStats(C.Structure):
                 ("lbvh_fallbacks", C.c_uint64), ("search_steps", C.c_uint64),
                 ("leaves", C.c_uint32), ("max_err", C.c_uint32),
                 ("leaves_over_window", C.c_uint32), ("trained", C.c_uint32),
-                ("root_a", C.c_double), ("root_b", C.c_double), ("mean_err", C.c_double),
+                ("root_shift", C.c_double), ("root_entries", C.c_double),
+                ("mean_err", C.c_double),
                 ("grad_norm_after", C.c_double), ("ms_build", C.c_double)]
 
 _lib = None

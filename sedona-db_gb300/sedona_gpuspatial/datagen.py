@@ -169,7 +169,9 @@ def workload4(n_probe=20_000_000, n_build=1_000_000, seed=None, k=8, distance=25
     bx, by = draw(n_build)
     px, py = draw(n_probe)
     return JoinInputs("knn8_dwithin25_20m_x_1m", points_column(bx, by),
-                      points_column(px, py), "knn", params={"k": k, "distance": distance})
+                      points_column(px, py), "knn",
+                      params={"k": k, "distance": distance, "build_xy": (bx, by),
+                              "probe_xy": (px, py)})
 
 
 def workload5(n_build=100_000_000, n_boxes=10_000_000, n_lookups=10_000_000, seed=None):
