@@ -47,6 +47,9 @@ struct SpjJoinConfig {
   uint32_t leaf_size;                      /* LBVH leaf size, 0 = default (4) */
   int32_t refine_form;                     /* SPJ_REFINE_* (default FAST_F32) */
   int32_t profile;                         /* 1: time phases with CUDA events */
+  int32_t probe_order; /* traversal order of probe rows: 0 = Morton order of the
+                          box centres from 65536 rows up, 1 = always, -1 = row
+                          order; the pairs and their order do not depend on it */
 };
 
 /* An Arrow binary (int32 offsets) or large_binary (int64 offsets) WKB column
@@ -232,6 +235,10 @@ int SpjKnnBuild(SpjKnn* knn, const double* xy, uint64_t n);
 int SpjKnnQuery(SpjKnn* knn, const double* probe_xy, uint64_t n_probe, uint32_t k,
                 uint32_t* out_idx, double* out_dist, int32_t device);
 void* SpjKnnStream(SpjKnn* knn);
+/* Cumulative counters since SpjKnnCreate: probe points queried, FP64
+ * distance keys evaluated, and probes whose k-set the FP32 pass could not
+ * prove (answered by the exact kernel). */
+int SpjKnnGetStats(SpjKnn* knn, uint64_t* queries, uint64_t* exact_evals, uint64_t* redone);
 
 /* ------------------------------------------------------------------------ */
 /* Probe without allocating.  No counterpart in the reference interface.     */

@@ -592,6 +592,8 @@ extern "C" int SpjJoinCreate(const SpjJoinConfig* config, SpjJoin** out) {
     ec.refine_form = config->refine_form;
     SPJ_CHECK(ec.refine_form == kPlainF64 || ec.refine_form == kFastF32, "unknown refine_form");
     ec.profile = config->profile != 0;
+    SPJ_CHECK(config->probe_order >= -1 && config->probe_order <= 1, "unknown probe_order");
+    ec.probe_order = config->probe_order;
     auto j = std::make_unique<SpjJoin>();
     j->rt = rt;
     j->engine = std::make_unique<JoinEngine>(rt->device_id, ec);
@@ -1034,6 +1036,16 @@ extern "C" int SpjKnnQuery(SpjKnn* k, const double* probe_xy, uint64_t n, uint32
 }
 
 extern "C" void* SpjKnnStream(SpjKnn* k) { return (void*)k->index->stream(); }
+
+extern "C" int SpjKnnGetStats(SpjKnn* k, uint64_t* queries, uint64_t* exact_evals,
+                              uint64_t* redone) {
+  return guarded(k->last_error, [&] {
+    SPJ_CHECK(queries && exact_evals && redone, "null output");
+    *queries = k->index->queries();
+    *exact_evals = k->index->exact_evals();
+    *redone = k->index->redone();
+  });
+}
 
 extern "C" int SpjHostRegister(void* ptr, uint64_t bytes) {
   cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);

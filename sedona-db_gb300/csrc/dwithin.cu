@@ -1,0 +1,180 @@
+// dwithin.cu — fused ST_DWithin traversal over point columns.
+#include "dwithin.cuh"
+#include "exact.cuh"
+
+#include <cstring>
+
+namespace spj {
+namespace {
+
+// Error bound of the split FP32 distance r = sqrt(d2) against the true
+// distance D of the FP64 points: |D - r| <= 2^-20 r + 2^-44 (max|b|_1 +
+// |q|_1) + 2^-120.  Per axis, with u = 2^-24: v = hi + lo + e, |e| <= 2^-48
+// |v|; the three FP32 roundings of (b.hi - q.hi) + (b.lo - q.lo) give
+// |dx - (b - q).x| <= 2u (1 + 2u) |dx| + 3 * 2^-48 (|b.x| + |q.x|); the two axes
+// add to <= 2^-22 |d| + 2^-46 (..); the square, sum and square root add
+// 2^-23 relative.  2^-20 covers the relative part twice over, 2^-44 the
+// absolute part four times over, 2^-120 FP32 results below the normal range.
+constexpr float kSplitUp = 1.00000095367431640625f;    // 1 + 2^-20
+constexpr float kSplitDown = 0.99999904632568359375f;  // 1 - 2^-20
+constexpr float kTwoM44 = 5.684341886080801486968994140625e-14f;
+constexpr float kTwoM120 = 7.5231638452626400509999138382223723380394595633413601376560e-37f;
+
+__global__ void k_split_points(const double2* __restrict__ pts, const uint32_t* __restrict__ ids,
+                               uint32_t m, double2* __restrict__ xy, float4* __restrict__ hl,
+                               unsigned* __restrict__ mag) {
+  unsigned bm = 0, big = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const double2 p = pts[ids[i]];
+    xy[i] = p;
+    const float hx = __double2float_rn(p.x), hy = __double2float_rn(p.y);
+    // v - RN32(v) is exact in FP64
+    hl[i] = make_float4(hx, hy, __double2float_rn(__dsub_rn(p.x, (double)hx)),
+                        __double2float_rn(__dsub_rn(p.y, (double)hy)));
+    const double ax = fabs(p.x), ay = fabs(p.y);
+    if (!(ax <= kSplitMaxCoord && ay <= kSplitMaxCoord)) big = 1;
+    else bm = max(bm, __float_as_uint(__double2float_ru(__dadd_ru(ax, ay))));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bm = max(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+    big |= __shfl_xor_sync(0xffffffffu, big, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative floats order as their bit patterns
+    if (bm) atomicMax(&mag[0], bm);
+    if (big) atomicOr(&mag[1], 1u);
+  }
+}
+
+template <bool kScatter>
+__global__ void __launch_bounds__(kTravThreads)
+    k_dwithin_fused(LbvhView t, const double2* __restrict__ bxy, const float4* __restrict__ bhl,
+                    float bmag, int split_ok, const float4* __restrict__ probe_box,
+                    const double2* __restrict__ probe_pt, uint32_t n, double d, float d_lo,
+                    float d_hi, const uint32_t* __restrict__ order, uint32_t* __restrict__ counts,
+                    const uint64_t* __restrict__ offs, uint32_t probe_base,
+                    uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
+                    uint64_t cap, DeviceStatus* st) {
+  __shared__ int stack[kTravStack * kTravThreads];
+  uint32_t esc = 0, tested = 0;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pi = order ? (int64_t)order[j] : j;
+    const float4 q = probe_box[pi];
+    uint32_t cnt = 0;
+    uint64_t pos = kScatter ? offs[pi] : 0;
+    if (q.x <= q.z && q.y <= q.w && t.nprims > 0) {
+      const double2 p = probe_pt[pi];
+      const bool split =
+          split_ok && fabs(p.x) <= kSplitMaxCoord && fabs(p.y) <= kSplitMaxCoord;
+      float hx = 0, hy = 0, lx = 0, ly = 0, cerr = 0;
+      if (split) {
+        hx = __double2float_rn(p.x);
+        hy = __double2float_rn(p.y);
+        lx = __double2float_rn(__dsub_rn(p.x, (double)hx));
+        ly = __double2float_rn(__dsub_rn(p.y, (double)hy));
+        cerr = __fadd_ru(__fmul_ru(__fadd_ru(bmag, __fadd_ru(fabsf(hx), fabsf(hy))), kTwoM44),
+                         kTwoM120);
+      }
+      lbvh_for_each_overlap(t, q, stack + threadIdx.x, [&](uint32_t k) {
+        tested++;
+        int r = -1;
+        if (split) {
+          const float4 h = bhl[k];
+          const float dx = __fadd_rn(__fsub_rn(h.x, hx), __fsub_rn(h.z, lx));
+          const float dy = __fadd_rn(__fsub_rn(h.y, hy), __fsub_rn(h.w, ly));
+          const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+          // D <= hi < d_lo <= d: RN(D) <= d.  D >= lo > d_hi >= d with lo a
+          // float above d_hi, so D exceeds d by an FP32 ulp: RN(D) > d.
+          if (__fadd_ru(__fmul_ru(__fsqrt_ru(d2), kSplitUp), cerr) < d_lo) r = 1;
+          else if (__fsub_rd(__fmul_rd(__fsqrt_rd(d2), kSplitDown), cerr) > d_hi) r = 0;
+        }
+        if (r < 0) {
+          esc++;
+          r = exact::dwithin_exact(bxy[k], p, d) ? 1 : 0;
+        }
+        if (r) {
+          if (kScatter) {
+            if (pos < cap) {
+              out_build[pos] = t.sorted_id[k];
+              out_probe[pos] = (uint32_t)pi + probe_base;
+            }
+            pos++;
+          } else {
+            cnt++;
+          }
+        }
+      });
+    }
+    if (!kScatter) counts[pi] = cnt;
+  }
+  if (!kScatter) {
+    for (int o = 16; o > 0; o >>= 1) {
+      esc += __shfl_xor_sync(0xffffffffu, esc, o);
+      tested += __shfl_xor_sync(0xffffffffu, tested, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (esc) atomicAdd(&st->counters[0], (unsigned long long)esc);
+      if (tested) atomicAdd(&st->counters[1], (unsigned long long)tested);
+    }
+  }
+}
+
+void float_neighbours(double d, float& lo, float& hi) {
+  lo = (float)d;
+  hi = (float)d;
+  if ((double)lo > d) lo = next_downf(lo);
+  if ((double)hi < d) hi = next_upf(hi);
+}
+
+}  // namespace
+
+void build_point_split(const double2* pts, const Lbvh& bvh, PointSplit& out, cudaStream_t s) {
+  const uint32_t m = bvh.nprims;
+  out.n = m;
+  out.xy.reserve(((size_t)m + 1) * 16, s);
+  out.hl.reserve(((size_t)m + 1) * 16, s);
+  out.tmp.reserve(8, s);
+  SPJ_CUDA(cudaMemsetAsync(out.tmp.get(), 0, 8, s));
+  if (m)
+    k_split_points<<<grid_for(m, 256), 256, 0, s>>>(pts, bvh.sorted_id.as<uint32_t>(), m,
+                                                    out.xy.as<double2>(), out.hl.as<float4>(),
+                                                    out.tmp.as<unsigned>());
+  SPJ_CUDA(cudaGetLastError());
+  unsigned mag[2];
+  SPJ_CUDA(cudaMemcpyAsync(mag, out.tmp.get(), 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  float b;
+  std::memcpy(&b, &mag[0], 4);
+  out.bmag = b;
+  out.ok = mag[1] == 0;
+}
+
+void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
+                   const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
+                   uint32_t* counts, DeviceStatus* st, cudaStream_t s) {
+  if (n == 0) return;
+  float lo, hi;
+  float_neighbours(d, lo, hi);
+  const int g = grid_for(n, kTravThreads, kNumSMs * 16);
+  k_dwithin_fused<false><<<g, kTravThreads, 0, s>>>(
+      t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
+      d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
+                     const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
+                     const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
+                     uint32_t* out_probe, uint64_t capacity, cudaStream_t s) {
+  if (n == 0) return;
+  float lo, hi;
+  float_neighbours(d, lo, hi);
+  const int g = grid_for(n, kTravThreads, kNumSMs * 16);
+  k_dwithin_fused<true><<<g, kTravThreads, 0, s>>>(
+      t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
+      d, lo, hi, order, nullptr, offs, probe_base, out_build, out_probe, capacity, nullptr);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+}  // namespace spj

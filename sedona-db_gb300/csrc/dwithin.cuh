@@ -1,0 +1,42 @@
+// dwithin.cuh — ST_DWithin between point columns, decided inside the LBVH
+// traversal: no candidate pairs are materialized.  The count pass and the
+// scatter pass run the same deterministic test on every (build point, probe
+// box) overlap the traversal finds, so the scatter writes exactly the counted
+// pairs, grouped by probe row, in the same order as the filter + refine +
+// compact path.
+//
+// Test per overlap: the FP32 distance of the (hi, lo) splits of both points
+// (v = hi + lo, hi = RN32(v), lo = RN32(v - hi)), whose error is at most
+// 2^-20 of the distance plus 2^-44 of the coordinate magnitude; a pair whose
+// error interval lies entirely below or above the FP32 neighbours of d is
+// decided, any other gets the exact correctly rounded hypot test.
+#pragma once
+#include "lbvh.cuh"
+
+namespace spj {
+
+// Build points in LBVH order: FP64, and FP32 (hi.x, hi.y, lo.x, lo.y).
+struct PointSplit {
+  uint32_t n = 0;
+  float bmag = 0;  // max |x| + |y| over the points, rounded up
+  bool ok = false; // every |coordinate| <= kSplitMaxCoord (FP32 squares stay finite)
+  DevBuf xy, hl, tmp;
+};
+constexpr double kSplitMaxCoord = 1e18;
+
+// pts: the build column's points (row order); bvh over their boxes.
+void build_point_split(const double2* pts, const Lbvh& bvh, PointSplit& out, cudaStream_t s);
+
+// The two passes.  probe_box: the probe points' boxes expanded by d
+// (expand_boxes); probe_pt: the probe points.  The count pass writes
+// counts[probe row] and adds the escalations / overlaps tested to
+// st->counters[0] / [1]; the scatter pass writes pairs at offs[probe row].
+void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
+                   const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
+                   uint32_t* counts, DeviceStatus* st, cudaStream_t s);
+void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
+                     const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
+                     const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
+                     uint32_t* out_probe, uint64_t capacity, cudaStream_t s);
+
+}  // namespace spj

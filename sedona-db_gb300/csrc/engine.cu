@@ -50,6 +50,7 @@ JoinEngine::~JoinEngine() {
   bg_ = DeviceGeoms();
   bsc_ = DecodeScratch();
   bvh_ = Lbvh();
+  bsplit_ = PointSplit();
   cudaStreamSynchronize(bs_);
   cudaStreamDestroy(bs_);
 }
@@ -60,14 +61,21 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
   decode_wkb(col, bg_, bsc_, false, s);
   if (bg_.nrings > 0) build_band_index(bg_, bsc_, s);
   build_lbvh(bg_.box.as<float4>(), bg_.n, cfg_.leaf_size, bvh_, s);
+  split_points();
   SPJ_CUDA(cudaStreamSynchronize(s));
   built_ = true;
+}
+
+void JoinEngine::split_points() {
+  bsplit_.n = 0;
+  if (bg_.all_points && bvh_.nprims > 0) build_point_split(bg_.pt.as<double2>(), bvh_, bsplit_, bs_);
 }
 
 void JoinEngine::reindex(uint32_t leaf_size) {
   SPJ_CHECK(built_, "reindex before the build side was finished");
   cfg_.leaf_size = leaf_size;
   build_lbvh(bg_.box.as<float4>(), bg_.n, leaf_size, bvh_, bs_);
+  split_points();
   SPJ_CUDA(cudaStreamSynchronize(bs_));
 }
 
@@ -110,12 +118,68 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     launches++;
   }
   const LbvhView tv = bvh_.view();
-  const uint64_t m = probe_count(tv, boxes, n, ws.psc, s);  // syncs
+  const uint32_t* order = nullptr;
+  if (cfg_.probe_order > 0 || (cfg_.probe_order == 0 && n >= kOrderMinRows)) {
+    order = probe_order(tv, boxes, n, ws.psc, s);
+    if (order) launches += 21;  // keys + 4 radix passes (histogram, 3-kernel scan, scatter)
+  }
+  if (predicate == kPredDWithin && cfg_.refine_form == kFastF32 && bsplit_.n == bvh_.nprims &&
+      bvh_.nprims > 0) {
+    // point build and probe sides: the distance test runs inside the
+    // traversal, no candidate pairs are materialized
+    reset_status(ws.status, s);
+    ws.psc.counts.reserve(((size_t)n + 1) * 4, s);
+    ws.psc.offsets.reserve(((size_t)n + 1) * 8, s);
+    const double2* ppt = ws.probe.pt.as<double2>();
+    dwithin_count(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.counts.as<uint32_t>(),
+                  ws.status.as<DeviceStatus>(), s);
+    scan_u32_u64(ws.psc.counts.as<uint32_t>(), ws.psc.offsets.as<uint64_t>(), n, ws.psc.tmp, s);
+    uint64_t total = 0;
+    DeviceStatus hst;
+    SPJ_CUDA(cudaMemcpyAsync(&total, ws.psc.offsets.as<uint64_t>() + n, 8,
+                             cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaMemcpyAsync(&hst, ws.status.get(), sizeof hst, cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
+    ws.out_build.reserve((total + 1) * 4, s);
+    ws.out_probe.reserve((total + 1) * 4, s);
+    dwithin_scatter(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.offsets.as<uint64_t>(),
+                    probe_base, ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), total,
+                    s);
+    launches += 5;
+    if (prof) {
+      SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
+      SPJ_CUDA(cudaEventRecord(ws.ev[4], s));
+    }
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    {
+      std::lock_guard<std::mutex> lk(stats_mu_);
+      stats_.calls++;
+      stats_.probe_rows += n;
+      stats_.candidates += hst.counters[1];
+      stats_.results += total;
+      stats_.escalations += hst.counters[0];
+      stats_.pairs_evaluated += hst.counters[1];
+      stats_.kernel_launches += launches;
+      stats_.probe_bytes +=
+          (uint64_t)col.data_len + (uint64_t)(col.n + 1) * (col.offsets64 ? 8 : 4);
+      if (prof) {
+        stats_.ms_decode += ev_ms(ws.ev[0], ws.ev[1]);
+        stats_.ms_filter += ev_ms(ws.ev[1], ws.ev[2]);
+        stats_.ms_refine += ev_ms(ws.ev[2], ws.ev[3]);
+        stats_.ms_compact += ev_ms(ws.ev[3], ws.ev[4]);
+      }
+    }
+    *d_build = ws.out_build.as<uint32_t>();
+    *d_probe = ws.out_probe.as<uint32_t>();
+    return total;
+  }
+  const uint64_t m = probe_count(tv, boxes, n, ws.psc, s, order);  // syncs
   SPJ_CHECK(m < (1ull << 34), "candidate pair count too large");
   ws.cand_build.reserve((m + 1) * 4, s);
   ws.cand_probe.reserve((m + 1) * 4, s);
   probe_scatter(tv, boxes, n, ws.psc, probe_base, ws.cand_build.as<uint32_t>(),
-                ws.cand_probe.as<uint32_t>(), s);
+                ws.cand_probe.as<uint32_t>(), s, order);
   launches += 5;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
 

@@ -11,6 +11,7 @@
 #include <mutex>
 
 #include "geoms.cuh"
+#include "dwithin.cuh"
 #include "lbvh.cuh"
 #include "refine.cuh"
 
@@ -22,7 +23,11 @@ struct EngineConfig {
   uint32_t leaf_size = 4;
   int refine_form = kFastF32;
   bool profile = false;  // time each phase with CUDA events on the engine stream
+  // traversal order of the probe rows: 0 = Morton order from kOrderMinRows
+  // rows up, 1 = always Morton order, -1 = row order
+  int probe_order = 0;
 };
+constexpr uint32_t kOrderMinRows = 1u << 16;
 
 // Per-phase device time (CUDA events on the launching stream) and counters.
 struct JoinStats {
@@ -85,11 +90,13 @@ class JoinEngine {
   void reset_stats();
 
  private:
+  void split_points();
   int device_;
   EngineConfig cfg_;
   DeviceGeoms bg_;
   DecodeScratch bsc_;
   Lbvh bvh_;
+  PointSplit bsplit_;  // point build sides: ST_DWithin decided in the traversal
   cudaStream_t bs_ = nullptr;  // build stream; owns the frees of bg_/bsc_/bvh_
   bool built_ = false;
   std::mutex stats_mu_;

@@ -1,13 +1,22 @@
 // knn.cu — KNN join: LBVH over the build points, depth-first traversal
-// nearest child first, a register-resident k-best list per probe thread.
+// nearest child first, a register-resident best list per probe thread,
+// probes taken in Morton order of their coordinates.
 //
 // Ranking key: the exact squared distance dx^2 + dy^2 of the FP64 deltas
 // dx = RN(b.x - p.x), dy = RN(b.y - p.y) (the deltas the reference's
 // Euclidean distance forms), held as a normalized double-double (hi, lo) and
 // compared lexicographically, then by build id.  Exact duplicates tie on the
 // key and fall back to the build id, as in the reference ground truth.
-// Chosen form: node pruning and point rejection in FP32 with a static error
-// bound; only points that may enter the k-best list get the FP64 key.
+//
+// Chosen form (k <= 16): every coordinate is split into an FP32 pair
+// hi = RN32(v), lo = RN32(v - hi), and the traversal ranks points by the FP32
+// squared distance of (b.hi - q.hi) + (b.lo - q.lo), whose error is a few
+// ulps of the distance itself plus 2^-44 of the coordinate magnitude (the
+// bound is derived at kSplitRel below).  It keeps the k+1 best; when the
+// (k+1)-th is provably farther than each of the first k (their error
+// intervals are disjoint), the k-set is exact, and only those k points get
+// the FP64 key that orders them.  Probes whose k-set is not proven this way
+// (near ties at rank k, exact duplicates) are queued for the exact kernel.
 // Plain form: every visited point gets the FP64 key.
 #include "knn.cuh"
 #include "prims.cuh"
@@ -20,6 +29,21 @@ namespace {
 
 constexpr int kKnnThreads = 128;
 constexpr int kKnnStack = 64;
+
+// |true distance - sqrt(d2)| <= kSplitRel * sqrt(d2) + cerr, cerr =
+// 2^-44 (max|b.x|+|b.y| + |q.x|+|q.y|) + 2^-120, for the split FP32 distance
+// d2.  Per axis, with u = 2^-24: b = hi + lo + e, |e| <= 2^-48 |b|; the three
+// FP32 roundings give |dx - (b - q).x| <= 2u |dx| (1 + 2u) + 3 * 2^-48 (|b.x| +
+// |q.x|); the two axes add to <= 2^-22 * |d| + 2^-46 (..); squaring, summing
+// and the square root add 2^-23 relative.  kSplitRel = 2^-20 covers the
+// relative part twice over, 2^-44 the absolute part four times over, and
+// 2^-120 the absolute error of FP32 results below the normal range.
+constexpr float kSplitUp = 1.00000095367431640625f;    // 1 + 2^-20
+constexpr float kSplitDown = 0.99999904632568359375f;  // 1 - 2^-20
+constexpr float kTwoM44 = 5.684341886080801486968994140625e-14f;
+constexpr float kTwoM120 = 7.5231638452626400509999138382223723380394595633413601376560e-37f;
+// coordinates up to this magnitude keep every split FP32 square finite
+constexpr double kSplitMaxCoord = 1e18;
 
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
   s = __dadd_rn(a, b);
@@ -52,19 +76,29 @@ __device__ __forceinline__ float box_dist(float2 q, float4 b) {
   return __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
 }
 
+__device__ __forceinline__ void write_empty(uint32_t* out_idx, double* out_dist, uint64_t qi,
+                                            uint32_t k) {
+  for (uint32_t j = 0; j < k; j++) {
+    out_idx[qi * k + j] = 0xFFFFFFFFu;
+    out_dist[qi * k + j] = INFINITY;
+  }
+}
+
+// Exact kernel.  With `order`, thread slot j serves probe order[j]; with
+// n_dev, the slot count is read from device memory (the queue the split
+// kernel filled).
 template <int K, bool kFast>
 __global__ void __launch_bounds__(kKnnThreads)
     k_knn(LbvhView t, const double2* __restrict__ bxy, const double2* __restrict__ probe,
-          uint64_t n, uint32_t k, float slack, uint32_t* __restrict__ out_idx,
-          double* __restrict__ out_dist, unsigned long long* __restrict__ exact_evals) {
+          uint64_t n, const uint32_t* __restrict__ order, const uint32_t* __restrict__ n_dev,
+          uint32_t k, float slack, uint32_t* __restrict__ out_idx, double* __restrict__ out_dist,
+          unsigned long long* __restrict__ exact_evals) {
   __shared__ int stack[kKnnStack * kKnnThreads];
   uint32_t evals = 0;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  const uint64_t trips = (n + stride - 1) / stride;
-  for (uint64_t tr = 0; tr < trips; tr++) {
-    const uint64_t qi = start + tr * stride;
-    if (qi >= n) continue;
+  const uint64_t nn = n_dev ? (uint64_t)*n_dev : n;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < nn;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t qi = order ? (uint64_t)order[j] : j;
     const double2 q = probe[qi];
     const float2 q32 = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
     // |q - q32| bound, plus the build-side bound
@@ -72,10 +106,10 @@ __global__ void __launch_bounds__(kKnnThreads)
     double kh[K], kl[K];
     uint32_t ki[K];
 #pragma unroll
-    for (int j = 0; j < K; j++) {
-      kh[j] = INFINITY;
-      kl[j] = 0;
-      ki[j] = 0xFFFFFFFFu;
+    for (int c = 0; c < K; c++) {
+      kh[c] = INFINITY;
+      kl[c] = 0;
+      ki[c] = 0xFFFFFFFFu;
     }
     uint32_t have = 0;
     float bound = INFINITY;  // FP32 upper bound of the k-th best distance
@@ -107,16 +141,16 @@ __global__ void __launch_bounds__(kKnnThreads)
           // insert into the sorted register list
           bool placed = false;
 #pragma unroll
-          for (int j = K - 1; j > 0; j--) {
+          for (int c2 = K - 1; c2 > 0; c2--) {
             if (!placed) {
-              if (key_less(h, l, id, kh[j - 1], kl[j - 1], ki[j - 1])) {
-                kh[j] = kh[j - 1];
-                kl[j] = kl[j - 1];
-                ki[j] = ki[j - 1];
+              if (key_less(h, l, id, kh[c2 - 1], kl[c2 - 1], ki[c2 - 1])) {
+                kh[c2] = kh[c2 - 1];
+                kl[c2] = kl[c2 - 1];
+                ki[c2] = ki[c2 - 1];
               } else {
-                kh[j] = h;
-                kl[j] = l;
-                ki[j] = id;
+                kh[c2] = h;
+                kl[c2] = l;
+                ki[c2] = id;
                 placed = true;
               }
             }
@@ -131,8 +165,8 @@ __global__ void __launch_bounds__(kKnnThreads)
             // k-th entry of the list sits at index k-1 (k <= K)
             double kth = kh[K - 1];
 #pragma unroll
-            for (int j = 0; j < K; j++)
-              if (j == (int)k - 1) kth = __dadd_rn(kh[j], kl[j]);
+            for (int c2 = 0; c2 < K; c2++)
+              if (c2 == (int)k - 1) kth = __dadd_rn(kh[c2], kl[c2]);
             bound = __double2float_ru(sqrt(kth) * (1.0 + 1e-12));
           }
         }
@@ -166,17 +200,194 @@ __global__ void __launch_bounds__(kKnnThreads)
       sp--;
       node = sp < kKnnStack ? stack[sp * kKnnThreads + threadIdx.x] : 0;
     }
-    for (uint32_t j = 0; j < k; j++) {
+    for (uint32_t c = 0; c < k; c++) {
       uint32_t id = 0xFFFFFFFFu;
       double d = INFINITY;
 #pragma unroll
-      for (int jj = 0; jj < K; jj++)
-        if (jj == (int)j && jj < (int)have) {
-          id = ki[jj];
-          d = sqrt(__dadd_rn(kh[jj], kl[jj]));
+      for (int cc = 0; cc < K; cc++)
+        if (cc == (int)c && cc < (int)have) {
+          id = ki[cc];
+          d = sqrt(__dadd_rn(kh[cc], kl[cc]));
         }
-      out_idx[qi * k + j] = id;
-      out_dist[qi * k + j] = d;
+      out_idx[qi * k + c] = id;
+      out_dist[qi * k + c] = d;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
+  if ((threadIdx.x & 31) == 0 && evals) atomicAdd(exact_evals, (unsigned long long)evals);
+}
+
+// Split-FP32 kernel (chosen form): see the file comment.  hl[pi] holds the
+// sorted build point pi as (hi.x, hi.y, lo.x, lo.y); bmag bounds |b.x|+|b.y|
+// over the build side.  Probes whose k-set is not proven are appended to
+// redo[] (count in *nredo) and their outputs left to the exact kernel.
+template <int K>
+__global__ void __launch_bounds__(kKnnThreads)
+    k_knn_split(LbvhView t, const float4* __restrict__ hl, const double2* __restrict__ bxy,
+                const double2* __restrict__ probe, uint64_t n, const uint32_t* __restrict__ order,
+                uint32_t k, float slack, float bmag, uint32_t* __restrict__ out_idx,
+                double* __restrict__ out_dist, uint32_t* __restrict__ redo,
+                uint32_t* __restrict__ nredo, unsigned long long* __restrict__ exact_evals) {
+  __shared__ int stack[kKnnStack * kKnnThreads];
+  uint32_t evals = 0;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t qi = order ? (uint64_t)order[j] : j;
+    const double2 q = probe[qi];
+    if (isnan(q.x) || isnan(q.y) || t.nprims == 0) {
+      write_empty(out_idx, out_dist, qi, k);
+      continue;
+    }
+    if (!(fabs(q.x) <= kSplitMaxCoord && fabs(q.y) <= kSplitMaxCoord)) {
+      redo[atomicAdd(nredo, 1u)] = (uint32_t)qi;
+      continue;
+    }
+    const float qhx = __double2float_rn(q.x), qhy = __double2float_rn(q.y);
+    // q - RN32(q) is exact in FP64
+    const float qlx = __double2float_rn(__dsub_rn(q.x, (double)qhx));
+    const float qly = __double2float_rn(__dsub_rn(q.y, (double)qhy));
+    const float2 q32 = make_float2(qhx, qhy);
+    const float qs = __fadd_ru(__fmul_ru(fabsf(qhx) + fabsf(qhy), 1.1920929e-07f), slack);
+    const float cerr =
+        __fadd_ru(__fmul_ru(__fadd_ru(bmag, __fadd_ru(fabsf(qhx), fabsf(qhy))), kTwoM44),
+                  kTwoM120);
+    // the K+1 smallest split distances seen, ascending
+    float ld[K + 1];
+    uint32_t lp[K + 1];
+#pragma unroll
+    for (int c = 0; c <= K; c++) {
+      ld[c] = INFINITY;
+      lp[c] = 0xFFFFFFFFu;
+    }
+    uint32_t have = 0;       // list entries, capped at k + 1
+    float bound = INFINITY;  // upper bound of the true distance of the (k+1)-th entry
+    int sp = 0;
+    int node = t.nleaves > 1 ? 0 : ~0;
+    while (true) {
+      if (node < 0) {
+        const uint32_t c = (uint32_t)(~node);
+        const uint32_t b0 = c * t.leaf_size, b1 = min(b0 + t.leaf_size, t.nprims);
+        for (uint32_t pi = b0; pi < b1; pi++) {
+          const float4 h = hl[pi];
+          const float dx = __fadd_rn(__fsub_rn(h.x, qhx), __fsub_rn(h.z, qlx));
+          const float dy = __fadd_rn(__fsub_rn(h.y, qhy), __fsub_rn(h.w, qly));
+          const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+          if (!(d2 < ld[K])) continue;
+          bool placed = false;
+#pragma unroll
+          for (int c2 = K; c2 > 0; c2--) {
+            if (!placed) {
+              if (d2 < ld[c2 - 1]) {
+                ld[c2] = ld[c2 - 1];
+                lp[c2] = lp[c2 - 1];
+              } else {
+                ld[c2] = d2;
+                lp[c2] = pi;
+                placed = true;
+              }
+            }
+          }
+          if (!placed) {
+            ld[0] = d2;
+            lp[0] = pi;
+          }
+          if (have <= k) have++;
+          if (have > k) {
+            float dk1 = ld[K];
+#pragma unroll
+            for (int c2 = 0; c2 <= K; c2++)
+              if (c2 == (int)k) dk1 = ld[c2];
+            bound = __fadd_ru(__fmul_ru(__fsqrt_ru(dk1), kSplitUp), cerr);
+          }
+        }
+      } else {
+        const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+        const int2 ch = t.node_child[node];
+        const float dl = __fsub_rd(__fmul_rd(box_dist(q32, lb), 0.99999905f), qs);
+        const float dr = __fsub_rd(__fmul_rd(box_dist(q32, rb), 0.99999905f), qs);
+        const bool vl = dl <= bound, vr = dr <= bound;
+        if (vl && vr) {
+          const int nearc = dl <= dr ? ch.x : ch.y;
+          const int farc = dl <= dr ? ch.y : ch.x;
+          if (sp < kKnnStack) stack[sp * kKnnThreads + threadIdx.x] = farc;
+          sp++;
+          node = nearc;
+          continue;
+        }
+        if (vl) {
+          node = ch.x;
+          continue;
+        }
+        if (vr) {
+          node = ch.y;
+          continue;
+        }
+      }
+      if (sp == 0) break;
+      sp--;
+      node = sp < kKnnStack ? stack[sp * kKnnThreads + threadIdx.x] : 0;
+    }
+    // With fewer than k+1 entries the bound never closed, so every build
+    // point was visited and listed.  Otherwise the k-set is proven when the
+    // (k+1)-th entry's lower bound exceeds the k-th entry's upper bound (the
+    // list is ascending, so the k-th bounds the first k).
+    if (have > k) {
+      float dk = ld[0], dk1 = ld[0];
+#pragma unroll
+      for (int c = 0; c <= K; c++) {
+        if (c == (int)k - 1) dk = ld[c];
+        if (c == (int)k) dk1 = ld[c];
+      }
+      const float up = __fadd_ru(__fmul_ru(__fsqrt_ru(dk), kSplitUp), cerr);
+      const float lo = __fsub_rd(__fmul_rd(__fsqrt_rd(dk1), kSplitDown), cerr);
+      if (!(lo > up)) {
+        redo[atomicAdd(nredo, 1u)] = (uint32_t)qi;
+        continue;
+      }
+    }
+    // exact keys of the proven set, ordered by (key, build id)
+    const uint32_t kk = min(k, have);
+    double kh[K], kl[K];
+    uint32_t ki[K];
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+      kh[c] = INFINITY;
+      kl[c] = 0;
+      ki[c] = 0xFFFFFFFFu;
+      if (c < (int)kk) {
+        sq_dist_dd(bxy[lp[c]], q, kh[c], kl[c]);
+        ki[c] = t.sorted_id[lp[c]];
+      }
+    }
+    evals += kk;
+    // odd-even transposition sort (K rounds)
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+#pragma unroll
+      for (int c = r & 1; c + 1 < K; c += 2) {
+        if (key_less(kh[c + 1], kl[c + 1], ki[c + 1], kh[c], kl[c], ki[c])) {
+          const double th = kh[c], tl = kl[c];
+          const uint32_t ti = ki[c];
+          kh[c] = kh[c + 1];
+          kl[c] = kl[c + 1];
+          ki[c] = ki[c + 1];
+          kh[c + 1] = th;
+          kl[c + 1] = tl;
+          ki[c + 1] = ti;
+        }
+      }
+    }
+    for (uint32_t c = 0; c < k; c++) {
+      uint32_t id = 0xFFFFFFFFu;
+      double d = INFINITY;
+#pragma unroll
+      for (int cc = 0; cc < K; cc++)
+        if (cc == (int)c && cc < (int)kk) {
+          id = ki[cc];
+          d = sqrt(__dadd_rn(kh[cc], kl[cc]));
+        }
+      out_idx[qi * k + c] = id;
+      out_dist[qi * k + c] = d;
     }
   }
   for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
@@ -193,10 +404,16 @@ __global__ void k_points_to_boxes(const double2* __restrict__ xy, uint64_t n,
   }
 }
 
+// sorted FP64 points and their (hi, lo) FP32 splits
 __global__ void k_gather_xy(const double2* __restrict__ xy, const uint32_t* __restrict__ ids,
-                            uint32_t m, double2* __restrict__ out) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
-    out[i] = xy[ids[i]];
+                            uint32_t m, double2* __restrict__ out, float4* __restrict__ hl) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const double2 p = xy[ids[i]];
+    out[i] = p;
+    const float hx = __double2float_rn(p.x), hy = __double2float_rn(p.y);
+    hl[i] = make_float4(hx, hy, __double2float_rn(__dsub_rn(p.x, (double)hx)),
+                        __double2float_rn(__dsub_rn(p.y, (double)hy)));
+  }
 }
 
 }  // namespace
@@ -210,10 +427,13 @@ KnnIndex::~KnnIndex() {
     cudaStreamSynchronize(stream_);
     bvh_ = Lbvh();
     xy_sorted_.release();
+    xy_split_.release();
     probe_.release();
     oidx_.release();
     odist_.release();
     counters_.release();
+    redo_.release();
+    osc_ = ProbeScratch();
     cudaStreamSynchronize(stream_);
     cudaStreamDestroy(stream_);
   }
@@ -230,22 +450,35 @@ void KnnIndex::build(const double* xy_host, uint64_t n) {
                                                                boxes.as<float4>());
   build_lbvh(boxes.as<float4>(), (uint32_t)n, leaf_size_, bvh_, s);
   xy_sorted_.reserve(((size_t)bvh_.nprims + 1) * 16, s);
+  xy_split_.reserve(((size_t)bvh_.nprims + 1) * 16, s);
   if (bvh_.nprims)
     k_gather_xy<<<grid_for(bvh_.nprims, 256), 256, 0, s>>>(
-        xy.as<double2>(), bvh_.sorted_id.as<uint32_t>(), bvh_.nprims, xy_sorted_.as<double2>());
+        xy.as<double2>(), bvh_.sorted_id.as<uint32_t>(), bvh_.nprims, xy_sorted_.as<double2>(),
+        xy_split_.as<float4>());
   // |p - RN32(p)| <= 2^-24 (|x| + |y|) <= 2^-24 * 2 * max|coord|
-  double mx = 0;
-  for (uint64_t i = 0; i < 2 * n; i++) {
-    double v = std::fabs(xy_host[i]);
-    if (v > mx && std::isfinite(v)) mx = v;
+  double mx = 0, l1 = 0;
+  bool split_ok = true;
+  for (uint64_t i = 0; i < n; i++) {
+    const double x = xy_host[2 * i], y = xy_host[2 * i + 1];
+    if (std::isnan(x) || std::isnan(y)) continue;  // left out of the tree
+    const double ax = std::fabs(x), ay = std::fabs(y);
+    if (!(ax <= kSplitMaxCoord && ay <= kSplitMaxCoord)) split_ok = false;
+    if (std::isfinite(ax) && ax > mx) mx = ax;
+    if (std::isfinite(ay) && ay > mx) mx = ay;
+    if (std::isfinite(ax + ay) && ax + ay > l1) l1 = ax + ay;
   }
   slack_ = (float)(mx * 2.0 * std::ldexp(1.0, -23));
+  split_ok_ = split_ok;
+  // rounded up so that it bounds max(|x| + |y|)
+  bmag_ = (float)l1;
+  if ((double)bmag_ < l1) bmag_ = std::nextafter(bmag_, INFINITY);
   SPJ_CUDA(cudaStreamSynchronize(s));
 }
 
 void KnnIndex::query(const double* probe_xy, uint64_t n, uint32_t k, uint32_t* out_idx,
                      double* out_dist, bool device_ptrs) {
   SPJ_CHECK(k >= 1 && k <= 32, "k must be in [1, 32]");
+  SPJ_CHECK(n < 0xFFFFFFFFull, "too many probe points");
   cudaStream_t s = stream_;
   const double2* dp;
   uint32_t* di;
@@ -264,36 +497,61 @@ void KnnIndex::query(const double* probe_xy, uint64_t n, uint32_t k, uint32_t* o
     dd = odist_.as<double>();
   }
   counters_.reserve(16, s);
-  SPJ_CUDA(cudaMemsetAsync(counters_.get(), 0, 8, s));
+  SPJ_CUDA(cudaMemsetAsync(counters_.get(), 0, 16, s));
   if (n) {
     const LbvhView t = bvh_.view();
+    const uint32_t* order = point_order(t, dp, (uint32_t)n, osc_, s);
     const int g = grid_for((int64_t)n, kKnnThreads, kNumSMs * 16);
     auto* ev = counters_.as<unsigned long long>();
-#define SPJ_KNN_LAUNCH(KK)                                                                    \
-  if (form_ == 1)                                                                             \
-    k_knn<KK, true><<<g, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, k, slack_,  \
-                                              di, dd, ev);                                    \
-  else                                                                                        \
-    k_knn<KK, false><<<g, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, k, slack_, \
-                                               di, dd, ev);
-    if (k <= 8) {
-      SPJ_KNN_LAUNCH(8)
-    } else if (k <= 16) {
-      SPJ_KNN_LAUNCH(16)
+    uint32_t* nredo = reinterpret_cast<uint32_t*>(ev + 1);
+    if (form_ == 1 && k <= 16 && split_ok_) {
+      redo_.reserve((n + 1) * 4, s);
+      uint32_t* redo = redo_.as<uint32_t>();
+      if (k <= 8)
+        k_knn_split<8><<<g, kKnnThreads, 0, s>>>(t, xy_split_.as<float4>(),
+                                                 xy_sorted_.as<double2>(), dp, n, order, k,
+                                                 slack_, bmag_, di, dd, redo, nredo, ev);
+      else
+        k_knn_split<16><<<g, kKnnThreads, 0, s>>>(t, xy_split_.as<float4>(),
+                                                  xy_sorted_.as<double2>(), dp, n, order, k,
+                                                  slack_, bmag_, di, dd, redo, nredo, ev);
+      // the queued probes through the exact kernel (slot count read on the device)
+      const int gr = grid_for((int64_t)n, kKnnThreads, kNumSMs * 4);
+      if (k <= 8)
+        k_knn<8, false><<<gr, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, redo,
+                                                   nredo, k, slack_, di, dd, ev);
+      else
+        k_knn<16, false><<<gr, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, redo,
+                                                    nredo, k, slack_, di, dd, ev);
     } else {
-      SPJ_KNN_LAUNCH(32)
-    }
+#define SPJ_KNN_LAUNCH(KK)                                                                       \
+  if (form_ == 1)                                                                                \
+    k_knn<KK, true><<<g, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, order, nullptr, \
+                                              k, slack_, di, dd, ev);                            \
+  else                                                                                           \
+    k_knn<KK, false><<<g, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, order,        \
+                                               nullptr, k, slack_, di, dd, ev);
+      if (k <= 8) {
+        SPJ_KNN_LAUNCH(8)
+      } else if (k <= 16) {
+        SPJ_KNN_LAUNCH(16)
+      } else {
+        SPJ_KNN_LAUNCH(32)
+      }
 #undef SPJ_KNN_LAUNCH
+    }
     SPJ_CUDA(cudaGetLastError());
   }
   if (!device_ptrs && n) {
     SPJ_CUDA(cudaMemcpyAsync(out_idx, di, n * k * 4, cudaMemcpyDeviceToHost, s));
     SPJ_CUDA(cudaMemcpyAsync(out_dist, dd, n * k * 8, cudaMemcpyDeviceToHost, s));
   }
-  unsigned long long ev = 0;
-  SPJ_CUDA(cudaMemcpyAsync(&ev, counters_.get(), 8, cudaMemcpyDeviceToHost, s));
+  unsigned long long cnt[2] = {0, 0};
+  SPJ_CUDA(cudaMemcpyAsync(cnt, counters_.get(), 16, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
-  exact_evals_ += ev;
+  exact_evals_ += cnt[0];
+  redone_ += (uint32_t)cnt[1];
+  queries_ += n;
 }
 
 }  // namespace spj

@@ -17,6 +17,9 @@ class KnnIndex {
              bool device_ptrs);
   cudaStream_t stream() const { return stream_; }
   uint64_t exact_evals() const { return exact_evals_; }
+  // probes whose k-set the split FP32 pass did not prove (sent to the exact kernel)
+  uint64_t redone() const { return redone_; }
+  uint64_t queries() const { return queries_; }
 
  private:
   uint32_t leaf_size_;
@@ -25,9 +28,13 @@ class KnnIndex {
   uint64_t n_ = 0;
   Lbvh bvh_;
   DevBuf xy_sorted_;  // build points in LBVH order
+  DevBuf xy_split_;   // the same as FP32 (hi.x, hi.y, lo.x, lo.y)
   float slack_ = 0;   // bound on |p - RN32(p)| over the build side
-  DevBuf probe_, oidx_, odist_, counters_;
-  uint64_t exact_evals_ = 0;
+  float bmag_ = 0;    // max |x| + |y| over the build side (rounded up)
+  bool split_ok_ = true;  // build coordinates within the split pass's range
+  DevBuf probe_, oidx_, odist_, counters_, redo_;
+  ProbeScratch osc_;  // Morton order of the probes
+  uint64_t exact_evals_ = 0, redone_ = 0, queries_ = 0;
 };
 
 }  // namespace spj

@@ -10,10 +10,6 @@ __device__ __forceinline__ bool box_valid(float4 b) {
   return b.x <= b.z && b.y <= b.w;  // false for NaN
 }
 
-__device__ __forceinline__ bool overlap(float4 a, float4 b) {
-  return !(a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y);
-}
-
 __device__ __forceinline__ float4 box_union(float4 a, float4 b) {
   return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w));
 }
@@ -176,67 +172,35 @@ __global__ void k_refit(const float4* __restrict__ sbox, uint32_t m, uint32_t L,
 // ---------------------------------------------------------------------------
 // traversal
 
-constexpr int kTravThreads = 128;
-constexpr int kStack = 64;
-
 template <bool kScatter>
 __global__ void __launch_bounds__(kTravThreads)
     k_probe(LbvhView t, const float4* __restrict__ probe_box, uint32_t nprobe,
             uint32_t* __restrict__ counts, const uint64_t* __restrict__ offs, uint32_t probe_base,
             uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
-            uint64_t cap = ~0ull) {
-  // per-thread stack in shared memory, [depth][thread] so a warp's pushes hit
-  // 32 distinct banks
-  __shared__ int stack[kStack * kTravThreads];
-  for (int64_t pi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pi < nprobe;
-       pi += (int64_t)gridDim.x * blockDim.x) {
+            uint64_t cap = ~0ull, const uint32_t* __restrict__ order = nullptr) {
+  __shared__ int stack[kTravStack * kTravThreads];
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nprobe;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    // with an order, thread slot j takes the j-th probe in Morton order of the
+    // box centres: a warp's 32 traversals then visit neighbouring subtrees
+    // (less divergence, node boxes shared through L1).  Counts and offsets
+    // stay indexed by probe row, so the output layout does not change.
+    const int64_t pi = order ? (int64_t)order[j] : j;
     const float4 q = probe_box[pi];
     uint32_t cnt = 0;
     uint64_t pos = kScatter ? offs[pi] : 0;
     if (box_valid(q) && t.nprims > 0) {
-      int sp = 0;
-      int node = t.nleaves > 1 ? 0 : ~0;  // root: internal node 0, or the single leaf
-      while (true) {
-        if (node < 0) {
-          const uint32_t c = (uint32_t)(~node);
-          const uint32_t b0 = c * t.leaf_size;
-          const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
-          for (uint32_t k = b0; k < b1; k++) {
-            if (overlap(t.sorted_box[k], q)) {
-              if (kScatter) {
-                if (pos < cap) {  // writes bounded by the output capacity
-                  out_build[pos] = t.sorted_id[k];
-                  out_probe[pos] = (uint32_t)pi + probe_base;
-                }
-                pos++;
-              } else {
-                cnt++;
-              }
-            }
+      lbvh_for_each_overlap(t, q, stack + threadIdx.x, [&](uint32_t k) {
+        if (kScatter) {
+          if (pos < cap) {  // writes bounded by the output capacity
+            out_build[pos] = t.sorted_id[k];
+            out_probe[pos] = (uint32_t)pi + probe_base;
           }
+          pos++;
         } else {
-          const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
-          const int2 ch = t.node_child[node];
-          const bool hl = overlap(lb, q), hr = overlap(rb, q);
-          if (hl && hr) {
-            if (sp < kStack) stack[sp * kTravThreads + threadIdx.x] = ch.y;
-            sp++;
-            node = ch.x;
-            continue;
-          }
-          if (hl) {
-            node = ch.x;
-            continue;
-          }
-          if (hr) {
-            node = ch.y;
-            continue;
-          }
+          cnt++;
         }
-        if (sp == 0) break;
-        sp--;
-        node = sp < kStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
-      }
+      });
     }
     if (!kScatter) counts[pi] = cnt;
   }
@@ -268,7 +232,89 @@ __global__ void k_expand(const double2* __restrict__ pts, const float4* __restri
   }
 }
 
+// The tree's root box and the scale of a 16-bit grid over it.
+struct RootGrid {
+  float4 r;
+  float sx, sy;
+  __device__ explicit RootGrid(const LbvhView& t) {
+    if (t.nleaves > 1) {
+      r = box_union(t.node_box[0], t.node_box[1]);
+    } else {
+      r = t.sorted_box[0];
+      for (uint32_t k = 1; k < t.nprims; k++) r = box_union(r, t.sorted_box[k]);
+    }
+    sx = r.z > r.x ? 65535.0f / (r.z - r.x) : 0.0f;
+    sy = r.w > r.y ? 65535.0f / (r.w - r.y) : 0.0f;
+  }
+  __device__ uint32_t key(float cx, float cy) const {
+    const uint32_t qx = (uint32_t)fminf(fmaxf((cx - r.x) * sx, 0.0f), 65535.0f);
+    const uint32_t qy = (uint32_t)fminf(fmaxf((cy - r.y) * sy, 0.0f), 65535.0f);
+    return (spread16(qy) << 1) | spread16(qx);
+  }
+};
+
+// Morton key (16 bits per axis) of each probe box centre over the tree's
+// root box, with the probe row as the value; empty (NaN) boxes sort last.
+__global__ void k_probe_keys(LbvhView t, const float4* __restrict__ probe_box, uint32_t n,
+                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const RootGrid g(t);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 b = probe_box[i];
+    keys[i] = box_valid(b) ? g.key(0.5f * b.x + 0.5f * b.z, 0.5f * b.y + 0.5f * b.w)
+                           : 0xFFFFFFFFu;
+    vals[i] = (uint32_t)i;
+  }
+}
+
+// The same over FP64 points (their RN32 coordinates); NaN points sort last.
+__global__ void k_point_keys(LbvhView t, const double2* __restrict__ xy, uint32_t n,
+                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const RootGrid g(t);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 p = xy[i];
+    keys[i] = isnan(p.x) || isnan(p.y)
+                  ? 0xFFFFFFFFu
+                  : g.key(__double2float_rn(p.x), __double2float_rn(p.y));
+    vals[i] = (uint32_t)i;
+  }
+}
+
 }  // namespace
+
+static const uint32_t* sort_order(uint32_t n, ProbeScratch& sc, cudaStream_t s) {
+  radix_sort_pairs(sc.okeys.as<uint32_t>(), sc.order.as<uint32_t>(), sc.akeys.as<uint32_t>(),
+                   sc.avals.as<uint32_t>(), n, 32, sc.tmp, s);
+  SPJ_CUDA(cudaGetLastError());
+  return sc.order.as<uint32_t>();
+}
+
+static void reserve_order(uint32_t n, ProbeScratch& sc, cudaStream_t s) {
+  const size_t bytes = ((size_t)n + 1) * 4;
+  sc.order.reserve(bytes, s);
+  sc.okeys.reserve(bytes, s);
+  sc.akeys.reserve(bytes, s);
+  sc.avals.reserve(bytes, s);
+}
+
+const uint32_t* probe_order(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                            ProbeScratch& sc, cudaStream_t s) {
+  if (nprobe < 2 || t.nprims == 0) return nullptr;
+  reserve_order(nprobe, sc, s);
+  k_probe_keys<<<grid_for(nprobe, 256), 256, 0, s>>>(t, probe_box, nprobe, sc.okeys.as<uint32_t>(),
+                                                     sc.order.as<uint32_t>());
+  return sort_order(nprobe, sc, s);
+}
+
+const uint32_t* point_order(const LbvhView& t, const double2* xy, uint32_t n, ProbeScratch& sc,
+                            cudaStream_t s) {
+  if (n < 2 || t.nprims == 0) return nullptr;
+  reserve_order(n, sc, s);
+  k_point_keys<<<grid_for(n, 256), 256, 0, s>>>(t, xy, n, sc.okeys.as<uint32_t>(),
+                                                sc.order.as<uint32_t>());
+  return sort_order(n, sc, s);
+}
 
 void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, cudaStream_t s) {
   SPJ_CHECK(leaf_size >= 1 && leaf_size <= 64, "leaf size must be in [1, 64]");
@@ -316,13 +362,13 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
 }
 
 uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
-                     ProbeScratch& sc, cudaStream_t s) {
+                     ProbeScratch& sc, cudaStream_t s, const uint32_t* order) {
   sc.counts.reserve(((size_t)nprobe + 1) * 4, s);
   sc.offsets.reserve(((size_t)nprobe + 1) * 8, s);
   if (nprobe == 0) return 0;
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<false><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, sc.counts.as<uint32_t>(),
-                                            nullptr, 0, nullptr, nullptr);
+                                            nullptr, 0, nullptr, nullptr, ~0ull, order);
   scan_u32_u64(sc.counts.as<uint32_t>(), sc.offsets.as<uint64_t>(), nprobe, sc.tmp, s);
   uint64_t total = 0;
   SPJ_CUDA(cudaMemcpyAsync(&total, sc.offsets.as<uint64_t>() + nprobe, 8, cudaMemcpyDeviceToHost,
@@ -333,31 +379,32 @@ uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe
 
 void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                    const ProbeScratch& sc, uint32_t probe_base, uint32_t* out_build,
-                   uint32_t* out_probe, cudaStream_t s) {
+                   uint32_t* out_probe, cudaStream_t s, const uint32_t* order) {
   if (nprobe == 0) return;
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr,
                                            sc.offsets.as<uint64_t>(), probe_base, out_build,
-                                           out_probe);
+                                           out_probe, ~0ull, order);
   SPJ_CUDA(cudaGetLastError());
 }
 
 void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
-                      uint32_t* counts, cudaStream_t s) {
+                      uint32_t* counts, cudaStream_t s, const uint32_t* order) {
   if (nprobe == 0) return;
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<false><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, counts, nullptr, 0, nullptr,
-                                            nullptr);
+                                            nullptr, ~0ull, order);
   SPJ_CUDA(cudaGetLastError());
 }
 
 void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                         const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
-                        uint32_t* out_probe, cudaStream_t s, uint64_t capacity) {
+                        uint32_t* out_probe, cudaStream_t s, uint64_t capacity,
+                        const uint32_t* order) {
   if (nprobe == 0) return;
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr, offs, probe_base,
-                                           out_build, out_probe, capacity);
+                                           out_build, out_probe, capacity, order);
   SPJ_CUDA(cudaGetLastError());
 }
 

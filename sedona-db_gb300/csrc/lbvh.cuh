@@ -46,6 +46,58 @@ struct Lbvh {
   }
 };
 
+namespace {
+
+constexpr int kTravThreads = 128;  // traversal block size
+constexpr int kTravStack = 64;     // per-thread stack depth (Karras depth <= 32 key bits + 32)
+
+__device__ __forceinline__ bool box_overlap(float4 a, float4 b) {
+  return !(a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y);
+}
+
+// Depth-first traversal calling fn(k) for every sorted primitive k whose box
+// overlaps q (closed intervals), in a fixed order (left child first).  stack
+// points at this thread's column of a shared [kTravStack][kTravThreads]
+// array, so a warp's pushes hit 32 distinct banks.
+template <class Fn>
+__device__ __forceinline__ void lbvh_for_each_overlap(const LbvhView& t, float4 q, int* stack,
+                                                      Fn&& fn) {
+  int sp = 0;
+  int node = t.nleaves > 1 ? 0 : ~0;  // root: internal node 0, or the single leaf
+  while (true) {
+    if (node < 0) {
+      const uint32_t c = (uint32_t)(~node);
+      const uint32_t b0 = c * t.leaf_size;
+      const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+      for (uint32_t k = b0; k < b1; k++)
+        if (box_overlap(t.sorted_box[k], q)) fn(k);
+    } else {
+      const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+      const int2 ch = t.node_child[node];
+      const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
+      if (hl && hr) {
+        if (sp < kTravStack) stack[sp * kTravThreads] = ch.y;
+        sp++;
+        node = ch.x;
+        continue;
+      }
+      if (hl) {
+        node = ch.x;
+        continue;
+      }
+      if (hr) {
+        node = ch.y;
+        continue;
+      }
+    }
+    if (sp == 0) break;
+    sp--;
+    node = sp < kTravStack ? stack[sp * kTravThreads] : 0;
+  }
+}
+
+}  // namespace
+
 // Builds the LBVH over boxes[0..n); NaN / inverted boxes are left out.
 void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, cudaStream_t s);
 
@@ -53,24 +105,37 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
 // intervals).  Pass 1 counts per probe; an exclusive scan gives each probe
 // its output offset; pass 2 writes build ids and probe ids.  Probe boxes with
 // NaN are empty.  probe_base is added to the probe ids written.
+// `order` (optional, a permutation of the probe rows) sets the order in which
+// traversal threads take probes; it changes neither the pairs nor where they
+// are written.
 struct ProbeScratch {
   DevBuf counts, offsets, tmp;
+  DevBuf order, okeys, akeys, avals;  // probe_order
 };
 // returns the number of candidate pairs (syncs the stream once)
 uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
-                     ProbeScratch& sc, cudaStream_t s);
+                     ProbeScratch& sc, cudaStream_t s, const uint32_t* order = nullptr);
 void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                    const ProbeScratch& sc, uint32_t probe_base, uint32_t* out_build,
-                   uint32_t* out_probe, cudaStream_t s);
+                   uint32_t* out_probe, cudaStream_t s, const uint32_t* order = nullptr);
+
+// The probe rows sorted by the Morton key of their box centre over the tree's
+// extent (sc.order); nullptr when there is nothing to order.
+const uint32_t* probe_order(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
+                            ProbeScratch& sc, cudaStream_t s);
+// The same for FP64 points (KNN queries).
+const uint32_t* point_order(const LbvhView& t, const double2* xy, uint32_t n, ProbeScratch& sc,
+                            cudaStream_t s);
 
 // The two traversal passes with caller-owned count / offset arrays (no
 // allocation): counts[nprobe] written by the first, offs[nprobe] read by the
 // second.
 void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
-                      uint32_t* counts, cudaStream_t s);
+                      uint32_t* counts, cudaStream_t s, const uint32_t* order = nullptr);
 void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                         const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
-                        uint32_t* out_probe, cudaStream_t s, uint64_t capacity = ~0ull);
+                        uint32_t* out_probe, cudaStream_t s, uint64_t capacity = ~0ull,
+                        const uint32_t* order = nullptr);
 
 // Expand point/box probes by a distance (f64), then round outward to f32
 // (rust/sedona-spatial-join/src/operand_evaluator.rs:605-607).

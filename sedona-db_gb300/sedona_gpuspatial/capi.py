@@ -121,7 +121,7 @@ SedonaSpatialRefiner._fields_ = [
 
 class SpjJoinConfig(C.Structure):
     _fields_ = [("runtime", C.POINTER(GpuSpatialRuntime)), ("leaf_size", C.c_uint32),
-                ("refine_form", C.c_int32), ("profile", C.c_int32)]
+                ("refine_form", C.c_int32), ("profile", C.c_int32), ("probe_order", C.c_int32)]
 
 
 class SpjDeviceWkb(C.Structure):
@@ -155,7 +155,7 @@ EXPORTS = [
     "SpjJoinFinishBuild", "SpjJoinBuildDevice", "SpjJoinProbeArrow", "SpjJoinProbeDevice",
     "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
-    "SpjKnnStream", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
+    "SpjKnnStream", "SpjKnnGetStats", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
     "SpjIndexProbeNoAlloc",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
     "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
@@ -227,6 +227,7 @@ def lib() -> C.CDLL:
             L.SpjKnnLastError.argtypes = [C.c_void_p]
             L.SpjKnnLastError.restype = C.c_char_p
             L.SpjKnnBuild.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+            L.SpjKnnGetStats.argtypes = [C.c_void_p] + [C.POINTER(C.c_uint64)] * 3
             L.SpjKnnQuery.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
                                       C.c_void_p, C.c_void_p, C.c_int32]
             L.SpjKnnStream.argtypes = [C.c_void_p]
@@ -441,10 +442,11 @@ class SpatialJoin:
     """The fused build/probe join (SpjJoin*, include/spj_gb300.h)."""
 
     def __init__(self, runtime: Optional[Runtime] = None, leaf_size: int = 0,
-                 refine_form: int = 1, profile: bool = False):
+                 refine_form: int = 1, profile: bool = False, probe_order: int = 0):
         self.runtime = runtime or Runtime.get()
         self.h = C.c_void_p()
-        cfg = SpjJoinConfig(C.pointer(self.runtime.rt), leaf_size, refine_form, int(profile))
+        cfg = SpjJoinConfig(C.pointer(self.runtime.rt), leaf_size, refine_form, int(profile),
+                            probe_order)
         if lib().SpjJoinCreate(C.byref(cfg), C.byref(self.h)) != 0:
             raise GpuSpatialError("SpjJoinCreate failed")
         self._keep = []
@@ -662,6 +664,11 @@ class KnnJoin:
 
     def stream(self) -> int:
         return lib().SpjKnnStream(self.h)
+
+    def stats(self) -> dict:
+        v = [C.c_uint64() for _ in range(3)]
+        _check(lib().SpjKnnGetStats(self.h, *[C.byref(x) for x in v]), "knn stats", self._err)
+        return dict(zip(("queries", "exact_evals", "redone"), (x.value for x in v)))
 
     def __del__(self):
         if getattr(self, "h", None):

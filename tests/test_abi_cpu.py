@@ -81,5 +81,7 @@ def test_struct_layouts_match_reference_abi():
     assert C.sizeof(capi.GpuSpatialRuntime) == 4 * p
     assert C.sizeof(capi.SedonaFloatIndex2D) == 10 * p
     assert C.sizeof(capi.SedonaSpatialRefiner) == 8 * p
-    assert C.sizeof(capi.GpuSpatialRuntimeConfig) == p + 4 + 4 + 4 + 4 - 4 or True
+    # const char*, int, bool (+3 padding), int; rounded up to pointer alignment
+    assert C.sizeof(capi.GpuSpatialRuntimeConfig) == (p + 12 + p - 1) // p * p
+    assert C.sizeof(capi.SpjJoinConfig) == p + 4 * 4
     assert C.sizeof(capi.GpuSpatialRefinerConfig) == p + 4 + 1 + 3 + 4 + (4 if p == 8 else 0)

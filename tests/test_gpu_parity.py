@@ -92,6 +92,27 @@ def test_dwithin(capi, oracle_mod, form):
     assert pairs(b, p) == exp
 
 
+@pytest.mark.parametrize("shape", ["pip", "polygons", "dwithin"])
+def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
+    """Traversal in Morton order of the probe boxes (probe_order=1) writes the
+    same pairs at the same positions as traversal in row order (-1)."""
+    from sedona_gpuspatial import datagen
+    if shape == "pip":
+        inp, pred, d = datagen.workload1(n_points=40000, n_polys=500), "within", 0.0
+    elif shape == "polygons":
+        inp, pred, d = datagen.workload2(n_buildings=20000, n_zones=300), "intersects", 0.0
+    else:
+        inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
+    out = {}
+    for order in (-1, 1):
+        j = capi.SpatialJoin(probe_order=order)
+        j.build(inp.build)
+        out[order] = j.probe(inp.probe, pred, distance=d)
+    np.testing.assert_array_equal(out[1][0], out[-1][0])
+    np.testing.assert_array_equal(out[1][1], out[-1][1])
+    assert pairs(*out[1]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred, d)
+
+
 def test_dwithin_exact_boundary(capi, oracle_mod):
     """Integer Pythagorean triples put pairs exactly at distance d."""
     from sedona_gpuspatial import wkb
@@ -116,6 +137,39 @@ def test_knn(capi, oracle_mod, form):
     kj.build(bx, by)
     idx, dist = kj.query(px, py, 8)
     oi, od = oracle_mod.knn(oracle_mod.Geoms(inp.build), oracle_mod.Geoms(inp.probe), 8, nthreads=4)
+    assert np.array_equal(idx, oi)
+    np.testing.assert_allclose(dist, od, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("case", ["lattice", "offset", "huge"])
+@pytest.mark.parametrize("k", [1, 5, 12, 20])
+def test_knn_split_pass_cases(capi, oracle_mod, case, k):
+    """The split-FP32 pass against the oracle where it must hand probes to the
+    exact kernel: exact distance ties on an integer lattice (ties at rank k),
+    points 1e-3 apart at 1e5 offsets (the hi/lo split carries the digits FP32
+    alone loses), and coordinates beyond the split range (exact kernel)."""
+    from sedona_gpuspatial import wkb
+    rng = np.random.default_rng(11 + k)
+    if case == "lattice":
+        g = np.arange(60, dtype=np.float64)
+        bx, by = [a.ravel() for a in np.meshgrid(g, g)]
+        px = rng.integers(0, 120, 3000) / 2.0
+        py = rng.integers(0, 120, 3000) / 2.0
+    elif case == "offset":
+        bx = 1e5 + rng.uniform(0, 3.0, 4000).round(3)
+        by = -1e5 + rng.uniform(0, 3.0, 4000).round(3)
+        px = 1e5 + rng.uniform(0, 3.0, 3000)
+        py = -1e5 + rng.uniform(0, 3.0, 3000)
+    else:
+        bx = rng.uniform(-1e20, 1e20, 3000)
+        by = rng.uniform(-1e20, 1e20, 3000)
+        px = rng.uniform(-1e20, 1e20, 1000)
+        py = rng.uniform(-1e20, 1e20, 1000)
+    kj = capi.KnnJoin(refine_form=1)
+    kj.build(bx, by)
+    idx, dist = kj.query(px, py, k)
+    oi, od = oracle_mod.knn(oracle_mod.Geoms(wkb.points_column(bx, by)),
+                            oracle_mod.Geoms(wkb.points_column(px, py)), k, nthreads=4)
     assert np.array_equal(idx, oi)
     np.testing.assert_allclose(dist, od, rtol=1e-12, atol=0)
 
