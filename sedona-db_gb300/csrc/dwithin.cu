@@ -20,12 +20,18 @@ constexpr float kSplitDown = 0.99999904632568359375f;  // 1 - 2^-20
 constexpr float kTwoM44 = 5.684341886080801486968994140625e-14f;
 constexpr float kTwoM120 = 7.5231638452626400509999138382223723380394595633413601376560e-37f;
 
-__global__ void k_split_points(const double2* __restrict__ pts, const uint32_t* __restrict__ ids,
-                               uint32_t m, double2* __restrict__ xy, float4* __restrict__ hl,
+__global__ void k_split_points(const double2* __restrict__ pts, uint32_t npts,
+                               const uint32_t* __restrict__ ids, uint32_t m,
+                               double2* __restrict__ xy, float4* __restrict__ hl,
                                unsigned* __restrict__ mag) {
   unsigned bm = 0, big = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    const double2 p = pts[ids[i]];
+    const uint32_t id = ids[i];
+    if (id >= npts) {  // not a row of the column: recorded, the host raises
+      big |= 2u;
+      continue;
+    }
+    const double2 p = pts[id];
     xy[i] = p;
     const float hx = __double2float_rn(p.x), hy = __double2float_rn(p.y);
     // v - RN32(v) is exact in FP64
@@ -42,7 +48,7 @@ __global__ void k_split_points(const double2* __restrict__ pts, const uint32_t* 
   if ((threadIdx.x & 31) == 0) {
     // non-negative floats order as their bit patterns
     if (bm) atomicMax(&mag[0], bm);
-    if (big) atomicOr(&mag[1], 1u);
+    if (big) atomicOr(&mag[1], big);
   }
 }
 
@@ -56,10 +62,15 @@ __global__ void __launch_bounds__(kTravThreads)
                     uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
                     uint64_t cap, DeviceStatus* st) {
   __shared__ int stack[kTravStack * kTravThreads];
+  const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint32_t esc = 0, tested = 0;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
        j += (int64_t)gridDim.x * blockDim.x) {
     const int64_t pi = order ? (int64_t)order[j] : j;
+    if (pi < 0 || pi >= n) {
+      traversal_fault(t, kBadProbe, (unsigned)pi);
+      continue;
+    }
     const float4 q = probe_box[pi];
     uint32_t cnt = 0;
     uint64_t pos = kScatter ? offs[pi] : 0;
@@ -76,35 +87,79 @@ __global__ void __launch_bounds__(kTravThreads)
         cerr = __fadd_ru(__fmul_ru(__fadd_ru(bmag, __fadd_ru(fabsf(hx), fabsf(hy))), kTwoM44),
                          kTwoM120);
       }
-      lbvh_for_each_overlap(t, q, stack + threadIdx.x, [&](uint32_t k) {
-        tested++;
-        int r = -1;
-        if (split) {
-          const float4 h = bhl[k];
-          const float dx = __fadd_rn(__fsub_rn(h.x, hx), __fsub_rn(h.z, lx));
-          const float dy = __fadd_rn(__fsub_rn(h.y, hy), __fsub_rn(h.w, ly));
-          const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-          // D <= hi < d_lo <= d: RN(D) <= d.  D >= lo > d_hi >= d with lo a
-          // float above d_hi, so D exceeds d by an FP32 ulp: RN(D) > d.
-          if (__fadd_ru(__fmul_ru(__fsqrt_ru(d2), kSplitUp), cerr) < d_lo) r = 1;
-          else if (__fsub_rd(__fmul_rd(__fsqrt_rd(d2), kSplitDown), cerr) > d_hi) r = 0;
+      int sp = 0;
+      int node = t.nleaves > 1 ? 0 : ~0;
+      uint64_t steps = 0;
+      while (true) {
+        if (++steps > max_steps) {
+          traversal_fault(t, kTooLong, (unsigned)pi);
+          break;
         }
-        if (r < 0) {
-          esc++;
-          r = exact::dwithin_exact(bxy[k], p, d) ? 1 : 0;
-        }
-        if (r) {
-          if (kScatter) {
-            if (pos < cap) {
-              out_build[pos] = t.sorted_id[k];
-              out_probe[pos] = (uint32_t)pi + probe_base;
+        if (node < 0) {
+          const uint32_t c = (uint32_t)(~node);
+          if (c >= t.nleaves) {
+            traversal_fault(t, kBadLeaf, c);
+            break;
+          }
+          const uint32_t b0 = c * t.leaf_size;
+          const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+          for (uint32_t k = b0; k < b1; k++) {
+            if (!box_overlap(t.sorted_box[k], q)) continue;
+            tested++;
+            int r = -1;
+            if (split) {
+              const float4 h = bhl[k];
+              const float dx = __fadd_rn(__fsub_rn(h.x, hx), __fsub_rn(h.z, lx));
+              const float dy = __fadd_rn(__fsub_rn(h.y, hy), __fsub_rn(h.w, ly));
+              const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+              // D <= hi < d_lo <= d: RN(D) <= d.  D >= lo > d_hi >= d with lo
+              // a float above d_hi, so D exceeds d by an FP32 ulp: RN(D) > d.
+              if (__fadd_ru(__fmul_ru(__fsqrt_ru(d2), kSplitUp), cerr) < d_lo) r = 1;
+              else if (__fsub_rd(__fmul_rd(__fsqrt_rd(d2), kSplitDown), cerr) > d_hi) r = 0;
             }
-            pos++;
-          } else {
-            cnt++;
+            if (r < 0) {
+              esc++;
+              r = exact::dwithin_exact(bxy[k], p, d) ? 1 : 0;
+            }
+            if (r) {
+              if (kScatter) {
+                if (pos < cap) {
+                  out_build[pos] = t.sorted_id[k];
+                  out_probe[pos] = (uint32_t)pi + probe_base;
+                }
+                pos++;
+              } else {
+                cnt++;
+              }
+            }
+          }
+        } else {
+          if ((uint32_t)node + 1 >= t.nleaves) {
+            traversal_fault(t, kBadNode, (unsigned)node);
+            break;
+          }
+          const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+          const int2 ch = t.node_child[node];
+          const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
+          if (hl && hr) {
+            if (sp < kTravStack) stack[sp * kTravThreads + threadIdx.x] = ch.y;
+            sp++;
+            node = ch.x;
+            continue;
+          }
+          if (hl) {
+            node = ch.x;
+            continue;
+          }
+          if (hr) {
+            node = ch.y;
+            continue;
           }
         }
-      });
+        if (sp == 0) break;
+        sp--;
+        node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
+      }
     }
     if (!kScatter) counts[pi] = cnt;
   }
@@ -129,7 +184,8 @@ void float_neighbours(double d, float& lo, float& hi) {
 
 }  // namespace
 
-void build_point_split(const double2* pts, const Lbvh& bvh, PointSplit& out, cudaStream_t s) {
+void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, PointSplit& out,
+                       cudaStream_t s) {
   const uint32_t m = bvh.nprims;
   out.n = m;
   out.xy.reserve(((size_t)m + 1) * 16, s);
@@ -137,7 +193,7 @@ void build_point_split(const double2* pts, const Lbvh& bvh, PointSplit& out, cud
   out.tmp.reserve(8, s);
   SPJ_CUDA(cudaMemsetAsync(out.tmp.get(), 0, 8, s));
   if (m)
-    k_split_points<<<grid_for(m, 256), 256, 0, s>>>(pts, bvh.sorted_id.as<uint32_t>(), m,
+    k_split_points<<<grid_for(m, 256), 256, 0, s>>>(pts, npts, bvh.sorted_id.as<uint32_t>(), m,
                                                     out.xy.as<double2>(), out.hl.as<float4>(),
                                                     out.tmp.as<unsigned>());
   SPJ_CUDA(cudaGetLastError());
@@ -146,6 +202,7 @@ void build_point_split(const double2* pts, const Lbvh& bvh, PointSplit& out, cud
   SPJ_CUDA(cudaStreamSynchronize(s));
   float b;
   std::memcpy(&b, &mag[0], 4);
+  SPJ_CHECK((mag[1] & 2u) == 0, "point split: sorted id out of range");
   out.bmag = b;
   out.ok = mag[1] == 0;
 }

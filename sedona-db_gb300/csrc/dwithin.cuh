@@ -24,8 +24,9 @@ struct PointSplit {
 };
 constexpr double kSplitMaxCoord = 1e18;
 
-// pts: the build column's points (row order); bvh over their boxes.
-void build_point_split(const double2* pts, const Lbvh& bvh, PointSplit& out, cudaStream_t s);
+// pts: the build column's npts points (row order); bvh over their boxes.
+void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, PointSplit& out,
+                       cudaStream_t s);
 
 // The two passes.  probe_box: the probe points' boxes expanded by d
 // (expand_boxes); probe_pt: the probe points.  The count pass writes

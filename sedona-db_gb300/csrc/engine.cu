@@ -68,7 +68,7 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
 
 void JoinEngine::split_points() {
   bsplit_.n = 0;
-  if (bg_.all_points && bvh_.nprims > 0) build_point_split(bg_.pt.as<double2>(), bvh_, bsplit_, bs_);
+  if (cfg_.fuse_dwithin && bg_.all_points && bvh_.nprims > 0) build_point_split(bg_.pt.as<double2>(), bg_.n, bvh_, bsplit_, bs_);
 }
 
 void JoinEngine::reindex(uint32_t leaf_size) {
@@ -123,8 +123,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     order = probe_order(tv, boxes, n, ws.psc, s);
     if (order) launches += 21;  // keys + 4 radix passes (histogram, 3-kernel scan, scatter)
   }
-  if (predicate == kPredDWithin && cfg_.refine_form == kFastF32 && bsplit_.n == bvh_.nprims &&
-      bvh_.nprims > 0) {
+  if (predicate == kPredDWithin && cfg_.fuse_dwithin && cfg_.refine_form == kFastF32 &&
+      bsplit_.n == bvh_.nprims && bvh_.nprims > 0) {
     // point build and probe sides: the distance test runs inside the
     // traversal, no candidate pairs are materialized
     reset_status(ws.status, s);
@@ -140,6 +140,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
                              cudaMemcpyDeviceToHost, s));
     SPJ_CUDA(cudaMemcpyAsync(&hst, ws.status.get(), sizeof hst, cudaMemcpyDeviceToHost, s));
     SPJ_CUDA(cudaStreamSynchronize(s));
+    check_traversal(tv, s);
     if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
     ws.out_build.reserve((total + 1) * 4, s);
     ws.out_probe.reserve((total + 1) * 4, s);

@@ -26,6 +26,9 @@ struct EngineConfig {
   // traversal order of the probe rows: 0 = Morton order from kOrderMinRows
   // rows up, 1 = always Morton order, -1 = row order
   int probe_order = 0;
+  // point build and probe sides: decide ST_DWithin inside the traversal
+  // (FAST_F32 form); otherwise filter, refine and compact
+  bool fuse_dwithin = false;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 

@@ -94,11 +94,16 @@ __global__ void __launch_bounds__(kKnnThreads)
           uint32_t k, float slack, uint32_t* __restrict__ out_idx, double* __restrict__ out_dist,
           unsigned long long* __restrict__ exact_evals) {
   __shared__ int stack[kKnnStack * kKnnThreads];
+  const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint32_t evals = 0;
   const uint64_t nn = n_dev ? (uint64_t)*n_dev : n;
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < nn;
        j += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t qi = order ? (uint64_t)order[j] : j;
+    if (qi >= n) {
+      traversal_fault(t, kBadProbe, (unsigned)qi);
+      continue;
+    }
     const double2 q = probe[qi];
     const float2 q32 = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
     // |q - q32| bound, plus the build-side bound
@@ -117,9 +122,18 @@ __global__ void __launch_bounds__(kKnnThreads)
     int sp = 0;
     int node = valid ? (t.nleaves > 1 ? 0 : ~0) : 0;
     bool done = !valid;
+    uint64_t steps = 0;
     while (!done) {
+      if (++steps > max_steps) {  // each node is visited at most once
+        traversal_fault(t, kTooLong, (unsigned)qi);
+        break;
+      }
       if (node < 0) {
         const uint32_t c = (uint32_t)(~node);
+        if (c >= t.nleaves) {
+          traversal_fault(t, kBadLeaf, c);
+          break;
+        }
         const uint32_t b0 = c * t.leaf_size, b1 = min(b0 + t.leaf_size, t.nprims);
         for (uint32_t pi = b0; pi < b1; pi++) {
           const double2 b = bxy[pi];
@@ -171,6 +185,10 @@ __global__ void __launch_bounds__(kKnnThreads)
           }
         }
       } else {
+        if ((uint32_t)node + 1 >= t.nleaves) {
+          traversal_fault(t, kBadNode, (unsigned)node);
+          break;
+        }
         const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
         const int2 ch = t.node_child[node];
         // conservative lower bounds of the true distance
@@ -229,10 +247,15 @@ __global__ void __launch_bounds__(kKnnThreads)
                 double* __restrict__ out_dist, uint32_t* __restrict__ redo,
                 uint32_t* __restrict__ nredo, unsigned long long* __restrict__ exact_evals) {
   __shared__ int stack[kKnnStack * kKnnThreads];
+  const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint32_t evals = 0;
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n;
        j += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t qi = order ? (uint64_t)order[j] : j;
+    if (qi >= n) {
+      traversal_fault(t, kBadProbe, (unsigned)qi);
+      continue;
+    }
     const double2 q = probe[qi];
     if (isnan(q.x) || isnan(q.y) || t.nprims == 0) {
       write_empty(out_idx, out_dist, qi, k);
@@ -263,9 +286,18 @@ __global__ void __launch_bounds__(kKnnThreads)
     float bound = INFINITY;  // upper bound of the true distance of the (k+1)-th entry
     int sp = 0;
     int node = t.nleaves > 1 ? 0 : ~0;
+    uint64_t steps = 0;
     while (true) {
+      if (++steps > max_steps) {  // each node is visited at most once
+        traversal_fault(t, kTooLong, (unsigned)qi);
+        break;
+      }
       if (node < 0) {
         const uint32_t c = (uint32_t)(~node);
+        if (c >= t.nleaves) {
+          traversal_fault(t, kBadLeaf, c);
+          break;
+        }
         const uint32_t b0 = c * t.leaf_size, b1 = min(b0 + t.leaf_size, t.nprims);
         for (uint32_t pi = b0; pi < b1; pi++) {
           const float4 h = hl[pi];
@@ -301,6 +333,10 @@ __global__ void __launch_bounds__(kKnnThreads)
           }
         }
       } else {
+        if ((uint32_t)node + 1 >= t.nleaves) {
+          traversal_fault(t, kBadNode, (unsigned)node);
+          break;
+        }
         const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
         const int2 ch = t.node_child[node];
         const float dl = __fsub_rd(__fmul_rd(box_dist(q32, lb), 0.99999905f), qs);
@@ -549,6 +585,7 @@ void KnnIndex::query(const double* probe_xy, uint64_t n, uint32_t k, uint32_t* o
   unsigned long long cnt[2] = {0, 0};
   SPJ_CUDA(cudaMemcpyAsync(cnt, counters_.get(), 16, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
+  check_traversal(bvh_.view(), s);
   exact_evals_ += cnt[0];
   redone_ += (uint32_t)cnt[1];
   queries_ += n;

@@ -178,7 +178,11 @@ __global__ void __launch_bounds__(kTravThreads)
             uint32_t* __restrict__ counts, const uint64_t* __restrict__ offs, uint32_t probe_base,
             uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
             uint64_t cap = ~0ull, const uint32_t* __restrict__ order = nullptr) {
+  // per-thread stack in shared memory, [depth][thread] so a warp's pushes hit
+  // 32 distinct banks
   __shared__ int stack[kTravStack * kTravThreads];
+  // a traversal visits each node at most once: 2 * nleaves steps bound it
+  const uint64_t max_steps = 2ull * t.nleaves + 2;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nprobe;
        j += (int64_t)gridDim.x * blockDim.x) {
     // with an order, thread slot j takes the j-th probe in Morton order of the
@@ -186,21 +190,70 @@ __global__ void __launch_bounds__(kTravThreads)
     // (less divergence, node boxes shared through L1).  Counts and offsets
     // stay indexed by probe row, so the output layout does not change.
     const int64_t pi = order ? (int64_t)order[j] : j;
+    if (pi < 0 || pi >= nprobe) {
+      traversal_fault(t, kBadProbe, (unsigned)pi);
+      continue;
+    }
     const float4 q = probe_box[pi];
     uint32_t cnt = 0;
     uint64_t pos = kScatter ? offs[pi] : 0;
     if (box_valid(q) && t.nprims > 0) {
-      lbvh_for_each_overlap(t, q, stack + threadIdx.x, [&](uint32_t k) {
-        if (kScatter) {
-          if (pos < cap) {  // writes bounded by the output capacity
-            out_build[pos] = t.sorted_id[k];
-            out_probe[pos] = (uint32_t)pi + probe_base;
-          }
-          pos++;
-        } else {
-          cnt++;
+      int sp = 0;
+      int node = t.nleaves > 1 ? 0 : ~0;  // root: internal node 0, or the single leaf
+      uint64_t steps = 0;
+      while (true) {
+        if (++steps > max_steps) {
+          traversal_fault(t, kTooLong, (unsigned)pi);
+          break;
         }
-      });
+        if (node < 0) {
+          const uint32_t c = (uint32_t)(~node);
+          if (c >= t.nleaves) {
+            traversal_fault(t, kBadLeaf, c);
+            break;
+          }
+          const uint32_t b0 = c * t.leaf_size;
+          const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+          for (uint32_t k = b0; k < b1; k++) {
+            if (box_overlap(t.sorted_box[k], q)) {
+              if (kScatter) {
+                if (pos < cap) {  // writes bounded by the output capacity
+                  out_build[pos] = t.sorted_id[k];
+                  out_probe[pos] = (uint32_t)pi + probe_base;
+                }
+                pos++;
+              } else {
+                cnt++;
+              }
+            }
+          }
+        } else {
+          if ((uint32_t)node + 1 >= t.nleaves) {
+            traversal_fault(t, kBadNode, (unsigned)node);
+            break;
+          }
+          const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+          const int2 ch = t.node_child[node];
+          const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
+          if (hl && hr) {
+            if (sp < kTravStack) stack[sp * kTravThreads + threadIdx.x] = ch.y;
+            sp++;
+            node = ch.x;
+            continue;
+          }
+          if (hl) {
+            node = ch.x;
+            continue;
+          }
+          if (hr) {
+            node = ch.y;
+            continue;
+          }
+        }
+        if (sp == 0) break;
+        sp--;
+        node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
+      }
     }
     if (!kScatter) counts[pi] = cnt;
   }
@@ -334,6 +387,8 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
   const uint32_t L = out.nleaves;
   out.node_box.reserve((size_t)(L > 1 ? 2 * (L - 1) : 1) * sizeof(float4), s);
   out.node_child.reserve((size_t)(L > 1 ? L - 1 : 1) * sizeof(int2), s);
+  out.fault.reserve(8, s);
+  SPJ_CUDA(cudaMemsetAsync(out.fault.get(), 0, 8, s));
   if (m == 0) return;
   uint32_t* ids = out.sorted_id.as<uint32_t>();
   k_compact_ids<<<g, 256, 0, s>>>(flag.as<uint8_t>(), pos.as<uint64_t>(), n, ids);
@@ -361,6 +416,17 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
   SPJ_CUDA(cudaStreamSynchronize(s));
 }
 
+void check_traversal(const LbvhView& t, cudaStream_t s) {
+  if (!t.fault) return;
+  unsigned f[2] = {0, 0};
+  SPJ_CUDA(cudaMemcpyAsync(f, t.fault, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  static const char* what[] = {"", "an out-of-range leaf index", "an out-of-range node index",
+                               "an out-of-range probe row", "more steps than the tree has nodes"};
+  SPJ_CHECK(f[0] == 0, std::string("LBVH traversal met ") + what[f[0] < 5 ? f[0] : 0] + " (" +
+                           std::to_string(f[1]) + ")");
+}
+
 uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                      ProbeScratch& sc, cudaStream_t s, const uint32_t* order) {
   sc.counts.reserve(((size_t)nprobe + 1) * 4, s);
@@ -374,6 +440,7 @@ uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe
   SPJ_CUDA(cudaMemcpyAsync(&total, sc.offsets.as<uint64_t>() + nprobe, 8, cudaMemcpyDeviceToHost,
                            s));
   SPJ_CUDA(cudaStreamSynchronize(s));
+  check_traversal(t, s);
   return total;
 }
 

@@ -25,11 +25,13 @@ struct LbvhView {
   const uint32_t* sorted_id = nullptr;
   const float4* node_box = nullptr;
   const int2* node_child = nullptr;
+  // [code, value]: the first out-of-range index a traversal met (code 0 = none)
+  unsigned* fault = nullptr;
 };
 
 struct Lbvh {
   uint32_t nprims = 0, nleaves = 0, leaf_size = 4;
-  DevBuf sorted_box, sorted_id, node_box, node_child;
+  DevBuf sorted_box, sorted_id, node_box, node_child, fault;
   LbvhView view() const {
     LbvhView v;
     v.nprims = nprims;
@@ -39,6 +41,7 @@ struct Lbvh {
     v.sorted_id = sorted_id.as<uint32_t>();
     v.node_box = node_box.as<float4>();
     v.node_child = node_child.as<int2>();
+    v.fault = fault.as<unsigned>();
     return v;
   }
   size_t device_bytes() const {
@@ -51,49 +54,16 @@ namespace {
 constexpr int kTravThreads = 128;  // traversal block size
 constexpr int kTravStack = 64;     // per-thread stack depth (Karras depth <= 32 key bits + 32)
 
-__device__ __forceinline__ bool box_overlap(float4 a, float4 b) {
-  return !(a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y);
+enum TraversalFault : unsigned { kBadLeaf = 1, kBadNode = 2, kBadProbe = 3, kTooLong = 4 };
+
+// Records the first out-of-range index a traversal met (the traversal of
+// that probe stops; the host turns the record into an error).
+__device__ __forceinline__ void traversal_fault(const LbvhView& t, unsigned code, unsigned v) {
+  if (t.fault && atomicCAS(&t.fault[0], 0u, code) == 0u) t.fault[1] = v;
 }
 
-// Depth-first traversal calling fn(k) for every sorted primitive k whose box
-// overlaps q (closed intervals), in a fixed order (left child first).  stack
-// points at this thread's column of a shared [kTravStack][kTravThreads]
-// array, so a warp's pushes hit 32 distinct banks.
-template <class Fn>
-__device__ __forceinline__ void lbvh_for_each_overlap(const LbvhView& t, float4 q, int* stack,
-                                                      Fn&& fn) {
-  int sp = 0;
-  int node = t.nleaves > 1 ? 0 : ~0;  // root: internal node 0, or the single leaf
-  while (true) {
-    if (node < 0) {
-      const uint32_t c = (uint32_t)(~node);
-      const uint32_t b0 = c * t.leaf_size;
-      const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
-      for (uint32_t k = b0; k < b1; k++)
-        if (box_overlap(t.sorted_box[k], q)) fn(k);
-    } else {
-      const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
-      const int2 ch = t.node_child[node];
-      const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
-      if (hl && hr) {
-        if (sp < kTravStack) stack[sp * kTravThreads] = ch.y;
-        sp++;
-        node = ch.x;
-        continue;
-      }
-      if (hl) {
-        node = ch.x;
-        continue;
-      }
-      if (hr) {
-        node = ch.y;
-        continue;
-      }
-    }
-    if (sp == 0) break;
-    sp--;
-    node = sp < kTravStack ? stack[sp * kTravThreads] : 0;
-  }
+__device__ __forceinline__ bool box_overlap(float4 a, float4 b) {
+  return !(a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y);
 }
 
 }  // namespace
@@ -112,6 +82,8 @@ struct ProbeScratch {
   DevBuf counts, offsets, tmp;
   DevBuf order, okeys, akeys, avals;  // probe_order
 };
+// Throws if a traversal over t recorded an out-of-range index (syncs s).
+void check_traversal(const LbvhView& t, cudaStream_t s);
 // returns the number of candidate pairs (syncs the stream once)
 uint64_t probe_count(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                      ProbeScratch& sc, cudaStream_t s, const uint32_t* order = nullptr);

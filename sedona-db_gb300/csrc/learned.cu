@@ -377,9 +377,18 @@ __global__ void __launch_bounds__(128)
         fallbacks++;
         // LBVH: build rows whose RN32 point equals the probe's RN32 point
         int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
+        uint64_t tsteps = 0;
         while (t.nprims > 0) {
+          if (++tsteps > 2ull * t.nleaves + 2) {  // each node is visited at most once
+            traversal_fault(t, kTooLong, i);
+            break;
+          }
           if (node < 0) {
             const uint32_t c = (uint32_t)(~node), b0 = c * t.leaf_size;
+            if (c >= t.nleaves) {
+              traversal_fault(t, kBadLeaf, c);
+              break;
+            }
             const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
             for (uint32_t k = b0; k < b1; k++)
               if (in_box(make_float2(t.sorted_box[k].x, t.sorted_box[k].y), pb)) {
@@ -387,6 +396,10 @@ __global__ void __launch_bounds__(128)
                 if (pteq(B.pt[id], p)) emit(id);
               }
           } else {
+            if ((uint32_t)node + 1 >= t.nleaves) {
+              traversal_fault(t, kBadNode, (unsigned)node);
+              break;
+            }
             const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
             const int2 ch = t.node_child[node];
             const bool hl = !(lb.x > pb.z || lb.z < pb.x || lb.y > pb.w || lb.w < pb.y);
@@ -436,9 +449,18 @@ __global__ void __launch_bounds__(128)
       } else {
         fallbacks++;
         int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
+        uint64_t tsteps = 0;
         while (t.nprims > 0) {
+          if (++tsteps > 2ull * t.nleaves + 2) {  // each node is visited at most once
+            traversal_fault(t, kTooLong, i);
+            break;
+          }
           if (node < 0) {
             const uint32_t c = (uint32_t)(~node), b0 = c * t.leaf_size;
+            if (c >= t.nleaves) {
+              traversal_fault(t, kBadLeaf, c);
+              break;
+            }
             const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
             for (uint32_t k = b0; k < b1; k++) {
               const float4 sb = t.sorted_box[k];
@@ -447,6 +469,10 @@ __global__ void __launch_bounds__(128)
               if (range_pred(P, i, B.pt[id], make_float2(sb.x, sb.y), aoe, esc)) emit(id);
             }
           } else {
+            if ((uint32_t)node + 1 >= t.nleaves) {
+              traversal_fault(t, kBadNode, (unsigned)node);
+              break;
+            }
             const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
             const int2 ch = t.node_child[node];
             const bool hl = !(lb.x > bx.z || lb.z < bx.x || lb.y > bx.w || lb.w < bx.y);
@@ -735,6 +761,7 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
   SPJ_CUDA(cudaMemcpyAsync(h, counters_.get(), 64, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
   SPJ_CUDA(cudaGetLastError());
+  check_traversal(tv_, s);
   stats_.lookups += h[0];
   stats_.window_misses += h[1];
   stats_.lbvh_fallbacks += h[2];

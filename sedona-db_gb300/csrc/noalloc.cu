@@ -107,6 +107,7 @@ extern "C" int SpjIndexProbeNoAlloc(struct SedonaFloatIndex2D* index, const floa
     uint64_t total = 0;
     SPJ_CUDA(cudaMemcpyAsync(&total, offs + n_rects, sizeof total, cudaMemcpyDeviceToHost, s));
     SPJ_CUDA(cudaStreamSynchronize(s));
+    spj::check_traversal(t, s);
     *n_pairs = total;
     if (total > capacity) {
       if (err) *err = "output capacity " + std::to_string(capacity) + " < " +

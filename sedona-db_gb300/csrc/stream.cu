@@ -251,6 +251,7 @@ uint64_t StreamJoin::run(int predicate, const uint32_t** d_build, const uint32_t
     SPJ_CUDA(cudaGraphLaunch(exec_, s_));
     SPJ_CUDA(cudaEventRecord(ev1_, s_));
     SPJ_CUDA(cudaStreamSynchronize(s_));
+    check_traversal(eng_.lbvh().view(), s_);
     m = h_tot_[0];
     total = h_tot_[1];
     if (m > ccap_) {
