@@ -1044,6 +1044,11 @@ static void* knn_worker(void* arg) {
             const ogeom_t* gb = &c->B->g[id];
             double d = hypot(px - gb->pt.x, py - gb->pt.y);
             if (have == k && !knn_better(d, id, bd[k - 1], bi[k - 1])) continue;
+            /* a point whose outward box straddles a cell edge is listed in
+               every cell it touches: keep one entry per build row */
+            int dup = 0;
+            for (int t = 0; t < have && !dup; t++) dup = bi[t] == id;
+            if (dup) continue;
             int j = have < k ? have++ : k - 1;
             while (j > 0 && knn_better(d, id, bd[j - 1], bi[j - 1])) {
               bd[j] = bd[j - 1];

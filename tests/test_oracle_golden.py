@@ -110,6 +110,33 @@ def test_knn_bruteforce(oracle_lib):
         assert np.array_equal(od[i], d[order])
 
 
+@pytest.mark.parametrize("case", ["offset", "lattice"])
+def test_knn_bruteforce_cell_edges_and_ties(oracle_lib, case):
+    """Points at 1e5 offsets on a 1e-3 lattice (outward f32 boxes straddle
+    grid cells, so one point sits in several cells) and exact distance ties
+    on an integer lattice: each build row at most once, ties by row id."""
+    from sedona_gpuspatial import wkb
+    rng = np.random.default_rng(8)
+    if case == "offset":
+        bx = 1e5 + rng.uniform(0, 3.0, 4000).round(3)
+        by = -1e5 + rng.uniform(0, 3.0, 4000).round(3)
+        px = 1e5 + rng.uniform(0, 3.0, 300)
+        py = -1e5 + rng.uniform(0, 3.0, 300)
+    else:
+        g = np.arange(40, dtype=np.float64)
+        bx, by = [a.ravel() for a in np.meshgrid(g, g)]
+        px = rng.integers(0, 80, 300) / 2.0
+        py = rng.integers(0, 80, 300) / 2.0
+    B = oracle_lib.Geoms(wkb.points_column(bx, by)); P = oracle_lib.Geoms(wkb.points_column(px, py))
+    for k in (1, 5, 12, 20):
+        ob, od = oracle_lib.knn(B, P, k, nthreads=2)
+        for i in range(0, 300, 7):
+            d = np.hypot(px[i] - bx, py[i] - by)
+            order = np.lexsort((np.arange(len(bx)), d))[:k]
+            assert np.array_equal(ob[i], order.astype(np.uint32)), (case, k, i)
+            assert np.array_equal(od[i], d[order])
+
+
 def test_dwithin_bruteforce(oracle_lib):
     from sedona_gpuspatial import wkb
     rng = np.random.default_rng(4)
