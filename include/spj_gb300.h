@@ -185,6 +185,7 @@ struct SpjLearnedStats {
   /* stage one: radix table of root_entries prefixes of (key - first key)
    * >> root_shift; mean_err: mean over leaves of the max |rank error| */
   double root_shift, root_entries, mean_err, grad_norm_after, ms_build;
+  uint64_t ranges; /* build-point ranges (key runs, LBVH leaves) the queries produced */
 };
 
 int SpjLearnedCreate(const struct SpjLearnedConfig* config, SpjLearned** out);

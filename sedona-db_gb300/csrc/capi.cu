@@ -981,6 +981,7 @@ extern "C" int SpjLearnedGetStats(SpjLearned* li, SpjLearnedStats* out) {
     out->mean_err = s.mean_err;
     out->grad_norm_after = s.grad_norm_after;
     out->ms_build = li->ms_build;
+    out->ranges = s.ranges;
   });
 }
 

@@ -307,194 +307,200 @@ __device__ __forceinline__ bool range_pred(const GeomsView& P, uint32_t pr, doub
   return false;
 }
 
+// First index >= lo whose key is not q (lo itself when keys[lo] != q):
+// gallop, then bisect.
+__device__ __forceinline__ uint32_t run_end(const uint32_t* keys, uint32_t n, uint32_t lo,
+                                            uint32_t q, uint32_t& steps) {
+  if (lo >= n || keys[lo] != q) return lo;
+  uint32_t a = lo, b = lo + 1, step = 1;
+  while (b < n && keys[b] == q) {  // keys[a] == q throughout
+    a = b;
+    step <<= 1;
+    b = (n - a > step) ? a + step : n;
+    steps++;
+  }
+  while (b - a > 1) {  // keys[a] == q, b == n or keys[b] != q
+    const uint32_t mid = a + ((b - a) >> 1);
+    steps++;
+    if (keys[mid] == q) a = mid;
+    else b = mid;
+  }
+  return b;
+}
+
+// Probe row classes: what a row contributes for the predicate.
+enum RowClass : int { kRowNone = 0, kRowLookup = 1, kRowRange = 2 };
+
+// pred(build point, probe row): point rows are equality lookups (touches is
+// always false for two points, tg.c:1102-1106); polygon rows are ranges:
+// within -> the polygon contains the point, intersects / coveredby -> covers;
+// contains / equals are always false for a point (tg.c:1157-1162).  Other
+// predicates are not supported (status, reported once in the counting pass).
+__device__ __forceinline__ int row_class(uint8_t kind, int predicate, DeviceStatus* st,
+                                         uint32_t row, bool report) {
+  if (kind == kPoint) {
+    if (predicate == kTouches) return kRowNone;
+    if (predicate == kDisjoint) {
+      if (report) status_fail(st, kUnsupported, row);
+      return kRowNone;
+    }
+    return kRowLookup;
+  }
+  if (kind == kPolygon || kind == kMultiPolygon) {
+    if (predicate == kContains || predicate == kEquals) return kRowNone;
+    if (predicate != kIntersects && predicate != kCoveredBy && predicate != kWithin) {
+      if (report) status_fail(st, kUnsupported, row);
+      return kRowNone;
+    }
+    return kRowRange;
+  }
+  return kRowNone;
+}
+
+constexpr uint32_t kRangeSorted = 0;  // ranks in the key-sorted build points
+constexpr uint32_t kRangeLeaf = 1;    // an LBVH leaf (sorted primitive indices)
+
+// ranges are written at pos < cap only (the count pass sized them)
+template <int kPass>
+__device__ __forceinline__ void put_range(uint4* ranges, uint64_t& pos, uint32_t& cnt,
+                                          uint32_t start, uint32_t len, uint32_t row,
+                                          uint32_t kind, uint64_t cap) {
+  if (len == 0) return;
+  if (kPass) {
+    if (pos < cap) ranges[pos] = make_uint4(start, len, row, kind);
+    pos++;
+  } else {
+    cnt++;
+  }
+}
+
+// The LBVH leaves whose boxes overlap q, as ranges (the fallback).
+template <int kPass>
+__device__ void leaf_ranges(const LbvhView& t, float4 q, int* stack, uint32_t row, uint4* ranges,
+                            uint64_t& pos, uint32_t& cnt, uint64_t cap) {
+  if (t.nprims == 0) return;
+  const uint64_t max_steps = 2ull * t.nleaves + 2;
+  uint64_t steps = 0;
+  int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
+  while (true) {
+    if (++steps > max_steps) {  // each node is visited at most once
+      traversal_fault(t, kTooLong, row);
+      break;
+    }
+    if (node < 0) {
+      const uint32_t c = (uint32_t)(~node);
+      if (c >= t.nleaves) {
+        traversal_fault(t, kBadLeaf, c);
+        break;
+      }
+      const uint32_t b0 = c * t.leaf_size, b1 = min(b0 + t.leaf_size, t.nprims);
+      put_range<kPass>(ranges, pos, cnt, b0, b1 - b0, row, kRangeLeaf, cap);
+    } else {
+      if ((uint32_t)node + 1 >= t.nleaves) {
+        traversal_fault(t, kBadNode, (unsigned)node);
+        break;
+      }
+      const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+      const int2 ch = t.node_child[node];
+      const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
+      if (hl && hr) {
+        if (sp < kTravStack) stack[sp * 128] = ch.y;
+        sp++;
+        node = ch.x;
+        continue;
+      }
+      if (hl || hr) {
+        node = hl ? ch.x : ch.y;
+        continue;
+      }
+    }
+    if (sp == 0) break;
+    sp--;
+    node = sp < kTravStack ? stack[sp * 128] : 0;
+  }
+}
+
+// Sort key of a probe row (its lookup key, or its box centre's), so that
+// neighbouring threads search neighbouring parts of the model and the keys.
+__global__ void k_row_keys(LearnedView v, GeomsView P, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const float4 b = P.box[i];
+    uint32_t key = 0xFFFFFFFFu;
+    if (b.x <= b.z && b.y <= b.w)
+      key = key_of(v, make_float2(0.5f * b.x + 0.5f * b.z, 0.5f * b.y + 0.5f * b.w));
+    keys[i] = key;
+    vals[i] = i;
+  }
+}
+
+// Phase A: per probe row, the build-point ranges that can hold its pairs:
+// for a lookup the run of its key among the sorted keys (found through the
+// model), for a box the runs of the grid cells it covers, and LBVH leaves
+// where the model's error exceeds the window or the box covers too many
+// cells.  Pass 0 counts, pass 1 writes at the scanned offsets (row order).
 template <int kPass>
 __global__ void __launch_bounds__(128)
-    k_learned_query(LearnedView v, LbvhView t, GeomsView B, GeomsView P, uint32_t probe_base,
-                    int predicate, uint32_t* __restrict__ counts,
-                    const uint64_t* __restrict__ offs, uint32_t* __restrict__ ob,
-                    uint32_t* __restrict__ op, unsigned long long* __restrict__ ctr,
-                    DeviceStatus* st) {
-  __shared__ int stack[64 * 128];
-  uint32_t steps = 0, misses = 0, fallbacks = 0, lookups = 0, esc = 0;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t trips = (P.n + stride - 1) / stride;
-  for (uint32_t tr = 0; tr < trips; tr++) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + tr * stride;
-    if (i >= P.n) continue;
-    const uint8_t kind = P.kind[i];
-    uint32_t cnt = 0;
-    uint64_t pos = kPass ? offs[i] : 0;
-    auto emit = [&](uint32_t build_row) {
-      if (kPass) {
-        ob[pos] = build_row;
-        op[pos] = i + probe_base;
-        pos++;
-      } else {
-        cnt++;
-      }
-    };
-    const bool is_point = kind == kPoint;
-    const bool is_poly = kind == kPolygon || kind == kMultiPolygon;
-    bool aoe = true;
-    bool ok = true;
-    if (is_point) {
-      // point-point: every predicate is equality except touches (always
-      // false, tg.c:1102-1106); disjoint is not a join predicate here
-      if (predicate == kTouches) ok = false;
-      if (predicate == kDisjoint) {
-        ok = false;
-        status_fail(st, kUnsupported, i);
-      }
-    } else if (is_poly) {
-      // pred(build point, probe polygon): within -> polygon contains point,
-      // intersects / coveredby -> polygon covers point; contains / equals
-      // are always false for a point (tg.c:1157-1162); the rest unsupported
-      if (predicate == kWithin) {
-        aoe = false;
-      } else if (predicate == kContains || predicate == kEquals) {
-        ok = false;
-      } else if (predicate != kIntersects && predicate != kCoveredBy) {
-        ok = false;
-        status_fail(st, kUnsupported, i);
-      }
-    }
-    if (!ok) {
-      if (!kPass) counts[i] = 0;
+    k_learned_ranges(LearnedView v, LbvhView t, GeomsView P, int predicate,
+                     const uint32_t* __restrict__ order, uint32_t* __restrict__ rcount,
+                     const uint64_t* __restrict__ roff, uint4* __restrict__ ranges,
+                     uint64_t cap, unsigned long long* __restrict__ ctr, DeviceStatus* st) {
+  __shared__ int stack[kTravStack * 128];
+  // steps: the model-guided lower_bound searches; rsteps: the runs of equal
+  // keys after them (independent of the model, not counted)
+  uint32_t steps = 0, misses = 0, fallbacks = 0, lookups = 0, rsteps = 0;
+  for (uint32_t jj = blockIdx.x * blockDim.x + threadIdx.x; jj < P.n;
+       jj += gridDim.x * blockDim.x) {
+    const uint32_t i = order ? order[jj] : jj;
+    if (i >= P.n) {
+      traversal_fault(t, kBadProbe, i);
       continue;
     }
-    if (is_point) {
-      const double2 p = P.pt[i];
+    const int cls = row_class(P.kind[i], predicate, st, i, kPass == 0);
+    uint32_t cnt = 0;
+    uint64_t pos = kPass ? roff[i] : 0;
+    if (cls == kRowLookup) {
       const float4 pb = P.box[i];
-      const float2 p32 = make_float2(pb.x, pb.y);
-      const uint32_t q = key_of(v, p32);
+      const uint32_t q = key_of(v, make_float2(pb.x, pb.y));
       bool bad = false;
       lookups++;
-      uint32_t j = learned_lower_bound(v, q, steps, misses, bad);
+      const uint32_t lo = learned_lower_bound(v, q, steps, misses, bad);
       if (!bad) {
-        for (; j < v.n && v.keys[j] == q; j++)
-          if (pteq(v.xy[j], p)) emit(v.ids[j]);
+        const uint32_t hi = run_end(v.keys, v.n, lo, q, rsteps);
+        put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap);
       } else {
         fallbacks++;
-        // LBVH: build rows whose RN32 point equals the probe's RN32 point
-        int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
-        uint64_t tsteps = 0;
-        while (t.nprims > 0) {
-          if (++tsteps > 2ull * t.nleaves + 2) {  // each node is visited at most once
-            traversal_fault(t, kTooLong, i);
-            break;
-          }
-          if (node < 0) {
-            const uint32_t c = (uint32_t)(~node), b0 = c * t.leaf_size;
-            if (c >= t.nleaves) {
-              traversal_fault(t, kBadLeaf, c);
-              break;
-            }
-            const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
-            for (uint32_t k = b0; k < b1; k++)
-              if (in_box(make_float2(t.sorted_box[k].x, t.sorted_box[k].y), pb)) {
-                const uint32_t id = t.sorted_id[k];
-                if (pteq(B.pt[id], p)) emit(id);
-              }
-          } else {
-            if ((uint32_t)node + 1 >= t.nleaves) {
-              traversal_fault(t, kBadNode, (unsigned)node);
-              break;
-            }
-            const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
-            const int2 ch = t.node_child[node];
-            const bool hl = !(lb.x > pb.z || lb.z < pb.x || lb.y > pb.w || lb.w < pb.y);
-            const bool hr = !(rb.x > pb.z || rb.z < pb.x || rb.y > pb.w || rb.w < pb.y);
-            if (hl && hr) {
-              if (sp < 64) stack[sp * 128 + threadIdx.x] = ch.y;
-              sp++;
-              node = ch.x;
-              continue;
-            }
-            if (hl || hr) {
-              node = hl ? ch.x : ch.y;
-              continue;
-            }
-          }
-          if (sp == 0) break;
-          sp--;
-          node = sp < 64 ? stack[sp * 128 + threadIdx.x] : 0;
-        }
+        leaf_ranges<kPass>(t, pb, stack + threadIdx.x, i, ranges, pos, cnt, cap);
       }
-    } else if (is_poly) {
+    } else if (cls == kRowRange) {
       const float4 bx = P.box[i];  // outward f32 box of the probe polygon
       const uint32_t cx0 = cell_of(bx.x, v.x0, v.sx), cx1 = cell_of(bx.z, v.x0, v.sx);
       const uint32_t cy0 = cell_of(bx.y, v.y0, v.sy), cy1 = cell_of(bx.w, v.y0, v.sy);
       const uint64_t ncell = (uint64_t)(cx1 - cx0 + 1) * (cy1 - cy0 + 1);
-      bool use_tree = ncell > kMaxCells;
-      if (!use_tree) {
-        // a leaf over the window anywhere in the box sends the row to the LBVH
+      if (bx.x <= bx.z && bx.y <= bx.w) {  // (an empty box has no pairs)
+        bool use_tree = ncell > kMaxCells;
+        // a cell whose leaf is over the window sends the row to the LBVH
         for (uint32_t cy = cy0; cy <= cy1 && !use_tree; cy++)
           for (uint32_t cx = cx0; cx <= cx1 && !use_tree; cx++)
             use_tree = v.err[root_leaf(v, hilbert16(cx, cy))] > v.window;
-      }
-      if (!use_tree) {
-        for (uint32_t cy = cy0; cy <= cy1; cy++) {
-          for (uint32_t cx = cx0; cx <= cx1; cx++) {
-            const uint32_t q = hilbert16(cx, cy);
-            bool bad = false;
-            lookups++;
-            uint32_t j = learned_lower_bound(v, q, steps, misses, bad);
-            for (; j < v.n && v.keys[j] == q; j++) {
-              const float2 p32 = v.xy32[j];
-              if (!in_box(p32, bx)) continue;
-              if (range_pred(P, i, v.xy[j], p32, aoe, esc)) emit(v.ids[j]);
+        if (!use_tree) {
+          for (uint32_t cy = cy0; cy <= cy1; cy++) {
+            for (uint32_t cx = cx0; cx <= cx1; cx++) {
+              const uint32_t q = hilbert16(cx, cy);
+              bool bad = false;
+              lookups++;
+              const uint32_t lo = learned_lower_bound(v, q, steps, misses, bad);
+              const uint32_t hi = run_end(v.keys, v.n, lo, q, rsteps);
+              put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap);
             }
           }
-        }
-      } else {
-        fallbacks++;
-        int sp = 0, node = t.nleaves > 1 ? 0 : ~0;
-        uint64_t tsteps = 0;
-        while (t.nprims > 0) {
-          if (++tsteps > 2ull * t.nleaves + 2) {  // each node is visited at most once
-            traversal_fault(t, kTooLong, i);
-            break;
-          }
-          if (node < 0) {
-            const uint32_t c = (uint32_t)(~node), b0 = c * t.leaf_size;
-            if (c >= t.nleaves) {
-              traversal_fault(t, kBadLeaf, c);
-              break;
-            }
-            const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
-            for (uint32_t k = b0; k < b1; k++) {
-              const float4 sb = t.sorted_box[k];
-              if (!in_box(make_float2(sb.x, sb.y), bx)) continue;
-              const uint32_t id = t.sorted_id[k];
-              if (range_pred(P, i, B.pt[id], make_float2(sb.x, sb.y), aoe, esc)) emit(id);
-            }
-          } else {
-            if ((uint32_t)node + 1 >= t.nleaves) {
-              traversal_fault(t, kBadNode, (unsigned)node);
-              break;
-            }
-            const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
-            const int2 ch = t.node_child[node];
-            const bool hl = !(lb.x > bx.z || lb.z < bx.x || lb.y > bx.w || lb.w < bx.y);
-            const bool hr = !(rb.x > bx.z || rb.z < bx.x || rb.y > bx.w || rb.w < bx.y);
-            if (hl && hr) {
-              if (sp < 64) stack[sp * 128 + threadIdx.x] = ch.y;
-              sp++;
-              node = ch.x;
-              continue;
-            }
-            if (hl || hr) {
-              node = hl ? ch.x : ch.y;
-              continue;
-            }
-          }
-          if (sp == 0) break;
-          sp--;
-          node = sp < 64 ? stack[sp * 128 + threadIdx.x] : 0;
+        } else {
+          fallbacks++;
+          leaf_ranges<kPass>(t, bx, stack + threadIdx.x, i, ranges, pos, cnt, cap);
         }
       }
     }
-    if (!kPass) counts[i] = cnt;
+    if (!kPass) rcount[i] = cnt;
   }
   if (kPass == 0) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -502,15 +508,99 @@ __global__ void __launch_bounds__(128)
       misses += __shfl_xor_sync(0xffffffffu, misses, o);
       fallbacks += __shfl_xor_sync(0xffffffffu, fallbacks, o);
       lookups += __shfl_xor_sync(0xffffffffu, lookups, o);
-      esc += __shfl_xor_sync(0xffffffffu, esc, o);
     }
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(&ctr[0], (unsigned long long)lookups);
       atomicAdd(&ctr[1], (unsigned long long)misses);
       atomicAdd(&ctr[2], (unsigned long long)fallbacks);
       atomicAdd(&ctr[3], (unsigned long long)steps);
-      atomicAdd(&ctr[4], (unsigned long long)esc);
     }
+  }
+}
+
+// Phase B: the candidates of the ranges, load-balanced.  A warp takes 32
+// consecutive ranges, scans their lengths, and walks the concatenated
+// candidates 32 at a time, each lane finding its range by a 5-step search
+// over the scan; lookups test point equality, boxes the RN32 in-box test and
+// then the polygon predicate.  Pass 0 counts per chunk of 32 ranges, pass 1
+// writes with ballot ranks at the chunk's scanned offset, so pairs stay in
+// range order (grouped by probe row).
+template <int kPass>
+__global__ void __launch_bounds__(128)
+    k_learned_eval(LearnedView v, LbvhView t, GeomsView B, GeomsView P, uint32_t probe_base,
+                   int predicate, const uint4* __restrict__ ranges, uint64_t nranges,
+                   uint32_t* __restrict__ ccount, const uint64_t* __restrict__ coff,
+                   uint32_t* __restrict__ ob, uint32_t* __restrict__ op, uint64_t cap,
+                   unsigned long long* __restrict__ ctr) {
+  const bool aoe = predicate != kWithin;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nchunks = (nranges + 31) / 32;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint32_t esc = 0;
+  for (uint64_t chunk = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; chunk < nchunks;
+       chunk += nwarps) {
+    const uint64_t r = chunk * 32 + lane;
+    const uint4 R = r < nranges ? ranges[r] : make_uint4(0, 0, 0, 0);
+    uint32_t incl = R.y;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += x;
+    }
+    const uint32_t excl = incl - R.y;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint64_t pos = kPass ? coff[chunk] : 0;
+    uint32_t cnt = 0;
+    for (uint32_t base = 0; base < total; base += 32) {
+      const uint32_t tt = base + lane;
+      // owner: the last lane whose exclusive offset is <= tt (it has len > 0)
+      int L = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t e = __shfl_sync(0xffffffffu, excl, L + step);
+        if (e <= tt) L += step;
+      }
+      const uint32_t start = __shfl_sync(0xffffffffu, R.x, L);
+      const uint32_t row = __shfl_sync(0xffffffffu, R.z, L);
+      const uint32_t kind = __shfl_sync(0xffffffffu, R.w, L);
+      const uint32_t eL = __shfl_sync(0xffffffffu, excl, L);
+      bool hit = false;
+      uint32_t id = 0;
+      if (tt < total) {
+        const uint32_t j = start + (tt - eL);
+        double2 pt;
+        float2 pt32;
+        if (kind == kRangeSorted) {
+          pt = v.xy[j];
+          pt32 = v.xy32[j];
+          id = v.ids[j];
+        } else {
+          const float4 sb = t.sorted_box[j];
+          pt32 = make_float2(sb.x, sb.y);
+          id = t.sorted_id[j];
+          pt = B.pt[id];
+        }
+        if (P.kind[row] == kPoint) hit = pteq(pt, P.pt[row]);
+        else hit = in_box(pt32, P.box[row]) && range_pred(P, row, pt, pt32, aoe, esc);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (kPass) {
+        if (hit) {
+          const uint64_t o = pos + __popc(m & ((1u << lane) - 1u));
+          if (o < cap) {
+            ob[o] = id;
+            op[o] = row + probe_base;
+          }
+        }
+        pos += __popc(m);
+      } else {
+        cnt += __popc(m);
+      }
+    }
+    if (!kPass && lane == 0) ccount[chunk] = cnt;
+  }
+  if (kPass == 0) {
+    for (int o = 16; o > 0; o >>= 1) esc += __shfl_xor_sync(0xffffffffu, esc, o);
+    if (lane == 0 && esc) atomicAdd(&ctr[4], (unsigned long long)esc);
   }
 }
 
@@ -734,29 +824,62 @@ void LearnedIndex::loss_and_grad(const std::vector<double>& a, const std::vector
 uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int predicate,
                              DevBuf& out_build, DevBuf& out_probe, cudaStream_t s) {
   const uint32_t np = probe.n;
-  counts_.reserve(((size_t)np + 1) * 4, s);
-  offs_.reserve(((size_t)np + 1) * 8, s);
   scratch_.reserve(sizeof(DeviceStatus), s);
   reset_status(scratch_, s);
   SPJ_CUDA(cudaMemsetAsync(counters_.get(), 0, 64, s));
   const LearnedView v = SPJ_LVIEW();
   DeviceStatus* st = scratch_.as<DeviceStatus>();
   auto* ctr = counters_.as<unsigned long long>();
-  const int g = grid_for(np, 128, kNumSMs * 16);
-  if (np)
-    k_learned_query<0><<<g, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate,
-                                         counts_.as<uint32_t>(), nullptr, nullptr, nullptr, ctr,
-                                         st);
+  if (np == 0) {
+    out_build.reserve(4, s);
+    out_probe.reserve(4, s);
+    return 0;
+  }
+  // probe rows in key order (locality of the model and key searches)
+  const size_t rb = ((size_t)np + 1) * 4;
+  order_.reserve(rb, s);
+  okeys_.reserve(rb, s);
+  akeys_.reserve(rb, s);
+  avals_.reserve(rb, s);
+  k_row_keys<<<grid_for(np, 256), 256, 0, s>>>(v, probe, okeys_.as<uint32_t>(),
+                                               order_.as<uint32_t>());
+  radix_sort_pairs(okeys_.as<uint32_t>(), order_.as<uint32_t>(), akeys_.as<uint32_t>(),
+                   avals_.as<uint32_t>(), np, 32, tmp_, s);
+  // phase A: ranges per row
+  counts_.reserve(rb, s);
+  offs_.reserve(((size_t)np + 1) * 8, s);
+  const int ga = grid_for(np, 128, kNumSMs * 16);
+  k_learned_ranges<0><<<ga, 128, 0, s>>>(v, tv_, probe, predicate, order_.as<uint32_t>(),
+                                         counts_.as<uint32_t>(), nullptr, nullptr, 0, ctr, st);
   scan_u32_u64(counts_.as<uint32_t>(), offs_.as<uint64_t>(), np, tmp_, s);
-  uint64_t total = 0;
-  SPJ_CUDA(cudaMemcpyAsync(&total, offs_.as<uint64_t>() + np, 8, cudaMemcpyDeviceToHost, s));
+  uint64_t nr = 0;
+  SPJ_CUDA(cudaMemcpyAsync(&nr, offs_.as<uint64_t>() + np, 8, cudaMemcpyDeviceToHost, s));
   check_status(scratch_, s, "learned query");  // syncs
+  check_traversal(tv_, s);
+  ranges_.reserve((nr + 1) * sizeof(uint4), s);
+  k_learned_ranges<1><<<ga, 128, 0, s>>>(v, tv_, probe, predicate, order_.as<uint32_t>(), nullptr,
+                                         offs_.as<uint64_t>(), ranges_.as<uint4>(), nr, ctr, st);
+  // phase B: candidates of the ranges, a warp per 32 ranges
+  const uint64_t nch = (nr + 31) / 32;
+  ccount_.reserve((nch + 1) * 4, s);
+  coff_.reserve((nch + 1) * 8, s);
+  const int gb = grid_for((int64_t)(nch * 32), 128, kNumSMs * 16);
+  uint64_t total = 0;
+  if (nch) {
+    k_learned_eval<0><<<gb, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate,
+                                         ranges_.as<uint4>(), nr, ccount_.as<uint32_t>(), nullptr,
+                                         nullptr, nullptr, 0, ctr);
+    scan_u32_u64(ccount_.as<uint32_t>(), coff_.as<uint64_t>(), (int64_t)nch, tmp_, s);
+    SPJ_CUDA(cudaMemcpyAsync(&total, coff_.as<uint64_t>() + nch, 8, cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+  }
   out_build.reserve((total + 1) * 4, s);
   out_probe.reserve((total + 1) * 4, s);
-  if (np)
-    k_learned_query<1><<<g, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate, nullptr,
-                                         offs_.as<uint64_t>(), out_build.as<uint32_t>(),
-                                         out_probe.as<uint32_t>(), ctr, st);
+  if (nch)
+    k_learned_eval<1><<<gb, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate,
+                                         ranges_.as<uint4>(), nr, nullptr, coff_.as<uint64_t>(),
+                                         out_build.as<uint32_t>(), out_probe.as<uint32_t>(), total,
+                                         ctr);
   unsigned long long h[8];
   SPJ_CUDA(cudaMemcpyAsync(h, counters_.get(), 64, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
@@ -766,6 +889,7 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
   stats_.window_misses += h[1];
   stats_.lbvh_fallbacks += h[2];
   stats_.search_steps += h[3];
+  stats_.ranges += nr;
   return total;
 }
 

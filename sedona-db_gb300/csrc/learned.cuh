@@ -33,6 +33,7 @@ struct LearnedStats {
   double grad_norm_after = 0;  // max |gradient| over leaves after the Newton step
   uint64_t lookups = 0, window_misses = 0, lbvh_fallbacks = 0;
   uint64_t search_steps = 0;  // binary-search steps over all lookups
+  uint64_t ranges = 0;        // build-point ranges handed to the candidate phase
 };
 
 struct LearnedView;
@@ -74,6 +75,7 @@ class LearnedIndex {
   DevBuf leaf_start_, leaf_a_, leaf_b_, leaf_kc_, leaf_err_, counters_, counts_, offs_, tmp_,
       scratch_;
   DevBuf root_tab_;
+  DevBuf order_, okeys_, akeys_, avals_, ranges_, ccount_, coff_;  // query scratch
   uint32_t root_shift_ = 0, root_p_ = 1;
   uint32_t k0_ = 0;
   LearnedStats stats_;

@@ -178,7 +178,8 @@ class SpjLearnedStats(C.Structure):
                 ("leaves_over_window", C.c_uint32), ("trained", C.c_uint32),
                 ("root_shift", C.c_double), ("root_entries", C.c_double),
                 ("mean_err", C.c_double),
-                ("grad_norm_after", C.c_double), ("ms_build", C.c_double)]
+                ("grad_norm_after", C.c_double), ("ms_build", C.c_double),
+                ("ranges", C.c_uint64)]
 
 _lib = None
 _lib_lock = threading.Lock()
