@@ -510,6 +510,14 @@ def run_learned(args, world, rank, local, pg):
     li = capi.LearnedIndex(rt, leaves=4096)
     li.build_device(db_)
     st_build = li.stats()
+    # window autotuned on a sample (a tenth of each probe column)
+    ns = max(1, len(boxes) // 10)
+    sb, ksb = to_device(boxes.slice(0, ns))
+    sl, ksl = to_device(lookups.slice(0, max(1, len(lookups) // 10)))
+    t0 = time.perf_counter()
+    window = li.autotune_window([sb, sl], "intersects")
+    tune_ms = (time.perf_counter() - t0) * 1e3
+    del ksb, ksl
 
     def step(obj, method):
         n = 0
@@ -538,6 +546,7 @@ def run_learned(args, world, rank, local, pg):
     after = li.stats()
     ms = barrier_max(pg, e0.elapsed_time(e1) / args.steps, dev)
     lookups_n = after["lookups"] - before["lookups"]
+    phases = {k: (after[k] - before[k]) / args.steps for k in ("ms_order", "ms_ranges", "ms_eval")}
     steps_per_lookup = (after["search_steps"] - before["search_steps"]) / max(1, lookups_n)
 
     # ablation: the untrained model (line through each leaf's end keys)
@@ -592,7 +601,11 @@ def run_learned(args, world, rank, local, pg):
                    "pairs_per_step": npairs, "leaves": 4096,
                    "l2": "probe columns > L2, no flush", "parallelism": f"replicas x{world}"},
         "probe_rows_per_s": n_rows * world / (ms * 1e-3),
-        "learned_index": {"build_ms": st_build["ms_build"], "max_err": st_build["max_err"],
+        "learned_index": {"build_ms": st_build["ms_build"], "window": window,
+                          "window_autotune_ms": tune_ms,
+                          "phases_ms_per_step": phases,
+                          "leaves_over_window_after_tuning": after["leaves_over_window"],
+                          "max_err": st_build["max_err"],
                           "mean_err": st_build["mean_err"],
                           "leaves_over_window": st_build["leaves_over_window"],
                           "lbvh_fallback_rows_per_step":

@@ -186,6 +186,10 @@ struct SpjLearnedStats {
    * >> root_shift; mean_err: mean over leaves of the max |rank error| */
   double root_shift, root_entries, mean_err, grad_norm_after, ms_build;
   uint64_t ranges; /* build-point ranges (key runs, LBVH leaves) the queries produced */
+  /* cumulative query phase times (CUDA events): probe ordering, ranges
+   * through the model, candidate evaluation and output */
+  double ms_order, ms_ranges, ms_eval;
+  uint32_t window;
 };
 
 int SpjLearnedCreate(const struct SpjLearnedConfig* config, SpjLearned** out);
@@ -212,6 +216,14 @@ int SpjLearnedExport(SpjLearned* li, uint32_t* keys, uint32_t* leaf_start, uint3
                      double* a, double* b, uint32_t* err);
 int SpjLearnedGetStats(SpjLearned* li, struct SpjLearnedStats* out);
 void* SpjLearnedStream(SpjLearned* li);
+/* The window: the largest per-leaf error the model serves; rows whose leaf
+ * error exceeds it take the LBVH fallback.  Queries only; no rebuild. */
+int SpjLearnedSetWindow(SpjLearned* li, uint32_t window);
+/* Times queries of the sample columns (device WKB) for windows 2^10 .. 2^17
+ * and the model's max error (no fallback), best of two runs each, sets the
+ * fastest and returns it in *window. */
+int SpjLearnedAutotuneWindow(SpjLearned* li, const struct SpjDeviceWkb* samples,
+                             uint32_t n_samples, int32_t predicate, uint32_t* window);
 
 /* ------------------------------------------------------------------------ */
 /* KNN join over point columns                                              */

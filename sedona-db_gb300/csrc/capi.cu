@@ -932,6 +932,73 @@ extern "C" int SpjLearnedQueryDevice(SpjLearned* li, const SpjDeviceWkb* probe, 
   });
 }
 
+extern "C" int SpjLearnedSetWindow(SpjLearned* li, uint32_t window) {
+  return guarded(li->last_error, [&] {
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    SPJ_CHECK(window >= 1, "window must be positive");
+    li->index->set_window(window);
+    li->window = window;
+  });
+}
+
+extern "C" int SpjLearnedAutotuneWindow(SpjLearned* li, const SpjDeviceWkb* samples,
+                                        uint32_t n_samples, int32_t predicate,
+                                        uint32_t* window) {
+  return guarded(li->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(li->rt->device_id));
+    SPJ_CHECK(li->index != nullptr, "learned index is not built");
+    SPJ_CHECK(samples && n_samples > 0 && window, "no samples or null output");
+    SPJ_CHECK(predicate >= 0 && predicate <= 7, "relation predicates only");
+    Workspace& ws = *li->ws;
+    std::vector<uint32_t> cand;
+    for (uint32_t w = 1u << 10; w <= (1u << 17); w <<= 1) cand.push_back(w);
+    const uint32_t mx = li->index->stats().max_err;
+    if (mx > cand.back()) cand.push_back(mx);
+    cudaEvent_t e0, e1;
+    SPJ_CUDA(cudaEventCreate(&e0));
+    SPJ_CUDA(cudaEventCreate(&e1));
+    const uint32_t before = li->index->window();
+    uint32_t best = before;
+    float best_ms = INFINITY;
+    try {
+      for (uint32_t w : cand) {
+        li->index->set_window(w);
+        float t_min = INFINITY;
+        for (int rep = 0; rep < 2; rep++) {
+          float t = 0;
+          for (uint32_t k = 0; k < n_samples; k++) {
+            decode_wkb(device_column(&samples[k]), ws.probe, ws.dsc, ws.last_probe_points,
+                       ws.stream);
+            ws.last_probe_points = ws.probe.all_points;
+            SPJ_CUDA(cudaEventRecord(e0, ws.stream));
+            li->index->query(ws.probe.view(), 0, predicate, li->out_b, li->out_p, ws.stream);
+            SPJ_CUDA(cudaEventRecord(e1, ws.stream));
+            SPJ_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            t += ms;
+          }
+          t_min = std::min(t_min, t);
+        }
+        if (t_min < best_ms) {
+          best_ms = t_min;
+          best = w;
+        }
+      }
+    } catch (...) {
+      li->index->set_window(before);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    li->index->set_window(best);
+    li->window = best;
+    *window = best;
+  });
+}
+
 extern "C" int SpjLearnedLossAndGrad(SpjLearned* li, const double* a, const double* b,
                                      double* loss, double* grad_a, double* grad_b) {
   return guarded(li->last_error, [&] {
@@ -982,6 +1049,10 @@ extern "C" int SpjLearnedGetStats(SpjLearned* li, SpjLearnedStats* out) {
     out->grad_norm_after = s.grad_norm_after;
     out->ms_build = li->ms_build;
     out->ranges = s.ranges;
+    out->ms_order = s.ms_order;
+    out->ms_ranges = s.ms_ranges;
+    out->ms_eval = s.ms_eval;
+    out->window = li->index->window();
   });
 }
 

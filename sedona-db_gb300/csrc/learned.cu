@@ -360,16 +360,22 @@ __device__ __forceinline__ int row_class(uint8_t kind, int predicate, DeviceStat
 constexpr uint32_t kRangeSorted = 0;  // ranks in the key-sorted build points
 constexpr uint32_t kRangeLeaf = 1;    // an LBVH leaf (sorted primitive indices)
 
+// A row's first kRangeCache ranges are kept by the counting pass (start,
+// len | kind << 31), so the writing pass copies them instead of searching
+// again; rows with more ranges search again.
+constexpr uint32_t kRangeCache = 4;
+
 // ranges are written at pos < cap only (the count pass sized them)
 template <int kPass>
 __device__ __forceinline__ void put_range(uint4* ranges, uint64_t& pos, uint32_t& cnt,
                                           uint32_t start, uint32_t len, uint32_t row,
-                                          uint32_t kind, uint64_t cap) {
+                                          uint32_t kind, uint64_t cap, uint2* cache) {
   if (len == 0) return;
   if (kPass) {
     if (pos < cap) ranges[pos] = make_uint4(start, len, row, kind);
     pos++;
   } else {
+    if (cnt < kRangeCache) cache[(size_t)row * kRangeCache + cnt] = make_uint2(start, len | (kind << 31));
     cnt++;
   }
 }
@@ -377,7 +383,7 @@ __device__ __forceinline__ void put_range(uint4* ranges, uint64_t& pos, uint32_t
 // The LBVH leaves whose boxes overlap q, as ranges (the fallback).
 template <int kPass>
 __device__ void leaf_ranges(const LbvhView& t, float4 q, int* stack, uint32_t row, uint4* ranges,
-                            uint64_t& pos, uint32_t& cnt, uint64_t cap) {
+                            uint64_t& pos, uint32_t& cnt, uint64_t cap, uint2* cache) {
   if (t.nprims == 0) return;
   const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint64_t steps = 0;
@@ -394,7 +400,7 @@ __device__ void leaf_ranges(const LbvhView& t, float4 q, int* stack, uint32_t ro
         break;
       }
       const uint32_t b0 = c * t.leaf_size, b1 = min(b0 + t.leaf_size, t.nprims);
-      put_range<kPass>(ranges, pos, cnt, b0, b1 - b0, row, kRangeLeaf, cap);
+      put_range<kPass>(ranges, pos, cnt, b0, b1 - b0, row, kRangeLeaf, cap, cache);
     } else {
       if ((uint32_t)node + 1 >= t.nleaves) {
         traversal_fault(t, kBadNode, (unsigned)node);
@@ -444,7 +450,8 @@ __global__ void __launch_bounds__(128)
     k_learned_ranges(LearnedView v, LbvhView t, GeomsView P, int predicate,
                      const uint32_t* __restrict__ order, uint32_t* __restrict__ rcount,
                      const uint64_t* __restrict__ roff, uint4* __restrict__ ranges,
-                     uint64_t cap, unsigned long long* __restrict__ ctr, DeviceStatus* st) {
+                     uint64_t cap, uint2* __restrict__ cache, unsigned long long* __restrict__ ctr,
+                     DeviceStatus* st) {
   __shared__ int stack[kTravStack * 128];
   // steps: the model-guided lower_bound searches; rsteps: the runs of equal
   // keys after them (independent of the model, not counted)
@@ -459,6 +466,17 @@ __global__ void __launch_bounds__(128)
     const int cls = row_class(P.kind[i], predicate, st, i, kPass == 0);
     uint32_t cnt = 0;
     uint64_t pos = kPass ? roff[i] : 0;
+    if (kPass) {
+      const uint64_t nr = roff[i + 1] - pos;
+      if (nr <= kRangeCache) {  // kept by the counting pass
+        for (uint32_t c = 0; c < (uint32_t)nr; c++) {
+          const uint2 e = cache[(size_t)i * kRangeCache + c];
+          if (pos < cap) ranges[pos] = make_uint4(e.x, e.y & 0x7FFFFFFFu, i, e.y >> 31);
+          pos++;
+        }
+        continue;
+      }
+    }
     if (cls == kRowLookup) {
       const float4 pb = P.box[i];
       const uint32_t q = key_of(v, make_float2(pb.x, pb.y));
@@ -467,10 +485,10 @@ __global__ void __launch_bounds__(128)
       const uint32_t lo = learned_lower_bound(v, q, steps, misses, bad);
       if (!bad) {
         const uint32_t hi = run_end(v.keys, v.n, lo, q, rsteps);
-        put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap);
+        put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap, cache);
       } else {
         fallbacks++;
-        leaf_ranges<kPass>(t, pb, stack + threadIdx.x, i, ranges, pos, cnt, cap);
+        leaf_ranges<kPass>(t, pb, stack + threadIdx.x, i, ranges, pos, cnt, cap, cache);
       }
     } else if (cls == kRowRange) {
       const float4 bx = P.box[i];  // outward f32 box of the probe polygon
@@ -491,12 +509,12 @@ __global__ void __launch_bounds__(128)
               lookups++;
               const uint32_t lo = learned_lower_bound(v, q, steps, misses, bad);
               const uint32_t hi = run_end(v.keys, v.n, lo, q, rsteps);
-              put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap);
+              put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap, cache);
             }
           }
         } else {
           fallbacks++;
-          leaf_ranges<kPass>(t, bx, stack + threadIdx.x, i, ranges, pos, cnt, cap);
+          leaf_ranges<kPass>(t, bx, stack + threadIdx.x, i, ranges, pos, cnt, cap, cache);
         }
       }
     }
@@ -525,13 +543,29 @@ __global__ void __launch_bounds__(128)
 // then the polygon predicate.  Pass 0 counts per chunk of 32 ranges, pass 1
 // writes with ballot ranks at the chunk's scanned offset, so pairs stay in
 // range order (grouped by probe row).
+// Words of hit masks per chunk of 32 ranges: ceil(candidates / 32).
+__global__ void k_chunk_words(const uint4* __restrict__ ranges, uint64_t nranges,
+                              uint32_t* __restrict__ words) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nchunks = (nranges + 31) / 32;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t chunk = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; chunk < nchunks;
+       chunk += nwarps) {
+    const uint64_t r = chunk * 32 + lane;
+    uint32_t len = r < nranges ? ranges[r].y : 0;
+    for (int o = 16; o > 0; o >>= 1) len += __shfl_xor_sync(0xffffffffu, len, o);
+    if (lane == 0) words[chunk] = (len + 31) / 32;
+  }
+}
+
 template <int kPass>
 __global__ void __launch_bounds__(128)
     k_learned_eval(LearnedView v, LbvhView t, GeomsView B, GeomsView P, uint32_t probe_base,
                    int predicate, const uint4* __restrict__ ranges, uint64_t nranges,
                    uint32_t* __restrict__ ccount, const uint64_t* __restrict__ coff,
-                   uint32_t* __restrict__ ob, uint32_t* __restrict__ op, uint64_t cap,
-                   unsigned long long* __restrict__ ctr) {
+                   const uint64_t* __restrict__ woff, uint32_t* __restrict__ masks,
+                   uint64_t nwords, uint32_t* __restrict__ ob, uint32_t* __restrict__ op,
+                   uint64_t cap, unsigned long long* __restrict__ ctr) {
   const bool aoe = predicate != kWithin;
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nchunks = (nranges + 31) / 32;
@@ -549,8 +583,10 @@ __global__ void __launch_bounds__(128)
     const uint32_t excl = incl - R.y;
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     uint64_t pos = kPass ? coff[chunk] : 0;
+    const uint64_t w0 = woff[chunk];
     uint32_t cnt = 0;
     for (uint32_t base = 0; base < total; base += 32) {
+      const uint64_t w = w0 + base / 32;
       const uint32_t tt = base + lane;
       // owner: the last lane whose exclusive offset is <= tt (it has len > 0)
       int L = 0;
@@ -565,24 +601,34 @@ __global__ void __launch_bounds__(128)
       const uint32_t eL = __shfl_sync(0xffffffffu, excl, L);
       bool hit = false;
       uint32_t id = 0;
-      if (tt < total) {
+      if (kPass == 0 && tt < total) {
         const uint32_t j = start + (tt - eL);
         double2 pt;
         float2 pt32;
         if (kind == kRangeSorted) {
           pt = v.xy[j];
           pt32 = v.xy32[j];
-          id = v.ids[j];
         } else {
           const float4 sb = t.sorted_box[j];
           pt32 = make_float2(sb.x, sb.y);
-          id = t.sorted_id[j];
-          pt = B.pt[id];
+          pt = B.pt[t.sorted_id[j]];
         }
         if (P.kind[row] == kPoint) hit = pteq(pt, P.pt[row]);
         else hit = in_box(pt32, P.box[row]) && range_pred(P, row, pt, pt32, aoe, esc);
       }
-      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      // pass 0 keeps the hit mask, pass 1 reads it back instead of testing again
+      unsigned m;
+      if (kPass == 0) {
+        m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0 && w < nwords) masks[w] = m;
+      } else {
+        m = w < nwords ? masks[w] : 0u;
+        hit = (m >> lane) & 1u;
+        if (hit) {
+          const uint32_t j = start + (tt - eL);
+          id = kind == kRangeSorted ? v.ids[j] : t.sorted_id[j];
+        }
+      }
       if (kPass) {
         if (hit) {
           const uint64_t o = pos + __popc(m & ((1u << lane) - 1u));
@@ -615,9 +661,22 @@ float o2f_host(uint32_t u) {
 
 LearnedIndex::LearnedIndex(uint32_t leaves, uint32_t window) : L_(leaves), window_(window) {
   SPJ_CHECK(leaves >= 1 && leaves <= 65535, "leaves must be in [1, 65535]");
+  for (auto& e : ev_) SPJ_CUDA(cudaEventCreate(&e));
 }
 
-LearnedIndex::~LearnedIndex() { cudaDeviceSynchronize(); }
+LearnedIndex::~LearnedIndex() {
+  cudaDeviceSynchronize();
+  for (auto& e : ev_)
+    if (e) cudaEventDestroy(e);
+}
+
+void LearnedIndex::set_window(uint32_t window) {
+  window_ = window;
+  uint32_t over = 0;
+  for (uint32_t l = 0; l < L_ && l < host_err_.size(); l++)
+    if (host_start_[l + 1] > host_start_[l] && host_err_[l] > window_) over++;
+  stats_.leaves_over_window = over;
+}
 
 static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevBuf& keys,
                              const DevBuf& ids, const DevBuf& xy, const DevBuf& xy32,
@@ -783,6 +842,8 @@ void LearnedIndex::measure_errors(cudaStream_t s) {
   SPJ_CUDA(cudaMemcpyAsync(st.data(), leaf_start_.get(), ((size_t)L_ + 1) * 4,
                            cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
+  host_err_ = e;
+  host_start_ = st;
   uint32_t mx = 0, over = 0, nonempty = 0;
   double sum = 0;
   for (uint32_t l = 0; l < L_; l++) {
@@ -836,6 +897,7 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
     return 0;
   }
   // probe rows in key order (locality of the model and key searches)
+  SPJ_CUDA(cudaEventRecord(ev_[0], s));
   const size_t rb = ((size_t)np + 1) * 4;
   order_.reserve(rb, s);
   okeys_.reserve(rb, s);
@@ -845,12 +907,15 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
                                                order_.as<uint32_t>());
   radix_sort_pairs(okeys_.as<uint32_t>(), order_.as<uint32_t>(), akeys_.as<uint32_t>(),
                    avals_.as<uint32_t>(), np, 32, tmp_, s);
+  SPJ_CUDA(cudaEventRecord(ev_[1], s));
   // phase A: ranges per row
   counts_.reserve(rb, s);
   offs_.reserve(((size_t)np + 1) * 8, s);
+  rcache_.reserve(((size_t)np + 1) * kRangeCache * sizeof(uint2), s);
   const int ga = grid_for(np, 128, kNumSMs * 16);
   k_learned_ranges<0><<<ga, 128, 0, s>>>(v, tv_, probe, predicate, order_.as<uint32_t>(),
-                                         counts_.as<uint32_t>(), nullptr, nullptr, 0, ctr, st);
+                                         counts_.as<uint32_t>(), nullptr, nullptr, 0,
+                                         rcache_.as<uint2>(), ctr, st);
   scan_u32_u64(counts_.as<uint32_t>(), offs_.as<uint64_t>(), np, tmp_, s);
   uint64_t nr = 0;
   SPJ_CUDA(cudaMemcpyAsync(&nr, offs_.as<uint64_t>() + np, 8, cudaMemcpyDeviceToHost, s));
@@ -858,28 +923,43 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
   check_traversal(tv_, s);
   ranges_.reserve((nr + 1) * sizeof(uint4), s);
   k_learned_ranges<1><<<ga, 128, 0, s>>>(v, tv_, probe, predicate, order_.as<uint32_t>(), nullptr,
-                                         offs_.as<uint64_t>(), ranges_.as<uint4>(), nr, ctr, st);
+                                         offs_.as<uint64_t>(), ranges_.as<uint4>(), nr,
+                                         rcache_.as<uint2>(), ctr, st);
+  SPJ_CUDA(cudaEventRecord(ev_[2], s));
   // phase B: candidates of the ranges, a warp per 32 ranges
   const uint64_t nch = (nr + 31) / 32;
   ccount_.reserve((nch + 1) * 4, s);
   coff_.reserve((nch + 1) * 8, s);
+  cwords_.reserve((nch + 1) * 4, s);
+  woff_.reserve((nch + 1) * 8, s);
   const int gb = grid_for((int64_t)(nch * 32), 128, kNumSMs * 16);
   uint64_t total = 0;
   if (nch) {
+    k_chunk_words<<<gb, 128, 0, s>>>(ranges_.as<uint4>(), nr, cwords_.as<uint32_t>());
+    scan_u32_u64(cwords_.as<uint32_t>(), woff_.as<uint64_t>(), (int64_t)nch, tmp_, s);
+    uint64_t nw = 0;
+    SPJ_CUDA(cudaMemcpyAsync(&nw, woff_.as<uint64_t>() + nch, 8, cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    masks_.reserve((nw + 1) * 4, s);
     k_learned_eval<0><<<gb, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate,
                                          ranges_.as<uint4>(), nr, ccount_.as<uint32_t>(), nullptr,
-                                         nullptr, nullptr, 0, ctr);
+                                         woff_.as<uint64_t>(), masks_.as<uint32_t>(), nw, nullptr,
+                                         nullptr, 0, ctr);
     scan_u32_u64(ccount_.as<uint32_t>(), coff_.as<uint64_t>(), (int64_t)nch, tmp_, s);
     SPJ_CUDA(cudaMemcpyAsync(&total, coff_.as<uint64_t>() + nch, 8, cudaMemcpyDeviceToHost, s));
     SPJ_CUDA(cudaStreamSynchronize(s));
-  }
-  out_build.reserve((total + 1) * 4, s);
-  out_probe.reserve((total + 1) * 4, s);
-  if (nch)
+    out_build.reserve((total + 1) * 4, s);
+    out_probe.reserve((total + 1) * 4, s);
     k_learned_eval<1><<<gb, 128, 0, s>>>(v, tv_, bv_, probe, probe_base, predicate,
                                          ranges_.as<uint4>(), nr, nullptr, coff_.as<uint64_t>(),
+                                         woff_.as<uint64_t>(), masks_.as<uint32_t>(), nw,
                                          out_build.as<uint32_t>(), out_probe.as<uint32_t>(), total,
                                          ctr);
+  } else {
+    out_build.reserve(4, s);
+    out_probe.reserve(4, s);
+  }
+  SPJ_CUDA(cudaEventRecord(ev_[3], s));
   unsigned long long h[8];
   SPJ_CUDA(cudaMemcpyAsync(h, counters_.get(), 64, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
@@ -890,6 +970,13 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
   stats_.lbvh_fallbacks += h[2];
   stats_.search_steps += h[3];
   stats_.ranges += nr;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+  stats_.ms_order += ms;
+  cudaEventElapsedTime(&ms, ev_[1], ev_[2]);
+  stats_.ms_ranges += ms;
+  cudaEventElapsedTime(&ms, ev_[2], ev_[3]);
+  stats_.ms_eval += ms;
   return total;
 }
 

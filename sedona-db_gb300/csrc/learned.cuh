@@ -34,6 +34,7 @@ struct LearnedStats {
   uint64_t lookups = 0, window_misses = 0, lbvh_fallbacks = 0;
   uint64_t search_steps = 0;  // binary-search steps over all lookups
   uint64_t ranges = 0;        // build-point ranges handed to the candidate phase
+  double ms_order = 0, ms_ranges = 0, ms_eval = 0;  // query phases (CUDA events)
 };
 
 struct LearnedView;
@@ -59,6 +60,10 @@ class LearnedIndex {
   uint64_t query(const GeomsView& probe, uint32_t probe_base, int predicate, DevBuf& out_build,
                  DevBuf& out_probe, cudaStream_t s);
   const LearnedStats& stats() const { return stats_; }
+  // Largest per-leaf error the model serves; leaves above it (and rows
+  // touching them) take the LBVH.  Only queries read it.
+  void set_window(uint32_t window);
+  uint32_t window() const { return window_; }
   void export_model(std::vector<uint32_t>& keys, std::vector<uint32_t>& leaf_start,
                     std::vector<uint32_t>& leaf_kc, std::vector<double>& a,
                     std::vector<double>& b, std::vector<uint32_t>& err, cudaStream_t s);
@@ -76,6 +81,9 @@ class LearnedIndex {
       scratch_;
   DevBuf root_tab_;
   DevBuf order_, okeys_, akeys_, avals_, ranges_, ccount_, coff_;  // query scratch
+  DevBuf rcache_, cwords_, woff_, masks_;
+  std::vector<uint32_t> host_err_, host_start_;  // per-leaf errors, leaf starts
+  cudaEvent_t ev_[4] = {};
   uint32_t root_shift_ = 0, root_p_ = 1;
   uint32_t k0_ = 0;
   LearnedStats stats_;

@@ -162,7 +162,7 @@ EXPORTS = [
     "SpjStreamCudaStream",
     "SpjLearnedCreate", "SpjLearnedRelease", "SpjLearnedLastError", "SpjLearnedBuildDevice",
     "SpjLearnedSetTrained", "SpjLearnedQueryDevice", "SpjLearnedLossAndGrad", "SpjLearnedExport",
-    "SpjLearnedGetStats", "SpjLearnedStream",
+    "SpjLearnedGetStats", "SpjLearnedStream", "SpjLearnedSetWindow", "SpjLearnedAutotuneWindow",
 ]
 
 
@@ -179,7 +179,8 @@ class SpjLearnedStats(C.Structure):
                 ("root_shift", C.c_double), ("root_entries", C.c_double),
                 ("mean_err", C.c_double),
                 ("grad_norm_after", C.c_double), ("ms_build", C.c_double),
-                ("ranges", C.c_uint64)]
+                ("ranges", C.c_uint64), ("ms_order", C.c_double), ("ms_ranges", C.c_double),
+                ("ms_eval", C.c_double), ("window", C.c_uint32)]
 
 _lib = None
 _lib_lock = threading.Lock()
@@ -267,6 +268,10 @@ def lib() -> C.CDLL:
             L.SpjLearnedGetStats.argtypes = [C.c_void_p, C.POINTER(SpjLearnedStats)]
             L.SpjLearnedStream.argtypes = [C.c_void_p]
             L.SpjLearnedStream.restype = C.c_void_p
+            L.SpjLearnedSetWindow.argtypes = [C.c_void_p, C.c_uint32]
+            L.SpjLearnedAutotuneWindow.argtypes = [C.c_void_p, C.POINTER(SpjDeviceWkb),
+                                                   C.c_uint32, C.c_int32,
+                                                   C.POINTER(C.c_uint32)]
             _lib = L
     return _lib
 
@@ -627,6 +632,16 @@ class LearnedIndex:
 
     def stream(self) -> int:
         return lib().SpjLearnedStream(self.h)
+
+    def set_window(self, window: int):
+        _check(lib().SpjLearnedSetWindow(self.h, window), "set_window", self._err)
+
+    def autotune_window(self, samples, predicate: str = "intersects") -> int:
+        arr = (SpjDeviceWkb * len(samples))(*samples)
+        w = C.c_uint32()
+        _check(lib().SpjLearnedAutotuneWindow(self.h, arr, len(samples), PREDICATES[predicate],
+                                              C.byref(w)), "autotune_window", self._err)
+        return w.value
 
     def __del__(self):
         if getattr(self, "h", None):

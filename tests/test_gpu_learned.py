@@ -121,3 +121,20 @@ def test_window_fallback_to_lbvh_is_exact(env):
         assert pairs(*device_pairs(db, dp, n)) == _oracle_pairs(oracle, cols["build"],
                                                                 cols[probe], "intersects")
     assert tiny.stats()["lbvh_fallbacks"] > 0
+
+
+def test_window_autotune_keeps_pairs(env):
+    """The autotuner picks one of its candidate windows (2^10 .. 2^17, or the
+    model's max error) and the pair set does not depend on the window."""
+    capi, oracle, li, dev, cols = env
+    ref = {p: pairs(*device_pairs(*li.query_device(dev[p][0], "intersects")))
+           for p in ("boxes", "lookups")}
+    w = li.autotune_window([dev["boxes"][0], dev["lookups"][0]], "intersects")
+    st = li.stats()
+    assert w in [1 << k for k in range(10, 18)] or w == st["max_err"]
+    assert st["window"] == w
+    for win in (w, 1, 1 << 20):
+        li.set_window(win)
+        for p in ("boxes", "lookups"):
+            assert pairs(*device_pairs(*li.query_device(dev[p][0], "intersects"))) == ref[p]
+    li.set_window(4096)
