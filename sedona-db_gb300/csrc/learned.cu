@@ -363,7 +363,7 @@ constexpr uint32_t kRangeLeaf = 1;    // an LBVH leaf (sorted primitive indices)
 // A row's first kRangeCache ranges are kept by the counting pass (start,
 // len | kind << 31), so the writing pass copies them instead of searching
 // again; rows with more ranges search again.
-constexpr uint32_t kRangeCache = 4;
+constexpr uint32_t kRangeCache = 8;
 
 // ranges are written at pos < cap only (the count pass sized them)
 template <int kPass>
