@@ -233,6 +233,32 @@ def run_ours(args, world, rank, local, pg):
     st = chosen["stats"]
     steps = args.steps
 
+    # execution options of the chosen form, each timed on its own join
+    # (they change speed only; the pair count is checked)
+    variants = {}
+    for opts in ({"candidate_order": 0}, {"refine_min_blocks": 3},
+                 {"candidate_order": 0, "refine_min_blocks": 3}, {"probe_order": -1}):
+        jv = make_join(1)
+        for k, v in opts.items():
+            jv.set_option(k, v)
+        for _ in range(2):
+            jv.probe_device(dcol, pred, distance)
+        sv = torch.cuda.ExternalStream(jv.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(sv):
+            e0.record(sv)
+        nv = 0
+        for _ in range(max(1, min(steps, 3))):
+            _, _, nv = jv.probe_device(dcol, pred, distance)
+        with torch.cuda.stream(sv):
+            e1.record(sv)
+        torch.cuda.synchronize()
+        assert nv == chosen["pairs"], (opts, nv, chosen["pairs"])
+        name = ",".join(f"{k}={v}" for k, v in opts.items())
+        variants[name] = e0.elapsed_time(e1) / max(1, min(steps, 3))
+        del jv
+
     # e2e: host (pinned) WKB -> C ABI -> host pairs, copies inside the timed region
     j = chosen["join"]
     off = np.ascontiguousarray(inp.probe.offsets)
@@ -315,6 +341,7 @@ def run_ours(args, world, rank, local, pg):
         "fp64_escalated_fraction": st["escalations"] / max(1, st["pairs_evaluated"]),
         "candidates_per_step": st["candidates"] / steps,
         "gpu_launches": int(st["kernel_launches"]),
+        "option_variants_ms_per_step": variants,
         "e2e": {"value": pairs_total / (e2e_ms * 1e-3), "unit": "pairs/s",
                 "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(off.nbytes + data.nbytes),

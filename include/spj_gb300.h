@@ -88,6 +88,14 @@ const char* SpjJoinLastError(SpjJoin* join);
 int SpjJoinPushBuildArrow(SpjJoin* join, const struct ArrowSchema* schema,
                           const struct ArrowArray* array);
 int SpjJoinFinishBuild(SpjJoin* join);
+/* Execution options (they change speed, never the pairs or their order):
+ *   "probe_order"       -1 row order, 0 Morton order from 65536 rows up, 1 always
+ *   "candidate_order"   0/1: refine candidates in the probes' Morton order
+ *   "refine_min_blocks" 1 or 3: FP32 refine built for that many resident
+ *                       256-thread blocks per SM (fewer registers at 3)
+ * The counterpart of the reference's gpu.* session options
+ * (rust/sedona-spatial-join-gpu/src/options.rs:20-51). */
+int SpjJoinSetOption(SpjJoin* join, const char* key, int64_t value);
 /* Build side from a device column (replaces any pushed batches). */
 int SpjJoinBuildDevice(SpjJoin* join, const struct SpjDeviceWkb* column);
 

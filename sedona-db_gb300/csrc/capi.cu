@@ -615,6 +615,26 @@ extern "C" void SpjJoinRelease(SpjJoin* j) {
 
 extern "C" const char* SpjJoinLastError(SpjJoin* j) { return j->last_error.c_str(); }
 
+extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
+  return guarded(j->last_error, [&] {
+    SPJ_CHECK(key != nullptr, "null option key");
+    EngineConfig& c = j->engine->config();
+    const std::string k(key);
+    if (k == "probe_order") {
+      SPJ_CHECK(value >= -1 && value <= 1, "probe_order must be -1, 0 or 1");
+      c.probe_order = (int)value;
+    } else if (k == "candidate_order") {
+      SPJ_CHECK(value == 0 || value == 1, "candidate_order must be 0 or 1");
+      c.candidate_order = value != 0;
+    } else if (k == "refine_min_blocks") {
+      SPJ_CHECK(value == 1 || value == 3, "refine_min_blocks must be 1 or 3");
+      c.refine_min_blocks = (int)value;
+    } else {
+      throw Error("unknown option '" + k + "'");
+    }
+  });
+}
+
 extern "C" int SpjJoinPushBuildArrow(SpjJoin* j, const ArrowSchema* schema,
                                      const ArrowArray* array) {
   return guarded(j->last_error, [&] { j->host.append(parse_arrow(schema, array)); });

@@ -182,6 +182,11 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   probe_scatter(tv, boxes, n, ws.psc, probe_base, ws.cand_build.as<uint32_t>(),
                 ws.cand_probe.as<uint32_t>(), s, order);
   launches += 5;
+  const uint32_t* cperm = nullptr;
+  if (cfg_.candidate_order) {
+    cperm = candidate_order(order, n, m, ws.psc, s);
+    if (cperm) launches += 5;  // gather, 3-kernel scan, scatter
+  }
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
 
   reset_status(ws.status, s);
@@ -190,11 +195,11 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   if (predicate == kPredDWithin)
     refine_dwithin(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                    probe_base, distance, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                   ws.status.as<DeviceStatus>(), s);
+                   ws.status.as<DeviceStatus>(), s, cperm);
   else
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                    ws.status.as<DeviceStatus>(), s);
+                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, cfg_.refine_min_blocks);
   launches += 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 

@@ -29,6 +29,10 @@ struct EngineConfig {
   // point build and probe sides: decide ST_DWithin inside the traversal
   // (FAST_F32 form); otherwise filter, refine and compact
   bool fuse_dwithin = false;
+  // refine candidates in the probes' Morton order (when the traversal used it)
+  bool candidate_order = true;
+  // FP32 refine compiled for this many resident 256-thread blocks per SM (1 or 3)
+  int refine_min_blocks = 1;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 

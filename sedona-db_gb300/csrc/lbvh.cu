@@ -334,7 +334,44 @@ __global__ void k_point_keys(LbvhView t, const double2* __restrict__ xy, uint32_
   }
 }
 
+__global__ void k_gather_counts(const uint32_t* __restrict__ order,
+                                const uint32_t* __restrict__ counts, uint32_t n,
+                                uint32_t* __restrict__ out) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    out[j] = counts[order[j]];
+}
+
+// perm[opos[j] + c] = offs[order[j]] + c for c < counts[order[j]]
+__global__ void k_cand_perm(const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
+                            const uint64_t* __restrict__ offs, const uint64_t* __restrict__ opos,
+                            uint32_t n, uint64_t m, uint32_t* __restrict__ perm) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t pi = order[j];
+    if (pi >= n) continue;
+    const uint64_t src = offs[pi], dst = opos[j];
+    const uint32_t c = counts[pi];
+    for (uint32_t t = 0; t < c; t++)
+      if (dst + t < m && src + t < m) perm[dst + t] = (uint32_t)(src + t);
+  }
+}
+
 }  // namespace
+
+const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
+                                ProbeScratch& sc, cudaStream_t s) {
+  if (!order || nprobe == 0 || m == 0 || m >= 0xFFFFFFFFull) return nullptr;
+  sc.ocount.reserve(((size_t)nprobe + 1) * 4, s);
+  sc.opos.reserve(((size_t)nprobe + 1) * 8, s);
+  sc.cperm.reserve((m + 1) * 4, s);
+  const int g = grid_for(nprobe, 256);
+  k_gather_counts<<<g, 256, 0, s>>>(order, sc.counts.as<uint32_t>(), nprobe,
+                                    sc.ocount.as<uint32_t>());
+  scan_u32_u64(sc.ocount.as<uint32_t>(), sc.opos.as<uint64_t>(), nprobe, sc.tmp, s);
+  k_cand_perm<<<g, 256, 0, s>>>(order, sc.counts.as<uint32_t>(), sc.offsets.as<uint64_t>(),
+                                sc.opos.as<uint64_t>(), nprobe, m, sc.cperm.as<uint32_t>());
+  SPJ_CUDA(cudaGetLastError());
+  return sc.cperm.as<uint32_t>();
+}
 
 static const uint32_t* sort_order(uint32_t n, ProbeScratch& sc, cudaStream_t s) {
   radix_sort_pairs(sc.okeys.as<uint32_t>(), sc.order.as<uint32_t>(), sc.akeys.as<uint32_t>(),

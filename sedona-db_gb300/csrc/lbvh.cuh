@@ -81,6 +81,7 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
 struct ProbeScratch {
   DevBuf counts, offsets, tmp;
   DevBuf order, okeys, akeys, avals;  // probe_order
+  DevBuf ocount, opos, cperm;         // candidate_order
 };
 // Throws if a traversal over t recorded an out-of-range index (syncs s).
 void check_traversal(const LbvhView& t, cudaStream_t s);
@@ -95,6 +96,12 @@ void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
 // extent (sc.order); nullptr when there is nothing to order.
 const uint32_t* probe_order(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                             ProbeScratch& sc, cudaStream_t s);
+// After the two traversal passes (sc.counts / sc.offsets by probe row): the
+// m candidate indices listed probe by probe in `order` (sc.cperm), so that a
+// refine in that order takes spatially neighbouring probes together.
+const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
+                                ProbeScratch& sc, cudaStream_t s);
+
 // The same for FP64 points (KNN queries).
 const uint32_t* point_order(const LbvhView& t, const double2* xy, uint32_t n, ProbeScratch& sc,
                             cudaStream_t s);

@@ -170,12 +170,15 @@ __device__ __forceinline__ void flush_counters(DeviceStatus* st, uint32_t esc, u
   }
 }
 
-template <bool kFast>
-__global__ void __launch_bounds__(256)
+// With perm, thread slot u evaluates candidate perm[u] (a permutation that
+// puts spatially neighbouring probes' candidates next to each other) and
+// writes its flag in place.  kMinBlocks trades registers for occupancy.
+template <bool kFast, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks)
     k_refine(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
              const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, int predicate,
-             uint8_t* __restrict__ flags, DeviceStatus* st,
-             const uint64_t* __restrict__ m_dev = nullptr) {
+             uint8_t* __restrict__ flags, DeviceStatus* st, const uint64_t* __restrict__ m_dev,
+             const uint32_t* __restrict__ perm) {
   uint32_t esc = 0, pairs = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   // with m_dev the pair count lives on the device (graph replays) and m is
@@ -186,10 +189,11 @@ __global__ void __launch_bounds__(256)
   const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   const uint64_t trips = (m + stride - 1) / stride;
   for (uint64_t t = 0; t < trips; t++) {
-    const uint64_t k = start + t * stride;
-    if (k >= m) continue;
+    const uint64_t u = start + t * stride;
+    if (u >= m) continue;
+    const uint64_t k = perm ? (uint64_t)perm[u] : u;
     if (k >= mm) {
-      flags[k] = 0;
+      if (k < m) flags[k] = 0;
       continue;
     }
     const uint32_t b = cb[k], p = cp[k] - probe_base;
@@ -211,13 +215,16 @@ template <bool kFast>
 __global__ void __launch_bounds__(256)
     k_dwithin(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
               const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, double d,
-              float d_lo, float d_hi, uint8_t* __restrict__ flags, DeviceStatus* st) {
+              float d_lo, float d_hi, uint8_t* __restrict__ flags, DeviceStatus* st,
+              const uint32_t* __restrict__ perm) {
   uint32_t esc = 0, pairs = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   const uint64_t trips = (m + stride - 1) / stride;
   for (uint64_t t = 0; t < trips; t++) {
-    const uint64_t k = start + t * stride;
+    const uint64_t u = start + t * stride;
+    if (u >= m) continue;
+    const uint64_t k = perm ? (uint64_t)perm[u] : u;
     if (k >= m) continue;
     const uint32_t bi = cb[k], pi = cp[k] - probe_base;
     pairs++;
@@ -278,21 +285,25 @@ __global__ void k_compact(const uint32_t* __restrict__ cb, const uint32_t* __res
 
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
-                     uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint64_t* m_dev) {
+                     uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint64_t* m_dev,
+                     const uint32_t* perm, int min_blocks) {
   if (m == 0) return;
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
-  if (form == kFastF32)
-    k_refine<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
-                                     m_dev);
+  if (form == kFastF32 && min_blocks >= 3)
+    k_refine<true, 3><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                        m_dev, perm);
+  else if (form == kFastF32)
+    k_refine<true, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                        m_dev, perm);
   else
-    k_refine<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
-                                      m_dev);
+    k_refine<false, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags,
+                                         st, m_dev, perm);
   SPJ_CUDA(cudaGetLastError());
 }
 
 void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                     const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
-                    uint8_t* flags, DeviceStatus* st, cudaStream_t s) {
+                    uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint32_t* perm) {
   if (m == 0) return;
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
   float d_lo = (float)distance, d_hi = (float)distance;
@@ -300,10 +311,10 @@ void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32
   if ((double)d_hi < distance) d_hi = next_upf(d_hi);
   if (form == kFastF32)
     k_dwithin<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_lo, d_hi,
-                                      flags, st);
+                                      flags, st, perm);
   else
     k_dwithin<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_lo, d_hi,
-                                       flags, st);
+                                       flags, st, perm);
   SPJ_CUDA(cudaGetLastError());
 }
 

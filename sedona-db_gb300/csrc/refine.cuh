@@ -26,18 +26,23 @@ enum RefineForm : int {
 // flags[k] = pred(build[cb[k]], probe[cp[k] - probe_base]) for k < m.
 // counters: status->counters[0] += FP64 escalations, [1] += pairs evaluated.
 // With m_dev the pair count is read on the device (CUDA-graph replays) and m
-// is the capacity of cb/cp/flags; flags past the count are cleared.
+// is the capacity of cb/cp/flags; flags past the count are cleared.  With
+// perm (a permutation of [0, m)), candidates are evaluated in that order
+// (flags still land at their own index).  min_blocks 3 compiles the FP32
+// form for three resident 256-thread blocks per SM (fewer registers).
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,
-                     const uint64_t* m_dev = nullptr);
+                     const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
+                     int min_blocks = 1);
 
 // flags[k] = hypot(build - probe) <= distance for point pairs.  The FP32
 // filter decides pairs whose distance is far from the threshold relative to
 // a static error bound; the rest are decided exactly (expansion arithmetic).
 void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                     const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
-                    uint8_t* flags, DeviceStatus* st, cudaStream_t s);
+                    uint8_t* flags, DeviceStatus* st, cudaStream_t s,
+                    const uint32_t* perm = nullptr);
 
 // Stream compaction of (cb, cp) by flags: positions from an exclusive scan
 // of the flags (pos has m+1 entries).  Order is preserved.

@@ -151,7 +151,8 @@ JOIN_CB = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c
 # exported symbols, declared in include/*.h
 EXPORTS = [
     "GpuSpatialRuntimeCreate", "GpuSpatialIndexFloat2DCreate", "GpuSpatialRefinerCreate",
-    "SpjJoinCreate", "SpjJoinRelease", "SpjJoinLastError", "SpjJoinPushBuildArrow",
+    "SpjJoinCreate", "SpjJoinRelease", "SpjJoinLastError", "SpjJoinSetOption",
+    "SpjJoinPushBuildArrow",
     "SpjJoinFinishBuild", "SpjJoinBuildDevice", "SpjJoinProbeArrow", "SpjJoinProbeDevice",
     "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
@@ -200,6 +201,7 @@ def lib() -> C.CDLL:
             L.GpuSpatialIndexFloat2DCreate.argtypes = [_IDX, C.POINTER(GpuSpatialIndexConfig)]
             L.GpuSpatialRefinerCreate.argtypes = [_REF, C.POINTER(GpuSpatialRefinerConfig)]
             L.SpjJoinCreate.argtypes = [C.POINTER(SpjJoinConfig), C.POINTER(C.c_void_p)]
+            L.SpjJoinSetOption.argtypes = [C.c_void_p, C.c_char_p, C.c_int64]
             L.SpjJoinRelease.argtypes = [C.c_void_p]
             L.SpjJoinRelease.restype = None
             L.SpjJoinLastError.argtypes = [C.c_void_p]
@@ -459,6 +461,9 @@ class SpatialJoin:
 
     def _err(self):
         return lib().SpjJoinLastError(self.h)
+
+    def set_option(self, key: str, value: int):
+        _check(lib().SpjJoinSetOption(self.h, key.encode(), int(value)), "set_option", self._err)
 
     def build(self, col: WkbColumn):
         a = ArrowBinary(col)

@@ -104,13 +104,26 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     else:
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
-    for order in (-1, 1):
-        j = capi.SpatialJoin(probe_order=order)
+    # (probe_order, candidate_order, refine_min_blocks): speed options only
+    variants = [(-1, 0, 1), (1, 1, 1), (1, 0, 3), (1, 1, 3)]
+    for v in variants:
+        j = capi.SpatialJoin(probe_order=v[0])
+        j.set_option("candidate_order", v[1])
+        j.set_option("refine_min_blocks", v[2])
         j.build(inp.build)
-        out[order] = j.probe(inp.probe, pred, distance=d)
-    np.testing.assert_array_equal(out[1][0], out[-1][0])
-    np.testing.assert_array_equal(out[1][1], out[-1][1])
-    assert pairs(*out[1]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred, d)
+        out[v] = j.probe(inp.probe, pred, distance=d)
+    for v in variants[1:]:
+        np.testing.assert_array_equal(out[v][0], out[variants[0]][0])
+        np.testing.assert_array_equal(out[v][1], out[variants[0]][1])
+    assert pairs(*out[variants[0]]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred, d)
+
+
+def test_unknown_option_is_an_error(capi):
+    j = capi.SpatialJoin()
+    with pytest.raises(capi.GpuSpatialError, match="unknown option"):
+        j.set_option("no_such_option", 1)
+    with pytest.raises(capi.GpuSpatialError, match="refine_min_blocks"):
+        j.set_option("refine_min_blocks", 2)
 
 
 def test_dwithin_exact_boundary(capi, oracle_mod):
