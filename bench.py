@@ -236,8 +236,8 @@ def run_ours(args, world, rank, local, pg):
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    for opts in ({"candidate_order": 0}, {"refine_min_blocks": 3},
-                 {"candidate_order": 0, "refine_min_blocks": 3}, {"probe_order": -1}):
+    for opts in ({"candidate_order": 1}, {"refine_min_blocks": 2}, {"refine_min_blocks": 4},
+                 {"probe_order": -1}):
         jv = make_join(1)
         for k, v in opts.items():
             jv.set_option(k, v)

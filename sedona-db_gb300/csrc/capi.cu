@@ -627,7 +627,7 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value == 0 || value == 1, "candidate_order must be 0 or 1");
       c.candidate_order = value != 0;
     } else if (k == "refine_min_blocks") {
-      SPJ_CHECK(value == 1 || value == 3, "refine_min_blocks must be 1 or 3");
+      SPJ_CHECK(value >= 2 && value <= 4, "refine_min_blocks must be 2, 3 or 4");
       c.refine_min_blocks = (int)value;
     } else {
       throw Error("unknown option '" + k + "'");

@@ -30,9 +30,9 @@ struct EngineConfig {
   // (FAST_F32 form); otherwise filter, refine and compact
   bool fuse_dwithin = false;
   // refine candidates in the probes' Morton order (when the traversal used it)
-  bool candidate_order = true;
-  // FP32 refine compiled for this many resident 256-thread blocks per SM (1 or 3)
-  int refine_min_blocks = 1;
+  bool candidate_order = false;
+  // FP32 refine compiled for this many resident 256-thread blocks per SM (2-4)
+  int refine_min_blocks = 3;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 

@@ -211,12 +211,10 @@ __global__ void __launch_bounds__(256, kMinBlocks)
 // ---------------------------------------------------------------------------
 // ST_DWithin
 
-template <bool kFast>
 __global__ void __launch_bounds__(256)
     k_dwithin(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
               const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, double d,
-              float d_lo, float d_hi, uint8_t* __restrict__ flags, DeviceStatus* st,
-              const uint32_t* __restrict__ perm) {
+              uint8_t* __restrict__ flags, DeviceStatus* st, const uint32_t* __restrict__ perm) {
   uint32_t esc = 0, pairs = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -234,23 +232,14 @@ __global__ void __launch_bounds__(256)
       continue;
     }
     const double2 b = B.pt[bi], p = P.pt[pi];
+    // FP64 squared distance of the reference's deltas against d^2 with a
+    // relative band of 1e-14, far above the few ulps of rounding in s2 and
+    // d2: outside the band the comparison is exact; inside it, expansion
+    // arithmetic decides.  (An FP32 first tier with a coordinate-magnitude
+    // error bound sent 0.56% of the pairs of the 20M x 1M workload to the
+    // expansion, which cost more on GB300 than the FP64 test it saves.)
     int r = -1;
-    if (kFast) {
-      // |r32 - hypot| <= err: coordinate rounding (u = 2^-24 per operand,
-      // doubled) plus the FP32 square / sum / sqrt rounding.
-      const float2 b32 = pt32(B, bi), p32 = pt32(P, pi);
-      const float bx = b32.x, by = b32.y;
-      const float px = p32.x, py = p32.y;
-      const float fx = __fsub_rn(bx, px), fy = __fsub_rn(by, py);
-      const float r32 = __fsqrt_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)));
-      const float mag = fabsf(bx) + fabsf(px) + fabsf(by) + fabsf(py) + fabsf(fx) + fabsf(fy);
-      const float err = __fadd_ru(__fmul_ru(mag, 2.384185791015625e-07f),   // 2^-22
-                                  __fmul_ru(r32, 4.76837158203125e-07f));   // 2^-21
-      // d_lo <= d <= d_hi are the neighbouring floats of d
-      if (__fadd_ru(r32, err) < d_lo) r = 1;
-      else if (__fsub_rd(r32, err) > d_hi) r = 0;
-    } else {
-      // plain form: FP64 squared distance with a relative margin
+    {
       const double dx = __dsub_rn(b.x, p.x), dy = __dsub_rn(b.y, p.y);
       const double s2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
       const double d2 = __dmul_rn(d, d);
@@ -289,11 +278,14 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      const uint32_t* perm, int min_blocks) {
   if (m == 0) return;
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
-  if (form == kFastF32 && min_blocks >= 3)
-    k_refine<true, 3><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+  if (form == kFastF32 && min_blocks == 4)
+    k_refine<true, 4><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                        m_dev, perm);
+  else if (form == kFastF32 && min_blocks == 2)
+    k_refine<true, 2><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
                                         m_dev, perm);
   else if (form == kFastF32)
-    k_refine<true, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+    k_refine<true, 3><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
                                         m_dev, perm);
   else
     k_refine<false, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags,
@@ -305,16 +297,9 @@ void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32
                     const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
                     uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint32_t* perm) {
   if (m == 0) return;
+  (void)form;  // one form: see k_dwithin
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
-  float d_lo = (float)distance, d_hi = (float)distance;
-  if ((double)d_lo > distance) d_lo = next_downf(d_lo);
-  if ((double)d_hi < distance) d_hi = next_upf(d_hi);
-  if (form == kFastF32)
-    k_dwithin<true><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_lo, d_hi,
-                                      flags, st, perm);
-  else
-    k_dwithin<false><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_lo, d_hi,
-                                       flags, st, perm);
+  k_dwithin<<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, flags, st, perm);
   SPJ_CUDA(cudaGetLastError());
 }
 

@@ -105,7 +105,7 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
     # (probe_order, candidate_order, refine_min_blocks): speed options only
-    variants = [(-1, 0, 1), (1, 1, 1), (1, 0, 3), (1, 1, 3)]
+    variants = [(-1, 0, 3), (1, 1, 2), (1, 0, 4), (1, 1, 3)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
@@ -123,7 +123,7 @@ def test_unknown_option_is_an_error(capi):
     with pytest.raises(capi.GpuSpatialError, match="unknown option"):
         j.set_option("no_such_option", 1)
     with pytest.raises(capi.GpuSpatialError, match="refine_min_blocks"):
-        j.set_option("refine_min_blocks", 2)
+        j.set_option("refine_min_blocks", 1)
 
 
 def test_dwithin_exact_boundary(capi, oracle_mod):
