@@ -91,8 +91,10 @@ int SpjJoinFinishBuild(SpjJoin* join);
 /* Execution options (they change speed, never the pairs or their order):
  *   "probe_order"       -1 row order, 0 Morton order from 65536 rows up, 1 always
  *   "candidate_order"   0/1: refine candidates in the probes' Morton order
- *   "refine_min_blocks" 2, 3 (default) or 4: FP32 refine built for that many
+ *   "refine_min_blocks" 2 to 6 (default 4): FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)
+ *   "fuse_dwithin"      0 (default) / 1: point-point ST_DWithin decided inside
+ *                       the traversal, no candidate pairs (set before the build)
  * The counterpart of the reference's gpu.* session options
  * (rust/sedona-spatial-join-gpu/src/options.rs:20-51). */
 int SpjJoinSetOption(SpjJoin* join, const char* key, int64_t value);

@@ -626,8 +626,11 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
     } else if (k == "candidate_order") {
       SPJ_CHECK(value == 0 || value == 1, "candidate_order must be 0 or 1");
       c.candidate_order = value != 0;
+    } else if (k == "fuse_dwithin") {
+      SPJ_CHECK(value == 0 || value == 1, "fuse_dwithin must be 0 or 1");
+      c.fuse_dwithin = value != 0;  // takes effect at the next build
     } else if (k == "refine_min_blocks") {
-      SPJ_CHECK(value >= 2 && value <= 4, "refine_min_blocks must be 2, 3 or 4");
+      SPJ_CHECK(value >= 2 && value <= 6, "refine_min_blocks must be in [2, 6]");
       c.refine_min_blocks = (int)value;
     } else {
       throw Error("unknown option '" + k + "'");

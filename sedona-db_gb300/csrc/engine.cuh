@@ -31,8 +31,8 @@ struct EngineConfig {
   bool fuse_dwithin = false;
   // refine candidates in the probes' Morton order (when the traversal used it)
   bool candidate_order = false;
-  // FP32 refine compiled for this many resident 256-thread blocks per SM (2-4)
-  int refine_min_blocks = 3;
+  // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
+  int refine_min_blocks = 4;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 

@@ -278,14 +278,20 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      const uint32_t* perm, int min_blocks) {
   if (m == 0) return;
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
-  if (form == kFastF32 && min_blocks == 4)
-    k_refine<true, 4><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+  if (form == kFastF32 && min_blocks == 6)
+    k_refine<true, 6><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                        m_dev, perm);
+  else if (form == kFastF32 && min_blocks == 5)
+    k_refine<true, 5><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                        m_dev, perm);
+  else if (form == kFastF32 && min_blocks == 3)
+    k_refine<true, 3><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
                                         m_dev, perm);
   else if (form == kFastF32 && min_blocks == 2)
     k_refine<true, 2><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
                                         m_dev, perm);
   else if (form == kFastF32)
-    k_refine<true, 3><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+    k_refine<true, 4><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
                                         m_dev, perm);
   else
     k_refine<false, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags,

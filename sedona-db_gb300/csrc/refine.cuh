@@ -28,14 +28,14 @@ enum RefineForm : int {
 // With m_dev the pair count is read on the device (CUDA-graph replays) and m
 // is the capacity of cb/cp/flags; flags past the count are cleared.  With
 // perm (a permutation of [0, m)), candidates are evaluated in that order
-// (flags still land at their own index).  min_blocks (2, 3 or 4) selects
+// (flags still land at their own index).  min_blocks (2 to 6) selects
 // the FP32 form compiled for that many resident 256-thread blocks per SM:
 // fewer registers, more warps to hide the latency of divergent pairs.
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,
                      const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
-                     int min_blocks = 3);
+                     int min_blocks = 4);
 
 // flags[k] = hypot(build - probe) <= distance for point pairs: an FP64
 // squared-distance test decides pairs outside a 1e-14 relative band around

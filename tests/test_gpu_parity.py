@@ -105,7 +105,7 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
     # (probe_order, candidate_order, refine_min_blocks): speed options only
-    variants = [(-1, 0, 3), (1, 1, 2), (1, 0, 4), (1, 1, 3)]
+    variants = [(-1, 0, 4), (1, 1, 2), (1, 0, 6), (1, 1, 5)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
