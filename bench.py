@@ -193,8 +193,10 @@ def run_ours(args, world, rank, local, pg):
     distance = float(inp.params.get("distance", 0.0))
     rt = capi.Runtime.get(local)
 
-    def make_join(form):
+    def make_join(form, opts=None):
         j = capi.SpatialJoin(rt, refine_form=form, profile=True)
+        for k, v in (opts or {}).items():
+            j.set_option(k, v)
         j.build(inp.build)
         return j
 
@@ -236,11 +238,12 @@ def run_ours(args, world, rank, local, pg):
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    for opts in ({"candidate_order": 1}, {"refine_min_blocks": 3}, {"refine_min_blocks": 5},
-                 {"refine_min_blocks": 6}, {"probe_order": -1}):
-        jv = make_join(1)
-        for k, v in opts.items():
-            jv.set_option(k, v)
+    option_sets = [{"candidate_order": 1}, {"refine_min_blocks": 3}, {"refine_min_blocks": 6},
+                   {"probe_order": -1}]
+    if pred == "dwithin" and args.try_fused:
+        option_sets.append({"fuse_dwithin": 1})
+    for opts in option_sets:
+        jv = make_join(1, opts)
         for _ in range(2):
             jv.probe_device(dcol, pred, distance)
         sv = torch.cuda.ExternalStream(jv.stream())
@@ -733,6 +736,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--try-fused", action="store_true",
+                    help="also time point-point ST_DWithin decided inside the traversal")
     args = ap.parse_args()
     world, rank, local, pg = (1, 0, 0, None)
     if args.impl == "reference":

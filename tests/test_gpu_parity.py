@@ -92,6 +92,35 @@ def test_dwithin(capi, oracle_mod, form):
     assert pairs(b, p) == exp
 
 
+@pytest.mark.parametrize("order", [-1, 1])
+def test_dwithin_fused_same_output(capi, oracle_mod, order):
+    """ST_DWithin decided inside the traversal (fuse_dwithin) writes the same
+    pairs at the same positions as filter + refine + compact, and matches the
+    oracle, including pairs exactly at the distance (Pythagorean triples)."""
+    from sedona_gpuspatial import datagen, wkb
+    inp = datagen.workload4(n_probe=20000, n_build=20000)
+    out = {}
+    for fuse in (0, 1):
+        j = capi.SpatialJoin(probe_order=order)
+        j.set_option("fuse_dwithin", fuse)
+        j.build(inp.build)
+        out[fuse] = j.probe(inp.probe, "dwithin", distance=250.0)
+        assert j.stats()["kernel_launches"] > 0
+    np.testing.assert_array_equal(out[1][0], out[0][0])
+    np.testing.assert_array_equal(out[1][1], out[0][1])
+    assert pairs(*out[1]) == oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin", 250.0)
+    bx = np.array([0, 3, 5, 8, 20, 7, 24], dtype=np.float64)
+    by = np.array([0, 4, 12, 15, 21, 24, 7], dtype=np.float64)
+    build = wkb.points_column(bx, by)
+    probe = wkb.points_column(np.array([0.0, 10.0]), np.array([0.0, 3.0]))
+    j = capi.SpatialJoin(probe_order=order)
+    j.set_option("fuse_dwithin", 1)
+    j.build(build)
+    for d in (5.0, 13.0, 17.0, 25.0, 29.0, 4.999999999999999):
+        b, p = j.probe(probe, "dwithin", distance=d)
+        assert pairs(b, p) == oracle_pairs(oracle_mod, build, probe, "dwithin", d), d
+
+
 @pytest.mark.parametrize("shape", ["pip", "polygons", "dwithin"])
 def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     """Traversal in Morton order of the probe boxes (probe_order=1) writes the
