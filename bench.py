@@ -194,7 +194,9 @@ def run_ours(args, world, rank, local, pg):
     rt = capi.Runtime.get(local)
 
     def make_join(form, opts=None):
-        j = capi.SpatialJoin(rt, refine_form=form, profile=True)
+        opts = dict(opts or {})
+        leaf = opts.pop("leaf_size", 0)
+        j = capi.SpatialJoin(rt, leaf_size=leaf, refine_form=form, profile=True)
         for k, v in (opts or {}).items():
             j.set_option(k, v)
         j.build(inp.build)
@@ -240,8 +242,8 @@ def run_ours(args, world, rank, local, pg):
     variants = {}
     option_sets = [{"candidate_order": 1}, {"refine_min_blocks": 3}, {"refine_min_blocks": 6},
                    {"probe_order": -1}]
-    if pred == "dwithin" and args.try_fused:
-        option_sets.append({"fuse_dwithin": 1})
+    if pred == "dwithin":
+        option_sets += [{"fuse_dwithin": 0}, {"leaf_size": 8}, {"leaf_size": 16}]
     for opts in option_sets:
         jv = make_join(1, opts)
         for _ in range(2):
@@ -736,8 +738,6 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--try-fused", action="store_true",
-                    help="also time point-point ST_DWithin decided inside the traversal")
     args = ap.parse_args()
     world, rank, local, pg = (1, 0, 0, None)
     if args.impl == "reference":

@@ -93,7 +93,7 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "candidate_order"   0/1: refine candidates in the probes' Morton order
  *   "refine_min_blocks" 2 to 6 (default 4): FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)
- *   "fuse_dwithin"      0 (default) / 1: point-point ST_DWithin decided inside
+ *   "fuse_dwithin"      1 (default) / 0: point-point ST_DWithin decided inside
  *                       the traversal, no candidate pairs (set before the build)
  * The counterpart of the reference's gpu.* session options
  * (rust/sedona-spatial-join-gpu/src/options.rs:20-51). */

@@ -28,7 +28,7 @@ struct EngineConfig {
   int probe_order = 0;
   // point build and probe sides: decide ST_DWithin inside the traversal
   // (FAST_F32 form); otherwise filter, refine and compact
-  bool fuse_dwithin = false;
+  bool fuse_dwithin = true;
   // refine candidates in the probes' Morton order (when the traversal used it)
   bool candidate_order = false;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
