@@ -199,7 +199,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   else
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, cfg_.refine_min_blocks);
+                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, cfg_.refine_min_blocks,
+                    cfg_.refine_group);
   launches += 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 
@@ -256,7 +257,8 @@ uint64_t JoinEngine::refine_pairs(Workspace& ws, const GeomsView& pv, const uint
                    ws.status.as<DeviceStatus>(), s);
   else
     refine_relation(bv, pv, cb, cp, m, 0, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                    ws.status.as<DeviceStatus>(), s);
+                    ws.status.as<DeviceStatus>(), s, nullptr, nullptr, cfg_.refine_min_blocks,
+                    cfg_.refine_group);
   ws.pos.reserve((m + 1) * 8, s);
   scan_u8_u64(ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), (int64_t)m, ws.scan_tmp, s);
   uint64_t total = 0;

@@ -33,6 +33,8 @@ struct EngineConfig {
   bool candidate_order = false;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;
+  // lanes per candidate pair in the FP32 refine (4, 8, 16; 0 = one lane each)
+  int refine_group = 8;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 

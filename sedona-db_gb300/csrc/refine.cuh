@@ -31,11 +31,13 @@ enum RefineForm : int {
 // (flags still land at their own index).  min_blocks (2 to 6) selects
 // the FP32 form compiled for that many resident 256-thread blocks per SM:
 // fewer registers, more warps to hide the latency of divergent pairs.
+// group (4, 8 or 16; FP32 form, no perm) evaluates each pair with that many
+// cooperating lanes splitting the ring loops; 0 keeps one lane per pair.
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,
                      const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
-                     int min_blocks = 4);
+                     int min_blocks = 4, int group = 0);
 
 // flags[k] = hypot(build - probe) <= distance for point pairs: an FP64
 // squared-distance test decides pairs outside a 1e-14 relative band around

@@ -133,12 +133,14 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     else:
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
-    # (probe_order, candidate_order, refine_min_blocks): speed options only
-    variants = [(-1, 0, 4), (1, 1, 2), (1, 0, 6), (1, 1, 5)]
+    # (probe_order, candidate_order, refine_min_blocks, refine_group): speed only
+    variants = [(-1, 0, 4, 0), (1, 1, 2, 0), (1, 0, 6, 0), (1, 0, 4, 8), (1, 0, 2, 4),
+                (-1, 0, 4, 16)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
         j.set_option("refine_min_blocks", v[2])
+        j.set_option("refine_group", v[3])
         j.build(inp.build)
         out[v] = j.probe(inp.probe, pred, distance=d)
     for v in variants[1:]:
