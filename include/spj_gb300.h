@@ -93,8 +93,8 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "candidate_order"   0/1: refine candidates in the probes' Morton order
  *   "refine_min_blocks" 2 to 6 (default 4): FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)
- *   "refine_group"      8 (default), 4, 16: lanes cooperating on one candidate
- *                       pair in the FP32 refine; 0 = one lane per pair
+ *   "refine_group"      0 (default: one lane per pair), 4, 8, 16: lanes
+ *                       cooperating on one candidate pair in the FP32 refine
  *   "fuse_dwithin"      1 (default) / 0: point-point ST_DWithin decided inside
  *                       the traversal, no candidate pairs (set before the build)
  * The counterpart of the reference's gpu.* session options

@@ -33,8 +33,11 @@ struct EngineConfig {
   bool candidate_order = false;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;
-  // lanes per candidate pair in the FP32 refine (4, 8, 16; 0 = one lane each)
-  int refine_group = 8;
+  // lanes per candidate pair in the FP32 refine (4, 8, 16; 0 = one lane each).
+  // One lane per pair measured fastest on the 2M x 50k polygon and 10M x 50k
+  // point workloads (their band lists are short); groups pay off only when
+  // rings have long band lists.
+  int refine_group = 0;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 
