@@ -95,6 +95,9 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *                       resident 256-thread blocks per SM (fewer registers)
  *   "refine_group"      0 (default: one lane per pair), 4, 8, 16: lanes
  *                       cooperating on one candidate pair in the FP32 refine
+ *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
+ *                       (clean cells answer point-in-ring tests in O(1)); set
+ *                       before the build
  *   "fuse_dwithin"      1 (default) / 0: point-point ST_DWithin decided inside
  *                       the traversal, no candidate pairs (set before the build)
  * The counterpart of the reference's gpu.* session options

@@ -630,6 +630,9 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value == 0 || value == 4 || value == 8 || value == 16,
                 "refine_group must be 0, 4, 8 or 16");
       c.refine_group = (int)value;
+    } else if (k == "cell_grid") {
+      SPJ_CHECK(value == 0 || value == 1, "cell_grid must be 0 or 1");
+      c.cell_grid = value != 0;  // takes effect at the next build
     } else if (k == "fuse_dwithin") {
       SPJ_CHECK(value == 0 || value == 1, "fuse_dwithin must be 0 or 1");
       c.fuse_dwithin = value != 0;  // takes effect at the next build

@@ -60,6 +60,8 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
   cudaStream_t s = bs_;
   decode_wkb(col, bg_, bsc_, false, s);
   if (bg_.nrings > 0) build_band_index(bg_, bsc_, s);
+  bg_.has_grid = false;
+  if (bg_.nrings > 0 && cfg_.cell_grid) build_cell_grid(bg_, bsc_, s);
   build_lbvh(bg_.box.as<float4>(), bg_.n, cfg_.leaf_size, bvh_, s);
   split_points();
   SPJ_CUDA(cudaStreamSynchronize(s));

@@ -19,7 +19,9 @@
 //   xy[nverts]              f64x2 vertices (16 B, one 128-bit load each)
 //   xy32[nverts]            f32x2 the same vertices rounded to nearest
 // and, for a build side that is refined against, a per-ring y-band edge index
-// (band_*), see refine.cu.
+// (band_*), see refine.cu, and a per-ring cell grid (grid_*): a G x G grid
+// over the ring's rect whose clean cells (no edge touches the closed cell)
+// carry the ring's inside / outside status, see cellgrid.cu.
 #pragma once
 #include "common.cuh"
 
@@ -46,6 +48,13 @@ struct GeomsView {
   const uint32_t* band_off = nullptr;    // per ring: nb+1 offsets into band_edges
   const uint16_t* band_edges = nullptr;  // edge index within the ring
   const float2* band_param = nullptr;    // per ring: (y origin, bands per unit y)
+  // cell grid (nullptr when not built): per ring (status offset, G; G = 0 for
+  // no grid), (x0, y0, w, h) with cell (i, j) = [x0 + i w, x0 + (i+1) w] x
+  // [y0 + j h, y0 + (j+1) h] in f32 arithmetic, and one status byte per cell
+  // (0 mixed, 1 inside, 2 outside)
+  const uint2* grid_meta = nullptr;
+  const float4* grid_rect = nullptr;
+  const uint8_t* grid_status = nullptr;
 };
 
 struct DeviceGeoms {
@@ -57,6 +66,8 @@ struct DeviceGeoms {
       xy32;
   DevBuf ring_bands, band_off, band_edges, band_param;
   bool has_bands = false;
+  DevBuf grid_meta, grid_rect, grid_status;
+  bool has_grid = false;
 
   GeomsView view() const {
     GeomsView v;
@@ -81,13 +92,19 @@ struct DeviceGeoms {
       v.band_edges = band_edges.as<uint16_t>();
       v.band_param = band_param.as<float2>();
     }
+    if (has_grid) {
+      v.grid_meta = grid_meta.as<uint2>();
+      v.grid_rect = grid_rect.as<float4>();
+      v.grid_status = grid_status.as<uint8_t>();
+    }
     return v;
   }
   size_t device_bytes() const {
     return kind.size() + pt.size() + box.size() + row_part.size() + part_ring.size() +
            ring_vtx.size() + ring_nsegs.size() + ring_rect.size() + ring_rect32.size() +
            xy.size() + xy32.size() +
-           ring_bands.size() + band_off.size() + band_edges.size() + band_param.size();
+           ring_bands.size() + band_off.size() + band_edges.size() + band_param.size() +
+           grid_meta.size() + grid_rect.size() + grid_status.size();
   }
 };
 
@@ -115,6 +132,11 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& scr
 
 // Build the per-ring y-band edge index used by the banded refine kernels.
 void build_band_index(DeviceGeoms& g, DecodeScratch& scratch, cudaStream_t s);
+
+// Build the per-ring cell grids (after the band index): rings with at least
+// kGridMinSegs segments get a G x G grid, G = clamp(2 ceil(sqrt(nsegs)), 8, 32).
+constexpr int kGridMinSegs = 12;
+void build_cell_grid(DeviceGeoms& g, DecodeScratch& scratch, cudaStream_t s);
 
 // Reads the device status word; throws with a message if a kernel failed.
 void check_status(DevBuf& status, cudaStream_t s, const char* what);

@@ -245,6 +245,63 @@ __device__ __forceinline__ int band_of(float y32, float y0, float inv_h, int nb)
   return (int)f;
 }
 
+// --- cell grid lookups -------------------------------------------------------
+// Boundary k of a grid axis: origin + k * step in f32 arithmetic (the same
+// expression the grid builder used, so cells tile the axis exactly).
+__device__ __forceinline__ float grid_edge(float o, float step, int k) {
+  return __fadd_rn(o, __fmul_rn((float)k, step));
+}
+
+// Index of a closed cell [edge(i), edge(i+1)] containing the FP64 coordinate
+// v, or -1 when v lies outside the grid.  The f32 estimate is corrected
+// against the exact boundary values.
+__device__ __forceinline__ int grid_index(float o, float step, int n, double v) {
+  if (!(v >= (double)grid_edge(o, step, 0)) || !(v <= (double)grid_edge(o, step, n))) return -1;
+  int i = (int)floorf(__fdiv_rn(__fsub_rn(__double2float_rn(v), o), step));
+  i = i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+  while (i > 0 && v < (double)grid_edge(o, step, i)) i--;
+  while (i < n - 1 && v > (double)grid_edge(o, step, i + 1)) i++;
+  return i;
+}
+
+// Status of the grid cell holding p (0 mixed / no grid, 1 inside, 2 outside).
+// A clean cell is touched by no edge, so every point of it has the ring's
+// status there, on tg's arithmetic as well (the argument of the isolation
+// exit in ring_intersects_ring).
+__device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r, double2 p) {
+  if (G.grid_meta == nullptr) return 0;
+  const uint2 m = G.grid_meta[r];
+  if (m.y == 0) return 0;
+  const float4 q = G.grid_rect[r];
+  const int i = grid_index(q.x, q.z, (int)m.y, p.x), j = grid_index(q.y, q.w, (int)m.y, p.y);
+  if (i < 0 || j < 0) return 0;
+  return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
+}
+
+// Status shared by every cell that the FP64 rect R touches, when all of them
+// are clean (adjacent clean cells share their status: an edge separating them
+// would touch both), else 0.  At most kMax cells are inspected.
+__device__ __forceinline__ int grid_rect_status(const GeomsView& G, uint32_t r, Rect64 R) {
+  constexpr int kMax = 16;
+  if (G.grid_meta == nullptr) return 0;
+  const uint2 m = G.grid_meta[r];
+  if (m.y == 0) return 0;
+  const float4 q = G.grid_rect[r];
+  const int n = (int)m.y;
+  const int i0 = grid_index(q.x, q.z, n, R.x), i1 = grid_index(q.x, q.z, n, R.z);
+  const int j0 = grid_index(q.y, q.w, n, R.y), j1 = grid_index(q.y, q.w, n, R.w);
+  if (i0 < 0 || i1 < 0 || j0 < 0 || j1 < 0) return 0;
+  if ((i1 - i0 + 1) * (j1 - j0 + 1) > kMax) return 0;
+  int st = -1;
+  for (int j = j0; j <= j1; j++)
+    for (int i = i0; i <= i1; i++) {
+      const int c = G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
+      if (c == 0 || (st >= 0 && c != st)) return 0;
+      st = c;
+    }
+  return st;
+}
+
 // Plain FP64 form: every segment through tg's FP64 sequence.
 __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r, double2 p,
                                                   bool aoe) {
@@ -273,6 +330,13 @@ __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r,
                                                  float2 p32, bool aoe, uint32_t& esc) {
   RingHit h{false, -1};
   if (!ring_rect_covers(G, r, p, p32)) return h;
+  {
+    const int st = grid_point_status(G, r, p);
+    if (st != 0) {  // clean cell: not on any edge, status known
+      h.hit = st == 1;
+      return h;
+    }
+  }
   const uint32_t V = G.ring_vtx[r];
   bool in = false;
   int idx = -1;
@@ -489,6 +553,13 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
   }
   const uint32_t Vo = Go->ring_vtx[ro];
   const int nso = Go->ring_nsegs[ro];
+  if (kFast && nso > 0) {
+    // the smaller ring's rect inside clean cells of the larger ring's grid:
+    // no edge comes near it (the isolation exit below), and the status of
+    // those cells is the answer
+    const int st = grid_rect_status(*Gr, rr, Go->ring_rect[ro]);
+    if (st != 0) return st == 1;
+  }
   if (kFast && nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
     // Isolation exit.  If every segment of the larger ring has a bbox
     // strictly separated from the smaller ring's bbox (a strict f32

@@ -49,6 +49,59 @@ def test_point_in_polygon_join(capi, oracle_mod, form, pred):
     assert pairs(b, p) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred)
 
 
+def _staircase_rings():
+    # integer-vertex rings with 24 to 80 segments (cell grids are built from
+    # 12 segments up): a staircase, a comb with 1-wide teeth, and a diamond
+    st = [(0, 0)]
+    for k in range(12):
+        st += [(k + 1, k), (k + 1, k + 1)]
+    st += [(0, 12), (0, 0)]
+    comb = [(0, 0), (40, 0), (40, 3)]
+    for k in range(19, -1, -1):
+        comb += [(2 * k + 1, 3), (2 * k + 1, 10), (2 * k, 10), (2 * k, 3)] if k else [(1, 3), (1, 10), (0, 10)]
+    comb += [(0, 0)]
+    dia = [(20, 0), (40, 20), (20, 40), (0, 20), (20, 0)]
+    dia = [tuple(np.array(a) + (np.array(b) - np.array(a)) * t / 8) for a, b in zip(dia[:-1], dia[1:])
+           for t in range(8)] + [(20, 0)]
+    return [st, comb, dia]
+
+
+@pytest.mark.parametrize("pred", PREDS)
+def test_cell_grid_edges_vertices_and_cell_boundaries(capi, oracle_mod, pred):
+    """Points on edges, on vertices, on grid-cell boundaries and strictly
+    inside / outside many-segment integer rings: the FP32 form with cell
+    grids (and without) against the oracle, and polygon-polygon pairs whose
+    boxes sit in clean cells or straddle edges."""
+    from sedona_gpuspatial import wkb
+    rings = _staircase_rings()
+    build = wkb.column_from_values([wkb.wkb_polygon([np.array(r, dtype=np.float64)]) for r in rings])
+    g = np.arange(-1, 41.5, 0.25)
+    px, py = [a.ravel() for a in np.meshgrid(g, g)]
+    probe = wkb.points_column(px, py)
+    exp = oracle_pairs(oracle_mod, build, probe, pred)
+    for grid in (1, 0):
+        j = capi.SpatialJoin(refine_form=1)
+        j.set_option("cell_grid", grid)
+        j.build(build)
+        b, p = j.probe(probe, pred)
+        assert pairs(b, p) == exp, grid
+    if pred == "intersects":
+        rng = np.random.default_rng(9)
+        sq = []
+        for _ in range(3000):
+            x, y = rng.integers(-2, 42, 2) / 2.0
+            w = rng.integers(0, 5) / 2.0 + 0.25
+            sq.append(wkb.wkb_polygon([np.array([(x, y), (x + w, y), (x + w, y + w), (x, y + w),
+                                                 (x, y)])]))
+        probe2 = wkb.column_from_values(sq)
+        exp2 = oracle_pairs(oracle_mod, build, probe2, "intersects")
+        for grid in (1, 0):
+            j = capi.SpatialJoin(refine_form=1)
+            j.set_option("cell_grid", grid)
+            j.build(build)
+            assert pairs(*j.probe(probe2, "intersects")) == exp2, grid
+
+
 @pytest.mark.parametrize("form", [0, 1])
 def test_polygon_polygon_intersects(capi, oracle_mod, form):
     from sedona_gpuspatial import datagen
@@ -133,14 +186,15 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     else:
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
-    # (probe_order, candidate_order, refine_min_blocks, refine_group): speed only
-    variants = [(-1, 0, 4, 0), (1, 1, 2, 0), (1, 0, 6, 0), (1, 0, 4, 8), (1, 0, 2, 4),
-                (-1, 0, 4, 16)]
+    # (probe_order, candidate_order, refine_min_blocks, refine_group, cell_grid)
+    variants = [(-1, 0, 4, 0, 0), (1, 1, 2, 0, 1), (1, 0, 6, 0, 1), (1, 0, 4, 8, 1),
+                (1, 0, 2, 4, 0), (-1, 0, 4, 16, 1)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
         j.set_option("refine_min_blocks", v[2])
         j.set_option("refine_group", v[3])
+        j.set_option("cell_grid", v[4])
         j.build(inp.build)
         out[v] = j.probe(inp.probe, pred, distance=d)
     for v in variants[1:]:
