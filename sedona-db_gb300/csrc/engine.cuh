@@ -34,7 +34,7 @@ struct EngineConfig {
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;
   // per-ring cell grids on the build side (clean cells answer point-in-ring
-  // and isolated ring-ring tests in O(1)); set before the build
+  // tests in O(1)); set before the build
   bool cell_grid = true;
   // lanes per candidate pair in the FP32 refine (4, 8, 16; 0 = one lane each).
   // One lane per pair measured fastest on the 2M x 50k polygon and 10M x 50k

@@ -21,7 +21,8 @@
 // and, for a build side that is refined against, a per-ring y-band edge index
 // (band_*), see refine.cu, and a per-ring cell grid (grid_*): a G x G grid
 // over the ring's rect whose clean cells (no edge touches the closed cell)
-// carry the ring's inside / outside status, see cellgrid.cu.
+// carry the ring's inside / outside status (used by point-in-ring tests), see
+// cellgrid.cu.
 #pragma once
 #include "common.cuh"
 

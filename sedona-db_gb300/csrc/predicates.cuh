@@ -278,30 +278,6 @@ __device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r,
   return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
 }
 
-// Status shared by every cell that the FP64 rect R touches, when all of them
-// are clean (adjacent clean cells share their status: an edge separating them
-// would touch both), else 0.  At most kMax cells are inspected.
-__device__ __forceinline__ int grid_rect_status(const GeomsView& G, uint32_t r, Rect64 R) {
-  constexpr int kMax = 16;
-  if (G.grid_meta == nullptr) return 0;
-  const uint2 m = G.grid_meta[r];
-  if (m.y == 0) return 0;
-  const float4 q = G.grid_rect[r];
-  const int n = (int)m.y;
-  const int i0 = grid_index(q.x, q.z, n, R.x), i1 = grid_index(q.x, q.z, n, R.z);
-  const int j0 = grid_index(q.y, q.w, n, R.y), j1 = grid_index(q.y, q.w, n, R.w);
-  if (i0 < 0 || i1 < 0 || j0 < 0 || j1 < 0) return 0;
-  if ((i1 - i0 + 1) * (j1 - j0 + 1) > kMax) return 0;
-  int st = -1;
-  for (int j = j0; j <= j1; j++)
-    for (int i = i0; i <= i1; i++) {
-      const int c = G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
-      if (c == 0 || (st >= 0 && c != st)) return 0;
-      st = c;
-    }
-  return st;
-}
-
 // Plain FP64 form: every segment through tg's FP64 sequence.
 __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r, double2 p,
                                                   bool aoe) {
@@ -553,13 +529,6 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
   }
   const uint32_t Vo = Go->ring_vtx[ro];
   const int nso = Go->ring_nsegs[ro];
-  if (kFast && nso > 0) {
-    // the smaller ring's rect inside clean cells of the larger ring's grid:
-    // no edge comes near it (the isolation exit below), and the status of
-    // those cells is the answer
-    const int st = grid_rect_status(*Gr, rr, Go->ring_rect[ro]);
-    if (st != 0) return st == 1;
-  }
   if (kFast && nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
     // Isolation exit.  If every segment of the larger ring has a bbox
     // strictly separated from the smaller ring's bbox (a strict f32
