@@ -695,6 +695,7 @@ def run_learned(args, world, rank, local, pg):
                    "l2": "probe columns > L2, no flush", "parallelism": f"replicas x{world}"},
         "probe_rows_per_s": n_rows * world / (ms * 1e-3),
         "learned_index": {"build_ms": st_build["ms_build"], "window": window,
+                          "window_box": after["window_box"],
                           "window_autotune_ms": tune_ms,
                           "phases_ms_per_step": phases,
                           "leaves_over_window_after_tuning": after["leaves_over_window"],

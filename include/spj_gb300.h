@@ -204,7 +204,8 @@ struct SpjLearnedStats {
   /* cumulative query phase times (CUDA events): probe ordering, ranges
    * through the model, candidate evaluation and output */
   double ms_order, ms_ranges, ms_eval;
-  uint32_t window;
+  uint32_t window;     /* lookups */
+  uint32_t window_box; /* the grid cells of range rows */
 };
 
 int SpjLearnedCreate(const struct SpjLearnedConfig* config, SpjLearned** out);
@@ -232,11 +233,13 @@ int SpjLearnedExport(SpjLearned* li, uint32_t* keys, uint32_t* leaf_start, uint3
 int SpjLearnedGetStats(SpjLearned* li, struct SpjLearnedStats* out);
 void* SpjLearnedStream(SpjLearned* li);
 /* The window: the largest per-leaf error the model serves; rows whose leaf
- * error exceeds it take the LBVH fallback.  Queries only; no rebuild. */
+ * error exceeds it take the LBVH fallback.  Sets the window of lookups and
+ * of range rows alike.  Queries only; no rebuild. */
 int SpjLearnedSetWindow(SpjLearned* li, uint32_t window);
 /* Times queries of the sample columns (device WKB) for windows 2^10 .. 2^17
- * and the model's max error (no fallback), best of two runs each, sets the
- * fastest and returns it in *window. */
+ * and the model's max error (no fallback), best of two runs each: first the
+ * window of range rows, then that of lookups; sets both and returns the
+ * lookup window in *window (both are in SpjLearnedStats). */
 int SpjLearnedAutotuneWindow(SpjLearned* li, const struct SpjDeviceWkb* samples,
                              uint32_t n_samples, int32_t predicate, uint32_t* window);
 

@@ -987,43 +987,58 @@ extern "C" int SpjLearnedAutotuneWindow(SpjLearned* li, const SpjDeviceWkb* samp
     cudaEvent_t e0, e1;
     SPJ_CUDA(cudaEventCreate(&e0));
     SPJ_CUDA(cudaEventCreate(&e1));
-    const uint32_t before = li->index->window();
-    uint32_t best = before;
-    float best_ms = INFINITY;
-    try {
-      for (uint32_t w : cand) {
-        li->index->set_window(w);
-        float t_min = INFINITY;
-        for (int rep = 0; rep < 2; rep++) {
-          float t = 0;
-          for (uint32_t k = 0; k < n_samples; k++) {
-            decode_wkb(device_column(&samples[k]), ws.probe, ws.dsc, ws.last_probe_points,
-                       ws.stream);
-            ws.last_probe_points = ws.probe.all_points;
-            SPJ_CUDA(cudaEventRecord(e0, ws.stream));
-            li->index->query(ws.probe.view(), 0, predicate, li->out_b, li->out_p, ws.stream);
-            SPJ_CUDA(cudaEventRecord(e1, ws.stream));
-            SPJ_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            t += ms;
-          }
-          t_min = std::min(t_min, t);
+    const uint32_t before = li->index->window(), before_box = li->index->window_box();
+    // the query time of all samples with windows (w lookups, wb range cells)
+    auto timed = [&](uint32_t w, uint32_t wb) {
+      li->index->set_windows(w, wb);
+      float t_min = INFINITY;
+      for (int rep = 0; rep < 2; rep++) {
+        float t = 0;
+        for (uint32_t k = 0; k < n_samples; k++) {
+          decode_wkb(device_column(&samples[k]), ws.probe, ws.dsc, ws.last_probe_points,
+                     ws.stream);
+          ws.last_probe_points = ws.probe.all_points;
+          SPJ_CUDA(cudaEventRecord(e0, ws.stream));
+          li->index->query(ws.probe.view(), 0, predicate, li->out_b, li->out_p, ws.stream);
+          SPJ_CUDA(cudaEventRecord(e1, ws.stream));
+          SPJ_CUDA(cudaEventSynchronize(e1));
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          t += ms;
         }
-        if (t_min < best_ms) {
-          best_ms = t_min;
+        t_min = std::min(t_min, t);
+      }
+      return t_min;
+    };
+    // lookup rows and range rows respond to their own window: tune the range
+    // window with lookups on the model throughout, then the lookup window
+    uint32_t best_box = before_box, best = before;
+    try {
+      float best_ms = INFINITY;
+      for (uint32_t wb : cand) {
+        const float t = timed(cand.back(), wb);
+        if (t < best_ms) {
+          best_ms = t;
+          best_box = wb;
+        }
+      }
+      best_ms = INFINITY;
+      for (uint32_t w : cand) {
+        const float t = timed(w, best_box);
+        if (t < best_ms) {
+          best_ms = t;
           best = w;
         }
       }
     } catch (...) {
-      li->index->set_window(before);
+      li->index->set_windows(before, before_box);
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       throw;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    li->index->set_window(best);
+    li->index->set_windows(best, best_box);
     li->window = best;
     *window = best;
   });
@@ -1083,6 +1098,7 @@ extern "C" int SpjLearnedGetStats(SpjLearned* li, SpjLearnedStats* out) {
     out->ms_ranges = s.ms_ranges;
     out->ms_eval = s.ms_eval;
     out->window = li->index->window();
+    out->window_box = li->index->window_box();
   });
 }
 

@@ -11,7 +11,8 @@
 namespace spj {
 
 struct LearnedView {
-  uint32_t n, L, window;
+  uint32_t n, L, window;  // window: lookups; window_box: the cells of range rows
+  uint32_t window_box;
   const uint32_t* keys;
   const uint32_t* ids;
   const double2* xy;
@@ -500,14 +501,18 @@ __global__ void __launch_bounds__(128)
         // a cell whose leaf is over the window sends the row to the LBVH
         for (uint32_t cy = cy0; cy <= cy1 && !use_tree; cy++)
           for (uint32_t cx = cx0; cx <= cx1 && !use_tree; cx++)
-            use_tree = v.err[root_leaf(v, hilbert16(cx, cy))] > v.window;
+            use_tree = v.err[root_leaf(v, hilbert16(cx, cy))] > v.window_box;
         if (!use_tree) {
           for (uint32_t cy = cy0; cy <= cy1; cy++) {
             for (uint32_t cx = cx0; cx <= cx1; cx++) {
               const uint32_t q = hilbert16(cx, cy);
               bool bad = false;
               lookups++;
-              const uint32_t lo = learned_lower_bound(v, q, steps, misses, bad);
+              // (the leaf's error is within window_box, checked above; the
+              // search below uses it whatever the lookup window is)
+              LearnedView vb = v;
+              vb.window = 0xFFFFFFFFu;
+              const uint32_t lo = learned_lower_bound(vb, q, steps, misses, bad);
               const uint32_t hi = run_end(v.keys, v.n, lo, q, rsteps);
               put_range<kPass>(ranges, pos, cnt, lo, hi - lo, i, kRangeSorted, cap, cache);
             }
@@ -659,7 +664,8 @@ float o2f_host(uint32_t u) {
 
 }  // namespace
 
-LearnedIndex::LearnedIndex(uint32_t leaves, uint32_t window) : L_(leaves), window_(window) {
+LearnedIndex::LearnedIndex(uint32_t leaves, uint32_t window)
+    : L_(leaves), window_(window), window_box_(window) {
   SPJ_CHECK(leaves >= 1 && leaves <= 65535, "leaves must be in [1, 65535]");
   for (auto& e : ev_) SPJ_CUDA(cudaEventCreate(&e));
 }
@@ -670,8 +676,11 @@ LearnedIndex::~LearnedIndex() {
     if (e) cudaEventDestroy(e);
 }
 
-void LearnedIndex::set_window(uint32_t window) {
+void LearnedIndex::set_window(uint32_t window) { set_windows(window, window); }
+
+void LearnedIndex::set_windows(uint32_t window, uint32_t window_box) {
   window_ = window;
+  window_box_ = window_box;
   uint32_t over = 0;
   for (uint32_t l = 0; l < L_ && l < host_err_.size(); l++)
     if (host_start_[l + 1] > host_start_[l] && host_err_[l] > window_) over++;
@@ -688,6 +697,7 @@ static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevB
   v.n = n;
   v.L = L;
   v.window = window;
+  v.window_box = window;
   v.keys = keys.as<uint32_t>();
   v.ids = ids.as<uint32_t>();
   v.xy = xy.as<double2>();
@@ -888,7 +898,8 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
   scratch_.reserve(sizeof(DeviceStatus), s);
   reset_status(scratch_, s);
   SPJ_CUDA(cudaMemsetAsync(counters_.get(), 0, 64, s));
-  const LearnedView v = SPJ_LVIEW();
+  LearnedView v = SPJ_LVIEW();
+  v.window_box = window_box_;
   DeviceStatus* st = scratch_.as<DeviceStatus>();
   auto* ctr = counters_.as<unsigned long long>();
   if (np == 0) {

@@ -63,7 +63,10 @@ class LearnedIndex {
   // Largest per-leaf error the model serves; leaves above it (and rows
   // touching them) take the LBVH.  Only queries read it.
   void set_window(uint32_t window);
+  // separate windows for point lookups and for the cells of range rows
+  void set_windows(uint32_t window, uint32_t window_box);
   uint32_t window() const { return window_; }
+  uint32_t window_box() const { return window_box_; }
   void export_model(std::vector<uint32_t>& keys, std::vector<uint32_t>& leaf_start,
                     std::vector<uint32_t>& leaf_kc, std::vector<double>& a,
                     std::vector<double>& b, std::vector<uint32_t>& err, cudaStream_t s);
@@ -71,7 +74,7 @@ class LearnedIndex {
  private:
   void fit_root(cudaStream_t s);
   void measure_errors(cudaStream_t s);
-  uint32_t L_, window_;
+  uint32_t L_, window_, window_box_ = 0;
   uint32_t n_ = 0;
   float x0_ = 0, y0_ = 0, sx_ = 0, sy_ = 0;  // grid map on RN32 coordinates
   GeomsView bv_;
