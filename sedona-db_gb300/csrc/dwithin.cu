@@ -123,10 +123,7 @@ __global__ void __launch_bounds__(kTravThreads)
             }
             if (r) {
               if (kScatter) {
-                if (pos < cap) {
-                  out_build[pos] = t.sorted_id[k];
-                  out_probe[pos] = (uint32_t)pi + probe_base;
-                }
+                if (pos < cap) out_build[pos] = t.sorted_id[k];  // probe ids: fill_probe_ids
                 pos++;
               } else {
                 cnt++;
@@ -232,6 +229,7 @@ void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* prob
       t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
       d, lo, hi, order, nullptr, offs, probe_base, out_build, out_probe, capacity, nullptr);
   SPJ_CUDA(cudaGetLastError());
+  fill_probe_ids(offs, n, probe_base, out_probe, capacity, s);
 }
 
 }  // namespace spj

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kTravThreads)
               if (kScatter) {
                 if (pos < cap) {  // writes bounded by the output capacity
                   out_build[pos] = t.sorted_id[k];
-                  out_probe[pos] = (uint32_t)pi + probe_base;
+                  if (out_probe) out_probe[pos] = (uint32_t)pi + probe_base;
                 }
                 pos++;
               } else {
@@ -334,6 +334,33 @@ __global__ void k_point_keys(LbvhView t, const double2* __restrict__ xy, uint32_
   }
 }
 
+// out_probe[e] = row + probe_base for every e in [offs[row], offs[row + 1]).
+// A warp takes 32 consecutive rows, whose runs form one contiguous range,
+// and writes it with coalesced stores, each lane finding the row of its
+// element by a 5-step search over the rows' starts.
+__global__ void k_fill_probe_ids(const uint64_t* __restrict__ offs, uint32_t n,
+                                 uint32_t probe_base, uint32_t* __restrict__ out, uint64_t cap) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n; w += nw) {
+    const uint64_t row = w * 32 + lane;
+    const uint64_t st = row < n ? offs[row] : ~0ull;
+    const uint64_t r_end = w * 32 + 32 < n ? w * 32 + 32 : n;
+    const uint64_t e0 = __shfl_sync(0xffffffffu, st, 0);
+    const uint64_t e1 = offs[r_end];
+    for (uint64_t base = e0; base < e1; base += 32) {
+      const uint64_t e = base + lane;
+      int L = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint64_t sL = __shfl_sync(0xffffffffu, st, L + step);
+        if (sL <= e) L += step;
+      }
+      if (e < e1 && e < cap) out[e] = (uint32_t)(w * 32 + L) + probe_base;
+    }
+  }
+}
+
 __global__ void k_gather_counts(const uint32_t* __restrict__ order,
                                 const uint32_t* __restrict__ counts, uint32_t n,
                                 uint32_t* __restrict__ out) {
@@ -356,6 +383,13 @@ __global__ void k_cand_perm(const uint32_t* __restrict__ order, const uint32_t* 
 }
 
 }  // namespace
+
+void fill_probe_ids(const uint64_t* offs, uint32_t n, uint32_t probe_base, uint32_t* out,
+                    uint64_t cap, cudaStream_t s) {
+  if (n == 0) return;
+  k_fill_probe_ids<<<grid_for((int64_t)n, 256), 256, 0, s>>>(offs, n, probe_base, out, cap);
+  SPJ_CUDA(cudaGetLastError());
+}
 
 const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
                                 ProbeScratch& sc, cudaStream_t s) {
@@ -488,8 +522,9 @@ void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr,
                                            sc.offsets.as<uint64_t>(), probe_base, out_build,
-                                           out_probe, ~0ull, order);
+                                           nullptr, ~0ull, order);
   SPJ_CUDA(cudaGetLastError());
+  fill_probe_ids(sc.offsets.as<uint64_t>(), nprobe, probe_base, out_probe, ~0ull, s);
 }
 
 void probe_count_into(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
@@ -508,8 +543,9 @@ void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t npr
   if (nprobe == 0) return;
   const int g = grid_for(nprobe, kTravThreads, kNumSMs * 16);
   k_probe<true><<<g, kTravThreads, 0, s>>>(t, probe_box, nprobe, nullptr, offs, probe_base,
-                                           out_build, out_probe, capacity, order);
+                                           out_build, nullptr, capacity, order);
   SPJ_CUDA(cudaGetLastError());
+  fill_probe_ids(offs, nprobe, probe_base, out_probe, capacity, s);
 }
 
 void expand_boxes(const double2* pts, const float4* boxes, const uint8_t* kind, uint32_t n,

@@ -96,6 +96,12 @@ void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
 // extent (sc.order); nullptr when there is nothing to order.
 const uint32_t* probe_order(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                             ProbeScratch& sc, cudaStream_t s);
+// out[e] = row + probe_base over each row's output run [offs[row], offs[row+1])
+// (offs: n+1 entries), writes bounded by cap; coalesced.  The scatter passes
+// write build ids and leave the probe ids to this kernel.
+void fill_probe_ids(const uint64_t* offs, uint32_t n, uint32_t probe_base, uint32_t* out,
+                    uint64_t cap, cudaStream_t s);
+
 // After the two traversal passes (sc.counts / sc.offsets by probe row): the
 // m candidate indices listed probe by probe in `order` (sc.cperm), so that a
 // refine in that order takes spatially neighbouring probes together.
