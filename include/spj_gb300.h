@@ -44,7 +44,8 @@ extern "C" {
 
 struct SpjJoinConfig {
   const struct GpuSpatialRuntime* runtime; /* initialized runtime (device) */
-  uint32_t leaf_size;                      /* LBVH leaf size, 0 = default (4) */
+  uint32_t leaf_size;                      /* LBVH leaf size, 0 = by build side (16 for
+                                              points, 4 otherwise) */
   int32_t refine_form;                     /* SPJ_REFINE_* (default FAST_F32) */
   int32_t profile;                         /* 1: time phases with CUDA events */
   int32_t probe_order; /* traversal order of probe rows: 0 = Morton order of the

@@ -62,7 +62,8 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
   if (bg_.nrings > 0) build_band_index(bg_, bsc_, s);
   bg_.has_grid = false;
   if (bg_.nrings > 0 && cfg_.cell_grid) build_cell_grid(bg_, bsc_, s);
-  build_lbvh(bg_.box.as<float4>(), bg_.n, cfg_.leaf_size, bvh_, s);
+  const uint32_t leaf = cfg_.leaf_size ? cfg_.leaf_size : (bg_.all_points ? 16u : 4u);
+  build_lbvh(bg_.box.as<float4>(), bg_.n, leaf, bvh_, s);
   split_points();
   SPJ_CUDA(cudaStreamSynchronize(s));
   built_ = true;

@@ -20,7 +20,9 @@ namespace spj {
 constexpr int kPredDWithin = 100;  // ST_DWithin(build, probe, distance)
 
 struct EngineConfig {
-  uint32_t leaf_size = 4;
+  // LBVH leaf size; 0 = by build side: 16 for point columns (ST_DWithin and
+  // equality traversals test cheap points), 4 otherwise
+  uint32_t leaf_size = 0;
   int refine_form = kFastF32;
   bool profile = false;  // time each phase with CUDA events on the engine stream
   // traversal order of the probe rows: 0 = Morton order from kOrderMinRows

@@ -303,10 +303,11 @@ __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r
 // (still with the FP32 classifier).  Segments are visited in increasing
 // index order, so idx (last ON segment) matches tg's sequential walk.
 __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r, double2 p,
-                                                 float2 p32, bool aoe, uint32_t& esc) {
+                                                 float2 p32, bool aoe, uint32_t& esc,
+                                                 bool use_grid = true) {
   RingHit h{false, -1};
   if (!ring_rect_covers(G, r, p, p32)) return h;
-  {
+  if (use_grid) {
     const int st = grid_point_status(G, r, p);
     if (st != 0) {  // clean cell: not on any edge, status known
       h.hit = st == 1;
@@ -355,10 +356,12 @@ __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r,
   return h;
 }
 
+// use_grid = false skips the cell-grid lookup (for points known to lie near
+// the ring's edges, where the cell is mixed)
 template <bool kFast>
 __device__ __forceinline__ RingHit ring_pip(const GeomsView& G, uint32_t r, double2 p, float2 p32,
-                                            bool aoe, uint32_t& esc) {
-  if (kFast) return ring_pip_fast(G, r, p, p32, aoe, esc);
+                                            bool aoe, uint32_t& esc, bool use_grid = true) {
+  if (kFast) return ring_pip_fast(G, r, p, p32, aoe, esc, use_grid);
   return ring_pip_plain(G, r, p, aoe);
 }
 
@@ -570,10 +573,12 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
     }
     if (!near) return ring_pip<kFast>(*Gr, rr, Go->xy[Vo], Go->xy32[Vo], true, esc).hit;
   }
+  // (the vertices of a ring that came near the larger ring's edges: the grid
+  // cells around them are mostly mixed, so they skip the lookup)
   for (int i = 0; i <= nso; i++) {
     const double2 v = Go->xy[Vo + i];
     const float2 v32 = Go->xy32[Vo + i];
-    if (ring_pip<kFast>(*Gr, rr, v, v32, true, esc).hit) return true;
+    if (ring_pip<kFast>(*Gr, rr, v, v32, true, esc, false).hit) return true;
   }
   const float4 R32 = Gr->ring_rect32[rr];
   for (int i = 0; i < nso; i++) {
