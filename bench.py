@@ -243,7 +243,8 @@ def run_ours(args, world, rank, local, pg):
     option_sets = [{"cell_grid": 0}, {"refine_group": 8}, {"refine_min_blocks": 6},
                    {"probe_order": -1}]
     if pred == "dwithin":
-        option_sets += [{"fuse_dwithin": 0}, {"leaf_size": 8}, {"leaf_size": 16}]
+        option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
+                        {"leaf_size": 4}, {"leaf_size": 32}]
     for opts in option_sets:
         jv = make_join(1, opts)
         for _ in range(2):

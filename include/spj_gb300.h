@@ -99,6 +99,8 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
+ *   "dwithin_slots"     64 (default), 0-1024: fused ST_DWithin keeps up to this
+ *                       many build ids per probe from its counting pass
  *   "fuse_dwithin"      1 (default) / 0: point-point ST_DWithin decided inside
  *                       the traversal, no candidate pairs (set before the build)
  * The counterpart of the reference's gpu.* session options

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kTravThreads)
                     float d_hi, const uint32_t* __restrict__ order, uint32_t* __restrict__ counts,
                     const uint64_t* __restrict__ offs, uint32_t probe_base,
                     uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
-                    uint64_t cap, DeviceStatus* st) {
+                    uint64_t cap, DeviceStatus* st, uint32_t* __restrict__ slots, uint32_t K) {
   __shared__ int stack[kTravStack * kTravThreads];
   const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint32_t esc = 0, tested = 0;
@@ -71,6 +71,9 @@ __global__ void __launch_bounds__(kTravThreads)
       traversal_fault(t, kBadProbe, (unsigned)pi);
       continue;
     }
+    // the scatter pass only traverses the probes whose results did not all
+    // fit in the counting pass's slots
+    if (kScatter && K > 0 && counts[pi] <= K) continue;
     const float4 q = probe_box[pi];
     uint32_t cnt = 0;
     uint64_t pos = kScatter ? offs[pi] : 0;
@@ -126,6 +129,7 @@ __global__ void __launch_bounds__(kTravThreads)
                 if (pos < cap) out_build[pos] = t.sorted_id[k];  // probe ids: fill_probe_ids
                 pos++;
               } else {
+                if (cnt < K) slots[(size_t)pi * K + cnt] = t.sorted_id[k];
                 cnt++;
               }
             }
@@ -172,6 +176,34 @@ __global__ void __launch_bounds__(kTravThreads)
   }
 }
 
+// out_build over each row's run from its slots, for rows with <= K results
+// (warp per 32 consecutive rows, coalesced stores; see fill_probe_ids)
+__global__ void k_copy_slots(const uint64_t* __restrict__ offs, const uint32_t* __restrict__ counts,
+                             const uint32_t* __restrict__ slots, uint32_t K, uint32_t n,
+                             uint32_t* __restrict__ out, uint64_t cap) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n; w += nw) {
+    const uint64_t row = w * 32 + lane;
+    const uint64_t st = row < n ? offs[row] : ~0ull;
+    const uint64_t r_end = w * 32 + 32 < n ? w * 32 + 32 : n;
+    const uint64_t e0 = __shfl_sync(0xffffffffu, st, 0);
+    const uint64_t e1 = offs[r_end];
+    for (uint64_t base = e0; base < e1; base += 32) {
+      const uint64_t e = base + lane;
+      int L = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint64_t sL = __shfl_sync(0xffffffffu, st, L + step);
+        if (sL <= e) L += step;
+      }
+      const uint64_t r = w * 32 + L;
+      const uint64_t sr = __shfl_sync(0xffffffffu, st, L);
+      if (e < e1 && e < cap && r < n && counts[r] <= K) out[e] = slots[r * K + (e - sr)];
+    }
+  }
+}
+
 void float_neighbours(double d, float& lo, float& hi) {
   lo = (float)d;
   hi = (float)d;
@@ -206,29 +238,35 @@ void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, Point
 
 void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                    const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
-                   uint32_t* counts, DeviceStatus* st, cudaStream_t s) {
+                   uint32_t* counts, DeviceStatus* st, cudaStream_t s, uint32_t* slots,
+                   uint32_t K) {
   if (n == 0) return;
   float lo, hi;
   float_neighbours(d, lo, hi);
   const int g = grid_for(n, kTravThreads, kNumSMs * 16);
   k_dwithin_fused<false><<<g, kTravThreads, 0, s>>>(
       t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
-      d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st);
+      d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, slots ? K : 0);
   SPJ_CUDA(cudaGetLastError());
 }
 
 void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                      const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                      const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
-                     uint32_t* out_probe, uint64_t capacity, cudaStream_t s) {
+                     uint32_t* out_probe, uint64_t capacity, cudaStream_t s,
+                     const uint32_t* counts, const uint32_t* slots, uint32_t K) {
   if (n == 0) return;
   float lo, hi;
   float_neighbours(d, lo, hi);
   const int g = grid_for(n, kTravThreads, kNumSMs * 16);
   k_dwithin_fused<true><<<g, kTravThreads, 0, s>>>(
       t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
-      d, lo, hi, order, nullptr, offs, probe_base, out_build, out_probe, capacity, nullptr);
+      d, lo, hi, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build, out_probe,
+      capacity, nullptr, nullptr, slots ? K : 0);
   SPJ_CUDA(cudaGetLastError());
+  if (slots && K > 0)
+    k_copy_slots<<<grid_for((int64_t)n, 256), 256, 0, s>>>(offs, counts, slots, K, n, out_build,
+                                                            capacity);
   fill_probe_ids(offs, n, probe_base, out_probe, capacity, s);
 }
 

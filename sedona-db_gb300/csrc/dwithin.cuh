@@ -30,14 +30,20 @@ void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, Point
 
 // The two passes.  probe_box: the probe points' boxes expanded by d
 // (expand_boxes); probe_pt: the probe points.  The count pass writes
-// counts[probe row] and adds the escalations / overlaps tested to
-// st->counters[0] / [1]; the scatter pass writes pairs at offs[probe row].
+// counts[probe row], keeps the first K build ids of each probe in
+// slots[row * K ..] (slots may be null), and adds the escalations / overlaps
+// tested to st->counters[0] / [1]; the scatter pass writes pairs at
+// offs[probe row]: rows with <= K results by a coalesced copy of their slots,
+// the others by traversing again.
 void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                    const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
-                   uint32_t* counts, DeviceStatus* st, cudaStream_t s);
+                   uint32_t* counts, DeviceStatus* st, cudaStream_t s, uint32_t* slots = nullptr,
+                   uint32_t K = 0);
 void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                      const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                      const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
-                     uint32_t* out_probe, uint64_t capacity, cudaStream_t s);
+                     uint32_t* out_probe, uint64_t capacity, cudaStream_t s,
+                     const uint32_t* counts = nullptr, const uint32_t* slots = nullptr,
+                     uint32_t K = 0);
 
 }  // namespace spj

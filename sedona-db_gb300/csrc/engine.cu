@@ -30,6 +30,7 @@ Workspace::~Workspace() {
   out_build.release();
   out_probe.release();
   scan_tmp.release();
+  slots.release();
   status.release();
   wkb_data.release();
   wkb_offsets.release();
@@ -134,8 +135,16 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     ws.psc.counts.reserve(((size_t)n + 1) * 4, s);
     ws.psc.offsets.reserve(((size_t)n + 1) * 8, s);
     const double2* ppt = ws.probe.pt.as<double2>();
+    // result slots per probe, kept by the counting pass (bounded memory)
+    uint32_t K = cfg_.dwithin_slots;
+    while (K > 0 && (uint64_t)n * K * 4 > kMaxSlotBytes) K >>= 1;
+    uint32_t* slots = nullptr;
+    if (K > 0) {
+      ws.slots.reserve((size_t)n * K * 4 + 16, s);
+      slots = ws.slots.as<uint32_t>();
+    }
     dwithin_count(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.counts.as<uint32_t>(),
-                  ws.status.as<DeviceStatus>(), s);
+                  ws.status.as<DeviceStatus>(), s, slots, K);
     scan_u32_u64(ws.psc.counts.as<uint32_t>(), ws.psc.offsets.as<uint64_t>(), n, ws.psc.tmp, s);
     uint64_t total = 0;
     DeviceStatus hst;
@@ -149,7 +158,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     ws.out_probe.reserve((total + 1) * 4, s);
     dwithin_scatter(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.offsets.as<uint64_t>(),
                     probe_base, ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), total,
-                    s);
+                    s, ws.psc.counts.as<uint32_t>(), slots, K);
     launches += 5;
     if (prof) {
       SPJ_CUDA(cudaEventRecord(ws.ev[3], s));

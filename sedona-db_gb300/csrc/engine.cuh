@@ -31,6 +31,8 @@ struct EngineConfig {
   // point build and probe sides: decide ST_DWithin inside the traversal
   // (FAST_F32 form); otherwise filter, refine and compact
   bool fuse_dwithin = true;
+  // fused ST_DWithin: build ids kept per probe by the counting pass (0 = none)
+  uint32_t dwithin_slots = 64;
   // refine candidates in the probes' Morton order (when the traversal used it)
   bool candidate_order = false;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
@@ -45,6 +47,7 @@ struct EngineConfig {
   int refine_group = 0;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
+constexpr uint64_t kMaxSlotBytes = 8ull << 30;  // cap of the fused ST_DWithin slot buffer
 
 // Per-phase device time (CUDA events on the launching stream) and counters.
 struct JoinStats {
@@ -67,6 +70,7 @@ struct Workspace {
   DecodeScratch dsc;
   ProbeScratch psc;
   DevBuf boxes_tmp, cand_build, cand_probe, flags, pos, out_build, out_probe, scan_tmp, status;
+  DevBuf slots;  // fused ST_DWithin result slots
   DevBuf wkb_data, wkb_offsets, wkb_validity;  // H2D staging of host columns
   cudaEvent_t ev[6] = {};
   bool last_probe_points = true;

@@ -153,15 +153,21 @@ def test_dwithin_fused_same_output(capi, oracle_mod, order):
     from sedona_gpuspatial import datagen, wkb
     inp = datagen.workload4(n_probe=20000, n_build=20000)
     out = {}
-    for fuse in (0, 1):
+    # (fuse_dwithin, dwithin_slots): result slots of the counting pass, with
+    # few slots most probes are traversed again by the scatter pass
+    variants = [(0, 64), (1, 64), (1, 4), (1, 0)]
+    for v in variants:
         j = capi.SpatialJoin(probe_order=order)
-        j.set_option("fuse_dwithin", fuse)
+        j.set_option("fuse_dwithin", v[0])
+        j.set_option("dwithin_slots", v[1])
         j.build(inp.build)
-        out[fuse] = j.probe(inp.probe, "dwithin", distance=250.0)
+        out[v] = j.probe(inp.probe, "dwithin", distance=250.0)
         assert j.stats()["kernel_launches"] > 0
-    np.testing.assert_array_equal(out[1][0], out[0][0])
-    np.testing.assert_array_equal(out[1][1], out[0][1])
-    assert pairs(*out[1]) == oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin", 250.0)
+    for v in variants[1:]:
+        np.testing.assert_array_equal(out[v][0], out[variants[0]][0])
+        np.testing.assert_array_equal(out[v][1], out[variants[0]][1])
+    assert pairs(*out[(1, 64)]) == oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin",
+                                                250.0)
     bx = np.array([0, 3, 5, 8, 20, 7, 24], dtype=np.float64)
     by = np.array([0, 4, 12, 15, 21, 24, 7], dtype=np.float64)
     build = wkb.points_column(bx, by)
