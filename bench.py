@@ -659,7 +659,8 @@ def run_learned(args, world, rank, local, pg):
     assert n_untrained == npairs
 
     # plain form / judge: the LBVH join, FP64 refine, same inputs
-    jp = capi.SpatialJoin(rt, refine_form=0)
+    # (leaf size 4: measured best for range boxes and lookups over points)
+    jp = capi.SpatialJoin(rt, leaf_size=4, refine_form=0)
     jp.build_device(db_)
     step(jp, "probe_device")
     torch.cuda.synchronize()
@@ -669,7 +670,7 @@ def run_learned(args, world, rank, local, pg):
     plain_ms = (time.perf_counter() - t0) * 1e3
     assert n_plain == npairs, (n_plain, npairs)
     # the LBVH join in its chosen form (FP32 filter, Morton-ordered probes)
-    jf = capi.SpatialJoin(rt, refine_form=1)
+    jf = capi.SpatialJoin(rt, leaf_size=4, refine_form=1)
     jf.build_device(db_)
     step(jf, "probe_device")
     torch.cuda.synchronize()

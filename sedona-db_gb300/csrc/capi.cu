@@ -898,7 +898,11 @@ extern "C" int SpjLearnedCreate(const SpjLearnedConfig* config, SpjLearned** out
     if (config->leaves) li->leaves = config->leaves;
     if (config->window) li->window = config->window;
     SPJ_CHECK(li->leaves <= 65535, "leaves must be at most 65535");
-    li->engine = std::make_unique<JoinEngine>(rt->device_id, EngineConfig());
+    // the fallback LBVH serves range boxes and lookups: 4 points per leaf
+    // (16, the default for point build sides, suits distance joins)
+    EngineConfig lc;
+    lc.leaf_size = 4;
+    li->engine = std::make_unique<JoinEngine>(rt->device_id, lc);
     li->ws = std::make_unique<Workspace>();
     *out = li.release();
     return 0;
