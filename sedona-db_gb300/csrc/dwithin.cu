@@ -52,6 +52,37 @@ __global__ void k_split_points(const double2* __restrict__ pts, uint32_t npts,
   }
 }
 
+// Whole-leaf decision from the leaf's f32 box (the union of its points'
+// RN32 boxes): +1 when every point of the leaf is within d, -1 when every
+// point is farther, 0 to test the points.  Per axis, the split difference of
+// a box coordinate c (an exact f32) and the probe is within 2^-21 of itself
+// plus 2^-46 |p| (the split analysis above, with no rounding of c), and a
+// point lies within 2^-24 |RN32| of its RN32 copy inside the box (e); the
+// bounds below add these to the farthest / nearest box offsets and decide
+// with the same neighbours of d as the point test.  Points outside the
+// probe's expanded box have no part in the result either way, so emitting a
+// whole leaf in index order gives what the per-point loop gives.
+__device__ __forceinline__ int leaf_class(float4 b, float hx, float hy, float lx, float ly,
+                                          float cerr, float d_lo, float d_hi) {
+  const float sx0 = __fsub_rn(__fsub_rn(b.x, hx), lx), sx1 = __fsub_rn(__fsub_rn(b.z, hx), lx);
+  const float sy0 = __fsub_rn(__fsub_rn(b.y, hy), ly), sy1 = __fsub_rn(__fsub_rn(b.w, hy), ly);
+  const float ex = __fadd_ru(__fmul_ru(fmaxf(fabsf(b.x), fabsf(b.z)), 5.9604645e-08f), cerr);
+  const float ey = __fadd_ru(__fmul_ru(fmaxf(fabsf(b.y), fabsf(b.w)), 5.9604645e-08f), cerr);
+  // farthest: |point - p| <= max(|s0|, |s1|) (1 + 2^-20) + e per axis
+  const float fx = __fadd_ru(__fmul_ru(fmaxf(fabsf(sx0), fabsf(sx1)), kSplitUp), ex);
+  const float fy = __fadd_ru(__fmul_ru(fmaxf(fabsf(sy0), fabsf(sy1)), kSplitUp), ey);
+  const float up = __fmul_ru(__fsqrt_ru(__fadd_ru(__fmul_ru(fx, fx), __fmul_ru(fy, fy))), kSplitUp);
+  if (up < d_lo) return 1;
+  // nearest: the probe's offset outside the box, less the same errors
+  const float nx = fmaxf(fmaxf(sx0, -sx1), 0.0f), ny = fmaxf(fmaxf(sy0, -sy1), 0.0f);
+  const float nxl = fmaxf(__fsub_rd(__fmul_rd(nx, kSplitDown), ex), 0.0f);
+  const float nyl = fmaxf(__fsub_rd(__fmul_rd(ny, kSplitDown), ey), 0.0f);
+  const float lo =
+      __fmul_rd(__fsqrt_rd(__fadd_rd(__fmul_rd(nxl, nxl), __fmul_rd(nyl, nyl))), kSplitDown);
+  if (lo > d_hi) return -1;
+  return 0;
+}
+
 template <bool kScatter>
 __global__ void __launch_bounds__(kTravThreads)
     k_dwithin_fused(LbvhView t, const double2* __restrict__ bxy, const float4* __restrict__ bhl,
@@ -106,6 +137,21 @@ __global__ void __launch_bounds__(kTravThreads)
           }
           const uint32_t b0 = c * t.leaf_size;
           const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+          const int cls = split ? leaf_class(t.leaf_box[c], hx, hy, lx, ly, cerr, d_lo, d_hi) : 0;
+          if (cls < 0) continue;  // every point of the leaf is farther than d
+          if (cls > 0) {          // every point of the leaf is within d
+            tested += b1 - b0;
+            for (uint32_t k = b0; k < b1; k++) {
+              if (kScatter) {
+                if (pos < cap) out_build[pos] = t.sorted_id[k];
+                pos++;
+              } else {
+                if (cnt < K) slots[(size_t)pi * K + cnt] = t.sorted_id[k];
+                cnt++;
+              }
+            }
+            continue;
+          }
           for (uint32_t k = b0; k < b1; k++) {
             if (!box_overlap(t.sorted_box[k], q)) continue;
             tested++;

@@ -169,6 +169,16 @@ __global__ void k_refit(const float4* __restrict__ sbox, uint32_t m, uint32_t L,
   }
 }
 
+__global__ void k_leaf_boxes(const float4* __restrict__ sbox, uint32_t m, uint32_t L, uint32_t ls,
+                             float4* __restrict__ out) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < L; c += gridDim.x * blockDim.x) {
+    const uint32_t b0 = c * ls, b1 = min(b0 + ls, m);
+    float4 bb = sbox[b0];
+    for (uint32_t k = b0 + 1; k < b1; k++) bb = box_union(bb, sbox[k]);
+    out[c] = bb;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // traversal
 
@@ -458,6 +468,7 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
   const uint32_t L = out.nleaves;
   out.node_box.reserve((size_t)(L > 1 ? 2 * (L - 1) : 1) * sizeof(float4), s);
   out.node_child.reserve((size_t)(L > 1 ? L - 1 : 1) * sizeof(int2), s);
+  out.leaf_box.reserve((size_t)(L > 0 ? L : 1) * sizeof(float4), s);
   out.fault.reserve(8, s);
   SPJ_CUDA(cudaMemsetAsync(out.fault.get(), 0, 8, s));
   if (m == 0) return;
@@ -473,6 +484,8 @@ void build_lbvh(const float4* boxes, uint32_t n, uint32_t leaf_size, Lbvh& out, 
   radix_sort_pairs(keys.as<uint32_t>(), ids, akeys.as<uint32_t>(), avals.as<uint32_t>(), m, 32,
                    tmp, s);
   k_gather_boxes<<<gm, 256, 0, s>>>(boxes, ids, m, out.sorted_box.as<float4>());
+  k_leaf_boxes<<<grid_for(L, 256), 256, 0, s>>>(out.sorted_box.as<float4>(), m, L, leaf_size,
+                                                out.leaf_box.as<float4>());
   if (L > 1) {
     DevBuf parent_int((size_t)L * 4, s), parent_leaf((size_t)L * 4, s), visits((size_t)L * 4, s);
     SPJ_CUDA(cudaMemsetAsync(visits.get(), 0, (size_t)L * 4, s));

@@ -25,13 +25,14 @@ struct LbvhView {
   const uint32_t* sorted_id = nullptr;
   const float4* node_box = nullptr;
   const int2* node_child = nullptr;
+  const float4* leaf_box = nullptr;  // [L] union of each leaf's primitive boxes
   // [code, value]: the first out-of-range index a traversal met (code 0 = none)
   unsigned* fault = nullptr;
 };
 
 struct Lbvh {
   uint32_t nprims = 0, nleaves = 0, leaf_size = 4;
-  DevBuf sorted_box, sorted_id, node_box, node_child, fault;
+  DevBuf sorted_box, sorted_id, node_box, node_child, leaf_box, fault;
   LbvhView view() const {
     LbvhView v;
     v.nprims = nprims;
@@ -41,11 +42,13 @@ struct Lbvh {
     v.sorted_id = sorted_id.as<uint32_t>();
     v.node_box = node_box.as<float4>();
     v.node_child = node_child.as<int2>();
+    v.leaf_box = leaf_box.as<float4>();
     v.fault = fault.as<unsigned>();
     return v;
   }
   size_t device_bytes() const {
-    return sorted_box.size() + sorted_id.size() + node_box.size() + node_child.size();
+    return sorted_box.size() + sorted_id.size() + node_box.size() + node_child.size() +
+           leaf_box.size();
   }
 };
 
