@@ -381,49 +381,89 @@ __global__ void __launch_bounds__(kKnnThreads)
         continue;
       }
     }
-    // exact keys of the proven set, ordered by (key, build id)
+    // Order of the proven set by (exact key, build id).  The list is already
+    // ascending in the split distance; two neighbours whose error intervals
+    // are disjoint are in exact order, and only neighbours whose intervals
+    // overlap (near ties, duplicates) compare exact double-double keys,
+    // computed on first use.  Odd-even transposition over the K slots
+    // (static register indices); slots past kk hold +inf and stay last.
     const uint32_t kk = min(k, have);
     double kh[K], kl[K];
     uint32_t ki[K];
+    bool kd[K];  // key computed
 #pragma unroll
     for (int c = 0; c < K; c++) {
       kh[c] = INFINITY;
       kl[c] = 0;
-      ki[c] = 0xFFFFFFFFu;
-      if (c < (int)kk) {
-        sq_dist_dd(bxy[lp[c]], q, kh[c], kl[c]);
-        ki[c] = t.sorted_id[lp[c]];
-      }
+      kd[c] = false;
+      ki[c] = c < (int)kk ? t.sorted_id[lp[c]] : 0xFFFFFFFFu;
+      if (c >= (int)kk) ld[c] = INFINITY;
     }
-    evals += kk;
-    // odd-even transposition sort (K rounds)
 #pragma unroll
     for (int r = 0; r < K; r++) {
 #pragma unroll
       for (int c = r & 1; c + 1 < K; c += 2) {
-        if (key_less(kh[c + 1], kl[c + 1], ki[c + 1], kh[c], kl[c], ki[c])) {
+        const float da = ld[c], db = ld[c + 1];
+        if (db == INFINITY) continue;  // slot c+1 is empty
+        bool swap;
+        const float up_a = __fadd_ru(__fmul_ru(__fsqrt_ru(da), kSplitUp), cerr);
+        const float lo_b = __fsub_rd(__fmul_rd(__fsqrt_rd(db), kSplitDown), cerr);
+        if (up_a < lo_b) {
+          swap = false;
+        } else {
+          const float up_b = __fadd_ru(__fmul_ru(__fsqrt_ru(db), kSplitUp), cerr);
+          const float lo_a = __fsub_rd(__fmul_rd(__fsqrt_rd(da), kSplitDown), cerr);
+          if (up_b < lo_a) {
+            swap = true;
+          } else {
+            if (!kd[c]) {
+              sq_dist_dd(bxy[lp[c]], q, kh[c], kl[c]);
+              kd[c] = true;
+              evals++;
+            }
+            if (!kd[c + 1]) {
+              sq_dist_dd(bxy[lp[c + 1]], q, kh[c + 1], kl[c + 1]);
+              kd[c + 1] = true;
+              evals++;
+            }
+            swap = key_less(kh[c + 1], kl[c + 1], ki[c + 1], kh[c], kl[c], ki[c]);
+          }
+        }
+        if (swap) {
+          const float td = ld[c];
+          const uint32_t tp = lp[c], ti = ki[c];
           const double th = kh[c], tl = kl[c];
-          const uint32_t ti = ki[c];
+          const bool tk = kd[c];
+          ld[c] = ld[c + 1];
+          lp[c] = lp[c + 1];
+          ki[c] = ki[c + 1];
           kh[c] = kh[c + 1];
           kl[c] = kl[c + 1];
-          ki[c] = ki[c + 1];
+          kd[c] = kd[c + 1];
+          ld[c + 1] = td;
+          lp[c + 1] = tp;
+          ki[c + 1] = ti;
           kh[c + 1] = th;
           kl[c + 1] = tl;
-          ki[c + 1] = ti;
+          kd[c + 1] = tk;
         }
       }
     }
+    // distances in FP64 from the reference's deltas (within a few ulps of
+    // the exact value; the order above is exact)
     for (uint32_t c = 0; c < k; c++) {
       uint32_t id = 0xFFFFFFFFu;
-      double d = INFINITY;
+      double dist = INFINITY;
 #pragma unroll
       for (int cc = 0; cc < K; cc++)
         if (cc == (int)c && cc < (int)kk) {
           id = ki[cc];
-          d = sqrt(__dadd_rn(kh[cc], kl[cc]));
+          const double2 b = bxy[lp[cc]];
+          const double dx = __dsub_rn(b.x, q.x), dy = __dsub_rn(b.y, q.y);
+          dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
         }
       out_idx[qi * k + c] = id;
-      out_dist[qi * k + c] = d;
+      out_dist[qi * k + c] = dist;
     }
   }
   for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
