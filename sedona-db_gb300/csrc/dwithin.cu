@@ -137,9 +137,9 @@ __global__ void __launch_bounds__(kTravThreads)
           }
           const uint32_t b0 = c * t.leaf_size;
           const uint32_t b1 = min(b0 + t.leaf_size, t.nprims);
+          // (both whole-leaf cases fall through to the pop below)
           const int cls = split ? leaf_class(t.leaf_box[c], hx, hy, lx, ly, cerr, d_lo, d_hi) : 0;
-          if (cls < 0) continue;  // every point of the leaf is farther than d
-          if (cls > 0) {          // every point of the leaf is within d
+          if (cls > 0) {  // every point of the leaf is within d
             tested += b1 - b0;
             for (uint32_t k = b0; k < b1; k++) {
               if (kScatter) {
@@ -150,9 +150,9 @@ __global__ void __launch_bounds__(kTravThreads)
                 cnt++;
               }
             }
-            continue;
           }
-          for (uint32_t k = b0; k < b1; k++) {
+          // cls < 0: every point of the leaf is farther than d
+          for (uint32_t k = b0; cls == 0 && k < b1; k++) {
             if (!box_overlap(t.sorted_box[k], q)) continue;
             tested++;
             int r = -1;
