@@ -383,69 +383,44 @@ __global__ void __launch_bounds__(kKnnThreads)
     }
     // Order of the proven set by (exact key, build id).  The list is already
     // ascending in the split distance; two neighbours whose error intervals
-    // are disjoint are in exact order, and only neighbours whose intervals
-    // overlap (near ties, duplicates) compare exact double-double keys,
-    // computed on first use.  Odd-even transposition over the K slots
-    // (static register indices); slots past kk hold +inf and stay last.
+    // [lo, up] are disjoint are in exact order, and only neighbours whose
+    // intervals overlap (near ties, duplicates) compare exact double-double
+    // keys (computed on the spot: this is rare).  Odd-even transposition over
+    // the K slots (static register indices); slots past kk stay last.
     const uint32_t kk = min(k, have);
-    double kh[K], kl[K];
+    float lo[K], up[K];
     uint32_t ki[K];
-    bool kd[K];  // key computed
 #pragma unroll
     for (int c = 0; c < K; c++) {
-      kh[c] = INFINITY;
-      kl[c] = 0;
-      kd[c] = false;
-      ki[c] = c < (int)kk ? t.sorted_id[lp[c]] : 0xFFFFFFFFu;
-      if (c >= (int)kk) ld[c] = INFINITY;
+      const bool v = c < (int)kk;
+      ki[c] = v ? t.sorted_id[lp[c]] : 0xFFFFFFFFu;
+      lo[c] = v ? __fsub_rd(__fmul_rd(__fsqrt_rd(ld[c]), kSplitDown), cerr) : INFINITY;
+      up[c] = v ? __fadd_ru(__fmul_ru(__fsqrt_ru(ld[c]), kSplitUp), cerr) : INFINITY;
     }
 #pragma unroll
     for (int r = 0; r < K; r++) {
 #pragma unroll
       for (int c = r & 1; c + 1 < K; c += 2) {
-        const float da = ld[c], db = ld[c + 1];
-        if (db == INFINITY) continue;  // slot c+1 is empty
-        bool swap;
-        const float up_a = __fadd_ru(__fmul_ru(__fsqrt_ru(da), kSplitUp), cerr);
-        const float lo_b = __fsub_rd(__fmul_rd(__fsqrt_rd(db), kSplitDown), cerr);
-        if (up_a < lo_b) {
-          swap = false;
-        } else {
-          const float up_b = __fadd_ru(__fmul_ru(__fsqrt_ru(db), kSplitUp), cerr);
-          const float lo_a = __fsub_rd(__fmul_rd(__fsqrt_rd(da), kSplitDown), cerr);
-          if (up_b < lo_a) {
-            swap = true;
-          } else {
-            if (!kd[c]) {
-              sq_dist_dd(bxy[lp[c]], q, kh[c], kl[c]);
-              kd[c] = true;
-              evals++;
-            }
-            if (!kd[c + 1]) {
-              sq_dist_dd(bxy[lp[c + 1]], q, kh[c + 1], kl[c + 1]);
-              kd[c + 1] = true;
-              evals++;
-            }
-            swap = key_less(kh[c + 1], kl[c + 1], ki[c + 1], kh[c], kl[c], ki[c]);
-          }
+        if (lo[c + 1] == INFINITY || up[c] < lo[c + 1]) continue;  // empty, or in order
+        bool swap = up[c + 1] < lo[c];
+        if (!swap) {
+          double ha, la, hb, lb;
+          sq_dist_dd(bxy[lp[c]], q, ha, la);
+          sq_dist_dd(bxy[lp[c + 1]], q, hb, lb);
+          evals += 2;
+          swap = key_less(hb, lb, ki[c + 1], ha, la, ki[c]);
         }
         if (swap) {
-          const float td = ld[c];
+          const float tl = lo[c], tu = up[c];
           const uint32_t tp = lp[c], ti = ki[c];
-          const double th = kh[c], tl = kl[c];
-          const bool tk = kd[c];
-          ld[c] = ld[c + 1];
+          lo[c] = lo[c + 1];
+          up[c] = up[c + 1];
           lp[c] = lp[c + 1];
           ki[c] = ki[c + 1];
-          kh[c] = kh[c + 1];
-          kl[c] = kl[c + 1];
-          kd[c] = kd[c + 1];
-          ld[c + 1] = td;
+          lo[c + 1] = tl;
+          up[c + 1] = tu;
           lp[c + 1] = tp;
           ki[c + 1] = ti;
-          kh[c + 1] = th;
-          kl[c + 1] = tl;
-          kd[c + 1] = tk;
         }
       }
     }
