@@ -549,12 +549,29 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
     const int nb = (int)(Gr->ring_bands[rr + 1] - B) - 1;
     const float2 prm = Gr->band_param[rr];
     const int b0 = band_of(by0, prm.x, prm.y, nb), b1 = band_of(by1, prm.x, prm.y, nb);
+    // The first vertex's point-in-ring test rides along: its band is one of
+    // b0..b1, so the same scan classifies that band's edges for it (the FP32
+    // tier of ring_pip_fast).  When the box is isolated and every one of
+    // those edges was decided, the parity is ring_pip's answer; otherwise
+    // ring_pip runs as before.
+    const double2 v0 = Go->xy[Vo];
+    const float2 v032 = Go->xy32[Vo];
+    const bool v_in_rect = ring_rect_covers(*Gr, rr, v0, v032);
+    const int bv = band_of(v032.y, prm.x, prm.y, nb);
+    bool v_decided = true;
+    unsigned v_par = 0;
     bool near = false;
     for (int bb = b0; bb <= b1 && !near; bb++) {
       const uint32_t e0 = Gr->band_off[B + bb], e1 = Gr->band_off[B + bb + 1];
+      const bool vband = v_in_rect && bb == bv;
       for (uint32_t k = e0; k < e1; k++) {
         const int i = Gr->band_edges[k];
         const float2 c = Gr->xy32[Vr + i], d = Gr->xy32[Vr + i + 1];
+        if (vband) {
+          const int pc = pip_seg_f32(c, d, v032);
+          if (pc == kIn) v_par ^= 1u;
+          else if (pc != kOut) v_decided = false;
+        }
         if (fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
             fmin0f(c.y, d.y) > by1)
           continue;  // bboxes strictly separated
@@ -571,7 +588,11 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
         break;
       }
     }
-    if (!near) return ring_pip<kFast>(*Gr, rr, Go->xy[Vo], Go->xy32[Vo], true, esc).hit;
+    if (!near) {
+      if (!v_in_rect) return false;  // ring_pip's first test
+      if (v_decided) return v_par != 0;
+      return ring_pip<kFast>(*Gr, rr, v0, v032, true, esc).hit;
+    }
   }
   // (the vertices of a ring that came near the larger ring's edges: the grid
   // cells around them are mostly mixed, so they skip the lookup)
