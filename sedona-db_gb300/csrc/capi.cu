@@ -580,7 +580,36 @@ struct SpjJoin {
   HostColumnBuilder host;
   std::vector<uint32_t> hb, hp;
   std::string last_error;
+  // second stream for device -> host pair copies (two copy engines at once)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ready = nullptr, copied = nullptr;
+  ~SpjJoin() {
+    if (copy_stream) {
+      cudaStreamSynchronize(copy_stream);
+      cudaStreamDestroy(copy_stream);
+    }
+    if (ready) cudaEventDestroy(ready);
+    if (copied) cudaEventDestroy(copied);
+  }
 };
+
+// Both pair arrays to host memory: build ids on the join's stream, probe ids
+// on a second stream, so that two copy engines move them at once.
+static void copy_pairs_to_host(SpjJoin* j, const uint32_t* db, const uint32_t* dp, uint64_t m,
+                               uint32_t* hb, uint32_t* hp) {
+  cudaStream_t s = j->ws->stream;
+  if (!j->copy_stream) {
+    SPJ_CUDA(cudaStreamCreateWithFlags(&j->copy_stream, cudaStreamNonBlocking));
+    SPJ_CUDA(cudaEventCreateWithFlags(&j->ready, cudaEventDisableTiming));
+    SPJ_CUDA(cudaEventCreateWithFlags(&j->copied, cudaEventDisableTiming));
+  }
+  SPJ_CUDA(cudaEventRecord(j->ready, s));
+  SPJ_CUDA(cudaStreamWaitEvent(j->copy_stream, j->ready, 0));
+  SPJ_CUDA(cudaMemcpyAsync(hp, dp, m * 4, cudaMemcpyDeviceToHost, j->copy_stream));
+  SPJ_CUDA(cudaMemcpyAsync(hb, db, m * 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaEventRecord(j->copied, j->copy_stream));
+  SPJ_CUDA(cudaStreamWaitEvent(s, j->copied, 0));
+}
 
 extern "C" int SpjJoinCreate(const SpjJoinConfig* config, SpjJoin** out) {
   try {
@@ -712,10 +741,7 @@ extern "C" int SpjJoinProbeArrow(SpjJoin* j, const ArrowSchema* schema, const Ar
     uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp);
     j->hb.resize(m);
     j->hp.resize(m);
-    if (m) {
-      SPJ_CUDA(cudaMemcpyAsync(j->hb.data(), db, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
-      SPJ_CUDA(cudaMemcpyAsync(j->hp.data(), dp, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
-    }
+    if (m) copy_pairs_to_host(j, db, dp, m, j->hb.data(), j->hp.data());
     SPJ_CUDA(cudaStreamSynchronize(j->ws->stream));
     cb_status = callback(j->hb.data(), j->hp.data(), m, user_data);
   });
@@ -749,8 +775,7 @@ extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
     }
     if (m) {
       SPJ_CHECK(out_build && out_probe, "null output buffers");
-      SPJ_CUDA(cudaMemcpyAsync(out_build, db, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
-      SPJ_CUDA(cudaMemcpyAsync(out_probe, dp, m * 4, cudaMemcpyDeviceToHost, j->ws->stream));
+      copy_pairs_to_host(j, db, dp, m, out_build, out_probe);
     }
     SPJ_CUDA(cudaStreamSynchronize(j->ws->stream));
   });
