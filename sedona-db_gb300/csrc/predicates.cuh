@@ -278,26 +278,6 @@ __device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r,
   return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
 }
 
-// Status of the single grid cell that holds the whole FP64 rect R (0 when R
-// spans several cells, the cell is mixed, or there is no grid).  The cell
-// index is only estimated in f32; the containment is checked exactly.
-__device__ __forceinline__ int grid_box_status(const GeomsView& G, uint32_t r, Rect64 R) {
-  if (G.grid_meta == nullptr) return 0;
-  const uint2 m = G.grid_meta[r];
-  if (m.y == 0) return 0;
-  const float4 q = G.grid_rect[r];
-  const int n = (int)m.y;
-  const float cx = __fmul_rn(0.5f, __fadd_rn(__double2float_rn(R.x), __double2float_rn(R.z)));
-  const float cy = __fmul_rn(0.5f, __fadd_rn(__double2float_rn(R.y), __double2float_rn(R.w)));
-  const int i = (int)floorf(__fdividef(__fsub_rn(cx, q.x), q.z));
-  const int j = (int)floorf(__fdividef(__fsub_rn(cy, q.y), q.w));
-  if (i < 0 || i >= n || j < 0 || j >= n) return 0;
-  if (!(R.x >= (double)grid_edge(q.x, q.z, i) && R.z <= (double)grid_edge(q.x, q.z, i + 1) &&
-        R.y >= (double)grid_edge(q.y, q.w, j) && R.w <= (double)grid_edge(q.y, q.w, j + 1)))
-    return 0;
-  return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
-}
-
 // Plain FP64 form: every segment through tg's FP64 sequence.
 __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r, double2 p,
                                                   bool aoe) {
@@ -552,13 +532,6 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
   }
   const uint32_t Vo = Go->ring_vtx[ro];
   const int nso = Go->ring_nsegs[ro];
-  if (kFast && nso > 0) {
-    // the smaller ring's rect inside one clean cell of the larger ring's
-    // grid: no edge comes near it (so the isolation exit below holds) and
-    // the cell's status is the point-in-ring answer for its first vertex
-    const int st = grid_box_status(*Gr, rr, Go->ring_rect[ro]);
-    if (st != 0) return st == 1;
-  }
   if (kFast && nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
     // Isolation exit.  If every segment of the larger ring has a bbox
     // strictly separated from the smaller ring's bbox (a strict f32
