@@ -240,7 +240,7 @@ def run_ours(args, world, rank, local, pg):
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    option_sets = [{"cell_grid": 0}, {"refine_group": 8}, {"refine_min_blocks": 6},
+    option_sets = [{"candidate_order": 2}, {"cell_grid": 0}, {"refine_min_blocks": 6},
                    {"probe_order": -1}]
     if pred == "dwithin":
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},

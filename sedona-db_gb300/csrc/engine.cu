@@ -195,9 +195,13 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
                 ws.cand_probe.as<uint32_t>(), s, order);
   launches += 5;
   const uint32_t* cperm = nullptr;
-  if (cfg_.candidate_order) {
+  if (cfg_.candidate_order == 1) {
     cperm = candidate_order(order, n, m, ws.psc, s);
     if (cperm) launches += 5;  // gather, 3-kernel scan, scatter
+  } else if (cfg_.candidate_order == 2) {
+    cperm = build_major_order(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
+                              probe_base, bg_.n, order, n, ws.psc, s);
+    if (cperm) launches += 22;  // rank, keys, 4 radix passes
   }
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
 

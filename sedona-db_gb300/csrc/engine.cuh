@@ -33,8 +33,9 @@ struct EngineConfig {
   bool fuse_dwithin = true;
   // fused ST_DWithin: build ids kept per probe by the counting pass (0 = none)
   uint32_t dwithin_slots = 64;
-  // refine candidates in the probes' Morton order (when the traversal used it)
-  bool candidate_order = false;
+  // refine order of the candidates: 0 as listed (by probe row), 1 the probes'
+  // Morton order, 2 by build row then probe Morton rank
+  int candidate_order = 0;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;
   // per-ring cell grids on the build side (clean cells answer point-in-ring

@@ -417,6 +417,61 @@ const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t
   return sc.cperm.as<uint32_t>();
 }
 
+namespace {
+
+__global__ void k_rank(const uint32_t* __restrict__ order, uint32_t n, uint32_t* __restrict__ rank) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t pi = order[j];
+    if (pi < n) rank[pi] = j;
+  }
+}
+
+// key = build id in the high 16 bits and the probe's Morton rank (scaled to
+// 16 bits) in the low ones, or the build id alone when it needs 17+ bits
+__global__ void k_cand_keys(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
+                            uint64_t m, uint32_t probe_base, const uint32_t* __restrict__ rank,
+                            uint32_t n, bool wide, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m;
+       k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = cb[k];
+    uint32_t key = b;
+    if (!wide) {
+      const uint32_t p = cp[k] - probe_base;
+      const uint32_t r = rank && p < n ? rank[p] : p;
+      key = (b << 16) | (uint32_t)(((uint64_t)r << 16) / (n ? n : 1));
+    }
+    keys[k] = key;
+    vals[k] = (uint32_t)k;
+  }
+}
+
+}  // namespace
+
+const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
+                                  uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
+                                  uint32_t nprobe, ProbeScratch& sc, cudaStream_t s) {
+  if (m < 2 || m >= 0xFFFFFFFFull) return nullptr;
+  const bool wide = nbuild > 65536;
+  sc.cperm.reserve((m + 1) * 4, s);
+  sc.ckeys.reserve((m + 1) * 4, s);
+  sc.ckeys_alt.reserve((m + 1) * 4, s);
+  sc.cvals_alt.reserve((m + 1) * 4, s);
+  const uint32_t* rank = nullptr;
+  if (order && !wide) {
+    sc.rank.reserve(((size_t)nprobe + 1) * 4, s);
+    k_rank<<<grid_for(nprobe, 256), 256, 0, s>>>(order, nprobe, sc.rank.as<uint32_t>());
+    rank = sc.rank.as<uint32_t>();
+  }
+  k_cand_keys<<<grid_for((int64_t)m, 256), 256, 0, s>>>(cb, cp, m, probe_base, rank, nprobe, wide,
+                                                      sc.ckeys.as<uint32_t>(),
+                                                      sc.cperm.as<uint32_t>());
+  radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(), sc.ckeys_alt.as<uint32_t>(),
+                   sc.cvals_alt.as<uint32_t>(), (int64_t)m, 32, sc.tmp, s);
+  SPJ_CUDA(cudaGetLastError());
+  return sc.cperm.as<uint32_t>();
+}
+
 static const uint32_t* sort_order(uint32_t n, ProbeScratch& sc, cudaStream_t s) {
   radix_sort_pairs(sc.okeys.as<uint32_t>(), sc.order.as<uint32_t>(), sc.akeys.as<uint32_t>(),
                    sc.avals.as<uint32_t>(), n, 32, sc.tmp, s);

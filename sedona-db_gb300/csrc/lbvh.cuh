@@ -85,6 +85,7 @@ struct ProbeScratch {
   DevBuf counts, offsets, tmp;
   DevBuf order, okeys, akeys, avals;  // probe_order
   DevBuf ocount, opos, cperm;         // candidate_order
+  DevBuf ckeys, ckeys_alt, cvals_alt, rank;  // build_major_order
 };
 // Throws if a traversal over t recorded an out-of-range index (syncs s).
 void check_traversal(const LbvhView& t, cudaStream_t s);
@@ -110,6 +111,13 @@ void fill_probe_ids(const uint64_t* offs, uint32_t n, uint32_t probe_base, uint3
 // refine in that order takes spatially neighbouring probes together.
 const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
                                 ProbeScratch& sc, cudaStream_t s);
+
+// The m candidates (cb, cp) ordered by build row, then by the probe's Morton
+// rank (order, when given) - a refine in that order takes one build
+// geometry with neighbouring probes together (sc.cperm).
+const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
+                                  uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
+                                  uint32_t nprobe, ProbeScratch& sc, cudaStream_t s);
 
 // The same for FP64 points (KNN queries).
 const uint32_t* point_order(const LbvhView& t, const double2* xy, uint32_t n, ProbeScratch& sc,

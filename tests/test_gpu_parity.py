@@ -193,8 +193,8 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
     # (probe_order, candidate_order, refine_min_blocks, refine_group, cell_grid)
-    variants = [(-1, 0, 4, 0, 0), (1, 1, 2, 0, 1), (1, 0, 6, 0, 1), (1, 0, 4, 8, 1),
-                (1, 0, 2, 4, 0), (-1, 0, 4, 16, 1)]
+    variants = [(-1, 0, 4, 0, 0), (1, 1, 2, 0, 1), (1, 2, 6, 0, 1), (1, 0, 4, 8, 1),
+                (1, 2, 2, 4, 0), (-1, 2, 4, 16, 1)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
