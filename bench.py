@@ -240,8 +240,8 @@ def run_ours(args, world, rank, local, pg):
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    option_sets = [{"candidate_order": 2}, {"cell_grid": 0}, {"refine_min_blocks": 6},
-                   {"probe_order": -1}]
+    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 6}, {"refine_min_blocks": 3},
+                   {"cell_grid": 0}, {"probe_order": -1}]
     if pred == "dwithin":
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
                         {"leaf_size": 4}, {"leaf_size": 32}]

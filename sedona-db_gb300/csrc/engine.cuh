@@ -34,8 +34,10 @@ struct EngineConfig {
   // fused ST_DWithin: build ids kept per probe by the counting pass (0 = none)
   uint32_t dwithin_slots = 64;
   // refine order of the candidates: 0 as listed (by probe row), 1 the probes'
-  // Morton order, 2 by build row then probe Morton rank
-  int candidate_order = 0;
+  // Morton order, 2 by build row then probe Morton rank (a warp then tests
+  // one build geometry's edges against neighbouring probes: shared loads and
+  // similar trip counts; 2M x 50k polygons: 77 vs 104 ms per step)
+  int candidate_order = 2;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;
   // per-ring cell grids on the build side (clean cells answer point-in-ring
