@@ -91,8 +91,9 @@ int SpjJoinPushBuildArrow(SpjJoin* join, const struct ArrowSchema* schema,
 int SpjJoinFinishBuild(SpjJoin* join);
 /* Execution options (they change speed, never the pairs or their order):
  *   "probe_order"       -1 row order, 0 Morton order from 65536 rows up, 1 always
- *   "candidate_order"   2 (default) by build row then probe Morton rank, 1 the
- *                       probes' Morton order, 0 as listed (refine order only)
+ *   "candidate_order"   3 (default) auto: 2 for relation predicates with 4M+
+ *                       candidates, else 0; 2 by build row then probe Morton
+ *                       rank, 1 the probes' Morton order, 0 as listed
  *   "refine_min_blocks" 2 to 6 (default 4): FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)
  *   "refine_group"      0 (default: one lane per pair), 4, 8, 16: lanes

@@ -653,7 +653,7 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value >= -1 && value <= 1, "probe_order must be -1, 0 or 1");
       c.probe_order = (int)value;
     } else if (k == "candidate_order") {
-      SPJ_CHECK(value >= 0 && value <= 2, "candidate_order must be 0, 1 or 2");
+      SPJ_CHECK(value >= 0 && value <= 3, "candidate_order must be 0, 1, 2 or 3");
       c.candidate_order = (int)value;
     } else if (k == "refine_group") {
       SPJ_CHECK(value == 0 || value == 4 || value == 8 || value == 16,

@@ -198,7 +198,11 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   if (cfg_.candidate_order == 1) {
     cperm = candidate_order(order, n, m, ws.psc, s);
     if (cperm) launches += 5;  // gather, 3-kernel scan, scatter
-  } else if (cfg_.candidate_order == 2) {
+  } else if (cfg_.candidate_order == 2 ||
+             (cfg_.candidate_order == 3 && predicate != kPredDWithin && m >= kBuildMajorMin)) {
+    // (auto, 3: point-point distance candidates are cheap to test, so
+    // reordering them costs more than it saves, and small candidate sets do
+    // not repay the sort)
     cperm = build_major_order(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                               probe_base, bg_.n, order, n, ws.psc, s);
     if (cperm) launches += 22;  // rank, keys, 4 radix passes

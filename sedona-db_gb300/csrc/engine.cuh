@@ -36,8 +36,9 @@ struct EngineConfig {
   // refine order of the candidates: 0 as listed (by probe row), 1 the probes'
   // Morton order, 2 by build row then probe Morton rank (a warp then tests
   // one build geometry's edges against neighbouring probes: shared loads and
-  // similar trip counts; 2M x 50k polygons: 77 vs 104 ms per step)
-  int candidate_order = 2;
+  // similar trip counts; 2M x 50k polygons: 77 vs 104 ms per step), 3 auto:
+  // 2 for relation predicates from kBuildMajorMin candidates up, else 0
+  int candidate_order = 3;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;
   // per-ring cell grids on the build side (clean cells answer point-in-ring
@@ -50,6 +51,7 @@ struct EngineConfig {
   int refine_group = 0;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
+constexpr uint64_t kBuildMajorMin = 1ull << 22;  // candidates before build-major order pays
 constexpr uint64_t kMaxSlotBytes = 8ull << 30;  // cap of the fused ST_DWithin slot buffer
 
 // Per-phase device time (CUDA events on the launching stream) and counters.

@@ -426,20 +426,20 @@ __global__ void k_rank(const uint32_t* __restrict__ order, uint32_t n, uint32_t*
   }
 }
 
-// key = build id in the high 16 bits and the probe's Morton rank (scaled to
-// 16 bits) in the low ones, or the build id alone when it needs 17+ bits
+// key = build id above rbits bits of the probe's Morton rank (scaled), or
+// the build id alone (rbits = 0)
 __global__ void k_cand_keys(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
                             uint64_t m, uint32_t probe_base, const uint32_t* __restrict__ rank,
-                            uint32_t n, bool wide, uint32_t* __restrict__ keys,
+                            uint32_t n, int rbits, uint32_t* __restrict__ keys,
                             uint32_t* __restrict__ vals) {
   for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m;
        k += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t b = cb[k];
     uint32_t key = b;
-    if (!wide) {
+    if (rbits > 0) {
       const uint32_t p = cp[k] - probe_base;
       const uint32_t r = rank && p < n ? rank[p] : p;
-      key = (b << 16) | (uint32_t)(((uint64_t)r << 16) / (n ? n : 1));
+      key = (b << rbits) | (uint32_t)(((uint64_t)r << rbits) / (n ? n : 1));
     }
     keys[k] = key;
     vals[k] = (uint32_t)k;
@@ -452,7 +452,13 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
                                   uint32_t nprobe, ProbeScratch& sc, cudaStream_t s) {
   if (m < 2 || m >= 0xFFFFFFFFull) return nullptr;
-  const bool wide = nbuild > 65536;
+  // build id bits, then probe-rank bits up to a whole number of 8-bit radix
+  // passes (24 bits: 3 passes for up to 65536 build rows)
+  int bbits = 1;
+  while (bbits < 32 && (nbuild - 1) >> bbits) bbits++;
+  const int total = bbits <= 24 ? 24 : 32;
+  const int rbits = bbits <= 24 ? total - bbits : 0;
+  const bool wide = rbits == 0;
   sc.cperm.reserve((m + 1) * 4, s);
   sc.ckeys.reserve((m + 1) * 4, s);
   sc.ckeys_alt.reserve((m + 1) * 4, s);
@@ -463,11 +469,11 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
     k_rank<<<grid_for(nprobe, 256), 256, 0, s>>>(order, nprobe, sc.rank.as<uint32_t>());
     rank = sc.rank.as<uint32_t>();
   }
-  k_cand_keys<<<grid_for((int64_t)m, 256), 256, 0, s>>>(cb, cp, m, probe_base, rank, nprobe, wide,
-                                                      sc.ckeys.as<uint32_t>(),
+  k_cand_keys<<<grid_for((int64_t)m, 256), 256, 0, s>>>(cb, cp, m, probe_base, rank, nprobe,
+                                                      rbits, sc.ckeys.as<uint32_t>(),
                                                       sc.cperm.as<uint32_t>());
   radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(), sc.ckeys_alt.as<uint32_t>(),
-                   sc.cvals_alt.as<uint32_t>(), (int64_t)m, 32, sc.tmp, s);
+                   sc.cvals_alt.as<uint32_t>(), (int64_t)m, total, sc.tmp, s);
   SPJ_CUDA(cudaGetLastError());
   return sc.cperm.as<uint32_t>();
 }
