@@ -6,9 +6,10 @@
 // input plus one write of the output: the scan is HBM-bound.
 //
 // Radix sort: per 8-bit digit, (1) a per-tile 256-bin histogram, (2) a scan of
-// the digit-major histogram table, (3) a stable block-local split sort of the
-// tile in shared memory by the 8 digit bits, then a scatter whose runs of
-// equal digits land on consecutive addresses.
+// the digit-major histogram table, (3) a stable block-local ranking of the
+// tile by digit (warp match + per-warp digit counters), a reorder in shared
+// memory, then a scatter whose runs of equal digits land on consecutive
+// addresses.
 #include "prims.cuh"
 
 namespace spj {
@@ -126,80 +127,79 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, int64_t n, int s
   hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void k_digit_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                                int64_t n, int shift, const uint32_t* __restrict__ offs,
-                                int64_t ntiles, uint32_t* __restrict__ okeys,
-                                uint32_t* __restrict__ ovals) {
+// One 8-bit LSD pass over a tile of kSortTile items: stable local ranking by
+// digit (warp w ranks its 256 items in 8 rounds of 32 with __match_any_sync
+// and per-warp digit counters; a scan over warps and digits gives each item
+// its place in the tile's digit-sorted order), a reorder in shared memory,
+// and a write of each digit run to its global offset (digit-major scan of the
+// tile histograms).  Pads (past n) carry key 0xFFFFFFFF, so they rank last in
+// digit 255 and land past the tile's valid items, which are all written.
+__global__ void __launch_bounds__(kSortThreads)
+    k_digit_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                    int64_t n, int shift, const uint32_t* __restrict__ offs, int64_t ntiles,
+                    uint32_t* __restrict__ okeys, uint32_t* __restrict__ ovals) {
+  constexpr int kWarps = kSortThreads / 32;
   __shared__ uint32_t sk[kSortTile];
   __shared__ uint32_t sv[kSortTile];
-  __shared__ uint32_t scan_sm[9];
-  __shared__ uint32_t dstart[256];
+  __shared__ uint32_t wcnt[kWarps][256];
+  __shared__ uint32_t doff[256];
   __shared__ uint32_t gbase[256];
+  __shared__ uint32_t scan_sm[9];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int t = threadIdx.x; t < kWarps * 256; t += kSortThreads) (&wcnt[0][0])[t] = 0;
+  __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * kSortTile;
   const int cnt = (int)min((int64_t)kSortTile, n - base);
-  // load the tile in blocked order (thread t holds [t*8, t*8+8))
-  uint32_t k[kSortItems], v[kSortItems];
+  uint32_t k[kSortItems], v[kSortItems], pos[kSortItems];
 #pragma unroll
   for (int j = 0; j < kSortItems; j++) {
-    int li = threadIdx.x * kSortItems + j;
-    if (li < cnt) {
-      k[j] = keys[base + li];
-      v[j] = vals[base + li];
-    } else {
-      k[j] = 0xFFFFFFFFu;  // pads sort to the end and are never written
-      v[j] = 0;
+    const int li = w * (32 * kSortItems) + j * 32 + lane;  // warp-contiguous chunk
+    const bool valid = li < cnt;
+    k[j] = valid ? keys[base + li] : 0xFFFFFFFFu;
+    v[j] = valid ? vals[base + li] : 0u;
+    const uint32_t d = (k[j] >> shift) & 0xFFu;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t b = 0;
+    if (lane == leader) {
+      b = wcnt[w][d];
+      wcnt[w][d] = b + (uint32_t)__popc(peers);
     }
+    b = __shfl_sync(peers, b, leader);
+    pos[j] = b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    __syncwarp();  // the counters' updates before the next round reads them
   }
-  // stable split sort by the 8 digit bits, LSB first
-  for (int b = 0; b < 8; b++) {
-    uint32_t ones = 0;
-#pragma unroll
-    for (int j = 0; j < kSortItems; j++) ones += (k[j] >> (shift + b)) & 1u;
-    if (shift + b >= 32) ones = 0;
-    uint32_t total_ones;
-    uint32_t ones_before = block_exclusive_scan_256<uint32_t>(ones, scan_sm, &total_ones);
-    const uint32_t nzero = kSortTile - total_ones;
-    uint32_t zeros_before = threadIdx.x * kSortItems - ones_before;
-#pragma unroll
-    for (int j = 0; j < kSortItems; j++) {
-      uint32_t bit = (shift + b < 32) ? ((k[j] >> (shift + b)) & 1u) : 0u;
-      uint32_t dst = bit ? nzero + ones_before : zeros_before;
-      if (bit) ones_before++;
-      else zeros_before++;
-      sk[dst] = k[j];
-      sv[dst] = v[j];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < kSortItems; j++) {
-      k[j] = sk[threadIdx.x * kSortItems + j];
-      v[j] = sv[threadIdx.x * kSortItems + j];
-    }
-    __syncthreads();
-  }
-  // first position of each digit in the sorted tile
-  dstart[threadIdx.x] = 0xFFFFFFFFu;
-  gbase[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
   __syncthreads();
+  {
+    // thread t owns digit t: offsets of each warp's run inside the digit,
+    // then the digit's offset inside the tile
+    const int d = threadIdx.x;
+    uint32_t run = 0;
 #pragma unroll
-  for (int j = 0; j < kSortItems; j++) {
-    int li = threadIdx.x * kSortItems + j;
-    if (li < cnt) {
-      uint32_t d = (k[j] >> shift) & 0xFF;
-      uint32_t prevd = li > 0 ? ((sk[li - 1] >> shift) & 0xFF) : 0xFFFFFFFFu;
-      if (li == 0 || prevd != d) dstart[d] = li;
+    for (int ww = 0; ww < kWarps; ww++) {
+      const uint32_t c = wcnt[ww][d];
+      wcnt[ww][d] = run;
+      run += c;
     }
+    uint32_t total;
+    doff[d] = block_exclusive_scan_256<uint32_t>(run, scan_sm, &total);
+    gbase[d] = offs[(int64_t)d * ntiles + blockIdx.x];
   }
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < kSortItems; j++) {
-    int li = threadIdx.x * kSortItems + j;
-    if (li < cnt) {
-      uint32_t d = (k[j] >> shift) & 0xFF;
-      uint64_t dst = (uint64_t)gbase[d] + (uint32_t)(li - dstart[d]);
-      okeys[dst] = k[j];
-      ovals[dst] = v[j];
-    }
+    const uint32_t d = (k[j] >> shift) & 0xFFu;
+    const uint32_t lp = doff[d] + wcnt[w][d] + pos[j];
+    sk[lp] = k[j];
+    sv[lp] = v[j];
+  }
+  __syncthreads();
+  for (int li = threadIdx.x; li < cnt; li += kSortThreads) {
+    const uint32_t key = sk[li];
+    const uint32_t d = (key >> shift) & 0xFFu;
+    const uint64_t dst = (uint64_t)gbase[d] + (uint32_t)(li - doff[d]);
+    okeys[dst] = key;
+    ovals[dst] = sv[li];
   }
 }
 
