@@ -194,7 +194,8 @@ def run_ours(args, world, rank, local, pg):
     rt = capi.Runtime.get(local)
 
     def make_join(form, opts=None):
-        opts = dict(opts or {})
+        # the chosen form takes --join-options; a variant's options go on top
+        opts = {**(args.join_options if form == 1 else {}), **(opts or {})}
         leaf = opts.pop("leaf_size", 0)
         j = capi.SpatialJoin(rt, leaf_size=leaf, refine_form=form, profile=True)
         for k, v in (opts or {}).items():
@@ -240,7 +241,8 @@ def run_ours(args, world, rank, local, pg):
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 6}, {"refine_min_blocks": 3},
+    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 6}, {"refine_min_blocks": 5},
+                   {"refine_min_blocks": 3},
                    {"cell_grid": 0}, {"probe_order": -1}]
     if pred == "dwithin":
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
@@ -344,7 +346,7 @@ def run_ours(args, world, rank, local, pg):
         "config": {"workload": WORKLOAD_NAMES[args.workload], "probe_rows": n_rows,
                    "build_rows": len(inp.build), "predicate": pred, "scale": args.scale,
                    "pairs_per_step": chosen["pairs"], "l2": "probe column > L2, no flush",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", **join_opts_cfg(args)},
         "probe_rows_per_s": n_rows * world / (chosen["ms"] * 1e-3),
         "plain_f64_form": {"pairs_per_s": plain["pairs"] * world / (plain["ms"] * 1e-3),
                            "ms_per_step": plain["ms"], "pairs": plain["pairs"],
@@ -381,6 +383,10 @@ def dev_i32(ptr: int, n: int):
     return torch.as_tensor(_A(), device="cuda")
 
 
+def join_opts_cfg(args):
+    return {"join_options": args.join_options} if args.join_options else {}
+
+
 def run_stream(args, world, rank, local, pg):
     """Workload 3: the probe column arrives as uneven record batches.  Chosen
     form: the batched stream (one CUDA-graph replay of the persistent
@@ -403,6 +409,8 @@ def run_stream(args, world, rank, local, pg):
         keep.append(k)
         start += n
     j = capi.SpatialJoin(rt, refine_form=1, profile=True)
+    for k, v in args.join_options.items():
+        j.set_option(k, v)
     j.build(inp.build)
     st = capi.StreamProbe(j)
     st.set_batches(dcols)
@@ -514,7 +522,8 @@ def run_stream(args, world, rank, local, pg):
                    "predicate": inp.predicate, "scale": args.scale, "pairs_per_step": npairs,
                    "autotuned": {"block": tuned[0], "chunk_rows": tuned[1], "leaf_size": tuned[2],
                                  "seconds": tune_s},
-                   "l2": "probe batches > L2, no flush", "parallelism": f"replicas x{world}"},
+                   "l2": "probe batches > L2, no flush", "parallelism": f"replicas x{world}",
+                   **join_opts_cfg(args)},
         "probe_rows_per_s": n_rows * world / (ms * 1e-3),
         "plain_f64_form": {"pairs_per_s": npairs / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                            "form": "one probe call per batch, FP64 refine",
@@ -794,6 +803,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--join-options", type=json.loads, default={},
+                    help='execution options of the chosen form, e.g. \'{"refine_min_blocks": 6}\'')
     args = ap.parse_args()
     world, rank, local, pg = (1, 0, 0, None)
     if args.impl == "reference":

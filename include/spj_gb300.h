@@ -92,7 +92,8 @@ int SpjJoinFinishBuild(SpjJoin* join);
 /* Execution options (they change speed, never the pairs or their order):
  *   "probe_order"       -1 row order, 0 Morton order from 65536 rows up, 1 always
  *   "candidate_order"   3 (default) auto: 2 for relation predicates with 4M+
- *                       candidates, else 0; 2 by build row then probe Morton
+ *                       candidates over a build side that is not all points,
+ *                       else 0; 2 by build row then probe Morton
  *                       rank, 1 the probes' Morton order, 0 as listed
  *   "refine_min_blocks" 2 to 6 (default 4): FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)

@@ -68,7 +68,6 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     if (s_ok) {
       const float4 q = s_rect;
-      const uint32_t V = G.ring_vtx[r];
       const uint32_t B = G.ring_bands[r];
       const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
       const float2 prm = G.band_param[r];
@@ -79,8 +78,8 @@ __global__ void __launch_bounds__(256)
         const int b0 = band_of(y0, prm.x, prm.y, nb), b1 = band_of(y1, prm.x, prm.y, nb);
         bool clean = true;
         for (uint32_t k = G.band_off[B + b0]; k < G.band_off[B + b1 + 1] && clean; k++) {
-          const int e = G.band_edges[k];
-          const float2 a = G.xy32[V + e], b = G.xy32[V + e + 1];
+          const float4 sg = G.band_seg[k];
+          const float2 a = make_float2(sg.x, sg.y), b = make_float2(sg.z, sg.w);
           if (fmax0f(a.x, b.x) < x0 || fmin0f(a.x, b.x) > x1 || fmax0f(a.y, b.y) < y0 ||
               fmin0f(a.y, b.y) > y1)
             continue;

@@ -199,10 +199,12 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     cperm = candidate_order(order, n, m, ws.psc, s);
     if (cperm) launches += 5;  // gather, 3-kernel scan, scatter
   } else if (cfg_.candidate_order == 2 ||
-             (cfg_.candidate_order == 3 && predicate != kPredDWithin && m >= kBuildMajorMin)) {
-    // (auto, 3: point-point distance candidates are cheap to test, so
-    // reordering them costs more than it saves, and small candidate sets do
-    // not repay the sort)
+             (cfg_.candidate_order == 3 && predicate != kPredDWithin && !bg_.all_points &&
+              m >= kBuildMajorMin)) {
+    // (auto, 3: the order pays when consecutive pairs re-read one build
+    // geometry's vertices and band index from cache; a point build row is
+    // 16 bytes with nothing to re-read, distance candidates are cheap to
+    // test, and small candidate sets do not repay the sort)
     cperm = build_major_order(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                               probe_base, bg_.n, order, n, ws.psc, s);
     if (cperm) launches += 22;  // rank, keys, 4 radix passes

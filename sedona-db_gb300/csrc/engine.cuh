@@ -37,7 +37,8 @@ struct EngineConfig {
   // Morton order, 2 by build row then probe Morton rank (a warp then tests
   // one build geometry's edges against neighbouring probes: shared loads and
   // similar trip counts; 2M x 50k polygons: 77 vs 104 ms per step), 3 auto:
-  // 2 for relation predicates from kBuildMajorMin candidates up, else 0
+  // 2 for relation predicates over a build side that is not all points,
+  // from kBuildMajorMin candidates up, else 0
   int candidate_order = 3;
   // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
   int refine_min_blocks = 4;

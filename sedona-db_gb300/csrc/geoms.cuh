@@ -48,6 +48,9 @@ struct GeomsView {
   const uint32_t* ring_bands = nullptr;  // nrings+1: start of each ring's band_off slice
   const uint32_t* band_off = nullptr;    // per ring: nb+1 offsets into band_edges
   const uint16_t* band_edges = nullptr;  // edge index within the ring
+  // the same entries' f32 segments (a.x, a.y, b.x, b.y): the FP32 tiers read
+  // one 16-byte word per entry instead of an index and then two vertices
+  const float4* band_seg = nullptr;
   const float2* band_param = nullptr;    // per ring: (y origin, bands per unit y)
   // cell grid (nullptr when not built): per ring (status offset, G; G = 0 for
   // no grid), (x0, y0, w, h) with cell (i, j) = [x0 + i w, x0 + (i+1) w] x
@@ -65,7 +68,7 @@ struct DeviceGeoms {
   bool any_polys = false;
   DevBuf kind, pt, box, row_part, part_ring, ring_vtx, ring_nsegs, ring_rect, ring_rect32, xy,
       xy32;
-  DevBuf ring_bands, band_off, band_edges, band_param;
+  DevBuf ring_bands, band_off, band_edges, band_seg, band_param;
   bool has_bands = false;
   DevBuf grid_meta, grid_rect, grid_status;
   bool has_grid = false;
@@ -91,6 +94,7 @@ struct DeviceGeoms {
       v.ring_bands = ring_bands.as<uint32_t>();
       v.band_off = band_off.as<uint32_t>();
       v.band_edges = band_edges.as<uint16_t>();
+      v.band_seg = band_seg.as<float4>();
       v.band_param = band_param.as<float2>();
     }
     if (has_grid) {
@@ -104,7 +108,8 @@ struct DeviceGeoms {
     return kind.size() + pt.size() + box.size() + row_part.size() + part_ring.size() +
            ring_vtx.size() + ring_nsegs.size() + ring_rect.size() + ring_rect32.size() +
            xy.size() + xy32.size() +
-           ring_bands.size() + band_off.size() + band_edges.size() + band_param.size() +
+           ring_bands.size() + band_off.size() + band_edges.size() + band_seg.size() +
+           band_param.size() +
            grid_meta.size() + grid_rect.size() + grid_status.size();
   }
 };

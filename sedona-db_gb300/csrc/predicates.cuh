@@ -300,8 +300,11 @@ __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r
 
 // Chosen form: y-band edge index + FP32 classification + FP64 escalation.
 // Without a band index on this column the ring's segments are all scanned
-// (still with the FP32 classifier).  Segments are visited in increasing
-// index order, so idx (last ON segment) matches tg's sequential walk.
+// (still with the FP32 classifier).  The answer does not depend on the
+// order of the visits: any ON segment makes it allow_on_edge, else it is the
+// parity of the IN segments (tg.c:2668-2735).  Banded entries are visited by
+// xmax descending, so idx is an ON segment, not necessarily tg's last one
+// (no caller reads it).
 __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r, double2 p,
                                                  float2 p32, bool aoe, uint32_t& esc,
                                                  bool use_grid = true) {
@@ -325,14 +328,18 @@ __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r,
     const int b = band_of(p32.y, prm.x, prm.y, nb);
     const uint32_t e0 = G.band_off[B + b], e1 = G.band_off[B + b + 1];
     for (uint32_t k = e0; k < e1; k++) {
-      const int i = G.band_edges[k];
-      const int c = pip_seg_f32(G.xy32[V + i], G.xy32[V + i + 1], p32);
+      const float4 sg = G.band_seg[k];
+      // entries run by xmax descending: from here on every segment lies
+      // strictly left of p, and tg's +x ray cast gives OUT for each
+      if (fmax0f(sg.x, sg.z) < p32.x) break;
+      const int c = pip_seg_f32(make_float2(sg.x, sg.y), make_float2(sg.z, sg.w), p32);
       if (c == kOut) continue;
       if (c == kIn) {
         if (idx == -1) in = !in;
         continue;
       }
       esc++;
+      const int i = G.band_edges[k];
       pip_seg_f64(G.xy[V + i], G.xy[V + i + 1], p, i, aoe, in, idx);
     }
   } else {
@@ -421,8 +428,9 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
   }
   const float qx0 = fmin0f(a32.x, b32.x), qx1 = fmax0f(a32.x, b32.x);
   const float qy0 = fmin0f(a32.y, b32.y), qy1 = fmax0f(a32.y, b32.y);
-  auto test = [&](int i) {
-    const float2 c = G.xy32[V + i], d = G.xy32[V + i + 1];
+  // segment (c, d) of the ring; its index (needed only by the FP64 tier)
+  // is band entry k's edge when banded, else k itself
+  auto test = [&](const float2 c, const float2 d, const uint32_t k, const bool banded_k) {
     if (fmin0f(c.x, d.x) > qx1 || fmax0f(c.x, d.x) < qx0 || fmin0f(c.y, d.y) > qy1 ||
         fmax0f(c.y, d.y) < qy0)
       return;  // strictly separated rects: tg's first test fails
@@ -439,6 +447,7 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
       return;
     }
     esc++;
+    const int i = banded_k ? (int)G.band_edges[k] : (int)k;
     if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
   };
   const bool banded = G.ring_bands != nullptr && G.band_param[r].y >= 0.0f;
@@ -450,18 +459,19 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
     for (int bb = b0; bb <= b1 && count < 2; bb++) {
       const uint32_t e0 = G.band_off[B + bb], e1 = G.band_off[B + bb + 1];
       for (uint32_t k = e0; k < e1 && count < 2; k++) {
-        const int i = G.band_edges[k];
-        if (bb > b0) {
-          // visit each segment once: only in the first band of the query it spans
-          const float2 c = G.xy32[V + i], d = G.xy32[V + i + 1];
-          if (band_of(fmin0f(c.y, d.y), prm.x, prm.y, nb) < bb) continue;
-        }
-        test(i);
+        const float4 sg = G.band_seg[k];
+        const float2 c = make_float2(sg.x, sg.y), d = make_float2(sg.z, sg.w);
+        // xmax descending: the rest of the band is strictly left of the query
+        if (fmax0f(c.x, d.x) < qx0) break;
+        // visit each segment once: only in the first band of the query it spans
+        if (bb > b0 && band_of(fmin0f(c.y, d.y), prm.x, prm.y, nb) < bb) continue;
+        test(c, d, k, true);
       }
     }
   } else {
     const int ns = G.ring_nsegs[r];
-    for (int i = 0; i < ns && count < 2; i++) test(i);
+    for (int i = 0; i < ns && count < 2; i++)
+      test(G.xy32[V + i], G.xy32[V + i + 1], (uint32_t)i, false);
   }
   return count;
 }
@@ -544,7 +554,6 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
     // The result is therefore the point-in-ring test of the first vertex.
     const float4 ob = Go->ring_rect32[ro];
     const float bx0 = ob.x, by0 = ob.y, bx1 = ob.z, by1 = ob.w;
-    const uint32_t Vr = Gr->ring_vtx[rr];
     const uint32_t B = Gr->ring_bands[rr];
     const int nb = (int)(Gr->ring_bands[rr + 1] - B) - 1;
     const float2 prm = Gr->band_param[rr];
@@ -565,8 +574,11 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
       const uint32_t e0 = Gr->band_off[B + bb], e1 = Gr->band_off[B + bb + 1];
       const bool vband = v_in_rect && bb == bv;
       for (uint32_t k = e0; k < e1; k++) {
-        const int i = Gr->band_edges[k];
-        const float2 c = Gr->xy32[Vr + i], d = Gr->xy32[Vr + i + 1];
+        const float4 sg = Gr->band_seg[k];
+        const float2 c = make_float2(sg.x, sg.y), d = make_float2(sg.z, sg.w);
+        // xmax descending: the rest of the band is strictly left of the box
+        // (bbox-separated) and of its first vertex (tg's ray cast: OUT)
+        if (fmax0f(c.x, d.x) < bx0) break;
         if (vband) {
           const int pc = pip_seg_f32(c, d, v032);
           if (pc == kIn) v_par ^= 1u;

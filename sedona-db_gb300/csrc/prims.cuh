@@ -1,7 +1,7 @@
 // prims.cuh — device-wide scan and radix sort used by the decode, LBVH and
 // two-pass count/scatter stages.  Written for sm_103a: 256-thread blocks,
 // warp-shuffle block scans, 8-bit LSD radix passes with block-local stable
-// splits in shared memory.
+// ranking (warp match) and a reorder in shared memory.
 #pragma once
 #include "common.cuh"
 

@@ -366,10 +366,11 @@ __global__ void k_band_count(uint32_t nrings, const int32_t* __restrict__ nsegs,
 
 __global__ void k_band_fill(uint32_t nrings, const int32_t* __restrict__ nsegs,
                             const uint32_t* __restrict__ ring_vtx, const double2* __restrict__ xy,
-                            const float2* __restrict__ param,
+                            const float2* __restrict__ xy32, const float2* __restrict__ param,
                             const uint32_t* __restrict__ ring_bands,
                             const uint64_t* __restrict__ ent_start,
-                            uint32_t* __restrict__ band_off, uint16_t* __restrict__ band_edges) {
+                            uint32_t* __restrict__ band_off, uint16_t* __restrict__ band_edges,
+                            float4* __restrict__ band_seg, uint32_t* __restrict__ band_id) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrings;
        r += (int64_t)gridDim.x * blockDim.x) {
     const int32_t ns = nsegs[r];
@@ -399,11 +400,53 @@ __global__ void k_band_fill(uint32_t nrings, const int32_t* __restrict__ nsegs,
       double ya = xy[V + i].y, yb = xy[V + i + 1].y;
       int lo = band_of(__double2float_rn(ya < yb ? ya : yb), pr.x, pr.y, nb);
       int hi = band_of(__double2float_rn(ya > yb ? ya : yb), pr.x, pr.y, nb);
-      for (int b = lo; b <= hi; b++) band_edges[off[b]++] = (uint16_t)i;
+      const float2 a32 = xy32[V + i], b32 = xy32[V + i + 1];
+      const float4 sg = make_float4(a32.x, a32.y, b32.x, b32.y);
+      for (int b = lo; b <= hi; b++) {
+        band_seg[off[b]] = sg;
+        band_id[off[b]] = B + (uint32_t)b;
+        band_edges[off[b]++] = (uint16_t)i;
+      }
     }
     // cursors advanced to the band ends: shift back to starts
     for (int b = nb; b > 0; b--) off[b] = off[b - 1];
     off[0] = (uint32_t)ent_start[r];
+  }
+}
+
+// Sort key of a band entry: its f32 segment's xmax, descending, NaN first
+// (NaN never satisfies the scans' "xmax < x" stop test, so it must come
+// before every entry they may stop at).  The map from f32 to an unsigned key
+// that orders like the floats is the sign-flip of the IEEE bits.
+__global__ void k_band_xkeys(uint32_t n, const float4* __restrict__ seg, uint32_t* __restrict__ keys,
+                             uint32_t* __restrict__ vals) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const float4 g = seg[e];
+    const float x = g.x > g.z ? g.x : g.z;
+    uint32_t k = 0;
+    if (!isnan(x)) {
+      const uint32_t u = __float_as_uint(x);
+      k = ~(u ^ ((u >> 31) ? 0xFFFFFFFFu : 0x80000000u));
+    }
+    keys[e] = k;
+    vals[e] = e;
+  }
+}
+
+__global__ void k_gather_band_id(uint32_t n, const uint32_t* __restrict__ band_id,
+                                 const uint32_t* __restrict__ perm, uint32_t* __restrict__ out) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    out[e] = band_id[perm[e]];
+}
+
+__global__ void k_band_permute(uint32_t n, const uint32_t* __restrict__ perm,
+                               const float4* __restrict__ seg_in,
+                               const uint16_t* __restrict__ edge_in, float4* __restrict__ seg_out,
+                               uint16_t* __restrict__ edge_out) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const uint32_t q = perm[e];
+    seg_out[e] = seg_in[q];
+    edge_out[e] = edge_in[q];
   }
 }
 
@@ -552,6 +595,7 @@ void build_band_index(DeviceGeoms& g, DecodeScratch& sc, cudaStream_t s) {
     SPJ_CUDA(cudaMemsetAsync(g.ring_bands.get(), 0, 4, s));
     g.band_off.reserve(4, s);
     g.band_edges.reserve(4, s);
+    g.band_seg.reserve(16, s);
     return;
   }
   sc.counts.reserve((size_t)2 * (nr + 1) * 4, s);
@@ -574,11 +618,38 @@ void build_band_index(DeviceGeoms& g, DecodeScratch& sc, cudaStream_t s) {
   k_u64_to_u32<<<grid_for(nr + 1, 256), 256, 0, s>>>(sb, g.ring_bands.as<uint32_t>(), nr + 1);
   g.band_off.reserve((size_t)(tb + 1) * 4, s);
   g.band_edges.reserve((size_t)(te + 1) * 2, s);
+  g.band_seg.reserve((size_t)(te + 1) * 16, s);
+  // entries in edge order first, then each band sorted by xmax descending
+  // (stable: band-major after two LSD sorts), so the FP32 scans stop at the
+  // first entry strictly left of the point or box they test
+  DevBuf seg0((size_t)(te + 1) * 16, s), edge0((size_t)(te + 1) * 2, s);
+  DevBuf bid((size_t)(te + 1) * 4, s), keys((size_t)(te + 1) * 4, s),
+      vals((size_t)(te + 1) * 4, s), akeys((size_t)(te + 1) * 4, s),
+      avals((size_t)(te + 1) * 4, s);
   k_band_fill<<<grid, 128, 0, s>>>(nr, g.ring_nsegs.as<int32_t>(), g.ring_vtx.as<uint32_t>(),
-                                   g.xy.as<double2>(), g.band_param.as<float2>(),
-                                   g.ring_bands.as<uint32_t>(), se, g.band_off.as<uint32_t>(),
-                                   g.band_edges.as<uint16_t>());
+                                   g.xy.as<double2>(), g.xy32.as<float2>(),
+                                   g.band_param.as<float2>(), g.ring_bands.as<uint32_t>(), se,
+                                   g.band_off.as<uint32_t>(), edge0.as<uint16_t>(),
+                                   seg0.as<float4>(), bid.as<uint32_t>());
   SPJ_CUDA(cudaGetLastError());
+  const uint32_t ne = (uint32_t)te;
+  if (ne > 0) {
+    const int eg = grid_for(ne, 256, kNumSMs * 8);
+    k_band_xkeys<<<eg, 256, 0, s>>>(ne, seg0.as<float4>(), keys.as<uint32_t>(),
+                                    vals.as<uint32_t>());
+    radix_sort_pairs(keys.as<uint32_t>(), vals.as<uint32_t>(), akeys.as<uint32_t>(),
+                     avals.as<uint32_t>(), ne, 32, sc.tmp, s);
+    k_gather_band_id<<<eg, 256, 0, s>>>(ne, bid.as<uint32_t>(), vals.as<uint32_t>(),
+                                        keys.as<uint32_t>());
+    int bits = 1;
+    while (bits < 32 && (tb >> bits) != 0) bits++;
+    radix_sort_pairs(keys.as<uint32_t>(), vals.as<uint32_t>(), akeys.as<uint32_t>(),
+                     avals.as<uint32_t>(), ne, bits, sc.tmp, s);
+    k_band_permute<<<eg, 256, 0, s>>>(ne, vals.as<uint32_t>(), seg0.as<float4>(),
+                                      edge0.as<uint16_t>(), g.band_seg.as<float4>(),
+                                      g.band_edges.as<uint16_t>());
+    SPJ_CUDA(cudaGetLastError());
+  }
   g.has_bands = true;
 }
 
