@@ -238,35 +238,6 @@ def run_ours(args, world, rank, local, pg):
     st = chosen["stats"]
     steps = args.steps
 
-    # execution options of the chosen form, each timed on its own join
-    # (they change speed only; the pair count is checked)
-    variants = {}
-    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 6}, {"refine_min_blocks": 5},
-                   {"refine_min_blocks": 3},
-                   {"cell_grid": 0}, {"probe_order": -1}]
-    if pred == "dwithin":
-        option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
-                        {"leaf_size": 4}, {"leaf_size": 32}]
-    for opts in option_sets:
-        jv = make_join(1, opts)
-        for _ in range(2):
-            jv.probe_device(dcol, pred, distance)
-        sv = torch.cuda.ExternalStream(jv.stream())
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        with torch.cuda.stream(sv):
-            e0.record(sv)
-        nv = 0
-        for _ in range(max(1, min(steps, 3))):
-            _, _, nv = jv.probe_device(dcol, pred, distance)
-        with torch.cuda.stream(sv):
-            e1.record(sv)
-        torch.cuda.synchronize()
-        assert nv == chosen["pairs"], (opts, nv, chosen["pairs"])
-        name = ",".join(f"{k}={v}" for k, v in opts.items())
-        variants[name] = e0.elapsed_time(e1) / max(1, min(steps, 3))
-        del jv
-
     # e2e: host (pinned) WKB -> C ABI -> host pairs, copies inside the timed region
     # (page-locked host buffers from cudaHostAlloc, through torch's pinned
     # allocator; the column is copied in before the timed region)
@@ -302,6 +273,49 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.synchronize()
     e2e_ms = barrier_max(pg, e0.elapsed_time(e1) / steps, dev)
     assert n_e2e == chosen["pairs"], (n_e2e, chosen["pairs"])
+
+    # the host link alone: one step's pairs copied device -> the same pinned
+    # host buffers, on the join's stream
+    db_, dp_, n_ = j.probe_device(dcol, pred, distance)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        t_ob[:n_].copy_(dev_i32(db_, n_), non_blocking=True)
+        t_op[:n_].copy_(dev_i32(dp_, n_), non_blocking=True)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    link_gbps = 8 * n_ / (e0.elapsed_time(e1) * 1e6) if n_ else None
+
+    # execution options of the chosen form, each timed on its own join
+    # (they change speed only; the pair count is checked)
+    variants = {}
+    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 4}, {"refine_min_blocks": 5},
+                   {"refine_min_blocks": 3},
+                   {"cell_grid": 0}, {"probe_order": -1}, {"refine_split": 1},
+                   {"candidate_order": 0, "refine_split": 0}, {"candidate_order": 4}]
+    if pred == "dwithin":
+        option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
+                        {"leaf_size": 4}, {"leaf_size": 32}]
+    for opts in option_sets:
+        jv = make_join(1, opts)
+        for _ in range(2):
+            jv.probe_device(dcol, pred, distance)
+        sv = torch.cuda.ExternalStream(jv.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(sv):
+            e0.record(sv)
+        nv = 0
+        for _ in range(max(1, min(steps, 3))):
+            _, _, nv = jv.probe_device(dcol, pred, distance)
+        with torch.cuda.stream(sv):
+            e1.record(sv)
+        torch.cuda.synchronize()
+        assert nv == chosen["pairs"], (opts, nv, chosen["pairs"])
+        name = ",".join(f"{k}={v}" for k, v in opts.items())
+        variants[name] = e0.elapsed_time(e1) / max(1, min(steps, 3))
+        del jv
+
 
     # roofline of the dominant kernel (refine) over the timed steps
     hbm_peak, peak_kind = load_peaks()
@@ -361,7 +375,8 @@ def run_ours(args, world, rank, local, pg):
         "e2e": {"value": pairs_total / (e2e_ms * 1e-3), "unit": "pairs/s",
                 "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(off.nbytes + data.nbytes),
-                "d2h_bytes_per_step": int(8 * n_e2e)},
+                "d2h_bytes_per_step": int(8 * n_e2e),
+                "d2h_link_GBps": link_gbps},
         "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved,
                      "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,

@@ -93,12 +93,21 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "probe_order"       -1 row order, 0 Morton order from 65536 rows up, 1 always
  *   "candidate_order"   3 (default) auto: 2 for relation predicates with 4M+
  *                       candidates over a build side that is not all points,
- *                       else 0; 2 by build row then probe Morton
+ *                       else 0; 4 by build row then the probe box's band
+ *                       and x in the build ring; 2 by build row then probe Morton
  *                       rank, 1 the probes' Morton order, 0 as listed
- *   "refine_min_blocks" 2 to 6 (default 4): FP32 refine built for that many
+ *   "refine_min_blocks" 0 (default: auto, 6 in build-major candidate order,
+ *                       else 4) or 2 to 6: FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)
  *   "refine_group"      0 (default: one lane per pair), 4, 8, 16: lanes
  *                       cooperating on one candidate pair in the FP32 refine
+ *   "refine_split"      2 (default: auto, on unless the candidates are in
+ *                       build-major order), 1 on, 0 off: FP32 refine of
+ *                       relation predicates in two passes (a cheap pass over
+ *                       all pairs queues the pairs it leaves open for a full
+ *                       pass)
+ *   "host_slices"       0 (default: auto), 1 (one call), 2-64: row slices of
+ *                       SpjJoinProbeHost (see there)
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
@@ -133,7 +142,12 @@ int SpjJoinProbeDevice(SpjJoin* join, const struct SpjDeviceWkb* column, int32_t
 /* Probe with a host column given as plain buffers (the same layout as an
  * Arrow binary array); results are copied into caller buffers of capacity
  * `capacity` pairs.  *n_pairs receives the full count; if it exceeds
- * capacity nothing is copied and ENOSPC is returned. */
+ * capacity ENOSPC is returned and the buffers' contents are unspecified.
+ * A column of 524,288 rows or more is probed in row slices (about 48 MB of
+ * WKB each, at most 8) on two workspaces in turn, so that the copies of the
+ * neighbouring slices run while one slice is probed; the pairs and their
+ * order are those of one call over the whole column.  Page-locked buffers
+ * (cudaHostAlloc / cudaHostRegister) let those copies run asynchronously. */
 int SpjJoinProbeHost(SpjJoin* join, int64_t length, const void* offsets,
                      int32_t offsets_are_64bit, const uint8_t* data, const uint8_t* validity,
                      int32_t predicate, double distance, uint32_t probe_base,

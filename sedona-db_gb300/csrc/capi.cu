@@ -576,39 +576,117 @@ struct SpjJoin {
   RuntimeData* rt = nullptr;
   std::unique_ptr<JoinEngine> engine;
   std::unique_ptr<WorkspacePool> pool;
-  std::unique_ptr<Workspace> ws;  // the join's own stream and scratch
+  std::unique_ptr<Workspace> ws;   // the join's own stream and scratch
+  std::unique_ptr<Workspace> ws2;  // second slot of the sliced host probe
   HostColumnBuilder host;
   std::vector<uint32_t> hb, hp;
   std::string last_error;
-  // second stream for device -> host pair copies (two copy engines at once)
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t ready = nullptr, copied = nullptr;
+  // per workspace slot: a second stream for device -> host pair copies (two
+  // copy engines at once) and its fork / join events
+  struct CopyLane {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ready = nullptr, copied = nullptr;
+  } lanes[2];
   ~SpjJoin() {
-    if (copy_stream) {
-      cudaStreamSynchronize(copy_stream);
-      cudaStreamDestroy(copy_stream);
+    for (auto& l : lanes) {
+      if (l.stream) {
+        cudaStreamSynchronize(l.stream);
+        cudaStreamDestroy(l.stream);
+      }
+      if (l.ready) cudaEventDestroy(l.ready);
+      if (l.copied) cudaEventDestroy(l.copied);
     }
-    if (ready) cudaEventDestroy(ready);
-    if (copied) cudaEventDestroy(copied);
   }
 };
 
-// Both pair arrays to host memory: build ids on the join's stream, probe ids
-// on a second stream, so that two copy engines move them at once.
+// Both pair arrays to host memory: build ids on the workspace's stream, probe
+// ids on the lane's second stream, so that two copy engines move them at
+// once.  Stream-ordered: the workspace's stream waits for both copies.
+static void copy_pairs_to_host(SpjJoin* j, Workspace& w, int lane, const uint32_t* db,
+                               const uint32_t* dp, uint64_t m, uint32_t* hb, uint32_t* hp) {
+  cudaStream_t s = w.stream;
+  SpjJoin::CopyLane& l = j->lanes[lane];
+  if (!l.stream) {
+    SPJ_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
+    SPJ_CUDA(cudaEventCreateWithFlags(&l.ready, cudaEventDisableTiming));
+    SPJ_CUDA(cudaEventCreateWithFlags(&l.copied, cudaEventDisableTiming));
+  }
+  SPJ_CUDA(cudaEventRecord(l.ready, s));
+  SPJ_CUDA(cudaStreamWaitEvent(l.stream, l.ready, 0));
+  SPJ_CUDA(cudaMemcpyAsync(hp, dp, m * 4, cudaMemcpyDeviceToHost, l.stream));
+  SPJ_CUDA(cudaMemcpyAsync(hb, db, m * 4, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaEventRecord(l.copied, l.stream));
+  SPJ_CUDA(cudaStreamWaitEvent(s, l.copied, 0));
+}
 static void copy_pairs_to_host(SpjJoin* j, const uint32_t* db, const uint32_t* dp, uint64_t m,
                                uint32_t* hb, uint32_t* hp) {
-  cudaStream_t s = j->ws->stream;
-  if (!j->copy_stream) {
-    SPJ_CUDA(cudaStreamCreateWithFlags(&j->copy_stream, cudaStreamNonBlocking));
-    SPJ_CUDA(cudaEventCreateWithFlags(&j->ready, cudaEventDisableTiming));
-    SPJ_CUDA(cudaEventCreateWithFlags(&j->copied, cudaEventDisableTiming));
+  copy_pairs_to_host(j, *j->ws, 0, db, dp, m, hb, hp);
+}
+
+// Sliced host probe: the rows are cut into slices probed one after another
+// on two workspaces in turn, so that the host -> device copy of slice i+1 and
+// the device -> host copy of slice i-1's pairs run while slice i is probed.
+// Pairs come out in the same order as one call over all rows (slices are
+// row ranges in order, and each call groups its pairs by probe row).
+constexpr uint64_t kSliceBytes = 48ull << 20;  // WKB bytes per slice, about
+constexpr int64_t kSliceMinRows = 1 << 18;
+constexpr int kMaxSlices = 8;
+
+static int host_slices(const HostWkbColumn& c, int configured) {
+  if (c.offsets == nullptr || c.n == 0) return 1;
+  if (configured > 0) return (int)std::max<int64_t>(1, std::min<int64_t>(configured, c.n));
+  if (c.n < 2 * kSliceMinRows) return 1;
+  int64_t b0, b1;
+  if (c.offsets64) {
+    b0 = reinterpret_cast<const int64_t*>(c.offsets)[0];
+    b1 = reinterpret_cast<const int64_t*>(c.offsets)[c.n];
+  } else {
+    b0 = reinterpret_cast<const int32_t*>(c.offsets)[0];
+    b1 = reinterpret_cast<const int32_t*>(c.offsets)[c.n];
   }
-  SPJ_CUDA(cudaEventRecord(j->ready, s));
-  SPJ_CUDA(cudaStreamWaitEvent(j->copy_stream, j->ready, 0));
-  SPJ_CUDA(cudaMemcpyAsync(hp, dp, m * 4, cudaMemcpyDeviceToHost, j->copy_stream));
-  SPJ_CUDA(cudaMemcpyAsync(hb, db, m * 4, cudaMemcpyDeviceToHost, s));
-  SPJ_CUDA(cudaEventRecord(j->copied, j->copy_stream));
-  SPJ_CUDA(cudaStreamWaitEvent(s, j->copied, 0));
+  const uint64_t bytes = b1 > b0 ? (uint64_t)(b1 - b0) : 0;
+  int64_t k = (int64_t)((bytes + kSliceBytes - 1) / kSliceBytes);
+  k = std::min<int64_t>(k, c.n / kSliceMinRows);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(k, kMaxSlices));
+}
+
+static HostWkbColumn host_slice(const HostWkbColumn& c, int64_t r0, int64_t r1) {
+  HostWkbColumn s = c;
+  s.n = r1 - r0;
+  s.offsets = static_cast<const uint8_t*>(c.offsets) + r0 * (c.offsets64 ? 8 : 4);
+  s.validity_offset = c.validity_offset + r0;
+  return s;
+}
+
+// Returns the total pair count; copies them only while they fit.
+static uint64_t probe_host_sliced(SpjJoin* j, const HostWkbColumn& hc, int nslices,
+                                  int32_t predicate, double distance, uint32_t probe_base,
+                                  uint32_t* out_build, uint32_t* out_probe, uint64_t capacity) {
+  if (!j->ws2) j->ws2 = std::make_unique<Workspace>();
+  Workspace* W[2] = {j->ws.get(), j->ws2.get()};
+  auto rows = [&](int i) { return hc.n * i / nslices; };
+  WkbDeviceColumn dc[2];
+  uint64_t bytes = 0, total = 0;
+  bool fits = true;
+  dc[0] = stage_column(*W[0], host_slice(hc, rows(0), rows(1)), &bytes);
+  for (int i = 0; i < nslices; i++) {
+    const int a = i & 1, b = a ^ 1;
+    // the next slice's host -> device copy, queued behind that slot's
+    // previous pair copies, runs while this slice is probed
+    if (i + 1 < nslices) dc[b] = stage_column(*W[b], host_slice(hc, rows(i + 1), rows(i + 2)), &bytes);
+    const uint32_t *db, *dp;
+    const uint64_t m = j->engine->probe(*W[a], dc[a], predicate, distance,
+                                        probe_base + (uint32_t)rows(i), &db, &dp);
+    if (fits && total + m > capacity) fits = false;
+    if (fits && m) {
+      SPJ_CHECK(out_build && out_probe, "null output buffers");
+      copy_pairs_to_host(j, *W[a], a, db, dp, m, out_build + total, out_probe + total);
+    }
+    total += m;
+  }
+  SPJ_CUDA(cudaStreamSynchronize(W[1]->stream));
+  SPJ_CUDA(cudaStreamSynchronize(W[0]->stream));
+  return total;
 }
 
 extern "C" int SpjJoinCreate(const SpjJoinConfig* config, SpjJoin** out) {
@@ -653,12 +731,18 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value >= -1 && value <= 1, "probe_order must be -1, 0 or 1");
       c.probe_order = (int)value;
     } else if (k == "candidate_order") {
-      SPJ_CHECK(value >= 0 && value <= 3, "candidate_order must be 0, 1, 2 or 3");
+      SPJ_CHECK(value >= 0 && value <= 4, "candidate_order must be 0, 1, 2, 3 or 4");
       c.candidate_order = (int)value;
     } else if (k == "refine_group") {
       SPJ_CHECK(value == 0 || value == 4 || value == 8 || value == 16,
                 "refine_group must be 0, 4, 8 or 16");
       c.refine_group = (int)value;
+    } else if (k == "refine_split") {
+      SPJ_CHECK(value >= 0 && value <= 2, "refine_split must be 0, 1 or 2");
+      c.refine_split = (int)value;
+    } else if (k == "host_slices") {
+      SPJ_CHECK(value >= 0 && value <= 64, "host_slices must be in [0, 64]");
+      c.host_slices = (int)value;
     } else if (k == "cell_grid") {
       SPJ_CHECK(value == 0 || value == 1, "cell_grid must be 0 or 1");
       c.cell_grid = value != 0;  // takes effect at the next build
@@ -669,7 +753,8 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value == 0 || value == 1, "fuse_dwithin must be 0 or 1");
       c.fuse_dwithin = value != 0;  // takes effect at the next build
     } else if (k == "refine_min_blocks") {
-      SPJ_CHECK(value >= 2 && value <= 6, "refine_min_blocks must be in [2, 6]");
+      SPJ_CHECK(value == 0 || (value >= 2 && value <= 6),
+                "refine_min_blocks must be 0 (auto) or in [2, 6]");
       c.refine_min_blocks = (int)value;
     } else {
       throw Error("unknown option '" + k + "'");
@@ -763,6 +848,14 @@ extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
     hc.offsets64 = offsets_are_64bit != 0;
     hc.data = data;
     hc.validity = validity;
+    const int nslices = host_slices(hc, j->engine->config().host_slices);
+    if (nslices > 1) {
+      const uint64_t m = probe_host_sliced(j, hc, nslices, predicate, distance, probe_base,
+                                           out_build, out_probe, capacity);
+      *n_pairs = m;
+      if (m > capacity) rc = ENOSPC;
+      return;
+    }
     uint64_t bytes = 0;
     WkbDeviceColumn dc = stage_column(*j->ws, hc, &bytes);
     const uint32_t *db, *dp;
@@ -770,7 +863,6 @@ extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
     *n_pairs = m;
     if (m > capacity) {
       rc = ENOSPC;
-      j->last_error = "output capacity too small: need " + std::to_string(m) + " pairs";
       return;
     }
     if (m) {
@@ -780,7 +872,11 @@ extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
     SPJ_CUDA(cudaStreamSynchronize(j->ws->stream));
   });
   if (g) return g;
-  if (rc) return rc;
+  if (rc) {
+    // (set after guarded(), which clears the message of a call that returns)
+    j->last_error = "output capacity too small: need " + std::to_string(*n_pairs) + " pairs";
+    return rc;
+  }
   return 0;
 }
 

@@ -38,10 +38,15 @@ struct EngineConfig {
   // one build geometry's edges against neighbouring probes: shared loads and
   // similar trip counts; 2M x 50k polygons: 77 vs 104 ms per step), 3 auto:
   // 2 for relation predicates over a build side that is not all points,
-  // from kBuildMajorMin candidates up, else 0
+  // from kBuildMajorMin candidates up, else 0; 4 by build row, then the
+  // probe box's band and left x within the build row's first ring
   int candidate_order = 3;
-  // FP32 refine compiled for this many resident 256-thread blocks per SM (2-6)
-  int refine_min_blocks = 4;
+  // FP32 refine compiled for this many resident 256-thread blocks per SM
+  // (2-6), or 0 auto: 6 in build-major candidate order (a warp's pairs share
+  // one build geometry, and more resident warps hide its load latency better
+  // than registers do: 2M x 50k polygons 58.5 vs 60.5 ms), else 4 (10M points
+  // x 50k zones: 96.7 vs 99.4 ms with 6)
+  int refine_min_blocks = 0;
   // per-ring cell grids on the build side (clean cells answer point-in-ring
   // tests in O(1)); set before the build
   bool cell_grid = true;
@@ -50,9 +55,24 @@ struct EngineConfig {
   // point workloads (their band lists are short); groups pay off only when
   // rings have long band lists.
   int refine_group = 0;
+  // FP32 refine in two passes: a cheap pass (isolation exit, first vertex)
+  // over every pair queues the pairs it leaves open, a full pass takes the
+  // queue (a warp's lanes then hold pairs of similar cost).  0 off, 1 on,
+  // 2 auto: on unless the candidates are in build-major order, where a
+  // warp's pairs already share one build geometry (2M x 50k polygons: 59.0
+  // ms one pass vs 61.0 split in build-major order; 78.0 vs 63.3 as listed)
+  int refine_split = 2;
+  // host probes (SpjJoinProbeHost): 0 auto (slices of about 48 MB of WKB
+  // from 524,288 rows up, at most 8), 1 one call, n > 1 that many slices
+  int host_slices = 0;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;
 constexpr uint64_t kBuildMajorMin = 1ull << 22;  // candidates before build-major order pays
+
+// refine_min_blocks as configured, with 0 (auto) resolved by the candidate order
+inline int refine_blocks(int configured, bool build_major) {
+  return configured ? configured : (build_major ? 6 : 4);
+}
 constexpr uint64_t kMaxSlotBytes = 8ull << 30;  // cap of the fused ST_DWithin slot buffer
 
 // Per-phase device time (CUDA events on the launching stream) and counters.
@@ -76,7 +96,8 @@ struct Workspace {
   DecodeScratch dsc;
   ProbeScratch psc;
   DevBuf boxes_tmp, cand_build, cand_probe, flags, pos, out_build, out_probe, scan_tmp, status;
-  DevBuf slots;  // fused ST_DWithin result slots
+  DevBuf slots;   // fused ST_DWithin result slots
+  DevBuf rqueue;  // pairs left open by the refine's cheap pass, then its count
   DevBuf wkb_data, wkb_offsets, wkb_validity;  // H2D staging of host columns
   cudaEvent_t ev[6] = {};
   bool last_probe_points = true;

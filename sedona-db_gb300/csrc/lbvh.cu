@@ -479,6 +479,20 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
   return sc.cperm.as<uint32_t>();
 }
 
+void reserve_candidate_keys(uint64_t m, ProbeScratch& sc, cudaStream_t s) {
+  sc.cperm.reserve((m + 1) * 4, s);
+  sc.ckeys.reserve((m + 1) * 4, s);
+  sc.ckeys_alt.reserve((m + 1) * 4, s);
+  sc.cvals_alt.reserve((m + 1) * 4, s);
+}
+
+const uint32_t* sort_candidate_keys(uint64_t m, int key_bits, ProbeScratch& sc, cudaStream_t s) {
+  radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(), sc.ckeys_alt.as<uint32_t>(),
+                   sc.cvals_alt.as<uint32_t>(), (int64_t)m, key_bits, sc.tmp, s);
+  SPJ_CUDA(cudaGetLastError());
+  return sc.cperm.as<uint32_t>();
+}
+
 static const uint32_t* sort_order(uint32_t n, ProbeScratch& sc, cudaStream_t s) {
   radix_sort_pairs(sc.okeys.as<uint32_t>(), sc.order.as<uint32_t>(), sc.akeys.as<uint32_t>(),
                    sc.avals.as<uint32_t>(), n, 32, sc.tmp, s);

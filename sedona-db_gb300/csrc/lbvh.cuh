@@ -119,6 +119,12 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
                                   uint32_t nprobe, ProbeScratch& sc, cudaStream_t s);
 
+// Sorts caller-made candidate keys: sc.ckeys holds m keys and sc.cperm the
+// candidate indices 0..m-1 (both reserved by reserve_candidate_keys); the
+// stable sort by key_bits bits returns the permutation (sc.cperm).
+void reserve_candidate_keys(uint64_t m, ProbeScratch& sc, cudaStream_t s);
+const uint32_t* sort_candidate_keys(uint64_t m, int key_bits, ProbeScratch& sc, cudaStream_t s);
+
 // The same for FP64 points (KNN queries).
 const uint32_t* point_order(const LbvhView& t, const double2* xy, uint32_t n, ProbeScratch& sc,
                             cudaStream_t s);

@@ -525,12 +525,19 @@ __device__ __forceinline__ bool ring_rects_intersect(const GeomsView& GA, uint32
 // the larger ring" and over its segments of "crosses >= 2 of the larger
 // ring's segments"; tg's per-segment rect test only skips terms that are
 // false, so the vertex tests run first and the result is the same.
-template <bool kFast>
-__device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32_t ra,
-                                                     const GeomsView& GB, uint32_t rb,
-                                                     uint32_t& esc) {
-  if (ring_npts(GA, ra) < 3 || ring_npts(GB, rb) < 3) return false;
-  if (!ring_rects_intersect<kFast>(GA, ra, GB, rb)) return false;
+//
+// kCheap (FP32 form with a band index) stops early: a pair that the
+// isolation exit does not decide, and whose first vertex is not in the larger
+// ring, returns kDeferred instead of running the vertex and segment loops.
+// Returns 1 / 0 (or kDeferred).
+constexpr int kDeferred = -2;
+
+template <bool kFast, bool kCheap = false>
+__device__ __forceinline__ int ring_intersects_ring(const GeomsView& GA, uint32_t ra,
+                                                    const GeomsView& GB, uint32_t rb,
+                                                    uint32_t& esc) {
+  if (ring_npts(GA, ra) < 3 || ring_npts(GB, rb) < 3) return 0;
+  if (!ring_rects_intersect<kFast>(GA, ra, GB, rb)) return 0;
   const GeomsView* Gr = &GA;
   const GeomsView* Go = &GB;
   uint32_t rr = ra, ro = rb;
@@ -601,9 +608,14 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
       }
     }
     if (!near) {
-      if (!v_in_rect) return false;  // ring_pip's first test
+      if (!v_in_rect) return 0;  // ring_pip's first test
       if (v_decided) return v_par != 0;
-      return ring_pip<kFast>(*Gr, rr, v0, v032, true, esc).hit;
+      return ring_pip<kFast>(*Gr, rr, v0, v032, true, esc).hit ? 1 : 0;
+    }
+    if (kCheap) {
+      // the vertex loop below starts with this test
+      if (ring_pip<kFast>(*Gr, rr, v0, v032, true, esc, false).hit) return 1;
+      return kDeferred;
     }
   }
   // (the vertices of a ring that came near the larger ring's edges: the grid
@@ -611,7 +623,7 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
   for (int i = 0; i <= nso; i++) {
     const double2 v = Go->xy[Vo + i];
     const float2 v32 = Go->xy32[Vo + i];
-    if (ring_pip<kFast>(*Gr, rr, v, v32, true, esc, false).hit) return true;
+    if (ring_pip<kFast>(*Gr, rr, v, v32, true, esc, false).hit) return 1;
   }
   const float4 R32 = Gr->ring_rect32[rr];
   for (int i = 0; i < nso; i++) {
@@ -628,9 +640,9 @@ __device__ __forceinline__ bool ring_intersects_ring(const GeomsView& GA, uint32
           fmax0(a.y, b.y) < R.y)
         continue;
     }
-    if (ring_seg_hits<kFast>(*Gr, rr, a, b, a32, b32, esc) >= 2) return true;
+    if (ring_seg_hits<kFast>(*Gr, rr, a, b, a32, b32, esc) >= 2) return 1;
   }
-  return false;
+  return 0;
 }
 
 // ---------------------------------------------------------------------------

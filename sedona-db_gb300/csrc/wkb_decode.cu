@@ -224,23 +224,34 @@ __global__ void k_wkb_struct(WkbDeviceColumn col, bool al, const uint8_t* __rest
 
 __device__ __forceinline__ bool feq(double x, double y) { return !((x < y) | (x > y)); }
 
+// kG lanes per ring (8 for columns of small rings such as building
+// footprints, 32 otherwise); consecutive groups take consecutive rings.
+// Each ring is a chain of dependent loads (its source offset, then its
+// points, then the closing copy), so more rings in flight per warp is what
+// shortens the pass.
+template <int kG>
 __global__ void k_wkb_coords(const uint8_t* __restrict__ d, uint64_t len, bool al,
                              uint32_t nrings, const uint64_t* __restrict__ ring_src,
                              const uint32_t* __restrict__ ring_npts,
                              const uint32_t* __restrict__ ring_vtx, double2* __restrict__ xy,
                              float2* __restrict__ xy32, Rect64* __restrict__ ring_rect,
                              float4* __restrict__ ring_rect32, int32_t* __restrict__ ring_nsegs) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = wid; r < nrings; r += nw) {
-    const uint64_t src = ring_src[r];
+  const int lane = threadIdx.x & (kG - 1);
+  const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kG;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) / kG;
+  // every group of the warp runs the same number of trips, so the shuffles
+  // below always see the whole warp
+  const int64_t trips = ((int64_t)nrings + nw - 1) / nw;
+  for (int64_t t = 0; t < trips; t++) {
+    const int64_t r = wid + t * nw;
+    const bool live = r < nrings;
+    const uint64_t src = live ? ring_src[r] : 0;
     const bool le = (src >> 63) != 0;
     const uint64_t o = src & ~(1ull << 63);
-    const uint32_t npts = ring_npts[r];
-    const uint32_t V = ring_vtx[r];
+    const uint32_t npts = live ? ring_npts[r] : 0;
+    const uint32_t V = live ? ring_vtx[r] : 0;
     double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
-    for (uint32_t j = lane; j < npts; j += 32) {
+    for (uint32_t j = lane; j < npts; j += kG) {
       uint32_t w[4];
       load_words<4>(d, o + 16ull * j, len, al, w);
       double x = wkb_f64(w[0], w[1], le), y = wkb_f64(w[2], w[3], le);
@@ -253,7 +264,7 @@ __global__ void k_wkb_coords(const uint8_t* __restrict__ d, uint64_t len, bool a
       if (y > mxy) mxy = y;
     }
 #pragma unroll
-    for (int m = 16; m > 0; m >>= 1) {
+    for (int m = kG / 2; m > 0; m >>= 1) {
       double a = __shfl_xor_sync(0xffffffffu, mnx, m);
       double b = __shfl_xor_sync(0xffffffffu, mny, m);
       double c = __shfl_xor_sync(0xffffffffu, mxx, m);
@@ -264,7 +275,7 @@ __global__ void k_wkb_coords(const uint8_t* __restrict__ d, uint64_t len, bool a
       if (e > mxy) mxy = e;
     }
     __syncwarp();
-    if (lane == 0) {
+    if (live && lane == 0) {
       ring_rect[r] = make_rect64(mnx, mny, mxx, mxy);
       ring_rect32[r] = make_float4(__double2float_rn(mnx), __double2float_rn(mny),
                                    __double2float_rn(mxx), __double2float_rn(mxy));
@@ -575,10 +586,19 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
       k_wkb_struct<false><<<grid, block, 0, s>>>(col, al, out.kind.as<uint8_t>(), spart, sring,
                                                  svert, out.part_ring.as<uint32_t>(),
                                                  out.ring_vtx.as<uint32_t>(), ring_src, ring_npts);
-    k_wkb_coords<<<grid_for((int64_t)out.nrings * 32, 256, kNumSMs * 32), 256, 0, s>>>(
-        col.data, col.data_len, al, out.nrings, ring_src, ring_npts, out.ring_vtx.as<uint32_t>(),
-        out.xy.as<double2>(), out.xy32.as<float2>(), out.ring_rect.as<Rect64>(),
-        out.ring_rect32.as<float4>(), out.ring_nsegs.as<int32_t>());
+    // (nverts counts each ring's extra closing vertex; a group's trips over
+    // a ring's vertices issue independent loads, so 8 lanes also serve rings
+    // of up to a few dozen points)
+    if ((uint64_t)out.nverts <= 24ull * out.nrings)
+      k_wkb_coords<8><<<grid_for((int64_t)out.nrings * 8, 256, kNumSMs * 32), 256, 0, s>>>(
+          col.data, col.data_len, al, out.nrings, ring_src, ring_npts,
+          out.ring_vtx.as<uint32_t>(), out.xy.as<double2>(), out.xy32.as<float2>(),
+          out.ring_rect.as<Rect64>(), out.ring_rect32.as<float4>(), out.ring_nsegs.as<int32_t>());
+    else
+      k_wkb_coords<32><<<grid_for((int64_t)out.nrings * 32, 256, kNumSMs * 32), 256, 0, s>>>(
+          col.data, col.data_len, al, out.nrings, ring_src, ring_npts,
+          out.ring_vtx.as<uint32_t>(), out.xy.as<double2>(), out.xy32.as<float2>(),
+          out.ring_rect.as<Rect64>(), out.ring_rect32.as<float4>(), out.ring_nsegs.as<int32_t>());
     k_row_box<<<grid, block, 0, s>>>(out.n, out.kind.as<uint8_t>(), out.row_part.as<uint32_t>(),
                                      out.part_ring.as<uint32_t>(), out.ring_rect.as<Rect64>(),
                                      out.box.as<float4>());
