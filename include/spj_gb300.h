@@ -144,9 +144,9 @@ int SpjJoinProbeDevice(SpjJoin* join, const struct SpjDeviceWkb* column, int32_t
  * `capacity` pairs.  *n_pairs receives the full count; if it exceeds
  * capacity ENOSPC is returned and the buffers' contents are unspecified.
  * A column of 524,288 rows or more is probed in row slices (about 48 MB of
- * WKB each, at most 8) on two workspaces in turn, so that the copies of the
- * neighbouring slices run while one slice is probed; the pairs and their
- * order are those of one call over the whole column.  Page-locked buffers
+ * WKB each, at most 8) by two host threads on two workspaces, so that two
+ * slices' kernels and the copies of their neighbours are in flight at once;
+ * the pairs and their order are those of one call over the whole column.  Page-locked buffers
  * (cudaHostAlloc / cudaHostRegister) let those copies run asynchronously. */
 int SpjJoinProbeHost(SpjJoin* join, int64_t length, const void* offsets,
                      int32_t offsets_are_64bit, const uint8_t* data, const uint8_t* validity,

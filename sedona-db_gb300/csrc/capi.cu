@@ -9,10 +9,13 @@
 #include <errno.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstring>
+#include <exception>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gpuspatial_c.h"
@@ -623,11 +626,10 @@ static void copy_pairs_to_host(SpjJoin* j, const uint32_t* db, const uint32_t* d
   copy_pairs_to_host(j, *j->ws, 0, db, dp, m, hb, hp);
 }
 
-// Sliced host probe: the rows are cut into slices probed one after another
-// on two workspaces in turn, so that the host -> device copy of slice i+1 and
-// the device -> host copy of slice i-1's pairs run while slice i is probed.
-// Pairs come out in the same order as one call over all rows (slices are
-// row ranges in order, and each call groups its pairs by probe row).
+// Sliced host probe: the rows are cut into slices, probed by two host
+// threads on two workspaces (even and odd slices).  Pairs come out in the
+// same order as one call over all rows (slices are row ranges in order, each
+// call groups its pairs by probe row, and slice i lands after slice i-1).
 constexpr uint64_t kSliceBytes = 48ull << 20;  // WKB bytes per slice, about
 constexpr int64_t kSliceMinRows = 1 << 18;
 constexpr int kMaxSlices = 8;
@@ -664,29 +666,62 @@ static uint64_t probe_host_sliced(SpjJoin* j, const HostWkbColumn& hc, int nslic
                                   uint32_t* out_build, uint32_t* out_probe, uint64_t capacity) {
   if (!j->ws2) j->ws2 = std::make_unique<Workspace>();
   Workspace* W[2] = {j->ws.get(), j->ws2.get()};
+  const int dev = j->rt->device_id;
   auto rows = [&](int i) { return hc.n * i / nslices; };
-  WkbDeviceColumn dc[2];
-  uint64_t bytes = 0, total = 0;
-  bool fits = true;
-  dc[0] = stage_column(*W[0], host_slice(hc, rows(0), rows(1)), &bytes);
-  for (int i = 0; i < nslices; i++) {
-    const int a = i & 1, b = a ^ 1;
-    // the next slice's host -> device copy, queued behind that slot's
-    // previous pair copies, runs while this slice is probed
-    if (i + 1 < nslices) dc[b] = stage_column(*W[b], host_slice(hc, rows(i + 1), rows(i + 2)), &bytes);
-    const uint32_t *db, *dp;
-    const uint64_t m = j->engine->probe(*W[a], dc[a], predicate, distance,
-                                        probe_base + (uint32_t)rows(i), &db, &dp);
-    if (fits && total + m > capacity) fits = false;
-    if (fits && m) {
-      SPJ_CHECK(out_build && out_probe, "null output buffers");
-      copy_pairs_to_host(j, *W[a], a, db, dp, m, out_build + total, out_probe + total);
+  // Two host threads, one per workspace, take the even and the odd slices:
+  // both slices' kernels are in flight on the GPU at once (the slow tail of
+  // one launch overlaps the other slice's work), and the copies of a slice
+  // overlap the other's kernels.  Slice i's pairs go to the host offset
+  // start[i], known once slice i-1 has counted its pairs.
+  std::vector<uint64_t> start((size_t)nslices + 1, 0);
+  std::vector<char> known((size_t)nslices + 1, 0);
+  known[0] = 1;
+  std::mutex mu;
+  std::condition_variable cv;
+  bool abort = false;
+  std::exception_ptr err[2];
+  auto worker = [&](int t) {
+    try {
+      SPJ_CUDA(cudaSetDevice(dev));
+      Workspace& w = *W[t];
+      for (int i = t; i < nslices; i += 2) {
+        uint64_t bytes = 0;
+        const WkbDeviceColumn dc = stage_column(w, host_slice(hc, rows(i), rows(i + 1)), &bytes);
+        const uint32_t *db, *dp;
+        const uint64_t m = j->engine->probe(w, dc, predicate, distance,
+                                            probe_base + (uint32_t)rows(i), &db, &dp);
+        uint64_t off = 0;
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return known[i] != 0 || abort; });
+          if (abort) return;
+          off = start[i];
+          start[i + 1] = off + m;
+          known[i + 1] = 1;
+        }
+        cv.notify_all();
+        if (m && off + m <= capacity) {
+          SPJ_CHECK(out_build && out_probe, "null output buffers");
+          // stream-ordered: this workspace's next slice starts after them
+          copy_pairs_to_host(j, w, t, db, dp, m, out_build + off, out_probe + off);
+        }
+      }
+      SPJ_CUDA(cudaStreamSynchronize(w.stream));
+    } catch (...) {
+      err[t] = std::current_exception();
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        abort = true;
+      }
+      cv.notify_all();
     }
-    total += m;
-  }
-  SPJ_CUDA(cudaStreamSynchronize(W[1]->stream));
-  SPJ_CUDA(cudaStreamSynchronize(W[0]->stream));
-  return total;
+  };
+  std::thread second(worker, 1);
+  worker(0);
+  second.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
+  return start[(size_t)nslices];
 }
 
 extern "C" int SpjJoinCreate(const SpjJoinConfig* config, SpjJoin** out) {
