@@ -589,6 +589,10 @@ struct SpjJoin {
   struct CopyLane {
     cudaStream_t stream = nullptr;
     cudaEvent_t ready = nullptr, copied = nullptr;
+    // sliced host probe: a slice's pair buffers, handed over by its
+    // workspace while their device -> host copy runs
+    DevBuf hold_build, hold_probe;
+    bool pending = false;  // `copied` marks a copy of the hold buffers
   } lanes[2];
   ~SpjJoin() {
     for (auto& l : lanes) {
@@ -624,6 +628,29 @@ static void copy_pairs_to_host(SpjJoin* j, Workspace& w, int lane, const uint32_
 static void copy_pairs_to_host(SpjJoin* j, const uint32_t* db, const uint32_t* dp, uint64_t m,
                                uint32_t* hb, uint32_t* hp) {
   copy_pairs_to_host(j, *j->ws, 0, db, dp, m, hb, hp);
+}
+
+// One slice's pairs (in w.out_*) to host memory without holding up w's next
+// slice: w's output buffers are swapped with the lane's hold buffers (whose
+// previous copy w's stream first waits for, long finished in steady state),
+// and the copies read the handed-over buffers on the lane's stream.
+static void copy_slice_to_host(SpjJoin* j, Workspace& w, int lane, const uint32_t* db,
+                               const uint32_t* dp, uint64_t m, uint32_t* hb, uint32_t* hp) {
+  SpjJoin::CopyLane& l = j->lanes[lane];
+  if (!l.stream) {
+    SPJ_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
+    SPJ_CUDA(cudaEventCreateWithFlags(&l.ready, cudaEventDisableTiming));
+    SPJ_CUDA(cudaEventCreateWithFlags(&l.copied, cudaEventDisableTiming));
+  }
+  if (l.pending) SPJ_CUDA(cudaStreamWaitEvent(w.stream, l.copied, 0));
+  std::swap(w.out_build, l.hold_build);
+  std::swap(w.out_probe, l.hold_probe);
+  SPJ_CUDA(cudaEventRecord(l.ready, w.stream));
+  SPJ_CUDA(cudaStreamWaitEvent(l.stream, l.ready, 0));
+  SPJ_CUDA(cudaMemcpyAsync(hb, db, m * 4, cudaMemcpyDeviceToHost, l.stream));
+  SPJ_CUDA(cudaMemcpyAsync(hp, dp, m * 4, cudaMemcpyDeviceToHost, l.stream));
+  SPJ_CUDA(cudaEventRecord(l.copied, l.stream));
+  l.pending = true;
 }
 
 // Sliced host probe: the rows are cut into slices, probed by two host
@@ -702,11 +729,11 @@ static uint64_t probe_host_sliced(SpjJoin* j, const HostWkbColumn& hc, int nslic
         cv.notify_all();
         if (m && off + m <= capacity) {
           SPJ_CHECK(out_build && out_probe, "null output buffers");
-          // stream-ordered: this workspace's next slice starts after them
-          copy_pairs_to_host(j, w, t, db, dp, m, out_build + off, out_probe + off);
+          copy_slice_to_host(j, w, t, db, dp, m, out_build + off, out_probe + off);
         }
       }
       SPJ_CUDA(cudaStreamSynchronize(w.stream));
+      if (j->lanes[t].stream) SPJ_CUDA(cudaStreamSynchronize(j->lanes[t].stream));
     } catch (...) {
       err[t] = std::current_exception();
       {
