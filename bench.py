@@ -657,6 +657,7 @@ def run_learned(args, world, rank, local, pg):
     ms = barrier_max(pg, e0.elapsed_time(e1) / args.steps, dev)
     lookups_n = after["lookups"] - before["lookups"]
     phases = {k: (after[k] - before[k]) / args.steps for k in ("ms_order", "ms_ranges", "ms_eval")}
+    launches = int(after["kernel_launches"] - before["kernel_launches"])
     steps_per_lookup = (after["search_steps"] - before["search_steps"]) / max(1, lookups_n)
 
     # ablation: the untrained model (line through each leaf's end keys)
@@ -740,6 +741,7 @@ def run_learned(args, world, rank, local, pg):
                      "achieved": achieved, "peak": hbm_peak, "peak_kind": peak_kind,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
                      "algorithmic_bytes_per_launch": alg},
+        "gpu_launches": launches,
         "clocks": sampler.summary(),
     }
     return out, None

@@ -226,6 +226,7 @@ struct SpjLearnedStats {
   double ms_order, ms_ranges, ms_eval;
   uint32_t window;     /* lookups */
   uint32_t window_box; /* the grid cells of range rows */
+  uint64_t kernel_launches; /* this library's kernels launched by queries */
 };
 
 int SpjLearnedCreate(const struct SpjLearnedConfig* config, SpjLearned** out);

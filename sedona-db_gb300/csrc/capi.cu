@@ -1058,6 +1058,7 @@ struct SpjLearned {
   uint32_t leaves = 4096, window = 4096;
   bool trained = true;
   double ms_build = 0;
+  uint64_t decode_launches = 0;  // probe-column decodes of queries
   std::unique_ptr<JoinEngine> engine;  // decodes the build points, owns the LBVH
   std::unique_ptr<Workspace> ws;
   std::unique_ptr<LearnedIndex> index;
@@ -1143,7 +1144,10 @@ extern "C" int SpjLearnedQueryDevice(SpjLearned* li, const SpjDeviceWkb* probe, 
     SPJ_CHECK(d_build && d_probe && n_pairs, "null outputs");
     SPJ_CHECK(predicate >= 0 && predicate <= 7, "relation predicates only");
     Workspace& ws = *li->ws;
-    decode_wkb(device_column(probe), ws.probe, ws.dsc, ws.last_probe_points, ws.stream);
+    const bool hint = ws.last_probe_points;
+    decode_wkb(device_column(probe), ws.probe, ws.dsc, hint, ws.stream);
+    // the decode's kernels: the point kernel alone, or the general path
+    li->decode_launches += ws.probe.all_points && hint ? 1 : 17;
     ws.last_probe_points = ws.probe.all_points;
     *n_pairs = li->index->query(ws.probe.view(), probe_base, predicate, li->out_b, li->out_p,
                                 ws.stream);
@@ -1289,6 +1293,7 @@ extern "C" int SpjLearnedGetStats(SpjLearned* li, SpjLearnedStats* out) {
     out->ms_eval = s.ms_eval;
     out->window = li->index->window();
     out->window_box = li->index->window_box();
+    out->kernel_launches = s.kernel_launches + li->decode_launches;
   });
 }
 

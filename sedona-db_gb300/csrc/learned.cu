@@ -907,6 +907,9 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
     out_probe.reserve(4, s);
     return 0;
   }
+  // row keys, 4 radix passes (5 each), ranges x2 + scan (3); with ranges:
+  // chunk words + scan, eval x2 + scan
+  stats_.kernel_launches += 1 + 20 + 2 + 3;
   // probe rows in key order (locality of the model and key searches)
   SPJ_CUDA(cudaEventRecord(ev_[0], s));
   const size_t rb = ((size_t)np + 1) * 4;
@@ -946,6 +949,7 @@ uint64_t LearnedIndex::query(const GeomsView& probe, uint32_t probe_base, int pr
   const int gb = grid_for((int64_t)(nch * 32), 128, kNumSMs * 16);
   uint64_t total = 0;
   if (nch) {
+    stats_.kernel_launches += 1 + 3 + 2 + 3;
     k_chunk_words<<<gb, 128, 0, s>>>(ranges_.as<uint4>(), nr, cwords_.as<uint32_t>());
     scan_u32_u64(cwords_.as<uint32_t>(), woff_.as<uint64_t>(), (int64_t)nch, tmp_, s);
     uint64_t nw = 0;

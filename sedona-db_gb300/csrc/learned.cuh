@@ -35,6 +35,7 @@ struct LearnedStats {
   uint64_t search_steps = 0;  // binary-search steps over all lookups
   uint64_t ranges = 0;        // build-point ranges handed to the candidate phase
   double ms_order = 0, ms_ranges = 0, ms_eval = 0;  // query phases (CUDA events)
+  uint64_t kernel_launches = 0;  // this library's kernels launched by queries
 };
 
 struct LearnedView;

@@ -181,7 +181,8 @@ class SpjLearnedStats(C.Structure):
                 ("mean_err", C.c_double),
                 ("grad_norm_after", C.c_double), ("ms_build", C.c_double),
                 ("ranges", C.c_uint64), ("ms_order", C.c_double), ("ms_ranges", C.c_double),
-                ("ms_eval", C.c_double), ("window", C.c_uint32), ("window_box", C.c_uint32)]
+                ("ms_eval", C.c_double), ("window", C.c_uint32), ("window_box", C.c_uint32),
+                ("kernel_launches", C.c_uint64)]
 
 _lib = None
 _lib_lock = threading.Lock()

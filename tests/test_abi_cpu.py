@@ -84,4 +84,6 @@ def test_struct_layouts_match_reference_abi():
     # const char*, int, bool (+3 padding), int; rounded up to pointer alignment
     assert C.sizeof(capi.GpuSpatialRuntimeConfig) == (p + 12 + p - 1) // p * p
     assert C.sizeof(capi.SpjJoinConfig) == p + 4 * 4
+    # 5 u64, 4 u32, 5 f64, u64 ranges, 3 f64, 2 u32 windows, u64 launches
+    assert C.sizeof(capi.SpjLearnedStats) == 5 * 8 + 4 * 4 + 5 * 8 + 8 + 3 * 8 + 2 * 4 + 8
     assert C.sizeof(capi.GpuSpatialRefinerConfig) == p + 4 + 1 + 3 + 4 + (4 if p == 8 else 0)
