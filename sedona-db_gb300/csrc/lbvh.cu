@@ -3,6 +3,8 @@
 #include "lbvh.cuh"
 #include "prims.cuh"
 
+#include <algorithm>
+
 namespace spj {
 namespace {
 
@@ -401,6 +403,29 @@ void fill_probe_ids(const uint64_t* offs, uint32_t n, uint32_t probe_base, uint3
   SPJ_CUDA(cudaGetLastError());
 }
 
+void reserve_candidate_order(uint32_t nprobe, uint64_t mcap, ProbeScratch& sc,
+                             cudaStream_t s) {
+  sc.ocount.reserve(((size_t)nprobe + 1) * 4, s);
+  sc.opos.reserve(((size_t)nprobe + 1) * 8, s);
+  sc.cperm.reserve((mcap + 1) * 4, s);
+  sc.tmp.reserve(std::max(scan_tile_sums_bytes(nprobe), radix_sort_tmp_bytes(nprobe)), s);
+}
+
+const uint32_t* candidate_order_into(const uint32_t* order, const uint32_t* counts,
+                                     const uint64_t* offs, uint32_t nprobe, uint64_t mcap,
+                                     ProbeScratch& sc, cudaStream_t s) {
+  if (!order || nprobe == 0 || mcap == 0 || mcap >= 0xFFFFFFFFull) return nullptr;
+  reserve_candidate_order(nprobe, mcap, sc, s);
+  const int g = grid_for(nprobe, 256);
+  k_gather_counts<<<g, 256, 0, s>>>(order, counts, nprobe, sc.ocount.as<uint32_t>());
+  scan_u32_u64_into(sc.ocount.as<uint32_t>(), sc.opos.as<uint64_t>(), nprobe,
+                    sc.tmp.as<uint64_t>(), s);
+  k_cand_perm<<<g, 256, 0, s>>>(order, counts, offs, sc.opos.as<uint64_t>(), nprobe, mcap,
+                                sc.cperm.as<uint32_t>());
+  SPJ_CUDA(cudaGetLastError());
+  return sc.cperm.as<uint32_t>();
+}
+
 const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
                                 ProbeScratch& sc, cudaStream_t s) {
   if (!order || nprobe == 0 || m == 0 || m >= 0xFFFFFFFFull) return nullptr;
@@ -506,6 +531,11 @@ static void reserve_order(uint32_t n, ProbeScratch& sc, cudaStream_t s) {
   sc.okeys.reserve(bytes, s);
   sc.akeys.reserve(bytes, s);
   sc.avals.reserve(bytes, s);
+}
+
+void reserve_probe_order(uint32_t nprobe, ProbeScratch& sc, cudaStream_t s) {
+  reserve_order(nprobe, sc, s);
+  sc.tmp.reserve(std::max(scan_tile_sums_bytes(nprobe), radix_sort_tmp_bytes(nprobe)), s);
 }
 
 const uint32_t* probe_order(const LbvhView& t, const float4* probe_box, uint32_t nprobe,

@@ -96,6 +96,9 @@ void probe_scatter(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
                    const ProbeScratch& sc, uint32_t probe_base, uint32_t* out_build,
                    uint32_t* out_probe, cudaStream_t s, const uint32_t* order = nullptr);
 
+// Reserves what probe_order needs for nprobe rows (so that a call inside a
+// stream capture allocates nothing).
+void reserve_probe_order(uint32_t nprobe, ProbeScratch& sc, cudaStream_t s);
 // The probe rows sorted by the Morton key of their box centre over the tree's
 // extent (sc.order); nullptr when there is nothing to order.
 const uint32_t* probe_order(const LbvhView& t, const float4* probe_box, uint32_t nprobe,
@@ -111,6 +114,14 @@ void fill_probe_ids(const uint64_t* offs, uint32_t n, uint32_t probe_base, uint3
 // refine in that order takes spatially neighbouring probes together.
 const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
                                 ProbeScratch& sc, cudaStream_t s);
+// The same from caller-owned per-row counts / offsets, for a candidate
+// buffer of capacity mcap whose fill count lives on the device (graph
+// replays): cperm[0, m) is the permutation of the m candidates, its entries
+// past m are unspecified.  reserve_candidate_order first, outside a capture.
+void reserve_candidate_order(uint32_t nprobe, uint64_t mcap, ProbeScratch& sc, cudaStream_t s);
+const uint32_t* candidate_order_into(const uint32_t* order, const uint32_t* counts,
+                                     const uint64_t* offs, uint32_t nprobe, uint64_t mcap,
+                                     ProbeScratch& sc, cudaStream_t s);
 
 // The m candidates (cb, cp) ordered by build row, then by the probe's Morton
 // rank (order, when given) - a refine in that order takes one build

@@ -88,6 +88,20 @@ __global__ void k_tile_scan(const Tin* __restrict__ in, int64_t n, const Tout* _
   }
 }
 
+// Scan with caller-owned tile sums ((tiles + 1) entries of Tout).
+template <class Tin, class Tout>
+void scan_into_impl(const Tin* in, Tout* out, int64_t n, Tout* sums, cudaStream_t s) {
+  if (n == 0) {
+    SPJ_CUDA(cudaMemsetAsync(out, 0, sizeof(Tout), s));
+    return;
+  }
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  k_tile_reduce<Tin, Tout><<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums);
+  k_scan_sums<Tout><<<1, 1024, 0, s>>>(sums, nt, out + n);
+  k_tile_scan<Tin, Tout><<<(unsigned)nt, kScanThreads, 0, s>>>(in, n, sums, out);
+  SPJ_CUDA(cudaGetLastError());
+}
+
 template <class Tin, class Tout>
 void scan_impl(const Tin* in, Tout* out, int64_t n, DevBuf& tmp, cudaStream_t s) {
   int64_t nt = (n + kScanTile - 1) / kScanTile;
@@ -233,21 +247,30 @@ void scan_u32_u32(const uint32_t* in, uint32_t* out, int64_t n, DevBuf& tmp, cud
   scan_impl<uint32_t, uint32_t>(in, out, n, tmp, s);
 }
 
+size_t radix_sort_tmp_bytes(int64_t n) {
+  const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
+  const int64_t nh = 256 * (ntiles < 1 ? 1 : ntiles);
+  const int64_t nt = (nh + kScanTile - 1) / kScanTile;
+  return (size_t)(2 * nh + 1 + nt + 1) * sizeof(uint32_t);
+}
+
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
                       int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s) {
   if (n <= 1) return;
   SPJ_CHECK(n < (int64_t)0xFFFFFFFF, "radix sort: too many keys");
   const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
   const int64_t nh = 256 * ntiles;
-  tmp.reserve((size_t)(2 * nh + 1) * sizeof(uint32_t) + 4096 * 8, s);
+  // histogram table, its scan, and the scan's tile sums, all in tmp (no
+  // allocation when tmp already holds radix_sort_tmp_bytes(n): graph capture)
+  tmp.reserve(radix_sort_tmp_bytes(n), s);
   uint32_t* hist = tmp.as<uint32_t>();
   uint32_t* offs = hist + nh;
-  DevBuf scan_tmp;
+  uint32_t* sums = offs + nh + 1;
   uint32_t *ik = keys, *iv = vals, *ok = alt_keys, *ov = alt_vals;
   int passes = 0;
   for (int shift = 0; shift < key_bits; shift += 8) {
     k_digit_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, n, shift, hist, ntiles);
-    scan_u32_u32(hist, offs, nh, scan_tmp, s);
+    scan_into_impl<uint32_t, uint32_t>(hist, offs, nh, sums, s);
     k_digit_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, iv, n, shift, offs, ntiles, ok,
                                                               ov);
     SPJ_CUDA(cudaGetLastError());

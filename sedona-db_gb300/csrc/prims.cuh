@@ -20,6 +20,9 @@ void scan_u32_u64_into(const uint32_t* in, uint64_t* out, int64_t n, uint64_t* t
 // replaced by the sorted sequences; alt_keys/alt_vals are scratch of size n.
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
                       int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s);
+// Bytes of tmp that radix_sort_pairs uses for n keys (reserve them before a
+// stream capture so that the sort allocates nothing inside it).
+size_t radix_sort_tmp_bytes(int64_t n);
 
 // Warp/block helpers usable from other kernels.
 template <class T>

@@ -28,7 +28,8 @@ enum RefineForm : int {
 // With m_dev the pair count is read on the device (CUDA-graph replays) and m
 // is the capacity of cb/cp/flags; flags past the count are cleared.  With
 // perm (a permutation of [0, m)), candidates are evaluated in that order
-// (flags still land at their own index).  min_blocks (2 to 6) selects
+// (flags still land at their own index); with perm and m_dev together, perm
+// is a permutation of [0, *m_dev) and the caller clears the flags past it.  min_blocks (2 to 6) selects
 // the FP32 form compiled for that many resident 256-thread blocks per SM:
 // fewer registers, more warps to hide the latency of divergent pairs.
 // group (4, 8 or 16; FP32 form, no perm) evaluates each pair with that many

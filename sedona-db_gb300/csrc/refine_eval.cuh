@@ -304,6 +304,9 @@ __global__ void __launch_bounds__(256, kMinBlocks)
     const uint64_t u = start + t * stride;
     if (u >= m) continue;
     if (kPhase == 2 && u >= nq) continue;
+    // a permutation with a device-side count covers slots [0, mm) only (the
+    // caller clears the flags past mm)
+    if (kPhase != 2 && perm != nullptr && m_dev != nullptr && u >= mm) continue;
     const uint64_t k = perm ? (uint64_t)perm[u] : u;
     if (k >= mm) {
       if (kPhase != 2 && k < m) flags[k] = 0;

@@ -113,6 +113,7 @@ StreamJoin::~StreamJoin() {
   for (DevBuf* b : {&batches_, &chunks_, &ctrl_, &kind_, &pt_, &box_, &counts_, &offs_, &sums_,
                     &cand_b_, &cand_p_, &flags_, &pos_, &sums2_, &out_b_, &out_p_})
     b->release();
+  psc_ = ProbeScratch();  // its buffers free on s_ too
   cudaStreamSynchronize(s_);
   cudaStreamDestroy(s_);
   cudaFreeHost(h_tot_);
@@ -189,6 +190,16 @@ void StreamJoin::build_graph(int predicate) {
   sums2_.reserve(scan_tile_sums_bytes((int64_t)ccap_), s_);
   out_b_.reserve((ocap_ + 1) * 4, s_);
   out_p_.reserve((ocap_ + 1) * 4, s_);
+  const EngineConfig cfg = eng_.config();
+  // probes in Morton order (coherent traversals, and a refine that takes
+  // neighbouring probes' candidates together); everything the ordering
+  // uses is reserved here, so the capture allocates nothing
+  const bool ordered = ccap_ < 0xFFFFFFFFull &&
+                       (cfg.probe_order > 0 || (cfg.probe_order == 0 && nrows_ >= kOrderMinRows));
+  if (ordered) {
+    reserve_probe_order(nrows_, psc_, s_);
+    reserve_candidate_order(nrows_, ccap_, psc_, s_);
+  }
   SPJ_CUDA(cudaStreamSynchronize(s_));
 
   const GeomsView B = eng_.build_geoms().view();
@@ -204,7 +215,6 @@ void StreamJoin::build_graph(int predicate) {
   const ChunkDesc* cd = chunks_.as<ChunkDesc>();
   const int grid = params_.block == 128 ? persistent_grid<128>() : persistent_grid<256>();
   const uint64_t* d_m = offs_.as<uint64_t>() + nrows_;  // candidate count
-  const EngineConfig cfg = eng_.config();
 
   cudaGraph_t g = nullptr;
   SPJ_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
@@ -216,13 +226,21 @@ void StreamJoin::build_graph(int predicate) {
   else
     k_stream_decode<256><<<grid, 256, 0, s_>>>(bd, cd, nchunks_, queue, kind_.as<uint8_t>(),
                                                pt_.as<double2>(), box_.as<float4>(), st);
-  probe_count_into(t, box_.as<float4>(), nrows_, counts_.as<uint32_t>(), s_);
+  const uint32_t* order = ordered ? probe_order(t, box_.as<float4>(), nrows_, psc_, s_) : nullptr;
+  probe_count_into(t, box_.as<float4>(), nrows_, counts_.as<uint32_t>(), s_, order);
   scan_u32_u64_into(counts_.as<uint32_t>(), offs_.as<uint64_t>(), nrows_, sums_.as<uint64_t>(),
                     s_);
   probe_scatter_from(t, box_.as<float4>(), nrows_, offs_.as<uint64_t>(), 0,
-                     cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), s_, ccap_);
+                     cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), s_, ccap_, order);
+  const uint32_t* cperm =
+      order ? candidate_order_into(order, counts_.as<uint32_t>(), offs_.as<uint64_t>(), nrows_,
+                                   ccap_, psc_, s_)
+            : nullptr;
+  // with a permutation the refine visits only the m candidates; the flags of
+  // the rest of the capacity are cleared here for the flag scan
+  if (cperm) SPJ_CUDA(cudaMemsetAsync(flags_.get(), 0, ccap_ + 1, s_));
   refine_relation(B, P, cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), ccap_, 0, predicate,
-                  cfg.refine_form, flags_.as<uint8_t>(), st, s_, d_m, nullptr,
+                  cfg.refine_form, flags_.as<uint8_t>(), st, s_, d_m, cperm,
                   refine_blocks(cfg.refine_min_blocks, false), cfg.refine_group);
   scan_u8_u64(flags_.as<uint8_t>(), pos_.as<uint64_t>(), (int64_t)ccap_, sums2_, s_);
   compact_pairs(cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), flags_.as<uint8_t>(),
@@ -238,8 +256,9 @@ void StreamJoin::build_graph(int predicate) {
   cudaGraphDestroy(g);
   SPJ_CUDA(e);
   graph_pred_ = predicate;
-  // memsets 2, decode 1, count 1, scan 3, scatter 1, refine 1, flag scan 3, compact 1
-  stats_.launches_per_replay = 13;
+  // memsets 2, decode 1, count 1, scan 3, scatter 1, refine 1, flag scan 3, compact 1;
+  // ordered: keys 1 + 4 radix passes of 5, candidate order 5, flags memset 1
+  stats_.launches_per_replay = 13 + (cperm ? 27 : (order ? 21 : 0));
 }
 
 uint64_t StreamJoin::run(int predicate, const uint32_t** d_build, const uint32_t** d_probe) {

@@ -8,11 +8,13 @@
 // runs:
 //   1. a persistent decode kernel pulling chunks from a work queue (one atomic
 //      per chunk) and decoding every row's point into one stream-wide column;
-//   2. the LBVH count pass, a scan, and the scatter pass over that column
-//      (candidate pairs, bounded by the candidate capacity);
-//   3. the refine kernel over the candidates (the pair count is read on the
-//      device), a scan of its flags, and the compaction (bounded by the output
-//      capacity);
+//   2. from 65,536 rows, the rows' Morton order (keys + radix sort), then the
+//      LBVH count pass, a scan, and the scatter pass over that column in that
+//      order (candidate pairs, bounded by the candidate capacity), and the
+//      candidates' permutation into the same order;
+//   3. the refine kernel over the candidates in that order (the pair count is
+//      read on the device), a scan of its flags, and the compaction (bounded
+//      by the output capacity);
 //   4. the copy-out of the two totals.
 // The host checks the totals after the replay; when a capacity was too small
 // it grows the buffers, re-captures and replays (the buffers then stay large
@@ -69,6 +71,7 @@ class StreamJoin {
   DevBuf batches_, chunks_, ctrl_;
   DevBuf kind_, pt_, box_, counts_, offs_, sums_;  // stream-wide decoded column
   DevBuf cand_b_, cand_p_, flags_, pos_, sums2_, out_b_, out_p_;
+  ProbeScratch psc_;  // the probes' Morton order and the candidates' permutation
   uint64_t* h_tot_ = nullptr;  // pinned: candidates, pairs, status, escalations
   uint64_t ccap_ = 0, ocap_ = 0;
   uint32_t nrows_ = 0, nchunks_ = 0, nbatches_ = 0;

@@ -533,6 +533,34 @@ def test_stream_matches_oracle(capi, oracle_mod, params):
         assert pairs(b, p) == exp
 
 
+def test_stream_probe_order_same_arrays(capi):
+    """From 65,536 rows the stream graph traverses and refines the rows in
+    Morton order; the pairs and their positions must equal the unordered
+    graph's (probe_order = -1)."""
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload3(n_points=150000, n_zones=600, seed=3)
+    rng = np.random.default_rng(4)
+    sizes, left = [], len(inp.probe)
+    while left:
+        s = int(min(left, rng.integers(100, 30000)))
+        sizes.append(s)
+        left -= s
+    dcols, keep = _device_batches(capi, inp.probe, sizes)
+    out = {}
+    for po in (-1, 0, 1):
+        j = capi.SpatialJoin(probe_order=po)
+        j.build(inp.build)
+        st = capi.StreamProbe(j)
+        st.set_batches(dcols)
+        for pred in ("contains", "intersects"):
+            db, dp, n = st.run(pred)
+            out[(po, pred)] = _device_pairs(db, dp, n)
+    for pred in ("contains", "intersects"):
+        for po in (0, 1):
+            np.testing.assert_array_equal(out[(po, pred)][0], out[(-1, pred)][0])
+            np.testing.assert_array_equal(out[(po, pred)][1], out[(-1, pred)][1])
+
+
 def test_stream_autotune_and_cache(capi, oracle_mod, tmp_path):
     from sedona_gpuspatial import datagen
     inp = datagen.workload3(n_points=20000, n_zones=200)
