@@ -283,6 +283,8 @@ def run_ours(args, world, rank, local, pg):
                    {"candidate_order": 0, "refine_split": 0}, {"candidate_order": 4}]
     if pred == "dwithin":
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
+                        {"dwithin_arena": 1}, {"dwithin_slots": 32},
+                        {"probe_order": -1, "dwithin_arena": 0},
                         {"leaf_size": 4}, {"leaf_size": 32}]
     for opts in option_sets:
         jv = make_join(1, opts)

@@ -111,6 +111,11 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
+ *   "dwithin_arena"     2 (default: auto, on when the probes are not in
+ *                       Morton order), 1 on, 0 off: fused ST_DWithin keeps
+ *                       the results past a probe's slots in an overflow
+ *                       arena (of the slots' size), so only probes it cannot
+ *                       hold are traversed again
  *   "dwithin_slots"     64 (default), 0-1024: fused ST_DWithin keeps up to this
  *                       many build ids per probe from its counting pass
  *   "fuse_dwithin"      1 (default) / 0: point-point ST_DWithin decided inside

@@ -808,6 +808,9 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
     } else if (k == "cell_grid") {
       SPJ_CHECK(value == 0 || value == 1, "cell_grid must be 0 or 1");
       c.cell_grid = value != 0;  // takes effect at the next build
+    } else if (k == "dwithin_arena") {
+      SPJ_CHECK(value >= 0 && value <= 2, "dwithin_arena must be 0, 1 or 2");
+      c.dwithin_arena = (int)value;
     } else if (k == "dwithin_slots") {
       SPJ_CHECK(value >= 0 && value <= 1024, "dwithin_slots must be in [0, 1024]");
       c.dwithin_slots = (uint32_t)value;

@@ -83,7 +83,34 @@ __device__ __forceinline__ int leaf_class(float4 b, float hx, float hy, float lx
   return 0;
 }
 
-template <bool kScatter>
+// Appends one build id to the probe's arena chain (counting pass).
+__device__ __forceinline__ void arena_put(const DwithinArena& A, uint32_t id, uint32_t& cur,
+                                          uint32_t& first, uint32_t& fill, bool& failed) {
+  if (failed) return;
+  if (cur == kArenaEnd || fill == kArenaChunkWords - 1) {
+    // one atomic per group of lanes that need a chunk at the same time (in
+    // Morton order neighbouring lanes overflow together)
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    unsigned long long b = 0;
+    if (lane == leader) b = atomicAdd(A.cursor, (unsigned long long)__popc(act));
+    b = __shfl_sync(act, b, leader);
+    const unsigned long long nc64 = b + (unsigned)__popc(act & ((1u << lane) - 1u));
+    if (nc64 >= A.chunks) {
+      failed = true;
+      return;
+    }
+    const uint32_t nc = (uint32_t)nc64;
+    if (cur == kArenaEnd) first = nc;
+    else A.words[(size_t)cur * kArenaChunkWords] = nc;
+    cur = nc;
+    fill = 0;
+  }
+  A.words[(size_t)cur * kArenaChunkWords + 1 + fill] = id;
+  fill++;
+}
+
+template <bool kScatter, bool kArena>
 __global__ void __launch_bounds__(kTravThreads)
     k_dwithin_fused(LbvhView t, const double2* __restrict__ bxy, const float4* __restrict__ bhl,
                     float bmag, int split_ok, const float4* __restrict__ probe_box,
@@ -91,7 +118,8 @@ __global__ void __launch_bounds__(kTravThreads)
                     float d_hi, const uint32_t* __restrict__ order, uint32_t* __restrict__ counts,
                     const uint64_t* __restrict__ offs, uint32_t probe_base,
                     uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
-                    uint64_t cap, DeviceStatus* st, uint32_t* __restrict__ slots, uint32_t K) {
+                    uint64_t cap, DeviceStatus* st, uint32_t* __restrict__ slots, uint32_t K,
+                    DwithinArena A) {
   __shared__ int stack[kTravStack * kTravThreads];
   const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint32_t esc = 0, tested = 0;
@@ -103,10 +131,13 @@ __global__ void __launch_bounds__(kTravThreads)
       continue;
     }
     // the scatter pass only traverses the probes whose results did not all
-    // fit in the counting pass's slots
-    if (kScatter && K > 0 && counts[pi] <= K) continue;
+    // fit in the counting pass's slots and arena
+    if (kScatter && K > 0 && (counts[pi] <= K || (kArena && A.head[pi] != kArenaFailed)))
+      continue;
     const float4 q = probe_box[pi];
     uint32_t cnt = 0;
+    uint32_t a_cur = kArenaEnd, a_first = kArenaEnd, a_fill = 0;
+    bool a_failed = false;
     uint64_t pos = kScatter ? offs[pi] : 0;
     if (q.x <= q.z && q.y <= q.w && t.nprims > 0) {
       const double2 p = probe_pt[pi];
@@ -147,6 +178,7 @@ __global__ void __launch_bounds__(kTravThreads)
                 pos++;
               } else {
                 if (cnt < K) slots[(size_t)pi * K + cnt] = t.sorted_id[k];
+                else if (kArena) arena_put(A, t.sorted_id[k], a_cur, a_first, a_fill, a_failed);
                 cnt++;
               }
             }
@@ -176,6 +208,7 @@ __global__ void __launch_bounds__(kTravThreads)
                 pos++;
               } else {
                 if (cnt < K) slots[(size_t)pi * K + cnt] = t.sorted_id[k];
+                else if (kArena) arena_put(A, t.sorted_id[k], a_cur, a_first, a_fill, a_failed);
                 cnt++;
               }
             }
@@ -208,7 +241,13 @@ __global__ void __launch_bounds__(kTravThreads)
         node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
       }
     }
-    if (!kScatter) counts[pi] = cnt;
+    if (!kScatter) {
+      counts[pi] = cnt;
+      if (kArena) {
+        if (a_cur != kArenaEnd) A.words[(size_t)a_cur * kArenaChunkWords] = kArenaEnd;
+        A.head[pi] = a_failed ? kArenaFailed : a_first;
+      }
+    }
   }
   if (!kScatter) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -222,11 +261,13 @@ __global__ void __launch_bounds__(kTravThreads)
   }
 }
 
-// out_build over each row's run from its slots, for rows with <= K results
-// (warp per 32 consecutive rows, coalesced stores; see fill_probe_ids)
+// out_build over each row's run from its slots: all of a row with <= K
+// results, the first K of a row whose rest is in the arena (warp per 32
+// consecutive rows, coalesced stores; see fill_probe_ids)
 __global__ void k_copy_slots(const uint64_t* __restrict__ offs, const uint32_t* __restrict__ counts,
                              const uint32_t* __restrict__ slots, uint32_t K, uint32_t n,
-                             uint32_t* __restrict__ out, uint64_t cap) {
+                             uint32_t* __restrict__ out, uint64_t cap,
+                             const uint32_t* __restrict__ head) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n; w += nw) {
@@ -245,7 +286,37 @@ __global__ void k_copy_slots(const uint64_t* __restrict__ offs, const uint32_t* 
       }
       const uint64_t r = w * 32 + L;
       const uint64_t sr = __shfl_sync(0xffffffffu, st, L);
-      if (e < e1 && e < cap && r < n && counts[r] <= K) out[e] = slots[r * K + (e - sr)];
+      if (e < e1 && e < cap && r < n) {
+        const uint64_t i = e - sr;
+        const bool mine = counts[r] <= K || (head != nullptr && head[r] != kArenaFailed && i < K);
+        if (mine) out[e] = slots[r * K + i];
+      }
+    }
+  }
+}
+
+// out_build past the first K of each row whose overflow is in the arena: a
+// warp per row, each chunk's ids copied by 31 lanes, the chain followed for
+// at most the chunks the row's count needs.
+__global__ void k_copy_arena(const uint64_t* __restrict__ offs, const uint32_t* __restrict__ counts,
+                             uint32_t K, uint32_t n, DwithinArena A, uint32_t* __restrict__ out,
+                             uint64_t cap) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t r = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
+    const uint32_t c = counts[r];
+    if (c <= K) continue;
+    uint32_t ch = A.head[r];
+    if (ch == kArenaFailed) continue;
+    const uint64_t end = offs[r] + c;
+    uint64_t e = offs[r] + K;
+    const uint32_t maxq = (c - K + kArenaChunkWords - 2) / (kArenaChunkWords - 1);
+    for (uint32_t q = 0; q < maxq && ch < A.chunks && e < end; q++) {
+      const uint64_t o = e + lane;
+      if (lane < kArenaChunkWords - 1 && o < end && o < cap)
+        out[o] = A.words[(size_t)ch * kArenaChunkWords + 1 + lane];
+      e += kArenaChunkWords - 1;
+      ch = A.words[(size_t)ch * kArenaChunkWords];
     }
   }
 }
@@ -285,14 +356,20 @@ void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, Point
 void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                    const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                    uint32_t* counts, DeviceStatus* st, cudaStream_t s, uint32_t* slots,
-                   uint32_t K) {
+                   uint32_t K, DwithinArena arena) {
   if (n == 0) return;
   float lo, hi;
   float_neighbours(d, lo, hi);
   const int g = grid_for(n, kTravThreads, kNumSMs * 16);
-  k_dwithin_fused<false><<<g, kTravThreads, 0, s>>>(
-      t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
-      d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, slots ? K : 0);
+  if (slots && K > 0 && arena.words)
+    k_dwithin_fused<false, true><<<g, kTravThreads, 0, s>>>(
+        t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
+        n, d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, K, arena);
+  else
+    k_dwithin_fused<false, false><<<g, kTravThreads, 0, s>>>(
+        t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
+        n, d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, slots ? K : 0,
+        DwithinArena());
   SPJ_CUDA(cudaGetLastError());
 }
 
@@ -300,19 +377,30 @@ void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* prob
                      const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                      const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
                      uint32_t* out_probe, uint64_t capacity, cudaStream_t s,
-                     const uint32_t* counts, const uint32_t* slots, uint32_t K) {
+                     const uint32_t* counts, const uint32_t* slots, uint32_t K,
+                     DwithinArena arena) {
+  if (!(slots && K > 0)) arena = DwithinArena();
   if (n == 0) return;
   float lo, hi;
   float_neighbours(d, lo, hi);
   const int g = grid_for(n, kTravThreads, kNumSMs * 16);
-  k_dwithin_fused<true><<<g, kTravThreads, 0, s>>>(
-      t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt, n,
-      d, lo, hi, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build, out_probe,
-      capacity, nullptr, nullptr, slots ? K : 0);
+  if (arena.words)
+    k_dwithin_fused<true, true><<<g, kTravThreads, 0, s>>>(
+        t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
+        n, d, lo, hi, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build,
+        out_probe, capacity, nullptr, nullptr, slots ? K : 0, arena);
+  else
+    k_dwithin_fused<true, false><<<g, kTravThreads, 0, s>>>(
+        t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
+        n, d, lo, hi, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build,
+        out_probe, capacity, nullptr, nullptr, slots ? K : 0, arena);
   SPJ_CUDA(cudaGetLastError());
   if (slots && K > 0)
     k_copy_slots<<<grid_for((int64_t)n, 256), 256, 0, s>>>(offs, counts, slots, K, n, out_build,
-                                                            capacity);
+                                                            capacity, arena.head);
+  if (arena.words)
+    k_copy_arena<<<grid_for((int64_t)n * 32, 256, kNumSMs * 32), 256, 0, s>>>(
+        offs, counts, K, n, arena, out_build, capacity);
   fill_probe_ids(offs, n, probe_base, out_probe, capacity, s);
 }
 

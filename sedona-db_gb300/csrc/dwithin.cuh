@@ -35,15 +35,31 @@ void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, Point
 // tested to st->counters[0] / [1]; the scatter pass writes pairs at
 // offs[probe row]: rows with <= K results by a coalesced copy of their slots,
 // the others by traversing again.
+// Overflow arena of the counting pass: a probe's results past its K slots
+// go to chunks of kArenaChunkWords words (word 0: the next chunk, or
+// kArenaEnd; then kArenaChunkWords - 1 build ids), taken with one atomic per
+// chunk from *cursor.  head[probe] is its first chunk, kArenaEnd when it has
+// none, or kArenaFailed when the arena ran out (that probe is traversed again
+// by the scatter pass).
+constexpr uint32_t kArenaChunkWords = 32;
+constexpr uint32_t kArenaEnd = 0xFFFFFFFFu;
+constexpr uint32_t kArenaFailed = 0xFFFFFFFEu;
+struct DwithinArena {
+  uint32_t* words = nullptr;
+  uint32_t chunks = 0;
+  unsigned long long* cursor = nullptr;  // 64-bit: failed takes never wrap it
+  uint32_t* head = nullptr;
+};
+
 void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                    const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                    uint32_t* counts, DeviceStatus* st, cudaStream_t s, uint32_t* slots = nullptr,
-                   uint32_t K = 0);
+                   uint32_t K = 0, DwithinArena arena = DwithinArena());
 void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                      const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                      const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
                      uint32_t* out_probe, uint64_t capacity, cudaStream_t s,
                      const uint32_t* counts = nullptr, const uint32_t* slots = nullptr,
-                     uint32_t K = 0);
+                     uint32_t K = 0, DwithinArena arena = DwithinArena());
 
 }  // namespace spj

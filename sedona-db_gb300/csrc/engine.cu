@@ -3,6 +3,7 @@
 #include "predicates.cuh"
 #include "prims.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -85,6 +86,7 @@ Workspace::~Workspace() {
   out_probe.release();
   scan_tmp.release();
   slots.release();
+  arena.release();
   rqueue.release();
   status.release();
   wkb_data.release();
@@ -194,12 +196,26 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     uint32_t K = cfg_.dwithin_slots;
     while (K > 0 && (uint64_t)n * K * 4 > kMaxSlotBytes) K >>= 1;
     uint32_t* slots = nullptr;
+    DwithinArena arena;
     if (K > 0) {
       ws.slots.reserve((size_t)n * K * 4 + 16, s);
       slots = ws.slots.as<uint32_t>();
+      if (cfg_.dwithin_arena == 1 || (cfg_.dwithin_arena == 2 && order == nullptr)) {
+        // 16 B cursor, n heads, then chunks of the slots' size in total
+        const uint64_t chunks =
+            std::max<uint64_t>(1024, (uint64_t)n * K / kArenaChunkWords);
+        const size_t head_bytes = ((size_t)n * 4 + 127) & ~(size_t)127;
+        ws.arena.reserve(128 + head_bytes + chunks * kArenaChunkWords * 4, s);
+        uint8_t* base = ws.arena.as<uint8_t>();
+        arena.cursor = reinterpret_cast<unsigned long long*>(base);
+        arena.head = reinterpret_cast<uint32_t*>(base + 128);
+        arena.words = reinterpret_cast<uint32_t*>(base + 128 + head_bytes);
+        arena.chunks = (uint32_t)std::min<uint64_t>(chunks, 0xFFFFFFF0ull);
+        SPJ_CUDA(cudaMemsetAsync(arena.cursor, 0, 8, s));
+      }
     }
     dwithin_count(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.counts.as<uint32_t>(),
-                  ws.status.as<DeviceStatus>(), s, slots, K);
+                  ws.status.as<DeviceStatus>(), s, slots, K, arena);
     scan_u32_u64(ws.psc.counts.as<uint32_t>(), ws.psc.offsets.as<uint64_t>(), n, ws.psc.tmp, s);
     uint64_t total = 0;
     DeviceStatus hst;
@@ -213,8 +229,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     ws.out_probe.reserve((total + 1) * 4, s);
     dwithin_scatter(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.offsets.as<uint64_t>(),
                     probe_base, ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), total,
-                    s, ws.psc.counts.as<uint32_t>(), slots, K);
-    launches += 5;
+                    s, ws.psc.counts.as<uint32_t>(), slots, K, arena);
+    launches += 5 + (arena.words ? 1 : 0);
     if (prof) {
       SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
       SPJ_CUDA(cudaEventRecord(ws.ev[4], s));

@@ -33,6 +33,14 @@ struct EngineConfig {
   bool fuse_dwithin = true;
   // fused ST_DWithin: build ids kept per probe by the counting pass (0 = none)
   uint32_t dwithin_slots = 64;
+  // fused ST_DWithin: results past the slots go to an overflow arena of the
+  // slots' size, so the scatter pass traverses only the probes the arena
+  // could not hold (the 24 % of 20M GMM probes with over 64 neighbours hold
+  // 80 % of the pairs).  0 off, 1 on, 2 auto: on when the probes are not in
+  // Morton order.  20M x 1M GMM points: in row order 297 -> 139 ms per step;
+  // in Morton order the counting pass slowed from 38 to 103 ms with it (the
+  // scatter pass fell from 33 to 9 ms), so auto leaves it off there
+  int dwithin_arena = 2;
   // refine order of the candidates: 0 as listed (by probe row), 1 the probes'
   // Morton order, 2 by build row then probe Morton rank (a warp then tests
   // one build geometry's edges against neighbouring probes: shared loads and
@@ -97,6 +105,7 @@ struct Workspace {
   ProbeScratch psc;
   DevBuf boxes_tmp, cand_build, cand_probe, flags, pos, out_build, out_probe, scan_tmp, status;
   DevBuf slots;   // fused ST_DWithin result slots
+  DevBuf arena;   // fused ST_DWithin overflow arena: cursor, heads, chunks
   DevBuf rqueue;  // pairs left open by the refine's cheap pass, then its count
   DevBuf wkb_data, wkb_offsets, wkb_validity;  // H2D staging of host columns
   cudaEvent_t ev[6] = {};

@@ -153,21 +153,26 @@ def test_dwithin_fused_same_output(capi, oracle_mod, order):
     from sedona_gpuspatial import datagen, wkb
     inp = datagen.workload4(n_probe=20000, n_build=20000)
     out = {}
-    # (fuse_dwithin, dwithin_slots): result slots of the counting pass, with
-    # few slots most probes are traversed again by the scatter pass
-    variants = [(0, 64), (1, 64), (1, 4), (1, 0)]
+    # (fuse_dwithin, dwithin_slots, dwithin_arena): result slots of the
+    # counting pass and its overflow arena (of the slots' size, at least 1024
+    # chunks); with few slots the arena runs out and the probes it could not
+    # hold are traversed again by the scatter pass, without it every probe
+    # past its slots is
+    variants = [(0, 64, 1), (1, 64, 1), (1, 64, 0), (1, 4, 1), (1, 1, 1), (1, 4, 0), (1, 0, 1),
+                (1, 64, 2)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=order)
         j.set_option("fuse_dwithin", v[0])
         j.set_option("dwithin_slots", v[1])
+        j.set_option("dwithin_arena", v[2])
         j.build(inp.build)
         out[v] = j.probe(inp.probe, "dwithin", distance=250.0)
         assert j.stats()["kernel_launches"] > 0
     for v in variants[1:]:
         np.testing.assert_array_equal(out[v][0], out[variants[0]][0])
         np.testing.assert_array_equal(out[v][1], out[variants[0]][1])
-    assert pairs(*out[(1, 64)]) == oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin",
-                                                250.0)
+    assert pairs(*out[(1, 64, 1)]) == oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin",
+                                                   250.0)
     bx = np.array([0, 3, 5, 8, 20, 7, 24], dtype=np.float64)
     by = np.array([0, 4, 12, 15, 21, 24, 7], dtype=np.float64)
     build = wkb.points_column(bx, by)
