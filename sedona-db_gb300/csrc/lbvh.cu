@@ -380,17 +380,40 @@ __global__ void k_gather_counts(const uint32_t* __restrict__ order,
     out[j] = counts[order[j]];
 }
 
-// perm[opos[j] + c] = offs[order[j]] + c for c < counts[order[j]]
+// perm[opos[j] + c] = offs[order[j]] + c for c < counts[order[j]].  A warp
+// takes 32 consecutive positions j, and its lanes write consecutive perm
+// entries (each finds its position by a binary search over the 32 run
+// starts), so the stores are coalesced.
 __global__ void k_cand_perm(const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
                             const uint64_t* __restrict__ offs, const uint64_t* __restrict__ opos,
                             uint32_t n, uint64_t m, uint32_t* __restrict__ perm) {
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    const uint32_t pi = order[j];
-    if (pi >= n) continue;
-    const uint64_t src = offs[pi], dst = opos[j];
-    const uint32_t c = counts[pi];
-    for (uint32_t t = 0; t < c; t++)
-      if (dst + t < m && src + t < m) perm[dst + t] = (uint32_t)(src + t);
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n; w += nw) {
+    const uint64_t j = w * 32 + lane;
+    const uint32_t pi = j < n ? order[j] : 0xFFFFFFFFu;
+    const bool ok = pi < n;
+    // this lane's run: [st, st + c) of perm, taken from offs[pi]
+    const uint64_t st = j < n ? opos[j] : ~0ull;
+    const uint64_t src0 = ok ? offs[pi] : 0;
+    const uint32_t c = ok ? counts[pi] : 0;
+    const uint64_t jend = w * 32 + 32 < n ? w * 32 + 32 : n;
+    const uint64_t e0 = __shfl_sync(0xffffffffu, st, 0);
+    const uint64_t e1 = opos[jend];
+    for (uint64_t base = e0; base < e1; base += 32) {
+      const uint64_t e = base + lane;
+      int L = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint64_t sL = __shfl_sync(0xffffffffu, st, L + step);
+        if (sL <= e) L += step;
+      }
+      const uint64_t sr = __shfl_sync(0xffffffffu, st, L);
+      const uint64_t src = __shfl_sync(0xffffffffu, src0, L) + (e - sr);
+      const uint32_t cl = __shfl_sync(0xffffffffu, c, L);
+      const bool okl = __shfl_sync(0xffffffffu, ok ? 1 : 0, L) != 0;
+      if (e < e1 && okl && e - sr < cl && e < m && src < m) perm[e] = (uint32_t)src;
+    }
   }
 }
 
