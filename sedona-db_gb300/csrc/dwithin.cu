@@ -121,6 +121,10 @@ __global__ void __launch_bounds__(kTravThreads)
                     uint64_t cap, DeviceStatus* st, uint32_t* __restrict__ slots, uint32_t K,
                     DwithinArena A) {
   __shared__ int stack[kTravStack * kTravThreads];
+  // staged output runs: the scatter pass's pair run, the counting pass's
+  // slot row (rows of K ids, so with K a multiple of kRunBuf its groups are
+  // whole sectors)
+  __shared__ uint32_t runbuf[kRunBuf * kTravThreads];
   const uint64_t max_steps = 2ull * t.nleaves + 2;
   uint32_t esc = 0, tested = 0;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
@@ -139,6 +143,10 @@ __global__ void __launch_bounds__(kTravThreads)
     uint32_t a_cur = kArenaEnd, a_first = kArenaEnd, a_fill = 0;
     bool a_failed = false;
     uint64_t pos = kScatter ? offs[pi] : 0;
+    // counting pass: the slot row [pi K, pi K + K)
+    uint64_t spos = (uint64_t)pi * K;
+    const uint64_t send = spos + K;
+    int staged = 0;
     if (q.x <= q.z && q.y <= q.w && t.nprims > 0) {
       const double2 p = probe_pt[pi];
       const bool split =
@@ -174,10 +182,9 @@ __global__ void __launch_bounds__(kTravThreads)
             tested += b1 - b0;
             for (uint32_t k = b0; k < b1; k++) {
               if (kScatter) {
-                if (pos < cap) out_build[pos] = t.sorted_id[k];
-                pos++;
+                run_put(out_build, cap, runbuf, pos, staged, t.sorted_id[k]);
               } else {
-                if (cnt < K) slots[(size_t)pi * K + cnt] = t.sorted_id[k];
+                if (cnt < K) run_put(slots, send, runbuf, spos, staged, t.sorted_id[k]);
                 else if (kArena) arena_put(A, t.sorted_id[k], a_cur, a_first, a_fill, a_failed);
                 cnt++;
               }
@@ -204,10 +211,10 @@ __global__ void __launch_bounds__(kTravThreads)
             }
             if (r) {
               if (kScatter) {
-                if (pos < cap) out_build[pos] = t.sorted_id[k];  // probe ids: fill_probe_ids
-                pos++;
+                // (probe ids: fill_probe_ids)
+                run_put(out_build, cap, runbuf, pos, staged, t.sorted_id[k]);
               } else {
-                if (cnt < K) slots[(size_t)pi * K + cnt] = t.sorted_id[k];
+                if (cnt < K) run_put(slots, send, runbuf, spos, staged, t.sorted_id[k]);
                 else if (kArena) arena_put(A, t.sorted_id[k], a_cur, a_first, a_fill, a_failed);
                 cnt++;
               }
@@ -241,6 +248,8 @@ __global__ void __launch_bounds__(kTravThreads)
         node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
       }
     }
+    if (staged) run_flush(kScatter ? out_build : slots, kScatter ? cap : send, runbuf,
+                          kScatter ? pos : spos, staged);
     if (!kScatter) {
       counts[pi] = cnt;
       if (kArena) {

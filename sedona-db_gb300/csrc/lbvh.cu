@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(kTravThreads)
   // per-thread stack in shared memory, [depth][thread] so a warp's pushes hit
   // 32 distinct banks
   __shared__ int stack[kTravStack * kTravThreads];
+  __shared__ uint32_t runbuf[kScatter ? kRunBuf * kTravThreads : 1];
   // a traversal visits each node at most once: 2 * nleaves steps bound it
   const uint64_t max_steps = 2ull * t.nleaves + 2;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nprobe;
@@ -209,6 +210,7 @@ __global__ void __launch_bounds__(kTravThreads)
     const float4 q = probe_box[pi];
     uint32_t cnt = 0;
     uint64_t pos = kScatter ? offs[pi] : 0;
+    int staged = 0;  // build ids staged in runbuf (scatter pass)
     if (box_valid(q) && t.nprims > 0) {
       int sp = 0;
       int node = t.nleaves > 1 ? 0 : ~0;  // root: internal node 0, or the single leaf
@@ -229,11 +231,9 @@ __global__ void __launch_bounds__(kTravThreads)
           for (uint32_t k = b0; k < b1; k++) {
             if (box_overlap(t.sorted_box[k], q)) {
               if (kScatter) {
-                if (pos < cap) {  // writes bounded by the output capacity
-                  out_build[pos] = t.sorted_id[k];
-                  if (out_probe) out_probe[pos] = (uint32_t)pi + probe_base;
-                }
-                pos++;
+                // writes bounded by the output capacity
+                if (out_probe && pos < cap) out_probe[pos] = (uint32_t)pi + probe_base;
+                run_put(out_build, cap, runbuf, pos, staged, t.sorted_id[k]);
               } else {
                 cnt++;
               }
@@ -267,6 +267,7 @@ __global__ void __launch_bounds__(kTravThreads)
         node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
       }
     }
+    if (kScatter && staged) run_flush(out_build, cap, runbuf, pos, staged);
     if (!kScatter) counts[pi] = cnt;
   }
 }

@@ -69,6 +69,43 @@ __device__ __forceinline__ bool box_overlap(float4 a, float4 b) {
   return !(a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y);
 }
 
+// Staging of one thread's output run (a traversal writes its results to
+// consecutive slots).  Ids collect in shared memory, laid out [slot][thread]
+// over kTravThreads threads, and go out when the next destination reaches a
+// multiple of kRunBuf: after a first partial group every group fills one
+// 32-byte sector, written as two 16-byte stores (when the buffer allows).
+// A traversal's lanes otherwise store 4 bytes at a time to 32 places.
+constexpr int kRunBuf = 8;
+
+__device__ __forceinline__ void run_flush(uint32_t* __restrict__ out, uint64_t cap,
+                                          const uint32_t* sm, uint64_t end, int n) {
+  const uint64_t start = end - (uint64_t)n;
+  const int tid = threadIdx.x;
+  if (n == kRunBuf && (start & (kRunBuf - 1)) == 0 && end <= cap &&
+      (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    uint4* o = reinterpret_cast<uint4*>(out + start);
+    o[0] = make_uint4(sm[0 * kTravThreads + tid], sm[1 * kTravThreads + tid],
+                      sm[2 * kTravThreads + tid], sm[3 * kTravThreads + tid]);
+    o[1] = make_uint4(sm[4 * kTravThreads + tid], sm[5 * kTravThreads + tid],
+                      sm[6 * kTravThreads + tid], sm[7 * kTravThreads + tid]);
+  } else {
+    for (int i = 0; i < n; i++)
+      if (start + i < cap) out[start + i] = sm[i * kTravThreads + tid];
+  }
+}
+
+// Appends id at out[pos] (pos advances); n ids are staged.
+__device__ __forceinline__ void run_put(uint32_t* __restrict__ out, uint64_t cap, uint32_t* sm,
+                                        uint64_t& pos, int& n, uint32_t id) {
+  sm[n * kTravThreads + threadIdx.x] = id;
+  n++;
+  pos++;
+  if ((pos & (kRunBuf - 1)) == 0 || n == kRunBuf) {
+    run_flush(out, cap, sm, pos, n);
+    n = 0;
+  }
+}
+
 }  // namespace
 
 // Builds the LBVH over boxes[0..n); NaN / inverted boxes are left out.
