@@ -106,8 +106,10 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *                       relation predicates in two passes (a cheap pass over
  *                       all pairs queues the pairs it leaves open for a full
  *                       pass)
- *   "host_slices"       0 (default: auto), 1 (one call), 2-64: row slices of
- *                       SpjJoinProbeHost (see there)
+ *   "refine_split_group" 0 (default), 4, 8, 16: lanes per queued pair in the
+ *                       second pass of the split refine
+ *   "host_slices"       0 (default: auto, 2 from 524,288 rows), 1 (one
+ *                       call), 2-64: row slices of SpjJoinProbeHost
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
@@ -148,10 +150,10 @@ int SpjJoinProbeDevice(SpjJoin* join, const struct SpjDeviceWkb* column, int32_t
  * Arrow binary array); results are copied into caller buffers of capacity
  * `capacity` pairs.  *n_pairs receives the full count; if it exceeds
  * capacity ENOSPC is returned and the buffers' contents are unspecified.
- * A column of 524,288 rows or more is probed in row slices (about 48 MB of
- * WKB each, at most 8) by two host threads on two workspaces, so that two
- * slices' kernels and the copies of their neighbours are in flight at once;
- * the pairs and their order are those of one call over the whole column.  Page-locked buffers
+ * A column of 524,288 rows or more is probed in two row slices (option
+ * "host_slices" sets another count) by two host threads on two workspaces,
+ * so that both slices' kernels and each slice's copies overlap; the pairs
+ * and their order are those of one call over the whole column.  Page-locked buffers
  * (cudaHostAlloc / cudaHostRegister) let those copies run asynchronously. */
 int SpjJoinProbeHost(SpjJoin* join, int64_t length, const void* offsets,
                      int32_t offsets_are_64bit, const uint8_t* data, const uint8_t* validity,

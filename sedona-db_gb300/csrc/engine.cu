@@ -323,8 +323,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   else
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb, cfg_.refine_group, rq,
-                    rqn);
+                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb,
+                    rq ? cfg_.refine_split_group : cfg_.refine_group, rq, rqn);
   launches += rq ? 2 : 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 

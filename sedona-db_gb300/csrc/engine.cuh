@@ -70,8 +70,12 @@ struct EngineConfig {
   // warp's pairs already share one build geometry (2M x 50k polygons: 59.0
   // ms one pass vs 61.0 split in build-major order; 78.0 vs 63.3 as listed)
   int refine_split = 2;
-  // host probes (SpjJoinProbeHost): 0 auto (slices of about 48 MB of WKB
-  // from 524,288 rows up, at most 8), 1 one call, n > 1 that many slices
+  // lanes per queued pair in the split refine's second pass (0, 4, 8, 16);
+  // 2M x 50k polygons with the split: 57.1 ms with one lane per pair, 67.6
+  // with 4, 69.4 with 8
+  int refine_split_group = 0;
+  // host probes (SpjJoinProbeHost): 0 auto (2 slices from 524,288 rows up),
+  // 1 one call, n > 1 that many slices
   int host_slices = 0;
 };
 constexpr uint32_t kOrderMinRows = 1u << 16;

@@ -87,12 +87,12 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
   if (m == 0) return;
   const RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
                        flags, st,    m_dev, perm, queue, qn,         s};
-  if (form == kFastF32 && perm == nullptr && (group == 4 || group == 8 || group == 16)) {
-    launch_refine_group(a, group, min_blocks);
+  if (form == kFastF32 && queue && qn && (min_blocks == 4 || min_blocks == 6)) {
+    launch_refine_split(a, min_blocks, group);
     return;
   }
-  if (form == kFastF32 && queue && qn && (min_blocks == 4 || min_blocks == 6)) {
-    launch_refine_split(a, min_blocks);
+  if (form == kFastF32 && perm == nullptr && (group == 4 || group == 8 || group == 16)) {
+    launch_refine_group(a, group, min_blocks);
     return;
   }
   if (form == kFastF32 && min_blocks != 4 && min_blocks >= 2 && min_blocks <= 6) {

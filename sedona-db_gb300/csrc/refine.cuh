@@ -34,9 +34,10 @@ enum RefineForm : int {
 // fewer registers, more warps to hide the latency of divergent pairs.
 // group (4, 8 or 16; FP32 form, no perm) evaluates each pair with that many
 // cooperating lanes splitting the ring loops; 0 keeps one lane per pair.
-// queue (m entries) and qn (one device word) split the FP32 refine (group 0,
-// min_blocks 4 or 6) into a cheap pass over all pairs that queues the pairs
-// it cannot decide, then a full pass over the queue; same flags.
+// queue (m entries) and qn (one device word) split the FP32 refine (min_blocks
+// 4 or 6) into a cheap pass over all pairs that queues the pairs it cannot
+// decide, then a full pass over the queue (with `group` lanes per queued
+// pair when group is 4, 8 or 16); same flags.
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,

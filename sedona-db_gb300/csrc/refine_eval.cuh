@@ -338,12 +338,15 @@ __global__ void __launch_bounds__(256, kMinBlocks)
 // (grid-stride over candidates per group); the group's leader writes the
 // flag.  Same contract as k_refine (m_dev: device-side count, flags past it
 // cleared).
-template <int kG, int kMinBlocks>
+template <int kG, int kMinBlocks, bool kQueue = false>
 __global__ void __launch_bounds__(256, kMinBlocks)
     k_refine_group(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
                    const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base,
                    int predicate, uint8_t* __restrict__ flags, DeviceStatus* st,
-                   const uint64_t* __restrict__ m_dev) {
+                   const uint64_t* __restrict__ m_dev, const uint32_t* __restrict__ queue = nullptr,
+                   const uint32_t* __restrict__ qn = nullptr) {
+  // kQueue: the groups take the candidates queue[0, *qn) (the second pass of
+  // the split refine); flags of other candidates are left alone
   uint32_t esc = 0, pairs = 0;
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kG - 1);
@@ -351,9 +354,11 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kG;
   const uint64_t ng = ((uint64_t)gridDim.x * blockDim.x) / kG;
   const uint64_t mm = m_dev ? min(*m_dev, m) : m;
-  for (uint64_t k = gid; k < m; k += ng) {
+  const uint64_t nu = kQueue ? min((uint64_t)*qn, m) : m;
+  for (uint64_t u = gid; u < nu; u += ng) {
+    const uint64_t k = kQueue ? (uint64_t)queue[u] : u;
     if (k >= mm) {
-      if (gl == 0) flags[k] = 0;
+      if (!kQueue && gl == 0 && k < m) flags[k] = 0;
       continue;
     }
     const uint32_t b = cb[k], p = cp[k] - probe_base;
@@ -387,8 +392,9 @@ struct RefineLaunch {
   cudaStream_t s;
 };
 // refine_split.cu: the cheap pass then the full pass over its queue
-// (min_blocks 4 or 6)
-void launch_refine_split(const RefineLaunch& a, int min_blocks);
+// (min_blocks 4 or 6); group (4, 8, 16) runs the full pass with that many
+// lanes per queued pair, 0 with one
+void launch_refine_split(const RefineLaunch& a, int min_blocks, int group = 0);
 // refine_group.cu: kG lanes per pair (group 4, 8 or 16)
 void launch_refine_group(const RefineLaunch& a, int group, int min_blocks);
 // refine_blocks.cu: one pass, FP32 form built for min_blocks 2, 3, 5 or 6

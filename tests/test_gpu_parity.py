@@ -202,7 +202,8 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     variants = [(-1, 0, 4, 0, 0, 0), (1, 1, 2, 0, 1, 1), (1, 2, 6, 0, 1, 0), (1, 0, 4, 8, 1, 1),
                 (1, 2, 2, 4, 0, 1), (-1, 2, 4, 16, 1, 1), (1, 3, 0, 0, 1, 1),
                 (0, 2, 0, 0, 1, 1), (-1, 0, 4, 0, 1, 1), (1, 2, 6, 0, 0, 1), (1, 3, 0, 0, 1, 2),
-                (-1, 0, 0, 0, 1, 2), (1, 4, 0, 0, 1, 2), (-1, 4, 4, 0, 0, 1)]
+                (-1, 0, 0, 0, 1, 2), (1, 4, 0, 0, 1, 2), (-1, 4, 4, 0, 0, 1),
+                (1, 3, 6, 0, 1, 1, 8), (-1, 0, 4, 0, 1, 1, 4), (1, 2, 0, 0, 0, 1, 16)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
@@ -210,6 +211,8 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
         j.set_option("refine_group", v[3])
         j.set_option("cell_grid", v[4])
         j.set_option("refine_split", v[5])
+        if len(v) > 6:
+            j.set_option("refine_split_group", v[6])
         j.build(inp.build)
         out[v] = j.probe(inp.probe, pred, distance=d)
     for v in variants[1:]:
