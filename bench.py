@@ -664,6 +664,54 @@ def run_learned(args, world, rank, local, pg):
     launches = int(after["kernel_launches"] - before["kernel_launches"])
     steps_per_lookup = (after["search_steps"] - before["search_steps"]) / max(1, lookups_n)
 
+    # e2e: every step copies both probe columns (offsets + WKB) from pinned
+    # host memory into their device buffers, queries, and copies the pairs
+    # into pinned host memory, all on the index's stream (stream order keeps
+    # a column's pair copies ahead of the next query, which reuses the
+    # index's output buffers)
+    host_parts = []
+    for k in (kbox, klk):
+        host_parts.append([torch.empty(t.numel() * t.element_size(), dtype=torch.uint8,
+                                       pin_memory=True).view(t.dtype) for t in k])
+        for h_, t_ in zip(host_parts[-1], k):
+            h_.copy_(t_.cpu())
+    h2d = sum(t.numel() * t.element_size() for k in (kbox, klk) for t in k)
+    cap = int(npairs * 1.01) + 16
+    hb = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+    hpr = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+
+    def e2e_step():
+        n = 0
+        for d, hps, k in zip((dbox, dlk), host_parts, (kbox, klk)):
+            with torch.cuda.stream(stream):
+                for h, t in zip(hps, k):
+                    t.copy_(h, non_blocking=True)
+            dbp, dpp, m = li.query_device(d, "intersects")
+            if m:
+                with torch.cuda.stream(stream):
+                    hb[n:n + m].copy_(dev_i32(dbp, m), non_blocking=True)
+                    hpr[n:n + m].copy_(dev_i32(dpp, m), non_blocking=True)
+            n += m
+        return n
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    for _ in range(args.steps):
+        n_e2e = e2e_step()
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = barrier_max(pg, e0.elapsed_time(e1) / args.steps, dev)
+    assert n_e2e == npairs, (n_e2e, npairs)
+    # torch's pinned allocator records an event on the stream a pinned block
+    # was copied on when the block is freed: free them while the index (and
+    # its stream) still exists
+    del host_parts, hb, hpr, h_, t_
+    torch.cuda.synchronize()
+
     # ablation: the untrained model (line through each leaf's end keys)
     li.set_trained(False)
     st_untrained = li.stats()
@@ -746,6 +794,9 @@ def run_learned(args, world, rank, local, pg):
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
                      "algorithmic_bytes_per_launch": alg},
         "gpu_launches": launches,
+        "e2e": {"value": npairs * world / (e2e_ms * 1e-3), "unit": "pairs/s",
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(8 * npairs)},
         "clocks": sampler.summary(),
     }
     return out, None
