@@ -252,6 +252,11 @@ __device__ __forceinline__ float grid_edge(float o, float step, int k) {
   return __fadd_rn(o, __fmul_rn((float)k, step));
 }
 
+// v32 strictly inside (a, b).
+__device__ __forceinline__ bool p_inside_open(float v32, float a, float b) {
+  return v32 > a && v32 < b;
+}
+
 // Index of a closed cell [edge(i), edge(i+1)] containing the FP64 coordinate
 // v, or -1 when v lies outside the grid.  The f32 estimate is corrected
 // against the exact boundary values.
@@ -264,17 +269,40 @@ __device__ __forceinline__ int grid_index(float o, float step, int n, double v) 
   return i;
 }
 
+// The same index from v's round-to-nearest copy v32, in FP32 alone when that
+// settles it.  A strict f32 comparison of RN values proves the exact one
+// (RN is monotone), so v32 strictly between two edges puts v strictly inside
+// that cell, and v32 strictly outside the first / last edge puts v outside
+// the grid.  Only a v32 equal to an edge (v within half an f32 ulp of it)
+// takes the FP64 lookup.
+__device__ __forceinline__ int grid_index32(float o, float step, int n, float v32, double v) {
+  const float e0 = grid_edge(o, step, 0), en = grid_edge(o, step, n);
+  if (p_inside_open(v32, e0, en)) {
+    int i = (int)floorf(__fdiv_rn(__fsub_rn(v32, o), step));
+    i = i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+    while (i > 0 && v32 < grid_edge(o, step, i)) i--;
+    while (i < n - 1 && v32 > grid_edge(o, step, i + 1)) i++;
+    if (v32 > grid_edge(o, step, i) && v32 < grid_edge(o, step, i + 1)) return i;
+  } else if (v32 < e0 || v32 > en || v32 != v32) {
+    return -1;
+  }
+  return grid_index(o, step, n, v);
+}
+
 // Status of the grid cell holding p (0 mixed / no grid, 1 inside, 2 outside).
 // A clean cell is touched by no edge, so every point of it has the ring's
 // status there, on tg's arithmetic as well (the argument of the isolation
-// exit in ring_intersects_ring).
-__device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r, double2 p) {
+// exit in ring_intersects_ring).  p32 is p rounded to nearest.
+__device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r, double2 p,
+                                                 float2 p32) {
   if (G.grid_meta == nullptr) return 0;
   const uint2 m = G.grid_meta[r];
   if (m.y == 0) return 0;
   const float4 q = G.grid_rect[r];
-  const int i = grid_index(q.x, q.z, (int)m.y, p.x), j = grid_index(q.y, q.w, (int)m.y, p.y);
-  if (i < 0 || j < 0) return 0;
+  const int i = grid_index32(q.x, q.z, (int)m.y, p32.x, p.x);
+  if (i < 0) return 0;
+  const int j = grid_index32(q.y, q.w, (int)m.y, p32.y, p.y);
+  if (j < 0) return 0;
   return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
 }
 
@@ -311,7 +339,7 @@ __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r,
   RingHit h{false, -1};
   if (!ring_rect_covers(G, r, p, p32)) return h;
   if (use_grid) {
-    const int st = grid_point_status(G, r, p);
+    const int st = grid_point_status(G, r, p, p32);
     if (st != 0) {  // clean cell: not on any edge, status known
       h.hit = st == 1;
       return h;
