@@ -20,6 +20,9 @@ struct LearnedView {
   const uint32_t* start;  // L + 1
   const double* a;
   const double* b;
+  // per leaf (a, b - start) in FP32: the query-time prediction of the
+  // position inside the leaf (the window search verifies its answer)
+  const float2* ab32;
   const uint32_t* kc;
   const uint32_t* err;
   const uint16_t* root_tab;  // root_p + 1 entries: leaves whose first key's prefix < p
@@ -111,13 +114,26 @@ __device__ __forceinline__ uint32_t learned_lower_bound(const LearnedView& v, ui
   if (bad) return 0;
   // the answer lies in [start_l, start_{l+1}] (the first key of leaf l is
   // < q unless l == 0, and leaf l+1's first key is >= q)
-  const double s_lo = (double)v.start[l];
-  const double s_hi = fmin((double)v.start[l + 1] + 1.0, (double)v.n);
-  const double pred = __fma_rn(v.a[l], (double)q - (double)v.kc[l], v.b[l]);
-  double lo_d = fmax(floor(pred) - (double)e - 1.0, s_lo);
-  double hi_d = fmin(ceil(pred) + (double)e + 2.0, s_hi);
-  if (!(hi_d >= lo_d)) hi_d = lo_d;  // also catches NaN
-  uint32_t lo = (uint32_t)lo_d, hi = (uint32_t)hi_d;
+  const uint32_t s_lo = v.start[l];
+  const uint32_t s_hi = min(v.start[l + 1] + 1u, v.n);
+  // The window around the prediction, relative to the leaf start, in FP32:
+  // e was measured on the FP64 line, and the FP32 line (a leaf-local
+  // intercept, so the values stay within the leaf's size) differs from it
+  // by far less than one position, covered by two more on each side.  GB300's
+  // FP64 rate made the FP64 form the range phase's busiest pipe.  The window
+  // is verified below either way.
+  const float2 ab = v.ab32[l];
+  const float predl =
+      __fmaf_rn(ab.x, (float)((int64_t)q - (int64_t)v.kc[l]), ab.y);
+  const float span = (float)(s_hi - s_lo);
+  uint32_t lo = s_lo, hi = s_hi;
+  if (isfinite(predl)) {
+    const float flo = floorf(predl) - (float)e - 3.0f;
+    const float fhi = ceilf(predl) + (float)e + 4.0f;
+    if (flo > 0.0f) lo = s_lo + (uint32_t)fminf(flo, span);
+    if (fhi < span) hi = s_lo + (uint32_t)fmaxf(fhi, 0.0f);
+  }
+  if (hi < lo) hi = lo;
   uint32_t p = bsearch_first_ge(v.keys, lo, hi, q, steps);
   const bool ok_lo = p == 0 || v.keys[p - 1] < q;
   const bool ok_hi = p == v.n || v.keys[p] >= q;
@@ -125,7 +141,7 @@ __device__ __forceinline__ uint32_t learned_lower_bound(const LearnedView& v, ui
     // outside the measured error (q between keys at a leaf edge): the
     // leaf's whole range, then (never needed by construction) everything
     misses++;
-    p = bsearch_first_ge(v.keys, (uint32_t)s_lo, (uint32_t)s_hi, q, steps);
+    p = bsearch_first_ge(v.keys, s_lo, s_hi, q, steps);
     if (!((p == 0 || v.keys[p - 1] < q) && (p == v.n || v.keys[p] >= q)))
       p = bsearch_first_ge(v.keys, 0, v.n, q, steps);
   }
@@ -292,6 +308,15 @@ __global__ void __launch_bounds__(kLeafThreads)
     m = fmax(m, sm[0]);
     err[l] = m > 4.0e9 ? 0xFFFFFFFFu : (uint32_t)ceil(m);
   }
+}
+
+// The query-time FP32 copy of each leaf's line: slope, and the intercept
+// relative to the leaf's first position.
+__global__ void k_leaf_ab32(uint32_t L, const double* __restrict__ a, const double* __restrict__ b,
+                            const uint32_t* __restrict__ start, float2* __restrict__ out) {
+  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x)
+    out[l] = make_float2(__double2float_rn(a[l]),
+                         __double2float_rn(__dsub_rn(b[l], (double)start[l])));
 }
 
 // --- queries --------------------------------------------------------------
@@ -690,7 +715,8 @@ void LearnedIndex::set_windows(uint32_t window, uint32_t window_box) {
 static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevBuf& keys,
                              const DevBuf& ids, const DevBuf& xy, const DevBuf& xy32,
                              const DevBuf& start, const DevBuf& a, const DevBuf& b,
-                             const DevBuf& kc, const DevBuf& err, const DevBuf& root_tab,
+                             const DevBuf& ab32, const DevBuf& kc, const DevBuf& err,
+                             const DevBuf& root_tab,
                              uint32_t root_shift, uint32_t root_p, uint32_t k0, float x0,
                              float y0, float sx, float sy) {
   LearnedView v;
@@ -705,6 +731,7 @@ static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevB
   v.start = start.as<uint32_t>();
   v.a = a.as<double>();
   v.b = b.as<double>();
+  v.ab32 = ab32.as<float2>();
   v.kc = kc.as<uint32_t>();
   v.err = err.as<uint32_t>();
   v.root_tab = root_tab.as<uint16_t>();
@@ -719,8 +746,8 @@ static LearnedView make_view(uint32_t n, uint32_t L, uint32_t window, const DevB
 }
 
 #define SPJ_LVIEW()                                                                           \
-  make_view(n_, L_, window_, keys_, ids_, xy_, xy32_, leaf_start_, leaf_a_, leaf_b_, leaf_kc_, \
-            leaf_err_, root_tab_, root_shift_, root_p_, k0_, x0_, y0_, sx_, sy_)
+  make_view(n_, L_, window_, keys_, ids_, xy_, xy32_, leaf_start_, leaf_a_, leaf_b_, leaf_ab32_, \
+            leaf_kc_, leaf_err_, root_tab_, root_shift_, root_p_, k0_, x0_, y0_, sx_, sy_)
 
 void LearnedIndex::build(const DeviceGeoms& pts, const Lbvh& bvh, cudaStream_t s) {
   bv_ = pts.view();
@@ -847,6 +874,10 @@ void LearnedIndex::measure_errors(cudaStream_t s) {
   k_leaf_err<<<L_, kLeafThreads, 0, s>>>(keys_.as<uint32_t>(), leaf_start_.as<uint32_t>(),
                                          leaf_kc_.as<uint32_t>(), leaf_a_.as<double>(),
                                          leaf_b_.as<double>(), leaf_err_.as<uint32_t>());
+  leaf_ab32_.reserve(((size_t)L_ + 1) * sizeof(float2), s);
+  k_leaf_ab32<<<grid_for(L_, 256), 256, 0, s>>>(L_, leaf_a_.as<double>(), leaf_b_.as<double>(),
+                                                leaf_start_.as<uint32_t>(),
+                                                leaf_ab32_.as<float2>());
   std::vector<uint32_t> e(L_), st(L_ + 1);
   SPJ_CUDA(cudaMemcpyAsync(e.data(), leaf_err_.get(), (size_t)L_ * 4, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaMemcpyAsync(st.data(), leaf_start_.get(), ((size_t)L_ + 1) * 4,

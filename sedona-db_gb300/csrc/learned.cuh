@@ -81,7 +81,7 @@ class LearnedIndex {
   GeomsView bv_;
   LbvhView tv_;
   DevBuf keys_, ids_, xy_, xy32_;  // sorted by key
-  DevBuf leaf_start_, leaf_a_, leaf_b_, leaf_kc_, leaf_err_, counters_, counts_, offs_, tmp_,
+  DevBuf leaf_start_, leaf_a_, leaf_b_, leaf_ab32_, leaf_kc_, leaf_err_, counters_, counts_, offs_, tmp_,
       scratch_;
   DevBuf root_tab_;
   DevBuf order_, okeys_, akeys_, avals_, ranges_, ccount_, coff_;  // query scratch
