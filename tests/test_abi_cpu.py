@@ -87,3 +87,23 @@ def test_struct_layouts_match_reference_abi():
     # 5 u64, 4 u32, 5 f64, u64 ranges, 3 f64, 2 u32 windows, u64 launches
     assert C.sizeof(capi.SpjLearnedStats) == 5 * 8 + 4 * 4 + 5 * 8 + 8 + 3 * 8 + 2 * 4 + 8
     assert C.sizeof(capi.GpuSpatialRefinerConfig) == p + 4 + 1 + 3 + 4 + (4 if p == 8 else 0)
+
+
+def test_option_keys_documented():
+    """Every execution option SpjJoinSetOption accepts is documented in the
+    public header and in the integration guide's options table, and vice
+    versa."""
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = open(os.path.join(root, "sedona-db_gb300", "csrc", "capi.cu")).read()
+    body = src[src.index("SpjJoinSetOption"):]
+    body = body[:body.index("\n}\n")]
+    accepted = set(re.findall(r'k == "([a-z_]+)"', body))
+    hdr = open(os.path.join(root, "include", "spj_gb300.h")).read()
+    block = hdr[hdr.index("Execution options"):hdr.index("int SpjJoinSetOption")]
+    documented = set(re.findall(r'^ \*   "([a-z_]+)"', block, re.M))
+    guide = open(os.path.join(root, "INTEGRATION.md")).read()
+    table = set(re.findall(r"^\| `([a-z_]+)` \|", guide, re.M))
+    assert accepted, "no option keys found"
+    assert accepted == documented, (accepted ^ documented)
+    assert accepted <= table, (accepted - table)
