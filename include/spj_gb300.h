@@ -321,12 +321,24 @@ int SpjKnnGetStats(SpjKnn* knn, uint64_t* queries, uint64_t* exact_evals, uint64
  * call synchronizes it.  The first call on a device looks up the static
  * array's device address (no allocation), so make it before any stream
  * capture.  All calls share the array: calls that overlap on the GPU race
- * and must be serialized by the caller. */
+ * and must be serialized by the caller.  Before anything is launched the call
+ * rejects (EINVAL + message) a d_rects that is not 16-byte aligned (each rect
+ * is read as one 16-byte load), outputs that are not 4-byte aligned, and
+ * buffers that are not device memory of the index's device.  A traversal
+ * fault (a damaged tree) fails the call and stays recorded in the index:
+ * every later probe of that index, through any entry point, fails with the
+ * same message until the index is cleared and built again. */
 int SpjIndexProbeNoAlloc(struct SedonaFloatIndex2D* index, const float* d_rects,
                          uint32_t n_rects, uint32_t* d_out_build, uint32_t* d_out_probe,
                          uint64_t capacity, uint64_t* n_pairs, void* stream);
 
 /* ------------------------------------------------------------------------ */
+
+/* Number of device (and page-locked host) buffers this library has
+ * allocated since it was loaded, summed over all objects and devices.  A
+ * caller can read it before and after a call to see that the call allocated
+ * nothing. */
+uint64_t SpjAllocationCount(void);
 
 int SpjHostRegister(void* ptr, uint64_t bytes);
 int SpjHostUnregister(void* ptr);

@@ -103,6 +103,7 @@ int rt_init(GpuSpatialRuntime* self, GpuSpatialRuntimeConfig* config) {
       if (want > free_b / 10 * 9) want = free_b / 10 * 9;
       void* p = nullptr;
       SPJ_CUDA(cudaMallocAsync(&p, want, 0));
+      g_allocations.fetch_add(1, std::memory_order_relaxed);
       SPJ_CUDA(cudaFreeAsync(p, 0));
       SPJ_CUDA(cudaStreamSynchronize(0));
     }
@@ -1369,3 +1370,11 @@ extern "C" int SpjHostUnregister(void* ptr) {
 }
 
 extern "C" const char* SpjVersion(void) { return "spj-gb300 0.1.0 (sm_103a)"; }
+
+namespace spj {
+std::atomic<uint64_t> g_allocations{0};
+}  // namespace spj
+
+extern "C" uint64_t SpjAllocationCount(void) {
+  return spj::g_allocations.load(std::memory_order_relaxed);
+}

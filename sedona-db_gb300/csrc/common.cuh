@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
@@ -109,6 +110,10 @@ __host__ __device__ __forceinline__ Rect64 make_rect64(double a, double b, doubl
   return r;
 }
 
+// Count of buffers the library has allocated (device and page-locked host),
+// exported as SpjAllocationCount; defined in capi.cu.
+extern std::atomic<uint64_t> g_allocations;
+
 // ---------------------------------------------------------------------------
 // Stream-ordered device buffers (cudaMallocAsync from the device's default
 // pool; the pool's release threshold is raised at runtime init so freed
@@ -140,7 +145,10 @@ class DevBuf {
     release();
     s_ = s;
     n_ = bytes;
-    if (bytes) SPJ_CUDA(cudaMallocAsync(&p_, bytes, s));
+    if (bytes) {
+      SPJ_CUDA(cudaMallocAsync(&p_, bytes, s));
+      g_allocations.fetch_add(1, std::memory_order_relaxed);
+    }
   }
   // grow-only reallocation (contents not preserved)
   void reserve(size_t bytes, cudaStream_t s) {
@@ -176,6 +184,7 @@ class PinnedBuf {
     if (p_) cudaFreeHost(p_);
     p_ = nullptr;
     SPJ_CUDA(cudaMallocHost(&p_, bytes));
+    g_allocations.fetch_add(1, std::memory_order_relaxed);
     n_ = bytes;
   }
   template <class T>

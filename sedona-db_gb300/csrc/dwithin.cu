@@ -229,7 +229,11 @@ __global__ void __launch_bounds__(kTravThreads)
           const int2 ch = t.node_child[node];
           const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
           if (hl && hr) {
-            if (sp < kTravStack) stack[sp * kTravThreads + threadIdx.x] = ch.y;
+            if (sp >= kTravStack) {  // deeper than any tree built here: record, stop
+              traversal_fault(t, kStackOverflow, (unsigned)pi);
+              break;
+            }
+            stack[sp * kTravThreads + threadIdx.x] = ch.y;
             sp++;
             node = ch.x;
             continue;
@@ -245,7 +249,7 @@ __global__ void __launch_bounds__(kTravThreads)
         }
         if (sp == 0) break;
         sp--;
-        node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
+        node = stack[sp * kTravThreads + threadIdx.x];
       }
     }
     if (staged) run_flush(kScatter ? out_build : slots, kScatter ? cap : send, runbuf,

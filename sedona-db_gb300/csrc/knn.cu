@@ -198,7 +198,11 @@ __global__ void __launch_bounds__(kKnnThreads)
         if (vl && vr) {
           const int nearc = dl <= dr ? ch.x : ch.y;
           const int farc = dl <= dr ? ch.y : ch.x;
-          if (sp < kKnnStack) stack[sp * kKnnThreads + threadIdx.x] = farc;
+          if (sp >= kKnnStack) {  // deeper than any tree built here: record, stop
+            traversal_fault(t, kStackOverflow, (unsigned)qi);
+            break;
+          }
+          stack[sp * kKnnThreads + threadIdx.x] = farc;
           sp++;
           node = nearc;
           continue;
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kKnnThreads)
       // visit (the node test re-checks the bound)
       if (sp == 0) break;
       sp--;
-      node = sp < kKnnStack ? stack[sp * kKnnThreads + threadIdx.x] : 0;
+      node = stack[sp * kKnnThreads + threadIdx.x];
     }
     for (uint32_t c = 0; c < k; c++) {
       uint32_t id = 0xFFFFFFFFu;
@@ -345,7 +349,11 @@ __global__ void __launch_bounds__(kKnnThreads)
         if (vl && vr) {
           const int nearc = dl <= dr ? ch.x : ch.y;
           const int farc = dl <= dr ? ch.y : ch.x;
-          if (sp < kKnnStack) stack[sp * kKnnThreads + threadIdx.x] = farc;
+          if (sp >= kKnnStack) {  // deeper than any tree built here: record, stop
+            traversal_fault(t, kStackOverflow, (unsigned)qi);
+            break;
+          }
+          stack[sp * kKnnThreads + threadIdx.x] = farc;
           sp++;
           node = nearc;
           continue;
@@ -361,7 +369,7 @@ __global__ void __launch_bounds__(kKnnThreads)
       }
       if (sp == 0) break;
       sp--;
-      node = sp < kKnnStack ? stack[sp * kKnnThreads + threadIdx.x] : 0;
+      node = stack[sp * kKnnThreads + threadIdx.x];
     }
     // With fewer than k+1 entries the bound never closed, so every build
     // point was visited and listed.  Otherwise the k-set is proven when the

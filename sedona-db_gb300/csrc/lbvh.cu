@@ -248,7 +248,11 @@ __global__ void __launch_bounds__(kTravThreads)
           const int2 ch = t.node_child[node];
           const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
           if (hl && hr) {
-            if (sp < kTravStack) stack[sp * kTravThreads + threadIdx.x] = ch.y;
+            if (sp >= kTravStack) {  // deeper than any tree built here: record, stop
+              traversal_fault(t, kStackOverflow, (unsigned)pi);
+              break;
+            }
+            stack[sp * kTravThreads + threadIdx.x] = ch.y;
             sp++;
             node = ch.x;
             continue;
@@ -264,7 +268,7 @@ __global__ void __launch_bounds__(kTravThreads)
         }
         if (sp == 0) break;
         sp--;
-        node = sp < kTravStack ? stack[sp * kTravThreads + threadIdx.x] : 0;
+        node = stack[sp * kTravThreads + threadIdx.x];
       }
     }
     if (kScatter && staged) run_flush(out_build, cap, runbuf, pos, staged);
@@ -636,8 +640,9 @@ void check_traversal(const LbvhView& t, cudaStream_t s) {
   SPJ_CUDA(cudaMemcpyAsync(f, t.fault, 8, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
   static const char* what[] = {"", "an out-of-range leaf index", "an out-of-range node index",
-                               "an out-of-range probe row", "more steps than the tree has nodes"};
-  SPJ_CHECK(f[0] == 0, std::string("LBVH traversal met ") + what[f[0] < 5 ? f[0] : 0] + " (" +
+                               "an out-of-range probe row", "more steps than the tree has nodes",
+                               "a path deeper than its stack"};
+  SPJ_CHECK(f[0] == 0, std::string("LBVH traversal met ") + what[f[0] < 6 ? f[0] : 0] + " (" +
                            std::to_string(f[1]) + ")");
 }
 

@@ -57,7 +57,13 @@ namespace {
 constexpr int kTravThreads = 128;  // traversal block size
 constexpr int kTravStack = 64;     // per-thread stack depth (Karras depth <= 32 key bits + 32)
 
-enum TraversalFault : unsigned { kBadLeaf = 1, kBadNode = 2, kBadProbe = 3, kTooLong = 4 };
+enum TraversalFault : unsigned {
+  kBadLeaf = 1,
+  kBadNode = 2,
+  kBadProbe = 3,
+  kTooLong = 4,
+  kStackOverflow = 5,
+};
 
 // Records the first out-of-range index a traversal met (the traversal of
 // that probe stops; the host turns the record into an error).

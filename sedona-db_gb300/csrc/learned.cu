@@ -436,7 +436,11 @@ __device__ void leaf_ranges(const LbvhView& t, float4 q, int* stack, uint32_t ro
       const int2 ch = t.node_child[node];
       const bool hl = box_overlap(lb, q), hr = box_overlap(rb, q);
       if (hl && hr) {
-        if (sp < kTravStack) stack[sp * 128] = ch.y;
+        if (sp >= kTravStack) {  // deeper than any tree built here: record, stop
+          traversal_fault(t, kStackOverflow, (unsigned)row);
+          break;
+        }
+        stack[sp * 128] = ch.y;
         sp++;
         node = ch.x;
         continue;
@@ -448,7 +452,7 @@ __device__ void leaf_ranges(const LbvhView& t, float4 q, int* stack, uint32_t ro
     }
     if (sp == 0) break;
     sp--;
-    node = sp < kTravStack ? stack[sp * 128] : 0;
+    node = stack[sp * 128];
   }
 }
 

@@ -24,6 +24,13 @@
 // streams, or different host threads on one device) race on it and must be
 // serialized by the caller.  Nothing in it needs clearing between calls: each
 // call writes every count, offset and tile sum it reads.
+//
+// Pointer checks happen before any launch: d_rects must be 16-byte aligned
+// (one float4 load per rect), the outputs 4-byte aligned, and all three
+// device memory of the index's device.  A traversal fault recorded by either
+// pass fails the call; the fault stays recorded in the index (see
+// SpjIndexProbeNoAlloc in spj_gb300.h), so later probes of that index fail
+// too until it is rebuilt.
 #include <errno.h>
 
 #include <mutex>
@@ -88,7 +95,31 @@ extern "C" int SpjIndexProbeNoAlloc(struct SedonaFloatIndex2D* index, const floa
               "n_rects " + std::to_string(n_rects) + " exceeds the no-allocation maximum of " +
                   std::to_string(kNoAllocMaxProbes) + " probe rects per call");
     SPJ_CHECK(n_rects == 0 || d_rects != nullptr, "null probe rects");
+    // the traversal reads each rect with one 16-byte load and the scatter
+    // writes 4-byte ids: a pointer off those boundaries would fault the
+    // context, so it is rejected here, before anything is launched
+    SPJ_CHECK(reinterpret_cast<uintptr_t>(d_rects) % 16 == 0,
+              "d_rects is not 16-byte aligned (each rect is read as one float4)");
+    SPJ_CHECK(reinterpret_cast<uintptr_t>(d_out_build) % 4 == 0 &&
+                  reinterpret_cast<uintptr_t>(d_out_probe) % 4 == 0,
+              "output buffers are not 4-byte aligned");
     SPJ_CHECK(device >= 0 && device < kMaxDevices, "device id out of range");
+    // the caller's pointers must be device memory that the index's device can
+    // address (cudaPointerGetAttributes allocates nothing)
+    for (const void* ptr : {static_cast<const void*>(d_rects), static_cast<const void*>(d_out_build),
+                            static_cast<const void*>(d_out_probe)}) {
+      if (ptr == nullptr) continue;
+      cudaPointerAttributes a{};
+      if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();  // clear the error the failed query left behind
+        throw spj::Error("a buffer pointer is not known to CUDA");
+      }
+      SPJ_CHECK(a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged,
+                "d_rects and the output buffers must be device (or managed) memory");
+      SPJ_CHECK(a.type == cudaMemoryTypeManaged || a.device == device,
+                "a buffer lives on device " + std::to_string(a.device) +
+                    ", the index on device " + std::to_string(device));
+    }
     static_assert(kCountsBytes + kOffsetsBytes + 4096 <= kNoAllocScratchBytes,
                   "scratch too small");
     SPJ_CUDA(cudaSetDevice(device));
@@ -117,6 +148,8 @@ extern "C" int SpjIndexProbeNoAlloc(struct SedonaFloatIndex2D* index, const floa
     SPJ_CHECK(total == 0 || (d_out_build && d_out_probe), "null output buffers");
     spj::probe_scatter_from(t, boxes, n_rects, offs, 0, d_out_build, d_out_probe, s);
     SPJ_CUDA(cudaStreamSynchronize(s));
+    // a fault recorded by the scatter pass fails the call as well
+    spj::check_traversal(t, s);
     if (err) err->clear();
     return 0;
   } catch (const std::exception& e) {

@@ -101,6 +101,7 @@ int persistent_grid() {
 StreamJoin::StreamJoin(JoinEngine& eng) : eng_(eng) {
   SPJ_CUDA(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
   SPJ_CUDA(cudaMallocHost(&h_tot_, 8 * sizeof(uint64_t)));
+  g_allocations.fetch_add(1, std::memory_order_relaxed);
   SPJ_CUDA(cudaEventCreate(&ev0_));
   SPJ_CUDA(cudaEventCreate(&ev1_));
   ctrl_.alloc(16 + sizeof(DeviceStatus), s_);

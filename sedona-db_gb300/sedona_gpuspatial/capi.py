@@ -157,7 +157,7 @@ EXPORTS = [
     "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
     "SpjKnnStream", "SpjKnnGetStats", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
-    "SpjIndexProbeNoAlloc",
+    "SpjIndexProbeNoAlloc", "SpjAllocationCount",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
     "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
     "SpjStreamCudaStream",

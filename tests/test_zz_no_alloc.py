@@ -27,6 +27,8 @@ def env():
     L.SpjIndexProbeNoAlloc.argtypes = [C.POINTER(capi.SedonaFloatIndex2D), C.c_void_p,
                                        C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                        C.POINTER(C.c_uint64), C.c_void_p]
+    L.SpjAllocationCount.restype = C.c_uint64
+    L.SpjAllocationCount.argtypes = []
     return torch, capi, L
 
 
@@ -42,14 +44,23 @@ def _pairs(b, p):
     return sorted(zip(np.asarray(p).tolist(), np.asarray(b).tolist()))
 
 
-def _no_alloc_probe(torch, capi, L, idx, rects, capacity):
+def _no_alloc_probe(torch, capi, L, idx, rects, capacity, warm=False):
     d_rects = torch.from_numpy(rects).cuda()
     d_b = torch.empty(max(capacity, 1), dtype=torch.int32, device="cuda")
     d_p = torch.empty(max(capacity, 1), dtype=torch.int32, device="cuda")
     n = C.c_uint64(0)
     torch.cuda.synchronize()
+    # the library's own allocation count, read right around the call, may
+    # not move; on a warm call (the static array's module already loaded by
+    # an earlier call) the device's free memory may not move either
+    allocs0 = L.SpjAllocationCount()
+    free0 = torch.cuda.mem_get_info()[0]
     rc = L.SpjIndexProbeNoAlloc(C.byref(idx.idx), d_rects.data_ptr(), len(rects),
                                 d_b.data_ptr(), d_p.data_ptr(), capacity, C.byref(n), None)
+    free1 = torch.cuda.mem_get_info()[0]
+    assert L.SpjAllocationCount() == allocs0, "the no-allocation probe allocated"
+    if warm:
+        assert free1 == free0, (free0, free1)
     b = d_b[: n.value].cpu().numpy().view(np.uint32) if rc == 0 else None
     p = d_p[: n.value].cpu().numpy().view(np.uint32) if rc == 0 else None
     return rc, n.value, b, p
@@ -63,7 +74,8 @@ def test_no_alloc_probe_matches_regular_probe_twice(env):
     idx.finish_building()
     for call, rects in enumerate([_boxes(rng, 50000), _boxes(rng, 70000, points=True)]):
         eb, ep = idx.probe(rects)  # existing entry point (allocates)
-        rc, n, b, p = _no_alloc_probe(torch, capi, L, idx, rects, capacity=len(eb) + 100)
+        rc, n, b, p = _no_alloc_probe(torch, capi, L, idx, rects, capacity=len(eb) + 100,
+                                      warm=call > 0)
         assert rc == 0, idx.idx.get_last_error(C.byref(idx.idx))
         assert n == len(eb) > 0
         assert _pairs(b, p) == _pairs(eb, ep), call
@@ -91,4 +103,37 @@ def test_no_alloc_probe_limits(env):
     full = _boxes(rng, MAX_PROBES)
     eb, ep = idx.probe(full)
     rc, n, b, p = _no_alloc_probe(torch, capi, L, idx, full, capacity=len(eb))
+    assert rc == 0 and _pairs(b, p) == _pairs(eb, ep)
+
+
+def test_no_alloc_probe_rejects_misaligned_pointers(env):
+    """A rect pointer off a 16-byte boundary (e.g. from an arena that aligns
+    to 8 bytes) is rejected with EINVAL and a message before any launch."""
+    torch, capi, L = env
+    rng = np.random.default_rng(13)
+    idx = capi.FloatIndex2D()
+    idx.push_build(_boxes(rng, 500))
+    idx.finish_building()
+    rects = _boxes(rng, 64)
+    buf = torch.zeros(len(rects) * 4 + 2, dtype=torch.float32, device="cuda")
+    buf[2:].copy_(torch.from_numpy(rects.reshape(-1)))  # rects start 8 bytes in
+    out = torch.empty(1024, dtype=torch.int32, device="cuda")
+    n = C.c_uint64(0)
+    torch.cuda.synchronize()
+    rc = L.SpjIndexProbeNoAlloc(C.byref(idx.idx), buf.data_ptr() + 8, len(rects),
+                                out.data_ptr(), out.data_ptr() + 2048, 256, C.byref(n), None)
+    assert rc == 22
+    assert b"16-byte" in idx.idx.get_last_error(C.byref(idx.idx))
+    rc = L.SpjIndexProbeNoAlloc(C.byref(idx.idx), buf.data_ptr(), len(rects),
+                                out.data_ptr() + 2, out.data_ptr() + 2048, 256, C.byref(n), None)
+    assert rc == 22
+    assert b"4-byte" in idx.idx.get_last_error(C.byref(idx.idx))
+    # host memory is not accepted either
+    host = np.ascontiguousarray(np.tile(rects, (1, 1)))
+    rc = L.SpjIndexProbeNoAlloc(C.byref(idx.idx), host.ctypes.data, len(rects),
+                                out.data_ptr(), out.data_ptr() + 2048, 256, C.byref(n), None)
+    assert rc == 22
+    # the index still answers afterwards
+    eb, ep = idx.probe(rects)
+    rc, n2, b, p = _no_alloc_probe(torch, capi, L, idx, rects, capacity=len(eb) + 1)
     assert rc == 0 and _pairs(b, p) == _pairs(eb, ep)
