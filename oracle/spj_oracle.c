@@ -30,6 +30,7 @@ typedef struct {
   int32_t nsegs;  /* tg num_segments (tg.c:2124-2134) */
   int64_t first;  /* index of first point in spj_geoms.pts; pts[first+npts] = pts[first] */
   orect_t rect;
+  int convex, clockwise; /* tg's ring flags (tg.c:1910-2113 process_points) */
 } oring_t;
 
 typedef struct { int64_t first_ring; int32_t nrings; } opoly_t;
@@ -39,6 +40,7 @@ typedef struct {
   opt_t pt;
   int64_t first_poly;
   int32_t npolys;
+  int32_t empty_parts; /* a multipolygon that had parts without rings */
   orect_t rect;
 } ogeom_t;
 
@@ -257,27 +259,143 @@ static int poly_touches_point(const spj_geoms* G, const opoly_t* P, opt_t p) {
   return 0;
 }
 
-/* tg.c:3046-3113 with allow_on_edge = true: count ring segments that
- * intersect seg, stop at two. */
-static int ring_intersects_segment_aoe(const spj_geoms* G, const oring_t* ring, oseg_t seg) {
-  if (!rect_intersects_rect(seg_rect(seg), ring->rect)) return 0;
-  if (ring_contains_point(G, ring, seg.a, 1).hit || ring_contains_point(G, ring, seg.b, 1).hit)
+/* ------------------------------------------------------------------------ */
+/* ring relations (tg.c:2910-3192)                                          */
+/* ------------------------------------------------------------------------ */
+
+/* tg_segment_rect(seg) intersects tg_segment_rect(other) (tg.c:1311-1330) */
+static inline int seg_rects_intersect(oseg_t a, oseg_t b) {
+  return rect_intersects_rect(seg_rect(a), seg_rect(b));
+}
+
+/* tg.c:2910-3039 tg_ring_contains_segment.  tg_ring_search (tg.c:2468-2485)
+ * visits the segments whose rect meets the query's; every visitor below asks
+ * "does any segment ..." and each test starts with the same rect test, so a
+ * plain loop over all segments gives the same answer. */
+static int ring_contains_segment(const spj_geoms* G, const oring_t* ring, oseg_t seg,
+                                 int allow_on_edge) {
+  if (!rect_covers_rect(ring->rect, seg_rect(seg))) return 0;
+  ring_result ra = ring_contains_point(G, ring, seg.a, allow_on_edge);
+  if (!ra.hit) return 0;
+  if (pteq(seg.b, seg.a)) return 1;
+  ring_result rb = ring_contains_point(G, ring, seg.b, allow_on_edge);
+  if (!rb.hit) return 0;
+  if (ring->convex) return 1;
+  if (allow_on_edge) {
+    if (ra.idx != -1) {
+      if (rb.idx != -1) {
+        if (rb.idx == ra.idx) return 1;
+        oseg_t sa = ring_seg(G, ring, ra.idx), sb = ring_seg(G, ring, rb.idx);
+        if (pteq(sa.a, seg.a) || pteq(sa.b, seg.a) || pteq(sb.a, seg.a) || pteq(sb.b, seg.a) ||
+            pteq(sa.a, seg.b) || pteq(sa.b, seg.b) || pteq(sb.a, seg.b) || pteq(sb.b, seg.b))
+          return 1;
+        if (rb.idx < ra.idx) {
+          oseg_t t = sa;
+          sa = sb;
+          sb = t;
+        }
+        /* winding of the ring made of the two edges (tg.c:2977-2990) */
+        opt_t q[5] = {sa.a, sa.b, sb.a, sb.b, sa.a};
+        double cwc = 0.0;
+        for (int i = 0; i < 4; i++) cwc += (q[i + 1].x - q[i].x) * (q[i + 1].y + q[i].y);
+        int clockwise = cwc > 0;
+        if (clockwise != ring->clockwise) return 0;
+        for (int i = 0; i < ring->nsegs; i++) { /* contsegiter1 */
+          oseg_t s = ring_seg(G, ring, i);
+          if (segment_intersects_segment(seg, s) && raycast(s, seg.a) != RC_ON &&
+              raycast(s, seg.b) != RC_ON)
+            return 0;
+        }
+        return 1;
+      }
+      for (int i = 0; i < ring->nsegs; i++) { /* contsegiter4 */
+        oseg_t s = ring_seg(G, ring, i);
+        if (segment_intersects_segment(seg, s) && raycast(s, seg.a) != RC_ON) return 0;
+      }
+      return 1;
+    } else if (rb.idx != -1) {
+      for (int i = 0; i < ring->nsegs; i++) { /* contsegiter2 */
+        oseg_t s = ring_seg(G, ring, i);
+        if (segment_intersects_segment(seg, s) && raycast(s, seg.b) != RC_ON) return 0;
+      }
+      return 1;
+    }
+    for (int i = 0; i < ring->nsegs; i++) { /* contsegiter5 */
+      oseg_t s = ring_seg(G, ring, i);
+      if (segment_intersects_segment(seg, s) && raycast(seg, s.a) != RC_ON &&
+          raycast(seg, s.b) != RC_ON)
+        return 0;
+    }
     return 1;
-  int count = 0;
-  orect_t sr = seg_rect(seg);
+  }
+  for (int i = 0; i < ring->nsegs; i++) { /* contsegiter3 */
+    if (segment_intersects_segment(seg, ring_seg(G, ring, i))) return 0;
+  }
+  return 1;
+}
+
+/* tg.c:3046-3113 tg_ring_intersects_segment.  With allow_on_edge the visitor
+ * counts intersecting segments up to two (order does not matter).  Without
+ * it the visitor keeps state (a collinear overlap resets the count, the first
+ * shared endpoint of each query end is skipped once), so the segments are
+ * visited as tg_ring_search does: ascending index, those whose rect meets
+ * the query's rect. */
+static int ring_intersects_segment(const spj_geoms* G, const oring_t* ring, oseg_t seg,
+                                   int allow_on_edge) {
+  if (!rect_intersects_rect(seg_rect(seg), ring->rect)) return 0;
+  if (ring_contains_point(G, ring, seg.a, allow_on_edge).hit ||
+      ring_contains_point(G, ring, seg.b, allow_on_edge).hit)
+    return 1;
+  int count = 0, a_on = 0, b_on = 0;
+  opt_t a = seg.a, b = seg.b;
   for (int i = 0; i < ring->nsegs && count < 2; i++) {
-    oseg_t rs = ring_seg(G, ring, i);
-    if (!rect_intersects_rect(seg_rect(rs), sr)) continue; /* tg_ring_search filter */
-    if (segment_intersects_segment(seg, rs)) count++;
+    oseg_t s = ring_seg(G, ring, i);
+    if (!seg_rects_intersect(s, seg)) continue;
+    if (!segment_intersects_segment(seg, s)) continue;
+    if (allow_on_edge) {
+      count++;
+      continue;
+    }
+    opt_t c = s.a, d = s.b;
+    int ccol = collinear(a.x, a.y, b.x, b.y, c.x, c.y);
+    int dcol = collinear(a.x, a.y, b.x, b.y, d.x, d.y);
+    if (ccol && dcol) {
+      count = 0; /* parallel */
+    } else {
+      if (!a_on && (pteq(a, c) || pteq(a, d))) {
+        a_on = 1;
+        continue;
+      }
+      if (!b_on && (pteq(b, c) || pteq(b, d))) {
+        b_on = 1;
+        continue;
+      }
+      count++;
+    }
   }
   return count >= 2;
 }
 
 static inline double rect_area(orect_t r) { return (r.maxx - r.minx) * (r.maxy - r.miny); }
 
-/* tg.c:3166-3192 with allow_on_edge = true */
+/* tg.c:3120-3156 tg_ring_contains_ring */
+static int ring_contains_ring(const spj_geoms* GA, const oring_t* a, const spj_geoms* GB,
+                              const oring_t* b, int allow_on_edge) {
+  if (ring_empty(a) || ring_empty(b)) return 0;
+  if (!rect_covers_rect(a->rect, b->rect)) return 0;
+  if (a->convex) {
+    for (int i = 0; i < b->npts; i++)
+      if (!ring_contains_point(GA, a, GB->pts[b->first + i], allow_on_edge).hit) return 0;
+  } else {
+    for (int i = 0; i < b->nsegs; i++)
+      if (!ring_contains_segment(GA, a, ring_seg(GB, b, i), allow_on_edge)) return 0;
+  }
+  return 1;
+}
+
+/* tg.c:3166-3192 tg_ring_intersects_ring */
 static int ring_intersects_ring(const spj_geoms* GA, const oring_t* ring, const spj_geoms* GB,
-                                const oring_t* other) {
+                                const oring_t* other, int allow_on_edge) {
   if (ring_empty(ring) || ring_empty(other)) return 0;
   if (!rect_intersects_rect(ring->rect, other->rect)) return 0;
   double a1 = rect_area(ring->rect), a2 = rect_area(other->rect);
@@ -290,78 +408,176 @@ static int ring_intersects_ring(const spj_geoms* GA, const oring_t* ring, const 
     GB = tg;
   }
   for (int i = 0; i < other->nsegs; i++) {
-    if (ring_intersects_segment_aoe(GA, ring, ring_seg(GB, other, i))) return 1;
+    if (ring_intersects_segment(GA, ring, ring_seg(GB, other, i), allow_on_edge)) return 1;
   }
   return 0;
 }
 
 /* ------------------------------------------------------------------------ */
-/* predicate dispatch (tg.c:5740-5760 intersects, 6028-6046 covers,          */
-/* 6538-6556 contains, 6771-6789 touches, 15299-15330 equals/within/...)     */
+/* polygon relations (tg.c:4040-4262); a polygon without holes is its ring  */
+/* (tg.c:3785-3789), which takes the ring fast paths                        */
+/* ------------------------------------------------------------------------ */
+
+static inline const oring_t* poly_ext(const spj_geoms* G, const opoly_t* P) {
+  return &G->rings[P->first_ring];
+}
+static inline const oring_t* poly_hole(const spj_geoms* G, const opoly_t* P, int h) {
+  return &G->rings[P->first_ring + 1 + h];
+}
+
+/* tg.c:4040-4092 tg_poly_covers_poly (= tg_poly_contains_poly, tg.c:4094-4096) */
+static int poly_covers_poly(const spj_geoms* GA, const opoly_t* A, const spj_geoms* GB,
+                            const opoly_t* B) {
+  if (A->nrings == 1 && B->nrings == 1)
+    return ring_contains_ring(GA, poly_ext(GA, A), GB, poly_ext(GB, B), 1);
+  if (ring_empty(poly_ext(GA, A)) || ring_empty(poly_ext(GB, B))) return 0;
+  const oring_t* bext = poly_ext(GB, B);
+  if (!ring_contains_ring(GA, poly_ext(GA, A), GB, bext, 1)) return 0;
+  int covers = 1;
+  for (int i = 0; i < A->nrings - 1; i++) {
+    const oring_t* h = poly_hole(GA, A, i);
+    if (ring_contains_ring(GA, h, GB, bext, 1) || ring_intersects_ring(GA, h, GB, bext, 0)) {
+      covers = 0;
+      for (int j = 0; j < B->nrings - 1; j++) {
+        if (ring_contains_ring(GB, poly_hole(GB, B, j), GA, h, 1)) {
+          covers = 1;
+          break;
+        }
+      }
+      if (!covers) break;
+    }
+  }
+  return covers;
+}
+
+/* tg.c:4100-4136 tg_poly_intersects_poly */
+static int poly_intersects_poly(const spj_geoms* GA, const opoly_t* A, const spj_geoms* GB,
+                                const opoly_t* B) {
+  if (A->nrings == 1 && B->nrings == 1)
+    return ring_intersects_ring(GA, poly_ext(GA, A), GB, poly_ext(GB, B), 1);
+  if (ring_empty(poly_ext(GA, A)) || ring_empty(poly_ext(GB, B))) return 0;
+  if (!ring_intersects_ring(GB, poly_ext(GB, B), GA, poly_ext(GA, A), 1)) return 0;
+  for (int i = 0; i < A->nrings - 1; i++)
+    if (ring_contains_ring(GA, poly_hole(GA, A, i), GB, poly_ext(GB, B), 0)) return 0;
+  for (int i = 0; i < B->nrings - 1; i++)
+    if (ring_contains_ring(GB, poly_hole(GB, B, i), GA, poly_ext(GA, A), 0)) return 0;
+  return 1;
+}
+
+/* tg.c:4184-4262 tg_poly_touches_poly */
+static int poly_touches_poly(const spj_geoms* GA, const opoly_t* A, const spj_geoms* GB,
+                             const opoly_t* B) {
+  const oring_t* aext = poly_ext(GA, A);
+  const oring_t* bext = poly_ext(GB, B);
+  if (!rect_intersects_rect(aext->rect, bext->rect)) return 0;
+  /* one polygon inside a hole of the other, touching the hole's boundary */
+  for (int ii = 0; ii < 2; ii++) {
+    const spj_geoms* GP = ii == 0 ? GA : GB;
+    const opoly_t* P = ii == 0 ? A : B;
+    const spj_geoms* GR = ii == 0 ? GB : GA;
+    const oring_t* ring = ii == 0 ? bext : aext;
+    for (int i = 0; i < P->nrings - 1; i++) {
+      const oring_t* hole = poly_hole(GP, P, i);
+      if (ring_contains_ring(GP, hole, GR, ring, 1)) {
+        for (int j = 0; j < ring->npts; j++)
+          if (ring_covers_point_as_line(GP, hole, GR->pts[ring->first + j])) return 1;
+        return 0;
+      }
+    }
+  }
+  int ansegs = aext->nsegs, bnsegs = bext->nsegs;
+  int atouches = 0, btouches = 0;
+  for (int ii = 0; ii < 2; ii++) {
+    const spj_geoms* Ga = ii == 0 ? GA : GB;
+    const oring_t* a = ii == 0 ? aext : bext;
+    const spj_geoms* Gb = ii == 0 ? GB : GA;
+    const oring_t* b = ii == 0 ? bext : aext;
+    int nsegs = ii == 0 ? bnsegs : ansegs;
+    int touches = 0;
+    for (int i = 0; i < nsegs; i++) {
+      oseg_t seg = ring_seg(Gb, b, i);
+      int i0 = ring_intersects_segment(Ga, a, seg, 1);
+      int i1 = ring_intersects_segment(Ga, a, seg, 0);
+      if (i0 && !i1) touches++;
+      else if (i0 || i1) return 0;
+    }
+    if (ii == 0) btouches = touches;
+    else atouches = touches;
+  }
+  if (atouches > 0 || btouches > 0) return !(atouches == ansegs && btouches == bnsegs);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* predicate dispatch over geometry kinds (tg.c:5544-5760 intersects,       */
+/* 5767-6046 covers, 6053-6556 contains, 6575-6789 touches,                 */
+/* 15299-15330 equals / within / coveredby / disjoint)                       */
 /* ------------------------------------------------------------------------ */
 
 #define UNSUPPORTED (-1)
 
-static int poly_poly_intersects(const spj_geoms* GA, const opoly_t* A, const spj_geoms* GB,
-                                const opoly_t* B) {
-  const oring_t* ea = &GA->rings[A->first_ring];
-  const oring_t* eb = &GB->rings[B->first_ring];
-  if (A->nrings == 1 && B->nrings == 1) {
-    /* tg.c:4103-4109 fast path: both are rings */
-    return ring_intersects_ring(GA, ea, GB, eb);
-  }
-  return UNSUPPORTED; /* holes on either side: ring_contains_ring needed */
+static inline const opoly_t* part_of(const spj_geoms* G, const ogeom_t* g, int i) {
+  return &G->polys[g->first_poly + i];
+}
+static inline int is_polygonal(const ogeom_t* g) {
+  return g->kind == SPJO_POLYGON || g->kind == SPJO_MULTIPOLYGON;
 }
 
-/* intersects(A, B) where A, B are single parts (point or polygon) */
-static int part_intersects(const spj_geoms* GA, int ka, opt_t pa, const opoly_t* A,
-                           const spj_geoms* GB, int kb, opt_t pb, const opoly_t* B) {
-  if (ka == SPJO_POINT && kb == SPJO_POINT) return pteq(pa, pb);
-  if (ka == SPJO_POINT) return poly_contains_point(GB, B, pa, 1);
-  if (kb == SPJO_POINT) return poly_contains_point(GA, A, pb, 1);
-  return poly_poly_intersects(GA, A, GB, B);
+/* a (multi)polygon covers / contains / touches a point */
+static int any_part_contains_point(const spj_geoms* G, const ogeom_t* g, opt_t p, int aoe) {
+  for (int i = 0; i < g->npolys; i++)
+    if (poly_contains_point(G, part_of(G, g, i), p, aoe)) return 1;
+  return 0;
 }
 
 static int geom_intersects(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, int64_t ib) {
   const ogeom_t* a = &GA->g[ia];
   const ogeom_t* b = &GB->g[ib];
   if (a->kind == SPJO_EMPTY || b->kind == SPJO_EMPTY) return 0;
-  int na = a->kind == SPJO_POINT ? 1 : a->npolys;
-  int nb = b->kind == SPJO_POINT ? 1 : b->npolys;
-  int unsupported = 0;
-  for (int i = 0; i < na; i++) {
-    const opoly_t* A = a->kind == SPJO_POINT ? NULL : &GA->polys[a->first_poly + i];
-    for (int j = 0; j < nb; j++) {
-      const opoly_t* B = b->kind == SPJO_POINT ? NULL : &GB->polys[b->first_poly + j];
-      int r = part_intersects(GA, a->kind == SPJO_POINT ? SPJO_POINT : SPJO_POLYGON, a->pt, A,
-                              GB, b->kind == SPJO_POINT ? SPJO_POINT : SPJO_POLYGON, b->pt, B);
-      if (r == 1) return 1;
-      if (r == UNSUPPORTED) unsupported = 1;
-    }
-  }
-  return unsupported ? UNSUPPORTED : 0;
+  if (a->kind == SPJO_POINT && b->kind == SPJO_POINT) return pteq(a->pt, b->pt);
+  if (a->kind == SPJO_POINT) return any_part_contains_point(GB, b, a->pt, 1);
+  if (b->kind == SPJO_POINT) return any_part_contains_point(GA, a, b->pt, 1);
+  /* any pair of parts, a's part first (poly_intersects_geom, multiiter) */
+  for (int i = 0; i < a->npolys; i++)
+    for (int j = 0; j < b->npolys; j++)
+      if (poly_intersects_poly(GA, part_of(GA, a, i), GB, part_of(GB, b, j))) return 1;
+  return 0;
 }
 
-/* covers(A, B) for A polygonal/point and B a point, or A point and B polygon */
 static int geom_covers(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, int64_t ib) {
   const ogeom_t* a = &GA->g[ia];
   const ogeom_t* b = &GB->g[ib];
   if (a->kind == SPJO_EMPTY || b->kind == SPJO_EMPTY) return 0;
   if (a->kind == SPJO_POINT && b->kind == SPJO_POINT) return pteq(a->pt, b->pt);
-  if (b->kind == SPJO_POINT) {
-    /* tg.c:5869-5898 polygon; tg.c:5983-6026 multipolygon: any part covers */
-    for (int i = 0; i < a->npolys; i++)
-      if (poly_contains_point(GA, &GA->polys[a->first_poly + i], b->pt, 1)) return 1;
-    return 0;
+  if (a->kind == SPJO_POINT) {
+    /* tg.c:1152-1155 per part (point_covers_base_geom: every part, and an
+     * empty part fails) */
+    if (b->empty_parts) return 0;
+    for (int j = 0; j < b->npolys; j++) {
+      const oring_t* e = poly_ext(GB, part_of(GB, b, j));
+      if (ring_empty(e)) return 0;
+      if (!(pteq(a->pt, (opt_t){e->rect.minx, e->rect.miny}) &&
+            pteq(a->pt, (opt_t){e->rect.maxx, e->rect.maxy})))
+        return 0;
+    }
+    return 1;
   }
-  if (a->kind == SPJO_POINT && b->kind == SPJO_POLYGON) {
-    /* tg.c:1152-1155 tg_point_covers_poly: the polygon's rect is the point */
-    const oring_t* e = &GB->rings[GB->polys[b->first_poly].first_ring];
-    if (ring_empty(e)) return 0;
-    return pteq(a->pt, (opt_t){e->rect.minx, e->rect.miny}) &&
-           pteq(a->pt, (opt_t){e->rect.maxx, e->rect.maxy});
+  if (b->kind == SPJO_POINT) return any_part_contains_point(GA, a, b->pt, 1);
+  if (a->kind == SPJO_POLYGON) {
+    /* poly_covers_base_geom: every part of b, an empty part fails */
+    if (b->empty_parts) return 0;
+    for (int j = 0; j < b->npolys; j++)
+      if (!poly_covers_poly(GA, part_of(GA, a, 0), GB, part_of(GB, b, j))) return 0;
+    return 1;
   }
-  return UNSUPPORTED;
+  /* a multipolygon: every non-empty part of b is covered by some part of a */
+  for (int j = 0; j < b->npolys; j++) {
+    int found = 0;
+    for (int i = 0; i < a->npolys && !found; i++)
+      found = poly_covers_poly(GA, part_of(GA, a, i), GB, part_of(GB, b, j));
+    if (!found) return 0;
+  }
+  return 1;
 }
 
 static int geom_contains(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, int64_t ib) {
@@ -373,11 +589,49 @@ static int geom_contains(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, i
   if (b->kind == SPJO_POINT) {
     /* polygon: tg.c:3940-3943; multipolygon: tg.c:6288-6307, an interior
      * hit in any part wins */
-    for (int i = 0; i < a->npolys; i++)
-      if (poly_contains_point(GA, &GA->polys[a->first_poly + i], b->pt, 0)) return 1;
-    return 0;
+    return any_part_contains_point(GA, a, b->pt, 0);
   }
-  return UNSUPPORTED;
+  if (a->kind == SPJO_POLYGON) {
+    /* poly_contains_base_geom: every part of b (tg_poly_contains_poly is
+     * tg_poly_covers_poly), an empty part fails */
+    if (b->empty_parts) return 0;
+    for (int j = 0; j < b->npolys; j++)
+      if (!poly_covers_poly(GA, part_of(GA, a, 0), GB, part_of(GB, b, j))) return 0;
+    return 1;
+  }
+  /* a multipolygon (tg.c:6477-6487): a covers b, and some part of b meets
+   * the interior of some part of a (intersects and does not touch) */
+  if (!geom_covers(GA, ia, GB, ib)) return 0;
+  for (int j = 0; j < b->npolys; j++)
+    for (int i = 0; i < a->npolys; i++) {
+      const opoly_t* pa = part_of(GA, a, i);
+      const opoly_t* pb = part_of(GB, b, j);
+      if (poly_intersects_poly(GA, pa, GB, pb) && !poly_touches_poly(GA, pa, GB, pb)) return 1;
+    }
+  return 0;
+}
+
+/* touches(one part of a, b) for a polygon part pa and b a point or
+ * (multi)polygon (poly_touches_geom, tg.c:6679-6733) */
+static int part_touches_geom(const spj_geoms* GA, const opoly_t* pa, const spj_geoms* GB,
+                             const ogeom_t* b) {
+  if (b->kind == SPJO_POINT) return poly_touches_point(GA, pa, b->pt);
+  if (b->kind == SPJO_POLYGON) return poly_touches_poly(GA, pa, GB, part_of(GB, b, 0));
+  int touches = 0;
+  for (int j = 0; j < b->npolys; j++) {
+    const opoly_t* pb = part_of(GB, b, j);
+    if (poly_touches_poly(GA, pa, GB, pb)) touches = 1;
+    else if (poly_intersects_poly(GA, pa, GB, pb)) return 0;
+  }
+  return touches;
+}
+
+static int part_intersects_geom(const spj_geoms* GA, const opoly_t* pa, const spj_geoms* GB,
+                                const ogeom_t* b) {
+  if (b->kind == SPJO_POINT) return poly_contains_point(GA, pa, b->pt, 1);
+  for (int j = 0; j < b->npolys; j++)
+    if (poly_intersects_poly(GA, pa, GB, part_of(GB, b, j))) return 1;
+  return 0;
 }
 
 static int geom_touches(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, int64_t ib) {
@@ -385,21 +639,29 @@ static int geom_touches(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, in
   const ogeom_t* b = &GB->g[ib];
   if (a->kind == SPJO_EMPTY || b->kind == SPJO_EMPTY) return 0;
   if (a->kind == SPJO_POINT && b->kind == SPJO_POINT) return 0; /* tg.c:1102-1106 */
-  if (a->kind == SPJO_POLYGON && b->kind == SPJO_POINT)
-    return poly_touches_point(GA, &GA->polys[a->first_poly], b->pt);
-  if (a->kind == SPJO_POINT && b->kind == SPJO_POLYGON)
-    return poly_touches_point(GB, &GB->polys[b->first_poly], a->pt);
-  return UNSUPPORTED;
+  if (a->kind == SPJO_POINT) {
+    /* tg_point_touches_poly per part, any part (tg.c:6575-6625) */
+    for (int j = 0; j < b->npolys; j++)
+      if (poly_touches_point(GB, part_of(GB, b, j), a->pt)) return 1;
+    return 0;
+  }
+  if (a->kind == SPJO_POLYGON) return part_touches_geom(GA, part_of(GA, a, 0), GB, b);
+  /* a multipolygon (tg.c:6735-6768) */
+  int touches = 0;
+  for (int i = 0; i < a->npolys; i++) {
+    const opoly_t* pa = part_of(GA, a, i);
+    if (part_touches_geom(GA, pa, GB, b)) touches = 1;
+    else if (part_intersects_geom(GA, pa, GB, b)) return 0;
+  }
+  return touches;
 }
 
 int spjo_predicate(const spj_geoms* B, int64_t bi, const spj_geoms* P, int64_t pi, int pred) {
   switch (pred) {
     case SPJO_INTERSECTS:
       return geom_intersects(B, bi, P, pi);
-    case SPJO_DISJOINT: {
-      int r = geom_intersects(B, bi, P, pi);
-      return r < 0 ? r : !r;
-    }
+    case SPJO_DISJOINT:
+      return !geom_intersects(B, bi, P, pi);
     case SPJO_CONTAINS:
       return geom_contains(B, bi, P, pi);
     case SPJO_WITHIN:
@@ -410,11 +672,8 @@ int spjo_predicate(const spj_geoms* B, int64_t bi, const spj_geoms* P, int64_t p
       return geom_covers(P, pi, B, bi);
     case SPJO_TOUCHES:
       return geom_touches(B, bi, P, pi);
-    case SPJO_EQUALS: {
-      int w = geom_contains(P, pi, B, bi);
-      if (w <= 0) return w;
-      return geom_contains(B, bi, P, pi);
-    }
+    case SPJO_EQUALS:
+      return geom_contains(P, pi, B, bi) && geom_contains(B, bi, P, pi);
   }
   return UNSUPPORTED;
 }
@@ -510,6 +769,47 @@ static int rd_header(wkb_reader* r, int* le, uint32_t* type) {
   return 0;
 }
 
+/* tg.c:1910-2113 process_points: a ring is concave when some vertex turn has
+ * the sign opposite to the first turn's (a first turn of exactly zero counts
+ * as positive), clockwise when the shoelace sum of (b.x - a.x) * (b.y + a.y)
+ * is positive.  The turns and the sum run over the points as stored (the
+ * closing point included), wrapping to the first points at the end. */
+static void ring_flags(const opt_t* p, int n, int* convex, int* clockwise) {
+  if (n < 2) {
+    *convex = 0;
+    *clockwise = 0;
+    return;
+  }
+  int concave = 0, dir = 0;
+  double cwc = 0;
+  for (int i = 0; i < n; i++) {
+    opt_t a = p[i], b, c;
+    if (i < n - 2) {
+      b = p[i + 1];
+      c = p[i + 2];
+    } else if (i == n - 1) {
+      b = p[0];
+      c = p[1];
+    } else {
+      b = p[i + 1];
+      c = p[0];
+    }
+    cwc += (b.x - a.x) * (b.y + a.y);
+    if (!concave) {
+      double z = (b.x - a.x) * (c.y - b.y) - (b.y - a.y) * (c.x - b.x);
+      if (dir == 0) {
+        dir = z < 0 ? -1 : 1;
+      } else if (z < 0) {
+        if (dir == 1) concave = 1;
+      } else if (z > 0) {
+        if (dir == -1) concave = 1;
+      }
+    }
+  }
+  *convex = !concave;
+  *clockwise = cwc > 0;
+}
+
 static int rd_polygon_body(spj_geoms* G, wkb_reader* r, int le, orect_t* grect) {
   uint32_t nrings;
   if (rd_u32(r, le, &nrings)) return -1;
@@ -540,6 +840,7 @@ static int rd_polygon_body(spj_geoms* G, wkb_reader* r, int le, orect_t* grect) 
     if (npts < 3) R->nsegs = 0;
     else if (pteq(G->pts[G->npts + npts - 1], G->pts[G->npts])) R->nsegs = (int32_t)npts - 1;
     else R->nsegs = (int32_t)npts;
+    ring_flags(&G->pts[G->npts], (int)npts, &R->convex, &R->clockwise);
     /* tg.c:2220 the extra closing point */
     G->pts[G->npts + npts] = npts ? G->pts[G->npts] : (opt_t){0, 0};
     G->npts += npts + 1;
@@ -592,11 +893,15 @@ static int parse_one(spj_geoms* G, int64_t row, const uint8_t* p, int64_t len, c
       if (rd_polygon_body(G, &r, le2, &g->rect)) return -1;
       if (G->polys[pb].nrings == 0) {
         G->npolys = pb; /* empty part */
+        g->empty_parts = 1;
         continue;
       }
       kept++;
     }
-    if (kept == 0) return 0;
+    if (kept == 0) {
+      g->empty_parts = 0;
+      return 0;
+    }
     g->kind = SPJO_MULTIPOLYGON;
     g->first_poly = before;
     g->npolys = kept;

@@ -11,7 +11,7 @@ PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tg_pr
 def load():
     z = np.load(PATH)
     cols = {}
-    for name in ("polys", "holed", "pts"):
+    for name in ("polys", "holed", "pts", "rel"):
         cols[name] = WkbColumn(z[name + "_offsets"].astype(np.int32), z[name + "_data"])
     return z, cols
 
@@ -32,6 +32,10 @@ SHAPES = {
     "poly_poly": ("polys", "polys"),
     "point_poly": ("pts", "polys"),
     "point_point": ("pts", "pts"),
+    "rel_rel": ("rel", "rel"),
+    "poly_poly_all": ("polys", "polys"),
+    "rel_point": ("rel", "pts"),
+    "point_rel": ("pts", "rel"),
 }
 
 

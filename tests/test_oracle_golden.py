@@ -24,18 +24,21 @@ def test_predicates_match_reference_tg(golden, oracle_lib, name):
         for a, i in enumerate(brows):
             for b, j in enumerate(prows):
                 r = L.spjo_predicate(geoms[bname].ptr, int(i), geoms[pname].ptr, int(j), int(code))
-                if r == -1:
-                    continue  # combination the oracle declares unsupported
                 if r != exp[k, a, b]:
                     bad.append((int(code), int(i), int(j), r, int(exp[k, a, b])))
     assert not bad, bad[:10]
 
 
-def test_unsupported_combinations_are_few(golden, oracle_lib):
-    # polygon-polygon with holes is the only unsupported family in the golden set
-    z, cols, geoms = golden
-    L = oracle_lib.lib()
-    assert L.spjo_predicate(geoms["polys"].ptr, 0, geoms["polys"].ptr, 1, 5) in (0, 1)
+def test_golden_tables_hold_every_relation(golden):
+    """The polygon-polygon tables carry positive outcomes for every predicate
+    (so the parity above is not vacuous), and contains equals covers between
+    polygons as in tg (tg_poly_contains_poly, tg.c:4094-4096)."""
+    z, cols, _ = golden
+    for name in ("rel_rel", "poly_poly_all"):
+        preds, _, _, exp = golden_io.cube(z, cols, name)
+        sums = {int(c): int(exp[k].sum()) for k, c in enumerate(preds)}
+        assert all(v > 0 for v in sums.values()), (name, sums)
+        assert sums[3] == sums[4] and sums[6] == sums[7], sums
 
 
 def test_raycast_known_answers(golden, oracle_lib):
