@@ -277,12 +277,9 @@ def run_ours(args, world, rank, local, pg):
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 4}, {"refine_min_blocks": 5},
-                   {"refine_min_blocks": 3},
+    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 4},
                    {"cell_grid": 0}, {"probe_order": -1}, {"refine_split": 1},
-                   {"candidate_order": 0, "refine_split": 0}, {"candidate_order": 4},
-                   {"refine_split": 1, "refine_split_group": 8},
-                   {"refine_split": 1, "refine_split_group": 4}]
+                   {"candidate_order": 0, "refine_split": 0}]
     if pred == "dwithin":
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
                         {"dwithin_arena": 1}, {"dwithin_slots": 32},

@@ -93,21 +93,16 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "probe_order"       -1 row order, 0 Morton order from 65536 rows up, 1 always
  *   "candidate_order"   3 (default) auto: 2 for relation predicates with 4M+
  *                       candidates over a build side that is not all points,
- *                       else 0; 4 by build row then the probe box's band
- *                       and x in the build ring; 2 by build row then probe Morton
- *                       rank, 1 the probes' Morton order, 0 as listed
+ *                       else 0; 2 by build row then probe Morton rank, 0 as
+ *                       listed
  *   "refine_min_blocks" 0 (default: auto, 6 in build-major candidate order,
- *                       else 4) or 2 to 6: FP32 refine built for that many
+ *                       else 4), 4 or 6: FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)
- *   "refine_group"      0 (default: one lane per pair), 4, 8, 16: lanes
- *                       cooperating on one candidate pair in the FP32 refine
  *   "refine_split"      2 (default: auto, on unless the candidates are in
  *                       build-major order), 1 on, 0 off: FP32 refine of
  *                       relation predicates in two passes (a cheap pass over
  *                       all pairs queues the pairs it leaves open for a full
  *                       pass)
- *   "refine_split_group" 0 (default), 4, 8, 16: lanes per queued pair in the
- *                       second pass of the split refine
  *   "host_slices"       0 (default: auto, 2 from 524,288 rows), 1 (one
  *                       call), 2-64: row slices of SpjJoinProbeHost
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side

@@ -785,19 +785,11 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value >= -1 && value <= 1, "probe_order must be -1, 0 or 1");
       c.probe_order = (int)value;
     } else if (k == "candidate_order") {
-      SPJ_CHECK(value >= 0 && value <= 4, "candidate_order must be 0, 1, 2, 3 or 4");
+      SPJ_CHECK(value == 0 || value == 2 || value == 3, "candidate_order must be 0, 2 or 3");
       c.candidate_order = (int)value;
-    } else if (k == "refine_group") {
-      SPJ_CHECK(value == 0 || value == 4 || value == 8 || value == 16,
-                "refine_group must be 0, 4, 8 or 16");
-      c.refine_group = (int)value;
     } else if (k == "refine_split") {
       SPJ_CHECK(value >= 0 && value <= 2, "refine_split must be 0, 1 or 2");
       c.refine_split = (int)value;
-    } else if (k == "refine_split_group") {
-      SPJ_CHECK(value == 0 || value == 4 || value == 8 || value == 16,
-                "refine_split_group must be 0, 4, 8 or 16");
-      c.refine_split_group = (int)value;
     } else if (k == "host_slices") {
       SPJ_CHECK(value >= 0 && value <= 64, "host_slices must be in [0, 64]");
       c.host_slices = (int)value;
@@ -814,8 +806,8 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value == 0 || value == 1, "fuse_dwithin must be 0 or 1");
       c.fuse_dwithin = value != 0;  // takes effect at the next build
     } else if (k == "refine_min_blocks") {
-      SPJ_CHECK(value == 0 || (value >= 2 && value <= 6),
-                "refine_min_blocks must be 0 (auto) or in [2, 6]");
+      SPJ_CHECK(value == 0 || value == 4 || value == 6,
+                "refine_min_blocks must be 0 (auto), 4 or 6");
       c.refine_min_blocks = (int)value;
     } else {
       throw Error("unknown option '" + k + "'");

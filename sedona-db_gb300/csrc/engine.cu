@@ -8,59 +8,6 @@
 #include <cstring>
 
 namespace spj {
-namespace {
-
-// Candidate order 4: key = build row above 16 bits that place the probe box
-// inside the build row's first ring: the band of the box's lower y (8 bits)
-// and the box's left x across the ring's rect (8 bits).  The isolation scan
-// of a box covers the bands from its lower y up and stops at the first entry
-// left of its left x, so neighbouring lanes then scan the same entries.
-// Rows without a band index take the probe's Morton rank instead.
-__global__ void k_cand_band_keys(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
-                                 uint64_t m, uint32_t probe_base, GeomsView B,
-                                 const float4* __restrict__ pbox, uint32_t np,
-                                 const uint32_t* __restrict__ rank, int bbits,
-                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
-  const int rbits = 32 - bbits;  // >= 16
-  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m;
-       k += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t b = cb[k], p = cp[k] - probe_base;
-    uint32_t sec = 0;  // 16 bits
-    bool banded = false;
-    if (B.ring_bands != nullptr && b < B.n && p < np &&
-        (B.kind[b] == kPolygon || B.kind[b] == kMultiPolygon)) {
-      const uint32_t r = B.part_ring[B.row_part[b]];
-      const float2 prm = B.band_param[r];
-      const float4 q = pbox[p];
-      if (r < B.nrings && prm.y >= 0.0f && q.x == q.x && q.y == q.y) {
-        const int nb = (int)(B.ring_bands[r + 1] - B.ring_bands[r]) - 1;
-        const int band = pred::band_of(q.y, prm.x, prm.y, nb);
-        const float4 R = B.ring_rect32[r];
-        const float w = R.z - R.x;
-        int xq = 0;
-        if (w > 0.0f) xq = (int)fminf(fmaxf((q.x - R.x) / w * 256.0f, 0.0f), 255.0f);
-        sec = ((uint32_t)min(max(band, 0), 255) << 8) | (uint32_t)xq;
-        banded = true;
-      }
-    }
-    if (!banded) {
-      const uint32_t r = rank && p < np ? rank[p] : (p < np ? p : 0);
-      sec = (uint32_t)(((uint64_t)r << 16) / (np ? np : 1));
-    }
-    keys[k] = (b << rbits) | (sec << (rbits - 16));
-    vals[k] = (uint32_t)k;
-  }
-}
-
-__global__ void k_probe_rank(const uint32_t* __restrict__ order, uint32_t n,
-                             uint32_t* __restrict__ rank) {
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    const uint32_t pi = order[j];
-    if (pi < n) rank[pi] = j;
-  }
-}
-
-}  // namespace
 
 Workspace::Workspace() {
   SPJ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -267,12 +214,9 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   launches += 5;
   const uint32_t* cperm = nullptr;
   bool build_major = false;
-  if (cfg_.candidate_order == 1) {
-    cperm = candidate_order(order, n, m, ws.psc, s);
-    if (cperm) launches += 5;  // gather, 3-kernel scan, scatter
-  } else if (cfg_.candidate_order == 2 ||
-             (cfg_.candidate_order == 3 && predicate != kPredDWithin && !bg_.all_points &&
-              m >= kBuildMajorMin)) {
+  if (cfg_.candidate_order == 2 ||
+      (cfg_.candidate_order == 3 && predicate != kPredDWithin && !bg_.all_points &&
+       m >= kBuildMajorMin)) {
     // (auto, 3: the order pays when consecutive pairs re-read one build
     // geometry's vertices and band index from cache; a point build row is
     // 16 bytes with nothing to re-read, distance candidates are cheap to
@@ -281,26 +225,6 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
                               probe_base, bg_.n, order, n, ws.psc, s);
     if (cperm) launches += 22;  // rank, keys, 4 radix passes
     build_major = cperm != nullptr;
-  } else if (cfg_.candidate_order == 4 && m >= 2 && m < 0xFFFFFFFFull && bg_.n > 0) {
-    int bbits = 1;
-    while (bbits < 32 && (bg_.n - 1) >> bbits) bbits++;
-    if (bbits <= 16) {
-      reserve_candidate_keys(m, ws.psc, s);
-      const uint32_t* rank = nullptr;
-      if (order) {
-        ws.psc.rank.reserve(((size_t)n + 1) * 4, s);
-        k_probe_rank<<<grid_for(n, 256), 256, 0, s>>>(order, (uint32_t)n,
-                                                      ws.psc.rank.as<uint32_t>());
-        rank = ws.psc.rank.as<uint32_t>();
-      }
-      k_cand_band_keys<<<grid_for((int64_t)m, 256), 256, 0, s>>>(
-          ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m, probe_base, bg_.view(),
-          boxes, (uint32_t)n, rank, bbits, ws.psc.ckeys.as<uint32_t>(),
-          ws.psc.cperm.as<uint32_t>());
-      cperm = sort_candidate_keys(m, 32, ws.psc, s);
-      launches += 18;  // rank, keys, 4 radix passes
-      build_major = true;
-    }
   }
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));
 
@@ -309,8 +233,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   uint32_t *rq = nullptr, *rqn = nullptr;
   const int mb = refine_blocks(cfg_.refine_min_blocks, build_major);
   const bool split = cfg_.refine_split == 1 || (cfg_.refine_split == 2 && !build_major);
-  if (split && cfg_.refine_form == kFastF32 && predicate != kPredDWithin &&
-      cfg_.refine_group == 0 && (mb == 4 || mb == 6)) {
+  if (split && cfg_.refine_form == kFastF32 && predicate != kPredDWithin) {
     ws.rqueue.reserve((m + 2) * 4, s);
     rq = ws.rqueue.as<uint32_t>();
     rqn = rq + m + 1;
@@ -323,8 +246,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   else
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb,
-                    rq ? cfg_.refine_split_group : cfg_.refine_group, rq, rqn);
+                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb, rq, rqn);
   launches += rq ? 2 : 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 
@@ -382,7 +304,7 @@ uint64_t JoinEngine::refine_pairs(Workspace& ws, const GeomsView& pv, const uint
   else
     refine_relation(bv, pv, cb, cp, m, 0, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
                     ws.status.as<DeviceStatus>(), s, nullptr, nullptr,
-                    refine_blocks(cfg_.refine_min_blocks, false), cfg_.refine_group);
+                    refine_blocks(cfg_.refine_min_blocks, false));
   ws.pos.reserve((m + 1) * 8, s);
   scan_u8_u64(ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), (int64_t)m, ws.scan_tmp, s);
   uint64_t total = 0;

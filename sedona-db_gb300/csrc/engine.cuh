@@ -41,28 +41,23 @@ struct EngineConfig {
   // in Morton order the counting pass slowed from 38 to 103 ms with it (the
   // scatter pass fell from 33 to 9 ms), so auto leaves it off there
   int dwithin_arena = 2;
-  // refine order of the candidates: 0 as listed (by probe row), 1 the probes'
-  // Morton order, 2 by build row then probe Morton rank (a warp then tests
-  // one build geometry's edges against neighbouring probes: shared loads and
-  // similar trip counts; 2M x 50k polygons: 77 vs 104 ms per step), 3 auto:
-  // 2 for relation predicates over a build side that is not all points,
-  // from kBuildMajorMin candidates up, else 0; 4 by build row, then the
-  // probe box's band and left x within the build row's first ring
+  // refine order of the candidates: 0 as listed (by probe row), 2 by build
+  // row then probe Morton rank (a warp then tests one build geometry's edges
+  // against neighbouring probes: shared loads and similar trip counts; 2M x
+  // 50k polygons: 77 vs 104 ms per step), 3 auto: 2 for relation predicates
+  // over a build side that is not all points, from kBuildMajorMin candidates
+  // up, else 0.  (The probes' Morton order and a band-and-x order inside the
+  // build ring measured slower on every workload and were removed.)
   int candidate_order = 3;
   // FP32 refine compiled for this many resident 256-thread blocks per SM
-  // (2-6), or 0 auto: 6 in build-major candidate order (a warp's pairs share
-  // one build geometry, and more resident warps hide its load latency better
-  // than registers do: 2M x 50k polygons 58.5 vs 60.5 ms), else 4 (10M points
-  // x 50k zones: 96.7 vs 99.4 ms with 6)
+  // (4 or 6), or 0 auto: 6 in build-major candidate order (a warp's pairs
+  // share one build geometry, and more resident warps hide its load latency
+  // better than registers do: 2M x 50k polygons 58.5 vs 60.5 ms), else 4
+  // (10M points x 50k zones: 96.7 vs 99.4 ms with 6)
   int refine_min_blocks = 0;
   // per-ring cell grids on the build side (clean cells answer point-in-ring
   // tests in O(1)); set before the build
   bool cell_grid = true;
-  // lanes per candidate pair in the FP32 refine (4, 8, 16; 0 = one lane each).
-  // One lane per pair measured fastest on the 2M x 50k polygon and 10M x 50k
-  // point workloads (their band lists are short); groups pay off only when
-  // rings have long band lists.
-  int refine_group = 0;
   // FP32 refine in two passes: a cheap pass (isolation exit, first vertex)
   // over every pair queues the pairs it leaves open, a full pass takes the
   // queue (a warp's lanes then hold pairs of similar cost).  0 off, 1 on,
@@ -70,10 +65,6 @@ struct EngineConfig {
   // warp's pairs already share one build geometry (2M x 50k polygons: 59.0
   // ms one pass vs 61.0 split in build-major order; 78.0 vs 63.3 as listed)
   int refine_split = 2;
-  // lanes per queued pair in the split refine's second pass (0, 4, 8, 16);
-  // 2M x 50k polygons with the split: 57.1 ms with one lane per pair, 67.6
-  // with 4, 69.4 with 8
-  int refine_split_group = 0;
   // host probes (SpjJoinProbeHost): 0 auto (2 slices from 524,288 rows up),
   // 1 one call, n > 1 that many slices
   int host_slices = 0;

@@ -673,181 +673,6 @@ __device__ __forceinline__ int ring_intersects_ring(const GeomsView& GA, uint32_
   return 0;
 }
 
-// ---------------------------------------------------------------------------
-// Group-cooperative forms (FP32 tiers only).  A group of kG consecutive
-// lanes (mask gm, lane gl within the group) evaluates one pair: the lanes
-// split a ring's band-edge entries, and the per-edge results are combined
-// with group votes.  Every combination is independent of the order in which
-// edges are visited, so each function returns what its sequential
-// counterpart above returns:
-//  * point in ring: "ON at some edge" makes the answer allow_on_edge, else
-//    the parity of the IN edges (tg's walk, tg.c:2668-2735, reaches the same
-//    answer in any order; the ON edge index is not needed here);
-//  * isolation exit: "some edge is near" is an OR;
-//  * segment hits: only whether at least two edges are hit matters.
-// All inputs that the lanes branch on outside the edge loops are the same
-// in every lane, so the lanes of a group reach each vote together.
-
-template <int kG>
-__device__ __forceinline__ bool ring_pip_group(const GeomsView& G, uint32_t r, double2 p,
-                                               float2 p32, bool aoe, uint32_t& esc,
-                                               unsigned gm, int gl) {
-  if (!ring_rect_covers(G, r, p, p32)) return false;
-  const uint32_t V = G.ring_vtx[r];
-  bool on = false;
-  unsigned ins = 0;
-  auto seg = [&](int i) {
-    const int c = pip_seg_f32(G.xy32[V + i], G.xy32[V + i + 1], p32);
-    if (c == kOut) return;
-    if (c == kIn) {
-      ins ^= 1u;
-      return;
-    }
-    esc++;
-    const double2 a = G.xy[V + i], b = G.xy[V + i + 1];
-    const double ymin = fmin0(a.y, b.y), ymax = fmax0(a.y, b.y);
-    if (p.y < ymin || p.y > ymax) return;
-    const int rc = raycast(a, b, p);
-    if (rc == kIn) ins ^= 1u;
-    else if (rc == kOn) on = true;
-  };
-  if (G.ring_bands != nullptr && G.band_param[r].y >= 0.0f) {
-    const uint32_t B = G.ring_bands[r];
-    const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
-    const float2 prm = G.band_param[r];
-    const int b = band_of(p32.y, prm.x, prm.y, nb);
-    const uint32_t e0 = G.band_off[B + b], e1 = G.band_off[B + b + 1];
-    for (uint32_t k = e0 + gl; k < e1; k += kG) seg(G.band_edges[k]);
-  } else {
-    const int ns = G.ring_nsegs[r];
-    for (int i = gl; i < ns; i += kG) seg(i);
-  }
-  if (__any_sync(gm, on)) return aoe;
-  return (__reduce_xor_sync(gm, ins) & 1u) != 0;
-}
-
-template <int kG>
-__device__ __forceinline__ bool poly_contains_point_group(const GeomsView& G, uint32_t part,
-                                                          double2 p, float2 p32, bool aoe,
-                                                          uint32_t& esc, unsigned gm, int gl) {
-  const uint32_t r0 = G.part_ring[part], r1 = G.part_ring[part + 1];
-  if (r1 - r0 == 1) return ring_pip_group<kG>(G, r0, p, p32, aoe, esc, gm, gl);
-  if (ring_npts(G, r0) < 3) return false;
-  if (!ring_pip_group<kG>(G, r0, p, p32, aoe, esc, gm, gl)) return false;
-  for (uint32_t h = r0 + 1; h < r1; h++)
-    if (ring_pip_group<kG>(G, h, p, p32, !aoe, esc, gm, gl)) return false;
-  return true;
-}
-
-// ring_seg_hits >= 2, lanes splitting the band entries of the segment's bands
-template <int kG>
-__device__ __forceinline__ bool ring_seg_hits2_group(const GeomsView& G, uint32_t r, double2 a,
-                                                     double2 b, float2 a32, float2 b32,
-                                                     uint32_t& esc, unsigned gm, int gl) {
-  const uint32_t V = G.ring_vtx[r];
-  const float qx0 = fmin0f(a32.x, b32.x), qx1 = fmax0f(a32.x, b32.x);
-  const float qy0 = fmin0f(a32.y, b32.y), qy1 = fmax0f(a32.y, b32.y);
-  unsigned count = 0;
-  auto test = [&](int i) {
-    const float2 c = G.xy32[V + i], d = G.xy32[V + i + 1];
-    if (fmin0f(c.x, d.x) > qx1 || fmax0f(c.x, d.x) < qx0 || fmin0f(c.y, d.y) > qy1 ||
-        fmax0f(c.y, d.y) < qy0)
-      return;
-    const int o1 = orient32(a32, b32, c), o2 = orient32(a32, b32, d);
-    if (o1 != 0 && o1 == o2) return;
-    const int o3 = orient32(c, d, a32), o4 = orient32(c, d, b32);
-    if (o3 != 0 && o3 == o4) return;
-    if (o1 != 0 && o2 != 0 && o3 != 0 && o4 != 0) {
-      count++;
-      return;
-    }
-    esc++;
-    if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
-  };
-  if (G.ring_bands != nullptr && G.band_param[r].y >= 0.0f) {
-    const uint32_t B = G.ring_bands[r];
-    const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
-    const float2 prm = G.band_param[r];
-    const int b0 = band_of(qy0, prm.x, prm.y, nb), b1 = band_of(qy1, prm.x, prm.y, nb);
-    // bands b0..b1 are consecutive in the CSR; an edge listed in several of
-    // them is tested in the first band of the query that it spans only
-    const uint32_t e0 = G.band_off[B + b0], e1 = G.band_off[B + b1 + 1];
-    int bb = b0;
-    for (uint32_t k = e0 + gl; k < e1; k += kG) {
-      while (bb < b1 && k >= G.band_off[B + bb + 1]) bb++;
-      const int i = G.band_edges[k];
-      if (bb > b0) {
-        const float2 c = G.xy32[V + i], d = G.xy32[V + i + 1];
-        if (band_of(fmin0f(c.y, d.y), prm.x, prm.y, nb) < bb) continue;
-      }
-      test(i);
-    }
-  } else {
-    const int ns = G.ring_nsegs[r];
-    for (int i = gl; i < ns; i += kG) test(i);
-  }
-  return __reduce_add_sync(gm, count) >= 2u;
-}
-
-template <int kG>
-__device__ __forceinline__ bool ring_intersects_ring_group(const GeomsView& GA, uint32_t ra,
-                                                           const GeomsView& GB, uint32_t rb,
-                                                           uint32_t& esc, unsigned gm, int gl) {
-  if (ring_npts(GA, ra) < 3 || ring_npts(GB, rb) < 3) return false;
-  if (!ring_rects_intersect<true>(GA, ra, GB, rb)) return false;
-  const GeomsView* Gr = &GA;
-  const GeomsView* Go = &GB;
-  uint32_t rr = ra, ro = rb;
-  if (swap_rings<true>(GA, ra, GB, rb)) {
-    Gr = &GB;
-    Go = &GA;
-    rr = rb;
-    ro = ra;
-  }
-  const uint32_t Vo = Go->ring_vtx[ro];
-  const int nso = Go->ring_nsegs[ro];
-  if (nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
-    // isolation exit (see ring_intersects_ring)
-    const float4 ob = Go->ring_rect32[ro];
-    const float bx0 = ob.x, by0 = ob.y, bx1 = ob.z, by1 = ob.w;
-    const uint32_t Vr = Gr->ring_vtx[rr];
-    const uint32_t B = Gr->ring_bands[rr];
-    const int nb = (int)(Gr->ring_bands[rr + 1] - B) - 1;
-    const float2 prm = Gr->band_param[rr];
-    const int b0 = band_of(by0, prm.x, prm.y, nb), b1 = band_of(by1, prm.x, prm.y, nb);
-    const uint32_t e0 = Gr->band_off[B + b0], e1 = Gr->band_off[B + b1 + 1];
-    bool near = false;
-    for (uint32_t k = e0 + gl; k < e1 && !near; k += kG) {
-      const int i = Gr->band_edges[k];
-      const float2 c = Gr->xy32[Vr + i], d = Gr->xy32[Vr + i + 1];
-      if (fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
-          fmin0f(c.y, d.y) > by1)
-        continue;
-      const int s0 = orient32(c, d, make_float2(bx0, by0));
-      if (s0 != 0 && orient32(c, d, make_float2(bx1, by0)) == s0 &&
-          orient32(c, d, make_float2(bx1, by1)) == s0 &&
-          orient32(c, d, make_float2(bx0, by1)) == s0)
-        continue;
-      near = true;
-    }
-    if (!__any_sync(gm, near))
-      return ring_pip_group<kG>(*Gr, rr, Go->xy[Vo], Go->xy32[Vo], true, esc, gm, gl);
-  }
-  for (int i = 0; i <= nso; i++)
-    if (ring_pip_group<kG>(*Gr, rr, Go->xy[Vo + i], Go->xy32[Vo + i], true, esc, gm, gl))
-      return true;
-  const float4 R32 = Gr->ring_rect32[rr];
-  for (int i = 0; i < nso; i++) {
-    const double2 a = Go->xy[Vo + i], b = Go->xy[Vo + i + 1];
-    const float2 a32 = Go->xy32[Vo + i], b32 = Go->xy32[Vo + i + 1];
-    if (fmin0f(a32.x, b32.x) > R32.z || fmax0f(a32.x, b32.x) < R32.x ||
-        fmin0f(a32.y, b32.y) > R32.w || fmax0f(a32.y, b32.y) < R32.y)
-      continue;
-    if (ring_seg_hits2_group<kG>(*Gr, rr, a, b, a32, b32, esc, gm, gl)) return true;
-  }
-  return false;
-}
-
 }  // namespace
 }  // namespace pred
 }  // namespace spj

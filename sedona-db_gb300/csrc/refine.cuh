@@ -29,21 +29,17 @@ enum RefineForm : int {
 // is the capacity of cb/cp/flags; flags past the count are cleared.  With
 // perm (a permutation of [0, m)), candidates are evaluated in that order
 // (flags still land at their own index); with perm and m_dev together, perm
-// is a permutation of [0, *m_dev) and the caller clears the flags past it.  min_blocks (2 to 6) selects
-// the FP32 form compiled for that many resident 256-thread blocks per SM:
-// fewer registers, more warps to hide the latency of divergent pairs.
-// group (4, 8 or 16; FP32 form, no perm) evaluates each pair with that many
-// cooperating lanes splitting the ring loops; 0 keeps one lane per pair.
-// queue (m entries) and qn (one device word) split the FP32 refine (min_blocks
-// 4 or 6) into a cheap pass over all pairs that queues the pairs it cannot
-// decide, then a full pass over the queue (with `group` lanes per queued
-// pair when group is 4, 8 or 16); same flags.
+// is a permutation of [0, *m_dev) and the caller clears the flags past it.
+// min_blocks (4 or 6) selects the FP32 form compiled for that many resident
+// 256-thread blocks per SM: fewer registers, more warps to hide the latency
+// of divergent pairs.  queue (m entries) and qn (one device word) split the
+// FP32 refine into a cheap pass over all pairs that queues the pairs it
+// cannot decide, then a full pass over the queue; same flags.
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,
                      const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
-                     int min_blocks = 4, int group = 0, uint32_t* queue = nullptr,
-                     uint32_t* qn = nullptr);
+                     int min_blocks = 4, uint32_t* queue = nullptr, uint32_t* qn = nullptr);
 
 // flags[k] = hypot(build - probe) <= distance for point pairs: an FP64
 // squared-distance test decides pairs outside a 1e-14 relative band around

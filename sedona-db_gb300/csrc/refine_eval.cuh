@@ -1,8 +1,8 @@
 // refine_eval.cuh — the device side of the relation-predicate refine: tg
-// dispatch per predicate (one lane per pair, or a group of lanes per pair)
-// and the refine kernels.  Included by the translation units that launch
-// them (refine.cu, refine_split.cu, refine_group.cu, refine_blocks.cu), which compile in
-// parallel; each gets its own copy of the kernels it instantiates.
+// dispatch per predicate (one lane per pair) and the refine kernels.
+// Included by the translation units that launch them (refine.cu,
+// refine_split.cu, refine_blocks.cu), which compile in parallel; each gets
+// its own copy of the kernels it instantiates.
 #pragma once
 #include "exact.cuh"
 #include "predicates.cuh"
@@ -160,106 +160,6 @@ __device__ int eval(const GeomsView& B, uint32_t b, const GeomsView& P, uint32_t
   return kUnsupportedResult;
 }
 
-// --- group-cooperative dispatch (FP32 form): kG lanes per pair -------------
-// Mirrors g_intersects / g_contains / g_covers / eval above, with the ring
-// loops split across the group (predicates.cuh); touches runs the
-// sequential code in every lane (same inputs, same answer).
-
-template <int kG>
-__device__ int g_intersects_group(const GeomsView& GA, uint32_t ia, const GeomsView& GB,
-                                  uint32_t ib, uint32_t& esc, unsigned gm, int gl) {
-  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
-  if (ka == kEmpty || kb == kEmpty) return 0;
-  if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
-  if (ka == kPoint || kb == kPoint) {
-    const GeomsView& GP = ka == kPoint ? GA : GB;
-    const GeomsView& GY = ka == kPoint ? GB : GA;
-    const uint32_t ip = ka == kPoint ? ia : ib, iy = ka == kPoint ? ib : ia;
-    const double2 p = GP.pt[ip];
-    const float2 p32 = pt32(GP, ip);
-    for (uint32_t q = GY.row_part[iy]; q < GY.row_part[iy + 1]; q++)
-      if (poly_contains_point_group<kG>(GY, q, p, p32, true, esc, gm, gl)) return 1;
-    return 0;
-  }
-  bool unsupported = false;
-  for (uint32_t qa = GA.row_part[ia]; qa < GA.row_part[ia + 1]; qa++) {
-    const uint32_t ra = GA.part_ring[qa];
-    const bool sa = GA.part_ring[qa + 1] - ra == 1;
-    for (uint32_t qb = GB.row_part[ib]; qb < GB.row_part[ib + 1]; qb++) {
-      const uint32_t rb = GB.part_ring[qb];
-      const bool sb = GB.part_ring[qb + 1] - rb == 1;
-      if (!(sa && sb)) {
-        unsupported = true;
-        continue;
-      }
-      if (ring_intersects_ring_group<kG>(GA, ra, GB, rb, esc, gm, gl)) return 1;
-    }
-  }
-  return unsupported ? kUnsupportedResult : 0;
-}
-
-template <int kG>
-__device__ int g_contains_group(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
-                                uint32_t& esc, unsigned gm, int gl) {
-  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
-  if (ka == kEmpty || kb == kEmpty) return 0;
-  if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
-  if (ka == kPoint) return 0;
-  if (kb == kPoint) {
-    const double2 p = GB.pt[ib];
-    const float2 p32 = pt32(GB, ib);
-    for (uint32_t q = GA.row_part[ia]; q < GA.row_part[ia + 1]; q++)
-      if (poly_contains_point_group<kG>(GA, q, p, p32, false, esc, gm, gl)) return 1;
-    return 0;
-  }
-  return kUnsupportedResult;
-}
-
-template <int kG>
-__device__ int g_covers_group(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
-                              uint32_t& esc, unsigned gm, int gl) {
-  const uint8_t ka = GA.kind[ia], kb = GB.kind[ib];
-  if (ka == kEmpty || kb == kEmpty) return 0;
-  if (ka == kPoint && kb == kPoint) return pteq(GA.pt[ia], GB.pt[ib]);
-  if (kb == kPoint) {
-    const double2 p = GB.pt[ib];
-    const float2 p32 = pt32(GB, ib);
-    for (uint32_t q = GA.row_part[ia]; q < GA.row_part[ia + 1]; q++)
-      if (poly_contains_point_group<kG>(GA, q, p, p32, true, esc, gm, gl)) return 1;
-    return 0;
-  }
-  return g_covers<true>(GA, ia, GB, ib, esc);  // point covering a polygon: no ring loops
-}
-
-template <int kG>
-__device__ int eval_group(const GeomsView& B, uint32_t b, const GeomsView& P, uint32_t p,
-                          int predicate, uint32_t& esc, unsigned gm, int gl) {
-  switch (predicate) {
-    case kIntersects:
-      return g_intersects_group<kG>(B, b, P, p, esc, gm, gl);
-    case kDisjoint: {
-      const int r = g_intersects_group<kG>(B, b, P, p, esc, gm, gl);
-      return r < 0 ? r : !r;
-    }
-    case kContains:
-      return g_contains_group<kG>(B, b, P, p, esc, gm, gl);
-    case kWithin:
-      return g_contains_group<kG>(P, p, B, b, esc, gm, gl);
-    case kCovers:
-      return g_covers_group<kG>(B, b, P, p, esc, gm, gl);
-    case kCoveredBy:
-      return g_covers_group<kG>(P, p, B, b, esc, gm, gl);
-    case kTouches:
-      return g_touches<true>(B, b, P, p, esc);
-    case kEquals: {
-      const int w = g_contains_group<kG>(P, p, B, b, esc, gm, gl);
-      if (w <= 0) return w;
-      return g_contains_group<kG>(B, b, P, p, esc, gm, gl);
-    }
-  }
-  return kUnsupportedResult;
-}
-
 __device__ __forceinline__ void flush_counters(DeviceStatus* st, uint32_t esc, uint32_t pairs) {
   // warp-aggregate, one atomic per warp
 #pragma unroll
@@ -334,47 +234,6 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   flush_counters(st, esc, pairs);
 }
 
-// Group-cooperative FP32 refine: kG consecutive lanes take one candidate
-// (grid-stride over candidates per group); the group's leader writes the
-// flag.  Same contract as k_refine (m_dev: device-side count, flags past it
-// cleared).
-template <int kG, int kMinBlocks, bool kQueue = false>
-__global__ void __launch_bounds__(256, kMinBlocks)
-    k_refine_group(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
-                   const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base,
-                   int predicate, uint8_t* __restrict__ flags, DeviceStatus* st,
-                   const uint64_t* __restrict__ m_dev, const uint32_t* __restrict__ queue = nullptr,
-                   const uint32_t* __restrict__ qn = nullptr) {
-  // kQueue: the groups take the candidates queue[0, *qn) (the second pass of
-  // the split refine); flags of other candidates are left alone
-  uint32_t esc = 0, pairs = 0;
-  const int lane = threadIdx.x & 31;
-  const int gl = lane & (kG - 1);
-  const unsigned gm = kG == 32 ? 0xffffffffu : (((1u << kG) - 1u) << (lane & ~(kG - 1)));
-  const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kG;
-  const uint64_t ng = ((uint64_t)gridDim.x * blockDim.x) / kG;
-  const uint64_t mm = m_dev ? min(*m_dev, m) : m;
-  const uint64_t nu = kQueue ? min((uint64_t)*qn, m) : m;
-  for (uint64_t u = gid; u < nu; u += ng) {
-    const uint64_t k = kQueue ? (uint64_t)queue[u] : u;
-    if (k >= mm) {
-      if (!kQueue && gl == 0 && k < m) flags[k] = 0;
-      continue;
-    }
-    const uint32_t b = cb[k], p = cp[k] - probe_base;
-    int r = eval_group<kG>(B, b, P, p, predicate, esc, gm, gl);
-    if (gl == 0) {
-      pairs++;
-      if (r < 0) {
-        status_fail(st, kUnsupported, k);
-        r = 0;
-      }
-      flags[k] = (uint8_t)r;
-    }
-  }
-  flush_counters(st, esc, pairs);
-}
-
 }  // namespace
 
 // Launch parameters shared by the refine launchers.
@@ -392,12 +251,9 @@ struct RefineLaunch {
   cudaStream_t s;
 };
 // refine_split.cu: the cheap pass then the full pass over its queue
-// (min_blocks 4 or 6); group (4, 8, 16) runs the full pass with that many
-// lanes per queued pair, 0 with one
-void launch_refine_split(const RefineLaunch& a, int min_blocks, int group = 0);
-// refine_group.cu: kG lanes per pair (group 4, 8 or 16)
-void launch_refine_group(const RefineLaunch& a, int group, int min_blocks);
-// refine_blocks.cu: one pass, FP32 form built for min_blocks 2, 3, 5 or 6
-void launch_refine_blocks(const RefineLaunch& a, int min_blocks);
+// (min_blocks 4 or 6)
+void launch_refine_split(const RefineLaunch& a, int min_blocks);
+// refine_blocks.cu: one pass, FP32 form built for 6 resident blocks per SM
+void launch_refine_blocks6(const RefineLaunch& a);
 
 }  // namespace spj

@@ -242,7 +242,7 @@ void StreamJoin::build_graph(int predicate) {
   if (cperm) SPJ_CUDA(cudaMemsetAsync(flags_.get(), 0, ccap_ + 1, s_));
   refine_relation(B, P, cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), ccap_, 0, predicate,
                   cfg.refine_form, flags_.as<uint8_t>(), st, s_, d_m, cperm,
-                  refine_blocks(cfg.refine_min_blocks, false), cfg.refine_group);
+                  refine_blocks(cfg.refine_min_blocks, false));
   scan_u8_u64(flags_.as<uint8_t>(), pos_.as<uint64_t>(), (int64_t)ccap_, sums2_, s_);
   compact_pairs(cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), flags_.as<uint8_t>(),
                 pos_.as<uint64_t>(), ccap_, out_b_.as<uint32_t>(), out_p_.as<uint32_t>(), s_,

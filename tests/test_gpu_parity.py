@@ -197,22 +197,16 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     else:
         inp, pred, d = datagen.workload4(n_probe=20000, n_build=20000), "dwithin", 250.0
     out = {}
-    # (probe_order, candidate_order, refine_min_blocks, refine_group, cell_grid,
-    #  refine_split)
-    variants = [(-1, 0, 4, 0, 0, 0), (1, 1, 2, 0, 1, 1), (1, 2, 6, 0, 1, 0), (1, 0, 4, 8, 1, 1),
-                (1, 2, 2, 4, 0, 1), (-1, 2, 4, 16, 1, 1), (1, 3, 0, 0, 1, 1),
-                (0, 2, 0, 0, 1, 1), (-1, 0, 4, 0, 1, 1), (1, 2, 6, 0, 0, 1), (1, 3, 0, 0, 1, 2),
-                (-1, 0, 0, 0, 1, 2), (1, 4, 0, 0, 1, 2), (-1, 4, 4, 0, 0, 1),
-                (1, 3, 6, 0, 1, 1, 8), (-1, 0, 4, 0, 1, 1, 4), (1, 2, 0, 0, 0, 1, 16)]
+    # (probe_order, candidate_order, refine_min_blocks, cell_grid, refine_split)
+    variants = [(-1, 0, 4, 0, 0), (1, 2, 6, 1, 0), (1, 3, 0, 1, 1), (0, 2, 0, 1, 1),
+                (-1, 0, 4, 1, 1), (1, 2, 6, 0, 1), (1, 3, 0, 1, 2), (-1, 0, 0, 1, 2),
+                (-1, 2, 4, 0, 1), (1, 0, 6, 1, 1)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
         j.set_option("refine_min_blocks", v[2])
-        j.set_option("refine_group", v[3])
-        j.set_option("cell_grid", v[4])
-        j.set_option("refine_split", v[5])
-        if len(v) > 6:
-            j.set_option("refine_split_group", v[6])
+        j.set_option("cell_grid", v[3])
+        j.set_option("refine_split", v[4])
         j.build(inp.build)
         out[v] = j.probe(inp.probe, pred, distance=d)
     for v in variants[1:]:
