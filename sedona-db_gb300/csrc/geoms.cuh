@@ -18,6 +18,15 @@
 //   ring_rect[nrings]       f64x4 exact vertex bounds of the ring
 //   xy[nverts]              f64x2 vertices (16 B, one 128-bit load each)
 //   xy32[nverts]            f32x2 the same vertices rounded to nearest
+//   row_flags[n]            u8   bit 0: a multipolygon row had parts without
+//                           rings (those parts are not stored; tg keeps them
+//                           as empty children, which a polygon covering the
+//                           row must also cover, tg.c:5872-5897)
+//   ring_flags[nrings]      u8   tg's ring flags (tg.c:1910-2113): bit 0
+//                           convex, bit 1 clockwise, bit 7 set once computed
+//                           (build_ring_flags; absent for columns that did
+//                           not need them, in which case the relate code
+//                           computes a ring's flags where it uses them)
 // and, for a build side that is refined against, a per-ring y-band edge index
 // (band_*), see refine.cu, and a per-ring cell grid (grid_*): a G x G grid
 // over the ring's rect whose clean cells (no edge touches the closed cell)
@@ -44,6 +53,8 @@ struct GeomsView {
   const float4* ring_rect32 = nullptr;  // the same rect rounded to nearest
   const double2* xy = nullptr;
   const float2* xy32 = nullptr;
+  const uint8_t* row_flags = nullptr;   // nullptr: no row had empty parts
+  const uint8_t* ring_flags = nullptr;  // nullptr: not computed
   // y-band edge index (nullptr when not built)
   const uint32_t* ring_bands = nullptr;  // nrings+1: start of each ring's band_off slice
   const uint32_t* band_off = nullptr;    // per ring: nb+1 offsets into band_edges
@@ -68,6 +79,8 @@ struct DeviceGeoms {
   bool any_polys = false;
   DevBuf kind, pt, box, row_part, part_ring, ring_vtx, ring_nsegs, ring_rect, ring_rect32, xy,
       xy32;
+  DevBuf row_flags, ring_flags;
+  bool has_row_flags = false, has_ring_flags = false;
   DevBuf ring_bands, band_off, band_edges, band_seg, band_param;
   bool has_bands = false;
   DevBuf grid_meta, grid_rect, grid_status;
@@ -90,6 +103,8 @@ struct DeviceGeoms {
     v.ring_rect32 = ring_rect32.as<float4>();
     v.xy = xy.as<double2>();
     v.xy32 = xy32.as<float2>();
+    if (has_row_flags) v.row_flags = row_flags.as<uint8_t>();
+    if (has_ring_flags) v.ring_flags = ring_flags.as<uint8_t>();
     if (has_bands) {
       v.ring_bands = ring_bands.as<uint32_t>();
       v.band_off = band_off.as<uint32_t>();
@@ -107,7 +122,7 @@ struct DeviceGeoms {
   size_t device_bytes() const {
     return kind.size() + pt.size() + box.size() + row_part.size() + part_ring.size() +
            ring_vtx.size() + ring_nsegs.size() + ring_rect.size() + ring_rect32.size() +
-           xy.size() + xy32.size() +
+           xy.size() + xy32.size() + row_flags.size() + ring_flags.size() +
            ring_bands.size() + band_off.size() + band_edges.size() + band_seg.size() +
            band_param.size() +
            grid_meta.size() + grid_rect.size() + grid_status.size();
@@ -135,6 +150,10 @@ struct DecodeScratch {
 // malformed WKB (message names the first bad row).
 void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& scratch,
                 bool points_hint, cudaStream_t s);
+
+// tg's convex / clockwise flags of every ring (ring_flags); cheap, but only
+// the polygon-polygon relations other than intersects read them.
+void build_ring_flags(DeviceGeoms& g, cudaStream_t s);
 
 // Build the per-ring y-band edge index used by the banded refine kernels.
 void build_band_index(DeviceGeoms& g, DecodeScratch& scratch, cudaStream_t s);

@@ -157,8 +157,10 @@ __device__ __forceinline__ void pip_seg_f64(double2 a, double2 b, double2 p, int
       if (idx == -1) in = !in;
       break;
     case kOn:
+      // tg keeps the last ON segment of its visit in index order; the
+      // largest index is that segment whatever order the caller visits in
       in = aoe;
-      idx = i;
+      if (i > idx) idx = i;
       break;
     default:
       break;
@@ -330,9 +332,8 @@ __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r
 // Without a band index on this column the ring's segments are all scanned
 // (still with the FP32 classifier).  The answer does not depend on the
 // order of the visits: any ON segment makes it allow_on_edge, else it is the
-// parity of the IN segments (tg.c:2668-2735).  Banded entries are visited by
-// xmax descending, so idx is an ON segment, not necessarily tg's last one
-// (no caller reads it).
+// parity of the IN segments (tg.c:2668-2735).  idx is tg's: the largest ON
+// segment index (tg visits in index order and keeps the last).
 __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r, double2 p,
                                                  float2 p32, bool aoe, uint32_t& esc,
                                                  bool use_grid = true) {

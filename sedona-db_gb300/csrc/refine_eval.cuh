@@ -8,6 +8,7 @@
 #include "predicates.cuh"
 #include "prims.cuh"
 #include "refine.cuh"
+#include "relate.cuh"
 
 #include <cmath>
 
@@ -33,7 +34,8 @@ __device__ __forceinline__ uint32_t nparts(const GeomsView& G, uint32_t i) {
 
 // tg.c:5740-5760 intersects dispatch.  kCheap: ring pairs may come back
 // kDeferred (see ring_intersects_ring); the pair is then deferred unless
-// another ring pair already decides it true.
+// another ring pair already decides it true.  Parts with holes take tg's
+// polygon path (relate.cuh).
 template <bool kFast, bool kCheap = false>
 __device__ int g_intersects(const GeomsView& GA, uint32_t ia, const GeomsView& GB, uint32_t ib,
                             uint32_t& esc) {
@@ -50,7 +52,7 @@ __device__ int g_intersects(const GeomsView& GA, uint32_t ia, const GeomsView& G
       if (poly_contains_point<kFast>(GY, q, p, p32, true, esc)) return 1;
     return 0;
   }
-  bool unsupported = false, deferred = false;
+  bool deferred = false;
   for (uint32_t qa = GA.row_part[ia]; qa < GA.row_part[ia + 1]; qa++) {
     const uint32_t ra = GA.part_ring[qa];
     const bool sa = GA.part_ring[qa + 1] - ra == 1;
@@ -58,7 +60,7 @@ __device__ int g_intersects(const GeomsView& GA, uint32_t ia, const GeomsView& G
       const uint32_t rb = GB.part_ring[qb];
       const bool sb = GB.part_ring[qb + 1] - rb == 1;
       if (!(sa && sb)) {
-        unsupported = true;
+        if (poly_intersects_poly<kFast>(GA, qa, GB, qb, esc)) return 1;
         continue;
       }
       const int r = ring_intersects_ring<kFast, kCheap>(GA, ra, GB, rb, esc);
@@ -66,8 +68,7 @@ __device__ int g_intersects(const GeomsView& GA, uint32_t ia, const GeomsView& G
       if (r == kDeferred) deferred = true;
     }
   }
-  if (deferred) return kDeferred;
-  return unsupported ? kUnsupportedResult : 0;
+  return deferred ? kDeferred : 0;
 }
 
 // tg.c:6538-6556 contains dispatch (point 'other' cases)
@@ -85,7 +86,7 @@ __device__ int g_contains(const GeomsView& GA, uint32_t ia, const GeomsView& GB,
       if (poly_contains_point<kFast>(GA, q, p, p32, false, esc)) return 1;
     return 0;
   }
-  return kUnsupportedResult;
+  return row_contains_rows<kFast>(GA, ia, GB, ib, esc);
 }
 
 // tg.c:6028-6046 covers dispatch
@@ -102,15 +103,20 @@ __device__ int g_covers(const GeomsView& GA, uint32_t ia, const GeomsView& GB, u
       if (poly_contains_point<kFast>(GA, q, p, p32, true, esc)) return 1;
     return 0;
   }
-  if (ka == kPoint && kb == kPolygon) {
-    // tg.c:1152-1155: the polygon's rect is the point itself
-    const uint32_t r = GB.part_ring[GB.row_part[ib]];
-    if (ring_npts(GB, r) < 3) return 0;
-    const Rect64 R = GB.ring_rect[r];
+  if (ka == kPoint) {
+    // tg.c:1152-1155 per part: the part's rect is the point itself (every
+    // part; an empty part of a multipolygon fails, tg.c:5770-5795)
+    if (has_empty_parts(GB, ib)) return 0;
     const double2 p = GA.pt[ia];
-    return pteq(p, make_double2(R.x, R.y)) && pteq(p, make_double2(R.z, R.w));
+    for (uint32_t q = GB.row_part[ib]; q < GB.row_part[ib + 1]; q++) {
+      const uint32_t r = GB.part_ring[q];
+      if (ring_npts(GB, r) < 3) return 0;
+      const Rect64 R = GB.ring_rect[r];
+      if (!(pteq(p, make_double2(R.x, R.y)) && pteq(p, make_double2(R.z, R.w)))) return 0;
+    }
+    return 1;
   }
-  return kUnsupportedResult;
+  return row_covers_rows<kFast>(GA, ia, GB, ib, esc);
 }
 
 // tg.c:6771-6789 touches dispatch
@@ -124,11 +130,14 @@ __device__ int g_touches(const GeomsView& GA, uint32_t ia, const GeomsView& GB, 
     const double2 p = GB.pt[ib];
     return poly_touches_point<kFast>(GA, GA.row_part[ia], p, pt32(GB, ib), esc);
   }
-  if (ka == kPoint && kb == kPolygon) {
+  if (ka == kPoint) {
+    // tg_point_touches_poly per part, any part (tg.c:6575-6625)
     const double2 p = GA.pt[ia];
-    return poly_touches_point<kFast>(GB, GB.row_part[ib], p, pt32(GA, ia), esc);
+    for (uint32_t q = GB.row_part[ib]; q < GB.row_part[ib + 1]; q++)
+      if (poly_touches_point<kFast>(GB, q, p, pt32(GA, ia), esc)) return 1;
+    return 0;
   }
-  return kUnsupportedResult;
+  return row_touches_row<kFast>(GA, ia, GB, ib, esc);
 }
 
 template <bool kFast, bool kCheap = false>
@@ -138,8 +147,8 @@ __device__ int eval(const GeomsView& B, uint32_t b, const GeomsView& P, uint32_t
     case kIntersects:
       return g_intersects<kFast, kCheap>(B, b, P, p, esc);
     case kDisjoint: {
-      int r = g_intersects<kFast, kCheap>(B, b, P, p, esc);
-      return r < 0 ? r : !r;
+      const int r = g_intersects<kFast, kCheap>(B, b, P, p, esc);
+      return r == kDeferred ? r : !r;
     }
     case kContains:
       return g_contains<kFast>(B, b, P, p, esc);

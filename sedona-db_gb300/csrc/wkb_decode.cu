@@ -19,6 +19,7 @@
 // (f32) out; per row 16 B box + 16 B point + 1 B kind out.
 #include "geoms.cuh"
 #include "prims.cuh"
+#include "relate_flags.cuh"
 #include "wkb_read.cuh"
 
 namespace spj {
@@ -79,12 +80,15 @@ template <bool kOff64>
 __global__ void k_wkb_count(WkbDeviceColumn col, bool al, uint8_t* __restrict__ kind,
                             double2* __restrict__ pt, float4* __restrict__ box,
                             uint32_t* __restrict__ cparts, uint32_t* __restrict__ crings,
-                            uint32_t* __restrict__ cverts, DeviceStatus* st, bool points_only) {
+                            uint32_t* __restrict__ cverts, DeviceStatus* st, bool points_only,
+                            uint8_t* __restrict__ rflags = nullptr,
+                            unsigned long long* __restrict__ any_rflag = nullptr) {
   const uint8_t* d = col.data;
   const double qnan = __longlong_as_double(0x7ff8000000000000ll);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < col.n;
        i += (int64_t)gridDim.x * blockDim.x) {
     uint8_t k = kEmpty;
+    bool empty_part = false;
     uint32_t np = 0, nr = 0;
     uint64_t nv = 0;
     double2 q = make_double2(qnan, qnan);
@@ -149,6 +153,8 @@ __global__ void k_wkb_count(WkbDeviceColumn col, bool al, uint8_t* __restrict__ 
                 np++;
                 nr += rings;
                 nv += verts;
+              } else if (code == kOk) {
+                empty_part = true;  // skipped; remembered for covers / contains
               }
             }
             if (code == kOk && np > 0) k = kMultiPolygon;
@@ -172,6 +178,11 @@ __global__ void k_wkb_count(WkbDeviceColumn col, bool al, uint8_t* __restrict__ 
       cparts[i] = np;
       crings[i] = nr;
       cverts[i] = (uint32_t)nv;
+    }
+    if (rflags) {
+      const bool f = empty_part && k == kMultiPolygon;
+      rflags[i] = f ? 1 : 0;
+      if (f) atomicOr(any_rflag, 1ull);
     }
   }
 }
@@ -314,6 +325,18 @@ __global__ void k_row_box(uint32_t n, const uint8_t* __restrict__ kind,
     outward(mnx, mxx, b.x, b.z);
     outward(mny, mxy, b.y, b.w);
     box[i] = b;
+  }
+}
+
+// tg's ring flags (tg.c:1910-2113 process_points), one thread per ring
+// (tg_ring_flags in relate_flags.cuh: the same walk as tg, in its order).
+__global__ void k_ring_flags(uint32_t nrings, const uint32_t* __restrict__ ring_vtx,
+                             const double2* __restrict__ xy, uint8_t* __restrict__ flags) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrings;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t V = ring_vtx[r];
+    const uint32_t npts = ring_vtx[r + 1] - V - 1;  // as stored in the WKB
+    flags[r] = tg_ring_flags(xy + V, npts);
   }
 }
 
@@ -523,6 +546,8 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
       out.ring_vtx.reserve(4, s);
       SPJ_CUDA(cudaMemsetAsync(out.ring_vtx.get(), 0, 4, s));
       out.has_bands = false;
+      out.has_row_flags = false;
+      out.has_ring_flags = false;
       return;
     }
     // a non-point row: fall through to the general path
@@ -537,19 +562,25 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
   uint64_t* sring = spart + (n + 1);
   uint64_t* svert = sring + (n + 1);
   reset_status(sc.status, s);
+  out.row_flags.reserve(n + 1, s);
+  // counters[7] of the status word: set when some row had empty parts
+  unsigned long long* any_rflag = &sc.status.as<DeviceStatus>()->counters[7];
   if (col.offsets64)
     k_wkb_count<true><<<grid, block, 0, s>>>(col, al, out.kind.as<uint8_t>(), out.pt.as<double2>(),
                                              out.box.as<float4>(), cparts, crings, cverts,
-                                             sc.status.as<DeviceStatus>(), false);
+                                             sc.status.as<DeviceStatus>(), false,
+                                             out.row_flags.as<uint8_t>(), any_rflag);
   else
     k_wkb_count<false><<<grid, block, 0, s>>>(col, al, out.kind.as<uint8_t>(),
                                               out.pt.as<double2>(), out.box.as<float4>(), cparts,
-                                              crings, cverts, sc.status.as<DeviceStatus>(), false);
+                                              crings, cverts, sc.status.as<DeviceStatus>(), false,
+                                              out.row_flags.as<uint8_t>(), any_rflag);
   SPJ_CUDA(cudaGetLastError());
   scan_u32_u64(cparts, spart, n, sc.tmp, s);
   scan_u32_u64(crings, sring, n, sc.tmp, s);
   scan_u32_u64(cverts, svert, n, sc.tmp, s);
-  uint64_t tot[3];
+  uint64_t tot[4];
+  SPJ_CUDA(cudaMemcpyAsync(&tot[3], any_rflag, 8, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaMemcpyAsync(&tot[0], spart + n, 8, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaMemcpyAsync(&tot[1], sring + n, 8, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaMemcpyAsync(&tot[2], svert + n, 8, cudaMemcpyDeviceToHost, s));
@@ -562,6 +593,8 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
   out.all_points = out.nparts == 0;
   out.any_points = true;  // conservative; only used as a hint
   out.has_bands = false;
+  out.has_row_flags = tot[3] != 0;
+  out.has_ring_flags = false;
 
   out.row_part.reserve((n + 1) * 4, s);
   k_u64_to_u32<<<grid_for(n + 1, 256), 256, 0, s>>>(spart, out.row_part.as<uint32_t>(), n + 1);
@@ -604,6 +637,15 @@ void decode_wkb(const WkbDeviceColumn& col, DeviceGeoms& out, DecodeScratch& sc,
                                      out.box.as<float4>());
   }
   SPJ_CUDA(cudaGetLastError());
+}
+
+void build_ring_flags(DeviceGeoms& g, cudaStream_t s) {
+  g.ring_flags.reserve((size_t)g.nrings + 1, s);
+  if (g.nrings > 0)
+    k_ring_flags<<<grid_for(g.nrings, 128, kNumSMs * 16), 128, 0, s>>>(
+        g.nrings, g.ring_vtx.as<uint32_t>(), g.xy.as<double2>(), g.ring_flags.as<uint8_t>());
+  SPJ_CUDA(cudaGetLastError());
+  g.has_ring_flags = true;
 }
 
 void build_band_index(DeviceGeoms& g, DecodeScratch& sc, cudaStream_t s) {
