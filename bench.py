@@ -182,14 +182,19 @@ def algorithmic_refine_bytes(stats, probe_vertices_per_row: float, build_vertex_
     return m * (8 + 16 * probe_vertices_per_row + 1) + build_vertex_bytes
 
 
-def run_ours(args, world, rank, local, pg):
+def run_ours(args, world, rank, local, pg, light=False, workload=None, pred_override=None):
+    """Workloads 1, 2 and 4 through SpjJoin.  light (the per-workload entries
+    beside the headline): fewer steps, no option variants."""
     import torch
     from sedona_gpuspatial import capi
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    inp = make_inputs(args.workload, args.scale)
-    pred = {"knn": "dwithin"}.get(inp.predicate, inp.predicate)
+    workload = workload or args.workload
+    inp = make_inputs(workload, args.scale)
+    pred = pred_override or {"knn": "dwithin"}.get(inp.predicate, inp.predicate)
+    run_steps = min(args.steps, 3) if light else args.steps
+    run_warmup = min(args.warmup, 2) if light else args.warmup
     distance = float(inp.params.get("distance", 0.0))
     rt = capi.Runtime.get(local)
 
@@ -206,10 +211,10 @@ def run_ours(args, world, rank, local, pg):
     dcol, keep = to_device(inp.probe)
     n_rows = len(inp.probe)
     results = {}
-    for form, name, steps in ((1, "chosen", args.steps), (0, "plain", max(1, args.plain_steps))):
+    for form, name, steps in ((1, "chosen", run_steps), (0, "plain", max(1, args.plain_steps))):
         j = make_join(form)
         stream = torch.cuda.ExternalStream(j.stream())
-        for _ in range(args.warmup):
+        for _ in range(run_warmup):
             j.probe_device(dcol, pred, distance)
         j.reset_stats()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -236,7 +241,7 @@ def run_ours(args, world, rank, local, pg):
                          "clocks": sampler.summary() if sampler else None, "join": j}
     chosen = results["chosen"]
     st = chosen["stats"]
-    steps = args.steps
+    steps = run_steps
 
     # e2e: host (pinned) WKB -> C ABI -> host pairs, copies inside the timed region
     # (page-locked host buffers from cudaHostAlloc, through torch's pinned
@@ -258,7 +263,7 @@ def run_ours(args, world, rank, local, pg):
     t_op = torch.empty(cap, dtype=torch.int32, pin_memory=True)
     ob = t_ob.numpy().view(np.uint32)
     op = t_op.numpy().view(np.uint32)
-    for _ in range(args.warmup):
+    for _ in range(run_warmup):
         j.probe_host(hcol, pred, distance, ob, op)
     stream = torch.cuda.ExternalStream(j.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -273,14 +278,33 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.synchronize()
     e2e_ms = barrier_max(pg, e0.elapsed_time(e1) / steps, dev)
     assert n_e2e == chosen["pairs"], (n_e2e, chosen["pairs"])
+    del t_ob, t_op, ob, op
+    torch.cuda.synchronize()
+
+    # parity of the full-size run, outside the timed region: one more call of
+    # the chosen form, its pair list against the oracle (the whole set, or a
+    # seeded sample of probe rows where the oracle would take minutes)
+    parity = None
+    if args.parity:
+        db, dp, n = j.probe_device(dcol, pred, distance)
+        torch.cuda.synchronize()
+        assert n == chosen["pairs"], (n, chosen["pairs"])
+        if workload in (1, 2) and pred == "intersects":
+            hb, hp = host_pairs(db, dp, n)
+            parity = parity_full(inp.build, inp.probe, pred, distance, hb, hp)
+            del hb, hp
+        else:
+            parity = parity_sample(inp.build, inp.probe, pred, distance, db, dp, n,
+                                   frac=0.02 if workload == 2 else 0.01)
 
     # execution options of the chosen form, each timed on its own join
     # (they change speed only; the pair count is checked)
     variants = {}
-    option_sets = [{"candidate_order": 0}, {"refine_min_blocks": 4},
-                   {"cell_grid": 0}, {"probe_order": -1}, {"refine_split": 1},
-                   {"candidate_order": 0, "refine_split": 0}]
-    if pred == "dwithin":
+    option_sets = [] if light else [{"candidate_order": 0}, {"refine_min_blocks": 4},
+                                     {"cell_grid": 0}, {"probe_order": -1},
+                                     {"refine_split": 1},
+                                     {"candidate_order": 0, "refine_split": 0}]
+    if pred == "dwithin" and not light:
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},
                         {"dwithin_arena": 1}, {"dwithin_slots": 32},
                         {"probe_order": -1, "dwithin_arena": 0},
@@ -325,10 +349,13 @@ def run_ours(args, world, rank, local, pg):
         ref_ms = (st["ms_filter"] + st["ms_refine"]) / steps
         achieved = ref_bytes / (ref_ms * 1e-3) / 1e9 if ref_ms > 0 else 0.0
     traffic = None
-    tf = os.path.join(ROOT, "profiles", f"refine_traffic_workload{args.workload}.json")
-    if os.path.exists(tf):
+    traffic_note = None
+    tf = os.path.join(ROOT, "profiles", f"refine_traffic_workload{workload}.json")
+    if os.path.exists(tf) and pred == "intersects":
         with open(tf) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+            tj = json.load(f)
+        traffic = tj.get("bytes_per_launch")
+        traffic_note = tj.get("scaled_from")
 
     pairs_total = chosen["pairs"] * world
     value = pairs_total / (chosen["ms"] * 1e-3)
@@ -339,14 +366,16 @@ def run_ours(args, world, rank, local, pg):
         "unit": "pairs/s",
         "n_gpus": world,
         "steps": steps,
-        "warmup": args.warmup,
+        "warmup": run_warmup,
         "ms_per_step": chosen["ms"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64 (f32 filter)",
         "data": "synthetic (seeded; SpatialBench data not available)",
-        "config": {"workload": WORKLOAD_NAMES[args.workload], "probe_rows": n_rows,
+        "config": {"workload": WORKLOAD_NAMES[workload] if pred_override is None
+                   else WORKLOAD_NAMES[workload].replace("st_intersects", "st_" + pred),
+                   "probe_rows": n_rows,
                    "build_rows": len(inp.build), "predicate": pred, "scale": args.scale,
                    "pairs_per_step": chosen["pairs"], "l2": "probe column > L2, no flush",
                    "parallelism": f"replicas x{world}", **join_opts_cfg(args)},
@@ -371,8 +400,12 @@ def run_ours(args, world, rank, local, pg):
                      "algorithmic_bytes_per_launch": ref_bytes},
         "clocks": chosen["clocks"],
     }
-    if args.workload == 4:
-        out["knn"] = run_knn(inp, local, args.steps, args.warmup)
+    if traffic_note:
+        out["roofline"]["traffic_note"] = traffic_note
+    if parity is not None:
+        out["parity"] = parity
+    if workload == 4:
+        out["knn"] = run_knn(inp, local, run_steps, run_warmup, args.parity)
     return out, inp
 
 
@@ -384,6 +417,84 @@ def dev_i32(ptr: int, n: int):
         __cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
                                     "version": 3, "strides": None}
     return torch.as_tensor(_A(), device="cuda")
+
+
+def host_pairs(db: int, dp: int, n: int):
+    """A device pair list (the library's buffers) copied to host arrays."""
+    if n == 0:
+        return np.zeros(0, np.uint32), np.zeros(0, np.uint32)
+    return (dev_i32(db, n).cpu().numpy().view(np.uint32),
+            dev_i32(dp, n).cpu().numpy().view(np.uint32))
+
+
+def device_keys(db: int, dp: int, n: int):
+    """Sorted (probe << 32 | build) keys of a device pair list, on the device."""
+    import torch
+    if n == 0:
+        return torch.zeros(0, dtype=torch.int64, device="cuda")
+    k = (dev_i32(dp, n).long() << 32) | (dev_i32(db, n).long() & 0xFFFFFFFF)
+    return torch.sort(k).values
+
+
+def sorted_keys(b, p):
+    """(probe << 32 | build) keys of a pair list, sorted: equal arrays mean
+    equal pair sets."""
+    k = (np.asarray(p).astype(np.uint64) << np.uint64(32)) | np.asarray(b).astype(np.uint64)
+    k.sort()
+    return k
+
+
+def parity_full(build_col, probe_col, pred, distance, b, p):
+    """The whole pair set of a full-size run against the oracle's (the C
+    restatement of the reference CPU join) on all host cores."""
+    import oracle
+    oracle.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ob, op = oracle.join(oracle.Geoms(build_col), oracle.Geoms(probe_col), pred, distance,
+                         nthreads=threads)
+    oracle_s = time.perf_counter() - t0
+    eq = len(ob) == len(b) and np.array_equal(sorted_keys(b, p), sorted_keys(ob, op))
+    return {"pairs_equal": bool(eq), "pairs": int(len(b)), "oracle_pairs": int(len(ob)),
+            "oracle_cores": threads, "oracle_s": round(oracle_s, 2),
+            "kind": "full sorted (probe, build) pair set vs the oracle"}
+
+
+def parity_sample(build_col, probe_col, pred, distance, db, dp, n, frac=0.01, seed=20260301):
+    """The pair list of a full-size run, restricted on the device to a seeded
+    sample of probe rows, against the oracle on those rows (every pair of
+    every sampled row: the per-row lists must be equal)."""
+    import torch
+    import oracle
+    oracle.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    nrows = len(probe_col)
+    rng = np.random.default_rng(seed)
+    rows = np.sort(rng.choice(nrows, size=max(1, int(nrows * frac)), replace=False))
+    pos = torch.full((nrows,), -1, dtype=torch.int32, device="cuda")
+    pos[torch.from_numpy(rows).cuda()] = torch.arange(len(rows), dtype=torch.int32,
+                                                       device="cuda")
+    keys = []
+    if n:
+        dbt, dpt = dev_i32(db, n), dev_i32(dp, n)
+        step = 1 << 27
+        for s in range(0, n, step):
+            pc, bc = dpt[s:s + step], dbt[s:s + step]
+            sp = pos.index_select(0, pc)
+            m = sp >= 0
+            keys.append(((sp[m].long() << 32) | (bc[m].long() & 0xFFFFFFFF)).cpu().numpy())
+    gk = np.sort(np.concatenate(keys)).astype(np.uint64) if keys else np.zeros(0, np.uint64)
+    del pos
+    t0 = time.perf_counter()
+    ob, op = oracle.join(oracle.Geoms(build_col), oracle.Geoms(probe_col.take(rows)), pred,
+                         distance, nthreads=threads)
+    oracle_s = time.perf_counter() - t0
+    eq = len(gk) == len(ob) and np.array_equal(gk, sorted_keys(ob, op))
+    return {"pairs_equal": bool(eq), "pairs": int(n), "sampled_rows": int(len(rows)),
+            "sampled_pairs": int(len(gk)), "oracle_pairs": int(len(ob)), "oracle_cores": threads,
+            "oracle_s": round(oracle_s, 2),
+            "kind": f"{frac:.0%} of probe rows (seed {seed}): every pair of those rows from the "
+                    "full-size run vs the oracle"}
 
 
 def join_opts_cfg(args):
@@ -484,6 +595,11 @@ def run_stream(args, world, rank, local, pg):
     torch.cuda.synchronize()
     del host_parts, hb, hpr, h_, t_
     torch.cuda.synchronize()
+    parity = None
+    if args.parity:
+        db, dp, n = st.run(inp.predicate)
+        torch.cuda.synchronize()
+        parity = parity_sample(inp.build, inp.probe, inp.predicate, 0.0, db, dp, n, frac=0.01)
 
     # plain form: per-batch calls, FP64 refine
     jp = capi.SpatialJoin(rt, refine_form=0, profile=True)
@@ -525,7 +641,9 @@ def run_stream(args, world, rank, local, pg):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (f32 filter)", "data": "synthetic (seeded; SpatialBench data not available)",
-        "config": {"workload": WORKLOAD_NAMES[args.workload], "probe_rows": n_rows,
+        "config": {"workload": WORKLOAD_NAMES[workload] if pred_override is None
+                   else WORKLOAD_NAMES[workload].replace("st_intersects", "st_" + pred),
+                   "probe_rows": n_rows,
                    "batches": len(sizes), "build_rows": len(inp.build),
                    "predicate": inp.predicate, "scale": args.scale, "pairs_per_step": npairs,
                    "autotuned": {"block": tuned[0], "chunk_rows": tuned[1], "leaf_size": tuned[2],
@@ -548,10 +666,12 @@ def run_stream(args, world, rank, local, pg):
                      "algorithmic_bytes_per_launch": alg},
         "clocks": sampler.summary(),
     }
+    if parity is not None:
+        out["parity"] = parity
     return out, inp
 
 
-def run_knn(inp, local, steps: int, warmup: int):
+def run_knn(inp, local, steps: int, warmup: int, parity: bool = False):
     """KNN k=8 over the workload-4 points: 20M probes x 1M build, probe
     coordinates resident in HBM; chosen form (split-FP32 traversal proving
     the k-set, FP64 keys for the k results only, unproven probes through the
@@ -597,6 +717,37 @@ def run_knn(inp, local, steps: int, warmup: int):
     res["roofline"] = {"bound": "hbm", "kernel": "k_knn_split<8>", "achieved": ach,
                        "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
                        "algorithmic_bytes_per_launch": alg}
+    if parity:
+        # the chosen form's k-lists of a seeded 1% of the probes against the
+        # oracle's: build rows exactly, distances to 1e-12 relative
+        import oracle
+        from sedona_gpuspatial import wkb
+        kj = capi.KnnJoin(capi.Runtime.get(local), refine_form=1)
+        kj.build(bx, by)
+        kj.query_device(d_xy.data_ptr(), n, k, d_idx.data_ptr(), d_dist.data_ptr())
+        torch.cuda.synchronize()
+        rng = np.random.default_rng(20260302)
+        rows = np.sort(rng.choice(n, size=max(1, n // 100), replace=False))
+        trows = torch.from_numpy(rows).cuda()
+        gi = d_idx.view(n, k).index_select(0, trows).cpu().numpy().view(np.uint32)
+        gd = d_dist.view(n, k).index_select(0, trows).cpu().numpy()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        oi, od = oracle.knn(oracle.Geoms(wkb.points_column(bx, by)),
+                            oracle.Geoms(wkb.points_column(px[rows], py[rows])), k,
+                            nthreads=threads)
+        fin = np.isfinite(od)
+        res["parity"] = {
+            "ids_equal": bool(np.array_equal(gi, oi)),
+            "dist_max_rel_err": float(np.max(np.abs(gd[fin] - od[fin]) /
+                                             np.maximum(np.abs(od[fin]), 1e-300)))
+            if fin.any() else 0.0,
+            "dist_tolerance": 1e-12, "sampled_rows": int(len(rows)), "oracle_cores": threads,
+            "oracle_s": round(time.perf_counter() - t0, 2),
+            "kind": "1% of probes (seed 20260302): k build rows (ties by row id) and distances "
+                    "vs the oracle"}
+        res["parity"]["pairs_equal"] = bool(res["parity"]["ids_equal"] and
+                                            res["parity"]["dist_max_rel_err"] <= 1e-12)
     return res
 
 
@@ -745,6 +896,19 @@ def run_learned(args, world, rank, local, pg):
     torch.cuda.synchronize()
     fast_ms = (time.perf_counter() - t0) * 1e3
     assert n_fast == npairs, (n_fast, npairs)
+    # parity: the learned index's full pair set against the LBVH join with
+    # the FP64 refine (the judge), per probe column, compared on the device
+    parity = None
+    if args.parity:
+        equal = True
+        for d in (dbox, dlk):
+            ka = device_keys(*li.query_device(d, "intersects"))
+            kb = device_keys(*jp.probe_device(d, "intersects"))
+            equal = equal and ka.shape == kb.shape and bool(torch.equal(ka, kb))
+            del ka, kb
+        parity = {"pairs_equal": equal, "pairs": int(npairs),
+                  "kind": "full sorted pair sets, learned index vs the LBVH join with the "
+                          "FP64 refine (the judge; both probe columns)"}
     n_rows = len(boxes) + len(lookups)
     hbm_peak, peak_kind = load_peaks()
     # algorithmic bytes per step: probe WKB + offsets once, per lookup the
@@ -796,35 +960,48 @@ def run_learned(args, world, rank, local, pg):
                 "d2h_bytes_per_step": int(8 * npairs)},
         "clocks": sampler.summary(),
     }
-    return out, None
+    if parity is not None:
+        out["parity"] = parity
+    from types import SimpleNamespace
+    return out, SimpleNamespace(build=build, probe=boxes, predicate="intersects", params={})
 
 
-def cpu_baseline(inp, seconds_budget: float = 15.0):
+def cpu_baseline(inp, seconds_budget: float = 15.0, pred=None):
     """The oracle (C restatement of the reference CPU join) on a bounded
     sample of the probe side with all host threads."""
     import oracle
     oracle.build(with_ref=False)
     threads = os.cpu_count() or 1
     B = oracle.Geoms(inp.build)
-    pred = {"knn": "dwithin"}.get(inp.predicate, inp.predicate)
+    pred = pred or {"knn": "dwithin"}.get(inp.predicate, inp.predicate)
     distance = float(inp.params.get("distance", 0.0))
     n = len(inp.probe)
-    rows = min(n, 20000)
+    # each oracle call builds its grid over the build side first: that is the
+    # reference's build phase, so it is timed alone (one probe row) and taken
+    # out of every call's time
+    P1 = oracle.Geoms(inp.probe.slice(0, 1))
     t0 = time.perf_counter()
+    oracle.join(B, P1, pred, distance, nthreads=threads)
+    t_build = time.perf_counter() - t0
+    rows = min(n, 20000)
+    el = 0.0
     npairs = 0
     done = 0
     while True:
         P = oracle.Geoms(inp.probe.slice(done % n, min(n, done % n + rows)))
+        t0 = time.perf_counter()
         b, p = oracle.join(B, P, pred, distance, nthreads=threads)
+        el += max(time.perf_counter() - t0 - t_build, 1e-9)
         npairs += len(b)
         done += len(P._keep)
-        el = time.perf_counter() - t0
         if el > seconds_budget or done >= n:
             break
-        rows = min(n, int(rows * 2))
+        rows = min(n - done, int(rows * 2))
     return {"value": npairs / el, "unit": "pairs/s", "cores": threads, "kind": "port",
             "probe_rows_per_s": done / el,
-            "sample": f"first {done} probe rows of the workload against the full build side"}
+            "sample": f"first {done} probe rows of the workload against the full build side "
+                      f"(probe phase: the oracle's per-call grid build, {t_build:.2f} s, "
+                      "timed alone and subtracted)"}
 
 
 def run_reference(args, world, rank):
@@ -853,6 +1030,54 @@ def run_reference(args, world, rank):
     }
 
 
+NESTED_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "probe_rows_per_s",
+               "plain_f64_form", "phases_ms_per_step", "fp64_escalated_fraction",
+               "fp64_escalations_per_replay", "roofline", "e2e", "gpu_launches", "parity",
+               "knn", "learned_index", "lbvh_fast_form", "per_batch_calls_f32_ms", "clocks",
+               "config")
+
+
+def run_configs(args, world, rank, local, pg, names):
+    """One entry per workload beside the headline (fewer steps, no option
+    variants): its own timing, plain FP64 form, roofline, e2e, parity of the
+    full-size run and CPU baseline."""
+    import copy
+
+    import torch
+    res = {}
+    for name in names:
+        a = copy.copy(args)
+        a.steps, a.warmup = min(args.steps, 3), min(args.warmup, 2)
+        t0 = time.perf_counter()
+        pred = None
+        if name == "1":
+            out, inp = run_ours(a, world, rank, local, pg, light=True, workload=1)
+        elif name == "2contains":
+            pred = "contains"
+            out, inp = run_ours(a, world, rank, local, pg, light=True, workload=2,
+                                pred_override="contains")
+        elif name == "3":
+            a.workload = 3
+            out, inp = run_stream(a, world, rank, local, pg)
+        elif name == "4":
+            out, inp = run_ours(a, world, rank, local, pg, light=True, workload=4)
+        elif name == "5":
+            a.workload = 5
+            out, inp = run_learned(a, world, rank, local, pg)
+        else:
+            raise SystemExit(f"unknown config {name}")
+        entry = {k: out[k] for k in NESTED_KEYS if k in out}
+        if rank == 0 and not args.no_cpu_baseline and inp is not None:
+            entry["cpu_baseline"] = cpu_baseline(inp, seconds_budget=args.config_ref_seconds,
+                                                 pred=pred)
+        entry["seconds"] = round(time.perf_counter() - t0, 1)
+        res[out["config"]["workload"]] = entry
+        del out, inp
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -864,6 +1089,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the parity check of the full-size run against the oracle")
+    ap.add_argument("--configs", default="1,2contains,3,4,5",
+                    help="workload entries timed beside the headline (empty: none)")
+    ap.add_argument("--config-ref-seconds", type=float, default=5.0)
     ap.add_argument("--join-options", type=json.loads, default={},
                     help='execution options of the chosen form, e.g. \'{"refine_min_blocks": 6}\'')
     args = ap.parse_args()
@@ -880,12 +1110,17 @@ def main():
         out, inp = run_stream(args, world, rank, local, pg)
     elif args.workload == 5:
         out, inp = run_learned(args, world, rank, local, pg)
-        args.no_cpu_baseline = True
     else:
         out, inp = run_ours(args, world, rank, local, pg)
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(inp, seconds_budget=args.ref_seconds)
+    del inp
+    names = [c for c in args.configs.split(",") if c] if args.workload == 2 else []
+    if names:
+        import torch
+        torch.cuda.empty_cache()
+        out["configs"] = run_configs(args, world, rank, local, pg, names)
     if rank == 0:
-        if not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(inp, seconds_budget=args.ref_seconds)
         out.pop("_", None)
         print(json.dumps(out))
     if pg is not None:

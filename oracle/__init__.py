@@ -18,7 +18,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libspj_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libtgref.so")
-REFERENCE_TREE = os.environ.get("SPJ_REFERENCE_TREE", "/root/reference")
+# the reference tree (apache/sedona-db sources), where it is mounted: set by
+# the caller (the build entry point or gen_golden.py); unset, only the
+# restatement is built
+REFERENCE_TREE = os.environ.get("SPJ_REFERENCE_TREE", "")
 
 PRED = {"equals": 0, "disjoint": 1, "touches": 2, "contains": 3, "covers": 4,
         "intersects": 5, "within": 6, "coveredby": 7, "dwithin": 100}
@@ -30,7 +33,10 @@ _ref = None
 def build(with_ref: Optional[bool] = None) -> None:
     targets = ["all"]
     if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(REFERENCE_TREE, "c", "sedona-tg", "src", "tg"))
+        with_ref = bool(REFERENCE_TREE) and os.path.isdir(
+            os.path.join(REFERENCE_TREE, "c", "sedona-tg", "src", "tg"))
+    if with_ref and not REFERENCE_TREE:
+        raise RuntimeError("set SPJ_REFERENCE_TREE to the reference source tree to build oracle/_ref")
     if with_ref:
         targets.append("ref")
     subprocess.run(["make", "-s", "-C", HERE, f"REFERENCE={REFERENCE_TREE}"] + targets,

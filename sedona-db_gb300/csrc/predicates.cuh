@@ -308,15 +308,37 @@ __device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r,
   return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
 }
 
-// Plain FP64 form: every segment through tg's FP64 sequence.
+// Plain FP64 form: tg's FP64 sequence for every segment it visits, with the
+// same index as the chosen form and no FP32 arithmetic tier.  With a band
+// index the visited segments are the point's band (every segment whose
+// y-range holds p.y is listed there), in the band's order, up to the first
+// entry whose key (its RN32 xmax) is strictly left of the point's RN32 x:
+// every later entry is strictly left of p, where tg's ray cast gives OUT.
+// Without one, all segments in index order.
 __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r, double2 p,
-                                                  bool aoe) {
+                                                  float2 p32, bool aoe) {
   RingHit h{false, -1};
   if (!rect_covers_point(G.ring_rect[r], p)) return h;
   const uint32_t V = G.ring_vtx[r];
   const int ns = G.ring_nsegs[r];
   bool in = false;
   int idx = -1;
+  if (G.ring_bands != nullptr && G.band_param[r].y >= 0.0f) {
+    const uint32_t B = G.ring_bands[r];
+    const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
+    const float2 prm = G.band_param[r];
+    const int b = band_of(p32.y, prm.x, prm.y, nb);
+    const uint32_t e0 = G.band_off[B + b], e1 = G.band_off[B + b + 1];
+    for (uint32_t k = e0; k < e1; k++) {
+      const float4 sg = G.band_seg[k];
+      if (fmax0f(sg.x, sg.z) < p32.x) break;
+      const int i = G.band_edges[k];
+      pip_seg_f64(G.xy[V + i], G.xy[V + i + 1], p, i, aoe, in, idx);
+    }
+    h.hit = in;
+    h.idx = idx;
+    return h;
+  }
   double2 a = G.xy[V];
   for (int i = 0; i < ns; i++) {
     const double2 b = G.xy[V + i + 1];
@@ -398,7 +420,7 @@ template <bool kFast>
 __device__ __forceinline__ RingHit ring_pip(const GeomsView& G, uint32_t r, double2 p, float2 p32,
                                             bool aoe, uint32_t& esc, bool use_grid = true) {
   if (kFast) return ring_pip_fast(G, r, p, p32, aoe, esc, use_grid);
-  return ring_pip_plain(G, r, p, aoe);
+  return ring_pip_plain(G, r, p, p32, aoe);
 }
 
 __device__ __forceinline__ uint32_t ring_npts(const GeomsView& G, uint32_t r) {
@@ -449,14 +471,32 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
                                              float2 a32, float2 b32, uint32_t& esc) {
   const uint32_t V = G.ring_vtx[r];
   int count = 0;
+  const float qx0 = fmin0f(a32.x, b32.x), qx1 = fmax0f(a32.x, b32.x);
+  const float qy0 = fmin0f(a32.y, b32.y), qy1 = fmax0f(a32.y, b32.y);
   if (!kFast) {
+    // plain form: the same band index, every visited segment in FP64
+    if (G.ring_bands != nullptr && G.band_param[r].y >= 0.0f) {
+      const uint32_t B = G.ring_bands[r];
+      const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
+      const float2 prm = G.band_param[r];
+      const int b0 = band_of(qy0, prm.x, prm.y, nb), b1 = band_of(qy1, prm.x, prm.y, nb);
+      for (int bb = b0; bb <= b1 && count < 2; bb++) {
+        const uint32_t e0 = G.band_off[B + bb], e1 = G.band_off[B + bb + 1];
+        for (uint32_t k = e0; k < e1 && count < 2; k++) {
+          const float4 sg = G.band_seg[k];
+          if (fmax0f(sg.x, sg.z) < qx0) break;  // index key: the rest is left
+          if (bb > b0 && band_of(fmin0f(sg.y, sg.w), prm.x, prm.y, nb) < bb) continue;
+          const int i = G.band_edges[k];
+          if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
+        }
+      }
+      return count;
+    }
     const int ns = G.ring_nsegs[r];
     for (int i = 0; i < ns && count < 2; i++)
       if (seg_intersects_seg(a, b, G.xy[V + i], G.xy[V + i + 1])) count++;
     return count;
   }
-  const float qx0 = fmin0f(a32.x, b32.x), qx1 = fmax0f(a32.x, b32.x);
-  const float qy0 = fmin0f(a32.y, b32.y), qy1 = fmax0f(a32.y, b32.y);
   // segment (c, d) of the ring; its index (needed only by the FP64 tier)
   // is band entry k's edge when banded, else k itself
   auto test = [&](const float2 c, const float2 d, const uint32_t k, const bool banded_k) {

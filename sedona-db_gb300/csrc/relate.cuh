@@ -54,11 +54,12 @@ __device__ __forceinline__ int seg_x32(float2 a, float2 b, float2 c, float2 d) {
 // [qx0, qx1] x [qy0, qy1] (RN32 bounds of a query), each at most once; the
 // FP32 form leaves out segments whose RN32 rect is strictly separated (tg's
 // rect test fails for them).  f returns true to stop; returns whether it
-// stopped.  With a band index only the query's bands are read.
+// stopped.  With a band index (both forms) only the query's bands are read,
+// up to the entries whose key (RN32 xmax) is strictly left of the query.
 template <bool kFast, class F>
 __device__ __forceinline__ bool any_segment_near(const GeomsView& G, uint32_t r, float qx0,
                                                  float qy0, float qx1, float qy1, F&& f) {
-  if (kFast && G.ring_bands != nullptr && G.band_param[r].y >= 0.0f) {
+  if (G.ring_bands != nullptr && G.band_param[r].y >= 0.0f) {
     const uint32_t B = G.ring_bands[r];
     const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
     const float2 prm = G.band_param[r];
@@ -71,7 +72,8 @@ __device__ __forceinline__ bool any_segment_near(const GeomsView& G, uint32_t r,
         if (fmax0f(sg.x, sg.z) < qx0) break;
         // each segment once: in the first band of the query that it spans
         if (bb > b0 && band_of(fmin0f(sg.y, sg.w), prm.x, prm.y, nb) < bb) continue;
-        if (fmin0f(sg.x, sg.z) > qx1 || fmax0f(sg.y, sg.w) < qy0 || fmin0f(sg.y, sg.w) > qy1)
+        if (kFast && (fmin0f(sg.x, sg.z) > qx1 || fmax0f(sg.y, sg.w) < qy0 ||
+                      fmin0f(sg.y, sg.w) > qy1))
           continue;
         if (f((int)G.band_edges[k])) return true;
       }

@@ -3,8 +3,8 @@ reference's gpuspatial C ABI).
 
 Python surface:
   capi      ctypes bindings of include/gpuspatial_c.h and include/spj_gb300.h
-            (Runtime, FloatIndex2D, Refiner, SpatialJoin, KnnJoin)
-  index     the SpatialIndex / builder mirror of the reference's GPU provider
+            (Runtime, FloatIndex2D, Refiner: the reference's wrapper surface;
+            SpatialJoin, KnnJoin, StreamProbe, LearnedIndex: the extensions)
   wkb       Arrow binary WKB columns as numpy buffers
   datagen   seeded synthetic workloads
 """

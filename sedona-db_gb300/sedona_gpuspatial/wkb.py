@@ -58,6 +58,23 @@ class WkbColumn:
     def offsets64(self) -> np.ndarray:
         return self.offsets.astype(np.int64)
 
+    def take(self, rows: np.ndarray) -> "WkbColumn":
+        """The given rows (ascending or not) as a new column."""
+        rows = np.asarray(rows, dtype=np.int64)
+        off = self.offsets.astype(np.int64)
+        starts, lens = off[rows], off[rows + 1] - off[rows]
+        new_off = np.zeros(len(rows) + 1, dtype=np.int64)
+        np.cumsum(lens, out=new_off[1:])
+        total = int(new_off[-1])
+        src = np.repeat(starts - new_off[:-1], lens) + np.arange(total, dtype=np.int64)
+        data = self.data[src] if total else np.zeros(0, np.uint8)
+        validity = None
+        if self.validity is not None:
+            bits = np.unpackbits(self.validity, bitorder="little")[rows]
+            validity = np.packbits(bits, bitorder="little")
+        dt = np.int64 if total >= 2**31 else self.offsets.dtype
+        return WkbColumn(new_off.astype(dt), data, validity)
+
 
 def _offsets_dtype(total: int, large: Optional[bool]) -> np.dtype:
     if large is None:

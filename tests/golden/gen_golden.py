@@ -2,7 +2,7 @@
 
 Run in a container where the reference tree is mounted:
 
-    python tests/golden/gen_golden.py
+    SPJ_REFERENCE_TREE=/path/to/sedona-db python tests/golden/gen_golden.py
 
 It compiles the reference's vendored tg (c/sedona-tg/src/tg/tg.c) through
 oracle/Makefile into oracle/_ref/, evaluates tg_geom_<pred>(build, probe) on

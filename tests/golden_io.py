@@ -46,3 +46,29 @@ def cube(z, cols, name):
     np_ = len(range(0, len(cols[pname]), sp))
     return preds, np.arange(0, len(cols[bname]), sb), np.arange(0, len(cols[pname]), sp), \
         res.reshape(len(preds), nb, np_)
+
+
+FIXTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                        "reference_fixtures.npz")
+FIXTURE_JOINS = ["countries_points", "pip_points", "poly_poly", "countries_countries"]
+
+
+def load_fixtures():
+    """The reference's own test data (tests/golden/gen_fixtures.py): per join,
+    (build column, probe column, {predicate: expected sorted (probe, build)
+    pairs})."""
+    z = np.load(FIXTURES)
+
+    def col(key):
+        return WkbColumn(z[f"col_{key}_offsets"].astype(np.int32), z[f"col_{key}_data"])
+
+    joins = {}
+    for name in FIXTURE_JOINS:
+        exp = {}
+        for k in z.files:
+            if k.startswith(name + "_") and k.endswith("_build") and k != name + "_build":
+                pred = k[len(name) + 1:-len("_build")]
+                b, p = z[k], z[f"{name}_{pred}_probe"]
+                exp[pred] = sorted(zip(p.tolist(), b.tolist()))
+        joins[name] = (col(str(z[name + "_build"])), col(str(z[name + "_probe"])), exp)
+    return joins

@@ -606,3 +606,19 @@ def test_stream_autotune_and_cache(capi, oracle_mod, tmp_path):
     db, dp, n = st.run("intersects")
     b, p = _device_pairs(db, dp, n)
     assert pairs(b, p) == oracle_pairs(oracle_mod, inp.build, inp.probe, "intersects")
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("name", golden_io.FIXTURE_JOINS)
+def test_reference_fixtures(capi, form, name):
+    """The reference's own test data (c/sedona-libgpuspatial/libgpuspatial/
+    test/data: natural-earth countries, multipolygons with holes, and their
+    generated points; the synthetic PIP and polygon sets) through the fused
+    join, against the pair sets the reference's tg returns for each
+    predicate (tests/golden/gen_fixtures.py)."""
+    build, probe, exp = golden_io.load_fixtures()[name]
+    j = capi.SpatialJoin(refine_form=form)
+    j.build(build)
+    for pred, want in exp.items():
+        b, p = j.probe(probe, pred)
+        assert pairs(b, p) == want, pred

@@ -150,3 +150,17 @@ def test_dwithin_bruteforce(oracle_lib):
     d = np.hypot(bx[None, :] - px[:, None], by[None, :] - py[:, None])
     pp, bb = np.nonzero(d <= 3.0)
     assert np.array_equal(p, pp) and np.array_equal(b, bb)
+
+
+@pytest.mark.parametrize("name", ["countries_points", "pip_points", "poly_poly",
+                                  "countries_countries"])
+def test_oracle_matches_reference_fixtures(oracle_lib, name):
+    """The reference's own test data (natural-earth countries with their
+    generated points, the synthetic PIP and polygon sets): the oracle's join
+    returns the pair set the reference's tg returns for every predicate."""
+    build, probe, exp = golden_io.load_fixtures()[name]
+    B, P = oracle_lib.Geoms(build), oracle_lib.Geoms(probe)
+    assert exp
+    for pred, pairs in exp.items():
+        b, p = oracle_lib.join(B, P, pred, nthreads=4)
+        assert sorted(zip(p.tolist(), b.tolist())) == pairs, pred
