@@ -301,7 +301,8 @@ def run_ours(args, world, rank, local, pg, light=False, workload=None, pred_over
     # (they change speed only; the pair count is checked)
     variants = {}
     option_sets = [] if light else [{"candidate_order": 0}, {"refine_min_blocks": 4},
-                                     {"cell_grid": 0}, {"probe_order": -1},
+                                     {"cell_grid": 0}, {"grid_rings": 0},
+                                     {"probe_order": -1},
                                      {"refine_split": 1},
                                      {"candidate_order": 0, "refine_split": 0}]
     if pred == "dwithin" and not light:
@@ -641,9 +642,7 @@ def run_stream(args, world, rank, local, pg):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (f32 filter)", "data": "synthetic (seeded; SpatialBench data not available)",
-        "config": {"workload": WORKLOAD_NAMES[workload] if pred_override is None
-                   else WORKLOAD_NAMES[workload].replace("st_intersects", "st_" + pred),
-                   "probe_rows": n_rows,
+        "config": {"workload": WORKLOAD_NAMES[args.workload], "probe_rows": n_rows,
                    "batches": len(sizes), "build_rows": len(inp.build),
                    "predicate": inp.predicate, "scale": args.scale, "pairs_per_step": npairs,
                    "autotuned": {"block": tuned[0], "chunk_rows": tuned[1], "leaf_size": tuned[2],
@@ -1072,6 +1071,10 @@ def run_configs(args, world, rank, local, pg, names):
                                                  pred=pred)
         entry["seconds"] = round(time.perf_counter() - t0, 1)
         res[out["config"]["workload"]] = entry
+        if rank == 0:
+            print(f"[bench] {out['config']['workload']}: {entry['ms_per_step']:.2f} ms/step, "
+                  f"parity {entry.get('parity', {}).get('pairs_equal')}, "
+                  f"{entry['seconds']} s", file=sys.stderr, flush=True)
         del out, inp
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
@@ -1114,6 +1117,9 @@ def main():
         out, inp = run_ours(args, world, rank, local, pg)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(inp, seconds_budget=args.ref_seconds)
+    if rank == 0:
+        print(f"[bench] headline: {out['ms_per_step']:.2f} ms/step, parity "
+              f"{out.get('parity', {}).get('pairs_equal')}", file=sys.stderr, flush=True)
     del inp
     names = [c for c in args.configs.split(",") if c] if args.workload == 2 else []
     if names:

@@ -108,6 +108,9 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
+ *   "grid_rings"        1 (default) / 0: ring-ring and ring-in-ring tests
+ *                       answer from the build ring's clean cells when the
+ *                       probe ring's box lies in them
  *   "dwithin_arena"     2 (default: auto, on when the probes are not in
  *                       Morton order), 1 on, 0 off: fused ST_DWithin keeps
  *                       the results past a probe's slots in an overflow
@@ -288,6 +291,28 @@ int SpjKnnBuild(SpjKnn* knn, const double* xy, uint64_t n);
  * Host or device pointers (device == 1) for all four arrays. */
 int SpjKnnQuery(SpjKnn* knn, const double* probe_xy, uint64_t n_probe, uint32_t k,
                 uint32_t* out_idx, double* out_dist, int32_t device);
+/* The same with variable-length results, as the reference's
+ * query_knn(probe, k, use_spheroid = false, include_tie_breakers, ...)
+ * returns them per probe (rust/sedona-spatial-join/src/index/spatial_index.rs:52-64,
+ * default_spatial_index.rs:306-502): probe i's results are
+ * out_idx / out_dist[offsets[i] .. offsets[i + 1]), its k nearest (fewer when
+ * the build side is smaller; none for a NaN / empty probe) and, with
+ * include_tie_breakers, every other build point whose distance is within
+ * 1e-9 of the k-th (DISTANCE_TOLERANCE, spatial_index.rs:32).  offsets
+ * (n_probe + 1 entries), out_idx and out_dist are host arrays; probe_xy is
+ * host or device memory (device == 1).  *total receives the result count;
+ * if it exceeds capacity, only offsets are written and ENOSPC is returned. */
+int SpjKnnQueryTies(SpjKnn* knn, const double* probe_xy, uint64_t n_probe, uint32_t k,
+                    int32_t include_tie_breakers, int32_t device, uint64_t* offsets,
+                    uint32_t* out_idx, double* out_dist, uint64_t capacity, uint64_t* total);
+/* query_knn over a WKB column (Arrow binary / large_binary, host memory):
+ * the column is decoded on the device; rows must be points, and empty or
+ * null rows get no results (default_spatial_index.rs:331-339).  Outputs as
+ * SpjKnnQueryTies. */
+int SpjKnnQueryArrow(SpjKnn* knn, const struct ArrowSchema* schema,
+                     const struct ArrowArray* array, uint32_t k, int32_t include_tie_breakers,
+                     uint64_t* offsets, uint32_t* out_idx, double* out_dist, uint64_t capacity,
+                     uint64_t* total);
 void* SpjKnnStream(SpjKnn* knn);
 /* Cumulative counters since SpjKnnCreate: probe points queried, FP64
  * distance keys evaluated, and probes whose k-set the FP32 pass could not

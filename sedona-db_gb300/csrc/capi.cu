@@ -796,6 +796,10 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
     } else if (k == "cell_grid") {
       SPJ_CHECK(value == 0 || value == 1, "cell_grid must be 0 or 1");
       c.cell_grid = value != 0;  // takes effect at the next build
+    } else if (k == "grid_rings") {
+      SPJ_CHECK(value == 0 || value == 1, "grid_rings must be 0 or 1");
+      c.grid_rings = value != 0;
+      j->engine->set_grid_rings(c.grid_rings);
     } else if (k == "dwithin_arena") {
       SPJ_CHECK(value >= 0 && value <= 2, "dwithin_arena must be 0, 1 or 2");
       c.dwithin_arena = (int)value;
@@ -1296,6 +1300,7 @@ extern "C" void* SpjLearnedStream(SpjLearned* li) { return (void*)li->ws->stream
 struct SpjKnn {
   RuntimeData* rt = nullptr;
   std::unique_ptr<KnnIndex> index;
+  std::unique_ptr<Workspace> ws;  // staging and decode of WKB probe columns
   std::string last_error;
 };
 
@@ -1337,6 +1342,53 @@ extern "C" int SpjKnnQuery(SpjKnn* k, const double* probe_xy, uint64_t n, uint32
     SPJ_CUDA(cudaSetDevice(k->rt->device_id));
     k->index->query(probe_xy, n, kk, out_idx, out_dist, device != 0);
   });
+}
+
+extern "C" int SpjKnnQueryTies(SpjKnn* k, const double* probe_xy, uint64_t n, uint32_t kk,
+                               int32_t include_tie_breakers, int32_t device, uint64_t* offsets,
+                               uint32_t* out_idx, double* out_dist, uint64_t capacity,
+                               uint64_t* total) {
+  int rc = guarded(k->last_error, [&] {
+    SPJ_CHECK(total != nullptr, "null total");
+    SPJ_CUDA(cudaSetDevice(k->rt->device_id));
+    *total = k->index->query_ties(probe_xy, n, kk, device != 0, offsets, out_idx, out_dist,
+                                  capacity, include_tie_breakers != 0);
+  });
+  if (rc == 0 && *total > capacity) {
+    k->last_error = "output capacity " + std::to_string(capacity) + " < " +
+                    std::to_string(*total) + " results";
+    return ENOSPC;
+  }
+  return rc;
+}
+
+extern "C" int SpjKnnQueryArrow(SpjKnn* k, const ArrowSchema* schema, const ArrowArray* array,
+                                uint32_t kk, int32_t include_tie_breakers, uint64_t* offsets,
+                                uint32_t* out_idx, double* out_dist, uint64_t capacity,
+                                uint64_t* total) {
+  int rc = guarded(k->last_error, [&] {
+    SPJ_CHECK(total != nullptr, "null total");
+    SPJ_CUDA(cudaSetDevice(k->rt->device_id));
+    if (!k->ws) k->ws = std::make_unique<Workspace>();
+    Workspace& ws = *k->ws;
+    const HostWkbColumn col = parse_arrow(schema, array);
+    uint64_t bytes = 0;
+    const WkbDeviceColumn d = stage_column(ws, col, &bytes);
+    decode_wkb(d, ws.probe, ws.dsc, true, ws.stream);
+    SPJ_CHECK(ws.probe.all_points,
+              "KNN probe rows must be points (empty and null rows give no results)");
+    SPJ_CUDA(cudaStreamSynchronize(ws.stream));
+    // empty and null rows decode to NaN points, which get no results
+    *total = k->index->query_ties(reinterpret_cast<const double*>(ws.probe.pt.get()),
+                                  (uint64_t)col.n, kk, true, offsets, out_idx, out_dist, capacity,
+                                  include_tie_breakers != 0);
+  });
+  if (rc == 0 && *total > capacity) {
+    k->last_error = "output capacity " + std::to_string(capacity) + " < " +
+                    std::to_string(*total) + " results";
+    return ENOSPC;
+  }
+  return rc;
 }
 
 extern "C" void* SpjKnnStream(SpjKnn* k) { return (void*)k->index->stream(); }

@@ -67,6 +67,8 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
   if (bg_.nrings > 0) build_band_index(bg_, bsc_, s);
   bg_.has_grid = false;
   if (bg_.nrings > 0 && cfg_.cell_grid) build_cell_grid(bg_, bsc_, s);
+  bg_.grid_rings = cfg_.grid_rings;
+  if (bg_.nrings > 0) build_ring_flags(bg_, s);
   const uint32_t leaf = cfg_.leaf_size ? cfg_.leaf_size : (bg_.all_points ? 16u : 4u);
   build_lbvh(bg_.box.as<float4>(), bg_.n, leaf, bvh_, s);
   split_points();

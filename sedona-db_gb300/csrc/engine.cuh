@@ -58,6 +58,9 @@ struct EngineConfig {
   // per-ring cell grids on the build side (clean cells answer point-in-ring
   // tests in O(1)); set before the build
   bool cell_grid = true;
+  // ring-ring and ring-in-ring tests answer from the build ring's clean cells
+  // when the probe ring's box lies in them
+  bool grid_rings = true;
   // FP32 refine in two passes: a cheap pass (isolation exit, first vertex)
   // over every pair queues the pairs it leaves open, a full pass takes the
   // queue (a warp's lanes then hold pairs of similar cost).  0 off, 1 on,
@@ -125,6 +128,7 @@ class JoinEngine {
   // Rebuild the LBVH over the decoded build boxes with another leaf size.
   void reindex(uint32_t leaf_size);
   const DeviceGeoms& build_geoms() const { return bg_; }
+  void set_grid_rings(bool on) { bg_.grid_rings = on; }
   const Lbvh& lbvh() const { return bvh_; }
 
   // Probe with a device WKB column.  Results (device pointers owned by the

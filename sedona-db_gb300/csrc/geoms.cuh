@@ -70,6 +70,9 @@ struct GeomsView {
   const uint2* grid_meta = nullptr;
   const float4* grid_rect = nullptr;
   const uint8_t* grid_status = nullptr;
+  // ring-ring and ring-in-ring tests may answer from the cells that hold the
+  // other ring's box (when they are all clean and alike)
+  bool grid_rings = false;
 };
 
 struct DeviceGeoms {
@@ -85,6 +88,7 @@ struct DeviceGeoms {
   bool has_bands = false;
   DevBuf grid_meta, grid_rect, grid_status;
   bool has_grid = false;
+  bool grid_rings = false;
 
   GeomsView view() const {
     GeomsView v;
@@ -116,6 +120,7 @@ struct DeviceGeoms {
       v.grid_meta = grid_meta.as<uint2>();
       v.grid_rect = grid_rect.as<float4>();
       v.grid_status = grid_status.as<uint8_t>();
+      v.grid_rings = grid_rings;
     }
     return v;
   }

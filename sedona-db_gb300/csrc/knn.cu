@@ -453,6 +453,115 @@ __global__ void __launch_bounds__(kKnnThreads)
   if ((threadIdx.x & 31) == 0 && evals) atomicAdd(exact_evals, (unsigned long long)evals);
 }
 
+// Tie rows of include_tie_breakers (rust/sedona-spatial-join/src/index/
+// default_spatial_index.rs:378-470): after a probe's k results come the
+// build points outside them whose distance is within DISTANCE_TOLERANCE
+// (1e-9, rust/sedona-spatial-join/src/index/spatial_index.rs:32) of the k-th
+// distance, found as the reference finds them, by a box search around the
+// probe.  A probe with fewer than k results has no ties.  The counting pass
+// writes each probe's output length (its valid results plus its ties); the
+// scatter pass writes the results, then the ties in traversal order.
+constexpr double kTieTolerance = 1e-9;
+
+template <bool kScatter>
+__global__ void __launch_bounds__(kKnnThreads)
+    k_knn_ties(LbvhView t, const double2* __restrict__ bxy, const double2* __restrict__ probe,
+               uint64_t n, uint32_t k, bool ties, const uint32_t* __restrict__ kidx,
+               const double* __restrict__ kdist, uint32_t* __restrict__ counts,
+               const uint64_t* __restrict__ offs, uint32_t* __restrict__ out_idx,
+               double* __restrict__ out_dist, uint64_t cap) {
+  __shared__ int stack[kKnnStack * kKnnThreads];
+  const uint64_t max_steps = 2ull * t.nleaves + 2;
+  for (uint64_t qi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; qi < n;
+       qi += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t* ki = kidx + qi * k;
+    uint32_t nvalid = 0;
+    while (nvalid < k && ki[nvalid] != 0xFFFFFFFFu) nvalid++;
+    uint64_t pos = kScatter ? offs[qi] : 0;
+    if (kScatter) {
+      for (uint32_t c = 0; c < nvalid; c++, pos++)
+        if (pos < cap) {
+          out_idx[pos] = ki[c];
+          out_dist[pos] = kdist[qi * k + c];
+        }
+    }
+    uint32_t cnt = 0;
+    const double2 q = probe[qi];
+    if (ties && nvalid == k && t.nprims > 0 && !(isnan(q.x) || isnan(q.y))) {
+      const double kth = kdist[qi * k + k - 1];
+      const double r = __dadd_ru(kth, kTieTolerance);
+      // every build point within r of q has its RN32 box in this box
+      const float4 qb = make_float4(__double2float_rd(__dsub_rd(q.x, r)),
+                                    __double2float_rd(__dsub_rd(q.y, r)),
+                                    __double2float_ru(__dadd_ru(q.x, r)),
+                                    __double2float_ru(__dadd_ru(q.y, r)));
+      int sp = 0;
+      int node = t.nleaves > 1 ? 0 : ~0;
+      uint64_t steps = 0;
+      while (true) {
+        if (++steps > max_steps) {
+          traversal_fault(t, kTooLong, (unsigned)qi);
+          break;
+        }
+        if (node < 0) {
+          const uint32_t c = (uint32_t)(~node);
+          if (c >= t.nleaves) {
+            traversal_fault(t, kBadLeaf, c);
+            break;
+          }
+          const uint32_t b0 = c * t.leaf_size, b1 = min(b0 + t.leaf_size, t.nprims);
+          for (uint32_t kk = b0; kk < b1; kk++) {
+            if (!box_overlap(t.sorted_box[kk], qb)) continue;
+            const uint32_t id = t.sorted_id[kk];
+            bool mine = false;
+            for (uint32_t c2 = 0; c2 < k; c2++) mine |= ki[c2] == id;
+            if (mine) continue;
+            const double2 b = bxy[kk];
+            const double dx = __dsub_rn(b.x, q.x), dy = __dsub_rn(b.y, q.y);
+            const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+            if (!(__dsub_rn(dist, kth) <= kTieTolerance)) continue;
+            if (kScatter) {
+              if (pos < cap) {
+                out_idx[pos] = id;
+                out_dist[pos] = dist;
+              }
+              pos++;
+            } else {
+              cnt++;
+            }
+          }
+        } else {
+          if ((uint32_t)node + 1 >= t.nleaves) {
+            traversal_fault(t, kBadNode, (unsigned)node);
+            break;
+          }
+          const float4 lb = t.node_box[2 * node], rb = t.node_box[2 * node + 1];
+          const int2 ch = t.node_child[node];
+          const bool hl = box_overlap(lb, qb), hr = box_overlap(rb, qb);
+          if (hl && hr) {
+            if (sp >= kKnnStack) {  // deeper than any tree built here: record, stop
+              traversal_fault(t, kStackOverflow, (unsigned)qi);
+              break;
+            }
+            stack[sp * kKnnThreads + threadIdx.x] = ch.y;
+            sp++;
+            node = ch.x;
+            continue;
+          }
+          if (hl || hr) {
+            node = hl ? ch.x : ch.y;
+            continue;
+          }
+        }
+        if (sp == 0) break;
+        sp--;
+        node = stack[sp * kKnnThreads + threadIdx.x];
+      }
+    }
+    if (!kScatter) counts[qi] = nvalid + cnt;
+  }
+}
+
 __global__ void k_points_to_boxes(const double2* __restrict__ xy, uint64_t n,
                                   float4* __restrict__ boxes) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -492,6 +601,14 @@ KnnIndex::~KnnIndex() {
     odist_.release();
     counters_.release();
     redo_.release();
+    tie_probe_.release();
+    tie_kidx_.release();
+    tie_kdist_.release();
+    tie_counts_.release();
+    tie_offs_.release();
+    tie_tmp_.release();
+    tie_out_idx_.release();
+    tie_out_dist_.release();
     osc_ = ProbeScratch();
     cudaStreamSynchronize(stream_);
     cudaStreamDestroy(stream_);
@@ -532,6 +649,56 @@ void KnnIndex::build(const double* xy_host, uint64_t n) {
   bmag_ = (float)l1;
   if ((double)bmag_ < l1) bmag_ = std::nextafter(bmag_, INFINITY);
   SPJ_CUDA(cudaStreamSynchronize(s));
+}
+
+uint64_t KnnIndex::query_ties(const double* probe_xy, uint64_t n, uint32_t k, bool device_ptrs,
+                              uint64_t* offsets, uint32_t* out_idx, double* out_dist,
+                              uint64_t capacity, bool ties) {
+  SPJ_CHECK(offsets != nullptr, "null offsets");
+  cudaStream_t s = stream_;
+  const double2* dp;
+  if (device_ptrs) {
+    dp = reinterpret_cast<const double2*>(probe_xy);
+  } else {
+    tie_probe_.reserve((n + 1) * 16, s);
+    if (n) SPJ_CUDA(cudaMemcpyAsync(tie_probe_.get(), probe_xy, n * 16, cudaMemcpyHostToDevice, s));
+    dp = tie_probe_.as<double2>();
+  }
+  tie_kidx_.reserve((n * k + 1) * 4, s);
+  tie_kdist_.reserve((n * k + 1) * 8, s);
+  query(reinterpret_cast<const double*>(dp), n, k, tie_kidx_.as<uint32_t>(),
+        tie_kdist_.as<double>(), true);  // syncs
+  tie_counts_.reserve((n + 1) * 4, s);
+  tie_offs_.reserve((n + 1) * 8, s);
+  const LbvhView t = bvh_.view();
+  const int g = grid_for((int64_t)n, kKnnThreads, kNumSMs * 16);
+  if (n)
+    k_knn_ties<false><<<g, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, k, ties,
+                                                 tie_kidx_.as<uint32_t>(), tie_kdist_.as<double>(),
+                                                 tie_counts_.as<uint32_t>(), nullptr, nullptr,
+                                                 nullptr, 0);
+  scan_u32_u64(tie_counts_.as<uint32_t>(), tie_offs_.as<uint64_t>(), (int64_t)n, tie_tmp_, s);
+  SPJ_CUDA(cudaMemcpyAsync(offsets, tie_offs_.get(), (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  check_traversal(t, s);
+  const uint64_t total = offsets[n];
+  if (total > capacity || n == 0) return total;
+  SPJ_CHECK(out_idx && out_dist, "null outputs");
+  tie_out_idx_.reserve((total + 1) * 4, s);
+  tie_out_dist_.reserve((total + 1) * 8, s);
+  k_knn_ties<true><<<g, kKnnThreads, 0, s>>>(t, xy_sorted_.as<double2>(), dp, n, k, ties,
+                                              tie_kidx_.as<uint32_t>(), tie_kdist_.as<double>(),
+                                              nullptr, tie_offs_.as<uint64_t>(),
+                                              tie_out_idx_.as<uint32_t>(),
+                                              tie_out_dist_.as<double>(), total);
+  SPJ_CUDA(cudaGetLastError());
+  if (total) {
+    SPJ_CUDA(cudaMemcpyAsync(out_idx, tie_out_idx_.get(), total * 4, cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaMemcpyAsync(out_dist, tie_out_dist_.get(), total * 8, cudaMemcpyDeviceToHost, s));
+  }
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  check_traversal(t, s);
+  return total;
 }
 
 void KnnIndex::query(const double* probe_xy, uint64_t n, uint32_t k, uint32_t* out_idx,

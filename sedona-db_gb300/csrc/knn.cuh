@@ -15,6 +15,15 @@ class KnnIndex {
   // probe_xy: n (x, y) FP64 pairs; outputs n*k entries; host or device arrays
   void query(const double* probe_xy, uint64_t n, uint32_t k, uint32_t* out_idx, double* out_dist,
              bool device_ptrs);
+  // Variable-length results: each probe's valid results (none for an empty
+  // probe) and, with ties, the build points outside them whose distance is
+  // within 1e-9 of the k-th (include_tie_breakers; the reference's
+  // DISTANCE_TOLERANCE).  offsets (host, n+1) receive each probe's run in
+  // out_idx / out_dist (host); returns the total; when it exceeds capacity
+  // nothing else is written.
+  uint64_t query_ties(const double* probe_xy, uint64_t n, uint32_t k, bool device_ptrs,
+                      uint64_t* offsets, uint32_t* out_idx, double* out_dist, uint64_t capacity,
+                      bool ties);
   cudaStream_t stream() const { return stream_; }
   uint64_t exact_evals() const { return exact_evals_; }
   // probes whose k-set the split FP32 pass did not prove (sent to the exact kernel)
@@ -33,6 +42,8 @@ class KnnIndex {
   float bmag_ = 0;    // max |x| + |y| over the build side (rounded up)
   bool split_ok_ = true;  // build coordinates within the split pass's range
   DevBuf probe_, oidx_, odist_, counters_, redo_;
+  DevBuf tie_probe_, tie_kidx_, tie_kdist_, tie_counts_, tie_offs_, tie_tmp_, tie_out_idx_,
+      tie_out_dist_;
   ProbeScratch osc_;  // Morton order of the probes
   uint64_t exact_evals_ = 0, redone_ = 0, queries_ = 0;
 };

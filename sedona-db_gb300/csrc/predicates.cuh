@@ -308,6 +308,35 @@ __device__ __forceinline__ int grid_point_status(const GeomsView& G, uint32_t r,
   return G.grid_status[m.x + (uint32_t)j * m.y + (uint32_t)i];
 }
 
+// Status shared by every grid cell that holds the closed box of another ring
+// (its exact rect R, RN32 rect q): 1 inside / 2 outside when those cells (at
+// most 2 x 2) are all clean with that status, else 0.  Clean cells are free
+// of the ring's edges (each edge strictly bbox-separated from the cell, or
+// the cell strictly on one side of its line), so no edge of this ring meets
+// the box (their union is a rectangle that holds it), tg's segment tests
+// against anything inside fail, and every point of the box has that status
+// in tg's arithmetic (the argument of the isolation exit below).
+__device__ __forceinline__ int grid_rect_status(const GeomsView& G, uint32_t r, Rect64 R,
+                                                float4 q) {
+  if (!G.grid_rings || G.grid_meta == nullptr) return 0;
+  const uint2 m = G.grid_meta[r];
+  if (m.y == 0) return 0;
+  const float4 g = G.grid_rect[r];
+  const int i0 = grid_index32(g.x, g.z, (int)m.y, q.x, R.x);
+  const int i1 = grid_index32(g.x, g.z, (int)m.y, q.z, R.z);
+  if (i0 < 0 || i1 < 0 || i1 - i0 > 1) return 0;
+  const int j0 = grid_index32(g.y, g.w, (int)m.y, q.y, R.y);
+  const int j1 = grid_index32(g.y, g.w, (int)m.y, q.w, R.w);
+  if (j0 < 0 || j1 < 0 || j1 - j0 > 1) return 0;
+  const uint8_t* st = G.grid_status + m.x;
+  const int s = st[(uint32_t)j0 * m.y + (uint32_t)i0];
+  if (s == 0) return 0;
+  for (int j = j0; j <= j1; j++)
+    for (int i = i0; i <= i1; i++)
+      if (st[(uint32_t)j * m.y + (uint32_t)i] != s) return 0;
+  return s;
+}
+
 // Plain FP64 form: tg's FP64 sequence for every segment it visits, with the
 // same index as the chosen form and no FP32 arithmetic tier.  With a band
 // index the visited segments are the point's band (every segment whose
@@ -618,6 +647,12 @@ __device__ __forceinline__ int ring_intersects_ring(const GeomsView& GA, uint32_
   }
   const uint32_t Vo = Go->ring_vtx[ro];
   const int nso = Go->ring_nsegs[ro];
+  if (kFast && nso > 0) {
+    // the smaller ring's box inside clean cells of the larger ring: no edge
+    // of the larger ring comes near, so the answer is the cells' status
+    const int st = grid_rect_status(*Gr, rr, Go->ring_rect[ro], Go->ring_rect32[ro]);
+    if (st != 0) return st == 1 ? 1 : 0;
+  }
   if (kFast && nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
     // Isolation exit.  If every segment of the larger ring has a bbox
     // strictly separated from the smaller ring's bbox (a strict f32

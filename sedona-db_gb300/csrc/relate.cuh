@@ -229,6 +229,12 @@ __device__ __noinline__ bool ring_contains_ring(const GeomsView& GA, uint32_t ra
   if (ring_npts(GA, ra) < 3 || ring_npts(GB, rb) < 3) return false;
   const Rect64 A = GA.ring_rect[ra], Bq = GB.ring_rect[rb];
   if (Bq.x < A.x || Bq.z > A.z || Bq.y < A.y || Bq.w > A.w) return false;
+  if (kFast) {
+    // b's box in clean cells of a: every point of b strictly inside (1) or
+    // outside (2) a, and no edge of a meets b, whatever allow_on_edge says
+    const int st = grid_rect_status(GA, ra, Bq, GB.ring_rect32[rb]);
+    if (st != 0) return st == 1;
+  }
   const uint32_t Vb = GB.ring_vtx[rb];
   if (ring_flags_of(GA, ra) & kRingConvex) {
     const uint32_t n = ring_npts(GB, rb);

@@ -156,6 +156,7 @@ EXPORTS = [
     "SpjJoinFinishBuild", "SpjJoinBuildDevice", "SpjJoinProbeArrow", "SpjJoinProbeDevice",
     "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
+    "SpjKnnQueryTies", "SpjKnnQueryArrow",
     "SpjKnnStream", "SpjKnnGetStats", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
     "SpjIndexProbeNoAlloc", "SpjAllocationCount",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
@@ -237,6 +238,15 @@ def lib() -> C.CDLL:
                                       C.c_void_p, C.c_void_p, C.c_int32]
             L.SpjKnnStream.argtypes = [C.c_void_p]
             L.SpjKnnStream.restype = C.c_void_p
+            L.SpjKnnQueryTies.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
+                                          C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
+            L.SpjKnnQueryArrow.argtypes = [C.c_void_p, C.POINTER(ArrowSchema),
+                                           C.POINTER(ArrowArray), C.c_uint32, C.c_int32,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                           C.POINTER(C.c_uint64)]
+            L.SpjAllocationCount.argtypes = []
+            L.SpjAllocationCount.restype = C.c_uint64
             L.SpjHostRegister.argtypes = [C.c_void_p, C.c_uint64]
             L.SpjHostUnregister.argtypes = [C.c_void_p]
             L.SpjVersion.restype = C.c_char_p
@@ -683,6 +693,40 @@ class KnnJoin:
 
     def query_device(self, d_xy: int, n: int, k: int, d_idx: int, d_dist: int):
         _check(lib().SpjKnnQuery(self.h, d_xy, n, k, d_idx, d_dist, 1), "knn query", self._err)
+
+    def _ragged(self, call, n: int):
+        """Runs a variable-length query (two tries: the first learns the size)."""
+        offsets = np.zeros(n + 1, dtype=np.uint64)
+        total = C.c_uint64(0)
+        cap = max(16, n * 2)
+        for _ in range(2):
+            idx = np.empty(cap, dtype=np.uint32)
+            dist = np.empty(cap, dtype=np.float64)
+            rc = call(offsets, idx, dist, cap, total)
+            if rc == 28:  # ENOSPC: retry with the reported size
+                cap = int(total.value)
+                continue
+            _check(rc, "knn query", self._err)
+            t = int(total.value)
+            return offsets.astype(np.int64), idx[:t], dist[:t]
+        raise GpuSpatialError("knn query: output size changed between calls")
+
+    def query_ties(self, x: np.ndarray, y: np.ndarray, k: int, include_tie_breakers: bool = True):
+        """Per probe i: idx / dist[offsets[i]:offsets[i+1]] are its k nearest
+        and, with include_tie_breakers, every other build point within 1e-9
+        of its k-th distance."""
+        xy = np.ascontiguousarray(np.stack([x, y], 1), dtype=np.float64)
+        return self._ragged(lambda o, i, d, cap, tot: lib().SpjKnnQueryTies(
+            self.h, xy.ctypes.data, len(xy), k, int(include_tie_breakers), 0, o.ctypes.data,
+            i.ctypes.data, d.ctypes.data, cap, C.byref(tot)), len(xy))
+
+    def query_wkb(self, col: WkbColumn, k: int, include_tie_breakers: bool = False):
+        """query_knn over a WKB point column (decoded on the device); empty
+        and null rows get no results.  Returns (offsets, idx, dist)."""
+        a = ArrowBinary(col)
+        return self._ragged(lambda o, i, d, cap, tot: lib().SpjKnnQueryArrow(
+            self.h, C.byref(a.schema), C.byref(a.array), k, int(include_tie_breakers),
+            o.ctypes.data, i.ctypes.data, d.ctypes.data, cap, C.byref(tot)), len(col))
 
     def stream(self) -> int:
         return lib().SpjKnnStream(self.h)

@@ -622,3 +622,65 @@ def test_reference_fixtures(capi, form, name):
     for pred, want in exp.items():
         b, p = j.probe(probe, pred)
         assert pairs(b, p) == want, pred
+
+
+@pytest.mark.parametrize("k", [1, 4, 8])
+def test_knn_tie_breakers(capi, k):
+    """include_tie_breakers (rust/sedona-spatial-join/src/index/
+    default_spatial_index.rs:378-470): on an integer lattice with probes on
+    the lattice and half-lattice, many build points tie at the k-th
+    distance; each probe gets its k nearest by (distance, row id), then every
+    other point within 1e-9 of the k-th distance (brute force in FP64)."""
+    g = np.arange(30.0)
+    bx, by = [a.ravel() for a in np.meshgrid(g, g)]
+    rng = np.random.default_rng(9)
+    px = rng.integers(-4, 64, 300) / 2.0
+    py = rng.integers(-4, 64, 300) / 2.0
+    kj = capi.KnnJoin()
+    kj.build(bx, by)
+    off, idx, dist = kj.query_ties(px, py, k, True)
+    ids = np.arange(len(bx))
+    extra = 0
+    for i in range(len(px)):
+        d = np.hypot(px[i] - bx, py[i] - by)
+        order = np.lexsort((ids, d))
+        kth = d[order[k - 1]]
+        exp = set(order[:k].tolist()) | set(np.nonzero(d - kth <= 1e-9)[0].tolist())
+        got = idx[off[i]:off[i + 1]]
+        assert got[:k].tolist() == order[:k].tolist(), i
+        assert len(got) == len(exp) and set(got.tolist()) == exp, i
+        np.testing.assert_allclose(dist[off[i]:off[i + 1]], d[got], rtol=1e-12, atol=0)
+        extra += len(got) - k
+    assert extra > 0  # the lattice does produce ties
+    off0, idx0, _ = kj.query_ties(px, py, k, False)
+    ri, _ = kj.query(px, py, k)
+    assert np.array_equal(np.diff(off0), np.full(len(px), k))
+    assert np.array_equal(idx0.reshape(-1, k), ri)
+
+
+def test_knn_wkb_column(capi, oracle_mod):
+    """query_knn over a WKB point column decoded on the device; empty (POINT
+    EMPTY) and null rows get no results, as in the reference
+    (default_spatial_index.rs:331-339)."""
+    from sedona_gpuspatial import wkb
+    rng = np.random.default_rng(10)
+    bx, by = rng.uniform(0, 100, 5000), rng.uniform(0, 100, 5000)
+    px, py = rng.uniform(-5, 105, 700), rng.uniform(-5, 105, 700)
+    vals = [wkb.wkb_point(float(x), float(y)) for x, y in zip(px, py)]
+    vals[3] = None
+    vals[10] = wkb.wkb_point(float("nan"), float("nan"))
+    vals[11] = wkb.wkb_point(float(px[11]), float(py[11]), big_endian=True)
+    kj = capi.KnnJoin()
+    kj.build(bx, by)
+    off, idx, dist = kj.query_wkb(wkb.column_from_values(vals), 6)
+    assert off[4] - off[3] == 0 and off[11] - off[10] == 0
+    keep = [i for i in range(len(vals)) if i not in (3, 10)]
+    B = oracle_mod.Geoms(wkb.points_column(bx, by))
+    P = oracle_mod.Geoms(wkb.points_column(px[keep], py[keep]))
+    ob, od = oracle_mod.knn(B, P, 6, nthreads=4)
+    for r, i in enumerate(keep):
+        assert idx[off[i]:off[i + 1]].tolist() == ob[r].tolist(), i
+        np.testing.assert_allclose(dist[off[i]:off[i + 1]], od[r], rtol=1e-12, atol=0)
+    poly = wkb.wkb_polygon([[(0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 0.0)]])
+    with pytest.raises(capi.GpuSpatialError, match="points"):
+        kj.query_wkb(wkb.column_from_values([vals[0], poly]), 2)
