@@ -129,7 +129,11 @@ int SpjJoinBuildDevice(SpjJoin* join, const struct SpjDeviceWkb* column);
 /* Probe with a host Arrow array; the refined pairs (probe ids offset by
  * probe_base) are delivered through callback, in ascending probe order,
  * possibly in several chunks; a non-zero return from callback stops the
- * probe and is returned. */
+ * probe and is returned.  predicate: a SedonaSpatialRelationPredicate, or
+ * SPJ_PREDICATE_DWITHIN with `distance` (or the distance column of
+ * SpjJoinSetProbeDistances): the reference's build.distance_ext(probe) <= d
+ * (rust/sedona-spatial-join/src/refine/geo.rs:312-321) between points,
+ * polygons and multipolygons; the probe rows' rects are expanded by d. */
 int SpjJoinProbeArrow(SpjJoin* join, const struct ArrowSchema* schema,
                       const struct ArrowArray* array, int32_t predicate, double distance,
                       uint32_t probe_base,
@@ -158,6 +162,16 @@ int SpjJoinProbeHost(SpjJoin* join, int64_t length, const void* offsets,
                      int32_t predicate, double distance, uint32_t probe_base,
                      uint32_t* out_build, uint32_t* out_probe, uint64_t capacity,
                      uint64_t* n_pairs);
+
+/* ST_DWithin with a distance column (rust/sedona-spatial-join/src/
+ * operand_evaluator.rs:556-627: the probe rows' rects are expanded by their
+ * own distance): the next probes with SPJ_PREDICATE_DWITHIN take distances[i]
+ * for probe row i (rows counted within the probed column) instead of their
+ * `distance` argument; the column must have n rows.  A negative or NaN
+ * distance (a null) matches nothing.  distances is host memory, or device
+ * memory when device == 1; it is copied.  NULL clears the column. */
+int SpjJoinSetProbeDistances(SpjJoin* join, const double* distances, uint64_t n,
+                             int32_t device);
 
 /* The CUDA stream (cudaStream_t) the join launches its kernels on. */
 void* SpjJoinStream(SpjJoin* join);

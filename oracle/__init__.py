@@ -77,6 +77,12 @@ def lib():
         L.spjo_join.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                                 C.POINTER(C.POINTER(C.c_uint32)),
                                 C.POINTER(C.POINTER(C.c_uint32)), C.c_char_p, C.c_int]
+        L.spjo_join_dists.restype = C.c_int64
+        L.spjo_join_dists.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_int,
+                                      C.POINTER(C.POINTER(C.c_uint32)),
+                                      C.POINTER(C.POINTER(C.c_uint32)), C.c_char_p, C.c_int]
+        L.spjo_geo_distance.restype = C.c_double
+        L.spjo_geo_distance.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
         L.spjo_knn.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.c_char_p,
                                C.c_int]
@@ -155,6 +161,24 @@ def join(build: Geoms, probe: Geoms, predicate: str, distance: float = 0.0,
     if n < 0:
         raise RuntimeError(err.value.decode())
     return _take_pairs(n, pb, pp)
+
+
+def join_dists(build: Geoms, probe: Geoms, dists: np.ndarray, nthreads: int = 1):
+    """ST_DWithin pairs with one distance per probe row, sorted by (probe, build)."""
+    L = lib()
+    d = np.ascontiguousarray(dists, dtype=np.float64)
+    assert len(d) == probe.n
+    pb, pp = C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)()
+    err = C.create_string_buffer(512)
+    n = L.spjo_join_dists(build.ptr, probe.ptr, d.ctypes.data_as(C.POINTER(C.c_double)),
+                          nthreads, C.byref(pb), C.byref(pp), err, 512)
+    if n < 0:
+        raise RuntimeError(err.value.decode())
+    return _take_pairs(n, pb, pp)
+
+
+def geo_distance(build: Geoms, bi: int, probe: Geoms, pi: int) -> float:
+    return lib().spjo_geo_distance(build.ptr, bi, probe.ptr, pi)
 
 
 def knn(build: Geoms, probe: Geoms, k: int, nthreads: int = 1):

@@ -656,6 +656,115 @@ static int geom_touches(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, in
   return touches;
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* Euclidean distance of the reference's ST_DWithin refine,                  */
+/* build.distance_ext(probe) <= d (rust/sedona-spatial-join/src/refine/      */
+/* geo.rs:312-321), as sedona-geo-generic-alg computes it                    */
+/* (rust/sedona-geo-generic-alg/src/algorithm/line_measures/metric_spaces/   */
+/* euclidean/utils.rs, distance.rs).  The reference's intersects tests are   */
+/* geo's; tg's stand in for them (they differ only where a distance is       */
+/* within FP64 rounding of zero).                                            */
+/* ------------------------------------------------------------------------ */
+
+/* utils.rs:127-165 distance_coord_to_line_generic */
+static double coord_line_dist(opt_t p, opt_t a, opt_t b) {
+  if (a.x == b.x && a.y == b.y) return hypot(p.x - a.x, p.y - a.y);
+  double dx = b.x - a.x, dy = b.y - a.y;
+  double d2 = dx * dx + dy * dy;
+  double r = ((p.x - a.x) * dx + (p.y - a.y) * dy) / d2;
+  if (r <= 0) return hypot(p.x - a.x, p.y - a.y);
+  if (r >= 1) return hypot(p.x - b.x, p.y - b.y);
+  double s = ((a.y - p.y) * dx - (a.x - p.x) * dy) / d2;
+  return fabs(s) * hypot(dx, dy);
+}
+
+/* utils.rs:291-314 distance_line_to_line_generic */
+static double line_line_dist(oseg_t s1, oseg_t s2) {
+  if (segment_intersects_segment(s1, s2)) return 0;
+  double d1 = coord_line_dist(s1.a, s2.a, s2.b), d2 = coord_line_dist(s1.b, s2.a, s2.b);
+  double d3 = coord_line_dist(s2.a, s1.a, s1.b), d4 = coord_line_dist(s2.b, s1.a, s1.b);
+  return fmin(fmin(fmin(d1, d2), d3), d4);
+}
+
+/* distance.rs:486-505 LineString to LineString (and utils.rs:36-73
+ * nearest_neighbour_distance, whose vertex passes cannot go below the
+ * segment pairs' minimum): min over segment pairs, 0 at the first pair
+ * that meets */
+static double ring_ring_dist(const spj_geoms* G1, const oring_t* r1, const spj_geoms* G2,
+                             const oring_t* r2) {
+  double m = DBL_MAX;
+  for (int i = 0; i < r1->nsegs; i++)
+    for (int j = 0; j < r2->nsegs; j++) {
+      double d = line_line_dist(ring_seg(G1, r1, i), ring_seg(G2, r2, j));
+      if (d == 0) return 0;
+      m = fmin(m, d);
+    }
+  return m == DBL_MAX ? 0 : m;
+}
+
+/* utils.rs:231-289 distance_point_to_polygon_generic */
+static double point_poly_dist(const spj_geoms* G, const opoly_t* P, opt_t p) {
+  if (poly_contains_point(G, P, p, 1)) return 0;
+  double m = DBL_MAX;
+  for (int h = 0; h < P->nrings; h++) {
+    const oring_t* r = &G->rings[P->first_ring + h];
+    for (int i = 0; i < r->nsegs; i++) {
+      oseg_t s = ring_seg(G, r, i);
+      m = fmin(m, coord_line_dist(p, s.a, s.b));
+    }
+  }
+  return m;
+}
+
+/* utils.rs:567-657 distance_polygon_to_polygon_generic */
+static double poly_poly_dist(const spj_geoms* GA, const opoly_t* A, const spj_geoms* GB,
+                             const opoly_t* B) {
+  if (poly_intersects_poly(GA, A, GB, B)) return 0;
+  const oring_t* ea = poly_ext(GA, A);
+  const oring_t* eb = poly_ext(GB, B);
+  if (A->nrings == 1 && B->nrings == 1) return ring_ring_dist(GA, ea, GB, eb);
+  /* b inside a (strictly inside a's shell at b's first point): the nearest
+   * of a's holes; the same the other way round */
+  if (A->nrings > 1 && ring_contains_point(GA, ea, GB->pts[eb->first], 0).hit) {
+    double m = DBL_MAX;
+    for (int h = 0; h < A->nrings - 1; h++)
+      m = fmin(m, ring_ring_dist(GB, eb, GA, poly_hole(GA, A, h)));
+    return m;
+  }
+  if (B->nrings > 1 && ring_contains_point(GB, eb, GA->pts[ea->first], 0).hit) {
+    double m = DBL_MAX;
+    for (int h = 0; h < B->nrings - 1; h++)
+      m = fmin(m, ring_ring_dist(GA, ea, GB, poly_hole(GB, B, h)));
+    return m;
+  }
+  return ring_ring_dist(GA, ea, GB, eb);
+}
+
+/* build.distance_ext(probe) over points, polygons and multipolygons: a
+ * multipolygon is the minimum over its parts (distance.rs:224-246; an empty
+ * part has distance 0, utils.rs:236-238) */
+double spjo_geo_distance(const spj_geoms* GA, int64_t ia, const spj_geoms* GB, int64_t ib) {
+  const ogeom_t* a = &GA->g[ia];
+  const ogeom_t* b = &GB->g[ib];
+  if (a->kind == SPJO_EMPTY || b->kind == SPJO_EMPTY) return 0;
+  if (a->kind == SPJO_POINT && b->kind == SPJO_POINT)
+    return hypot(a->pt.x - b->pt.x, a->pt.y - b->pt.y);
+  if (a->empty_parts || b->empty_parts) return 0;
+  double m = DBL_MAX;
+  if (a->kind == SPJO_POINT || b->kind == SPJO_POINT) {
+    const spj_geoms* GY = a->kind == SPJO_POINT ? GB : GA;
+    const ogeom_t* y = a->kind == SPJO_POINT ? b : a;
+    opt_t p = a->kind == SPJO_POINT ? a->pt : b->pt;
+    for (int i = 0; i < y->npolys; i++) m = fmin(m, point_poly_dist(GY, part_of(GY, y, i), p));
+    return m;
+  }
+  for (int i = 0; i < a->npolys; i++)
+    for (int j = 0; j < b->npolys; j++)
+      m = fmin(m, poly_poly_dist(GA, part_of(GA, a, i), GB, part_of(GB, b, j)));
+  return m;
+}
+
 int spjo_predicate(const spj_geoms* B, int64_t bi, const spj_geoms* P, int64_t pi, int pred) {
   switch (pred) {
     case SPJO_INTERSECTS:
@@ -1141,6 +1250,7 @@ typedef struct {
   const ogrid_t* grid;
   int pred;
   double distance;
+  const double* dists; /* per probe row (NULL: distance for every row) */
   int64_t p0, p1;
   /* per-probe scratch */
   uint32_t* cand;
@@ -1170,7 +1280,8 @@ static void* join_worker(void* arg) {
   for (int64_t pi = c->p0; pi < c->p1; pi++) {
     float pb[4];
     if (c->pboxes) memcpy(pb, c->pboxes + 4 * pi, sizeof pb);
-    else box_of(&c->P->g[pi], 0, c->pred == SPJO_DWITHIN ? c->distance : 0, pb);
+    else box_of(&c->P->g[pi], 0,
+                c->pred == SPJO_DWITHIN ? (c->dists ? c->dists[pi] : c->distance) : 0, pb);
     c->ncand = 0;
     if (grid_query(c->grid, c->bboxes, pb, collect, c)) {
       c->status = -1;
@@ -1184,16 +1295,9 @@ static void* join_worker(void* arg) {
       if (!c->B) {
         keep = 1; /* rect join */
       } else if (c->pred == SPJO_DWITHIN) {
-        const ogeom_t* gb = &c->B->g[bi];
-        const ogeom_t* gp = &c->P->g[pi];
-        if (gb->kind != SPJO_POINT || gp->kind != SPJO_POINT) {
-          c->status = -1;
-          snprintf(c->err, sizeof c->err, "ST_DWithin is supported for point pairs only");
-          return NULL;
-        }
-        /* geo.rs:312-321 build.distance_ext(probe) <= d; distance.rs:296-300 */
-        double d = hypot(gb->pt.x - gp->pt.x, gb->pt.y - gp->pt.y);
-        keep = d <= c->distance;
+        /* geo.rs:312-321 build.distance_ext(probe) <= d */
+        const double dd = c->dists ? c->dists[pi] : c->distance;
+        keep = spjo_geo_distance(c->B, bi, c->P, pi) <= dd;
       } else {
         keep = spjo_predicate(c->B, bi, c->P, pi, c->pred);
         if (keep < 0) {
@@ -1216,7 +1320,8 @@ static void* join_worker(void* arg) {
 
 static int64_t run_join(const spj_geoms* B, const spj_geoms* P, const float* bboxes, int64_t nb,
                         const float* pboxes, int64_t np, int pred, double distance,
-                        int nthreads, uint32_t** ob, uint32_t** op, char* err, int errlen) {
+                        const double* dists, int nthreads, uint32_t** ob, uint32_t** op,
+                        char* err, int errlen) {
   ogrid_t grid;
   if (grid_build(&grid, bboxes, nb)) {
     grid_free(&grid);
@@ -1237,6 +1342,7 @@ static int64_t run_join(const spj_geoms* B, const spj_geoms* P, const float* bbo
     jobs[t].grid = &grid;
     jobs[t].pred = pred;
     jobs[t].distance = distance;
+    jobs[t].dists = dists;
     jobs[t].p0 = t * chunk < np ? t * chunk : np;
     jobs[t].p1 = (t + 1) * chunk < np ? (t + 1) * chunk : np;
   }
@@ -1283,7 +1389,7 @@ static int64_t run_join(const spj_geoms* B, const spj_geoms* P, const float* bbo
 
 int64_t spjo_rect_join(const float* build_rects, int64_t nb, const float* probe_rects,
                        int64_t np, int nthreads, uint32_t** out_build, uint32_t** out_probe) {
-  return run_join(NULL, NULL, build_rects, nb, probe_rects, np, SPJO_INTERSECTS, 0, nthreads,
+  return run_join(NULL, NULL, build_rects, nb, probe_rects, np, SPJO_INTERSECTS, 0, NULL, nthreads,
                   out_build, out_probe, NULL, 0);
 }
 
@@ -1293,7 +1399,19 @@ int64_t spjo_join(const spj_geoms* B, const spj_geoms* P, int pred, double dista
   float* bb = (float*)malloc((size_t)(B->n > 0 ? B->n : 1) * 16);
   if (!bb) return -1;
   spjo_boxes(B, 0, bb);
-  int64_t r = run_join(B, P, bb, B->n, NULL, P->n, pred, distance, nthreads, out_build,
+  int64_t r = run_join(B, P, bb, B->n, NULL, P->n, pred, distance, NULL, nthreads, out_build,
+                       out_probe, err, errlen);
+  free(bb);
+  return r;
+}
+
+int64_t spjo_join_dists(const spj_geoms* B, const spj_geoms* P, const double* dists,
+                        int nthreads, uint32_t** out_build, uint32_t** out_probe, char* err,
+                        int errlen) {
+  float* bb = (float*)malloc((size_t)(B->n > 0 ? B->n : 1) * 16);
+  if (!bb) return -1;
+  spjo_boxes(B, 0, bb);
+  int64_t r = run_join(B, P, bb, B->n, NULL, P->n, SPJO_DWITHIN, 0, dists, nthreads, out_build,
                        out_probe, err, errlen);
   free(bb);
   return r;

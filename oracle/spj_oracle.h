@@ -95,6 +95,14 @@ int64_t spjo_join(const spj_geoms* build, const spj_geoms* probe, int pred, doub
  * the smallest hypot distance, ties broken by build row id.  Output rows are
  * (probe, rank) ordered; out arrays hold n_probe*k entries, unused slots have
  * build = 0xFFFFFFFF and dist = +inf.  Returns 0 or -1. */
+/* ST_DWithin with one distance per probe row (the reference's distance
+ * column, rust/sedona-spatial-join/src/operand_evaluator.rs:556-627). */
+int64_t spjo_join_dists(const spj_geoms* build, const spj_geoms* probe, const double* dists,
+                        int nthreads, uint32_t** out_build, uint32_t** out_probe, char* err,
+                        int errlen);
+/* build.distance_ext(probe): the Euclidean distance the DWithin refine uses. */
+double spjo_geo_distance(const spj_geoms* build, int64_t bi, const spj_geoms* probe, int64_t pi);
+
 int spjo_knn(const spj_geoms* build, const spj_geoms* probe, int k, int nthreads,
              uint32_t* out_build, double* out_dist, char* err, int errlen);
 

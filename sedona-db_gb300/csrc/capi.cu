@@ -579,6 +579,11 @@ extern "C" int GpuSpatialRefinerCreate(SedonaSpatialRefiner* refiner,
 struct SpjJoin {
   RuntimeData* rt = nullptr;
   std::unique_ptr<JoinEngine> engine;
+  // ST_DWithin distance column (one per probe row), set by
+  // SpjJoinSetProbeDistances; freed on the join's own stream
+  DevBuf dist;
+  uint64_t dist_n = 0;
+  bool has_dist = false;
   std::unique_ptr<WorkspacePool> pool;
   std::unique_ptr<Workspace> ws;   // the join's own stream and scratch
   std::unique_ptr<Workspace> ws2;  // second slot of the sliced host probe
@@ -596,6 +601,11 @@ struct SpjJoin {
     bool pending = false;  // `copied` marks a copy of the hold buffers
   } lanes[2];
   ~SpjJoin() {
+    // the distance column frees on the workspace's stream: before it goes
+    if (ws) {
+      dist.release();
+      cudaStreamSynchronize(ws->stream);
+    }
     for (auto& l : lanes) {
       if (l.stream) {
         cudaStreamSynchronize(l.stream);
@@ -856,14 +866,43 @@ extern "C" int SpjJoinBuildDevice(SpjJoin* j, const SpjDeviceWkb* column) {
   });
 }
 
+// The distance column for this probe (nullptr: the call's one distance).
+static const double* probe_distances(SpjJoin* j, int32_t predicate, int64_t rows) {
+  if (predicate != SPJ_PREDICATE_DWITHIN || !j->has_dist) return nullptr;
+  SPJ_CHECK((uint64_t)rows == j->dist_n,
+            "distance column has " + std::to_string(j->dist_n) + " rows, the probe column " +
+                std::to_string(rows));
+  return j->dist.as<double>();
+}
+
+extern "C" int SpjJoinSetProbeDistances(SpjJoin* j, const double* distances, uint64_t n,
+                                        int32_t device) {
+  return guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    j->has_dist = false;
+    j->dist_n = 0;
+    if (distances == nullptr) return;
+    cudaStream_t s = j->ws->stream;
+    j->dist.reserve((n + 1) * sizeof(double), s);
+    if (n)
+      SPJ_CUDA(cudaMemcpyAsync(j->dist.get(), distances, n * sizeof(double),
+                               device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    j->dist_n = n;
+    j->has_dist = true;
+  });
+}
+
 extern "C" int SpjJoinProbeDevice(SpjJoin* j, const SpjDeviceWkb* column, int32_t predicate,
                                   double distance, uint32_t probe_base, const uint32_t** d_build,
                                   const uint32_t** d_probe, uint64_t* n_pairs) {
   return guarded(j->last_error, [&] {
     SPJ_CUDA(cudaSetDevice(j->rt->device_id));
     SPJ_CHECK(d_build && d_probe && n_pairs, "null outputs");
+    SPJ_CHECK(column != nullptr, "null column");
+    const double* dr = probe_distances(j, predicate, column->length);
     *n_pairs = j->engine->probe(*j->ws, device_column(column), predicate, distance, probe_base,
-                                d_build, d_probe);
+                                d_build, d_probe, dr);
   });
 }
 
@@ -877,10 +916,11 @@ extern "C" int SpjJoinProbeArrow(SpjJoin* j, const ArrowSchema* schema, const Ar
     SPJ_CUDA(cudaSetDevice(j->rt->device_id));
     SPJ_CHECK(callback != nullptr, "null callback");
     HostWkbColumn hc = parse_arrow(schema, array);
+    const double* dr = probe_distances(j, predicate, hc.n);
     uint64_t bytes = 0;
     WkbDeviceColumn dc = stage_column(*j->ws, hc, &bytes);
     const uint32_t *db, *dp;
-    uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp);
+    uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp, dr);
     j->hb.resize(m);
     j->hp.resize(m);
     if (m) copy_pairs_to_host(j, db, dp, m, j->hb.data(), j->hp.data());
@@ -905,7 +945,9 @@ extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
     hc.offsets64 = offsets_are_64bit != 0;
     hc.data = data;
     hc.validity = validity;
-    const int nslices = host_slices(hc, j->engine->config().host_slices);
+    const double* dr = probe_distances(j, predicate, length);
+    // (a distance column is probed in one call: its rows stay aligned)
+    const int nslices = dr ? 1 : host_slices(hc, j->engine->config().host_slices);
     if (nslices > 1) {
       const uint64_t m = probe_host_sliced(j, hc, nslices, predicate, distance, probe_base,
                                            out_build, out_probe, capacity);
@@ -916,7 +958,7 @@ extern "C" int SpjJoinProbeHost(SpjJoin* j, int64_t length, const void* offsets,
     uint64_t bytes = 0;
     WkbDeviceColumn dc = stage_column(*j->ws, hc, &bytes);
     const uint32_t *db, *dp;
-    uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp);
+    uint64_t m = j->engine->probe(*j->ws, dc, predicate, distance, probe_base, &db, &dp, dr);
     *n_pairs = m;
     if (m > capacity) {
       rc = ENOSPC;

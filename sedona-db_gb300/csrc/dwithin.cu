@@ -114,8 +114,9 @@ template <bool kScatter, bool kArena>
 __global__ void __launch_bounds__(kTravThreads)
     k_dwithin_fused(LbvhView t, const double2* __restrict__ bxy, const float4* __restrict__ bhl,
                     float bmag, int split_ok, const float4* __restrict__ probe_box,
-                    const double2* __restrict__ probe_pt, uint32_t n, double d, float d_lo,
-                    float d_hi, const uint32_t* __restrict__ order, uint32_t* __restrict__ counts,
+                    const double2* __restrict__ probe_pt, uint32_t n, double d0, float d_lo0,
+                    float d_hi0, const double* __restrict__ d_row,
+                    const uint32_t* __restrict__ order, uint32_t* __restrict__ counts,
                     const uint64_t* __restrict__ offs, uint32_t probe_base,
                     uint32_t* __restrict__ out_build, uint32_t* __restrict__ out_probe,
                     uint64_t cap, DeviceStatus* st, uint32_t* __restrict__ slots, uint32_t K,
@@ -139,6 +140,17 @@ __global__ void __launch_bounds__(kTravThreads)
     if (kScatter && K > 0 && (counts[pi] <= K || (kArena && A.head[pi] != kArenaFailed)))
       continue;
     const float4 q = probe_box[pi];
+    // the probe row's distance and its FP32 neighbours (the expanded box of
+    // a row with a negative or NaN distance is empty: no traversal)
+    double d = d0;
+    float d_lo = d_lo0, d_hi = d_hi0;
+    if (d_row) {
+      d = d_row[pi];
+      d_lo = __double2float_rn(d);
+      d_hi = d_lo;
+      if ((double)d_lo > d) d_lo = next_downf(d_lo);
+      if ((double)d_hi < d) d_hi = next_upf(d_hi);
+    }
     uint32_t cnt = 0;
     uint32_t a_cur = kArenaEnd, a_first = kArenaEnd, a_fill = 0;
     bool a_failed = false;
@@ -369,7 +381,7 @@ void build_point_split(const double2* pts, uint32_t npts, const Lbvh& bvh, Point
 void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                    const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                    uint32_t* counts, DeviceStatus* st, cudaStream_t s, uint32_t* slots,
-                   uint32_t K, DwithinArena arena) {
+                   uint32_t K, DwithinArena arena, const double* d_row) {
   if (n == 0) return;
   float lo, hi;
   float_neighbours(d, lo, hi);
@@ -377,12 +389,12 @@ void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_
   if (slots && K > 0 && arena.words)
     k_dwithin_fused<false, true><<<g, kTravThreads, 0, s>>>(
         t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
-        n, d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, K, arena);
+        n, d, lo, hi, d_row, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, K, arena);
   else
     k_dwithin_fused<false, false><<<g, kTravThreads, 0, s>>>(
         t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
-        n, d, lo, hi, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots, slots ? K : 0,
-        DwithinArena());
+        n, d, lo, hi, d_row, order, counts, nullptr, 0, nullptr, nullptr, 0, st, slots,
+        slots ? K : 0, DwithinArena());
   SPJ_CUDA(cudaGetLastError());
 }
 
@@ -391,7 +403,7 @@ void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* prob
                      const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
                      uint32_t* out_probe, uint64_t capacity, cudaStream_t s,
                      const uint32_t* counts, const uint32_t* slots, uint32_t K,
-                     DwithinArena arena) {
+                     DwithinArena arena, const double* d_row) {
   if (!(slots && K > 0)) arena = DwithinArena();
   if (n == 0) return;
   float lo, hi;
@@ -400,12 +412,12 @@ void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* prob
   if (arena.words)
     k_dwithin_fused<true, true><<<g, kTravThreads, 0, s>>>(
         t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
-        n, d, lo, hi, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build,
+        n, d, lo, hi, d_row, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build,
         out_probe, capacity, nullptr, nullptr, slots ? K : 0, arena);
   else
     k_dwithin_fused<true, false><<<g, kTravThreads, 0, s>>>(
         t, bs.xy.as<double2>(), bs.hl.as<float4>(), bs.bmag, bs.ok ? 1 : 0, probe_box, probe_pt,
-        n, d, lo, hi, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build,
+        n, d, lo, hi, d_row, order, const_cast<uint32_t*>(counts), offs, probe_base, out_build,
         out_probe, capacity, nullptr, nullptr, slots ? K : 0, arena);
   SPJ_CUDA(cudaGetLastError());
   if (slots && K > 0)

@@ -51,15 +51,18 @@ struct DwithinArena {
   uint32_t* head = nullptr;
 };
 
+// d_row (device, one per probe row) replaces d when given.
 void dwithin_count(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                    const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                    uint32_t* counts, DeviceStatus* st, cudaStream_t s, uint32_t* slots = nullptr,
-                   uint32_t K = 0, DwithinArena arena = DwithinArena());
+                   uint32_t K = 0, DwithinArena arena = DwithinArena(),
+                   const double* d_row = nullptr);
 void dwithin_scatter(const LbvhView& t, const PointSplit& bs, const float4* probe_box,
                      const double2* probe_pt, uint32_t n, double d, const uint32_t* order,
                      const uint64_t* offs, uint32_t probe_base, uint32_t* out_build,
                      uint32_t* out_probe, uint64_t capacity, cudaStream_t s,
                      const uint32_t* counts = nullptr, const uint32_t* slots = nullptr,
-                     uint32_t K = 0, DwithinArena arena = DwithinArena());
+                     uint32_t K = 0, DwithinArena arena = DwithinArena(),
+                     const double* d_row = nullptr);
 
 }  // namespace spj

@@ -97,14 +97,15 @@ static inline float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 
 uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predicate,
                            double distance, uint32_t probe_base, const uint32_t** d_build,
-                           const uint32_t** d_probe) {
+                           const uint32_t** d_probe, const double* d_row) {
   SPJ_CHECK(built_, "probe called before the build side was finished");
   SPJ_CHECK(predicate == kPredDWithin || (predicate >= 0 && predicate <= 7),
             "unknown predicate code " + std::to_string(predicate));
   SPJ_CHECK(col.n >= 0 && (uint64_t)col.n + probe_base <= 0xFFFFFFFFull,
             "probe row ids exceed 32 bits");
-  if (predicate == kPredDWithin) SPJ_CHECK(distance >= 0 && !std::isnan(distance),
-                                           "ST_DWithin distance must be a non-negative number");
+  if (predicate == kPredDWithin && d_row == nullptr)
+    SPJ_CHECK(distance >= 0 && !std::isnan(distance),
+              "ST_DWithin distance must be a non-negative number");
   cudaStream_t s = ws.stream;
   const bool prof = cfg_.profile;
   uint64_t launches = 0;
@@ -119,11 +120,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
 
   const float4* boxes = ws.probe.box.as<float4>();
   if (predicate == kPredDWithin) {
-    SPJ_CHECK(ws.probe.all_points && bg_.all_points,
-              "ST_DWithin is supported for point build and probe sides");
     ws.boxes_tmp.reserve(((size_t)n + 1) * sizeof(float4), s);
-    expand_boxes(ws.probe.pt.as<double2>(), ws.probe.box.as<float4>(),
-                 ws.probe.kind.as<uint8_t>(), n, distance, ws.boxes_tmp.as<float4>(), s);
+    expand_boxes(ws.probe.view(), distance, d_row, ws.boxes_tmp.as<float4>(), s);
     boxes = ws.boxes_tmp.as<float4>();
     launches++;
   }
@@ -134,7 +132,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     if (order) launches += 21;  // keys + 4 radix passes (histogram, 3-kernel scan, scatter)
   }
   if (predicate == kPredDWithin && cfg_.fuse_dwithin && cfg_.refine_form == kFastF32 &&
-      bsplit_.n == bvh_.nprims && bvh_.nprims > 0) {
+      ws.probe.all_points && bsplit_.n == bvh_.nprims && bvh_.nprims > 0) {
     // point build and probe sides: the distance test runs inside the
     // traversal, no candidate pairs are materialized
     reset_status(ws.status, s);
@@ -164,7 +162,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
       }
     }
     dwithin_count(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.counts.as<uint32_t>(),
-                  ws.status.as<DeviceStatus>(), s, slots, K, arena);
+                  ws.status.as<DeviceStatus>(), s, slots, K, arena, d_row);
     scan_u32_u64(ws.psc.counts.as<uint32_t>(), ws.psc.offsets.as<uint64_t>(), n, ws.psc.tmp, s);
     uint64_t total = 0;
     DeviceStatus hst;
@@ -178,7 +176,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     ws.out_probe.reserve((total + 1) * 4, s);
     dwithin_scatter(tv, bsplit_, boxes, ppt, n, distance, order, ws.psc.offsets.as<uint64_t>(),
                     probe_base, ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), total,
-                    s, ws.psc.counts.as<uint32_t>(), slots, K, arena);
+                    s, ws.psc.counts.as<uint32_t>(), slots, K, arena, d_row);
     launches += 5 + (arena.words ? 1 : 0);
     if (prof) {
       SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
@@ -244,7 +242,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   if (predicate == kPredDWithin)
     refine_dwithin(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                    probe_base, distance, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                   ws.status.as<DeviceStatus>(), s, cperm);
+                   ws.status.as<DeviceStatus>(), s, cperm, d_row);
   else
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),

@@ -134,8 +134,11 @@ class JoinEngine {
   // Probe with a device WKB column.  Results (device pointers owned by the
   // workspace, valid until its next call) are grouped by probe row in
   // ascending probe order; probe ids are offset by probe_base.
+  // d_row (device, one per probe row): ST_DWithin distances per row; a
+  // negative or NaN distance matches nothing.
   uint64_t probe(Workspace& ws, const WkbDeviceColumn& col, int predicate, double distance,
-                 uint32_t probe_base, const uint32_t** d_build, const uint32_t** d_probe);
+                 uint32_t probe_base, const uint32_t** d_build, const uint32_t** d_probe,
+                 const double* d_row = nullptr);
 
   // Refine caller-supplied candidate pairs (device arrays) against an
   // already decoded probe column; output compacted into ws.out_*.

@@ -276,16 +276,33 @@ __global__ void __launch_bounds__(kTravThreads)
   }
 }
 
-__global__ void k_expand(const double2* __restrict__ pts, const float4* __restrict__ boxes,
-                         const uint8_t* __restrict__ kind, uint32_t n, double d,
+__global__ void k_expand(GeomsView G, double d0, const double* __restrict__ d_row,
                          float4* __restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < G.n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float q = __int_as_float(0x7fc00000);
     float4 o = make_float4(q, q, q, q);
-    if (kind[i] == 1) {
-      double2 p = pts[i];
-      double lo[2] = {p.x - d, p.y - d}, hi[2] = {p.x + d, p.y + d};
+    const double d = d_row ? d_row[i] : d0;
+    const uint8_t k = G.kind[i];
+    if (k != 0 && d >= 0) {
+      // the row's exact bounds (a point's coordinates, a polygon's ring
+      // rects), expanded by d in FP64, then rounded outward
+      double2 mn, mx;
+      if (k == 1) {
+        mn = mx = G.pt[i];
+      } else {
+        mn = make_double2(INFINITY, INFINITY);
+        mx = make_double2(-INFINITY, -INFINITY);
+        const uint32_t r0 = G.part_ring[G.row_part[i]], r1 = G.part_ring[G.row_part[i + 1]];
+        for (uint32_t r = r0; r < r1; r++) {
+          const Rect64 R = G.ring_rect[r];
+          mn.x = fmin(mn.x, R.x);
+          mn.y = fmin(mn.y, R.y);
+          mx.x = fmax(mx.x, R.z);
+          mx.y = fmax(mx.y, R.w);
+        }
+      }
+      double lo[2] = {mn.x - d, mn.y - d}, hi[2] = {mx.x + d, mx.y + d};
       float fl[2], fh[2];
       for (int a = 0; a < 2; a++) {
         float x = __double2float_rn(lo[a]), y = __double2float_rn(hi[a]);
@@ -295,8 +312,6 @@ __global__ void k_expand(const double2* __restrict__ pts, const float4* __restri
         fh[a] = y;
       }
       o = make_float4(fl[0], fl[1], fh[0], fh[1]);
-    } else if (kind[i] != 0) {
-      o = boxes[i];  // non-point rows: distance joins are point-only; caller rejects
     }
     out[i] = o;
   }
@@ -696,10 +711,11 @@ void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t npr
   fill_probe_ids(offs, nprobe, probe_base, out_probe, capacity, s);
 }
 
-void expand_boxes(const double2* pts, const float4* boxes, const uint8_t* kind, uint32_t n,
-                  double distance, float4* out, cudaStream_t s) {
+void expand_boxes(const GeomsView& g, double distance, const double* d_row, float4* out,
+                  cudaStream_t s) {
+  const uint32_t n = g.n;
   if (n == 0) return;
-  k_expand<<<grid_for(n, 256), 256, 0, s>>>(pts, boxes, kind, n, distance, out);
+  k_expand<<<grid_for(n, 256), 256, 0, s>>>(g, distance, d_row, out);
   SPJ_CUDA(cudaGetLastError());
 }
 

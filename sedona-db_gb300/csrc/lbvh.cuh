@@ -14,6 +14,7 @@
 // pair of child boxes (two 128-bit loads) plus one 8-byte child pair.
 #pragma once
 #include "common.cuh"
+#include "geoms.cuh"
 
 namespace spj {
 
@@ -193,9 +194,11 @@ void probe_scatter_from(const LbvhView& t, const float4* probe_box, uint32_t npr
                         uint32_t* out_probe, cudaStream_t s, uint64_t capacity = ~0ull,
                         const uint32_t* order = nullptr);
 
-// Expand point/box probes by a distance (f64), then round outward to f32
-// (rust/sedona-spatial-join/src/operand_evaluator.rs:605-607).
-void expand_boxes(const double2* pts, const float4* boxes, const uint8_t* kind, uint32_t n,
-                  double distance, float4* out, cudaStream_t s);
+// Each row's exact bounds expanded by a distance (f64: one value, or d_row,
+// one per row, on the device), then rounded outward to f32
+// (rust/sedona-spatial-join/src/operand_evaluator.rs:556-627, 605-607); empty
+// rows and negative or NaN distances give an empty (NaN) box.
+void expand_boxes(const GeomsView& g, double distance, const double* d_row, float4* out,
+                  cudaStream_t s);
 
 }  // namespace spj

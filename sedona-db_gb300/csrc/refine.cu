@@ -7,6 +7,7 @@
 // (src/rt/shaders/polygon_point_query.cu) or a recursive DE-9IM relate
 // (src/relate_engine.cu:294-336).  Here both sides are already decoded in HBM
 // and the predicate is the tg semantics the reference CPU join uses.
+#include "distance.cuh"
 #include "refine_eval.cuh"
 
 namespace spj {
@@ -21,7 +22,9 @@ using exact::dwithin_exact;
 __global__ void __launch_bounds__(256)
     k_dwithin(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
               const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, double d,
-              uint8_t* __restrict__ flags, DeviceStatus* st, const uint32_t* __restrict__ perm) {
+              const double* __restrict__ d_row, uint8_t* __restrict__ flags, DeviceStatus* st,
+              const uint32_t* __restrict__ perm) {
+  const double d0 = d;
   uint32_t esc = 0, pairs = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -33,9 +36,17 @@ __global__ void __launch_bounds__(256)
     if (k >= m) continue;
     const uint32_t bi = cb[k], pi = cp[k] - probe_base;
     pairs++;
-    if (B.kind[bi] != kPoint || P.kind[pi] != kPoint) {
-      status_fail(st, kUnsupported, k);
+    // the probe row's distance (a per-row column or one value); a negative
+    // or NaN distance keeps nothing
+    const double d = d_row ? d_row[pi] : d0;
+    if (!(d >= 0)) {
       flags[k] = 0;
+      continue;
+    }
+    if (B.kind[bi] != kPoint || P.kind[pi] != kPoint) {
+      // polygons: the reference's distance in FP64, compared with d
+      esc++;
+      flags[k] = row_distance<true>(B, bi, P, pi, esc) <= d ? 1 : 0;
       continue;
     }
     const double2 b = B.pt[bi], p = P.pt[pi];
@@ -106,11 +117,13 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
 
 void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                     const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
-                    uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint32_t* perm) {
+                    uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint32_t* perm,
+                    const double* d_row) {
   if (m == 0) return;
   (void)form;  // one form: see k_dwithin
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
-  k_dwithin<<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, flags, st, perm);
+  k_dwithin<<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, distance, d_row, flags, st,
+                              perm);
   SPJ_CUDA(cudaGetLastError());
 }
 

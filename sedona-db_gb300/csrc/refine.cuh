@@ -41,14 +41,16 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
                      int min_blocks = 4, uint32_t* queue = nullptr, uint32_t* qn = nullptr);
 
-// flags[k] = hypot(build - probe) <= distance for point pairs: an FP64
-// squared-distance test decides pairs outside a 1e-14 relative band around
-// d^2, expansion arithmetic the rest (both forms; the form argument is kept
-// for the interface).
+// flags[k] = distance(build, probe) <= d.  Point pairs: hypot, decided by an
+// FP64 squared-distance test outside a 1e-14 relative band around d^2 and by
+// expansion arithmetic inside it.  Pairs with a polygon: the reference's
+// FP64 distance (distance.cuh).  d is one value, or with d_row (device, one
+// per probe row, indexed by probe id - probe_base) the probe row's; a
+// negative or NaN distance keeps nothing.  Both forms run the same code.
 void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                     const uint32_t* cp, uint64_t m, uint32_t probe_base, double distance, int form,
                     uint8_t* flags, DeviceStatus* st, cudaStream_t s,
-                    const uint32_t* perm = nullptr);
+                    const uint32_t* perm = nullptr, const double* d_row = nullptr);
 
 // Stream compaction of (cb, cp) by flags: positions from an exclusive scan
 // of the flags (pos has m+1 entries).  Order is preserved.

@@ -156,7 +156,7 @@ EXPORTS = [
     "SpjJoinFinishBuild", "SpjJoinBuildDevice", "SpjJoinProbeArrow", "SpjJoinProbeDevice",
     "SpjJoinProbeHost", "SpjJoinStream", "SpjJoinGetStats", "SpjJoinResetStats",
     "SpjKnnCreate", "SpjKnnRelease", "SpjKnnLastError", "SpjKnnBuild", "SpjKnnQuery",
-    "SpjKnnQueryTies", "SpjKnnQueryArrow",
+    "SpjKnnQueryTies", "SpjKnnQueryArrow", "SpjJoinSetProbeDistances",
     "SpjKnnStream", "SpjKnnGetStats", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
     "SpjIndexProbeNoAlloc", "SpjAllocationCount",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
@@ -238,6 +238,8 @@ def lib() -> C.CDLL:
                                       C.c_void_p, C.c_void_p, C.c_int32]
             L.SpjKnnStream.argtypes = [C.c_void_p]
             L.SpjKnnStream.restype = C.c_void_p
+            L.SpjJoinSetProbeDistances.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64,
+                                                   C.c_int32]
             L.SpjKnnQueryTies.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
                                           C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
@@ -512,6 +514,16 @@ class SpatialJoin:
             len(out_b), C.byref(n))
         _check(rc, "probe_host", self._err)
         return n.value
+
+    def set_probe_distances(self, distances: Optional[np.ndarray]):
+        """ST_DWithin distance column: one distance per probe row for the
+        next probes (None clears it)."""
+        if distances is None:
+            _check(lib().SpjJoinSetProbeDistances(self.h, None, 0, 0), "set distances", self._err)
+            return
+        d = np.ascontiguousarray(distances, dtype=np.float64)
+        _check(lib().SpjJoinSetProbeDistances(self.h, d.ctypes.data, len(d), 0),
+               "set distances", self._err)
 
     def probe_device(self, dcol: SpjDeviceWkb, predicate: str = "intersects",
                      distance: float = 0.0, probe_base: int = 0):

@@ -684,3 +684,62 @@ def test_knn_wkb_column(capi, oracle_mod):
     poly = wkb.wkb_polygon([[(0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 0.0)]])
     with pytest.raises(capi.GpuSpatialError, match="points"):
         kj.query_wkb(wkb.column_from_values([vals[0], poly]), 2)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_dwithin_with_polygons(capi, oracle_mod, form):
+    """ST_DWithin between points and polygons and between polygons: the
+    reference's build.distance_ext(probe) <= d (refine/geo.rs:312-321, the
+    distances of sedona-geo-generic-alg's euclidean/utils.rs), probe rects
+    expanded by d; point build sides against polygon probes too."""
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload1(n_points=20000, n_polys=300)
+    for build, probe, d in ((inp.build, inp.probe, 2.0), (inp.probe, inp.build, 1.5)):
+        j = capi.SpatialJoin(refine_form=form)
+        j.build(build)
+        b, p = j.probe(probe, "dwithin", distance=d)
+        exp = oracle_pairs(oracle_mod, build, probe, "dwithin", d)
+        assert len(exp) > 100
+        assert pairs(b, p) == exp
+    inp2 = datagen.workload2(n_buildings=4000, n_zones=80)
+    j = capi.SpatialJoin(refine_form=form)
+    j.build(inp2.build)
+    b, p = j.probe(inp2.probe, "dwithin", distance=120.0)
+    exp = oracle_pairs(oracle_mod, inp2.build, inp2.probe, "dwithin", 120.0)
+    assert len(exp) > 100
+    assert pairs(b, p) == exp
+
+
+def test_dwithin_distance_column(capi, oracle_mod):
+    """A distance per probe row (operand_evaluator.rs:556-627): point pairs
+    (decided inside the traversal) and polygon pairs, with null (NaN) and
+    negative distances matching nothing."""
+    from sedona_gpuspatial import datagen
+    rng = np.random.default_rng(21)
+    inp = datagen.workload4(n_probe=20000, n_build=20000)
+    d = rng.uniform(0, 400, len(inp.probe))
+    d[::17] = np.nan
+    d[5::23] = -1.0
+    j = capi.SpatialJoin()
+    j.build(inp.build)
+    j.set_probe_distances(d)
+    b, p = j.probe(inp.probe, "dwithin", distance=0.0)
+    ob, op = oracle_mod.join_dists(oracle_mod.Geoms(inp.build), oracle_mod.Geoms(inp.probe), d,
+                                   nthreads=4)
+    assert len(ob) > 1000
+    assert pairs(b, p) == pairs(ob, op)
+    j.set_probe_distances(None)
+    b2, p2 = j.probe(inp.probe, "dwithin", distance=100.0)
+    assert pairs(b2, p2) == oracle_pairs(oracle_mod, inp.build, inp.probe, "dwithin", 100.0)
+    inp1 = datagen.workload1(n_points=10000, n_polys=200)
+    dp = rng.uniform(0, 3, len(inp1.probe))
+    dp[::11] = np.nan
+    j1 = capi.SpatialJoin()
+    j1.build(inp1.build)
+    j1.set_probe_distances(dp)
+    b, p = j1.probe(inp1.probe, "dwithin", distance=0.0)
+    ob, op = oracle_mod.join_dists(oracle_mod.Geoms(inp1.build), oracle_mod.Geoms(inp1.probe),
+                                   dp, nthreads=4)
+    assert pairs(b, p) == pairs(ob, op)
+    with pytest.raises(capi.GpuSpatialError, match="distance column"):
+        j1.probe(inp1.probe.slice(0, 100), "dwithin", distance=0.0)

@@ -164,3 +164,36 @@ def test_oracle_matches_reference_fixtures(oracle_lib, name):
     for pred, pairs in exp.items():
         b, p = oracle_lib.join(B, P, pred, nthreads=4)
         assert sorted(zip(p.tolist(), b.tolist())) == pairs, pred
+
+
+def test_geo_distance_known_answers(oracle_lib):
+    """build.distance_ext(probe) as restated from the reference's
+    sedona-geo-generic-alg (euclidean/utils.rs): point-polygon, polygon-
+    polygon, a polygon inside another's hole, multipolygons."""
+    from sedona_gpuspatial import wkb
+
+    def sq(x0, y0, x1, y1):
+        return [(x0, y0), (x1, y0), (x1, y1), (x0, y1), (x0, y0)]
+
+    build = wkb.column_from_values([
+        wkb.wkb_polygon([sq(0.0, 0.0, 1.0, 1.0)]),
+        wkb.wkb_polygon([sq(0.0, 0.0, 10.0, 10.0), sq(2.0, 2.0, 8.0, 8.0)]),
+        wkb.wkb_multipolygon([[sq(0.0, 0.0, 1.0, 1.0)], [sq(5.0, 0.0, 6.0, 1.0)]]),
+        wkb.wkb_point(0.0, 0.0),
+    ])
+    probe = wkb.column_from_values([
+        wkb.wkb_point(3.0, 0.5), wkb.wkb_point(0.5, 0.5), wkb.wkb_point(4.0, 5.0),
+        wkb.wkb_polygon([sq(3.0, 0.0, 4.0, 1.0)]), wkb.wkb_polygon([sq(4.0, 4.0, 5.0, 6.0)]),
+        wkb.wkb_point(3.0, 4.0),
+    ])
+    B, P = oracle_lib.Geoms(build), oracle_lib.Geoms(probe)
+    d = lambda b, p: oracle_lib.geo_distance(B, b, P, p)  # noqa: E731
+    assert d(0, 0) == 2.0 and d(0, 1) == 0.0 and d(0, 3) == 2.0
+    assert d(1, 2) == 2.0            # a point in the hole: 2 to the hole's edge
+    assert d(1, 4) == 2.0            # a polygon inside the hole: 2 to the hole's edge
+    assert d(2, 0) == 2.0 and d(2, 3) == 1.0   # the nearest part of a multipolygon
+    assert d(3, 5) == 5.0            # points: hypot
+    b, p = oracle_lib.join_dists(B, P, np.array([2.0, 0.0, 0.5, 1.0, 2.0, 4.0]), nthreads=2)
+    got = sorted(zip(p.tolist(), b.tolist()))
+    assert (0, 0) in got and (1, 0) in got and (4, 1) in got and (3, 2) in got
+    assert (5, 3) not in got and (3, 0) not in got
