@@ -301,9 +301,9 @@ def run_ours(args, world, rank, local, pg, light=False, workload=None, pred_over
     # (they change speed only; the pair count is checked)
     variants = {}
     option_sets = [] if light else [{"candidate_order": 0}, {"refine_min_blocks": 4},
-                                     {"cell_grid": 0}, {"grid_rings": 0},
+                                     {"cell_grid": 0}, {"grid_rings": 1},
                                      {"probe_order": -1},
-                                     {"refine_split": 1},
+                                     {"refine_split": 1}, {"refine_split": 3},
                                      {"candidate_order": 0, "refine_split": 0}]
     if pred == "dwithin" and not light:
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},

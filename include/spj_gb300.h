@@ -102,13 +102,14 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *                       build-major order), 1 on, 0 off: FP32 refine of
  *                       relation predicates in two passes (a cheap pass over
  *                       all pairs queues the pairs it leaves open for a full
- *                       pass)
+ *                       pass); 3 on, with the queue sorted back into the
+ *                       candidate order before the full pass
  *   "host_slices"       0 (default: auto, 2 from 524,288 rows), 1 (one
  *                       call), 2-64: row slices of SpjJoinProbeHost
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
- *   "grid_rings"        1 (default) / 0: ring-ring and ring-in-ring tests
+ *   "grid_rings"        0 (default) / 1: ring-ring and ring-in-ring tests
  *                       answer from the build ring's clean cells when the
  *                       probe ring's box lies in them
  *   "dwithin_arena"     2 (default: auto, on when the probes are not in

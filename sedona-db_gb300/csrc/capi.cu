@@ -798,7 +798,7 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
       SPJ_CHECK(value == 0 || value == 2 || value == 3, "candidate_order must be 0, 2 or 3");
       c.candidate_order = (int)value;
     } else if (k == "refine_split") {
-      SPJ_CHECK(value >= 0 && value <= 2, "refine_split must be 0, 1 or 2");
+      SPJ_CHECK(value >= 0 && value <= 3, "refine_split must be 0, 1, 2 or 3");
       c.refine_split = (int)value;
     } else if (k == "host_slices") {
       SPJ_CHECK(value >= 0 && value <= 64, "host_slices must be in [0, 64]");

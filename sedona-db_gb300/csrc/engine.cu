@@ -232,7 +232,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   ws.flags.reserve(m + 1, s);
   uint32_t *rq = nullptr, *rqn = nullptr;
   const int mb = refine_blocks(cfg_.refine_min_blocks, build_major);
-  const bool split = cfg_.refine_split == 1 || (cfg_.refine_split == 2 && !build_major);
+  const bool split = cfg_.refine_split == 1 || cfg_.refine_split == 3 ||
+                     (cfg_.refine_split == 2 && !build_major);
   if (split && cfg_.refine_form == kFastF32 && predicate != kPredDWithin) {
     ws.rqueue.reserve((m + 2) * 4, s);
     rq = ws.rqueue.as<uint32_t>();
@@ -246,7 +247,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   else
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
-                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb, rq, rqn);
+                    ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb, rq, rqn,
+                    cfg_.refine_split == 3);
   launches += rq ? 2 : 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 

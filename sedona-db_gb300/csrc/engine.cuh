@@ -59,14 +59,17 @@ struct EngineConfig {
   // tests in O(1)); set before the build
   bool cell_grid = true;
   // ring-ring and ring-in-ring tests answer from the build ring's clean cells
-  // when the probe ring's box lies in them
-  bool grid_rings = true;
+  // when the probe ring's box lies in them (2M buildings x 50k star zones:
+  // 63.0 ms per step with it, 52.7 without: the zones' spiky edges leave few
+  // buildings inside clean cells, and the lookup costs every pair)
+  bool grid_rings = false;
   // FP32 refine in two passes: a cheap pass (isolation exit, first vertex)
   // over every pair queues the pairs it leaves open, a full pass takes the
   // queue (a warp's lanes then hold pairs of similar cost).  0 off, 1 on,
   // 2 auto: on unless the candidates are in build-major order, where a
   // warp's pairs already share one build geometry (2M x 50k polygons: 59.0
-  // ms one pass vs 61.0 split in build-major order; 78.0 vs 63.3 as listed)
+  // ms one pass vs 61.0 split in build-major order; 78.0 vs 63.3 as listed);
+  // 3 on, with the open pairs' queue sorted back into candidate order
   int refine_split = 2;
   // host probes (SpjJoinProbeHost): 0 auto (2 slices from 524,288 rows up),
   // 1 one call, n > 1 that many slices

@@ -34,12 +34,14 @@ enum RefineForm : int {
 // 256-thread blocks per SM: fewer registers, more warps to hide the latency
 // of divergent pairs.  queue (m entries) and qn (one device word) split the
 // FP32 refine into a cheap pass over all pairs that queues the pairs it
-// cannot decide, then a full pass over the queue; same flags.
+// cannot decide, then a full pass over the queue (ordered_queue: sorted back
+// into perm's order first); same flags.
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,
                      const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
-                     int min_blocks = 4, uint32_t* queue = nullptr, uint32_t* qn = nullptr);
+                     int min_blocks = 4, uint32_t* queue = nullptr, uint32_t* qn = nullptr,
+                     bool ordered_queue = false);
 
 // flags[k] = distance(build, probe) <= d.  Point pairs: hypot, decided by an
 // FP64 squared-distance test outside a 1e-14 relative band around d^2 and by

@@ -198,7 +198,11 @@ __global__ void __launch_bounds__(256, kMinBlocks)
              const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, int predicate,
              uint8_t* __restrict__ flags, DeviceStatus* st, const uint64_t* __restrict__ m_dev,
              const uint32_t* __restrict__ perm, uint32_t* __restrict__ queue = nullptr,
-             uint32_t* __restrict__ qn = nullptr) {
+             uint32_t* __restrict__ qn = nullptr,
+             const uint32_t* __restrict__ slot_perm = nullptr) {
+  // slot_perm (the split refine with an ordered queue): phase 1 queues the
+  // slots u of perm instead of the candidates (the host sorts them), and
+  // phase 2 maps a queued slot back through slot_perm
   uint32_t esc = 0, pairs = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   // with m_dev the pair count lives on the device (graph replays) and m is
@@ -216,7 +220,8 @@ __global__ void __launch_bounds__(256, kMinBlocks)
     // a permutation with a device-side count covers slots [0, mm) only (the
     // caller clears the flags past mm)
     if (kPhase != 2 && perm != nullptr && m_dev != nullptr && u >= mm) continue;
-    const uint64_t k = perm ? (uint64_t)perm[u] : u;
+    uint64_t k = perm ? (uint64_t)perm[u] : u;
+    if (kPhase == 2 && slot_perm != nullptr) k = k < m ? (uint64_t)slot_perm[k] : ~0ull;
     if (k >= mm) {
       if (kPhase != 2 && k < m) flags[k] = 0;
       continue;
@@ -230,7 +235,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(qn, (uint32_t)__popc(act));
       base = __shfl_sync(act, base, leader);
-      queue[base + __popc(act & ((1u << lane) - 1u))] = (uint32_t)k;
+      queue[base + __popc(act & ((1u << lane) - 1u))] = slot_perm ? (uint32_t)u : (uint32_t)k;
       continue;
     }
     pairs++;
@@ -260,8 +265,9 @@ struct RefineLaunch {
   cudaStream_t s;
 };
 // refine_split.cu: the cheap pass then the full pass over its queue
-// (min_blocks 4 or 6)
-void launch_refine_split(const RefineLaunch& a, int min_blocks);
+// (min_blocks 4 or 6); ordered (with a perm): the queue is sorted back into
+// the perm's order before the full pass
+void launch_refine_split(const RefineLaunch& a, int min_blocks, bool ordered = false);
 // refine_blocks.cu: one pass, FP32 form built for 6 resident blocks per SM
 void launch_refine_blocks6(const RefineLaunch& a);
 

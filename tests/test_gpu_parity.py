@@ -235,7 +235,7 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     # (probe_order, candidate_order, refine_min_blocks, cell_grid, refine_split)
     variants = [(-1, 0, 4, 0, 0), (1, 2, 6, 1, 0), (1, 3, 0, 1, 1), (0, 2, 0, 1, 1),
                 (-1, 0, 4, 1, 1), (1, 2, 6, 0, 1), (1, 3, 0, 1, 2), (-1, 0, 0, 1, 2),
-                (-1, 2, 4, 0, 1), (1, 0, 6, 1, 1)]
+                (-1, 2, 4, 0, 1), (1, 0, 6, 1, 1), (1, 2, 6, 1, 3), (-1, 0, 4, 1, 3)]
     for v in variants:
         j = capi.SpatialJoin(probe_order=v[0])
         j.set_option("candidate_order", v[1])
