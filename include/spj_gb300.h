@@ -335,6 +335,63 @@ void* SpjKnnStream(SpjKnn* knn);
 int SpjKnnGetStats(SpjKnn* knn, uint64_t* queries, uint64_t* exact_evals, uint64_t* redone);
 
 /* ------------------------------------------------------------------------ */
+/* Result materialisation on the device.                                    */
+/*                                                                          */
+/* The joined batch is built from the refined (build, probe) index pairs by */
+/* one Arrow `take` per column (build_batch_from_indices,                   */
+/* rust/sedona-spatial-join/src/utils/join_utils.rs:346-405, called from    */
+/* build_joined_batch, rust/sedona-spatial-join/src/stream.rs:1466-1502);   */
+/* outer, semi, anti and mark joins keep a visited bitmap of build rows     */
+/* (mark_build_side_rows_as_visited, stream.rs:1447-1455) and emit the      */
+/* unmatched (or matched) rows at the end (get_final_indices_from_bit_map,  */
+/* join_utils.rs:95-124).  These entry points do both on device buffers so  */
+/* the pairs never leave HBM.  Every pointer except the counts is device    */
+/* memory; stream is a cudaStream_t (NULL = default stream); each call      */
+/* synchronizes it.  Errors: EINVAL with SpjMaterializeLastError (per       */
+/* thread), ENOSPC when an output is too small (the needed size is still    */
+/* returned).                                                               */
+
+/* An index of this value gathers a null row (the missing side of an outer
+ * join's unmatched rows); so does an index >= n_values. */
+#define SPJ_NULL_INDEX 0xFFFFFFFFu
+
+const char* SpjMaterializeLastError(void);
+/* out[i] = values[idx[i]] for fixed-width values of width 1, 2, 4, 8 or 16
+ * bytes (Arrow primitive / fixed-size columns; a boolean column is gathered
+ * by SpjGatherValidity over its value bits); a null index writes zero bytes. */
+int SpjGatherFixed(const void* d_values, uint32_t width, uint64_t n_values,
+                   const uint32_t* d_idx, uint64_t n, void* d_out, void* stream);
+/* The validity bitmap of the gathered rows: bit i (LSB order, written as
+ * 32-bit words, so d_out_bitmap holds ceil(n / 32) words and is 4-byte
+ * aligned) is set when idx[i] is not null and the source row is valid (bit
+ * validity_offset + idx[i] of d_validity; NULL = every row valid).
+ * *null_count (host) receives the number of clear bits. */
+int SpjGatherValidity(const uint8_t* d_validity, int64_t validity_offset, uint64_t n_values,
+                      const uint32_t* d_idx, uint64_t n, uint8_t* d_out_bitmap,
+                      uint64_t* null_count, void* stream);
+/* Gather of a binary / utf8 column (WKB geometry included): source offsets
+ * int32 (offsets_are_64bit = 0) or int64, n_values + 1 of them; output
+ * offsets are int64 (n + 1 of them, large_binary layout, always written) and
+ * the values' bytes go to d_out_data.  *out_bytes (host) receives the total;
+ * when it exceeds capacity, only the offsets are written and ENOSPC is
+ * returned.  Null indices give empty values. */
+int SpjGatherBinary(const void* d_offsets, int32_t offsets_are_64bit, const uint8_t* d_data,
+                    uint64_t n_values, const uint32_t* d_idx, uint64_t n,
+                    int64_t* d_out_offsets, uint8_t* d_out_data, uint64_t capacity,
+                    uint64_t* out_bytes, void* stream);
+/* Set bit idx[i] of a row bitmap (ceil(n_rows / 32) 32-bit words, LSB
+ * order, which is Arrow's bitmap layout on a little-endian machine; the
+ * caller zeroes it once per build side).  Indices >= n_rows are skipped. */
+int SpjVisitedMark(uint32_t* d_bitmap, uint64_t n_rows, const uint32_t* d_idx, uint64_t n,
+                   void* stream);
+/* The rows whose bit is set (visited = 1: semi joins) or clear (visited = 0:
+ * left, left anti and full joins), ascending, into d_out_idx; *count (host)
+ * receives how many; when it exceeds capacity nothing is written and ENOSPC
+ * is returned.  A mark join reads the bitmap itself. */
+int SpjVisitedCollect(const uint32_t* d_bitmap, uint64_t n_rows, int32_t visited,
+                      uint32_t* d_out_idx, uint64_t capacity, uint64_t* count, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Probe without allocating.  No counterpart in the reference interface.     */
 
 /* Largest n_rects one SpjIndexProbeNoAlloc call accepts. */

@@ -159,6 +159,8 @@ EXPORTS = [
     "SpjKnnQueryTies", "SpjKnnQueryArrow", "SpjJoinSetProbeDistances",
     "SpjKnnStream", "SpjKnnGetStats", "SpjHostRegister", "SpjHostUnregister", "SpjVersion",
     "SpjIndexProbeNoAlloc", "SpjAllocationCount",
+    "SpjMaterializeLastError", "SpjGatherFixed", "SpjGatherValidity", "SpjGatherBinary",
+    "SpjVisitedMark", "SpjVisitedCollect",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
     "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
     "SpjStreamCudaStream",
@@ -247,6 +249,20 @@ def lib() -> C.CDLL:
                                            C.POINTER(ArrowArray), C.c_uint32, C.c_int32,
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
                                            C.POINTER(C.c_uint64)]
+            L.SpjMaterializeLastError.argtypes = []
+            L.SpjMaterializeLastError.restype = C.c_char_p
+            L.SpjGatherFixed.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_void_p,
+                                         C.c_uint64, C.c_void_p, C.c_void_p]
+            L.SpjGatherValidity.argtypes = [C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p,
+                                            C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64),
+                                            C.c_void_p]
+            L.SpjGatherBinary.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64,
+                                          C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                          C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]
+            L.SpjVisitedMark.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                                         C.c_void_p]
+            L.SpjVisitedCollect.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p,
+                                            C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]
             L.SpjAllocationCount.argtypes = []
             L.SpjAllocationCount.restype = C.c_uint64
             L.SpjHostRegister.argtypes = [C.c_void_p, C.c_uint64]
