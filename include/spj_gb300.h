@@ -335,6 +335,63 @@ void* SpjKnnStream(SpjKnn* knn);
 int SpjKnnGetStats(SpjKnn* knn, uint64_t* queries, uint64_t* exact_evals, uint64_t* redone);
 
 /* ------------------------------------------------------------------------ */
+/* GeoParquet -> device.                                                    */
+/*                                                                          */
+/* The reference reads GeoParquet with arrow-rs on the CPU                  */
+/* (rust/sedona-geoparquet/src/file_opener.rs:125-210; geometry columns and */
+/* the primary column from the "geo" key, metadata.rs:382-460) and parses   */
+/* the WKB values again on the CPU before the join (operand_evaluator.rs).  */
+/* Here the host reads only the footer and the page headers; the column     */
+/* chunks go to HBM in one copy and their pages are decompressed (SNAPPY or */
+/* stored) and decoded (definition levels, PLAIN and dictionary-encoded     */
+/* BYTE_ARRAY values, data pages v1 and v2) by kernels, into a device       */
+/* column for SpjJoinBuildDevice / SpjJoinProbeDevice / SpjLearned*.        */
+/* Other codecs and encodings, nested columns and GeoParquet's native       */
+/* (non-WKB) encodings are rejected with a message.                         */
+
+typedef struct SpjParquet SpjParquet;
+
+/* Opens a file and parses its footer (host only, no device work).  On
+ * failure *out is NULL and SpjParquetLastError(NULL) has the message. */
+int SpjParquetOpen(const char* path, SpjParquet** out);
+void SpjParquetRelease(SpjParquet* file);
+/* The handle's last error; with NULL, the calling thread's last
+ * SpjParquetOpen / SpjParquetWriteWkb error. */
+const char* SpjParquetLastError(SpjParquet* file);
+int SpjParquetInfo(SpjParquet* file, int64_t* num_rows, int32_t* num_row_groups,
+                   int32_t* num_columns);
+/* Leaf column i's name (dotted path), or with i = -1 the GeoParquet primary
+ * geometry column; EINVAL when absent or when cap is too small. */
+int SpjParquetColumnName(SpjParquet* file, int32_t i, char* buf, uint64_t cap);
+int SpjParquetRowGroupRows(SpjParquet* file, int32_t row_group, int64_t* rows);
+/* Reads row groups [rg_begin, rg_end) (rg_end < 0: to the last) of a WKB
+ * column (NULL: the primary geometry column) onto `device`.  *out receives a
+ * device Arrow large_binary column (int64 offsets; validity NULL when the
+ * rows have no nulls) owned by the handle and valid until its next read or
+ * release.  Synchronous. */
+int SpjParquetReadWkb(SpjParquet* file, const char* column, int32_t rg_begin, int32_t rg_end,
+                      int32_t device, struct SpjDeviceWkb* out);
+/* The last read: device time in ms (H2D copy through the last kernel, CUDA
+ * events), bytes read from the file, decompressed page bytes, WKB bytes. */
+int SpjParquetGetStats(SpjParquet* file, double* ms_device, uint64_t* file_bytes,
+                       uint64_t* page_bytes, uint64_t* value_bytes);
+
+struct SpjParquetWriteOptions {
+  int32_t compression;    /* 0 none, 1 SNAPPY */
+  int32_t page_version;   /* 1 or 2 (data page v1 / v2) */
+  int64_t row_group_rows; /* 0 = 1,048,576 */
+  int64_t page_bytes;     /* values per page, 0 = 1 MiB */
+};
+/* Writes a host WKB column (Arrow binary / large_binary buffers) as a
+ * GeoParquet 1.1 file with one optional BYTE_ARRAY column, PLAIN encoded
+ * (the reference's writer: rust/sedona-geoparquet/src/writer.rs); host only.
+ * options may be NULL (SNAPPY, v1 pages). */
+int SpjParquetWriteWkb(const char* path, const char* column, int64_t length,
+                       const void* offsets, int32_t offsets_are_64bit, const uint8_t* data,
+                       const uint8_t* validity, int64_t validity_offset,
+                       const struct SpjParquetWriteOptions* options);
+
+/* ------------------------------------------------------------------------ */
 /* Result materialisation on the device.                                    */
 /*                                                                          */
 /* The joined batch is built from the refined (build, probe) index pairs by */

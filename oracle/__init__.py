@@ -89,6 +89,9 @@ def lib():
         L.spjo_digest.restype = C.c_uint64
         L.spjo_digest.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int64]
         L.spjo_free.argtypes = [C.c_void_p]
+        L.spjo_parquet_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                        C.POINTER(C.c_void_p), C.c_char_p, C.c_int]
         _lib = L
     return _lib
 
@@ -238,3 +241,29 @@ def ref():
 def ref_predicate(build_wkb: bytes, probe_wkb: bytes, pred: str, index: int = 3) -> int:
     return ref().tgref_pred(build_wkb, len(build_wkb), probe_wkb, len(probe_wkb), PRED[pred],
                             index)
+
+
+def parquet_read(path: str, column: Optional[str] = None):
+    """A GeoParquet BYTE_ARRAY column read on the CPU (spj_parquet.c):
+    (int64 offsets with nulls empty, uint8 data, bool valid)."""
+    L = lib()
+    n = C.c_int64()
+    po, pd, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    err = C.create_string_buffer(512)
+    rc = L.spjo_parquet_read(path.encode(), column.encode() if column else None, C.byref(n),
+                             C.byref(po), C.byref(pd), C.byref(pv), err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    try:
+        rows = n.value
+        off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_int64)), shape=(rows + 1,)).copy()
+        nbytes = int(off[-1])
+        data = (np.ctypeslib.as_array(C.cast(pd, C.POINTER(C.c_uint8)), shape=(nbytes,)).copy()
+                if nbytes else np.zeros(0, np.uint8))
+        valid = (np.ctypeslib.as_array(C.cast(pv, C.POINTER(C.c_uint8)), shape=(rows,)).copy()
+                 .astype(bool) if rows else np.zeros(0, bool))
+    finally:
+        L.spjo_free(po)
+        L.spjo_free(pd)
+        L.spjo_free(pv)
+    return off, data, valid

@@ -111,6 +111,14 @@ uint64_t spjo_digest(const uint32_t* build, const uint32_t* probe, int64_t n);
 
 void spjo_free(void* p);
 
+/* GeoParquet (spj_parquet.c): a flat BYTE_ARRAY column (NULL: the "geo"
+ * metadata's primary column) of every row group.  On success returns 0 and
+ * malloc'd arrays: offsets (n + 1, nulls are empty), data, valid (one byte
+ * per row); free them with spjo_free.  On failure returns -1 with a message
+ * in err. */
+int spjo_parquet_read(const char* path, const char* column, int64_t* n_rows, int64_t** offsets,
+                      uint8_t** data, uint8_t** valid, char* err, int errcap);
+
 #ifdef __cplusplus
 }
 #endif

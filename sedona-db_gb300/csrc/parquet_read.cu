@@ -1,0 +1,824 @@
+// parquet_read.cu — GeoParquet WKB column chunks decoded on the device, and
+// the SpjParquet* entry points.
+//
+// One read (all on the handle's stream, one H2D copy of the chunk bytes):
+//   host           footer (parsed at open); chunk bytes -> page-locked
+//                  buffer; page headers -> page table
+//   k_unsnap       warp per compressed page: Snappy elements decoded in
+//                  order, each element's bytes moved by the 32 lanes (a
+//                  back-reference shorter than its length repeats its
+//                  pattern, so every lane's byte is known without waiting)
+//   k_dict_pages   warp per dictionary page: PLAIN byte arrays -> entries
+//   k_data_pages   warp per data page: RLE / bit-packed definition levels ->
+//                  per-row validity; PLAIN values (equal-length values are
+//                  located in parallel after a parallel check of every length
+//                  word, others by a walk) or dictionary indices -> per-row
+//                  (address, length)
+//   scan           lengths -> int64 offsets
+//   k_copy_values  warp per row: value bytes -> the output data buffer
+//   k_pack_valid   validity bytes -> an Arrow bitmap (only with nulls)
+// Every read of page bytes is bounded by its page; a malformed page sets a
+// status word (first error: code, page) that the host turns into a message.
+#include <errno.h>
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+
+#include "../../include/spj_gb300.h"
+#include "parquet.cuh"
+#include "prims.cuh"
+
+namespace spj {
+namespace pq {
+namespace {
+
+enum PqError : uint32_t {
+  kErrSnappy = 1,
+  kErrLevels = 2,
+  kErrPlain = 3,
+  kErrDictIndex = 4,
+  kErrDictPage = 5,
+  kErrPageShort = 6,
+};
+
+__device__ __forceinline__ void set_error(uint32_t* status, uint32_t code, uint32_t page) {
+  if (atomicCAS(status, 0u, code) == 0u) status[1] = page;
+}
+
+__device__ __forceinline__ uint32_t ld_le32(const uint8_t* p) {
+  return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+
+__device__ __forceinline__ bool rd_varint(const uint8_t*& p, const uint8_t* end, uint64_t& v) {
+  v = 0;
+  for (int sh = 0; sh < 64; sh += 7) {
+    if (p >= end) return false;
+    const uint8_t b = *p++;
+    v |= (uint64_t)(b & 0x7f) << sh;
+    if (!(b & 0x80)) return true;
+  }
+  return false;
+}
+
+// Snappy block decompression by one warp (every lane runs the same element
+// loop); false on malformed input.
+__device__ bool unsnap_warp(const uint8_t* in, uint32_t in_n, uint8_t* out, uint32_t out_n) {
+  const int lane = threadIdx.x & 31;
+  const uint8_t* ip = in;
+  const uint8_t* end = in + in_n;
+  uint64_t ulen;
+  if (!rd_varint(ip, end, ulen) || ulen != out_n) return false;
+  uint32_t op = 0;
+  while (ip < end) {
+    const uint8_t tag = *ip++;
+    uint32_t len, off = 0;
+    const int kind = tag & 3;
+    if (kind == 0) {
+      len = (uint32_t)(tag >> 2) + 1;
+      if (len > 60) {
+        const int nb = (int)len - 60;
+        if (end - ip < nb) return false;
+        uint32_t v = 0;
+        for (int b = 0; b < nb; b++) v |= (uint32_t)ip[b] << (8 * b);
+        ip += nb;
+        if (v == 0xffffffffu) return false;
+        len = v + 1;
+      }
+      if ((uint64_t)(end - ip) < len || (uint64_t)op + len > out_n) return false;
+      for (uint32_t i = lane; i < len; i += 32) out[op + i] = ip[i];
+      ip += len;
+    } else {
+      if (kind == 1) {
+        if (end - ip < 1) return false;
+        len = ((tag >> 2) & 7) + 4;
+        off = ((uint32_t)(tag >> 5) << 8) | ip[0];
+        ip += 1;
+      } else if (kind == 2) {
+        if (end - ip < 2) return false;
+        len = (uint32_t)(tag >> 2) + 1;
+        off = (uint32_t)ip[0] | ((uint32_t)ip[1] << 8);
+        ip += 2;
+      } else {
+        if (end - ip < 4) return false;
+        len = (uint32_t)(tag >> 2) + 1;
+        off = ld_le32(ip);
+        ip += 4;
+      }
+      if (off == 0 || off > op || (uint64_t)op + len > out_n) return false;
+      const uint8_t* from = out + op - off;
+      if (off >= len) {
+        for (uint32_t i = lane; i < len; i += 32) out[op + i] = from[i];
+      } else {
+        for (uint32_t i = lane; i < len; i += 32) out[op + i] = from[i % off];
+      }
+    }
+    op += len;
+    __syncwarp();  // the bytes just written may be the next element's source
+  }
+  return op == out_n;
+}
+
+__global__ void k_unsnap(const PageInfo* __restrict__ pages, uint32_t np,
+                         const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                         uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
+    const PageInfo pg = pages[p];
+    if (pg.in_src) continue;
+    const uint8_t* in = src + pg.src;
+    uint8_t* out = dst + pg.dst;
+    if (pg.lvl_bytes > pg.src_size || pg.lvl_bytes > pg.raw_size) {
+      if (lane == 0) set_error(status, kErrPageShort, p);
+      continue;
+    }
+    for (uint32_t i = lane; i < pg.lvl_bytes; i += 32) out[i] = in[i];
+    const bool ok = unsnap_warp(in + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
+                                out + pg.lvl_bytes, pg.raw_size - pg.lvl_bytes);
+    if (!ok && lane == 0) set_error(status, kErrSnappy, p);
+  }
+}
+
+__device__ __forceinline__ const uint8_t* page_bytes(const PageInfo& pg, const uint8_t* src,
+                                                     const uint8_t* dst) {
+  return pg.in_src ? src + pg.src : dst + pg.dst;
+}
+
+// Dictionary pages: lane 0 walks the PLAIN values (dictionaries are small).
+__global__ void k_dict_pages(const PageInfo* __restrict__ pages, uint32_t np,
+                             const uint8_t* __restrict__ src, const uint8_t* __restrict__ dst,
+                             const uint64_t* __restrict__ dict_base,
+                             uint64_t* __restrict__ dict_ptr, uint32_t* __restrict__ dict_len,
+                             uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
+    const PageInfo pg = pages[p];
+    if (pg.kind != 0 || lane != 0) continue;
+    const uint8_t* q = page_bytes(pg, src, dst);
+    const uint8_t* end = q + pg.raw_size;
+    const uint64_t base = dict_base[pg.dict];
+    for (uint32_t k = 0; k < pg.num_values; k++) {
+      if (end - q < 4) {
+        set_error(status, kErrDictPage, p);
+        break;
+      }
+      const uint32_t l = ld_le32(q);
+      if ((uint64_t)(end - q - 4) < l) {
+        set_error(status, kErrDictPage, p);
+        break;
+      }
+      dict_ptr[base + k] = reinterpret_cast<uint64_t>(q + 4);
+      dict_len[base + k] = l;
+      q += 4 + l;
+    }
+  }
+}
+
+// RLE / bit-packed hybrid decode of `count` values of width bw (<= 32) by a
+// warp: run headers are read by every lane (the same address), each run's
+// values are written by the lanes in parallel.  false on malformed input.
+template <class W>
+__device__ bool rle_hybrid_warp(const uint8_t* p, const uint8_t* end, int bw, uint32_t count,
+                                W&& write) {
+  const int lane = threadIdx.x & 31;
+  const int vbytes = (bw + 7) >> 3;
+  const uint64_t mask = bw == 32 ? 0xffffffffull : ((1ull << bw) - 1);
+  uint32_t i = 0;
+  while (i < count) {
+    uint64_t h;
+    if (!rd_varint(p, end, h)) return false;
+    if (h & 1) {
+      const uint64_t groups = h >> 1;
+      if (groups == 0 || groups > (1ull << 32)) return false;
+      const uint64_t take = min(groups * 8, (uint64_t)(count - i));
+      const uint64_t need = (take * (uint64_t)bw + 7) >> 3;
+      if ((uint64_t)(end - p) < need) return false;
+      for (uint64_t k = lane; k < take; k += 32) {
+        uint32_t v = 0;
+        if (bw) {
+          const uint64_t bit = k * (uint64_t)bw;
+          const uint8_t* b = p + (bit >> 3);
+          const int sh = (int)(bit & 7);
+          const uint64_t last = ((bit + (uint64_t)bw - 1) >> 3) - (bit >> 3);  // < 5
+          uint64_t w = 0;
+          for (uint64_t j = 0; j <= last; j++) w |= (uint64_t)b[j] << (8 * j);
+          v = (uint32_t)((w >> sh) & mask);
+        }
+        write(i + (uint32_t)k, v);
+      }
+      const uint64_t run_bytes = groups * (uint64_t)bw;
+      p = (uint64_t)(end - p) < run_bytes ? end : p + run_bytes;
+      i += (uint32_t)take;
+    } else {
+      const uint64_t run = h >> 1;
+      if (run == 0) return false;
+      if (end - p < vbytes) return false;
+      uint32_t v = 0;
+      for (int j = 0; j < vbytes; j++) v |= (uint32_t)p[j] << (8 * j);
+      p += vbytes;
+      const uint64_t take = min(run, (uint64_t)(count - i));
+      for (uint64_t k = lane; k < take; k += 32) write(i + (uint32_t)k, v);
+      i += (uint32_t)take;
+    }
+  }
+  return true;
+}
+
+struct RowArrays {
+  uint8_t* valid;     // per row: 1 valid
+  uint64_t* tmp_ptr;  // per non-null value of a page, at first_row + rank
+  uint32_t* tmp_len;
+  uint64_t* vptr;     // per row: value address (0 for null)
+  uint32_t* vlen;     // per row: value length (0 for null)
+  unsigned long long* nulls;
+};
+
+__global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
+                             const uint8_t* __restrict__ src, const uint8_t* __restrict__ dst,
+                             const uint64_t* __restrict__ dict_base,
+                             const uint32_t* __restrict__ dict_n,
+                             const uint64_t* __restrict__ dict_ptr,
+                             const uint32_t* __restrict__ dict_len, RowArrays ra,
+                             uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
+    const PageInfo pg = pages[p];
+    if (pg.kind == 0) continue;
+    const uint8_t* raw = page_bytes(pg, src, dst);
+    const uint8_t* end = raw + pg.raw_size;
+    const uint64_t fr = pg.first_row;
+    const uint32_t nv = pg.num_values;
+    uint8_t* valid = ra.valid + fr;
+    // definition levels
+    const uint8_t* vp = raw;
+    if (pg.max_def == 0) {
+      for (uint32_t i = lane; i < nv; i += 32) valid[i] = 1;
+    } else {
+      bool ok = true;
+      const uint8_t* lv = raw;
+      const uint8_t* lend = raw;
+      if (pg.kind == 1) {
+        if (pg.raw_size < 4 || ld_le32(raw) > pg.raw_size - 4) {
+          ok = false;
+        } else {
+          lv = raw + 4;
+          lend = lv + ld_le32(raw);
+          vp = lend;
+        }
+      } else {
+        lend = raw + pg.def_len;
+        vp = raw + pg.lvl_bytes;
+      }
+      if (ok)
+        ok = rle_hybrid_warp(lv, lend, 1, nv,
+                             [&](uint32_t i, uint32_t v) { valid[i] = (uint8_t)(v & 1); });
+      if (!ok) {
+        if (lane == 0) set_error(status, kErrLevels, p);
+        continue;
+      }
+    }
+    __syncwarp();
+    uint32_t m = 0;  // non-null values
+    for (uint32_t i0 = 0; i0 < nv; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      m += __popc(__ballot_sync(0xffffffffu, i < nv && valid[i]));
+    }
+    // values, by non-null rank
+    uint64_t* tptr = ra.tmp_ptr + fr;
+    uint32_t* tlen = ra.tmp_len + fr;
+    if (pg.encoding == kPlain) {
+      const uint64_t avail = (uint64_t)(end - vp);
+      bool fixed = false;
+      if (m > 0 && avail >= 4) {
+        const uint32_t L0 = ld_le32(vp);
+        const uint64_t stride = (uint64_t)L0 + 4;
+        if (stride * m == avail) {
+          bool same = true;
+          for (uint32_t k = lane; k < m; k += 32) same &= ld_le32(vp + k * stride) == L0;
+          fixed = __all_sync(0xffffffffu, same);
+          if (fixed)
+            for (uint32_t k = lane; k < m; k += 32) {
+              tptr[k] = reinterpret_cast<uint64_t>(vp + k * stride + 4);
+              tlen[k] = L0;
+            }
+        }
+      }
+      if (!fixed) {
+        bool good = true;
+        if (lane == 0) {
+          const uint8_t* q = vp;
+          for (uint32_t k = 0; k < m; k++) {
+            if (end - q < 4) {
+              good = false;
+              break;
+            }
+            const uint32_t l = ld_le32(q);
+            if ((uint64_t)(end - q - 4) < l) {
+              good = false;
+              break;
+            }
+            tptr[k] = reinterpret_cast<uint64_t>(q + 4);
+            tlen[k] = l;
+            q += 4 + l;
+          }
+        }
+        good = __shfl_sync(0xffffffffu, good, 0);
+        if (!good) {
+          if (lane == 0) set_error(status, kErrPlain, p);
+          continue;
+        }
+      }
+    } else {
+      // dictionary indices: a bit-width byte, then the hybrid runs
+      const uint32_t dn = dict_n[pg.dict];
+      const uint64_t db = dict_base[pg.dict];
+      bool good = m == 0 || (end - vp >= 1 && vp[0] <= 32);
+      if (good && m > 0)
+        good = rle_hybrid_warp(vp + 1, end, vp[0], m, [&](uint32_t k, uint32_t v) { tlen[k] = v; });
+      if (!good) {
+        if (lane == 0) set_error(status, kErrLevels, p);
+        continue;
+      }
+      __syncwarp();
+      bool inb = true;
+      for (uint32_t k = lane; k < m; k += 32) {
+        const uint32_t d = tlen[k];
+        if (d >= dn) {
+          inb = false;
+          continue;
+        }
+        tptr[k] = dict_ptr[db + d];
+        tlen[k] = dict_len[db + d];
+      }
+      if (!__all_sync(0xffffffffu, inb)) {
+        if (lane == 0) set_error(status, kErrDictIndex, p);
+        continue;
+      }
+    }
+    __syncwarp();
+    // rows: the rank of each valid row among the page's valid rows
+    uint32_t base = 0, nnull = 0;
+    for (uint32_t i0 = 0; i0 < nv; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const bool v = i < nv && valid[i];
+      const unsigned b = __ballot_sync(0xffffffffu, v);
+      if (i < nv) {
+        if (v) {
+          const uint32_t r = base + __popc(b & lt);
+          ra.vptr[fr + i] = tptr[r];
+          ra.vlen[fr + i] = tlen[r];
+        } else {
+          ra.vptr[fr + i] = 0;
+          ra.vlen[fr + i] = 0;
+        }
+      }
+      base += __popc(b);
+      nnull += __popc(__ballot_sync(0xffffffffu, i < nv && !v));
+    }
+    if (lane == 0 && nnull) atomicAdd(ra.nulls, (unsigned long long)nnull);
+  }
+}
+
+// warp per row: the value's bytes (4-byte words when source and destination
+// share their alignment)
+__global__ void k_copy_values(const uint64_t* __restrict__ vptr,
+                              const uint32_t* __restrict__ vlen,
+                              const uint64_t* __restrict__ pos, uint64_t n,
+                              uint8_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nwarps) {
+    const uint32_t l = vlen[r];
+    if (l == 0) continue;
+    const uint8_t* s = reinterpret_cast<const uint8_t*>(vptr[r]);
+    uint8_t* d = out + pos[r];
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(s), da = reinterpret_cast<uintptr_t>(d);
+    if (((sa ^ da) & 3) == 0) {
+      const uint32_t head = min(l, (uint32_t)((4 - (sa & 3)) & 3));
+      if ((uint32_t)lane < head) d[lane] = s[lane];
+      const uint32_t words = (l - head) / 4;
+      const uint32_t* sw = reinterpret_cast<const uint32_t*>(s + head);
+      uint32_t* dw = reinterpret_cast<uint32_t*>(d + head);
+      for (uint32_t w = lane; w < words; w += 32) dw[w] = sw[w];
+      const uint32_t t0 = head + words * 4;
+      if (t0 + lane < l) d[t0 + lane] = s[t0 + lane];
+    } else {
+      for (uint32_t b = lane; b < l; b += 32) d[b] = s[b];
+    }
+  }
+}
+
+__global__ void k_offsets64(const uint64_t* __restrict__ pos, uint64_t n,
+                            int64_t* __restrict__ out) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = (int64_t)pos[i];
+}
+
+__global__ void k_pack_valid(const uint8_t* __restrict__ valid, uint64_t n,
+                             uint32_t* __restrict__ bits) {
+  const uint64_t nw = (n + 31) / 32;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t v = 0;
+    for (int b = 0; b < 32; b++) {
+      const uint64_t i = w * 32 + b;
+      if (i < n && valid[i]) v |= 1u << b;
+    }
+    bits[w] = v;
+  }
+}
+
+const char* error_name(uint32_t code) {
+  switch (code) {
+    case kErrSnappy: return "malformed Snappy data";
+    case kErrLevels: return "malformed RLE / bit-packed run";
+    case kErrPlain: return "PLAIN byte array values run past the page";
+    case kErrDictIndex: return "dictionary index out of range";
+    case kErrDictPage: return "malformed dictionary page";
+    case kErrPageShort: return "page shorter than its level bytes";
+    default: return "unknown error";
+  }
+}
+
+}  // namespace
+}  // namespace pq
+}  // namespace spj
+
+using namespace spj;
+
+struct SpjParquet {
+  std::string path;
+  int fd = -1;
+  uint64_t file_len = 0;
+  pq::FileMeta meta;
+  std::string last_error;
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  PinnedBuf stage_h;
+  uint64_t stage_h_cap = 0;
+  DevBuf stage, pages, pagebuf, dict_base, dict_n, dict_ptr, dict_len, valid, tmp_ptr, tmp_len,
+      vptr, vlen, pos, scan_tmp, out_off, out_data, out_valid, status, nulls;
+  double ms = 0;
+  uint64_t file_bytes = 0, page_bytes = 0, value_bytes = 0;
+
+  // device buffers go before the stream they are freed on
+  void release_device() {
+    for (DevBuf* b : {&stage, &pages, &pagebuf, &dict_base, &dict_n, &dict_ptr, &dict_len,
+                      &valid, &tmp_ptr, &tmp_len, &vptr, &vlen, &pos, &scan_tmp, &out_off,
+                      &out_data, &out_valid, &status, &nulls})
+      b->release();
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+      stream = nullptr;
+    }
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    ev0 = ev1 = nullptr;
+  }
+  ~SpjParquet() {
+    if (device >= 0) {
+      cudaSetDevice(device);
+      release_device();
+    }
+    if (fd >= 0) ::close(fd);
+  }
+  void read_at(uint64_t off, uint64_t n, uint8_t* out) const {
+    while (n) {
+      const ssize_t r = ::pread(fd, out, n, (off_t)off);
+      if (r <= 0) throw Error("parquet: read failed at byte " + std::to_string(off));
+      out += r;
+      off += (uint64_t)r;
+      n -= (uint64_t)r;
+    }
+  }
+};
+
+namespace {
+
+thread_local std::string g_pq_error;  // SpjParquetOpen and writer failures
+
+int pq_fail(SpjParquet* p, const std::exception& e) {
+  if (p) p->last_error = e.what();
+  else g_pq_error = e.what();
+  return EINVAL;
+}
+
+int find_leaf(const pq::FileMeta& m, const std::string& name) {
+  for (size_t i = 0; i < m.leaves.size(); i++)
+    if (m.leaves[i].name == name) return (int)i;
+  return -1;
+}
+
+}  // namespace
+
+extern "C" int SpjParquetOpen(const char* path, SpjParquet** out) {
+  try {
+    SPJ_CHECK(path != nullptr && out != nullptr, "null path or output");
+    *out = nullptr;
+    auto p = std::make_unique<SpjParquet>();
+    p->path = path;
+    p->fd = ::open(path, O_RDONLY);
+    if (p->fd < 0) throw Error(std::string("parquet: cannot open ") + path);
+    struct stat st;
+    if (fstat(p->fd, &st) != 0) throw Error("parquet: cannot stat the file");
+    p->file_len = (uint64_t)st.st_size;
+    SPJ_CHECK(p->file_len >= 12, "parquet: file too short");
+    uint64_t want = std::min<uint64_t>(p->file_len, 1 << 16);
+    std::vector<uint8_t> tail;
+    for (int tries = 0;; tries++) {
+      tail.resize(want);
+      p->read_at(p->file_len - want, want, tail.data());
+      const uint64_t need = pq::parse_footer(tail.data(), want, p->file_len, p->meta);
+      if (need == 0) break;
+      SPJ_CHECK(tries == 0 && need <= p->file_len, "parquet: footer larger than announced");
+      want = need;
+    }
+    *out = p.release();
+    g_pq_error.clear();
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(nullptr, e);
+  }
+}
+
+extern "C" void SpjParquetRelease(SpjParquet* p) { delete p; }
+
+extern "C" const char* SpjParquetLastError(SpjParquet* p) {
+  return p ? p->last_error.c_str() : g_pq_error.c_str();
+}
+
+extern "C" int SpjParquetInfo(SpjParquet* p, int64_t* num_rows, int32_t* num_row_groups,
+                              int32_t* num_columns) {
+  try {
+    SPJ_CHECK(p && num_rows && num_row_groups && num_columns, "null argument");
+    *num_rows = p->meta.num_rows;
+    *num_row_groups = (int32_t)p->meta.row_groups.size();
+    *num_columns = (int32_t)p->meta.leaves.size();
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(p, e);
+  }
+}
+
+extern "C" int SpjParquetColumnName(SpjParquet* p, int32_t i, char* buf, uint64_t cap) {
+  try {
+    SPJ_CHECK(p && buf && cap > 0, "null argument");
+    std::string name;
+    if (i < 0) {
+      SPJ_CHECK(!p->meta.primary_column.empty(), "the file has no GeoParquet primary column");
+      name = p->meta.primary_column;
+    } else {
+      SPJ_CHECK((size_t)i < p->meta.leaves.size(), "column index out of range");
+      name = p->meta.leaves[i].name;
+    }
+    SPJ_CHECK(name.size() < cap, "name buffer too small");
+    memcpy(buf, name.c_str(), name.size() + 1);
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(p, e);
+  }
+}
+
+extern "C" int SpjParquetRowGroupRows(SpjParquet* p, int32_t rg, int64_t* rows) {
+  try {
+    SPJ_CHECK(p && rows, "null argument");
+    SPJ_CHECK(rg >= 0 && (size_t)rg < p->meta.row_groups.size(), "row group out of range");
+    *rows = p->meta.row_groups[rg].num_rows;
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(p, e);
+  }
+}
+
+extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_begin,
+                                 int32_t rg_end, int32_t device, SpjDeviceWkb* out) {
+  using namespace spj::pq;
+  try {
+    SPJ_CHECK(p && out, "null argument");
+    const FileMeta& m = p->meta;
+    const std::string name = column ? column : m.primary_column;
+    SPJ_CHECK(!name.empty(), "no column given and the file has no GeoParquet primary column");
+    for (auto& ge : m.geo_encodings)
+      if (ge.first == name && ge.second != "WKB")
+        throw Error("column " + name + " has GeoParquet encoding " + ge.second +
+                    " (only WKB columns are read)");
+    const int ci = find_leaf(m, name);
+    SPJ_CHECK(ci >= 0, "no column named " + name);
+    const Leaf& leaf = m.leaves[ci];
+    SPJ_CHECK(leaf.top_level && leaf.max_rep == 0, "column " + name + " is nested");
+    SPJ_CHECK(leaf.type == kByteArray, "column " + name + " is not BYTE_ARRAY");
+    const int nrg = (int)m.row_groups.size();
+    if (rg_end < 0 || rg_end > nrg) rg_end = nrg;
+    SPJ_CHECK(rg_begin >= 0 && rg_begin <= rg_end, "bad row group range");
+
+    // device and stream
+    if (p->device != device && p->device >= 0) {
+      SPJ_CUDA(cudaSetDevice(p->device));
+      p->release_device();
+    }
+    p->device = device;
+    SPJ_CUDA(cudaSetDevice(device));
+    if (!p->stream) {
+      SPJ_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+      SPJ_CUDA(cudaEventCreate(&p->ev0));
+      SPJ_CUDA(cudaEventCreate(&p->ev1));
+    }
+    cudaStream_t s = p->stream;
+
+    // the column chunks' byte ranges, read into the page-locked buffer
+    struct Range {
+      uint64_t off, len, at;
+      int codec;
+    };
+    std::vector<Range> ranges;
+    uint64_t total = 0, rows_expected = 0;
+    for (int g = rg_begin; g < rg_end; g++) {
+      const ColumnChunk& c = m.row_groups[g].columns[ci];
+      SPJ_CHECK(c.type == kByteArray, "column chunk type is not BYTE_ARRAY");
+      int64_t start = c.data_page_offset;
+      if (c.dictionary_page_offset > 0 && c.dictionary_page_offset < start)
+        start = c.dictionary_page_offset;
+      SPJ_CHECK(start >= 4 && c.total_compressed >= 0 &&
+                    (uint64_t)start + (uint64_t)c.total_compressed <= p->file_len,
+                "column chunk outside the file");
+      ranges.push_back({(uint64_t)start, (uint64_t)c.total_compressed, total, c.codec});
+      total += (uint64_t)c.total_compressed;
+      rows_expected += (uint64_t)m.row_groups[g].num_rows;
+    }
+    SPJ_CHECK(rows_expected < (1ull << 32), "more than 2^32 - 1 rows in one read");
+    if (total + 16 > p->stage_h_cap) {
+      p->stage_h.reserve(total + 16);
+      p->stage_h_cap = total + 16;
+    }
+    uint8_t* hb = p->stage_h.as<uint8_t>();
+    for (auto& r : ranges) p->read_at(r.off, r.len, hb + r.at);
+    p->file_bytes = total;
+
+    // page table
+    std::vector<PageInfo> pages;
+    uint64_t row = 0;
+    int ndict = 0;
+    for (auto& r : ranges)
+      if (walk_pages(hb, r.at, r.at + r.len, r.codec, leaf.max_def, ndict, &row, pages)) ndict++;
+    SPJ_CHECK(row == rows_expected, "the pages hold " + std::to_string(row) +
+                                        " values, the row groups " +
+                                        std::to_string(rows_expected) + " rows");
+    const uint64_t n = row;
+    uint64_t dst = 0, dict_total = 0, pbytes = 0;
+    std::vector<uint64_t> dict_base(ndict + 1, 0);
+    std::vector<uint32_t> dict_n(ndict + 1, 0);
+    for (auto& pg : pages) {
+      pbytes += pg.raw_size;
+      if (!pg.in_src) {
+        pg.dst = dst;
+        dst += (pg.raw_size + 15) & ~15ull;
+      }
+      if (pg.kind == 0) {
+        dict_base[pg.dict] = dict_total;
+        dict_n[pg.dict] = pg.num_values;
+        dict_total += pg.num_values;
+      }
+    }
+    p->page_bytes = pbytes;
+    const uint32_t np = (uint32_t)pages.size();
+
+    SPJ_CUDA(cudaEventRecord(p->ev0, s));
+    p->stage.reserve(total + 16, s);
+    SPJ_CUDA(cudaMemcpyAsync(p->stage.get(), hb, total, cudaMemcpyHostToDevice, s));
+    // the small tables come from pageable vectors: the copies complete
+    // before the stream synchronisation below, while the vectors live
+    p->pages.reserve(sizeof(PageInfo) * (np + 1), s);
+    SPJ_CUDA(cudaMemcpyAsync(p->pages.get(), pages.data(), sizeof(PageInfo) * np,
+                             cudaMemcpyHostToDevice, s));
+    p->dict_base.reserve(8 * (ndict + 1), s);
+    p->dict_n.reserve(4 * (ndict + 1), s);
+    SPJ_CUDA(cudaMemcpyAsync(p->dict_base.get(), dict_base.data(), 8 * (ndict + 1),
+                             cudaMemcpyHostToDevice, s));
+    SPJ_CUDA(cudaMemcpyAsync(p->dict_n.get(), dict_n.data(), 4 * (ndict + 1),
+                             cudaMemcpyHostToDevice, s));
+    p->pagebuf.reserve(dst + 16, s);
+    p->dict_ptr.reserve(8 * (dict_total + 1), s);
+    p->dict_len.reserve(4 * (dict_total + 1), s);
+    p->valid.reserve(n + 16, s);
+    p->tmp_ptr.reserve(8 * (n + 1), s);
+    p->tmp_len.reserve(4 * (n + 1), s);
+    p->vptr.reserve(8 * (n + 1), s);
+    p->vlen.reserve(4 * (n + 1), s);
+    p->pos.reserve(8 * (n + 1), s);
+    p->out_off.reserve(8 * (n + 1), s);
+    p->status.reserve(8, s);
+    p->nulls.reserve(8, s);
+    SPJ_CUDA(cudaMemsetAsync(p->status.get(), 0, 8, s));
+    SPJ_CUDA(cudaMemsetAsync(p->nulls.get(), 0, 8, s));
+    const PageInfo* dpages = p->pages.as<PageInfo>();
+    const uint8_t* dsrc = p->stage.as<uint8_t>();
+    uint8_t* dpb = p->pagebuf.as<uint8_t>();
+    uint32_t* st = p->status.as<uint32_t>();
+    if (np) {
+      const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
+      k_unsnap<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, st);
+      if (ndict)
+        k_dict_pages<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
+                                       p->dict_ptr.as<uint64_t>(), p->dict_len.as<uint32_t>(),
+                                       st);
+      RowArrays ra{p->valid.as<uint8_t>(),    p->tmp_ptr.as<uint64_t>(),
+                   p->tmp_len.as<uint32_t>(), p->vptr.as<uint64_t>(),
+                   p->vlen.as<uint32_t>(),    p->nulls.as<unsigned long long>()};
+      k_data_pages<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
+                                     p->dict_n.as<uint32_t>(), p->dict_ptr.as<uint64_t>(),
+                                     p->dict_len.as<uint32_t>(), ra, st);
+      SPJ_CUDA(cudaGetLastError());
+    }
+    uint32_t hst[2] = {0, 0};
+    SPJ_CUDA(cudaMemcpyAsync(hst, st, 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long hnulls = 0;
+    SPJ_CUDA(cudaMemcpyAsync(&hnulls, p->nulls.get(), 8, cudaMemcpyDeviceToHost, s));
+    scan_u32_u64(p->vlen.as<uint32_t>(), p->pos.as<uint64_t>(), (int64_t)n, p->scan_tmp, s);
+    uint64_t vbytes = 0;
+    SPJ_CUDA(cudaMemcpyAsync(&vbytes, p->pos.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    if (hst[0]) {
+      const uint32_t bad = hst[1] < np ? hst[1] : 0;
+      throw Error(std::string("parquet: ") + pq::error_name(hst[0]) + " in page " +
+                  std::to_string(bad) + " of the read (" + std::to_string(np) + " pages)");
+    }
+    p->value_bytes = vbytes;
+    p->out_data.reserve(vbytes + 16, s);
+    k_offsets64<<<grid_for((int64_t)n + 1, 256), 256, 0, s>>>(p->pos.as<uint64_t>(), n,
+                                                              p->out_off.as<int64_t>());
+    if (n)
+      k_copy_values<<<grid_for((int64_t)n * 32, 256, kNumSMs * 32), 256, 0, s>>>(
+          p->vptr.as<uint64_t>(), p->vlen.as<uint32_t>(), p->pos.as<uint64_t>(), n,
+          p->out_data.as<uint8_t>());
+    const uint8_t* validity = nullptr;
+    if (hnulls) {
+      p->out_valid.reserve(((n + 31) / 32) * 4 + 16, s);
+      k_pack_valid<<<grid_for((int64_t)(n + 31) / 32, 256), 256, 0, s>>>(
+          p->valid.as<uint8_t>(), n, p->out_valid.as<uint32_t>());
+      validity = p->out_valid.as<uint8_t>();
+    }
+    SPJ_CUDA(cudaGetLastError());
+    SPJ_CUDA(cudaEventRecord(p->ev1, s));
+    SPJ_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    SPJ_CUDA(cudaEventElapsedTime(&ms, p->ev0, p->ev1));
+    p->ms = ms;
+    out->length = (int64_t)n;
+    out->offsets = p->out_off.get();
+    out->offsets_are_64bit = 1;
+    out->data = p->out_data.as<uint8_t>();
+    out->data_length = vbytes;
+    out->validity = validity;
+    out->validity_offset = 0;
+    p->last_error.clear();
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(p, e);
+  }
+}
+
+extern "C" int SpjParquetGetStats(SpjParquet* p, double* ms_device, uint64_t* file_bytes,
+                                  uint64_t* page_bytes, uint64_t* value_bytes) {
+  try {
+    SPJ_CHECK(p && ms_device && file_bytes && page_bytes && value_bytes, "null argument");
+    *ms_device = p->ms;
+    *file_bytes = p->file_bytes;
+    *page_bytes = p->page_bytes;
+    *value_bytes = p->value_bytes;
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(p, e);
+  }
+}
+
+extern "C" int SpjParquetWriteWkb(const char* path, const char* column, int64_t length,
+                                  const void* offsets, int32_t offsets_are_64bit,
+                                  const uint8_t* data, const uint8_t* validity,
+                                  int64_t validity_offset,
+                                  const SpjParquetWriteOptions* options) {
+  try {
+    pq::WriteOptions o;
+    if (options) {
+      o.compression = options->compression;
+      o.page_version = options->page_version;
+      if (options->row_group_rows > 0) o.row_group_rows = options->row_group_rows;
+      if (options->page_bytes > 0) o.page_bytes = options->page_bytes;
+    }
+    pq::write_wkb(path, column, length, offsets, offsets_are_64bit != 0, data, validity,
+                  validity_offset, o);
+    g_pq_error.clear();
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(nullptr, e);
+  }
+}

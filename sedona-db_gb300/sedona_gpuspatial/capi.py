@@ -148,6 +148,11 @@ class SpjKnnConfig(C.Structure):
 JOIN_CB = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint64,
                       C.c_void_p)
 
+class SpjParquetWriteOptions(C.Structure):
+    _fields_ = [("compression", C.c_int32), ("page_version", C.c_int32),
+                ("row_group_rows", C.c_int64), ("page_bytes", C.c_int64)]
+
+
 # exported symbols, declared in include/*.h
 EXPORTS = [
     "GpuSpatialRuntimeCreate", "GpuSpatialIndexFloat2DCreate", "GpuSpatialRefinerCreate",
@@ -161,6 +166,9 @@ EXPORTS = [
     "SpjIndexProbeNoAlloc", "SpjAllocationCount",
     "SpjMaterializeLastError", "SpjGatherFixed", "SpjGatherValidity", "SpjGatherBinary",
     "SpjVisitedMark", "SpjVisitedCollect",
+    "SpjParquetOpen", "SpjParquetRelease", "SpjParquetLastError", "SpjParquetInfo",
+    "SpjParquetColumnName", "SpjParquetRowGroupRows", "SpjParquetReadWkb", "SpjParquetGetStats",
+    "SpjParquetWriteWkb",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
     "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
     "SpjStreamCudaStream",
@@ -263,6 +271,22 @@ def lib() -> C.CDLL:
                                          C.c_void_p]
             L.SpjVisitedCollect.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p,
                                             C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]
+            L.SpjParquetOpen.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+            L.SpjParquetRelease.argtypes = [C.c_void_p]
+            L.SpjParquetRelease.restype = None
+            L.SpjParquetLastError.argtypes = [C.c_void_p]
+            L.SpjParquetLastError.restype = C.c_char_p
+            L.SpjParquetInfo.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+            L.SpjParquetColumnName.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_uint64]
+            L.SpjParquetRowGroupRows.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
+            L.SpjParquetReadWkb.argtypes = [C.c_void_p, C.c_char_p, C.c_int32, C.c_int32,
+                                            C.c_int32, C.POINTER(SpjDeviceWkb)]
+            L.SpjParquetGetStats.argtypes = [C.c_void_p, C.POINTER(C.c_double)] + \
+                [C.POINTER(C.c_uint64)] * 3
+            L.SpjParquetWriteWkb.argtypes = [C.c_char_p, C.c_char_p, C.c_int64, C.c_void_p,
+                                             C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                                             C.POINTER(SpjParquetWriteOptions)]
             L.SpjAllocationCount.argtypes = []
             L.SpjAllocationCount.restype = C.c_uint64
             L.SpjHostRegister.argtypes = [C.c_void_p, C.c_uint64]
