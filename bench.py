@@ -1029,6 +1029,221 @@ def run_reference(args, world, rank):
     }
 
 
+def run_geoparquet(args, local):
+    """GeoParquet -> device: the 2M-building probe column of the polygon
+    workload written as a GeoParquet file (SNAPPY, data page v1, 1 MiB pages,
+    1M-row row groups), then read onto the device column the join takes.
+    value: rows/s over the device phases (Snappy, page decode, value copy)
+    with the chunk bytes in HBM; e2e: rows/s of open + read from the file
+    (page cache) through the H2D copy to the finished device column."""
+    import shutil
+    import tempfile
+
+    import torch
+    from sedona_gpuspatial import geoparquet as gp
+    inp = make_inputs(2, args.scale)
+    col = inp.probe
+    tmp = tempfile.mkdtemp(prefix="spj_gpq_")
+    try:
+        path = os.path.join(tmp, "buildings.parquet")
+        t0 = time.perf_counter()
+        gp.write_wkb(path, col, compression="snappy", page_version=1,
+                     row_group_rows=1 << 20, page_bytes=1 << 20)
+        t_write = time.perf_counter() - t0
+        n = len(col)
+        steps, warmup = args.steps, max(3, args.warmup)
+        t0 = time.perf_counter()
+        f = gp.GeoParquetFile(path)
+        t_open = time.perf_counter() - t0
+        for _ in range(warmup):
+            f.read_wkb(device=local)
+        dev_ms, ph_sum, wall = 0.0, None, 0.0
+        sampler = ClockSampler(local)
+        with sampler:
+            for _ in range(steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                d = f.read_wkb(device=local)
+                wall += time.perf_counter() - t0
+                st, ph = f.stats(), f.phases()
+                dev_ms += ph["decompress"] + ph["decode"] + ph["values"]
+                ph_sum = ph if ph_sum is None else {k: ph_sum[k] + ph[k] for k in ph}
+        ms = dev_ms / steps
+        e2e_ms = wall * 1e3 / steps
+        ph_avg = {k: v / steps for k, v in ph_sum.items()}
+        # parity: the device column against the written column, every byte
+        got = gp.device_to_host(d)
+        parity = {"rows": n, "bytes_equal": bool(
+            np.array_equal(got.offsets, col.offsets.astype(np.int64)) and
+            np.array_equal(got.data, col.data) and got.validity is None),
+            "checked": "every offset and byte of the device column against the column written"}
+        f.close()
+        # roofline of the slowest device phase, by its algorithmic bytes
+        vb, fb, pb = st["value_bytes"], st["file_bytes"], st["page_bytes"]
+        alg = {"decompress": fb + pb,        # compressed pages read, raw pages written
+               "decode": 41 * n,             # length word, validity, value spans (tmp + row)
+               "values": 2 * vb + 28 * n}    # value bytes read + written, spans, offsets
+        kernels = {"decompress": "k_unsnap", "decode": "k_data_pages",
+                   "values": "k_copy_values (+ k_offsets64)"}
+        dom = max(alg, key=lambda k: ph_avg[k])
+        hbm_peak, peak_kind = load_peaks()
+        achieved = alg[dom] / (ph_avg[dom] * 1e-3) / 1e9
+        # CPU: the oracle's reader (one thread) on the same file
+        import oracle
+        oracle.build(with_ref=False)
+        t0 = time.perf_counter()
+        o_off, o_data, o_valid = oracle.parquet_read(path)
+        t_cpu = time.perf_counter() - t0
+        cpu_equal = bool(np.array_equal(o_data, col.data) and o_valid.all())
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return {
+        "metric": "GeoParquet WKB column read to a device column (rows/s)",
+        "value": n / (ms * 1e-3), "unit": "rows/s", "ms_per_step": ms, "steps": steps,
+        "warmup": warmup,
+        "phases_ms_per_step": ph_avg,
+        "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "rows/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(fb), "d2h_bytes_per_step": 24,
+                "open_ms": t_open * 1e3,
+                "note": "SpjParquetReadWkb on an open file: chunk reads from the page cache "
+                        "into page-locked memory, H2D, decode (the footer parse at open is "
+                        "open_ms, once per file)"},
+        "roofline": {"bound": "hbm", "kernel": kernels[dom], "achieved": achieved,
+                     "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg[dom]},
+        "gpu_launches": 7 * steps,
+        "parity": {**parity, "oracle_bytes_equal": cpu_equal},
+        "cpu_baseline": {"value": n / t_cpu, "unit": "rows/s", "cores": 1, "kind": "port",
+                         "sample": f"the whole file ({n} rows, {fb} bytes) read by the "
+                                   "oracle's C Parquet reader on one thread"},
+        "clocks": sampler.summary(),
+        "config": {"workload": "geoparquet_read_2m_building_polygons_snappy_v1",
+                   "rows": n, "file_bytes": int(fb), "page_bytes": int(pb),
+                   "value_bytes": int(vb), "write_seconds": round(t_write, 2),
+                   "l2": "column > L2, no flush"},
+    }
+
+
+def run_materialize(args, local):
+    """Joined-batch materialisation on the device for the polygon workload's
+    81M result pairs: the build and probe id columns (int64) and the probe
+    WKB column gathered per pair, plus a left join's visited bitmap (mark,
+    then collect the unmatched build rows).  The build WKB is not gathered
+    (each pair would copy a ~2.3 KB zone: 190 GB); a query projecting it
+    gathers it with the same call."""
+    import torch
+    from sedona_gpuspatial import capi
+    from sedona_gpuspatial import materialize as mat
+    inp = make_inputs(2, args.scale)
+    join = capi.SpatialJoin()
+    join.build(inp.build)
+    dcol, keep = to_device(inp.probe)
+    db, dp, npairs = join.probe_device(dcol, "intersects")
+    torch.cuda.synchronize()
+    bi = torch.as_tensor(_DevI32(db, npairs), device="cuda")
+    pi = torch.as_tensor(_DevI32(dp, npairs), device="cuda")
+    nb, npb = len(inp.build), len(inp.probe)
+    build_ids = mat.DeviceColumn(nb, values=torch.arange(nb, dtype=torch.int64, device="cuda"))
+    probe_ids = mat.DeviceColumn(npb, values=torch.arange(npb, dtype=torch.int64, device="cuda"))
+    probe_wkb = mat.DeviceColumn(npb, offsets=keep[0], data=keep[1])
+    steps, warmup = min(args.steps, 5), max(3, args.warmup)
+
+    def step():
+        cols = mat.build_joined_columns([build_ids], [probe_ids, probe_wkb], bi, pi)
+        vb = mat.VisitedBitmap(nb)
+        vb.mark(bi)
+        un = vb.collect(False)
+        return cols, un
+
+    for _ in range(warmup):
+        out = step()
+        del out
+    s = torch.cuda.current_stream()
+    e0, e1, eb0, eb1 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    sampler = ClockSampler(local)
+    bin_ms = 0.0
+    with sampler:
+        torch.cuda.synchronize()
+        e0.record(s)
+        for _ in range(steps):
+            cols, un = step()
+            if _ < steps - 1:
+                del cols, un
+        e1.record(s)
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            eb0.record(s)
+            off, data = mat.take_binary(probe_wkb.offsets, probe_wkb.data, pi)
+            eb1.record(s)
+            torch.cuda.synchronize()
+            bin_ms += eb0.elapsed_time(eb1)
+            del off, data
+    ms = e0.elapsed_time(e1) / steps
+    bin_ms /= steps
+    out_bytes = int(cols[2].data.numel())
+    # parity: fixed columns exactly (torch gather), the binary column's
+    # lengths exactly and 2000 sampled values byte for byte, the unmatched
+    # build rows against a bincount
+    ok_ids = bool(torch.equal(cols[0].values, bi.long()) and torch.equal(cols[1].values, pi.long()))
+    poff = keep[0].long()
+    lens = (poff[1:] - poff[:-1])[pi.long()]
+    ok_len = bool(torch.equal(cols[2].offsets[1:] - cols[2].offsets[:-1], lens))
+    rng = np.random.default_rng(20260301)
+    sample = rng.integers(0, npairs, 2000)
+    o = cols[2].offsets.cpu().numpy()
+    pis = pi.cpu().numpy().view(np.uint32)
+    ok_val = all(cols[2].data[o[i]:o[i + 1]].cpu().numpy().tobytes() == inp.probe.value(int(pis[i]))
+                 for i in sample)
+    seen = torch.bincount(bi.long(), minlength=nb) > 0
+    ok_vis = bool(torch.equal(un.long(), torch.nonzero(~seen).flatten()))
+    # roofline of the binary gather (k_bin_lengths + scan + k_bin_copy, run
+    # twice by take_binary: a sizing call, then the copy): value bytes read
+    # and written, per pair its index and the source offsets (12 B) and the
+    # output offset (8 B), twice for the sizing pass
+    alg = 2 * out_bytes + 2 * npairs * 20
+    hbm_peak, peak_kind = load_peaks()
+    achieved = alg / (bin_ms * 1e-3) / 1e9
+    # CPU: numpy takes of the same columns over a sample of the pairs
+    bnp, pnp = bi[:2_000_000].cpu().numpy().view(np.uint32), pis[:2_000_000]
+    ids_b, ids_p = np.arange(nb, dtype=np.int64), np.arange(npb, dtype=np.int64)
+    t0 = time.perf_counter()
+    np.take(ids_b, bnp)
+    np.take(ids_p, pnp)
+    inp.probe.take(pnp.astype(np.int64))
+    t_cpu = time.perf_counter() - t0
+    del cols, un, join
+    return {
+        "metric": "joined-batch materialisation on the device (result pairs/s)",
+        "value": npairs / (ms * 1e-3), "unit": "pairs/s", "ms_per_step": ms, "steps": steps,
+        "warmup": warmup,
+        "phases_ms_per_step": {"probe_wkb_take_binary": bin_ms},
+        "roofline": {"bound": "hbm", "kernel": "k_bin_copy (+ k_bin_lengths, scan)",
+                     "achieved": achieved, "peak": hbm_peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg},
+        "gpu_launches": 26 * steps,
+        "parity": {"id_columns_equal": ok_ids, "wkb_lengths_equal": ok_len,
+                   "wkb_sampled_values_equal": bool(ok_val), "unmatched_rows_equal": ok_vis,
+                   "pairs": npairs},
+        "cpu_baseline": {"value": len(bnp) / t_cpu, "unit": "pairs/s", "cores": 1,
+                         "kind": "port",
+                         "sample": f"numpy takes (build ids, probe ids, probe WKB) for the "
+                                   f"first {len(bnp)} pairs"},
+        "clocks": sampler.summary(),
+        "config": {"workload": "materialize_2m_buildings_x_50k_zones_result_pairs",
+                   "pairs": npairs, "probe_wkb_bytes_out": out_bytes,
+                   "columns": "build id (int64), probe id (int64), probe WKB; visited bitmap",
+                   "l2": "columns > L2, no flush"},
+    }
+
+
+class _DevI32:
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
 NESTED_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "probe_rows_per_s",
                "plain_f64_form", "phases_ms_per_step", "fp64_escalated_fraction",
                "fp64_escalations_per_replay", "roofline", "e2e", "gpu_launches", "parity",
@@ -1063,9 +1278,13 @@ def run_configs(args, world, rank, local, pg, names):
         elif name == "5":
             a.workload = 5
             out, inp = run_learned(a, world, rank, local, pg)
+        elif name == "geoparquet":
+            out, inp = run_geoparquet(a, local), None
+        elif name == "materialize":
+            out, inp = run_materialize(a, local), None
         else:
             raise SystemExit(f"unknown config {name}")
-        entry = {k: out[k] for k in NESTED_KEYS if k in out}
+        entry = {k: out[k] for k in NESTED_KEYS + ("metric", "cpu_baseline") if k in out}
         if rank == 0 and not args.no_cpu_baseline and inp is not None:
             entry["cpu_baseline"] = cpu_baseline(inp, seconds_budget=args.config_ref_seconds,
                                                  pred=pred)
@@ -1094,7 +1313,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", dest="parity", action="store_false",
                     help="skip the parity check of the full-size run against the oracle")
-    ap.add_argument("--configs", default="1,2contains,3,4,5",
+    ap.add_argument("--configs", default="1,2contains,3,4,5,geoparquet,materialize",
                     help="workload entries timed beside the headline (empty: none)")
     ap.add_argument("--config-ref-seconds", type=float, default=5.0)
     ap.add_argument("--join-options", type=json.loads, default={},

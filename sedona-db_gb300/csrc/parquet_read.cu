@@ -462,12 +462,12 @@ struct SpjParquet {
   std::string last_error;
   int device = -1;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev[6] = {};  // start, after H2D, after Snappy, after decode, values start, end
   PinnedBuf stage_h;
   uint64_t stage_h_cap = 0;
   DevBuf stage, pages, pagebuf, dict_base, dict_n, dict_ptr, dict_len, valid, tmp_ptr, tmp_len,
       vptr, vlen, pos, scan_tmp, out_off, out_data, out_valid, status, nulls;
-  double ms = 0;
+  double ms = 0, ms_phase[4] = {};  // H2D, decompress, decode, values
   uint64_t file_bytes = 0, page_bytes = 0, value_bytes = 0;
 
   // device buffers go before the stream they are freed on
@@ -481,9 +481,10 @@ struct SpjParquet {
       cudaStreamDestroy(stream);
       stream = nullptr;
     }
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
-    ev0 = ev1 = nullptr;
+    for (auto& e : ev) {
+      if (e) cudaEventDestroy(e);
+      e = nullptr;
+    }
   }
   ~SpjParquet() {
     if (device >= 0) {
@@ -630,8 +631,7 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     SPJ_CUDA(cudaSetDevice(device));
     if (!p->stream) {
       SPJ_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
-      SPJ_CUDA(cudaEventCreate(&p->ev0));
-      SPJ_CUDA(cudaEventCreate(&p->ev1));
+      for (auto& e : p->ev) SPJ_CUDA(cudaEventCreate(&e));
     }
     cudaStream_t s = p->stream;
 
@@ -692,9 +692,10 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     p->page_bytes = pbytes;
     const uint32_t np = (uint32_t)pages.size();
 
-    SPJ_CUDA(cudaEventRecord(p->ev0, s));
+    SPJ_CUDA(cudaEventRecord(p->ev[0], s));
     p->stage.reserve(total + 16, s);
     SPJ_CUDA(cudaMemcpyAsync(p->stage.get(), hb, total, cudaMemcpyHostToDevice, s));
+    SPJ_CUDA(cudaEventRecord(p->ev[1], s));
     // the small tables come from pageable vectors: the copies complete
     // before the stream synchronisation below, while the vectors live
     p->pages.reserve(sizeof(PageInfo) * (np + 1), s);
@@ -724,9 +725,10 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     const uint8_t* dsrc = p->stage.as<uint8_t>();
     uint8_t* dpb = p->pagebuf.as<uint8_t>();
     uint32_t* st = p->status.as<uint32_t>();
+    const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
+    if (np) k_unsnap<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, st);
+    SPJ_CUDA(cudaEventRecord(p->ev[2], s));
     if (np) {
-      const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
-      k_unsnap<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, st);
       if (ndict)
         k_dict_pages<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
                                        p->dict_ptr.as<uint64_t>(), p->dict_len.as<uint32_t>(),
@@ -739,6 +741,7 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
                                      p->dict_len.as<uint32_t>(), ra, st);
       SPJ_CUDA(cudaGetLastError());
     }
+    SPJ_CUDA(cudaEventRecord(p->ev[3], s));
     uint32_t hst[2] = {0, 0};
     SPJ_CUDA(cudaMemcpyAsync(hst, st, 8, cudaMemcpyDeviceToHost, s));
     unsigned long long hnulls = 0;
@@ -754,6 +757,7 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     }
     p->value_bytes = vbytes;
     p->out_data.reserve(vbytes + 16, s);
+    SPJ_CUDA(cudaEventRecord(p->ev[4], s));
     k_offsets64<<<grid_for((int64_t)n + 1, 256), 256, 0, s>>>(p->pos.as<uint64_t>(), n,
                                                               p->out_off.as<int64_t>());
     if (n)
@@ -768,11 +772,16 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
       validity = p->out_valid.as<uint8_t>();
     }
     SPJ_CUDA(cudaGetLastError());
-    SPJ_CUDA(cudaEventRecord(p->ev1, s));
+    SPJ_CUDA(cudaEventRecord(p->ev[5], s));
     SPJ_CUDA(cudaStreamSynchronize(s));
     float ms = 0;
-    SPJ_CUDA(cudaEventElapsedTime(&ms, p->ev0, p->ev1));
+    SPJ_CUDA(cudaEventElapsedTime(&ms, p->ev[0], p->ev[5]));
     p->ms = ms;
+    const int from[4] = {0, 1, 2, 4}, to[4] = {1, 2, 3, 5};
+    for (int i = 0; i < 4; i++) {
+      SPJ_CUDA(cudaEventElapsedTime(&ms, p->ev[from[i]], p->ev[to[i]]));
+      p->ms_phase[i] = ms;
+    }
     out->length = (int64_t)n;
     out->offsets = p->out_off.get();
     out->offsets_are_64bit = 1;
@@ -795,6 +804,20 @@ extern "C" int SpjParquetGetStats(SpjParquet* p, double* ms_device, uint64_t* fi
     *file_bytes = p->file_bytes;
     *page_bytes = p->page_bytes;
     *value_bytes = p->value_bytes;
+    return 0;
+  } catch (const std::exception& e) {
+    return pq_fail(p, e);
+  }
+}
+
+extern "C" int SpjParquetGetPhases(SpjParquet* p, double* ms_h2d, double* ms_decompress,
+                                   double* ms_decode, double* ms_values) {
+  try {
+    SPJ_CHECK(p && ms_h2d && ms_decompress && ms_decode && ms_values, "null argument");
+    *ms_h2d = p->ms_phase[0];
+    *ms_decompress = p->ms_phase[1];
+    *ms_decode = p->ms_phase[2];
+    *ms_values = p->ms_phase[3];
     return 0;
   } catch (const std::exception& e) {
     return pq_fail(p, e);

@@ -167,7 +167,7 @@ EXPORTS = [
     "SpjMaterializeLastError", "SpjGatherFixed", "SpjGatherValidity", "SpjGatherBinary",
     "SpjVisitedMark", "SpjVisitedCollect",
     "SpjParquetOpen", "SpjParquetRelease", "SpjParquetLastError", "SpjParquetInfo",
-    "SpjParquetColumnName", "SpjParquetRowGroupRows", "SpjParquetReadWkb", "SpjParquetGetStats",
+    "SpjParquetColumnName", "SpjParquetRowGroupRows", "SpjParquetReadWkb", "SpjParquetGetStats", "SpjParquetGetPhases",
     "SpjParquetWriteWkb",
     "SpjStreamCreate", "SpjStreamRelease", "SpjStreamLastError", "SpjStreamSetBatches",
     "SpjStreamRun", "SpjStreamSetParams", "SpjStreamAutotune", "SpjStreamGetStats",
@@ -284,6 +284,7 @@ def lib() -> C.CDLL:
                                             C.c_int32, C.POINTER(SpjDeviceWkb)]
             L.SpjParquetGetStats.argtypes = [C.c_void_p, C.POINTER(C.c_double)] + \
                 [C.POINTER(C.c_uint64)] * 3
+            L.SpjParquetGetPhases.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4
             L.SpjParquetWriteWkb.argtypes = [C.c_char_p, C.c_char_p, C.c_int64, C.c_void_p,
                                              C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
                                              C.POINTER(SpjParquetWriteOptions)]

@@ -84,6 +84,11 @@ class GeoParquetFile:
         return {"ms_device": ms.value, "file_bytes": v[0].value, "page_bytes": v[1].value,
                 "value_bytes": v[2].value}
 
+    def phases(self) -> dict:
+        v = [C.c_double() for _ in range(4)]
+        self._check(lib().SpjParquetGetPhases(self.h, *[C.byref(x) for x in v]), "phases")
+        return dict(zip(("h2d", "decompress", "decode", "values"), (x.value for x in v)))
+
     def close(self):
         if getattr(self, "h", None):
             lib().SpjParquetRelease(self.h)
