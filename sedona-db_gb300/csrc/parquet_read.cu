@@ -4,8 +4,11 @@
 // One read (all on the handle's stream, one H2D copy of the chunk bytes):
 //   host           footer (parsed at open); chunk bytes -> page-locked
 //                  buffer; page headers -> page table
-//   k_unsnap       warp per compressed page: Snappy elements decoded in
-//                  order, each element's bytes moved by the 32 lanes (a
+//   k_snappy_scan  warp per compressed page: element headers walked
+//                  through a shared-memory window; the input position of
+//                  every 64 KiB output block
+//   k_snappy_frags warp per 64 KiB output block: the block built in shared
+//                  memory, each element's bytes moved by the 32 lanes (a
 //                  back-reference shorter than its length repeats its
 //                  pattern, so every lane's byte is known without waiting)
 //   k_dict_pages   warp per dictionary page: PLAIN byte arrays -> entries
@@ -122,24 +125,279 @@ __device__ bool unsnap_warp(const uint8_t* in, uint32_t in_n, uint8_t* out, uint
   return op == out_n;
 }
 
-__global__ void k_unsnap(const PageInfo* __restrict__ pages, uint32_t np,
-                         const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
-                         uint32_t* status) {
+// ---------------------------------------------------------------------------
+// A warp's window on a global byte range, staged in shared memory with
+// 16-byte loads.  Every lane keeps the same walk position, so the calls
+// below are warp-uniform.  The staged bytes may run past `lim` up to the next
+// 16-byte boundary: every device buffer these kernels read keeps 16 bytes of
+// slack after its last page, so those loads stay inside the allocation, and
+// bytes past `lim` are never used.
+struct WarpWindow {
+  const uint8_t* lim;
+  uint8_t* buf;   // shared memory, 16-byte aligned
+  uint32_t cap;   // bytes, multiple of 16
+  const uint8_t* w0;
+  const uint8_t* w1;
+};
+
+__device__ __forceinline__ void win_init(WarpWindow& w, uint8_t* buf, uint32_t cap,
+                                         const uint8_t* lim) {
+  w.buf = buf;
+  w.cap = cap;
+  w.lim = lim;
+  w.w0 = w.w1 = nullptr;
+}
+
+__device__ __forceinline__ void win_load(WarpWindow& w, const uint8_t* at) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();  // every lane is done with the previous window
+  const uint8_t* a0 =
+      reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(at) & ~uintptr_t(15));
+  const uint8_t* hi = reinterpret_cast<const uint8_t*>(
+      (reinterpret_cast<uintptr_t>(w.lim) + 15) & ~uintptr_t(15));
+  const uint8_t* a1 = hi - a0 > (ptrdiff_t)w.cap ? a0 + w.cap : hi;
+  const int nvec = (int)((a1 - a0) >> 4);
+  const uint4* s = reinterpret_cast<const uint4*>(a0);
+  uint4* d = reinterpret_cast<uint4*>(w.buf);
+  for (int i = lane; i < nvec; i += 32) d[i] = s[i];
+  __syncwarp();
+  w.w0 = a0;
+  w.w1 = a1;
+}
+
+// [p, p + n) readable from the window (n <= cap - 16 and p + n <= lim)
+__device__ __forceinline__ void win_need(WarpWindow& w, const uint8_t* p, uint32_t n) {
+  if (p < w.w0 || p + n > w.w1) win_load(w, p);
+}
+
+__device__ __forceinline__ uint8_t win_at(const WarpWindow& w, const uint8_t* p) {
+  return w.buf[p - w.w0];
+}
+
+// One Snappy element header at ip (< lim): literal or copy, its length, copy
+// offset and header bytes.  false when the header runs past lim.
+__device__ __forceinline__ bool snappy_elem(WarpWindow& w, const uint8_t* ip, uint32_t& len,
+                                            uint32_t& off, uint32_t& hdr, bool& lit) {
+  const uint64_t avail = (uint64_t)(w.lim - ip);
+  win_need(w, ip, (uint32_t)(avail < 5 ? avail : 5));
+  const uint8_t tag = win_at(w, ip);
+  const int kind = tag & 3;
+  off = 0;
+  lit = kind == 0;
+  if (lit) {
+    len = (uint32_t)(tag >> 2) + 1;
+    hdr = 1;
+    if (len > 60) {
+      const uint32_t nb = len - 60;
+      if (avail < 1 + (uint64_t)nb) return false;
+      uint32_t v = 0;
+      for (uint32_t b = 0; b < nb; b++) v |= (uint32_t)win_at(w, ip + 1 + b) << (8 * b);
+      if (v == 0xffffffffu) return false;
+      len = v + 1;
+      hdr = 1 + nb;
+    }
+    return true;
+  }
+  const uint32_t nb = kind == 1 ? 1 : kind == 2 ? 2 : 4;
+  if (avail < 1 + (uint64_t)nb) return false;
+  hdr = 1 + nb;
+  if (kind == 1) {
+    len = ((tag >> 2) & 7) + 4;
+    off = ((uint32_t)(tag >> 5) << 8) | win_at(w, ip + 1);
+  } else {
+    len = (uint32_t)(tag >> 2) + 1;
+    for (uint32_t b = 0; b < nb; b++) off |= (uint32_t)win_at(w, ip + 1 + b) << (8 * b);
+  }
+  return true;
+}
+
+constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
+constexpr uint32_t kScanWin = 8192;        // per warp, k_snappy_scan
+constexpr uint32_t kFragInWin = 8192;      // per warp, k_snappy_frags (after the output)
+constexpr uint32_t kWalkWin = 16384;       // per warp, PLAIN walks
+enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
+
+// Pass 1, warp per compressed page: walks the element headers (literal
+// bytes are skipped, not read) through a shared-memory window, checks the
+// stream, and records where each 64 KiB block of output starts in the input.
+// Snappy writers compress 64 KiB blocks independently; a page whose elements
+// all stay inside their block (no element straddles a block end, no copy
+// reaches into an earlier block) is decoded block-parallel by pass 2, any
+// other by one warp over the whole page.
+__global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
+                              const uint8_t* __restrict__ src,
+                              const uint64_t* __restrict__ frag_base,
+                              uint32_t* __restrict__ frag_ip, uint8_t* __restrict__ mode,
+                              uint32_t* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  WarpWindow w;
   for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
     const PageInfo pg = pages[p];
-    if (pg.in_src) continue;
-    const uint8_t* in = src + pg.src;
-    uint8_t* out = dst + pg.dst;
-    if (pg.lvl_bytes > pg.src_size || pg.lvl_bytes > pg.raw_size) {
-      if (lane == 0) set_error(status, kErrPageShort, p);
+    if (pg.in_src) {
+      if (lane == 0) mode[p] = kModeStored;
       continue;
     }
-    for (uint32_t i = lane; i < pg.lvl_bytes; i += 32) out[i] = in[i];
-    const bool ok = unsnap_warp(in + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
-                                out + pg.lvl_bytes, pg.raw_size - pg.lvl_bytes);
-    if (!ok && lane == 0) set_error(status, kErrSnappy, p);
+    bool ok = pg.lvl_bytes <= pg.src_size && pg.lvl_bytes <= pg.raw_size;
+    bool indep = true;
+    if (ok) {
+      const uint8_t* in = src + pg.src + pg.lvl_bytes;
+      const uint8_t* lim = src + pg.src + pg.src_size;
+      const uint32_t out_n = pg.raw_size - pg.lvl_bytes;
+      win_init(w, smem + (threadIdx.x >> 5) * kScanWin, kScanWin, lim);
+      // the uncompressed length
+      const uint64_t avail = (uint64_t)(lim - in);
+      win_need(w, in, (uint32_t)(avail < 5 ? avail : 5));
+      uint64_t ulen = 0;
+      uint32_t vb = 0;
+      ok = false;
+      for (; vb < 5 && vb < avail; vb++) {
+        const uint8_t b = win_at(w, in + vb);
+        ulen |= (uint64_t)(b & 0x7f) << (7 * vb);
+        if (!(b & 0x80)) {
+          ok = true;
+          vb++;
+          break;
+        }
+      }
+      ok = ok && ulen == out_n;
+      const uint8_t* ip = in + vb;
+      const uint64_t fb = frag_base[p];
+      if (lane == 0) frag_ip[fb] = (uint32_t)(ip - in);
+      uint32_t op = 0, fs = 0, fk = 0;
+      while (ok && ip < lim) {
+        uint32_t len, off, hdr;
+        bool lit;
+        if (!snappy_elem(w, ip, len, off, hdr, lit)) {
+          ok = false;
+          break;
+        }
+        if (lit ? (uint64_t)(lim - ip) < hdr + (uint64_t)len : (off == 0 || off > op)) {
+          ok = false;
+          break;
+        }
+        if ((uint64_t)op + len > out_n) {
+          ok = false;
+          break;
+        }
+        if (!lit && op - off < fs) indep = false;
+        const uint64_t fe = (uint64_t)fs + kFragBytes;
+        if ((uint64_t)op + len > fe) indep = false;
+        ip += hdr + (lit ? len : 0);
+        op += len;
+        if (indep && op == fe && op < out_n) {
+          fk++;
+          fs = op;
+          if (lane == 0) frag_ip[fb + fk] = (uint32_t)(ip - in);
+        }
+      }
+      ok = ok && op == out_n;
+    }
+    if (lane == 0) {
+      mode[p] = !ok ? kModeBad : indep ? kModeFragments : kModeSequential;
+      if (!ok) set_error(status, kErrSnappy, p);
+    }
+  }
+}
+
+// Pass 2, one warp (block) per 64 KiB output block: the block is built in
+// shared memory (back-references read shared memory, not the global bytes
+// just written), its input streamed through a shared-memory window, then
+// stored with 16-byte stores where the destination allows.  Work item
+// (page, block 0) also copies a v2 page's level bytes and, for a page pass 1
+// found not block-independent, decodes the whole page with unsnap_warp.
+__global__ void __launch_bounds__(32) k_snappy_frags(
+    const PageInfo* __restrict__ pages, const uint2* __restrict__ work, uint32_t nwork,
+    const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+    const uint64_t* __restrict__ frag_base, const uint32_t* __restrict__ frag_ip,
+    const uint8_t* __restrict__ mode, uint32_t* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  uint8_t* win = smem;  // kFragBytes of output
+  const int lane = threadIdx.x & 31;
+  WarpWindow w;
+  for (uint32_t t = blockIdx.x; t < nwork; t += gridDim.x) {
+    const uint2 wk = work[t];
+    const uint32_t p = wk.x, k = wk.y;
+    const PageInfo pg = pages[p];
+    const uint8_t m = mode[p];
+    if (m != kModeFragments && m != kModeSequential) continue;
+    const uint8_t* in0 = src + pg.src;
+    uint8_t* out0 = dst + pg.dst;
+    if (k == 0)
+      for (uint32_t i = lane; i < pg.lvl_bytes; i += 32) out0[i] = in0[i];
+    if (m == kModeSequential) {
+      if (k == 0) {
+        const bool ok = unsnap_warp(in0 + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
+                                    out0 + pg.lvl_bytes, pg.raw_size - pg.lvl_bytes);
+        if (!ok && lane == 0) set_error(status, kErrSnappy, p);
+      }
+      continue;
+    }
+    const uint32_t out_n = pg.raw_size - pg.lvl_bytes;
+    const uint32_t f0 = k * kFragBytes;
+    if (f0 >= out_n) continue;
+    const uint32_t fl = min(kFragBytes, out_n - f0);
+    const uint8_t* in = in0 + pg.lvl_bytes;
+    const uint8_t* lim = in0 + pg.src_size;
+    win_init(w, smem + kFragBytes, kFragInWin, lim);
+    const uint8_t* ip = in + frag_ip[frag_base[p] + k];
+    uint32_t op = 0;
+    bool ok = true;
+    while (op < fl) {
+      uint32_t len, off, hdr;
+      bool lit;
+      if (ip >= lim || !snappy_elem(w, ip, len, off, hdr, lit) || op + len > fl) {
+        ok = false;
+        break;
+      }
+      if (lit) {
+        const uint8_t* lp = ip + hdr;
+        if ((uint64_t)(lim - lp) < len) {
+          ok = false;
+          break;
+        }
+        uint32_t rem = len;
+        while (rem) {
+          win_need(w, lp, 1);
+          const uint32_t c = min(rem, (uint32_t)(w.w1 - lp));
+          const uint8_t* sb = w.buf + (lp - w.w0);
+          for (uint32_t i = lane; i < c; i += 32) win[op + i] = sb[i];
+          op += c;
+          lp += c;
+          rem -= c;
+        }
+        ip = lp;
+      } else {
+        if (off == 0 || off > op) {
+          ok = false;
+          break;
+        }
+        if (off >= len) {
+          for (uint32_t i = lane; i < len; i += 32) win[op + i] = win[op - off + i];
+        } else {
+          for (uint32_t i = lane; i < len; i += 32) win[op + i] = win[op - off + i % off];
+        }
+        op += len;
+        ip += hdr;
+      }
+      __syncwarp();
+    }
+    __syncwarp();
+    if (!ok) {
+      if (lane == 0) set_error(status, kErrSnappy, p);
+      continue;
+    }
+    uint8_t* g = out0 + pg.lvl_bytes + f0;
+    if ((reinterpret_cast<uintptr_t>(g) & 15) == 0) {
+      const uint32_t nv = fl >> 4;
+      for (uint32_t i = lane; i < nv; i += 32)
+        reinterpret_cast<uint4*>(g)[i] = reinterpret_cast<const uint4*>(win)[i];
+      for (uint32_t i = (nv << 4) + lane; i < fl; i += 32) g[i] = win[i];
+    } else {
+      for (uint32_t i = lane; i < fl; i += 32) g[i] = win[i];
+    }
+    __syncwarp();  // the next block reuses the shared memory
   }
 }
 
@@ -148,32 +406,40 @@ __device__ __forceinline__ const uint8_t* page_bytes(const PageInfo& pg, const u
   return pg.in_src ? src + pg.src : dst + pg.dst;
 }
 
-// Dictionary pages: lane 0 walks the PLAIN values (dictionaries are small).
+// Dictionary pages: every lane walks the PLAIN values through the warp's
+// shared-memory window; lane k % 32 writes entry k.
 __global__ void k_dict_pages(const PageInfo* __restrict__ pages, uint32_t np,
                              const uint8_t* __restrict__ src, const uint8_t* __restrict__ dst,
                              const uint64_t* __restrict__ dict_base,
                              uint64_t* __restrict__ dict_ptr, uint32_t* __restrict__ dict_len,
                              uint32_t* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  WarpWindow w;
   for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
     const PageInfo pg = pages[p];
-    if (pg.kind != 0 || lane != 0) continue;
+    if (pg.kind != 0) continue;
     const uint8_t* q = page_bytes(pg, src, dst);
     const uint8_t* end = q + pg.raw_size;
+    win_init(w, smem + (threadIdx.x >> 5) * kWalkWin, kWalkWin, end);
     const uint64_t base = dict_base[pg.dict];
     for (uint32_t k = 0; k < pg.num_values; k++) {
       if (end - q < 4) {
-        set_error(status, kErrDictPage, p);
+        if (lane == 0) set_error(status, kErrDictPage, p);
         break;
       }
-      const uint32_t l = ld_le32(q);
+      win_need(w, q, 4);
+      const uint32_t l = (uint32_t)win_at(w, q) | ((uint32_t)win_at(w, q + 1) << 8) |
+                         ((uint32_t)win_at(w, q + 2) << 16) | ((uint32_t)win_at(w, q + 3) << 24);
       if ((uint64_t)(end - q - 4) < l) {
-        set_error(status, kErrDictPage, p);
+        if (lane == 0) set_error(status, kErrDictPage, p);
         break;
       }
-      dict_ptr[base + k] = reinterpret_cast<uint64_t>(q + 4);
-      dict_len[base + k] = l;
+      if ((k & 31) == (uint32_t)lane) {
+        dict_ptr[base + k] = reinterpret_cast<uint64_t>(q + 4);
+        dict_len[base + k] = l;
+      }
       q += 4 + l;
     }
   }
@@ -245,6 +511,7 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
                              const uint64_t* __restrict__ dict_ptr,
                              const uint32_t* __restrict__ dict_len, RowArrays ra,
                              uint32_t* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -311,25 +578,30 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
         }
       }
       if (!fixed) {
+        // every lane walks the length words through the warp's window
+        WarpWindow w;
+        win_init(w, smem + (threadIdx.x >> 5) * kWalkWin, kWalkWin, end);
         bool good = true;
-        if (lane == 0) {
-          const uint8_t* q = vp;
-          for (uint32_t k = 0; k < m; k++) {
-            if (end - q < 4) {
-              good = false;
-              break;
-            }
-            const uint32_t l = ld_le32(q);
-            if ((uint64_t)(end - q - 4) < l) {
-              good = false;
-              break;
-            }
+        const uint8_t* q = vp;
+        for (uint32_t k = 0; k < m; k++) {
+          if (end - q < 4) {
+            good = false;
+            break;
+          }
+          win_need(w, q, 4);
+          const uint32_t l = (uint32_t)win_at(w, q) | ((uint32_t)win_at(w, q + 1) << 8) |
+                             ((uint32_t)win_at(w, q + 2) << 16) |
+                             ((uint32_t)win_at(w, q + 3) << 24);
+          if ((uint64_t)(end - q - 4) < l) {
+            good = false;
+            break;
+          }
+          if ((k & 31) == (uint32_t)lane) {
             tptr[k] = reinterpret_cast<uint64_t>(q + 4);
             tlen[k] = l;
-            q += 4 + l;
           }
+          q += 4 + l;
         }
-        good = __shfl_sync(0xffffffffu, good, 0);
         if (!good) {
           if (lane == 0) set_error(status, kErrPlain, p);
           continue;
@@ -466,7 +738,8 @@ struct SpjParquet {
   PinnedBuf stage_h;
   uint64_t stage_h_cap = 0;
   DevBuf stage, pages, pagebuf, dict_base, dict_n, dict_ptr, dict_len, valid, tmp_ptr, tmp_len,
-      vptr, vlen, pos, scan_tmp, out_off, out_data, out_valid, status, nulls;
+      vptr, vlen, pos, scan_tmp, out_off, out_data, out_valid, status, nulls, frag_base, frag_ip,
+      mode, work;
   double ms = 0, ms_phase[4] = {};  // H2D, decompress, decode, values
   uint64_t file_bytes = 0, page_bytes = 0, value_bytes = 0;
 
@@ -474,7 +747,8 @@ struct SpjParquet {
   void release_device() {
     for (DevBuf* b : {&stage, &pages, &pagebuf, &dict_base, &dict_n, &dict_ptr, &dict_len,
                       &valid, &tmp_ptr, &tmp_len, &vptr, &vlen, &pos, &scan_tmp, &out_off,
-                      &out_data, &out_valid, &status, &nulls})
+                      &out_data, &out_valid, &status, &nulls, &frag_base, &frag_ip, &mode,
+                      &work})
       b->release();
     if (stream) {
       cudaStreamSynchronize(stream);
@@ -691,6 +965,22 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     }
     p->page_bytes = pbytes;
     const uint32_t np = (uint32_t)pages.size();
+    // Snappy work: per compressed page one item per 64 KiB output block (at
+    // least one, which also copies a v2 page's level bytes)
+    std::vector<uint64_t> frag_base(np + 1, 0);
+    std::vector<uint2> work;
+    uint64_t nfrag = 0;
+    for (uint32_t i = 0; i < np; i++) {
+      frag_base[i] = nfrag;
+      if (pages[i].in_src) continue;
+      const uint64_t out_n = pages[i].raw_size >= pages[i].lvl_bytes
+                                 ? pages[i].raw_size - pages[i].lvl_bytes : 0;
+      const uint64_t nf = std::max<uint64_t>(1, (out_n + kFragBytes - 1) / kFragBytes);
+      for (uint64_t k = 0; k < nf; k++) work.push_back(make_uint2(i, (uint32_t)k));
+      nfrag += nf;
+    }
+    frag_base[np] = nfrag;
+    const uint32_t nwork = (uint32_t)work.size();
 
     SPJ_CUDA(cudaEventRecord(p->ev[0], s));
     p->stage.reserve(total + 16, s);
@@ -707,6 +997,15 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
                              cudaMemcpyHostToDevice, s));
     SPJ_CUDA(cudaMemcpyAsync(p->dict_n.get(), dict_n.data(), 4 * (ndict + 1),
                              cudaMemcpyHostToDevice, s));
+    p->frag_base.reserve(8 * (np + 1), s);
+    p->frag_ip.reserve(4 * (nfrag + 1), s);
+    p->mode.reserve(np + 16, s);
+    p->work.reserve(8 * (nwork + 1), s);
+    SPJ_CUDA(cudaMemcpyAsync(p->frag_base.get(), frag_base.data(), 8 * (np + 1),
+                             cudaMemcpyHostToDevice, s));
+    if (nwork)
+      SPJ_CUDA(cudaMemcpyAsync(p->work.get(), work.data(), 8 * (size_t)nwork,
+                               cudaMemcpyHostToDevice, s));
     p->pagebuf.reserve(dst + 16, s);
     p->dict_ptr.reserve(8 * (dict_total + 1), s);
     p->dict_len.reserve(4 * (dict_total + 1), s);
@@ -725,18 +1024,35 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     const uint8_t* dsrc = p->stage.as<uint8_t>();
     uint8_t* dpb = p->pagebuf.as<uint8_t>();
     uint32_t* st = p->status.as<uint32_t>();
-    const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
-    if (np) k_unsnap<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, st);
+    if (nwork) {
+      // Snappy: scan (warp per page), then block-parallel decode
+      SPJ_CUDA(cudaFuncSetAttribute(k_snappy_frags, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(kFragBytes + kFragInWin)));
+      k_snappy_scan<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 4 * kScanWin, s>>>(
+          dpages, np, dsrc, p->frag_base.as<uint64_t>(), p->frag_ip.as<uint32_t>(),
+          p->mode.as<uint8_t>(), st);
+      k_snappy_frags<<<(unsigned)std::min<uint64_t>(nwork, kNumSMs * 3 * 8), 32,
+                       kFragBytes + kFragInWin, s>>>(
+          dpages, p->work.as<uint2>(), nwork, dsrc, dpb, p->frag_base.as<uint64_t>(),
+          p->frag_ip.as<uint32_t>(), p->mode.as<uint8_t>(), st);
+    }
     SPJ_CUDA(cudaEventRecord(p->ev[2], s));
+    const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
+    const int walk_smem = 8 * kWalkWin;
     if (np) {
+      SPJ_CUDA(cudaFuncSetAttribute(k_dict_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    walk_smem));
+      SPJ_CUDA(cudaFuncSetAttribute(k_data_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    walk_smem));
       if (ndict)
-        k_dict_pages<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
-                                       p->dict_ptr.as<uint64_t>(), p->dict_len.as<uint32_t>(),
-                                       st);
+        k_dict_pages<<<g, 256, walk_smem, s>>>(dpages, np, dsrc, dpb,
+                                               p->dict_base.as<uint64_t>(),
+                                               p->dict_ptr.as<uint64_t>(),
+                                               p->dict_len.as<uint32_t>(), st);
       RowArrays ra{p->valid.as<uint8_t>(),    p->tmp_ptr.as<uint64_t>(),
                    p->tmp_len.as<uint32_t>(), p->vptr.as<uint64_t>(),
                    p->vlen.as<uint32_t>(),    p->nulls.as<unsigned long long>()};
-      k_data_pages<<<g, 256, 0, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
+      k_data_pages<<<g, 256, walk_smem, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
                                      p->dict_n.as<uint32_t>(), p->dict_ptr.as<uint64_t>(),
                                      p->dict_len.as<uint32_t>(), ra, st);
       SPJ_CUDA(cudaGetLastError());
