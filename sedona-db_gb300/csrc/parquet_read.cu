@@ -4,13 +4,14 @@
 // One read (all on the handle's stream, one H2D copy of the chunk bytes):
 //   host           footer (parsed at open); chunk bytes -> page-locked
 //                  buffer; page headers -> page table
-//   k_snappy_scan  warp per compressed page: element headers walked
-//                  through a shared-memory window; the input position of
-//                  every 64 KiB output block
-//   k_snappy_frags warp per 64 KiB output block: the block built in shared
-//                  memory, each element's bytes moved by the 32 lanes (a
-//                  back-reference shorter than its length repeats its
-//                  pattern, so every lane's byte is known without waiting)
+//   k_snappy_scan  warp per compressed page: element headers walked through
+//                  a shared-memory window; the input position of every
+//                  64 KiB output block
+//   k_snappy_frags warp per 64 KiB output block: each element's bytes moved
+//                  by the 32 lanes (a back-reference shorter than its length
+//                  repeats its pattern, so every lane's byte is known without
+//                  waiting); k_snappy_pages: warp per page for pages whose
+//                  elements cross block ends
 //   k_dict_pages   warp per dictionary page: PLAIN byte arrays -> entries
 //   k_data_pages   warp per data page: RLE / bit-packed definition levels ->
 //                  per-row validity; PLAIN values (equal-length values are
@@ -126,104 +127,114 @@ __device__ bool unsnap_warp(const uint8_t* in, uint32_t in_n, uint8_t* out, uint
 }
 
 // ---------------------------------------------------------------------------
-// A warp's window on a global byte range, staged in shared memory with
-// 16-byte loads.  Every lane keeps the same walk position, so the calls
-// below are warp-uniform.  The staged bytes may run past `lim` up to the next
-// 16-byte boundary: every device buffer these kernels read keeps 16 bytes of
-// slack after its last page, so those loads stay inside the allocation, and
-// bytes past `lim` are never used.
-struct WarpWindow {
-  const uint8_t* lim;
-  uint8_t* buf;   // shared memory, 16-byte aligned
-  uint32_t cap;   // bytes, multiple of 16
-  const uint8_t* w0;
-  const uint8_t* w1;
+// A warp's window on a byte range [base, base + n), staged in shared memory
+// with 16-byte loads; positions are 32-bit offsets from base.  Every lane
+// keeps the same walk position, so the reloads are warp-uniform.  A stage
+// starts at the 16-byte boundary at or below the position and may end up to
+// 15 bytes past the range: every device buffer these kernels read starts
+// 256-byte aligned and keeps 16 bytes of slack after its last page, so those
+// loads stay inside the allocation, and bytes outside the range are never
+// used.  The shared buffer has 16 bytes beyond `cap` for win_u32's second
+// word.
+struct Win {
+  const uint8_t* base;
+  uint32_t n;
+  uint8_t* buf;
+  uint32_t cap;
+  int32_t p0;  // position of buf[0]
+  int32_t hi;  // end of the staged positions
 };
 
-__device__ __forceinline__ void win_init(WarpWindow& w, uint8_t* buf, uint32_t cap,
-                                         const uint8_t* lim) {
+__device__ __forceinline__ void win_init(Win& w, const uint8_t* base, uint32_t n, uint8_t* buf,
+                                         uint32_t cap) {
+  w.base = base;
+  w.n = n;
   w.buf = buf;
   w.cap = cap;
-  w.lim = lim;
-  w.w0 = w.w1 = nullptr;
+  w.p0 = 0;
+  w.hi = 0;
 }
 
-__device__ __forceinline__ void win_load(WarpWindow& w, const uint8_t* at) {
+__device__ __noinline__ void win_stage(Win& w, uint32_t pos) {
   const int lane = threadIdx.x & 31;
-  __syncwarp();  // every lane is done with the previous window
-  const uint8_t* a0 =
-      reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(at) & ~uintptr_t(15));
-  const uint8_t* hi = reinterpret_cast<const uint8_t*>(
-      (reinterpret_cast<uintptr_t>(w.lim) + 15) & ~uintptr_t(15));
-  const uint8_t* a1 = hi - a0 > (ptrdiff_t)w.cap ? a0 + w.cap : hi;
-  const int nvec = (int)((a1 - a0) >> 4);
+  __syncwarp();  // every lane is done with the previous stage
+  const uintptr_t a = reinterpret_cast<uintptr_t>(w.base) + pos;
+  const uintptr_t a0 = a & ~uintptr_t(15);
+  const uintptr_t e = (reinterpret_cast<uintptr_t>(w.base) + w.n + 15) & ~uintptr_t(15);
+  const uint32_t bytes = e - a0 < w.cap ? (uint32_t)(e - a0) : w.cap;
   const uint4* s = reinterpret_cast<const uint4*>(a0);
   uint4* d = reinterpret_cast<uint4*>(w.buf);
-  for (int i = lane; i < nvec; i += 32) d[i] = s[i];
+  for (uint32_t i = lane; i < (bytes >> 4); i += 32) d[i] = s[i];
   __syncwarp();
-  w.w0 = a0;
-  w.w1 = a1;
+  w.p0 = (int32_t)pos - (int32_t)(a - a0);
+  w.hi = w.p0 + (int32_t)bytes;
 }
 
-// [p, p + n) readable from the window (n <= cap - 16 and p + n <= lim)
-__device__ __forceinline__ void win_need(WarpWindow& w, const uint8_t* p, uint32_t n) {
-  if (p < w.w0 || p + n > w.w1) win_load(w, p);
+// positions [pos, pos + k) staged (k <= 16)
+__device__ __forceinline__ void win_need(Win& w, uint32_t pos, uint32_t k) {
+  if ((int32_t)pos < w.p0 || (int32_t)(pos + k) > w.hi) win_stage(w, pos);
+}
+__device__ __forceinline__ uint32_t win_u8(const Win& w, uint32_t pos) {
+  return w.buf[pos - w.p0];
+}
+// four bytes at pos, little-endian: two aligned shared loads and a funnel shift
+__device__ __forceinline__ uint32_t win_u32(const Win& w, uint32_t pos) {
+  const uint32_t o = pos - (uint32_t)w.p0;
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(w.buf + (o & ~3u));
+  return __funnelshift_r(q[0], q[1], (o & 3) * 8);
 }
 
-__device__ __forceinline__ uint8_t win_at(const WarpWindow& w, const uint8_t* p) {
-  return w.buf[p - w.w0];
-}
+constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
+constexpr uint32_t kScanWin = 4096;        // per warp, k_snappy_scan
+constexpr uint32_t kFragWin = 2048;        // per warp, k_snappy_frags (headers only)
+constexpr uint32_t kWalkWin = 8192;        // per warp, PLAIN walks
+enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
 
-// One Snappy element header at ip (< lim): literal or copy, its length, copy
-// offset and header bytes.  false when the header runs past lim.
-__device__ __forceinline__ bool snappy_elem(WarpWindow& w, const uint8_t* ip, uint32_t& len,
-                                            uint32_t& off, uint32_t& hdr, bool& lit) {
-  const uint64_t avail = (uint64_t)(w.lim - ip);
-  win_need(w, ip, (uint32_t)(avail < 5 ? avail : 5));
-  const uint8_t tag = win_at(w, ip);
-  const int kind = tag & 3;
-  off = 0;
-  lit = kind == 0;
-  if (lit) {
-    len = (uint32_t)(tag >> 2) + 1;
+// One Snappy element header at position ip of the window's range: output
+// length, copy offset (0 for a literal; a copy's offset is never 0), and
+// input bytes to the next element (header plus a literal's bytes).  false
+// when it runs past the range or is a copy with offset 0.
+__device__ __forceinline__ bool snappy_header(Win& w, uint32_t ip, uint32_t& len, uint32_t& off,
+                                              uint32_t& adv, uint32_t& hdr) {
+  win_need(w, ip, 5);
+  const uint32_t tag = win_u8(w, ip);
+  const uint32_t kind = tag & 3;
+  const uint32_t room = w.n - ip;  // >= 1
+  if (kind == 0) {
+    off = 0;
+    len = (tag >> 2) + 1;
     hdr = 1;
     if (len > 60) {
       const uint32_t nb = len - 60;
-      if (avail < 1 + (uint64_t)nb) return false;
-      uint32_t v = 0;
-      for (uint32_t b = 0; b < nb; b++) v |= (uint32_t)win_at(w, ip + 1 + b) << (8 * b);
+      if (nb + 1 > room) return false;
+      const uint32_t v = win_u32(w, ip + 1) & (nb == 4 ? 0xffffffffu : ((1u << (8 * nb)) - 1));
       if (v == 0xffffffffu) return false;
       len = v + 1;
       hdr = 1 + nb;
     }
+    if ((uint64_t)hdr + len > room) return false;
+    adv = hdr + len;
     return true;
   }
-  const uint32_t nb = kind == 1 ? 1 : kind == 2 ? 2 : 4;
-  if (avail < 1 + (uint64_t)nb) return false;
-  hdr = 1 + nb;
+  hdr = kind == 1 ? 2 : kind == 2 ? 3 : 5;
+  if (hdr > room) return false;
   if (kind == 1) {
     len = ((tag >> 2) & 7) + 4;
-    off = ((uint32_t)(tag >> 5) << 8) | win_at(w, ip + 1);
+    off = ((tag >> 5) << 8) | win_u8(w, ip + 1);
   } else {
-    len = (uint32_t)(tag >> 2) + 1;
-    for (uint32_t b = 0; b < nb; b++) off |= (uint32_t)win_at(w, ip + 1 + b) << (8 * b);
+    len = (tag >> 2) + 1;
+    const uint32_t v = win_u32(w, ip + 1);
+    off = kind == 2 ? (v & 0xffffu) : v;
   }
-  return true;
+  adv = hdr;
+  return off != 0;
 }
 
-constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
-constexpr uint32_t kScanWin = 8192;        // per warp, k_snappy_scan
-constexpr uint32_t kFragInWin = 8192;      // per warp, k_snappy_frags (after the output)
-constexpr uint32_t kWalkWin = 16384;       // per warp, PLAIN walks
-enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
-
-// Pass 1, warp per compressed page: walks the element headers (literal
-// bytes are skipped, not read) through a shared-memory window, checks the
-// stream, and records where each 64 KiB block of output starts in the input.
-// Snappy writers compress 64 KiB blocks independently; a page whose elements
-// all stay inside their block (no element straddles a block end, no copy
-// reaches into an earlier block) is decoded block-parallel by pass 2, any
-// other by one warp over the whole page.
+// Pass 1, warp per compressed page: walks the element headers (a literal's
+// bytes are skipped, not read) and records where each 64 KiB block of output
+// starts in the input.  Snappy writers compress 64 KiB blocks on their own,
+// so a page whose elements never straddle a block end is decoded
+// block-parallel by pass 2; any other page by one warp (pass 3).
 __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
                               const uint8_t* __restrict__ src,
                               const uint64_t* __restrict__ frag_base,
@@ -232,64 +243,54 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  WarpWindow w;
+  Win w;
   for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
     const PageInfo pg = pages[p];
     if (pg.in_src) {
       if (lane == 0) mode[p] = kModeStored;
       continue;
     }
-    bool ok = pg.lvl_bytes <= pg.src_size && pg.lvl_bytes <= pg.raw_size;
+    bool ok = pg.lvl_bytes <= pg.src_size && pg.lvl_bytes <= pg.raw_size &&
+              pg.src_size > pg.lvl_bytes;
     bool indep = true;
     if (ok) {
-      const uint8_t* in = src + pg.src + pg.lvl_bytes;
-      const uint8_t* lim = src + pg.src + pg.src_size;
+      const uint32_t n_in = pg.src_size - pg.lvl_bytes;
       const uint32_t out_n = pg.raw_size - pg.lvl_bytes;
-      win_init(w, smem + (threadIdx.x >> 5) * kScanWin, kScanWin, lim);
-      // the uncompressed length
-      const uint64_t avail = (uint64_t)(lim - in);
-      win_need(w, in, (uint32_t)(avail < 5 ? avail : 5));
-      uint64_t ulen = 0;
-      uint32_t vb = 0;
+      win_init(w, src + pg.src + pg.lvl_bytes, n_in, smem + (threadIdx.x >> 5) * (kScanWin + 16),
+               kScanWin);
+      win_need(w, 0, 5);
+      uint32_t ulen = 0, vb = 0;
       ok = false;
-      for (; vb < 5 && vb < avail; vb++) {
-        const uint8_t b = win_at(w, in + vb);
-        ulen |= (uint64_t)(b & 0x7f) << (7 * vb);
+      for (; vb < 5 && vb < n_in; vb++) {
+        const uint32_t b = win_u8(w, vb);
+        ulen |= (b & 0x7f) << (7 * vb);
         if (!(b & 0x80)) {
-          ok = true;
+          ok = vb < 4 || b < 16;  // 32 bits at most
           vb++;
           break;
         }
       }
       ok = ok && ulen == out_n;
-      const uint8_t* ip = in + vb;
       const uint64_t fb = frag_base[p];
-      if (lane == 0) frag_ip[fb] = (uint32_t)(ip - in);
-      uint32_t op = 0, fs = 0, fk = 0;
-      while (ok && ip < lim) {
-        uint32_t len, off, hdr;
-        bool lit;
-        if (!snappy_elem(w, ip, len, off, hdr, lit)) {
+      if (lane == 0) frag_ip[fb] = vb;
+      uint32_t ip = vb, op = 0, fk = 0;
+      uint32_t fe = kFragBytes;
+      while (ok && ip < n_in) {
+        uint32_t len, off, adv, hdr;
+        if (!snappy_header(w, ip, len, off, adv, hdr) || len > out_n - op) {
           ok = false;
           break;
         }
-        if (lit ? (uint64_t)(lim - ip) < hdr + (uint64_t)len : (off == 0 || off > op)) {
-          ok = false;
-          break;
-        }
-        if ((uint64_t)op + len > out_n) {
-          ok = false;
-          break;
-        }
-        if (!lit && op - off < fs) indep = false;
-        const uint64_t fe = (uint64_t)fs + kFragBytes;
-        if ((uint64_t)op + len > fe) indep = false;
-        ip += hdr + (lit ? len : 0);
+        ip += adv;
         op += len;
-        if (indep && op == fe && op < out_n) {
-          fk++;
-          fs = op;
-          if (lane == 0) frag_ip[fb + fk] = (uint32_t)(ip - in);
+        if (op >= fe && indep) {
+          if (op > fe) {
+            indep = false;  // an element straddles a block end
+          } else if (op < out_n) {
+            fk++;
+            fe += kFragBytes;
+            if (lane == 0) frag_ip[fb + fk] = ip;
+          }
         }
       }
       ok = ok && op == out_n;
@@ -301,103 +302,87 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
   }
 }
 
-// Pass 2, one warp (block) per 64 KiB output block: the block is built in
-// shared memory (back-references read shared memory, not the global bytes
-// just written), its input streamed through a shared-memory window, then
-// stored with 16-byte stores where the destination allows.  Work item
-// (page, block 0) also copies a v2 page's level bytes and, for a page pass 1
-// found not block-independent, decodes the whole page with unsnap_warp.
-__global__ void __launch_bounds__(32) k_snappy_frags(
+// Pass 2, warp per 64 KiB output block of a block-independent page: element
+// headers through a small shared-memory window, literal bytes copied from
+// the input, copies from the block's own output, all by the 32 lanes.  A copy
+// that reaches before its block sends the page to pass 3.  Work item (page,
+// block 0) also copies a v2 page's level bytes.
+__global__ void __launch_bounds__(128) k_snappy_frags(
     const PageInfo* __restrict__ pages, const uint2* __restrict__ work, uint32_t nwork,
     const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
     const uint64_t* __restrict__ frag_base, const uint32_t* __restrict__ frag_ip,
-    const uint8_t* __restrict__ mode, uint32_t* status) {
+    uint8_t* __restrict__ mode, uint32_t* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  uint8_t* win = smem;  // kFragBytes of output
   const int lane = threadIdx.x & 31;
-  WarpWindow w;
-  for (uint32_t t = blockIdx.x; t < nwork; t += gridDim.x) {
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  Win w;
+  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nwork; t += nwarps) {
     const uint2 wk = work[t];
     const uint32_t p = wk.x, k = wk.y;
     const PageInfo pg = pages[p];
-    const uint8_t m = mode[p];
-    if (m != kModeFragments && m != kModeSequential) continue;
+    if (mode[p] != kModeFragments) continue;
     const uint8_t* in0 = src + pg.src;
     uint8_t* out0 = dst + pg.dst;
     if (k == 0)
       for (uint32_t i = lane; i < pg.lvl_bytes; i += 32) out0[i] = in0[i];
-    if (m == kModeSequential) {
-      if (k == 0) {
-        const bool ok = unsnap_warp(in0 + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
-                                    out0 + pg.lvl_bytes, pg.raw_size - pg.lvl_bytes);
-        if (!ok && lane == 0) set_error(status, kErrSnappy, p);
-      }
-      continue;
-    }
     const uint32_t out_n = pg.raw_size - pg.lvl_bytes;
     const uint32_t f0 = k * kFragBytes;
     if (f0 >= out_n) continue;
     const uint32_t fl = min(kFragBytes, out_n - f0);
     const uint8_t* in = in0 + pg.lvl_bytes;
-    const uint8_t* lim = in0 + pg.src_size;
-    win_init(w, smem + kFragBytes, kFragInWin, lim);
-    const uint8_t* ip = in + frag_ip[frag_base[p] + k];
-    uint32_t op = 0;
-    bool ok = true;
+    uint8_t* out = out0 + pg.lvl_bytes + f0;
+    win_init(w, in, pg.src_size - pg.lvl_bytes, smem + (threadIdx.x >> 5) * (kFragWin + 16),
+             kFragWin);
+    uint32_t ip = frag_ip[frag_base[p] + k], op = 0;
+    bool ok = true, local = true;
     while (op < fl) {
-      uint32_t len, off, hdr;
-      bool lit;
-      if (ip >= lim || !snappy_elem(w, ip, len, off, hdr, lit) || op + len > fl) {
+      uint32_t len, off, adv, hdr;
+      if (ip >= w.n || !snappy_header(w, ip, len, off, adv, hdr) || len > fl - op) {
         ok = false;
         break;
       }
-      if (lit) {
-        const uint8_t* lp = ip + hdr;
-        if ((uint64_t)(lim - lp) < len) {
-          ok = false;
-          break;
-        }
-        uint32_t rem = len;
-        while (rem) {
-          win_need(w, lp, 1);
-          const uint32_t c = min(rem, (uint32_t)(w.w1 - lp));
-          const uint8_t* sb = w.buf + (lp - w.w0);
-          for (uint32_t i = lane; i < c; i += 32) win[op + i] = sb[i];
-          op += c;
-          lp += c;
-          rem -= c;
-        }
-        ip = lp;
+      if (off == 0) {
+        const uint8_t* s = in + ip + hdr;
+        for (uint32_t i = lane; i < len; i += 32) out[op + i] = s[i];
       } else {
-        if (off == 0 || off > op) {
-          ok = false;
+        if (off > op) {  // reaches into an earlier block (or before the stream)
+          local = false;
           break;
         }
+        const uint8_t* s = out + op - off;
         if (off >= len) {
-          for (uint32_t i = lane; i < len; i += 32) win[op + i] = win[op - off + i];
+          for (uint32_t i = lane; i < len; i += 32) out[op + i] = s[i];
         } else {
-          for (uint32_t i = lane; i < len; i += 32) win[op + i] = win[op - off + i % off];
+          for (uint32_t i = lane; i < len; i += 32) out[op + i] = s[i % off];
         }
-        op += len;
-        ip += hdr;
       }
-      __syncwarp();
+      __syncwarp();  // the bytes just written may be the next copy's source
+      ip += adv;
+      op += len;
     }
-    __syncwarp();
-    if (!ok) {
-      if (lane == 0) set_error(status, kErrSnappy, p);
-      continue;
+    if (lane == 0) {
+      if (!local) mode[p] = kModeSequential;
+      else if (!ok) set_error(status, kErrSnappy, p);
     }
-    uint8_t* g = out0 + pg.lvl_bytes + f0;
-    if ((reinterpret_cast<uintptr_t>(g) & 15) == 0) {
-      const uint32_t nv = fl >> 4;
-      for (uint32_t i = lane; i < nv; i += 32)
-        reinterpret_cast<uint4*>(g)[i] = reinterpret_cast<const uint4*>(win)[i];
-      for (uint32_t i = (nv << 4) + lane; i < fl; i += 32) g[i] = win[i];
-    } else {
-      for (uint32_t i = lane; i < fl; i += 32) g[i] = win[i];
-    }
-    __syncwarp();  // the next block reuses the shared memory
+  }
+}
+
+// Pass 3, warp per page that pass 1 or 2 found not block-independent: the
+// whole page by one warp.
+__global__ void k_snappy_pages(const PageInfo* __restrict__ pages, uint32_t np,
+                               const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                               const uint8_t* __restrict__ mode, uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
+    if (mode[p] != kModeSequential) continue;
+    const PageInfo pg = pages[p];
+    const uint8_t* in0 = src + pg.src;
+    uint8_t* out0 = dst + pg.dst;
+    for (uint32_t i = lane; i < pg.lvl_bytes; i += 32) out0[i] = in0[i];
+    const bool ok = unsnap_warp(in0 + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
+                                out0 + pg.lvl_bytes, pg.raw_size - pg.lvl_bytes);
+    if (!ok && lane == 0) set_error(status, kErrSnappy, p);
   }
 }
 
@@ -416,28 +401,27 @@ __global__ void k_dict_pages(const PageInfo* __restrict__ pages, uint32_t np,
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  WarpWindow w;
+  Win w;
   for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
     const PageInfo pg = pages[p];
     if (pg.kind != 0) continue;
-    const uint8_t* q = page_bytes(pg, src, dst);
-    const uint8_t* end = q + pg.raw_size;
-    win_init(w, smem + (threadIdx.x >> 5) * kWalkWin, kWalkWin, end);
+    const uint8_t* page = page_bytes(pg, src, dst);
+    win_init(w, page, pg.raw_size, smem + (threadIdx.x >> 5) * (kWalkWin + 16), kWalkWin);
     const uint64_t base = dict_base[pg.dict];
+    uint32_t q = 0;
     for (uint32_t k = 0; k < pg.num_values; k++) {
-      if (end - q < 4) {
+      if (pg.raw_size - q < 4) {
         if (lane == 0) set_error(status, kErrDictPage, p);
         break;
       }
       win_need(w, q, 4);
-      const uint32_t l = (uint32_t)win_at(w, q) | ((uint32_t)win_at(w, q + 1) << 8) |
-                         ((uint32_t)win_at(w, q + 2) << 16) | ((uint32_t)win_at(w, q + 3) << 24);
-      if ((uint64_t)(end - q - 4) < l) {
+      const uint32_t l = win_u32(w, q);
+      if (pg.raw_size - q - 4 < l) {
         if (lane == 0) set_error(status, kErrDictPage, p);
         break;
       }
       if ((k & 31) == (uint32_t)lane) {
-        dict_ptr[base + k] = reinterpret_cast<uint64_t>(q + 4);
+        dict_ptr[base + k] = reinterpret_cast<uint64_t>(page + q + 4);
         dict_len[base + k] = l;
       }
       q += 4 + l;
@@ -579,25 +563,24 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
       }
       if (!fixed) {
         // every lane walks the length words through the warp's window
-        WarpWindow w;
-        win_init(w, smem + (threadIdx.x >> 5) * kWalkWin, kWalkWin, end);
+        Win w;
+        const uint32_t avail32 = (uint32_t)avail;
+        win_init(w, vp, avail32, smem + (threadIdx.x >> 5) * (kWalkWin + 16), kWalkWin);
         bool good = true;
-        const uint8_t* q = vp;
+        uint32_t q = 0;
         for (uint32_t k = 0; k < m; k++) {
-          if (end - q < 4) {
+          if (avail32 - q < 4) {
             good = false;
             break;
           }
           win_need(w, q, 4);
-          const uint32_t l = (uint32_t)win_at(w, q) | ((uint32_t)win_at(w, q + 1) << 8) |
-                             ((uint32_t)win_at(w, q + 2) << 16) |
-                             ((uint32_t)win_at(w, q + 3) << 24);
-          if ((uint64_t)(end - q - 4) < l) {
+          const uint32_t l = win_u32(w, q);
+          if (avail32 - q - 4 < l) {
             good = false;
             break;
           }
           if ((k & 31) == (uint32_t)lane) {
-            tptr[k] = reinterpret_cast<uint64_t>(q + 4);
+            tptr[k] = reinterpret_cast<uint64_t>(vp + q + 4);
             tlen[k] = l;
           }
           q += 4 + l;
@@ -1025,20 +1008,21 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     uint8_t* dpb = p->pagebuf.as<uint8_t>();
     uint32_t* st = p->status.as<uint32_t>();
     if (nwork) {
-      // Snappy: scan (warp per page), then block-parallel decode
-      SPJ_CUDA(cudaFuncSetAttribute(k_snappy_frags, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(kFragBytes + kFragInWin)));
-      k_snappy_scan<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 4 * kScanWin, s>>>(
-          dpages, np, dsrc, p->frag_base.as<uint64_t>(), p->frag_ip.as<uint32_t>(),
-          p->mode.as<uint8_t>(), st);
-      k_snappy_frags<<<(unsigned)std::min<uint64_t>(nwork, kNumSMs * 3 * 8), 32,
-                       kFragBytes + kFragInWin, s>>>(
+      // Snappy: header scan (warp per page), block-parallel decode, then the
+      // pages that are not block-independent
+      k_snappy_scan<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 4 * (kScanWin + 16),
+                      s>>>(dpages, np, dsrc, p->frag_base.as<uint64_t>(),
+                           p->frag_ip.as<uint32_t>(), p->mode.as<uint8_t>(), st);
+      k_snappy_frags<<<grid_for((int64_t)nwork * 32, 128, kNumSMs * 16), 128,
+                       4 * (kFragWin + 16), s>>>(
           dpages, p->work.as<uint2>(), nwork, dsrc, dpb, p->frag_base.as<uint64_t>(),
           p->frag_ip.as<uint32_t>(), p->mode.as<uint8_t>(), st);
+      k_snappy_pages<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 0, s>>>(
+          dpages, np, dsrc, dpb, p->mode.as<uint8_t>(), st);
     }
     SPJ_CUDA(cudaEventRecord(p->ev[2], s));
     const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
-    const int walk_smem = 8 * kWalkWin;
+    const int walk_smem = 8 * (kWalkWin + 16);
     if (np) {
       SPJ_CUDA(cudaFuncSetAttribute(k_dict_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     walk_smem));

@@ -139,7 +139,11 @@ def cross_block_file(path, rng):
     src = starts[3] + 2
     L = 48
     body[d:d + L] = body[src:src + L]
-    comp = (_varint(len(body)) + _snappy_literal(bytes(body[:d])) +
+    # the first literal ends exactly at the block end, so only the copy
+    # crosses blocks (the block-parallel pass finds it and hands the page
+    # to the per-page pass)
+    comp = (_varint(len(body)) + _snappy_literal(bytes(body[:65536])) +
+            _snappy_literal(bytes(body[65536:d])) +
             bytes([2 | ((L - 1) << 2)]) + (d - src).to_bytes(2, "little") +
             _snappy_literal(bytes(body[d + L:])))
     assert d - src < 65536 and d - src > d - 65536
