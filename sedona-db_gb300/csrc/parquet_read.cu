@@ -155,7 +155,7 @@ __device__ __forceinline__ void win_init(Win& w, const uint8_t* base, uint32_t n
   w.hi = 0;
 }
 
-__device__ __noinline__ void win_stage(Win& w, uint32_t pos) {
+__device__ __forceinline__ void win_stage(Win& w, uint32_t pos) {
   const int lane = threadIdx.x & 31;
   __syncwarp();  // every lane is done with the previous stage
   const uintptr_t a = reinterpret_cast<uintptr_t>(w.base) + pos;
