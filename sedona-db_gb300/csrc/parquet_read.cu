@@ -185,7 +185,6 @@ __device__ __forceinline__ uint32_t win_u32(const Win& w, uint32_t pos) {
 }
 
 constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
-constexpr uint32_t kScanWin = 4096;        // per warp, k_snappy_scan
 constexpr uint32_t kFragWin = 2048;        // per warp, k_snappy_frags (headers only)
 constexpr uint32_t kWalkWin = 8192;        // per warp, PLAIN walks
 enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
@@ -230,11 +229,53 @@ __device__ __forceinline__ bool snappy_header(Win& w, uint32_t ip, uint32_t& len
   return off != 0;
 }
 
-// Pass 1, warp per compressed page: walks the element headers (a literal's
-// bytes are skipped, not read) and records where each 64 KiB block of output
+// Pass 1, warp per compressed page: finds where each 64 KiB block of output
 // starts in the input.  Snappy writers compress 64 KiB blocks on their own,
 // so a page whose elements never straddle a block end is decoded
-// block-parallel by pass 2; any other page by one warp (pass 3).
+// block-parallel by pass 2; any other page by one warp (pass 3).  The walk
+// over element headers is a chain (each header gives the next one's
+// position), so the 32 lanes first parse a header at every position of a
+// staged chunk in parallel (most positions fall inside literal bytes and
+// are never used), and the walk then only chases table entries.
+constexpr uint32_t kScanChunk = 4096;  // table positions per stage
+constexpr uint32_t kScanStage = kScanChunk + 32;
+constexpr uint32_t kScanSmem = kScanStage + 16 + 4 * kScanChunk;  // per warp
+constexpr uint32_t kFar = 0xFFFFu;  // adv field: re-parse the header (a literal of 64 KiB or more)
+
+// the element at position j of the staged range as (adv | len << 16): 0 if
+// invalid, adv = kFar if either field needs more than 16 bits
+__device__ __forceinline__ uint32_t scan_entry(const Win& w, uint32_t j) {
+  const uint32_t room = w.n - j;
+  const uint32_t tag = win_u8(w, j);
+  const uint32_t kind = tag & 3;
+  if (kind == 0) {
+    uint32_t len = (tag >> 2) + 1, hdr = 1;
+    if (len > 60) {
+      const uint32_t nb = len - 60;
+      if (nb + 1 > room) return 0;
+      const uint32_t v = win_u32(w, j + 1) & (nb == 4 ? 0xffffffffu : ((1u << (8 * nb)) - 1));
+      if (v >= 0xffffu) return v == 0xffffffffu ? 0u : kFar;
+      len = v + 1;
+      hdr = 1 + nb;
+    }
+    if (hdr + len > room) return 0;
+    const uint32_t adv = hdr + len;
+    return adv >= kFar ? kFar : (adv | (len << 16));
+  }
+  const uint32_t hdr = kind == 1 ? 2 : kind == 2 ? 3 : 5;
+  if (hdr > room) return 0;
+  uint32_t len, off;
+  if (kind == 1) {
+    len = ((tag >> 2) & 7) + 4;
+    off = ((tag >> 5) << 8) | win_u8(w, j + 1);
+  } else {
+    len = (tag >> 2) + 1;
+    const uint32_t v = win_u32(w, j + 1);
+    off = kind == 2 ? (v & 0xffffu) : v;
+  }
+  return off == 0 ? 0u : (hdr | (len << 16));
+}
+
 __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
                               const uint8_t* __restrict__ src,
                               const uint64_t* __restrict__ frag_base,
@@ -243,6 +284,8 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  uint8_t* mine = smem + (threadIdx.x >> 5) * kScanSmem;
+  uint32_t* tbl = reinterpret_cast<uint32_t*>(mine + kScanStage + 16);
   Win w;
   for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
     const PageInfo pg = pages[p];
@@ -256,9 +299,8 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
     if (ok) {
       const uint32_t n_in = pg.src_size - pg.lvl_bytes;
       const uint32_t out_n = pg.raw_size - pg.lvl_bytes;
-      win_init(w, src + pg.src + pg.lvl_bytes, n_in, smem + (threadIdx.x >> 5) * (kScanWin + 16),
-               kScanWin);
-      win_need(w, 0, 5);
+      win_init(w, src + pg.src + pg.lvl_bytes, n_in, mine, kScanStage);
+      win_stage(w, 0);
       uint32_t ulen = 0, vb = 0;
       ok = false;
       for (; vb < 5 && vb < n_in; vb++) {
@@ -273,23 +315,38 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
       ok = ok && ulen == out_n;
       const uint64_t fb = frag_base[p];
       if (lane == 0) frag_ip[fb] = vb;
-      uint32_t ip = vb, op = 0, fk = 0;
+      uint32_t pos = vb, op = 0, fk = 0;
       uint32_t fe = kFragBytes;
-      while (ok && ip < n_in) {
-        uint32_t len, off, adv, hdr;
-        if (!snappy_header(w, ip, len, off, adv, hdr) || len > out_n - op) {
-          ok = false;
-          break;
+      while (ok && pos < n_in) {
+        win_stage(w, pos);
+        const uint32_t p0 = (uint32_t)w.p0;  // <= pos
+        const uint32_t tend = min(p0 + kScanChunk, n_in);
+        for (uint32_t t = lane; t < kScanChunk; t += 32) {
+          const uint32_t j = p0 + t;
+          tbl[t] = (j >= pos && j < tend) ? scan_entry(w, j) : 0u;
         }
-        ip += adv;
-        op += len;
-        if (op >= fe && indep) {
-          if (op > fe) {
-            indep = false;  // an element straddles a block end
-          } else if (op < out_n) {
-            fk++;
-            fe += kFragBytes;
-            if (lane == 0) frag_ip[fb + fk] = ip;
+        __syncwarp();
+        while (pos < tend) {
+          const uint32_t e = tbl[pos - p0];
+          uint32_t adv = e & 0xffffu, len = e >> 16;
+          if (adv == kFar) {
+            uint32_t off, hdr;
+            if (!snappy_header(w, pos, len, off, adv, hdr)) adv = 0;
+          }
+          if (adv == 0 || len > out_n - op) {
+            ok = false;
+            break;
+          }
+          pos += adv;
+          op += len;
+          if (op >= fe && indep) {
+            if (op > fe) {
+              indep = false;  // an element straddles a block end
+            } else if (op < out_n) {
+              fk++;
+              fe += kFragBytes;
+              if (lane == 0) frag_ip[fb + fk] = pos;
+            }
           }
         }
       }
@@ -507,10 +564,12 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
     const uint64_t fr = pg.first_row;
     const uint32_t nv = pg.num_values;
     uint8_t* valid = ra.valid + fr;
-    // definition levels
+    // definition levels, counting the non-null values as they are written
     const uint8_t* vp = raw;
+    uint32_t ones = 0;
     if (pg.max_def == 0) {
       for (uint32_t i = lane; i < nv; i += 32) valid[i] = 1;
+      ones = lane == 0 ? nv : 0;
     } else {
       bool ok = true;
       const uint8_t* lv = raw;
@@ -528,22 +587,21 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
         vp = raw + pg.lvl_bytes;
       }
       if (ok)
-        ok = rle_hybrid_warp(lv, lend, 1, nv,
-                             [&](uint32_t i, uint32_t v) { valid[i] = (uint8_t)(v & 1); });
+        ok = rle_hybrid_warp(lv, lend, 1, nv, [&](uint32_t i, uint32_t v) {
+          valid[i] = (uint8_t)(v & 1);
+          ones += v & 1;
+        });
       if (!ok) {
         if (lane == 0) set_error(status, kErrLevels, p);
         continue;
       }
     }
-    __syncwarp();
-    uint32_t m = 0;  // non-null values
-    for (uint32_t i0 = 0; i0 < nv; i0 += 32) {
-      const uint32_t i = i0 + lane;
-      m += __popc(__ballot_sync(0xffffffffu, i < nv && valid[i]));
-    }
-    // values, by non-null rank
-    uint64_t* tptr = ra.tmp_ptr + fr;
-    uint32_t* tlen = ra.tmp_len + fr;
+    const uint32_t m = __reduce_add_sync(0xffffffffu, ones);  // non-null values
+    // values, by non-null rank; a page without nulls writes its rows' spans
+    // directly (rank = row)
+    const bool all_valid = m == nv;
+    uint64_t* tptr = all_valid ? ra.vptr + fr : ra.tmp_ptr + fr;
+    uint32_t* tlen = all_valid ? ra.vlen + fr : ra.tmp_len + fr;
     if (pg.encoding == kPlain) {
       const uint64_t avail = (uint64_t)(end - vp);
       bool fixed = false;
@@ -617,6 +675,7 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
         continue;
       }
     }
+    if (all_valid) continue;
     __syncwarp();
     // rows: the rank of each valid row among the page's valid rows
     uint32_t base = 0, nnull = 0;
@@ -1010,8 +1069,9 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     if (nwork) {
       // Snappy: header scan (warp per page), block-parallel decode, then the
       // pages that are not block-independent
-      k_snappy_scan<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 4 * (kScanWin + 16),
-                      s>>>(dpages, np, dsrc, p->frag_base.as<uint64_t>(),
+      SPJ_CUDA(cudaFuncSetAttribute(k_snappy_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(4 * kScanSmem)));
+      k_snappy_scan<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 4 * kScanSmem, s>>>(dpages, np, dsrc, p->frag_base.as<uint64_t>(),
                            p->frag_ip.as<uint32_t>(), p->mode.as<uint8_t>(), st);
       k_snappy_frags<<<grid_for((int64_t)nwork * 32, 128, kNumSMs * 16), 128,
                        4 * (kFragWin + 16), s>>>(
