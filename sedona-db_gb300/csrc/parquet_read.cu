@@ -242,38 +242,30 @@ constexpr uint32_t kScanStage = kScanChunk + 32;
 constexpr uint32_t kScanSmem = kScanStage + 16 + 4 * kScanChunk;  // per warp
 constexpr uint32_t kFar = 0xFFFFu;  // adv field: re-parse the header (a literal of 64 KiB or more)
 
-// the element at position j of the staged range as (adv | len << 16): 0 if
-// invalid, adv = kFar if either field needs more than 16 bits
-__device__ __forceinline__ uint32_t scan_entry(const Win& w, uint32_t j) {
-  const uint32_t room = w.n - j;
-  const uint32_t tag = win_u8(w, j);
+// The element at staged offset t (position p0 + t) as (adv | len << 16),
+// computed without branches so that the 32 lanes, each at a different tag
+// kind, never diverge: adv = 0 marks a copy with offset 0, adv = kFar a
+// literal whose fields need more than 16 bits (the walk parses those
+// itself).  Lengths that run past the range are caught by the walk.
+__device__ __forceinline__ uint32_t scan_entry(const uint8_t* buf, uint32_t t) {
+  const uint32_t tag = buf[t];
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(buf + ((t + 1) & ~3u));
+  const uint32_t u = __funnelshift_r(q[0], q[1], ((t + 1) & 3) * 8);
   const uint32_t kind = tag & 3;
-  if (kind == 0) {
-    uint32_t len = (tag >> 2) + 1, hdr = 1;
-    if (len > 60) {
-      const uint32_t nb = len - 60;
-      if (nb + 1 > room) return 0;
-      const uint32_t v = win_u32(w, j + 1) & (nb == 4 ? 0xffffffffu : ((1u << (8 * nb)) - 1));
-      if (v >= 0xffffu) return v == 0xffffffffu ? 0u : kFar;
-      len = v + 1;
-      hdr = 1 + nb;
-    }
-    if (hdr + len > room) return 0;
-    const uint32_t adv = hdr + len;
-    return adv >= kFar ? kFar : (adv | (len << 16));
-  }
-  const uint32_t hdr = kind == 1 ? 2 : kind == 2 ? 3 : 5;
-  if (hdr > room) return 0;
-  uint32_t len, off;
-  if (kind == 1) {
-    len = ((tag >> 2) & 7) + 4;
-    off = ((tag >> 5) << 8) | win_u8(w, j + 1);
-  } else {
-    len = (tag >> 2) + 1;
-    const uint32_t v = win_u32(w, j + 1);
-    off = kind == 2 ? (v & 0xffffu) : v;
-  }
-  return off == 0 ? 0u : (hdr | (len << 16));
+  // literal
+  const uint32_t sl = (tag >> 2) + 1;
+  const uint32_t nb = sl > 60 ? sl - 60 : 0;
+  const uint32_t mask = nb == 4 ? 0xffffffffu : ((1u << (8 * nb)) - 1);
+  const uint32_t ext = u & mask;
+  const bool lfar = nb != 0 && ext >= 0xff00u;
+  const uint32_t llen = nb ? ext + 1 : sl;
+  const uint32_t lent = lfar ? kFar : ((1 + nb + llen) | (llen << 16));
+  // copy
+  const uint32_t chdr = kind == 1 ? 2u : kind == 2 ? 3u : 5u;
+  const uint32_t clen = kind == 1 ? ((tag >> 2) & 7) + 4 : (tag >> 2) + 1;
+  const uint32_t coff = kind == 1 ? (((tag >> 5) << 8) | (u & 0xffu)) : kind == 2 ? (u & 0xffffu) : u;
+  const uint32_t cent = coff == 0 ? 0u : (chdr | (clen << 16));
+  return kind == 0 ? lent : cent;
 }
 
 __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
@@ -321,10 +313,10 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
         win_stage(w, pos);
         const uint32_t p0 = (uint32_t)w.p0;  // <= pos
         const uint32_t tend = min(p0 + kScanChunk, n_in);
-        for (uint32_t t = lane; t < kScanChunk; t += 32) {
-          const uint32_t j = p0 + t;
-          tbl[t] = (j >= pos && j < tend) ? scan_entry(w, j) : 0u;
-        }
+        const uint32_t t0 = pos - p0, t1 = tend - p0;
+#pragma unroll 8
+        for (uint32_t t = lane; t < kScanChunk; t += 32)
+          if (t >= t0 && t < t1) tbl[t] = scan_entry(w.buf, t);
         __syncwarp();
         while (pos < tend) {
           const uint32_t e = tbl[pos - p0];
@@ -333,7 +325,7 @@ __global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
             uint32_t off, hdr;
             if (!snappy_header(w, pos, len, off, adv, hdr)) adv = 0;
           }
-          if (adv == 0 || len > out_n - op) {
+          if (adv == 0 || adv > n_in - pos || len > out_n - op) {
             ok = false;
             break;
           }
