@@ -3,10 +3,10 @@
 //
 // One read (all on the handle's stream, one H2D copy of the chunk bytes):
 //   host           footer (parsed at open); chunk bytes -> page-locked
-//                  buffer; page headers -> page table
-//   k_snappy_scan  warp per compressed page: element headers walked through
-//                  a shared-memory window; the input position of every
-//                  64 KiB output block
+//                  buffer; page headers -> page table; while the bytes are
+//                  copied, the Snappy block index of each compressed page
+//                  (snappy_block_index: a chain of element headers, walked
+//                  on host threads)
 //   k_snappy_frags warp per 64 KiB output block: each element's bytes moved
 //                  by the 32 lanes (a back-reference shorter than its length
 //                  repeats its pattern, so every lane's byte is known without
@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <thread>
 
 #include "../../include/spj_gb300.h"
 #include "parquet.cuh"
@@ -229,133 +230,11 @@ __device__ __forceinline__ bool snappy_header(Win& w, uint32_t ip, uint32_t& len
   return off != 0;
 }
 
-// Pass 1, warp per compressed page: finds where each 64 KiB block of output
-// starts in the input.  Snappy writers compress 64 KiB blocks on their own,
-// so a page whose elements never straddle a block end is decoded
-// block-parallel by pass 2; any other page by one warp (pass 3).  The walk
-// over element headers is a chain (each header gives the next one's
-// position), so the 32 lanes first parse a header at every position of a
-// staged chunk in parallel (most positions fall inside literal bytes and
-// are never used), and the walk then only chases table entries.
-constexpr uint32_t kScanChunk = 4096;  // table positions per stage
-constexpr uint32_t kScanStage = kScanChunk + 32;
-constexpr uint32_t kScanSmem = kScanStage + 16 + 4 * kScanChunk;  // per warp
-constexpr uint32_t kFar = 0xFFFFu;  // adv field: re-parse the header (a literal of 64 KiB or more)
-
-// The element at staged offset t (position p0 + t) as (adv | len << 16),
-// computed without branches so that the 32 lanes, each at a different tag
-// kind, never diverge: adv = 0 marks a copy with offset 0, adv = kFar a
-// literal whose fields need more than 16 bits (the walk parses those
-// itself).  Lengths that run past the range are caught by the walk.
-__device__ __forceinline__ uint32_t scan_entry(const uint8_t* buf, uint32_t t) {
-  const uint32_t tag = buf[t];
-  const uint32_t* q = reinterpret_cast<const uint32_t*>(buf + ((t + 1) & ~3u));
-  const uint32_t u = __funnelshift_r(q[0], q[1], ((t + 1) & 3) * 8);
-  const uint32_t kind = tag & 3;
-  // literal
-  const uint32_t sl = (tag >> 2) + 1;
-  const uint32_t nb = sl > 60 ? sl - 60 : 0;
-  const uint32_t mask = nb == 4 ? 0xffffffffu : ((1u << (8 * nb)) - 1);
-  const uint32_t ext = u & mask;
-  const bool lfar = nb != 0 && ext >= 0xff00u;
-  const uint32_t llen = nb ? ext + 1 : sl;
-  const uint32_t lent = lfar ? kFar : ((1 + nb + llen) | (llen << 16));
-  // copy
-  const uint32_t chdr = kind == 1 ? 2u : kind == 2 ? 3u : 5u;
-  const uint32_t clen = kind == 1 ? ((tag >> 2) & 7) + 4 : (tag >> 2) + 1;
-  const uint32_t coff = kind == 1 ? (((tag >> 5) << 8) | (u & 0xffu)) : kind == 2 ? (u & 0xffffu) : u;
-  const uint32_t cent = coff == 0 ? 0u : (chdr | (clen << 16));
-  return kind == 0 ? lent : cent;
-}
-
-__global__ void k_snappy_scan(const PageInfo* __restrict__ pages, uint32_t np,
-                              const uint8_t* __restrict__ src,
-                              const uint64_t* __restrict__ frag_base,
-                              uint32_t* __restrict__ frag_ip, uint8_t* __restrict__ mode,
-                              uint32_t* status) {
-  extern __shared__ __align__(16) uint8_t smem[];
-  const int lane = threadIdx.x & 31;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  uint8_t* mine = smem + (threadIdx.x >> 5) * kScanSmem;
-  uint32_t* tbl = reinterpret_cast<uint32_t*>(mine + kScanStage + 16);
-  Win w;
-  for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
-    const PageInfo pg = pages[p];
-    if (pg.in_src) {
-      if (lane == 0) mode[p] = kModeStored;
-      continue;
-    }
-    bool ok = pg.lvl_bytes <= pg.src_size && pg.lvl_bytes <= pg.raw_size &&
-              pg.src_size > pg.lvl_bytes;
-    bool indep = true;
-    if (ok) {
-      const uint32_t n_in = pg.src_size - pg.lvl_bytes;
-      const uint32_t out_n = pg.raw_size - pg.lvl_bytes;
-      win_init(w, src + pg.src + pg.lvl_bytes, n_in, mine, kScanStage);
-      win_stage(w, 0);
-      uint32_t ulen = 0, vb = 0;
-      ok = false;
-      for (; vb < 5 && vb < n_in; vb++) {
-        const uint32_t b = win_u8(w, vb);
-        ulen |= (b & 0x7f) << (7 * vb);
-        if (!(b & 0x80)) {
-          ok = vb < 4 || b < 16;  // 32 bits at most
-          vb++;
-          break;
-        }
-      }
-      ok = ok && ulen == out_n;
-      const uint64_t fb = frag_base[p];
-      if (lane == 0) frag_ip[fb] = vb;
-      uint32_t pos = vb, op = 0, fk = 0;
-      uint32_t fe = kFragBytes;
-      while (ok && pos < n_in) {
-        win_stage(w, pos);
-        const uint32_t p0 = (uint32_t)w.p0;  // <= pos
-        const uint32_t tend = min(p0 + kScanChunk, n_in);
-        const uint32_t t0 = pos - p0, t1 = tend - p0;
-#pragma unroll 8
-        for (uint32_t t = lane; t < kScanChunk; t += 32)
-          if (t >= t0 && t < t1) tbl[t] = scan_entry(w.buf, t);
-        __syncwarp();
-        while (pos < tend) {
-          const uint32_t e = tbl[pos - p0];
-          uint32_t adv = e & 0xffffu, len = e >> 16;
-          if (adv == kFar) {
-            uint32_t off, hdr;
-            if (!snappy_header(w, pos, len, off, adv, hdr)) adv = 0;
-          }
-          if (adv == 0 || adv > n_in - pos || len > out_n - op) {
-            ok = false;
-            break;
-          }
-          pos += adv;
-          op += len;
-          if (op >= fe && indep) {
-            if (op > fe) {
-              indep = false;  // an element straddles a block end
-            } else if (op < out_n) {
-              fk++;
-              fe += kFragBytes;
-              if (lane == 0) frag_ip[fb + fk] = pos;
-            }
-          }
-        }
-      }
-      ok = ok && op == out_n;
-    }
-    if (lane == 0) {
-      mode[p] = !ok ? kModeBad : indep ? kModeFragments : kModeSequential;
-      if (!ok) set_error(status, kErrSnappy, p);
-    }
-  }
-}
-
-// Pass 2, warp per 64 KiB output block of a block-independent page: element
+// Warp per 64 KiB output block of a block-independent page: element
 // headers through a small shared-memory window, literal bytes copied from
 // the input, copies from the block's own output, all by the 32 lanes.  A copy
-// that reaches before its block sends the page to pass 3.  Work item (page,
-// block 0) also copies a v2 page's level bytes.
+// that reaches before its block sends the page to k_snappy_pages.  Work item
+// (page, block 0) also copies a v2 page's level bytes.
 __global__ void __launch_bounds__(128) k_snappy_frags(
     const PageInfo* __restrict__ pages, const uint2* __restrict__ work, uint32_t nwork,
     const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
@@ -416,8 +295,8 @@ __global__ void __launch_bounds__(128) k_snappy_frags(
   }
 }
 
-// Pass 3, warp per page that pass 1 or 2 found not block-independent: the
-// whole page by one warp.
+// Warp per page that the block index or the block pass found not
+// block-independent: the whole page by one warp.
 __global__ void k_snappy_pages(const PageInfo* __restrict__ pages, uint32_t np,
                                const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
                                const uint8_t* __restrict__ mode, uint32_t* status) {
@@ -754,6 +633,74 @@ const char* error_name(uint32_t code) {
   }
 }
 
+// The Snappy block index of one compressed page, on the host: the input
+// position of every 64 KiB output block.  Snappy writers compress 64 KiB
+// blocks on their own, so when no element straddles a block end the blocks
+// decode in parallel on the device (kModeFragments); otherwise the page is
+// decoded by one warp (kModeSequential).  The walk over element headers is a
+// chain (each header gives the next one's position; literal bytes are
+// skipped) that a CPU core runs several times faster than one GPU warp, so
+// the host walks the pages, on several threads, while the chunk bytes are
+// copied to the device.  Malformed headers give kModeBad.
+uint8_t snappy_block_index(const uint8_t* in, uint32_t n_in, uint32_t out_n,
+                           uint32_t* frag_ip) {
+  uint64_t ulen = 0;
+  uint32_t pos = 0;
+  for (;; pos++) {
+    if (pos >= n_in || pos >= 5) return kModeBad;
+    ulen |= (uint64_t)(in[pos] & 0x7f) << (7 * pos);
+    if (!(in[pos] & 0x80)) break;
+  }
+  pos++;
+  if (ulen != out_n) return kModeBad;
+  frag_ip[0] = pos;
+  uint32_t op = 0, fk = 0;
+  uint64_t fe = kFragBytes;
+  bool indep = true;
+  while (pos < n_in) {
+    const uint32_t tag = in[pos];
+    const uint32_t room = n_in - pos;
+    uint64_t len, adv;
+    if ((tag & 3) == 0) {
+      len = (tag >> 2) + 1;
+      uint32_t hdr = 1;
+      if (len > 60) {
+        const uint32_t nb = (uint32_t)len - 60;
+        if (nb + 1 > room) return kModeBad;
+        uint64_t v = 0;
+        for (uint32_t b = 0; b < nb; b++) v |= (uint64_t)in[pos + 1 + b] << (8 * b);
+        len = v + 1;
+        hdr = 1 + nb;
+      }
+      adv = hdr + len;
+    } else {
+      const uint32_t kind = tag & 3;
+      adv = kind == 1 ? 2 : kind == 2 ? 3 : 5;
+      if (adv > room) return kModeBad;
+      len = kind == 1 ? ((tag >> 2) & 7) + 4 : (tag >> 2) + 1;
+      uint32_t off = 0;
+      if (kind == 1)
+        off = ((tag >> 5) << 8) | in[pos + 1];
+      else
+        for (uint32_t b = 0; b + 1 < adv; b++) off |= (uint32_t)in[pos + 1 + b] << (8 * b);
+      if (off == 0 || off > op) return kModeBad;
+    }
+    if (adv > room || len > out_n - op) return kModeBad;
+    pos += (uint32_t)adv;
+    op += (uint32_t)len;
+    if (indep && op >= fe) {
+      if (op > fe) {
+        indep = false;  // an element straddles a block end
+      } else if (op < out_n) {
+        frag_ip[++fk] = pos;
+        fe += kFragBytes;
+      }
+    }
+  }
+  if (op != out_n) return kModeBad;
+  return indep ? kModeFragments : kModeSequential;
+}
+
 }  // namespace
 }  // namespace pq
 }  // namespace spj
@@ -1020,6 +967,37 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     p->stage.reserve(total + 16, s);
     SPJ_CUDA(cudaMemcpyAsync(p->stage.get(), hb, total, cudaMemcpyHostToDevice, s));
     SPJ_CUDA(cudaEventRecord(p->ev[1], s));
+    // while the chunk bytes travel: the Snappy block index of every compressed
+    // page, on host threads (before any copy from pageable memory, which
+    // would wait for the copy above)
+    std::vector<uint8_t> mode(np + 1, kModeStored);
+    std::vector<uint32_t> frag_ip(nfrag + 1, 0);
+    {
+      std::vector<uint32_t> todo;
+      for (uint32_t i = 0; i < np; i++)
+        if (!pages[i].in_src) todo.push_back(i);
+      auto run = [&](size_t t, size_t nt) {
+        for (size_t j = t; j < todo.size(); j += nt) {
+          const PageInfo& pg = pages[todo[j]];
+          mode[todo[j]] =
+              pg.lvl_bytes < pg.src_size && pg.lvl_bytes <= pg.raw_size
+                  ? snappy_block_index(hb + pg.src + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
+                                       pg.raw_size - pg.lvl_bytes,
+                                       frag_ip.data() + frag_base[todo[j]])
+                  : (uint8_t)kModeBad;
+        }
+      };
+      const size_t nt = std::min<size_t>({16, std::max(1u, std::thread::hardware_concurrency()),
+                                          (todo.size() + 3) / 4});
+      std::vector<std::thread> th;
+      for (size_t t = 1; t < nt; t++) th.emplace_back(run, t, nt);
+      run(0, std::max<size_t>(nt, 1));
+      for (auto& t : th) t.join();
+      for (uint32_t i = 0; i < np; i++)
+        if (mode[i] == kModeBad)
+          throw Error("parquet: malformed Snappy data in page " + std::to_string(i) +
+                      " of the read (" + std::to_string(np) + " pages)");
+    }
     // the small tables come from pageable vectors: the copies complete
     // before the stream synchronisation below, while the vectors live
     p->pages.reserve(sizeof(PageInfo) * (np + 1), s);
@@ -1037,6 +1015,9 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     p->work.reserve(8 * (nwork + 1), s);
     SPJ_CUDA(cudaMemcpyAsync(p->frag_base.get(), frag_base.data(), 8 * (np + 1),
                              cudaMemcpyHostToDevice, s));
+    SPJ_CUDA(cudaMemcpyAsync(p->frag_ip.get(), frag_ip.data(), 4 * (nfrag + 1),
+                             cudaMemcpyHostToDevice, s));
+    SPJ_CUDA(cudaMemcpyAsync(p->mode.get(), mode.data(), np + 1, cudaMemcpyHostToDevice, s));
     if (nwork)
       SPJ_CUDA(cudaMemcpyAsync(p->work.get(), work.data(), 8 * (size_t)nwork,
                                cudaMemcpyHostToDevice, s));
@@ -1059,12 +1040,8 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     uint8_t* dpb = p->pagebuf.as<uint8_t>();
     uint32_t* st = p->status.as<uint32_t>();
     if (nwork) {
-      // Snappy: header scan (warp per page), block-parallel decode, then the
-      // pages that are not block-independent
-      SPJ_CUDA(cudaFuncSetAttribute(k_snappy_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(4 * kScanSmem)));
-      k_snappy_scan<<<grid_for((int64_t)np * 32, 128, kNumSMs * 16), 128, 4 * kScanSmem, s>>>(dpages, np, dsrc, p->frag_base.as<uint64_t>(),
-                           p->frag_ip.as<uint32_t>(), p->mode.as<uint8_t>(), st);
+      // Snappy: block-parallel decode, then the pages that are not
+      // block-independent
       k_snappy_frags<<<grid_for((int64_t)nwork * 32, 128, kNumSMs * 16), 128,
                        4 * (kFragWin + 16), s>>>(
           dpages, p->work.as<uint2>(), nwork, dsrc, dpb, p->frag_base.as<uint64_t>(),
