@@ -335,6 +335,84 @@ void* SpjKnnStream(SpjKnn* knn);
 int SpjKnnGetStats(SpjKnn* knn, uint64_t* queries, uint64_t* exact_evals, uint64_t* redone);
 
 /* ------------------------------------------------------------------------ */
+/* Partitioned (out-of-core) join.                                          */
+/*                                                                          */
+/* For build sides larger than the device: the reference's out-of-core    */
+/* join partitions the build side with a KDB tree built from a sample of   */
+/* its boxes (rust/sedona-spatial-join/src/prepare.rs:260-340,             */
+/* partitioning/kdb.rs), assigns every build row to the leaf it overlaps   */
+/* most and every probe row to the one partition whose build bounds it     */
+/* meets (Multi when several: partitioning/flat.rs), spills both sides and */
+/* joins partition by partition.  Here both columns stay in host memory:   */
+/* their boxes are decoded in row ranges, the tree is built on the host    */
+/* and applied on the device, and every pass gathers one partition's build */
+/* rows (and its probe rows plus the Multi rows) onto the device -- read   */
+/* by the device straight from host memory where it can read pageable      */
+/* memory (Grace's coherent link), else gathered by host threads into      */
+/* page-locked staging -- and builds and probes them with the join's       */
+/* options.  Every pair is delivered once.                                 */
+
+/* A WKB column (Arrow binary / large_binary layout) in host memory. */
+struct SpjHostWkb {
+  int64_t length;
+  const void* offsets;
+  int32_t offsets_are_64bit;
+  const uint8_t* data;
+  const uint8_t* validity; /* LSB bitmap or NULL */
+  int64_t validity_offset;
+};
+
+struct SpjPartitionOptions {
+  uint32_t num_partitions;     /* target KDB leaves; 0: from build_budget_bytes */
+  uint32_t sample_rows;        /* build boxes sampled for the tree; 0 = 10,000 */
+  uint64_t build_budget_bytes; /* device bytes one partition's build side may take
+                                  (about 2.5x its WKB bytes); 0 with 0 partitions:
+                                  one partition */
+  uint64_t seed;               /* of the sample */
+  int32_t host_gather;         /* 1: gather each pass's rows on the host even
+                                  where the device can read host memory */
+};
+
+struct SpjPartitionStats {
+  uint32_t partitions, passes;
+  uint64_t build_rows_max;    /* build rows of the largest partition */
+  uint64_t probe_rows_multi;  /* probe rows meeting several partitions */
+  uint64_t probe_rows_none;   /* probe rows meeting none (null, empty or outside) */
+  uint64_t probe_rows_probed; /* probe rows over all passes */
+  uint64_t pairs;
+  double ms_boxes, ms_partition, ms_passes; /* host wall time of the phases */
+  int32_t direct_host_reads;  /* 1: the device read the columns in host memory */
+};
+
+/* The join of two host columns in partition passes.  Each pass's pairs (row
+ * ids of the two columns) are delivered through callback; a non-zero return
+ * stops the join and is returned.  Within a pass the pairs are grouped by
+ * probe row (the partition's own probe rows first, then the Multi rows), in
+ * ascending row order within each group; passes run in leaf order.
+ * predicate / distance as SpjJoinProbeArrow (a distance column set with
+ * SpjJoinSetProbeDistances applies).  The join's build side is replaced:
+ * afterwards it holds the last partition.  stats may be NULL. */
+int SpjJoinPartitioned(SpjJoin* join, const struct SpjHostWkb* build,
+                       const struct SpjHostWkb* probe, int32_t predicate, double distance,
+                       const struct SpjPartitionOptions* options,
+                       int (*callback)(const uint32_t* build_indices,
+                                       const uint32_t* probe_indices, uint64_t length,
+                                       void* user_data),
+                       void* user_data, struct SpjPartitionStats* stats);
+/* The last SpjJoinPartitioned call's partitioning, for checks against the
+ * reference's rules.  counts[4] (host) receives the leaves, the samples, the
+ * tree's max items per node and max levels; with the other pointers NULL
+ * only counts is written.  Otherwise (host arrays): extent[4]; leaves and
+ * bounds (4 floats per leaf: min x, min y, max x, max y; the bounds of a
+ * partition without build rows are NaN); samples (4 per sample, insertion
+ * order); build_part (per build row: leaf, or 0xFFFFFFFF for a row without
+ * a box); probe_part (per probe row: leaf, leaves for Multi, leaves + 1 for
+ * None). */
+int SpjJoinPartitionLayout(SpjJoin* join, uint32_t* counts, float* extent, float* leaves,
+                           float* bounds, float* samples, uint32_t* build_part,
+                           uint32_t* probe_part);
+
+/* ------------------------------------------------------------------------ */
 /* GeoParquet -> device.                                                    */
 /*                                                                          */
 /* The reference reads GeoParquet with arrow-rs on the CPU                  */

@@ -23,6 +23,7 @@
 #include "engine.cuh"
 #include "knn.cuh"
 #include "learned.cuh"
+#include "partition.cuh"
 #include "stream.cuh"
 #include "prims.cuh"
 
@@ -590,6 +591,7 @@ struct SpjJoin {
   HostColumnBuilder host;
   std::vector<uint32_t> hb, hp;
   std::string last_error;
+  PartitionLayout layout;  // the last partitioned join's partitioning
   // per workspace slot: a second stream for device -> host pair copies (two
   // copy engines at once) and its fork / join events
   struct CopyLane {
@@ -890,6 +892,84 @@ extern "C" int SpjJoinSetProbeDistances(SpjJoin* j, const double* distances, uin
     SPJ_CUDA(cudaStreamSynchronize(s));
     j->dist_n = n;
     j->has_dist = true;
+  });
+}
+
+static HostWkbColumn host_column(const SpjHostWkb* c) {
+  SPJ_CHECK(c != nullptr, "null column");
+  SPJ_CHECK(c->length >= 0 && (c->length == 0 || (c->offsets && c->data)), "null buffers");
+  HostWkbColumn h;
+  h.n = c->length;
+  h.offsets = c->offsets;
+  h.offsets64 = c->offsets_are_64bit != 0;
+  h.data = c->data;
+  h.validity = c->validity;
+  h.validity_offset = c->validity_offset;
+  return h;
+}
+
+extern "C" int SpjJoinPartitioned(SpjJoin* j, const SpjHostWkb* build, const SpjHostWkb* probe,
+                                  int32_t predicate, double distance,
+                                  const SpjPartitionOptions* options,
+                                  int (*callback)(const uint32_t*, const uint32_t*, uint64_t,
+                                                  void*),
+                                  void* user_data, SpjPartitionStats* stats) {
+  int cb_status = 0;
+  int rc = guarded(j->last_error, [&] {
+    SPJ_CUDA(cudaSetDevice(j->rt->device_id));
+    SPJ_CHECK(callback != nullptr, "null callback");
+    const HostWkbColumn hb = host_column(build), hp = host_column(probe);
+    PartitionOptions o;
+    if (options) {
+      o.num_partitions = options->num_partitions;
+      o.sample_rows = options->sample_rows;
+      o.build_budget_bytes = options->build_budget_bytes;
+      o.seed = options->seed;
+      o.host_gather = options->host_gather != 0;
+    }
+    const double* dr = probe_distances(j, predicate, hp.n);
+    j->host.clear();
+    PartitionStats st;
+    cb_status = run_partitioned(
+        *j->engine, *j->ws, hb, hp, predicate, distance, dr, o, &st, &j->layout,
+        [&](const uint32_t* b, const uint32_t* p, uint64_t n) {
+          return callback(b, p, n, user_data);
+        });
+    if (stats) {
+      stats->partitions = st.partitions;
+      stats->passes = st.passes;
+      stats->build_rows_max = st.build_rows_max;
+      stats->probe_rows_multi = st.probe_rows_multi;
+      stats->probe_rows_none = st.probe_rows_none;
+      stats->probe_rows_probed = st.probe_rows_probed;
+      stats->pairs = st.pairs;
+      stats->ms_boxes = st.ms_boxes;
+      stats->ms_partition = st.ms_partition;
+      stats->ms_passes = st.ms_passes;
+      stats->direct_host_reads = st.direct_host_reads ? 1 : 0;
+    }
+  });
+  return rc ? rc : cb_status;
+}
+
+extern "C" int SpjJoinPartitionLayout(SpjJoin* j, uint32_t* counts, float* extent, float* leaves,
+                                      float* bounds, float* samples, uint32_t* build_part,
+                                      uint32_t* probe_part) {
+  return guarded(j->last_error, [&] {
+    SPJ_CHECK(counts != nullptr, "null counts");
+    const PartitionLayout& L = j->layout;
+    counts[0] = (uint32_t)L.leaves.size();
+    counts[1] = (uint32_t)L.samples.size();
+    counts[2] = L.max_items;
+    counts[3] = L.max_levels;
+    if (extent) memcpy(extent, &L.extent, 16);
+    if (leaves && !L.leaves.empty()) memcpy(leaves, L.leaves.data(), 16 * L.leaves.size());
+    if (bounds && !L.bounds.empty()) memcpy(bounds, L.bounds.data(), 16 * L.bounds.size());
+    if (samples && !L.samples.empty()) memcpy(samples, L.samples.data(), 16 * L.samples.size());
+    if (build_part && !L.build_part.empty())
+      memcpy(build_part, L.build_part.data(), 4 * L.build_part.size());
+    if (probe_part && !L.probe_part.empty())
+      memcpy(probe_part, L.probe_part.data(), 4 * L.probe_part.size());
   });
 }
 

@@ -17,6 +17,7 @@
 
 #include "../../include/spj_gb300.h"
 #include "common.cuh"
+#include "materialize.cuh"
 #include "prims.cuh"
 
 namespace spj {
@@ -188,6 +189,53 @@ cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 bool aligned(const void* p, size_t a) { return reinterpret_cast<uintptr_t>(p) % a == 0; }
 
 }  // namespace
+
+uint64_t gather_binary(const WkbDeviceColumn& col, const uint32_t* d_idx, uint64_t n,
+                       DevBuf& out_off, DevBuf& out_data, DevBuf& scratch_len,
+                       DevBuf& scratch_pos, DevBuf& scan_tmp, cudaStream_t s) {
+  scratch_len.reserve(((size_t)n + 1) * 4, s);
+  scratch_pos.reserve(((size_t)n + 1) * 8, s);
+  out_off.reserve(((size_t)n + 1) * 8, s);
+  const int g = grid_for((int64_t)n, 256, kNumSMs * 16);
+  if (n) {
+    if (col.offsets64)
+      k_bin_lengths<true><<<g, 256, 0, s>>>(col.offsets, d_idx, n, (uint64_t)col.n,
+                                            scratch_len.as<uint32_t>());
+    else
+      k_bin_lengths<false><<<g, 256, 0, s>>>(col.offsets, d_idx, n, (uint64_t)col.n,
+                                             scratch_len.as<uint32_t>());
+  }
+  scan_u32_u64(scratch_len.as<uint32_t>(), scratch_pos.as<uint64_t>(), (int64_t)n, scan_tmp, s);
+  uint64_t total = 0;
+  SPJ_CUDA(cudaMemcpyAsync(&total, scratch_pos.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  k_u64_to_i64_offsets<<<grid_for((int64_t)n + 1, 256), 256, 0, s>>>(
+      scratch_pos.as<uint64_t>(), n, out_off.as<int64_t>());
+  out_data.reserve(total + 16, s);
+  if (n && total) {
+    const int gw = grid_for((int64_t)n * 32, 256, kNumSMs * 32);
+    if (col.offsets64)
+      k_bin_copy<true><<<gw, 256, 0, s>>>(col.offsets, col.data, d_idx, n, (uint64_t)col.n,
+                                          scratch_pos.as<uint64_t>(), out_data.as<uint8_t>(),
+                                          total);
+    else
+      k_bin_copy<false><<<gw, 256, 0, s>>>(col.offsets, col.data, d_idx, n, (uint64_t)col.n,
+                                           scratch_pos.as<uint64_t>(), out_data.as<uint8_t>(),
+                                           total);
+  }
+  SPJ_CUDA(cudaGetLastError());
+  SPJ_CUDA(cudaStreamSynchronize(s));
+  return total;
+}
+
+void gather_u64(const uint64_t* values, uint64_t n_values, const uint32_t* d_idx, uint64_t n,
+                uint64_t* out, cudaStream_t s) {
+  if (!n) return;
+  k_gather_fixed<uint64_t><<<grid_for((int64_t)n, 256, kNumSMs * 16), 256, 0, s>>>(
+      values, d_idx, n, n_values, out);
+  SPJ_CUDA(cudaGetLastError());
+}
+
 }  // namespace spj
 
 using namespace spj;

@@ -148,6 +148,25 @@ class SpjKnnConfig(C.Structure):
 JOIN_CB = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint64,
                       C.c_void_p)
 
+class SpjHostWkb(C.Structure):
+    _fields_ = [("length", C.c_int64), ("offsets", C.c_void_p), ("offsets_are_64bit", C.c_int32),
+                ("data", C.c_void_p), ("validity", C.c_void_p), ("validity_offset", C.c_int64)]
+
+
+class SpjPartitionOptions(C.Structure):
+    _fields_ = [("num_partitions", C.c_uint32), ("sample_rows", C.c_uint32),
+                ("build_budget_bytes", C.c_uint64), ("seed", C.c_uint64),
+                ("host_gather", C.c_int32)]
+
+
+class SpjPartitionStats(C.Structure):
+    _fields_ = [("partitions", C.c_uint32), ("passes", C.c_uint32),
+                ("build_rows_max", C.c_uint64), ("probe_rows_multi", C.c_uint64),
+                ("probe_rows_none", C.c_uint64), ("probe_rows_probed", C.c_uint64),
+                ("pairs", C.c_uint64), ("ms_boxes", C.c_double), ("ms_partition", C.c_double),
+                ("ms_passes", C.c_double), ("direct_host_reads", C.c_int32)]
+
+
 class SpjParquetWriteOptions(C.Structure):
     _fields_ = [("compression", C.c_int32), ("page_version", C.c_int32),
                 ("row_group_rows", C.c_int64), ("page_bytes", C.c_int64)]
@@ -166,6 +185,7 @@ EXPORTS = [
     "SpjIndexProbeNoAlloc", "SpjAllocationCount",
     "SpjMaterializeLastError", "SpjGatherFixed", "SpjGatherValidity", "SpjGatherBinary",
     "SpjVisitedMark", "SpjVisitedCollect",
+    "SpjJoinPartitioned", "SpjJoinPartitionLayout",
     "SpjParquetOpen", "SpjParquetRelease", "SpjParquetLastError", "SpjParquetInfo",
     "SpjParquetColumnName", "SpjParquetRowGroupRows", "SpjParquetReadWkb", "SpjParquetGetStats", "SpjParquetGetPhases",
     "SpjParquetWriteWkb",
@@ -271,6 +291,11 @@ def lib() -> C.CDLL:
                                          C.c_void_p]
             L.SpjVisitedCollect.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p,
                                             C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]
+            L.SpjJoinPartitioned.argtypes = [C.c_void_p, C.POINTER(SpjHostWkb),
+                                             C.POINTER(SpjHostWkb), C.c_int32, C.c_double,
+                                             C.POINTER(SpjPartitionOptions), JOIN_CB,
+                                             C.c_void_p, C.POINTER(SpjPartitionStats)]
+            L.SpjJoinPartitionLayout.argtypes = [C.c_void_p] + [C.c_void_p] * 7
             L.SpjParquetOpen.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
             L.SpjParquetRelease.argtypes = [C.c_void_p]
             L.SpjParquetRelease.restype = None
@@ -565,6 +590,64 @@ class SpatialJoin:
         d = np.ascontiguousarray(distances, dtype=np.float64)
         _check(lib().SpjJoinSetProbeDistances(self.h, d.ctypes.data, len(d), 0),
                "set distances", self._err)
+
+    def join_partitioned(self, build: WkbColumn, probe: WkbColumn, predicate: str = "intersects",
+                         distance: float = 0.0, num_partitions: int = 0,
+                         build_budget_bytes: int = 0, sample_rows: int = 0, seed: int = 0,
+                         host_gather: bool = False):
+        """The join of two host columns in partition passes (SpjJoinPartitioned):
+        (build ids, probe ids, stats).  The join's build side is replaced."""
+        keep = []
+
+        def host(col):
+            off = np.ascontiguousarray(col.offsets)
+            data = np.ascontiguousarray(col.data) if len(col.data) else np.zeros(8, np.uint8)
+            val = np.ascontiguousarray(col.validity) if col.validity is not None else None
+            keep.extend([off, data, val])
+            return SpjHostWkb(len(col), off.ctypes.data, int(off.dtype == np.int64),
+                              data.ctypes.data, val.ctypes.data if val is not None else None, 0)
+
+        hb, hp = host(build), host(probe)
+        self._last_rows = (len(build), len(probe))
+        chunks = []
+
+        def cb(b, p, n, _ud):
+            if n:
+                chunks.append((np.ctypeslib.as_array(b, shape=(n,)).copy(),
+                               np.ctypeslib.as_array(p, shape=(n,)).copy()))
+            return 0
+
+        ccb = JOIN_CB(cb)
+        opt = SpjPartitionOptions(num_partitions, sample_rows, build_budget_bytes, seed,
+                                  int(host_gather))
+        st = SpjPartitionStats()
+        rc = lib().SpjJoinPartitioned(self.h, C.byref(hb), C.byref(hp), PREDICATES[predicate],
+                                      distance, C.byref(opt), ccb, None, C.byref(st))
+        _check(rc, "join_partitioned", self._err)
+        b = np.concatenate([c[0] for c in chunks]) if chunks else np.zeros(0, np.uint32)
+        p = np.concatenate([c[1] for c in chunks]) if chunks else np.zeros(0, np.uint32)
+        return b, p, {f: getattr(st, f) for f, _ in SpjPartitionStats._fields_}
+
+    def partition_layout(self) -> dict:
+        """The last partitioned join's partitioning (SpjJoinPartitionLayout)."""
+        counts = np.zeros(4, np.uint32)
+        _check(lib().SpjJoinPartitionLayout(self.h, counts.ctypes.data, *[None] * 6), "layout",
+               self._err)
+        nl, ns = int(counts[0]), int(counts[1])
+        extent = np.zeros(4, np.float32)
+        leaves = np.zeros((max(nl, 1), 4), np.float32)
+        bounds = np.zeros((max(nl, 1), 4), np.float32)
+        samples = np.zeros((max(ns, 1), 4), np.float32)
+        nb, npr = getattr(self, "_last_rows", (0, 0))
+        bpart = np.zeros(max(nb, 1), np.uint32)
+        ppart = np.zeros(max(npr, 1), np.uint32)
+        _check(lib().SpjJoinPartitionLayout(self.h, counts.ctypes.data, extent.ctypes.data,
+                                            leaves.ctypes.data, bounds.ctypes.data,
+                                            samples.ctypes.data, bpart.ctypes.data,
+                                            ppart.ctypes.data), "layout", self._err)
+        return {"extent": extent, "leaves": leaves[:nl], "bounds": bounds[:nl],
+                "samples": samples[:ns], "max_items": int(counts[2]),
+                "max_levels": int(counts[3]), "build_part": bpart[:nb], "probe_part": ppart[:npr]}
 
     def probe_device(self, dcol: SpjDeviceWkb, predicate: str = "intersects",
                      distance: float = 0.0, probe_base: int = 0):
