@@ -1239,6 +1239,92 @@ def run_materialize(args, local):
     }
 
 
+def run_outofcore(args, local):
+    """The partitioned (out-of-core) join on the polygon workload with its
+    roles swapped, so that the large side is the one partitioned: the 2M
+    buildings are the build side (held in host memory, split into KDB
+    partitions by a device budget of a quarter of their decoded size) and
+    the 50k zones probe every partition they meet.  value: pairs/s of
+    SpjJoinPartitioned from the host columns to the pairs on the host (its
+    inputs live in host memory by design, so value and e2e coincide)."""
+    from types import SimpleNamespace
+
+    import torch
+    from sedona_gpuspatial import capi
+    inp = make_inputs(2, args.scale)
+    build, probe = inp.probe, inp.build  # buildings build, zones probe
+    budget = int(build.nbytes * 5 // 2 // 4)
+    steps, warmup = min(args.steps, 3), 1
+    j = capi.SpatialJoin(profile=True)
+    for _ in range(warmup):
+        j.join_partitioned(build, probe, "intersects", build_budget_bytes=budget, seed=1)
+    j.reset_stats()
+    sampler = ClockSampler(local)
+    wall = 0.0
+    with sampler:
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b, p, st = j.join_partitioned(build, probe, "intersects", build_budget_bytes=budget,
+                                          seed=1)
+            wall += time.perf_counter() - t0
+    ms = wall * 1e3 / steps
+    js = j.stats()
+    npairs = len(b)
+    # parity: the same pair set as the one-pass join of the same sides
+    one = capi.SpatialJoin()
+    one.build(build)
+    t0 = time.perf_counter()
+    ob, op = one.probe(probe, "intersects")
+    one_ms = (time.perf_counter() - t0) * 1e3
+    keys = np.sort(p.astype(np.uint64) * np.uint64(len(build)) + b.astype(np.uint64))
+    okeys = np.sort(op.astype(np.uint64) * np.uint64(len(build)) + ob.astype(np.uint64))
+    parity = {"pairs": npairs, "pairs_equal_one_pass": bool(np.array_equal(keys, okeys)),
+              "unique": bool(len(np.unique(keys)) == len(keys)),
+              "checked": "sorted pair set against the one-pass GPU join of the same sides "
+                         "(whose pair set the headline checks against the oracle)"}
+    # roofline: the refine over all passes (algorithmic bytes as the headline's)
+    hbm_peak, peak_kind = load_peaks()
+    probe_vpr = probe_vertices_per_row(probe)
+    # the build side's vertices once over all passes: about its WKB bytes
+    ref_bytes = algorithmic_refine_bytes({"candidates": js["candidates"] / steps}, probe_vpr,
+                                         int(len(build.data)))
+    ref_ms = js["ms_refine"] / steps
+    achieved = ref_bytes / (ref_ms * 1e-3) / 1e9 if ref_ms > 0 else 0.0
+    cpu = cpu_baseline(SimpleNamespace(build=build, probe=probe, predicate="intersects",
+                                       params={}), seconds_budget=args.config_ref_seconds)
+    return {
+        "metric": "partitioned join pairs/s from host columns (build side in KDB partitions)",
+        "value": npairs / (ms * 1e-3), "unit": "pairs/s", "ms_per_step": ms, "steps": steps,
+        "warmup": warmup,
+        "phases_ms_per_step": {"boxes": st["ms_boxes"], "partition": st["ms_partition"],
+                               "passes": st["ms_passes"],
+                               "refine_device": js["ms_refine"] / steps,
+                               "filter_device": js["ms_filter"] / steps,
+                               "decode_device": js["ms_decode"] / steps},
+        "partitions": {k: st[k] for k in ("partitions", "passes", "build_rows_max",
+                                          "probe_rows_multi", "probe_rows_none",
+                                          "probe_rows_probed", "direct_host_reads")},
+        "one_pass_e2e_ms": one_ms,
+        "e2e": {"value": npairs / (ms * 1e-3), "unit": "pairs/s", "ms_per_step": ms,
+                "h2d_bytes_per_step": int(build.nbytes + probe.nbytes),
+                "d2h_bytes_per_step": int(8 * npairs),
+                "note": "both columns in host memory; every pass reads its rows from there"},
+        "roofline": {"bound": "hbm", "kernel": "k_refine<fast> (all passes)",
+                     "achieved": achieved, "peak": hbm_peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": ref_bytes},
+        "gpu_launches": int(js["kernel_launches"] / max(1, steps)),
+        "parity": parity,
+        "cpu_baseline": cpu,
+        "clocks": sampler.summary(),
+        "config": {"workload": "outofcore_2m_buildings_build_x_50k_zones_probe_kdb_partitions",
+                   "build_rows": len(build), "probe_rows": len(probe),
+                   "build_budget_bytes": budget, "predicate": "intersects",
+                   "l2": "columns > L2, no flush"},
+    }
+
+
 class _DevI32:
     def __init__(self, ptr, n):
         self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
@@ -1246,6 +1332,7 @@ class _DevI32:
 
 
 NESTED_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "probe_rows_per_s",
+               "partitions", "one_pass_e2e_ms",
                "plain_f64_form", "phases_ms_per_step", "fp64_escalated_fraction",
                "fp64_escalations_per_replay", "roofline", "e2e", "gpu_launches", "parity",
                "knn", "learned_index", "lbvh_fast_form", "per_batch_calls_f32_ms", "clocks",
@@ -1283,6 +1370,8 @@ def run_configs(args, world, rank, local, pg, names):
             out, inp = run_geoparquet(a, local), None
         elif name == "materialize":
             out, inp = run_materialize(a, local), None
+        elif name == "outofcore":
+            out, inp = run_outofcore(a, local), None
         else:
             raise SystemExit(f"unknown config {name}")
         entry = {k: out[k] for k in NESTED_KEYS + ("metric", "cpu_baseline") if k in out}
@@ -1314,7 +1403,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", dest="parity", action="store_false",
                     help="skip the parity check of the full-size run against the oracle")
-    ap.add_argument("--configs", default="1,2contains,3,4,5,geoparquet,materialize",
+    ap.add_argument("--configs", default="1,2contains,3,4,5,geoparquet,materialize,outofcore",
                     help="workload entries timed beside the headline (empty: none)")
     ap.add_argument("--config-ref-seconds", type=float, default=5.0)
     ap.add_argument("--join-options", type=json.loads, default={},
