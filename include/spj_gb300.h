@@ -371,6 +371,9 @@ struct SpjPartitionOptions {
   uint64_t seed;               /* of the sample */
   int32_t host_gather;         /* 1: gather each pass's rows on the host even
                                   where the device can read host memory */
+  int32_t record_layout;       /* 1: keep every row's partition for
+                                  SpjJoinPartitionLayout (a copy of 4 bytes per
+                                  row to the host) */
 };
 
 struct SpjPartitionStats {
@@ -407,7 +410,7 @@ int SpjJoinPartitioned(SpjJoin* join, const struct SpjHostWkb* build,
  * partition without build rows are NaN); samples (4 per sample, insertion
  * order); build_part (per build row: leaf, or 0xFFFFFFFF for a row without
  * a box); probe_part (per probe row: leaf, leaves for Multi, leaves + 1 for
- * None). */
+ * None); build_part and probe_part only after a call with record_layout. */
 int SpjJoinPartitionLayout(SpjJoin* join, uint32_t* counts, float* extent, float* leaves,
                            float* bounds, float* samples, uint32_t* build_part,
                            uint32_t* probe_part);

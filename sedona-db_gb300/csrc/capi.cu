@@ -926,6 +926,7 @@ extern "C" int SpjJoinPartitioned(SpjJoin* j, const SpjHostWkb* build, const Spj
       o.build_budget_bytes = options->build_budget_bytes;
       o.seed = options->seed;
       o.host_gather = options->host_gather != 0;
+      o.record_layout = options->record_layout != 0;
     }
     const double* dr = probe_distances(j, predicate, hp.n);
     j->host.clear();

@@ -264,15 +264,22 @@ __global__ void k_iota(uint32_t* __restrict__ v, uint64_t n) {
     v[i] = (uint32_t)i;
 }
 
-// kNone -> nbins - 1 so that the keys sort into bins
+// kNone -> nbins - 1 so that the keys sort into bins; one atomic per group
+// of lanes with the same bin (most rows of a warp share one)
 __global__ void k_hist(uint32_t* __restrict__ part, uint64_t n, uint32_t nbins,
                        uint32_t* __restrict__ count) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t p = part[i];
-    if (p >= nbins) p = nbins - 1;
-    part[i] = p;
-    atomicAdd(count + p, 1u);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t end = (n + 31) / 32 * 32;  // whole warps take every turn
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < end; i += stride) {
+    uint32_t p = 0xFFFFFFFFu;
+    if (i < n) {
+      p = part[i];
+      if (p >= nbins) p = nbins - 1;
+      part[i] = p;
+    }
+    const unsigned grp = __match_any_sync(0xffffffffu, p);
+    if (i < n && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1))
+      atomicAdd(count + p, (uint32_t)__popc(grp));
   }
 }
 
@@ -599,6 +606,10 @@ int run_partitioned(JoinEngine& eng, Workspace& ws, const HostWkbColumn& build,
     layout->max_items = (uint32_t)max_items;
     layout->max_levels = target;
     layout->leaves = leaf_ext;
+    layout->build_part.clear();
+    layout->probe_part.clear();
+  }
+  if (layout && opt.record_layout) {
     layout->build_part.resize(nb);
     layout->probe_part.resize(np);
     if (nb)

@@ -29,6 +29,7 @@ struct PartitionOptions {
   uint64_t build_budget_bytes = 0;  // device bytes per partition's build side (0: one)
   uint64_t seed = 0;
   bool host_gather = false;       // stage each pass's rows on the host
+  bool record_layout = false;     // copy every row's partition to the layout
 };
 
 struct PartitionStats {

@@ -156,7 +156,7 @@ class SpjHostWkb(C.Structure):
 class SpjPartitionOptions(C.Structure):
     _fields_ = [("num_partitions", C.c_uint32), ("sample_rows", C.c_uint32),
                 ("build_budget_bytes", C.c_uint64), ("seed", C.c_uint64),
-                ("host_gather", C.c_int32)]
+                ("host_gather", C.c_int32), ("record_layout", C.c_int32)]
 
 
 class SpjPartitionStats(C.Structure):
@@ -594,7 +594,7 @@ class SpatialJoin:
     def join_partitioned(self, build: WkbColumn, probe: WkbColumn, predicate: str = "intersects",
                          distance: float = 0.0, num_partitions: int = 0,
                          build_budget_bytes: int = 0, sample_rows: int = 0, seed: int = 0,
-                         host_gather: bool = False):
+                         host_gather: bool = False, record_layout: bool = False):
         """The join of two host columns in partition passes (SpjJoinPartitioned):
         (build ids, probe ids, stats).  The join's build side is replaced."""
         keep = []
@@ -619,7 +619,7 @@ class SpatialJoin:
 
         ccb = JOIN_CB(cb)
         opt = SpjPartitionOptions(num_partitions, sample_rows, build_budget_bytes, seed,
-                                  int(host_gather))
+                                  int(host_gather), int(record_layout))
         st = SpjPartitionStats()
         rc = lib().SpjJoinPartitioned(self.h, C.byref(hb), C.byref(hp), PREDICATES[predicate],
                                       distance, C.byref(opt), ccb, None, C.byref(st))

@@ -59,7 +59,7 @@ def test_partitioning_follows_reference_rules(capi, oracle_lib):
     inp = _inputs("polys")
     j = capi.SpatialJoin()
     j.join_partitioned(inp.build, inp.probe, "intersects", num_partitions=12, sample_rows=3000,
-                       seed=3)
+                       seed=3, record_layout=True)
     L = j.partition_layout()
     # the tree: rebuilt from the exported sample with the same parameters
     kdb = partition_ref.Kdb(L["max_items"], L["max_levels"], L["extent"])
@@ -134,6 +134,6 @@ def test_partitioned_budget_and_callback_stop(capi):
         return 9
 
     rc = capi.lib().SpjJoinPartitioned(j.h, C.byref(hb), C.byref(hp), 5, 0.0,
-                                       C.byref(capi.SpjPartitionOptions(8, 0, 0, 0, 0)),
+                                       C.byref(capi.SpjPartitionOptions(8, 0, 0, 0, 0, 0)),
                                        capi.JOIN_CB(cb), None, None)
     assert rc == 9 and len(calls) == 1
