@@ -7,6 +7,8 @@ Python surface:
             SpatialJoin, KnnJoin, StreamProbe, LearnedIndex: the extensions)
   wkb       Arrow binary WKB columns as numpy buffers
   datagen   seeded synthetic workloads
+  geoparquet  GeoParquet WKB columns read onto the device; a GeoParquet writer
+  materialize joined-batch gathers and the visited bitmap on the device
 """
 from .wkb import WkbColumn  # noqa: F401
 
