@@ -224,7 +224,13 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     // test, and small candidate sets do not repay the sort)
     cperm = build_major_order(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                               probe_base, bg_.n, order, n, ws.psc, s);
-    if (cperm) launches += 22;  // rank, keys, 4 radix passes
+    if (cperm) {
+      // Morton list (counts gather, scan, k_cand_perm), build-row gather and
+      // one radix pass per 8 bits of the build row; else rank, keys and 4 passes
+      int bits = 1;
+      while (bits < 32 && (bg_.n - 1) >> bits) bits++;
+      launches += order && bits <= 24 ? 6 + 5 * ((bits + 7) / 8) : 22;
+    }
     build_major = cperm != nullptr;
   }
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[2], s));

@@ -516,10 +516,39 @@ __global__ void k_cand_keys(const uint32_t* __restrict__ cb, const uint32_t* __r
 
 }  // namespace
 
+namespace {
+__global__ void k_gather_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
+                             uint64_t n, uint32_t* __restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = src[idx[i]];
+}
+}  // namespace
+
 const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
                                   uint32_t nprobe, ProbeScratch& sc, cudaStream_t s) {
   if (m < 2 || m >= 0xFFFFFFFFull) return nullptr;
+  int bb = 1;
+  while (bb < 32 && (nbuild - 1) >> bb) bb++;
+  if (order && bb <= 24) {
+    // the candidates listed in the probes' Morton order (k_cand_perm, coalesced),
+    // then a stable sort of that list by build row alone: build row, then the
+    // probe's full Morton rank, with ceil(bits / 8) radix passes
+    const uint32_t* mperm = candidate_order(order, nprobe, m, sc, s);
+    if (mperm) {
+      sc.ckeys.reserve((m + 1) * 4, s);
+      sc.ckeys_alt.reserve((m + 1) * 4, s);
+      sc.cvals_alt.reserve((m + 1) * 4, s);
+      k_gather_u32<<<grid_for((int64_t)m, 256), 256, 0, s>>>(cb, mperm, m,
+                                                             sc.ckeys.as<uint32_t>());
+      radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(),
+                       sc.ckeys_alt.as<uint32_t>(), sc.cvals_alt.as<uint32_t>(), (int64_t)m,
+                       bb, sc.tmp, s);
+      SPJ_CUDA(cudaGetLastError());
+      return sc.cperm.as<uint32_t>();
+    }
+  }
   // build id bits, then the probe's Morton rank in the remaining bits of a
   // 32-bit key (its resolution matters: 8 rank bits for 50k build rows gave
   // 98 ms per step on 2M x 50k polygons, 16 bits 77 ms)

@@ -169,7 +169,10 @@ const uint32_t* candidate_order_into(const uint32_t* order, const uint32_t* coun
 
 // The m candidates (cb, cp) ordered by build row, then by the probe's Morton
 // rank (order, when given) - a refine in that order takes one build
-// geometry with neighbouring probes together (sc.cperm).
+// geometry with neighbouring probes together (sc.cperm).  With an order the
+// candidates are first listed in the probes' Morton order and that list is
+// sorted stably by build row (full rank resolution, one radix pass per 8
+// build-row bits); without one, by a 32-bit key of build row and row id.
 const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
                                   uint32_t nprobe, ProbeScratch& sc, cudaStream_t s);
