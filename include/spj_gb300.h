@@ -112,9 +112,6 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "grid_rings"        0 (default) / 1: ring-ring and ring-in-ring tests
  *                       answer from the build ring's clean cells when the
  *                       probe ring's box lies in them
- *   "stage_bands"       0 (default) / 1: the one-pass FP32 refine in
- *                       build-major order keeps each warp's build row's band
- *                       entries (up to 256) in shared memory
  *   "dwithin_arena"     2 (default: auto, on when the probes are not in
  *                       Morton order), 1 on, 0 off: fused ST_DWithin keeps
  *                       the results past a probe's slots in an overflow
