@@ -808,10 +808,6 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
     } else if (k == "cell_grid") {
       SPJ_CHECK(value == 0 || value == 1, "cell_grid must be 0 or 1");
       c.cell_grid = value != 0;  // takes effect at the next build
-    } else if (k == "stage_bands") {
-      SPJ_CHECK(value == 0 || value == 1, "stage_bands must be 0 or 1");
-      c.stage_bands = value != 0;
-      j->engine->set_stage_bands(c.stage_bands);
     } else if (k == "grid_rings") {
       SPJ_CHECK(value == 0 || value == 1, "grid_rings must be 0 or 1");
       c.grid_rings = value != 0;

@@ -68,7 +68,6 @@ void JoinEngine::build(const WkbDeviceColumn& col) {
   bg_.has_grid = false;
   if (bg_.nrings > 0 && cfg_.cell_grid) build_cell_grid(bg_, bsc_, s);
   bg_.grid_rings = cfg_.grid_rings;
-  bg_.stage_bands = cfg_.stage_bands;
   if (bg_.nrings > 0) build_ring_flags(bg_, s);
   const uint32_t leaf = cfg_.leaf_size ? cfg_.leaf_size : (bg_.all_points ? 16u : 4u);
   build_lbvh(bg_.box.as<float4>(), bg_.n, leaf, bvh_, s);
@@ -247,14 +246,12 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     rqn = rq + m + 1;
   }
   const GeomsView bv = bg_.view(), pv = ws.probe.view();
-  GeomsView bvs = bv;  // the relation refine's view: may stage band entries
-  bvs.stage_bands = bg_.stage_bands && bg_.has_bands;
   if (predicate == kPredDWithin)
     refine_dwithin(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                    probe_base, distance, cfg_.refine_form, ws.flags.as<uint8_t>(),
                    ws.status.as<DeviceStatus>(), s, cperm, d_row);
   else
-    refine_relation(bvs, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
+    refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
                     ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb, rq, rqn,
                     cfg_.refine_split == 3);

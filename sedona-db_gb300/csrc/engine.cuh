@@ -63,7 +63,6 @@ struct EngineConfig {
   // 63.0 ms per step with it, 52.7 without: the zones' spiky edges leave few
   // buildings inside clean cells, and the lookup costs every pair)
   bool grid_rings = false;
-  bool stage_bands = false;
   // FP32 refine in two passes: a cheap pass (isolation exit, first vertex)
   // over every pair queues the pairs it leaves open, a full pass takes the
   // queue (a warp's lanes then hold pairs of similar cost).  0 off, 1 on,
@@ -133,7 +132,6 @@ class JoinEngine {
   void reindex(uint32_t leaf_size);
   const DeviceGeoms& build_geoms() const { return bg_; }
   void set_grid_rings(bool on) { bg_.grid_rings = on; }
-  void set_stage_bands(bool on) { bg_.stage_bands = on; }
   const Lbvh& lbvh() const { return bvh_; }
 
   // Probe with a device WKB column.  Results (device pointers owned by the

@@ -73,35 +73,7 @@ struct GeomsView {
   // ring-ring and ring-in-ring tests may answer from the cells that hold the
   // other ring's box (when they are all clean and alike)
   bool grid_rings = false;
-  // set only in the view handed to the staged refine kernel (k_refine with
-  // kStage): each warp keeps its build row's band entries in shared memory
-  bool stage_bands = false;
 };
-
-// The staged refine's dynamic shared memory: per warp of a 256-thread block a
-// descriptor (first entry, entries) in the first 64 bytes, then per warp a
-// slice of kStageEntries band entries.
-constexpr uint32_t kStageEntries = 256;
-constexpr uint32_t kStageHeader = 4;  // float4 elements holding the 8 descriptors
-extern __shared__ float4 stage_smem[];
-
-// The band entries of a ring whose first entry number is `first`, as its
-// scan should read them: the warp's shared-memory copy when the staged
-// refine holds that ring's build row, else global memory.  Entry numbers stay
-// global either way (the shared copy is reached through a base moved back by
-// the staged row's first entry number).  A build row's entries are contiguous,
-// so one ring's entries are either all staged or not at all.
-__device__ __forceinline__ const float4* band_segs(const GeomsView& G, uint32_t first) {
-  if (G.stage_bands) {
-    const uint32_t w = threadIdx.x >> 5;
-    const uint2 d = reinterpret_cast<const uint2*>(stage_smem)[w];
-    if (first - d.x < d.y)
-      return reinterpret_cast<const float4*>(
-          reinterpret_cast<uintptr_t>(stage_smem + kStageHeader + w * kStageEntries) -
-          (uintptr_t)d.x * sizeof(float4));
-  }
-  return G.band_seg;
-}
 
 struct DeviceGeoms {
   uint32_t n = 0, nparts = 0, nrings = 0, nverts = 0;
@@ -117,7 +89,6 @@ struct DeviceGeoms {
   DevBuf grid_meta, grid_rect, grid_status;
   bool has_grid = false;
   bool grid_rings = false;
-  bool stage_bands = false;
 
   GeomsView view() const {
     GeomsView v;

@@ -358,9 +358,8 @@ __device__ __forceinline__ RingHit ring_pip_plain(const GeomsView& G, uint32_t r
     const float2 prm = G.band_param[r];
     const int b = band_of(p32.y, prm.x, prm.y, nb);
     const uint32_t e0 = G.band_off[B + b], e1 = G.band_off[B + b + 1];
-    const float4* segs = band_segs(G, G.band_off[B]);
     for (uint32_t k = e0; k < e1; k++) {
-      const float4 sg = segs[k];
+      const float4 sg = G.band_seg[k];
       if (fmax0f(sg.x, sg.z) < p32.x) break;
       const int i = G.band_edges[k];
       pip_seg_f64(G.xy[V + i], G.xy[V + i + 1], p, i, aoe, in, idx);
@@ -408,9 +407,8 @@ __device__ __forceinline__ RingHit ring_pip_fast(const GeomsView& G, uint32_t r,
     const float2 prm = G.band_param[r];
     const int b = band_of(p32.y, prm.x, prm.y, nb);
     const uint32_t e0 = G.band_off[B + b], e1 = G.band_off[B + b + 1];
-    const float4* segs = band_segs(G, G.band_off[B]);
     for (uint32_t k = e0; k < e1; k++) {
-      const float4 sg = segs[k];
+      const float4 sg = G.band_seg[k];
       // entries run by xmax descending: from here on every segment lies
       // strictly left of p, and tg's +x ray cast gives OUT for each
       if (fmax0f(sg.x, sg.z) < p32.x) break;
@@ -556,11 +554,10 @@ __device__ __forceinline__ int ring_seg_hits(const GeomsView& G, uint32_t r, dou
     const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
     const float2 prm = G.band_param[r];
     const int b0 = band_of(qy0, prm.x, prm.y, nb), b1 = band_of(qy1, prm.x, prm.y, nb);
-    const float4* segs = band_segs(G, G.band_off[B]);
     for (int bb = b0; bb <= b1 && count < 2; bb++) {
       const uint32_t e0 = G.band_off[B + bb], e1 = G.band_off[B + bb + 1];
       for (uint32_t k = e0; k < e1 && count < 2; k++) {
-        const float4 sg = segs[k];
+        const float4 sg = G.band_seg[k];
         const float2 c = make_float2(sg.x, sg.y), d = make_float2(sg.z, sg.w);
         // xmax descending: the rest of the band is strictly left of the query
         if (fmax0f(c.x, d.x) < qx0) break;
@@ -684,12 +681,11 @@ __device__ __forceinline__ int ring_intersects_ring(const GeomsView& GA, uint32_
     bool v_decided = true;
     unsigned v_par = 0;
     bool near = false;
-    const float4* segs = band_segs(*Gr, Gr->band_off[B]);
     for (int bb = b0; bb <= b1 && !near; bb++) {
       const uint32_t e0 = Gr->band_off[B + bb], e1 = Gr->band_off[B + bb + 1];
       const bool vband = v_in_rect && bb == bv;
       for (uint32_t k = e0; k < e1; k++) {
-        const float4 sg = segs[k];
+        const float4 sg = Gr->band_seg[k];
         const float2 c = make_float2(sg.x, sg.y), d = make_float2(sg.z, sg.w);
         // xmax descending: the rest of the band is strictly left of the box
         // (bbox-separated) and of its first vertex (tg's ray cast: OUT)

@@ -96,12 +96,8 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      const uint32_t* perm, int min_blocks, uint32_t* queue, uint32_t* qn,
                      bool ordered_queue) {
   if (m == 0) return;
-  RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
-                 flags, st,    m_dev, perm, queue, qn,         s};
-  // only the one-pass FP32 kernel for 6 blocks per SM stages band entries
-  const bool staged = form == kFastF32 && !(queue && qn) && min_blocks == 6;
-  if (!staged) a.build.stage_bands = false;
-  const GeomsView& build_v = a.build;
+  const RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
+                       flags, st,    m_dev, perm, queue, qn,         s};
   if (form == kFastF32 && queue && qn) {
     launch_refine_split(a, min_blocks, ordered_queue);
     return;
@@ -112,10 +108,10 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
   }
   const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
   if (form == kFastF32)
-    k_refine<true, 4><<<g, 256, 0, s>>>(build_v, probe, cb, cp, m, probe_base, predicate, flags,
-                                        st, m_dev, perm);
+    k_refine<true, 4><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
+                                        m_dev, perm);
   else
-    k_refine<false, 1><<<g, 256, 0, s>>>(build_v, probe, cb, cp, m, probe_base, predicate, flags,
+    k_refine<false, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags,
                                          st, m_dev, perm);
   SPJ_CUDA(cudaGetLastError());
 }

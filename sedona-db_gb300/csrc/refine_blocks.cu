@@ -8,15 +8,8 @@ namespace spj {
 
 void launch_refine_blocks6(const RefineLaunch& a) {
   const int g = grid_for((int64_t)a.m, 256, kNumSMs * 16);
-  if (a.build.stage_bands && a.build.band_seg != nullptr) {
-    const int smem = (int)((kStageHeader + 8 * kStageEntries) * sizeof(float4));
-    k_refine<true, 6, 0, true><<<g, 256, smem, a.s>>>(a.build, a.probe, a.cb, a.cp, a.m,
-                                                      a.probe_base, a.predicate, a.flags, a.st,
-                                                      a.m_dev, a.perm);
-  } else {
-    k_refine<true, 6><<<g, 256, 0, a.s>>>(a.build, a.probe, a.cb, a.cp, a.m, a.probe_base,
-                                          a.predicate, a.flags, a.st, a.m_dev, a.perm);
-  }
+  k_refine<true, 6><<<g, 256, 0, a.s>>>(a.build, a.probe, a.cb, a.cp, a.m, a.probe_base,
+                                        a.predicate, a.flags, a.st, a.m_dev, a.perm);
   SPJ_CUDA(cudaGetLastError());
 }
 

@@ -192,13 +192,7 @@ __device__ __forceinline__ void flush_counters(DeviceStatus* st, uint32_t esc, u
 // perm) in full.  Splitting the work this way keeps a warp's lanes on pairs
 // of similar cost: a few pairs near a zone's edges take ten times the steps
 // of an isolated one, and would otherwise hold 31 idle lanes.
-// kStage (FP32 form, candidates in build-major order, B.stage_bands set):
-// each warp copies the band entries of its first pair's build row into its
-// kStageEntries-entry slice of shared memory (rows with more entries are not
-// staged) and records them in its descriptor; the band scans of every lane
-// whose ring lies in that row read there (band_segs): a warp's 32 pairs
-// mostly share one zone, whose entries every pair scans.
-template <bool kFast, int kMinBlocks, int kPhase = 0, bool kStage = false>
+template <bool kFast, int kMinBlocks, int kPhase = 0>
 __global__ void __launch_bounds__(256, kMinBlocks)
     k_refine(GeomsView B, GeomsView P, const uint32_t* __restrict__ cb,
              const uint32_t* __restrict__ cp, uint64_t m, uint32_t probe_base, int predicate,
@@ -219,52 +213,8 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   const uint64_t trips = (m + stride - 1) / stride;
   const uint64_t nq = kPhase == 2 ? min((uint64_t)*qn, m) : 0;
-  float4* wseg = kStage ? stage_smem + kStageHeader + (threadIdx.x >> 5) * kStageEntries : nullptr;
-  uint2* wdesc = kStage ? reinterpret_cast<uint2*>(stage_smem) + (threadIdx.x >> 5) : nullptr;
-  uint32_t zone = 0xFFFFFFFFu;
-  if (kStage) {
-    if ((threadIdx.x & 31) == 0) *wdesc = make_uint2(0u, 0u);
-    __syncwarp();
-  }
   for (uint64_t t = 0; t < trips; t++) {
     const uint64_t u = start + t * stride;
-    if (kStage) {
-      // the warp's first slot names the build row to stage (all lanes take
-      // part: the trips are uniform)
-      const int lane = threadIdx.x & 31;
-      uint32_t z = 0xFFFFFFFFu, e0 = 0, n = 0;
-      if (lane == 0) {
-        const uint64_t u0 = u;  // lane 0's slot
-        if (u0 < mm) {
-          const uint64_t k0 = perm ? (uint64_t)perm[u0] : u0;
-          if (k0 < mm) {
-            const uint32_t zb = cb[k0];
-            if (zb < B.n) {
-              const uint32_t r0 = B.part_ring[B.row_part[zb]];
-              const uint32_t r1 = B.part_ring[B.row_part[zb + 1]];
-              if (r1 > r0 && r1 <= B.nrings) {
-                e0 = B.band_off[B.ring_bands[r0]];
-                const uint32_t e1 = B.band_off[B.ring_bands[r1] - 1];
-                if (e1 >= e0 && e1 - e0 <= kStageEntries) {
-                  z = zb;
-                  n = e1 - e0;
-                }
-              }
-            }
-          }
-        }
-      }
-      z = __shfl_sync(0xffffffffu, z, 0);
-      if (z != zone) {
-        e0 = __shfl_sync(0xffffffffu, e0, 0);
-        n = __shfl_sync(0xffffffffu, n, 0);
-        __syncwarp();  // the lanes are done with the previous stage
-        for (uint32_t i = lane; i < n; i += 32) wseg[i] = B.band_seg[e0 + i];
-        if (lane == 0) *wdesc = make_uint2(e0, z == 0xFFFFFFFFu ? 0u : n);
-        __syncwarp();
-        zone = z;
-      }
-    }
     if (u >= m) continue;
     if (kPhase == 2 && u >= nq) continue;
     // a permutation with a device-side count covers slots [0, mm) only (the

@@ -64,11 +64,10 @@ __device__ __forceinline__ bool any_segment_near(const GeomsView& G, uint32_t r,
     const int nb = (int)(G.ring_bands[r + 1] - B) - 1;
     const float2 prm = G.band_param[r];
     const int b0 = band_of(qy0, prm.x, prm.y, nb), b1 = band_of(qy1, prm.x, prm.y, nb);
-    const float4* segs = band_segs(G, G.band_off[B]);
     for (int bb = b0; bb <= b1; bb++) {
       const uint32_t e0 = G.band_off[B + bb], e1 = G.band_off[B + bb + 1];
       for (uint32_t k = e0; k < e1; k++) {
-        const float4 sg = segs[k];
+        const float4 sg = G.band_seg[k];
         // xmax descending: the rest of the band is strictly left of the query
         if (fmax0f(sg.x, sg.z) < qx0) break;
         // each segment once: in the first band of the query that it spans

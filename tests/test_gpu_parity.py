@@ -250,28 +250,6 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     assert pairs(*out[variants[0]]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred, d)
 
 
-@pytest.mark.parametrize("pred", PREDS)
-def test_stage_bands_same_pairs(capi, oracle_mod, pred):
-    """The build-major refine with each warp's zone band entries staged in
-    shared memory (stage_bands) writes the same pairs at the same positions
-    as the unstaged kernel, for every relation predicate."""
-    from sedona_gpuspatial import datagen
-    inp = datagen.workload2(n_buildings=30000, n_zones=400)
-    out = []
-    for stage in (0, 1):
-        j = capi.SpatialJoin()
-        j.set_option("candidate_order", 2)
-        j.set_option("refine_min_blocks", 6)
-        j.set_option("refine_split", 0)
-        j.set_option("stage_bands", stage)
-        j.build(inp.build)
-        out.append(j.probe(inp.probe, pred))
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    np.testing.assert_array_equal(out[0][1], out[1][1])
-    if pred in ("intersects", "within"):
-        assert pairs(*out[1]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred)
-
-
 def test_unknown_option_is_an_error(capi):
     j = capi.SpatialJoin()
     with pytest.raises(capi.GpuSpatialError, match="unknown option"):
