@@ -94,10 +94,11 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint64_t* m_dev,
                      const uint32_t* perm, int min_blocks, uint32_t* queue, uint32_t* qn,
-                     bool ordered_queue) {
+                     bool ordered_queue, uint32_t chunk_trips) {
   if (m == 0) return;
-  const RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
-                       flags, st,    m_dev, perm, queue, qn,         s};
+  RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
+                 flags, st,    m_dev, perm, queue, qn,         s};
+  a.chunk_trips = chunk_trips;
   if (form == kFastF32 && queue && qn) {
     launch_refine_split(a, min_blocks, ordered_queue);
     return;

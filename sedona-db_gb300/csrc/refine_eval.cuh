@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
              uint8_t* __restrict__ flags, DeviceStatus* st, const uint64_t* __restrict__ m_dev,
              const uint32_t* __restrict__ perm, uint32_t* __restrict__ queue = nullptr,
              uint32_t* __restrict__ qn = nullptr,
-             const uint32_t* __restrict__ slot_perm = nullptr) {
+             const uint32_t* __restrict__ slot_perm = nullptr, uint32_t chunk_trips = 0) {
   // slot_perm (the split refine with an ordered queue): phase 1 queues the
   // slots u of perm instead of the candidates (the host sorts them), and
   // phase 2 maps a queued slot back through slot_perm
@@ -210,11 +210,17 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   const uint64_t mm = m_dev ? min(*m_dev, m) : m;
   // every lane runs the same number of loop trips so the warp-wide flush
   // below sees all 32 lanes
-  const uint64_t start = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  const uint64_t trips = (m + stride - 1) / stride;
+  // chunk_trips > 0: each block takes chunk_trips consecutive runs of
+  // blockDim.x slots (so that its trips meet the same build rows, whose band
+  // entries stay in L1); 0: the grid strides over all slots
+  const uint64_t start = chunk_trips
+                             ? blockIdx.x * (uint64_t)blockDim.x * chunk_trips + threadIdx.x
+                             : blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t step = chunk_trips ? (uint64_t)blockDim.x : stride;
+  const uint64_t trips = chunk_trips ? chunk_trips : (m + stride - 1) / stride;
   const uint64_t nq = kPhase == 2 ? min((uint64_t)*qn, m) : 0;
   for (uint64_t t = 0; t < trips; t++) {
-    const uint64_t u = start + t * stride;
+    const uint64_t u = start + t * step;
     if (u >= m) continue;
     if (kPhase == 2 && u >= nq) continue;
     // a permutation with a device-side count covers slots [0, mm) only (the
@@ -263,6 +269,7 @@ struct RefineLaunch {
   const uint32_t* perm;
   uint32_t *queue, *qn;
   cudaStream_t s;
+  uint32_t chunk_trips = 0;  // one-pass kernel for 6 blocks: see k_refine
 };
 // refine_split.cu: the cheap pass then the full pass over its queue
 // (min_blocks 4 or 6); ordered (with a perm): the queue is sorted back into
