@@ -304,8 +304,6 @@ def run_ours(args, world, rank, local, pg, light=False, workload=None, pred_over
                                      {"cell_grid": 0}, {"grid_rings": 1},
                                      {"probe_order": -1},
                                      {"refine_split": 1}, {"refine_split": 3},
-                                     {"refine_chunk": 4}, {"refine_chunk": 16},
-                                     {"refine_chunk": 64},
                                      {"candidate_order": 0, "refine_split": 0}]
     if pred == "dwithin" and not light:
         option_sets += [{"fuse_dwithin": 0}, {"dwithin_slots": 0}, {"dwithin_slots": 128},

@@ -109,9 +109,6 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "cell_grid"         1 (default) / 0: per-ring cell grids on the build side
  *                       (clean cells answer point-in-ring tests in O(1)); set
  *                       before the build
- *   "refine_chunk"      0 (default: the grid strides over the candidates),
- *                       1-1024: the one-pass refine in build-major order gives
- *                       each block that many consecutive runs of 256 pairs
  *   "grid_rings"        0 (default) / 1: ring-ring and ring-in-ring tests
  *                       answer from the build ring's clean cells when the
  *                       probe ring's box lies in them

@@ -808,9 +808,6 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
     } else if (k == "cell_grid") {
       SPJ_CHECK(value == 0 || value == 1, "cell_grid must be 0 or 1");
       c.cell_grid = value != 0;  // takes effect at the next build
-    } else if (k == "refine_chunk") {
-      SPJ_CHECK(value >= 0 && value <= 1024, "refine_chunk must be 0-1024");
-      c.refine_chunk = (uint32_t)value;
     } else if (k == "grid_rings") {
       SPJ_CHECK(value == 0 || value == 1, "grid_rings must be 0 or 1");
       c.grid_rings = value != 0;

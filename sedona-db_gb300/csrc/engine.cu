@@ -254,7 +254,7 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     refine_relation(bv, pv, ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
                     probe_base, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
                     ws.status.as<DeviceStatus>(), s, nullptr, cperm, mb, rq, rqn,
-                    cfg_.refine_split == 3, cfg_.refine_chunk);
+                    cfg_.refine_split == 3);
   launches += rq ? 2 : 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 

@@ -63,7 +63,6 @@ struct EngineConfig {
   // 63.0 ms per step with it, 52.7 without: the zones' spiky edges leave few
   // buildings inside clean cells, and the lookup costs every pair)
   bool grid_rings = false;
-  uint32_t refine_chunk = 0;  // one-pass build-major refine: trips per block (0: grid stride)
   // FP32 refine in two passes: a cheap pass (isolation exit, first vertex)
   // over every pair queues the pairs it leaves open, a full pass takes the
   // queue (a warp's lanes then hold pairs of similar cost).  0 off, 1 on,

@@ -94,11 +94,10 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      const uint32_t* cp, uint64_t m, uint32_t probe_base, int predicate, int form,
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s, const uint64_t* m_dev,
                      const uint32_t* perm, int min_blocks, uint32_t* queue, uint32_t* qn,
-                     bool ordered_queue, uint32_t chunk_trips) {
+                     bool ordered_queue) {
   if (m == 0) return;
-  RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
-                 flags, st,    m_dev, perm, queue, qn,         s};
-  a.chunk_trips = chunk_trips;
+  const RefineLaunch a{build, probe, cb,    cp,   m,     probe_base, predicate,
+                       flags, st,    m_dev, perm, queue, qn,         s};
   if (form == kFastF32 && queue && qn) {
     launch_refine_split(a, min_blocks, ordered_queue);
     return;
@@ -107,13 +106,14 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
     launch_refine_blocks6(a);
     return;
   }
-  const int g = grid_for((int64_t)m, 256, kNumSMs * 16);
+  const uint32_t trips = m_dev ? 0 : kRefineChunkTrips;
+  const unsigned g = refine_grid(m, trips);
   if (form == kFastF32)
     k_refine<true, 4><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags, st,
-                                        m_dev, perm);
+                                        m_dev, perm, nullptr, nullptr, nullptr, trips);
   else
     k_refine<false, 1><<<g, 256, 0, s>>>(build, probe, cb, cp, m, probe_base, predicate, flags,
-                                         st, m_dev, perm);
+                                         st, m_dev, perm, nullptr, nullptr, nullptr, trips);
   SPJ_CUDA(cudaGetLastError());
 }
 

@@ -41,7 +41,7 @@ void refine_relation(const GeomsView& build, const GeomsView& probe, const uint3
                      uint8_t* flags, DeviceStatus* st, cudaStream_t s,
                      const uint64_t* m_dev = nullptr, const uint32_t* perm = nullptr,
                      int min_blocks = 4, uint32_t* queue = nullptr, uint32_t* qn = nullptr,
-                     bool ordered_queue = false, uint32_t chunk_trips = 0);
+                     bool ordered_queue = false);
 
 // flags[k] = distance(build, probe) <= d.  Point pairs: hypot, decided by an
 // FP64 squared-distance test outside a 1e-14 relative band around d^2 and by

@@ -250,28 +250,6 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     assert pairs(*out[variants[0]]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred, d)
 
 
-@pytest.mark.parametrize("pred", ["intersects", "contains", "touches"])
-def test_refine_chunk_same_pairs(capi, oracle_mod, pred):
-    """The build-major refine with each block on consecutive runs of pairs
-    (refine_chunk) writes the same pairs at the same positions as with the
-    grid striding over them."""
-    from sedona_gpuspatial import datagen
-    inp = datagen.workload2(n_buildings=30000, n_zones=400)
-    out = []
-    for chunk in (0, 1, 7, 64):
-        j = capi.SpatialJoin()
-        j.set_option("candidate_order", 2)
-        j.set_option("refine_min_blocks", 6)
-        j.set_option("refine_split", 0)
-        j.set_option("refine_chunk", chunk)
-        j.build(inp.build)
-        out.append(j.probe(inp.probe, pred))
-    for o in out[1:]:
-        np.testing.assert_array_equal(o[0], out[0][0])
-        np.testing.assert_array_equal(o[1], out[0][1])
-    assert pairs(*out[0]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred)
-
-
 def test_unknown_option_is_an_error(capi):
     j = capi.SpatialJoin()
     with pytest.raises(capi.GpuSpatialError, match="unknown option"):
