@@ -95,6 +95,9 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *                       candidates over a build side that is not all points,
  *                       else 0; 2 by build row then probe Morton rank, 0 as
  *                       listed
+ *   "order_tiles"       -1 (default: auto, tiles of 524,288 candidates),
+ *                       0-16: build-major order within 2^n equal tiles of
+ *                       the probes' Morton-ordered candidate list
  *   "refine_min_blocks" 0 (default: auto, 6 in build-major candidate order,
  *                       else 4), 4 or 6: FP32 refine built for that many
  *                       resident 256-thread blocks per SM (fewer registers)

@@ -799,6 +799,9 @@ extern "C" int SpjJoinSetOption(SpjJoin* j, const char* key, int64_t value) {
     } else if (k == "candidate_order") {
       SPJ_CHECK(value == 0 || value == 2 || value == 3, "candidate_order must be 0, 2 or 3");
       c.candidate_order = (int)value;
+    } else if (k == "order_tiles") {
+      SPJ_CHECK(value >= -1 && value <= 16, "order_tiles must be -1 (auto) or in [0, 16]");
+      c.order_tiles = (int)value;
     } else if (k == "refine_split") {
       SPJ_CHECK(value >= 0 && value <= 3, "refine_split must be 0, 1, 2 or 3");
       c.refine_split = (int)value;

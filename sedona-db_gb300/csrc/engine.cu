@@ -222,7 +222,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
     // 16 bytes with nothing to re-read, distance candidates are cheap to
     // test, and small candidate sets do not repay the sort)
     cperm = build_major_order(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), m,
-                              probe_base, bg_.n, order, n, ws.psc, s);
+                              probe_base, bg_.n, order, n,
+                              order_tile_count(cfg_.order_tiles, m), ws.psc, s);
     if (cperm) {
       // Morton list (counts gather, scan, k_cand_perm), build-row gather and
       // one radix pass per 8 bits of the build row; else rank, keys and 4 passes

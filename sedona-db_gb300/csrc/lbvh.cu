@@ -523,18 +523,21 @@ __global__ void k_gather_u32(const uint32_t* __restrict__ src, const uint32_t* _
        i += (uint64_t)gridDim.x * blockDim.x)
     out[i] = src[idx[i]];
 }
+
 }  // namespace
 
 const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
-                                  uint32_t nprobe, ProbeScratch& sc, cudaStream_t s) {
+                                  uint32_t nprobe, uint64_t tiles, ProbeScratch& sc,
+                                  cudaStream_t s) {
   if (m < 2 || m >= 0xFFFFFFFFull) return nullptr;
   int bb = 1;
   while (bb < 32 && (nbuild - 1) >> bb) bb++;
   if (order && bb <= 24) {
     // the candidates listed in the probes' Morton order (k_cand_perm, coalesced),
     // then a stable sort of that list by build row alone: build row, then the
-    // probe's full Morton rank, with ceil(bits / 8) radix passes
+    // probe's full Morton rank, with ceil(bits / 8) radix passes; with tiles,
+    // each tile of the list is sorted in place by the same passes
     const uint32_t* mperm = candidate_order(order, nprobe, m, sc, s);
     if (mperm) {
       sc.ckeys.reserve((m + 1) * 4, s);
@@ -544,7 +547,7 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
                                                              sc.ckeys.as<uint32_t>());
       radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(),
                        sc.ckeys_alt.as<uint32_t>(), sc.cvals_alt.as<uint32_t>(), (int64_t)m,
-                       bb, sc.tmp, s);
+                       bb, sc.tmp, s, (int64_t)tiles);
       SPJ_CUDA(cudaGetLastError());
       return sc.cperm.as<uint32_t>();
     }

@@ -173,9 +173,14 @@ const uint32_t* candidate_order_into(const uint32_t* order, const uint32_t* coun
 // candidates are first listed in the probes' Morton order and that list is
 // sorted stably by build row (full rank resolution, one radix pass per 8
 // build-row bits); without one, by a 32-bit key of build row and row id.
+// tiles > 1 (with an order): the Morton list is cut into that many tiles of
+// about equal length (whole radix-sort tiles of 2048 items) and the
+// build-row order holds within each tile, so the refine reads one tile's
+// probe rows at a time.
 const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
-                                  uint32_t nprobe, ProbeScratch& sc, cudaStream_t s);
+                                  uint32_t nprobe, uint64_t tiles, ProbeScratch& sc,
+                                  cudaStream_t s);
 
 // Sorts caller-made candidate keys: sc.ckeys holds m keys and sc.cperm the
 // candidate indices 0..m-1 (both reserved by reserve_candidate_keys); the

@@ -125,8 +125,20 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 
+// Place of (digit d, tile b) in the histogram table.  The tiles form
+// segments of seg_tiles consecutive tiles (the last may be shorter); the
+// table is segment-major, then digit-major, so its scan gives every item a
+// place inside its own segment's range and a pass sorts each segment alone.
+// seg_tiles = ntiles: one segment, the plain digit-major table.
+__device__ __forceinline__ int64_t hist_slot(uint32_t d, int64_t b, int64_t ntiles,
+                                             int64_t seg_tiles) {
+  const int64_t b0 = b / seg_tiles * seg_tiles;
+  const int64_t nb = min(seg_tiles, ntiles - b0);
+  return b0 * 256 + (int64_t)d * nb + (b - b0);
+}
+
 __global__ void k_digit_hist(const uint32_t* __restrict__ keys, int64_t n, int shift,
-                             uint32_t* __restrict__ hist, int64_t ntiles) {
+                             uint32_t* __restrict__ hist, int64_t ntiles, int64_t seg_tiles) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -137,21 +149,22 @@ __global__ void k_digit_hist(const uint32_t* __restrict__ keys, int64_t n, int s
     if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
   }
   __syncthreads();
-  // digit-major layout: offset of (digit, tile) after the scan
-  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+  hist[hist_slot(threadIdx.x, blockIdx.x, ntiles, seg_tiles)] = h[threadIdx.x];
 }
 
 // One 8-bit LSD pass over a tile of kSortTile items: stable local ranking by
 // digit (warp w ranks its 256 items in 8 rounds of 32 with __match_any_sync
 // and per-warp digit counters; a scan over warps and digits gives each item
 // its place in the tile's digit-sorted order), a reorder in shared memory,
-// and a write of each digit run to its global offset (digit-major scan of the
-// tile histograms).  Pads (past n) carry key 0xFFFFFFFF, so they rank last in
-// digit 255 and land past the tile's valid items, which are all written.
+// and a write of each digit run to its global offset (scan of the tile
+// histograms, hist_slot).  Pads (past n) carry key 0xFFFFFFFF, so they rank
+// last in digit 255 and land past the tile's valid items, which are all
+// written.
 __global__ void __launch_bounds__(kSortThreads)
     k_digit_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                     int64_t n, int shift, const uint32_t* __restrict__ offs, int64_t ntiles,
-                    uint32_t* __restrict__ okeys, uint32_t* __restrict__ ovals) {
+                    int64_t seg_tiles, uint32_t* __restrict__ okeys,
+                    uint32_t* __restrict__ ovals) {
   constexpr int kWarps = kSortThreads / 32;
   __shared__ uint32_t sk[kSortTile];
   __shared__ uint32_t sv[kSortTile];
@@ -197,7 +210,7 @@ __global__ void __launch_bounds__(kSortThreads)
     }
     uint32_t total;
     doff[d] = block_exclusive_scan_256<uint32_t>(run, scan_sm, &total);
-    gbase[d] = offs[(int64_t)d * ntiles + blockIdx.x];
+    gbase[d] = offs[hist_slot(d, blockIdx.x, ntiles, seg_tiles)];
   }
   __syncthreads();
 #pragma unroll
@@ -255,10 +268,12 @@ size_t radix_sort_tmp_bytes(int64_t n) {
 }
 
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
-                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s) {
+                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s, int64_t segments) {
   if (n <= 1) return;
   SPJ_CHECK(n < (int64_t)0xFFFFFFFF, "radix sort: too many keys");
   const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
+  const int64_t seg_tiles =
+      segments > 1 ? (ntiles + segments - 1) / segments : ntiles;
   const int64_t nh = 256 * ntiles;
   // histogram table, its scan, and the scan's tile sums, all in tmp (no
   // allocation when tmp already holds radix_sort_tmp_bytes(n): graph capture)
@@ -269,10 +284,11 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32
   uint32_t *ik = keys, *iv = vals, *ok = alt_keys, *ov = alt_vals;
   int passes = 0;
   for (int shift = 0; shift < key_bits; shift += 8) {
-    k_digit_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, n, shift, hist, ntiles);
+    k_digit_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, n, shift, hist, ntiles,
+                                                           seg_tiles);
     scan_into_impl<uint32_t, uint32_t>(hist, offs, nh, sums, s);
-    k_digit_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, iv, n, shift, offs, ntiles, ok,
-                                                              ov);
+    k_digit_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, iv, n, shift, offs, ntiles,
+                                                              seg_tiles, ok, ov);
     SPJ_CUDA(cudaGetLastError());
     std::swap(ik, ok);
     std::swap(iv, ov);

@@ -18,8 +18,12 @@ void scan_u32_u64_into(const uint32_t* in, uint64_t* out, int64_t n, uint64_t* t
 
 // Stable LSD sort of (keys, vals) by key bits [0, key_bits).  keys/vals are
 // replaced by the sorted sequences; alt_keys/alt_vals are scratch of size n.
+// segments > 1: the sequence is cut into that many consecutive segments of
+// whole 2048-item sort tiles (ceil(tiles / segments) tiles each, the last
+// shorter) and each segment is sorted in place, with the same passes.
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
-                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s);
+                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s,
+                      int64_t segments = 0);
 // Bytes of tmp that radix_sort_pairs uses for n keys (reserve them before a
 // stream capture so that the sort allocates nothing inside it).
 size_t radix_sort_tmp_bytes(int64_t n);

@@ -250,6 +250,26 @@ def test_probe_order_keeps_pairs_and_layout(capi, oracle_mod, shape):
     assert pairs(*out[variants[0]]) == oracle_pairs(oracle_mod, inp.build, inp.probe, pred, d)
 
 
+@pytest.mark.parametrize("tiles", [1, 3, 6, 10])
+def test_order_tiles_same_pairs(capi, oracle_mod, tiles):
+    """Build-major order within tiles of the Morton-ordered candidate list
+    (each tile sorted in place by the segmented radix sort) refines a
+    permutation of the candidates: the same pairs at the same positions as
+    the candidates taken as listed."""
+    from sedona_gpuspatial import datagen
+    inp = datagen.workload2(n_buildings=30000, n_zones=400)
+    out = {}
+    for order, t in [(0, 0), (2, tiles)]:
+        j = capi.SpatialJoin(probe_order=1)
+        j.set_option("candidate_order", order)
+        j.set_option("order_tiles", t)
+        j.build(inp.build)
+        out[t] = j.probe(inp.probe, "intersects")
+    np.testing.assert_array_equal(out[tiles][0], out[0][0])
+    np.testing.assert_array_equal(out[tiles][1], out[0][1])
+    assert pairs(*out[0]) == oracle_pairs(oracle_mod, inp.build, inp.probe, "intersects", 0.0)
+
+
 def test_unknown_option_is_an_error(capi):
     j = capi.SpatialJoin()
     with pytest.raises(capi.GpuSpatialError, match="unknown option"):
