@@ -29,7 +29,9 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <exception>
 #include <memory>
 #include <thread>
 
@@ -163,15 +165,21 @@ __device__ __forceinline__ void win_stage(Win& w, uint32_t pos) {
   const uintptr_t a0 = a & ~uintptr_t(15);
   const uintptr_t e = (reinterpret_cast<uintptr_t>(w.base) + w.n + 15) & ~uintptr_t(15);
   const uint32_t bytes = e - a0 < w.cap ? (uint32_t)(e - a0) : w.cap;
+  // asynchronous 16-byte copies: every lane's loads are in flight at once
+  // (plain loads and stores through generic pointers would wait for each
+  // load before the next, as the two may alias), then one wait
   const uint4* s = reinterpret_cast<const uint4*>(a0);
-  uint4* d = reinterpret_cast<uint4*>(w.buf);
-  for (uint32_t i = lane; i < (bytes >> 4); i += 32) d[i] = s[i];
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(w.buf);
+  for (uint32_t i = lane; i < (bytes >> 4); i += 32)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + i * 16), "l"(s + i)
+                 : "memory");
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncwarp();
   w.p0 = (int32_t)pos - (int32_t)(a - a0);
   w.hi = w.p0 + (int32_t)bytes;
 }
 
-// positions [pos, pos + k) staged (k <= 16)
+// positions [pos, pos + k) staged (k <= cap - 16, and pos + k <= n)
 __device__ __forceinline__ void win_need(Win& w, uint32_t pos, uint32_t k) {
   if ((int32_t)pos < w.p0 || (int32_t)(pos + k) > w.hi) win_stage(w, pos);
 }
@@ -186,7 +194,7 @@ __device__ __forceinline__ uint32_t win_u32(const Win& w, uint32_t pos) {
 }
 
 constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
-constexpr uint32_t kFragWin = 2048;        // per warp, k_snappy_frags (headers only)
+constexpr uint32_t kFragWin = 2048;        // per warp, k_snappy_frags (headers, literals)
 constexpr uint32_t kWalkWin = 8192;        // per warp, PLAIN walks
 enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
 
@@ -231,8 +239,9 @@ __device__ __forceinline__ bool snappy_header(Win& w, uint32_t ip, uint32_t& len
 }
 
 // Warp per 64 KiB output block of a block-independent page: element
-// headers through a small shared-memory window, literal bytes copied from
-// the input, copies from the block's own output, all by the 32 lanes.  A copy
+// headers and literal bytes through a shared-memory window of the input
+// (restaged a window at a time, so an element does not wait on a global
+// load), copies from the block's own output, all by the 32 lanes.  A copy
 // that reaches before its block sends the page to k_snappy_pages.  Work item
 // (page, block 0) also copies a v2 page's level bytes.
 __global__ void __launch_bounds__(128) k_snappy_frags(
@@ -270,8 +279,15 @@ __global__ void __launch_bounds__(128) k_snappy_frags(
         break;
       }
       if (off == 0) {
-        const uint8_t* s = in + ip + hdr;
-        for (uint32_t i = lane; i < len; i += 32) out[op + i] = s[i];
+        // in pieces that fit the window (snappy_header checked that the
+        // literal lies inside the input)
+        for (uint32_t done = 0; done < len;) {
+          const uint32_t piece = min(len - done, kFragWin - 16);
+          win_need(w, ip + hdr + done, piece);
+          const uint8_t* s = w.buf + (ip + hdr + done - w.p0);
+          for (uint32_t i = lane; i < piece; i += 32) out[op + done + i] = s[i];
+          done += piece;
+        }
       } else {
         if (off > op) {  // reaches into an earlier block (or before the stream)
           local = false;
@@ -495,8 +511,10 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
         Win w;
         const uint32_t avail32 = (uint32_t)avail;
         win_init(w, vp, avail32, smem + (threadIdx.x >> 5) * (kWalkWin + 16), kWalkWin);
+        // lane j keeps the span of value k0 + j of each group of 32 and the
+        // warp stores a group at once (no per-value divergent store)
         bool good = true;
-        uint32_t q = 0;
+        uint32_t q = 0, my_q = 0, my_l = 0;
         for (uint32_t k = 0; k < m; k++) {
           if (avail32 - q < 4) {
             good = false;
@@ -508,9 +526,15 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
             good = false;
             break;
           }
-          if ((k & 31) == (uint32_t)lane) {
-            tptr[k] = reinterpret_cast<uint64_t>(vp + q + 4);
-            tlen[k] = l;
+          const bool mine = (k & 31) == (uint32_t)lane;
+          my_q = mine ? q + 4 : my_q;
+          my_l = mine ? l : my_l;
+          if ((k & 31) == 31 || k + 1 == m) {
+            const uint32_t k0 = k & ~31u;
+            if (k0 + lane <= k) {
+              tptr[k0 + lane] = reinterpret_cast<uint64_t>(vp + my_q);
+              tlen[k0 + lane] = my_l;
+            }
           }
           q += 4 + l;
         }
@@ -757,6 +781,42 @@ struct SpjParquet {
       n -= (uint64_t)r;
     }
   }
+  // The byte ranges (file offset, length, destination) in 8 MiB pieces on
+  // up to 16 host threads: one thread's copy out of the page cache runs far
+  // below the memory bandwidth of the host.
+  struct ReadPiece {
+    uint64_t off, len;
+    uint8_t* out;
+  };
+  void read_parallel(const std::vector<ReadPiece>& ranges) const {
+    constexpr uint64_t kPiece = 8ull << 20;
+    std::vector<ReadPiece> pieces;
+    for (const ReadPiece& r : ranges)
+      for (uint64_t d = 0; d < r.len; d += kPiece)
+        pieces.push_back({r.off + d, std::min(kPiece, r.len - d), r.out + d});
+    const size_t nt = std::min<size_t>(
+        {16, std::max(1u, std::thread::hardware_concurrency()), pieces.size()});
+    if (nt <= 1) {
+      for (const ReadPiece& q : pieces) read_at(q.off, q.len, q.out);
+      return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::exception_ptr> err(nt);
+    auto run = [&](size_t t) {
+      try {
+        for (size_t i = next++; i < pieces.size(); i = next++)
+          read_at(pieces[i].off, pieces[i].len, pieces[i].out);
+      } catch (...) {
+        err[t] = std::current_exception();
+      }
+    };
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; t++) th.emplace_back(run, t);
+    run(0);
+    for (auto& t : th) t.join();
+    for (auto& e : err)
+      if (e) std::rethrow_exception(e);
+  }
 };
 
 namespace {
@@ -916,7 +976,11 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
       p->stage_h_cap = total + 16;
     }
     uint8_t* hb = p->stage_h.as<uint8_t>();
-    for (auto& r : ranges) p->read_at(r.off, r.len, hb + r.at);
+    {
+      std::vector<SpjParquet::ReadPiece> rd;
+      for (auto& r : ranges) rd.push_back({r.off, r.len, hb + r.at});
+      p->read_parallel(rd);
+    }
     p->file_bytes = total;
 
     // page table
