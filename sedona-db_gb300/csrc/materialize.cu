@@ -9,8 +9,8 @@
 //
 // All HBM-bound: a gathered fixed-width value reads its width once and writes
 // it once (the index 4 B); a binary value reads and writes its bytes once,
-// with a length pass, a scan and a copy pass (warp per value above 64 bytes,
-// so long WKB values move as coalesced 4-byte words).
+// with a length pass, a scan and a copy pass (8 lanes per value, the
+// destination written as whole 4-byte words whatever the alignments).
 #include <errno.h>
 
 #include <string>
@@ -98,37 +98,37 @@ __global__ void k_bin_lengths(const void* __restrict__ off, const uint32_t* __re
   }
 }
 
-// warp per value: bytes moved by 32 lanes (whole 4-byte words when source
-// and destination share their alignment, else byte by byte)
+// A warp takes 32 values: lane k reads value k's index, source range and
+// output position (one memory latency for all 32), then lane groups of 8
+// copy 4 values at a time (group_copy: whole destination words, any
+// alignment).
 template <bool kOff64>
 __global__ void k_bin_copy(const void* __restrict__ off, const uint8_t* __restrict__ data,
                            const uint32_t* __restrict__ idx, uint64_t n, uint64_t nsrc,
                            const uint64_t* __restrict__ pos, uint8_t* __restrict__ out,
                            uint64_t cap) {
-  const int lane = threadIdx.x & 31;
+  constexpr int G = 8;
+  const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
-    const uint32_t j = idx[i];
-    if (j == SPJ_NULL_INDEX || j >= nsrc) continue;
-    uint64_t s, e;
-    bin_range<kOff64>(off, j, s, e);
-    const uint64_t d = pos[i];
-    const uint64_t l = e > s ? e - s : 0;
-    if (d + l > cap) continue;  // bounded by the output buffer
-    const uintptr_t sa = reinterpret_cast<uintptr_t>(data + s);
-    const uintptr_t da = reinterpret_cast<uintptr_t>(out + d);
-    if (((sa ^ da) & 3) == 0) {
-      // head bytes up to a word boundary, whole words, tail bytes
-      const uint64_t head = min(l, (uint64_t)((4 - (sa & 3)) & 3));
-      if ((uint64_t)lane < head) out[d + lane] = data[s + lane];
-      const uint64_t words = (l - head) / 4;
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(data + s + head);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(out + d + head);
-      for (uint64_t w = lane; w < words; w += 32) dst[w] = src[w];
-      const uint64_t t0 = head + words * 4;
-      if (t0 + lane < l) out[d + t0 + lane] = data[s + t0 + lane];
-    } else {
-      for (uint64_t b = lane; b < l; b += 32) out[d + b] = data[s + b];
+  for (uint64_t i0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; i0 < n;
+       i0 += nwarps * 32) {
+    const uint64_t i = i0 + lane;
+    uint64_t s = 0, d = 0, l = 0;
+    if (i < n) {
+      const uint32_t j = idx[i];
+      if (j != SPJ_NULL_INDEX && j < nsrc) {
+        uint64_t e;
+        bin_range<kOff64>(off, j, s, e);
+        d = pos[i];
+        l = e > s ? e - s : 0;
+        if (d + l > cap) l = 0;  // bounded by the output buffer
+      }
+    }
+    for (int v = 0; v < 32; v += 32 / G) {
+      const uint64_t vs = __shfl_sync(0xffffffffu, s, v + grp);
+      const uint64_t vd = __shfl_sync(0xffffffffu, d, v + grp);
+      const uint64_t vl = __shfl_sync(0xffffffffu, l, v + grp);
+      if (vl) group_copy<G>(data + vs, out + vd, vl, gl);
     }
   }
 }

@@ -19,7 +19,8 @@
 //                  word, others by a walk) or dictionary indices -> per-row
 //                  (address, length)
 //   scan           lengths -> int64 offsets
-//   k_copy_values  warp per row: value bytes -> the output data buffer
+//   k_copy_values  8 lanes per row, 4 rows at a time per warp: value bytes ->
+//                  the output data buffer
 //   k_pack_valid   validity bytes -> an Arrow bitmap (only with nulls)
 // Every read of page bytes is bounded by its page; a malformed page sets a
 // status word (first error: code, page) that the host turns into a message.
@@ -595,31 +596,31 @@ __global__ void k_data_pages(const PageInfo* __restrict__ pages, uint32_t np,
   }
 }
 
-// warp per row: the value's bytes (4-byte words when source and destination
-// share their alignment)
+// A warp takes 32 rows: lane k reads row k's span and output position, then
+// lane groups of 8 copy 4 values at a time (group_copy: whole destination
+// words, any alignment).
 __global__ void k_copy_values(const uint64_t* __restrict__ vptr,
                               const uint32_t* __restrict__ vlen,
                               const uint64_t* __restrict__ pos, uint64_t n,
                               uint8_t* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
+  constexpr int G = 8;
+  const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nwarps) {
-    const uint32_t l = vlen[r];
-    if (l == 0) continue;
-    const uint8_t* s = reinterpret_cast<const uint8_t*>(vptr[r]);
-    uint8_t* d = out + pos[r];
-    const uintptr_t sa = reinterpret_cast<uintptr_t>(s), da = reinterpret_cast<uintptr_t>(d);
-    if (((sa ^ da) & 3) == 0) {
-      const uint32_t head = min(l, (uint32_t)((4 - (sa & 3)) & 3));
-      if ((uint32_t)lane < head) d[lane] = s[lane];
-      const uint32_t words = (l - head) / 4;
-      const uint32_t* sw = reinterpret_cast<const uint32_t*>(s + head);
-      uint32_t* dw = reinterpret_cast<uint32_t*>(d + head);
-      for (uint32_t w = lane; w < words; w += 32) dw[w] = sw[w];
-      const uint32_t t0 = head + words * 4;
-      if (t0 + lane < l) d[t0 + lane] = s[t0 + lane];
-    } else {
-      for (uint32_t b = lane; b < l; b += 32) d[b] = s[b];
+  for (uint64_t r0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; r0 < n;
+       r0 += nwarps * 32) {
+    const uint64_t r = r0 + lane;
+    uint64_t sp = 0, d = 0;
+    uint32_t l = 0;
+    if (r < n) {
+      l = vlen[r];
+      sp = vptr[r];
+      d = pos[r];
+    }
+    for (int v = 0; v < 32; v += 32 / G) {
+      const uint64_t vs = __shfl_sync(0xffffffffu, sp, v + grp);
+      const uint64_t vd = __shfl_sync(0xffffffffu, d, v + grp);
+      const uint32_t vl = __shfl_sync(0xffffffffu, l, v + grp);
+      if (vl) group_copy<G>(reinterpret_cast<const uint8_t*>(vs), out + vd, vl, gl);
     }
   }
 }

@@ -59,4 +59,43 @@ __device__ __forceinline__ T block_exclusive_scan_256(T v, T* smem, T* total) {
   return r;
 }
 
+// Copies l bytes from src to dst with the G lanes (G >= 4) of a lane group,
+// gl = the lane's place in the group.  The destination is written as whole
+// 4-byte words between a head and a tail of under 4 bytes each; each word is
+// assembled from the two aligned source words it straddles (a funnel shift),
+// whatever the two alignments.  A lane issues up to 8 word loads before its
+// stores, so a value of up to G * 32 bytes costs one memory latency.  (An
+// aligned source word that holds a byte of the value lies in the value's
+// allocation.)
+template <int G>
+__device__ __forceinline__ void group_copy(const uint8_t* __restrict__ src,
+                                           uint8_t* __restrict__ dst, uint64_t l, int gl) {
+  static_assert(G >= 4, "head and tail bytes take one lane each");
+  const uintptr_t da = reinterpret_cast<uintptr_t>(dst);
+  const uint64_t head = min(l, (uint64_t)((4 - (da & 3)) & 3));
+  if ((uint64_t)gl < head) dst[gl] = src[gl];
+  const uint64_t words = (l - head) >> 2;
+  const uintptr_t sa = reinterpret_cast<uintptr_t>(src + head);
+  const uint32_t sh = (uint32_t)(sa & 3) * 8;
+  const uint32_t* sw = reinterpret_cast<const uint32_t*>(sa & ~uintptr_t(3));
+  uint32_t* dw = reinterpret_cast<uint32_t*>(dst + head);
+  constexpr int kU = 8;
+  for (uint64_t w0 = 0; w0 < words; w0 += (uint64_t)G * kU) {
+    uint32_t lo[kU], hi[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const uint64_t w = w0 + (uint64_t)(u * G + gl);
+      lo[u] = w < words ? sw[w] : 0u;
+      hi[u] = w < words && sh ? sw[w + 1] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const uint64_t w = w0 + (uint64_t)(u * G + gl);
+      if (w < words) dw[w] = __funnelshift_r(lo[u], hi[u], sh);
+    }
+  }
+  const uint64_t t0 = head + words * 4;
+  if (t0 + gl < l) dst[t0 + gl] = src[t0 + gl];
+}
+
 }  // namespace spj
