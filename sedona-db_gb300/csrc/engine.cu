@@ -28,7 +28,6 @@ Workspace::~Workspace() {
   cand_build.release();
   cand_probe.release();
   flags.release();
-  pos.release();
   out_build.release();
   out_probe.release();
   scan_tmp.release();
@@ -259,11 +258,14 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   launches += rq ? 2 : 1;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[3], s));
 
-  ws.pos.reserve((m + 1) * 8, s);
-  scan_u8_u64(ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), (int64_t)m, ws.scan_tmp, s);
+  // compaction: tile counts and their scan, then the survivors tile by tile
+  ws.scan_tmp.reserve(compact_sums_bytes((int64_t)m), s);
+  uint64_t* sums = ws.scan_tmp.as<uint64_t>();
+  compact_count(ws.flags.as<uint8_t>(), (int64_t)m, sums, s);
   uint64_t total = 0;
   DeviceStatus hst;
-  SPJ_CUDA(cudaMemcpyAsync(&total, ws.pos.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(&total, sums + compact_tiles((int64_t)m), 8, cudaMemcpyDeviceToHost,
+                           s));
   SPJ_CUDA(cudaMemcpyAsync(&hst, ws.status.get(), sizeof hst, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
   if (hst.first_bad != ~0ull) {
@@ -271,10 +273,10 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   }
   ws.out_build.reserve((total + 1) * 4, s);
   ws.out_probe.reserve((total + 1) * 4, s);
-  compact_pairs(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(), ws.flags.as<uint8_t>(),
-                ws.pos.as<uint64_t>(), m, ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(),
-                s);
-  launches += 4;
+  compact_pairs_tiles(ws.cand_build.as<uint32_t>(), ws.cand_probe.as<uint32_t>(),
+                      ws.flags.as<uint8_t>(), (int64_t)m, sums, ws.out_build.as<uint32_t>(),
+                      ws.out_probe.as<uint32_t>(), total, s);
+  launches += 3;
   if (prof) SPJ_CUDA(cudaEventRecord(ws.ev[4], s));
   SPJ_CUDA(cudaStreamSynchronize(s));
   {
@@ -314,19 +316,21 @@ uint64_t JoinEngine::refine_pairs(Workspace& ws, const GeomsView& pv, const uint
     refine_relation(bv, pv, cb, cp, m, 0, predicate, cfg_.refine_form, ws.flags.as<uint8_t>(),
                     ws.status.as<DeviceStatus>(), s, nullptr, nullptr,
                     refine_blocks(cfg_.refine_min_blocks, false));
-  ws.pos.reserve((m + 1) * 8, s);
-  scan_u8_u64(ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), (int64_t)m, ws.scan_tmp, s);
+  ws.scan_tmp.reserve(compact_sums_bytes((int64_t)m), s);
+  uint64_t* sums = ws.scan_tmp.as<uint64_t>();
+  compact_count(ws.flags.as<uint8_t>(), (int64_t)m, sums, s);
   uint64_t total = 0;
   DeviceStatus hst;
-  SPJ_CUDA(cudaMemcpyAsync(&total, ws.pos.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+  SPJ_CUDA(cudaMemcpyAsync(&total, sums + compact_tiles((int64_t)m), 8, cudaMemcpyDeviceToHost,
+                           s));
   SPJ_CUDA(cudaMemcpyAsync(&hst, ws.status.get(), sizeof hst, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaStreamSynchronize(s));
   if (hst.first_bad != ~0ull)
     throw Error(std::string("refine: ") + status_message((uint32_t)(hst.first_bad >> 40)));
   ws.out_build.reserve((total + 1) * 4, s);
   ws.out_probe.reserve((total + 1) * 4, s);
-  compact_pairs(cb, cp, ws.flags.as<uint8_t>(), ws.pos.as<uint64_t>(), m,
-                ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), s);
+  compact_pairs_tiles(cb, cp, ws.flags.as<uint8_t>(), (int64_t)m, sums,
+                      ws.out_build.as<uint32_t>(), ws.out_probe.as<uint32_t>(), total, s);
   SPJ_CUDA(cudaStreamSynchronize(s));
   {
     std::lock_guard<std::mutex> lk(stats_mu_);

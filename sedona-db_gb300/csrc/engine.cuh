@@ -117,7 +117,7 @@ struct Workspace {
   DeviceGeoms probe;
   DecodeScratch dsc;
   ProbeScratch psc;
-  DevBuf boxes_tmp, cand_build, cand_probe, flags, pos, out_build, out_probe, scan_tmp, status;
+  DevBuf boxes_tmp, cand_build, cand_probe, flags, out_build, out_probe, scan_tmp, status;
   DevBuf slots;   // fused ST_DWithin result slots
   DevBuf arena;   // fused ST_DWithin overflow arena: cursor, heads, chunks
   DevBuf rqueue;  // pairs left open by the refine's cheap pass, then its count

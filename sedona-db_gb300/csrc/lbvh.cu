@@ -547,7 +547,7 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
                                                              sc.ckeys.as<uint32_t>());
       radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(),
                        sc.ckeys_alt.as<uint32_t>(), sc.cvals_alt.as<uint32_t>(), (int64_t)m,
-                       bb, sc.tmp, s, (int64_t)tiles);
+                       bb, sc.tmp, s, (int64_t)tiles, false);
       SPJ_CUDA(cudaGetLastError());
       return sc.cperm.as<uint32_t>();
     }

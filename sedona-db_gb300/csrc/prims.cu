@@ -88,6 +88,51 @@ __global__ void k_tile_scan(const Tin* __restrict__ in, int64_t n, const Tout* _
   }
 }
 
+// Stream compaction of candidate pairs by 0/1 flags, per 4096-flag tile:
+// the tile's flags (16 per thread, one 16-byte load when aligned), a block
+// scan of their counts, the survivors gathered in shared memory, then
+// written as one coalesced run at the tile's offset (sums: exclusive tile
+// offsets).  No per-element position array is written or read.
+__global__ void __launch_bounds__(kScanThreads)
+    k_compact_tile(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
+                   const uint8_t* __restrict__ flags, int64_t n,
+                   const uint64_t* __restrict__ sums, uint32_t* __restrict__ ob,
+                   uint32_t* __restrict__ op, uint64_t out_cap) {
+  __shared__ uint32_t sb[kScanTile], sp[kScanTile];
+  __shared__ uint32_t sm[9];
+  const int64_t mybase = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t f = 0;  // bit j: flag of item mybase + j
+  if (mybase + kScanItems <= n && (reinterpret_cast<uintptr_t>(flags + mybase) & 15) == 0) {
+    const uint4 v = *reinterpret_cast<const uint4*>(flags + mybase);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++)
+      f |= (uint32_t)(((w[j >> 2] >> (8 * (j & 3))) & 0xffu) != 0) << j;
+  } else {
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++)
+      if (mybase + j < n && flags[mybase + j]) f |= 1u << j;
+  }
+  uint32_t total;
+  uint32_t lo = block_exclusive_scan_256<uint32_t>((uint32_t)__popc(f), sm, &total);
+#pragma unroll
+  for (int j = 0; j < kScanItems; j++)
+    if ((f >> j) & 1u) {
+      sb[lo] = cb[mybase + j];
+      sp[lo] = cp[mybase + j];
+      lo++;
+    }
+  __syncthreads();
+  const uint64_t tb = sums[blockIdx.x];
+  for (uint32_t k = threadIdx.x; k < total; k += kScanThreads) {
+    const uint64_t o = tb + k;
+    if (o < out_cap) {  // bounded by the output capacity
+      ob[o] = sb[k];
+      op[o] = sp[k];
+    }
+  }
+}
+
 // Scan with caller-owned tile sums ((tiles + 1) entries of Tout).
 template <class Tin, class Tout>
 void scan_into_impl(const Tin* in, Tout* out, int64_t n, Tout* sums, cudaStream_t s) {
@@ -225,7 +270,7 @@ __global__ void __launch_bounds__(kSortThreads)
     const uint32_t key = sk[li];
     const uint32_t d = (key >> shift) & 0xFFu;
     const uint64_t dst = (uint64_t)gbase[d] + (uint32_t)(li - doff[d]);
-    okeys[dst] = key;
+    if (okeys) okeys[dst] = key;  // (null: the last pass of a sort whose keys are not kept)
     ovals[dst] = sv[li];
   }
 }
@@ -260,6 +305,31 @@ void scan_u32_u32(const uint32_t* in, uint32_t* out, int64_t n, DevBuf& tmp, cud
   scan_impl<uint32_t, uint32_t>(in, out, n, tmp, s);
 }
 
+size_t compact_sums_bytes(int64_t n) {
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  return (size_t)((nt < 1 ? 1 : nt) + 1) * sizeof(uint64_t);
+}
+
+void compact_count(const uint8_t* flags, int64_t n, uint64_t* sums, cudaStream_t s) {
+  if (n <= 0) {
+    SPJ_CUDA(cudaMemsetAsync(sums, 0, sizeof(uint64_t), s));
+    return;
+  }
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  k_tile_reduce<uint8_t, uint64_t><<<(unsigned)nt, kScanThreads, 0, s>>>(flags, n, sums);
+  k_scan_sums<uint64_t><<<1, 1024, 0, s>>>(sums, nt, sums + nt);
+  SPJ_CUDA(cudaGetLastError());
+}
+
+void compact_pairs_tiles(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags, int64_t n,
+                         const uint64_t* sums, uint32_t* ob, uint32_t* op, uint64_t out_cap,
+                         cudaStream_t s) {
+  if (n <= 0) return;
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  k_compact_tile<<<(unsigned)nt, kScanThreads, 0, s>>>(cb, cp, flags, n, sums, ob, op, out_cap);
+  SPJ_CUDA(cudaGetLastError());
+}
+
 size_t radix_sort_tmp_bytes(int64_t n) {
   const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
   const int64_t nh = 256 * (ntiles < 1 ? 1 : ntiles);
@@ -268,7 +338,8 @@ size_t radix_sort_tmp_bytes(int64_t n) {
 }
 
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
-                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s, int64_t segments) {
+                      int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s, int64_t segments,
+                      bool keys_out) {
   if (n <= 1) return;
   SPJ_CHECK(n < (int64_t)0xFFFFFFFF, "radix sort: too many keys");
   const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
@@ -284,18 +355,19 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32
   uint32_t *ik = keys, *iv = vals, *ok = alt_keys, *ov = alt_vals;
   int passes = 0;
   for (int shift = 0; shift < key_bits; shift += 8) {
+    const bool last = shift + 8 >= key_bits;
     k_digit_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, n, shift, hist, ntiles,
                                                            seg_tiles);
     scan_into_impl<uint32_t, uint32_t>(hist, offs, nh, sums, s);
-    k_digit_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ik, iv, n, shift, offs, ntiles,
-                                                              seg_tiles, ok, ov);
+    k_digit_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(
+        ik, iv, n, shift, offs, ntiles, seg_tiles, last && !keys_out ? nullptr : ok, ov);
     SPJ_CUDA(cudaGetLastError());
     std::swap(ik, ok);
     std::swap(iv, ov);
     passes++;
   }
   if (passes & 1) {
-    SPJ_CUDA(cudaMemcpyAsync(keys, ik, n * 4, cudaMemcpyDeviceToDevice, s));
+    if (keys_out) SPJ_CUDA(cudaMemcpyAsync(keys, ik, n * 4, cudaMemcpyDeviceToDevice, s));
     SPJ_CUDA(cudaMemcpyAsync(vals, iv, n * 4, cudaMemcpyDeviceToDevice, s));
   }
 }

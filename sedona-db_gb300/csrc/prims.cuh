@@ -16,14 +16,28 @@ size_t scan_tile_sums_bytes(int64_t n);
 void scan_u32_u64_into(const uint32_t* in, uint64_t* out, int64_t n, uint64_t* tile_sums,
                        cudaStream_t s);
 
+// Stream compaction of n candidate pairs (cb, cp) by 0/1 flags, in order,
+// without a per-element position array.  compact_count writes the exclusive
+// offsets of the 4096-flag tiles to sums (compact_sums_bytes(n) bytes) and the
+// survivor count to sums[tiles]; compact_pairs_tiles then writes the
+// survivors (at most out_cap of them) to ob / op.
+size_t compact_sums_bytes(int64_t n);
+void compact_count(const uint8_t* flags, int64_t n, uint64_t* sums, cudaStream_t s);
+inline int64_t compact_tiles(int64_t n) { return n > 0 ? (n + 4095) / 4096 : 0; }
+void compact_pairs_tiles(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags, int64_t n,
+                         const uint64_t* sums, uint32_t* ob, uint32_t* op, uint64_t out_cap,
+                         cudaStream_t s);
+
 // Stable LSD sort of (keys, vals) by key bits [0, key_bits).  keys/vals are
 // replaced by the sorted sequences; alt_keys/alt_vals are scratch of size n.
 // segments > 1: the sequence is cut into that many consecutive segments of
 // whole 2048-item sort tiles (ceil(tiles / segments) tiles each, the last
 // shorter) and each segment is sorted in place, with the same passes.
+// keys_out false: only vals are sorted on return (the last pass writes no
+// keys, and keys is left undefined).
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
                       int64_t n, int key_bits, DevBuf& tmp, cudaStream_t s,
-                      int64_t segments = 0);
+                      int64_t segments = 0, bool keys_out = true);
 // Bytes of tmp that radix_sort_pairs uses for n keys (reserve them before a
 // stream capture so that the sort allocates nothing inside it).
 size_t radix_sort_tmp_bytes(int64_t n);
