@@ -224,11 +224,11 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
                               probe_base, bg_.n, order, n,
                               order_tile_count(cfg_.order_tiles, m), ws.psc, s);
     if (cperm) {
-      // Morton list (counts gather, scan, k_cand_perm), build-row gather and
+      // Morton list with its build rows (counts gather, scan, k_cand_perm) and
       // one radix pass per 8 bits of the build row; else rank, keys and 4 passes
       int bits = 1;
       while (bits < 32 && (bg_.n - 1) >> bits) bits++;
-      launches += order && bits <= 24 ? 6 + 5 * ((bits + 7) / 8) : 22;
+      launches += order && bits <= 24 ? 5 + 5 * ((bits + 7) / 8) : 22;
     }
     build_major = cperm != nullptr;
   }

@@ -400,13 +400,16 @@ __global__ void k_gather_counts(const uint32_t* __restrict__ order,
     out[j] = counts[order[j]];
 }
 
-// perm[opos[j] + c] = offs[order[j]] + c for c < counts[order[j]].  A warp
+// perm[opos[j] + c] = offs[order[j]] + c for c < counts[order[j]] (and, with
+// keys, keys[...] = cb[that candidate]).  A warp
 // takes 32 consecutive positions j, and its lanes write consecutive perm
 // entries (each finds its position by a binary search over the 32 run
 // starts), so the stores are coalesced.
 __global__ void k_cand_perm(const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
                             const uint64_t* __restrict__ offs, const uint64_t* __restrict__ opos,
-                            uint32_t n, uint64_t m, uint32_t* __restrict__ perm) {
+                            uint32_t n, uint64_t m, uint32_t* __restrict__ perm,
+                            const uint32_t* __restrict__ cb = nullptr,
+                            uint32_t* __restrict__ keys = nullptr) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n; w += nw) {
@@ -432,7 +435,10 @@ __global__ void k_cand_perm(const uint32_t* __restrict__ order, const uint32_t* 
       const uint64_t src = __shfl_sync(0xffffffffu, src0, L) + (e - sr);
       const uint32_t cl = __shfl_sync(0xffffffffu, c, L);
       const bool okl = __shfl_sync(0xffffffffu, ok ? 1 : 0, L) != 0;
-      if (e < e1 && okl && e - sr < cl && e < m && src < m) perm[e] = (uint32_t)src;
+      if (e < e1 && okl && e - sr < cl && e < m && src < m) {
+        perm[e] = (uint32_t)src;
+        if (keys) keys[e] = cb[src];  // the build row, gathered on the way
+      }
     }
   }
 }
@@ -470,7 +476,8 @@ const uint32_t* candidate_order_into(const uint32_t* order, const uint32_t* coun
 }
 
 const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
-                                ProbeScratch& sc, cudaStream_t s) {
+                                ProbeScratch& sc, cudaStream_t s, const uint32_t* cb,
+                                uint32_t* keys) {
   if (!order || nprobe == 0 || m == 0 || m >= 0xFFFFFFFFull) return nullptr;
   sc.ocount.reserve(((size_t)nprobe + 1) * 4, s);
   sc.opos.reserve(((size_t)nprobe + 1) * 8, s);
@@ -480,7 +487,8 @@ const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t
                                     sc.ocount.as<uint32_t>());
   scan_u32_u64(sc.ocount.as<uint32_t>(), sc.opos.as<uint64_t>(), nprobe, sc.tmp, s);
   k_cand_perm<<<g, 256, 0, s>>>(order, sc.counts.as<uint32_t>(), sc.offsets.as<uint64_t>(),
-                                sc.opos.as<uint64_t>(), nprobe, m, sc.cperm.as<uint32_t>());
+                                sc.opos.as<uint64_t>(), nprobe, m, sc.cperm.as<uint32_t>(), cb,
+                                keys);
   SPJ_CUDA(cudaGetLastError());
   return sc.cperm.as<uint32_t>();
 }
@@ -516,15 +524,6 @@ __global__ void k_cand_keys(const uint32_t* __restrict__ cb, const uint32_t* __r
 
 }  // namespace
 
-namespace {
-__global__ void k_gather_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
-                             uint64_t n, uint32_t* __restrict__ out) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x)
-    out[i] = src[idx[i]];
-}
-
-}  // namespace
 
 const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64_t m,
                                   uint32_t probe_base, uint32_t nbuild, const uint32_t* order,
@@ -538,13 +537,11 @@ const uint32_t* build_major_order(const uint32_t* cb, const uint32_t* cp, uint64
     // then a stable sort of that list by build row alone: build row, then the
     // probe's full Morton rank, with ceil(bits / 8) radix passes; with tiles,
     // each tile of the list is sorted in place by the same passes
-    const uint32_t* mperm = candidate_order(order, nprobe, m, sc, s);
+    sc.ckeys.reserve((m + 1) * 4, s);
+    const uint32_t* mperm = candidate_order(order, nprobe, m, sc, s, cb, sc.ckeys.as<uint32_t>());
     if (mperm) {
-      sc.ckeys.reserve((m + 1) * 4, s);
       sc.ckeys_alt.reserve((m + 1) * 4, s);
       sc.cvals_alt.reserve((m + 1) * 4, s);
-      k_gather_u32<<<grid_for((int64_t)m, 256), 256, 0, s>>>(cb, mperm, m,
-                                                             sc.ckeys.as<uint32_t>());
       radix_sort_pairs(sc.ckeys.as<uint32_t>(), sc.cperm.as<uint32_t>(),
                        sc.ckeys_alt.as<uint32_t>(), sc.cvals_alt.as<uint32_t>(), (int64_t)m,
                        bb, sc.tmp, s, (int64_t)tiles, false);

@@ -155,9 +155,11 @@ void fill_probe_ids(const uint64_t* offs, uint32_t n, uint32_t probe_base, uint3
 
 // After the two traversal passes (sc.counts / sc.offsets by probe row): the
 // m candidate indices listed probe by probe in `order` (sc.cperm), so that a
-// refine in that order takes spatially neighbouring probes together.
+// refine in that order takes spatially neighbouring probes together.  With
+// keys (m entries), keys[j] = cb[cperm[j]] is written in the same pass.
 const uint32_t* candidate_order(const uint32_t* order, uint32_t nprobe, uint64_t m,
-                                ProbeScratch& sc, cudaStream_t s);
+                                ProbeScratch& sc, cudaStream_t s, const uint32_t* cb = nullptr,
+                                uint32_t* keys = nullptr);
 // The same from caller-owned per-row counts / offsets, for a candidate
 // buffer of capacity mcap whose fill count lives on the device (graph
 // replays): cperm[0, m) is the permutation of the m candidates, its entries
