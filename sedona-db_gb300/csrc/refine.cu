@@ -73,21 +73,6 @@ __global__ void __launch_bounds__(256)
   flush_counters(st, esc, pairs);
 }
 
-__global__ void k_compact(const uint32_t* __restrict__ cb, const uint32_t* __restrict__ cp,
-                          const uint8_t* __restrict__ flags, const uint64_t* __restrict__ pos,
-                          uint64_t m, uint32_t* __restrict__ ob, uint32_t* __restrict__ op,
-                          uint64_t out_cap) {
-  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m;
-       k += (uint64_t)gridDim.x * blockDim.x) {
-    if (flags[k]) {
-      const uint64_t o = pos[k];
-      if (o >= out_cap) continue;  // bounded by the output capacity
-      ob[o] = cb[k];
-      op[o] = cp[k];
-    }
-  }
-}
-
 }  // namespace
 
 void refine_relation(const GeomsView& build, const GeomsView& probe, const uint32_t* cb,
@@ -129,13 +114,5 @@ void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32
   SPJ_CUDA(cudaGetLastError());
 }
 
-void compact_pairs(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags,
-                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s,
-                   uint64_t out_cap) {
-  if (m == 0) return;
-  k_compact<<<grid_for((int64_t)m, 256, kNumSMs * 16), 256, 0, s>>>(cb, cp, flags, pos, m, ob, op,
-                                                                     out_cap);
-  SPJ_CUDA(cudaGetLastError());
-}
 
 }  // namespace spj

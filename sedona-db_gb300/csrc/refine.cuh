@@ -54,10 +54,4 @@ void refine_dwithin(const GeomsView& build, const GeomsView& probe, const uint32
                     uint8_t* flags, DeviceStatus* st, cudaStream_t s,
                     const uint32_t* perm = nullptr, const double* d_row = nullptr);
 
-// Stream compaction of (cb, cp) by flags: positions from an exclusive scan
-// of the flags (pos has m+1 entries).  Order is preserved.
-void compact_pairs(const uint32_t* cb, const uint32_t* cp, const uint8_t* flags,
-                   const uint64_t* pos, uint64_t m, uint32_t* ob, uint32_t* op, cudaStream_t s,
-                   uint64_t out_cap = ~0ull);
-
 }  // namespace spj

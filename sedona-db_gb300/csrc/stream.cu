@@ -112,7 +112,7 @@ StreamJoin::~StreamJoin() {
   destroy_graph();
   cudaStreamSynchronize(s_);
   for (DevBuf* b : {&batches_, &chunks_, &ctrl_, &kind_, &pt_, &box_, &counts_, &offs_, &sums_,
-                    &cand_b_, &cand_p_, &flags_, &pos_, &sums2_, &out_b_, &out_p_})
+                    &cand_b_, &cand_p_, &flags_, &sums2_, &out_b_, &out_p_})
     b->release();
   psc_ = ProbeScratch();  // its buffers free on s_ too
   cudaStreamSynchronize(s_);
@@ -187,8 +187,7 @@ void StreamJoin::build_graph(int predicate) {
   cand_b_.reserve((ccap_ + 1) * 4, s_);
   cand_p_.reserve((ccap_ + 1) * 4, s_);
   flags_.reserve(ccap_ + 1, s_);
-  pos_.reserve((ccap_ + 1) * 8, s_);
-  sums2_.reserve(scan_tile_sums_bytes((int64_t)ccap_), s_);
+  sums2_.reserve(compact_sums_bytes((int64_t)ccap_), s_);
   out_b_.reserve((ocap_ + 1) * 4, s_);
   out_p_.reserve((ocap_ + 1) * 4, s_);
   const EngineConfig cfg = eng_.config();
@@ -243,13 +242,14 @@ void StreamJoin::build_graph(int predicate) {
   refine_relation(B, P, cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), ccap_, 0, predicate,
                   cfg.refine_form, flags_.as<uint8_t>(), st, s_, d_m, cperm,
                   refine_blocks(cfg.refine_min_blocks, false));
-  scan_u8_u64(flags_.as<uint8_t>(), pos_.as<uint64_t>(), (int64_t)ccap_, sums2_, s_);
-  compact_pairs(cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), flags_.as<uint8_t>(),
-                pos_.as<uint64_t>(), ccap_, out_b_.as<uint32_t>(), out_p_.as<uint32_t>(), s_,
-                ocap_);
+  // compaction per 4096-flag tile (the flags past m are clear)
+  compact_count(flags_.as<uint8_t>(), (int64_t)ccap_, sums2_.as<uint64_t>(), s_);
+  compact_pairs_tiles(cand_b_.as<uint32_t>(), cand_p_.as<uint32_t>(), flags_.as<uint8_t>(),
+                      (int64_t)ccap_, sums2_.as<uint64_t>(), out_b_.as<uint32_t>(),
+                      out_p_.as<uint32_t>(), ocap_, s_);
   SPJ_CUDA(cudaMemcpyAsync(h_tot_, d_m, 8, cudaMemcpyDeviceToHost, s_));
-  SPJ_CUDA(cudaMemcpyAsync(h_tot_ + 1, pos_.as<uint64_t>() + ccap_, 8, cudaMemcpyDeviceToHost,
-                           s_));
+  SPJ_CUDA(cudaMemcpyAsync(h_tot_ + 1, sums2_.as<uint64_t>() + compact_tiles((int64_t)ccap_), 8,
+                           cudaMemcpyDeviceToHost, s_));
   SPJ_CUDA(cudaMemcpyAsync(h_tot_ + 2, &st->first_bad, 8, cudaMemcpyDeviceToHost, s_));
   SPJ_CUDA(cudaMemcpyAsync(h_tot_ + 3, &st->counters[0], 8, cudaMemcpyDeviceToHost, s_));
   SPJ_CUDA(cudaStreamEndCapture(s_, &g));
@@ -257,9 +257,9 @@ void StreamJoin::build_graph(int predicate) {
   cudaGraphDestroy(g);
   SPJ_CUDA(e);
   graph_pred_ = predicate;
-  // memsets 2, decode 1, count 1, scan 3, scatter 1, refine 1, flag scan 3, compact 1;
+  // memsets 2, decode 1, count 1, scan 3, scatter 1, refine 1, flag counts 2, compact 1;
   // ordered: keys 1 + 4 radix passes of 5, candidate order 5, flags memset 1
-  stats_.launches_per_replay = 13 + (cperm ? 27 : (order ? 21 : 0));
+  stats_.launches_per_replay = 12 + (cperm ? 27 : (order ? 21 : 0));
 }
 
 uint64_t StreamJoin::run(int predicate, const uint32_t** d_build, const uint32_t** d_probe) {

@@ -70,7 +70,7 @@ class StreamJoin {
   StreamParams params_;
   DevBuf batches_, chunks_, ctrl_;
   DevBuf kind_, pt_, box_, counts_, offs_, sums_;  // stream-wide decoded column
-  DevBuf cand_b_, cand_p_, flags_, pos_, sums2_, out_b_, out_p_;
+  DevBuf cand_b_, cand_p_, flags_, sums2_, out_b_, out_p_;
   ProbeScratch psc_;  // the probes' Morton order and the candidates' permutation
   uint64_t* h_tot_ = nullptr;  // pinned: candidates, pairs, status, escalations
   uint64_t ccap_ = 0, ocap_ = 0;
