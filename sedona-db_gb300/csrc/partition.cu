@@ -170,15 +170,27 @@ __global__ void k_extent(const float4* __restrict__ box, uint64_t n, uint32_t* a
     mxx = max(mxx, f2o(b.z));
     mxy = max(mxy, f2o(b.w));
   }
+  // warp, then block, then one global atomic per word and block (global
+  // atomics on four words from every warp would serialise in L2)
+  __shared__ uint32_t blk[4];
+  if (threadIdx.x < 4) blk[threadIdx.x] = threadIdx.x < 2 ? 0xffffffffu : 0u;
+  __syncthreads();
   mnx = __reduce_min_sync(0xffffffffu, mnx);
   mny = __reduce_min_sync(0xffffffffu, mny);
   mxx = __reduce_max_sync(0xffffffffu, mxx);
   mxy = __reduce_max_sync(0xffffffffu, mxy);
   if ((threadIdx.x & 31) == 0) {
-    atomicMin(acc + 0, mnx);
-    atomicMin(acc + 1, mny);
-    atomicMax(acc + 2, mxx);
-    atomicMax(acc + 3, mxy);
+    atomicMin(blk + 0, mnx);
+    atomicMin(blk + 1, mny);
+    atomicMax(blk + 2, mxx);
+    atomicMax(blk + 3, mxy);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicMin(acc + 0, blk[0]);
+    atomicMin(acc + 1, blk[1]);
+    atomicMax(acc + 2, blk[2]);
+    atomicMax(acc + 3, blk[3]);
   }
 }
 
@@ -220,17 +232,68 @@ __global__ void k_kdb_assign(const float4* __restrict__ box, uint64_t n,
   }
 }
 
+// The union of each partition's build boxes (ordered-integer min / max).  A
+// warp reduces its rows partition by partition (the distinct partitions of
+// 32 rows), then the block accumulates in shared memory (nparts <=
+// kBoundsSmemParts; dynamic shared memory of 16 * nparts bytes) and issues
+// one global atomic per word it touched; with more partitions the warps'
+// results go to global memory directly.  (Four global atomics per row on a
+// few words serialise in L2.)
+constexpr uint32_t kBoundsSmemParts = 1024;
 __global__ void k_bounds(const float4* __restrict__ box, const uint32_t* __restrict__ part,
                          uint64_t n, uint32_t nparts, uint32_t* acc) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t p = part[i];
-    if (p >= nparts) continue;
-    const float4 b = box[i];
-    atomicMin(acc + 4 * p + 0, f2o(b.x));
-    atomicMin(acc + 4 * p + 1, f2o(b.y));
-    atomicMax(acc + 4 * p + 2, f2o(b.z));
-    atomicMax(acc + 4 * p + 3, f2o(b.w));
+  extern __shared__ uint32_t sacc[];
+  const bool smem = nparts <= kBoundsSmemParts;
+  if (smem) {
+    for (uint32_t k = threadIdx.x; k < 4 * nparts; k += blockDim.x)
+      sacc[k] = (k & 3) < 2 ? 0xffffffffu : 0u;
+    __syncthreads();
+  }
+  uint32_t* dst = smem ? sacc : acc;
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t end = (n + 31) / 32 * 32;  // whole warps take every turn
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < end; i += stride) {
+    uint32_t p = nparts;
+    uint32_t x0 = 0xffffffffu, y0 = 0xffffffffu, x1 = 0u, y1 = 0u;
+    if (i < n) {
+      p = part[i];
+      if (p < nparts) {
+        const float4 b = box[i];
+        x0 = f2o(b.x);
+        y0 = f2o(b.y);
+        x1 = f2o(b.z);
+        y1 = f2o(b.w);
+      }
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, p < nparts);
+    while (todo) {
+      const int leader = __ffs(todo) - 1;
+      const uint32_t pl = __shfl_sync(0xffffffffu, p, leader);
+      const bool mine = p == pl;
+      const uint32_t a = __reduce_min_sync(0xffffffffu, mine ? x0 : 0xffffffffu);
+      const uint32_t b = __reduce_min_sync(0xffffffffu, mine ? y0 : 0xffffffffu);
+      const uint32_t c = __reduce_max_sync(0xffffffffu, mine ? x1 : 0u);
+      const uint32_t d = __reduce_max_sync(0xffffffffu, mine ? y1 : 0u);
+      if (lane == leader) {
+        atomicMin(dst + 4 * pl + 0, a);
+        atomicMin(dst + 4 * pl + 1, b);
+        atomicMax(dst + 4 * pl + 2, c);
+        atomicMax(dst + 4 * pl + 3, d);
+      }
+      todo &= ~__ballot_sync(0xffffffffu, mine);
+    }
+  }
+  if (smem) {
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < 4 * nparts; k += blockDim.x) {
+      const uint32_t v = sacc[k];
+      if ((k & 3) < 2) {
+        if (v != 0xffffffffu) atomicMin(acc + k, v);
+      } else if (v != 0u) {
+        atomicMax(acc + k, v);
+      }
+    }
   }
 }
 
@@ -268,6 +331,11 @@ __global__ void k_iota(uint32_t* __restrict__ v, uint64_t n) {
 // of lanes with the same bin (most rows of a warp share one)
 __global__ void k_hist(uint32_t* __restrict__ part, uint64_t n, uint32_t nbins,
                        uint32_t* __restrict__ count) {
+  // the block's counts in shared memory (dynamic, 4 * nbins bytes), then one
+  // global atomic per non-empty bin and block
+  extern __shared__ uint32_t scount[];
+  for (uint32_t k = threadIdx.x; k < nbins; k += blockDim.x) scount[k] = 0;
+  __syncthreads();
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t end = (n + 31) / 32 * 32;  // whole warps take every turn
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < end; i += stride) {
@@ -279,8 +347,11 @@ __global__ void k_hist(uint32_t* __restrict__ part, uint64_t n, uint32_t nbins,
     }
     const unsigned grp = __match_any_sync(0xffffffffu, p);
     if (i < n && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1))
-      atomicAdd(count + p, (uint32_t)__popc(grp));
+      atomicAdd(scount + p, (uint32_t)__popc(grp));
   }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < nbins; k += blockDim.x)
+    if (scount[k]) atomicAdd(count + k, scount[k]);
 }
 
 __global__ void k_map_pairs(const uint32_t* __restrict__ db, const uint32_t* __restrict__ dp,
@@ -581,7 +652,8 @@ int run_partitioned(JoinEngine& eng, Workspace& ws, const HostWkbColumn& build,
     }
     SPJ_CUDA(cudaMemcpyAsync(bacc.get(), ia.data(), ia.size() * 4, cudaMemcpyHostToDevice, s));
     if (nb)
-      k_bounds<<<grid_for((int64_t)nb, 256, kNumSMs * 16), 256, 0, s>>>(
+      k_bounds<<<grid_for((int64_t)nb, 256, kNumSMs * 16), 256,
+                 nleaves <= kBoundsSmemParts ? 16 * (size_t)nleaves : 0, s>>>(
           bbox.as<float4>(), bpart.as<uint32_t>(), nb, nleaves, bacc.as<uint32_t>());
     SPJ_CUDA(cudaMemcpyAsync(ia.data(), bacc.get(), ia.size() * 4, cudaMemcpyDeviceToHost, s));
     SPJ_CUDA(cudaStreamSynchronize(s));
@@ -627,11 +699,11 @@ int run_partitioned(JoinEngine& eng, Workspace& ws, const HostWkbColumn& build,
   SPJ_CUDA(cudaMemsetAsync(bcnt.get(), 0, 4 * (size_t)bbins, s));
   SPJ_CUDA(cudaMemsetAsync(pcnt.get(), 0, 4 * (size_t)pbins, s));
   if (nb)
-    k_hist<<<grid_for((int64_t)nb, 256, kNumSMs * 16), 256, 0, s>>>(bpart.as<uint32_t>(), nb,
-                                                                     bbins, bcnt.as<uint32_t>());
+    k_hist<<<grid_for((int64_t)nb, 256, kNumSMs * 16), 256, 4 * (size_t)bbins, s>>>(
+        bpart.as<uint32_t>(), nb, bbins, bcnt.as<uint32_t>());
   if (np)
-    k_hist<<<grid_for((int64_t)np, 256, kNumSMs * 16), 256, 0, s>>>(ppart.as<uint32_t>(), np,
-                                                                     pbins, pcnt.as<uint32_t>());
+    k_hist<<<grid_for((int64_t)np, 256, kNumSMs * 16), 256, 4 * (size_t)pbins, s>>>(
+        ppart.as<uint32_t>(), np, pbins, pcnt.as<uint32_t>());
   std::vector<uint32_t> hb(bbins), hp(pbins);
   SPJ_CUDA(cudaMemcpyAsync(hb.data(), bcnt.get(), 4 * (size_t)bbins, cudaMemcpyDeviceToHost, s));
   SPJ_CUDA(cudaMemcpyAsync(hp.data(), pcnt.get(), 4 * (size_t)pbins, cudaMemcpyDeviceToHost, s));
