@@ -618,6 +618,79 @@ __device__ __forceinline__ bool ring_rects_intersect(const GeomsView& GA, uint32
   return !(Bq.x > A.z || Bq.z < A.x || Bq.y > A.w || Bq.w < A.y);
 }
 
+// Isolation test of ring ro of Go against ring rr of Gr, in the FP32 form,
+// with rr's y-band index.  If every segment of rr has a bbox strictly
+// separated from ro's bbox (a strict f32 comparison of round-to-nearest
+// values proves the f64 one), or has that whole box strictly on one side of
+// its line (all four corners, decided orientations), then
+//  - no segment test between rr and ro can succeed (tg's first test is the
+//    bbox test, and a segment that misses the box misses every segment in
+//    it), and
+//  - for every point v of ro's box, each ray-cast decision is one of tg's
+//    comparison-only exits or the exact side test, i.e. the exact half-open
+//    crossing rule; no segment crosses the box, so that parity is the same
+//    for every point of ro: ro lies strictly inside rr or strictly outside.
+// Returns 1 / 0 in that case (the point-in-ring answer of ro's first vertex,
+// which every point of ro shares), kIsoNear when a segment of rr comes near
+// the box, kIsoNoIndex when rr has no band index (or ro no segments).
+constexpr int kIsoNear = -4, kIsoNoIndex = -5;
+template <bool kFast>
+__device__ __forceinline__ int ring_isolation(const GeomsView& Gr, uint32_t rr,
+                                              const GeomsView& Go, uint32_t ro, uint32_t& esc) {
+  if (!kFast || Go.ring_nsegs[ro] <= 0 || Gr.ring_bands == nullptr ||
+      !(Gr.band_param[rr].y >= 0.0f))
+    return kIsoNoIndex;
+  const float4 ob = Go.ring_rect32[ro];
+  const float bx0 = ob.x, by0 = ob.y, bx1 = ob.z, by1 = ob.w;
+  const uint32_t B = Gr.ring_bands[rr];
+  const int nb = (int)(Gr.ring_bands[rr + 1] - B) - 1;
+  const float2 prm = Gr.band_param[rr];
+  const int b0 = band_of(by0, prm.x, prm.y, nb), b1 = band_of(by1, prm.x, prm.y, nb);
+  // The first vertex's point-in-ring test rides along: its band is one of
+  // b0..b1, so the same scan classifies that band's edges for it (the FP32
+  // tier of ring_pip_fast).  When the box is isolated and every one of those
+  // edges was decided, the parity is ring_pip's answer; otherwise ring_pip
+  // runs as before.
+  const uint32_t Vo = Go.ring_vtx[ro];
+  const double2 v0 = Go.xy[Vo];
+  const float2 v032 = Go.xy32[Vo];
+  const bool v_in_rect = ring_rect_covers(Gr, rr, v0, v032);
+  const int bv = band_of(v032.y, prm.x, prm.y, nb);
+  bool v_decided = true;
+  unsigned v_par = 0;
+  bool near = false;
+  for (int bb = b0; bb <= b1 && !near; bb++) {
+    const uint32_t e0 = Gr.band_off[B + bb], e1 = Gr.band_off[B + bb + 1];
+    const bool vband = v_in_rect && bb == bv;
+    for (uint32_t k = e0; k < e1; k++) {
+      const float4 sg = Gr.band_seg[k];
+      const float2 c = make_float2(sg.x, sg.y), d = make_float2(sg.z, sg.w);
+      // xmax descending: the rest of the band is strictly left of the box
+      // (bbox-separated) and of its first vertex (tg's ray cast: OUT)
+      if (fmax0f(c.x, d.x) < bx0) break;
+      if (vband) {
+        const int pc = pip_seg_f32(c, d, v032);
+        if (pc == kIn) v_par ^= 1u;
+        else if (pc != kOut) v_decided = false;
+      }
+      if (fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
+          fmin0f(c.y, d.y) > by1)
+        continue;  // bboxes strictly separated
+      const int s0 = orient32(c, d, make_float2(bx0, by0));
+      if (s0 != 0 && orient32(c, d, make_float2(bx1, by0)) == s0 &&
+          orient32(c, d, make_float2(bx1, by1)) == s0 &&
+          orient32(c, d, make_float2(bx0, by1)) == s0)
+        continue;
+      near = true;
+      break;
+    }
+  }
+  if (near) return kIsoNear;
+  if (!v_in_rect) return 0;  // ring_pip's first test
+  if (v_decided) return v_par != 0;
+  return ring_pip<kFast>(Gr, rr, v0, v032, true, esc).hit ? 1 : 0;
+}
+
 // tg.c:3166-3192 + tg.c:3089-3113 with allow_on_edge = true, for two rings.
 // The result is the OR over the smaller ring's vertices of "vertex in or on
 // the larger ring" and over its segments of "crosses >= 2 of the larger
@@ -653,72 +726,12 @@ __device__ __forceinline__ int ring_intersects_ring(const GeomsView& GA, uint32_
     const int st = grid_rect_status(*Gr, rr, Go->ring_rect[ro], Go->ring_rect32[ro]);
     if (st != 0) return st == 1 ? 1 : 0;
   }
-  if (kFast && nso > 0 && Gr->ring_bands != nullptr && Gr->band_param[rr].y >= 0.0f) {
-    // Isolation exit.  If every segment of the larger ring has a bbox
-    // strictly separated from the smaller ring's bbox (a strict f32
-    // comparison of round-to-nearest values proves the f64 one), then
-    //  - no segment test can succeed (tg's first test is the bbox test), and
-    //  - for every vertex v of the smaller ring, each ray-cast decision is one
-    //    of tg's comparison-only exits (v lies outside every segment's closed
-    //    bbox), i.e. the exact half-open crossing rule; no segment crosses the
-    //    smaller ring's bbox, so that parity is the same for all its vertices.
-    // The result is therefore the point-in-ring test of the first vertex.
-    const float4 ob = Go->ring_rect32[ro];
-    const float bx0 = ob.x, by0 = ob.y, bx1 = ob.z, by1 = ob.w;
-    const uint32_t B = Gr->ring_bands[rr];
-    const int nb = (int)(Gr->ring_bands[rr + 1] - B) - 1;
-    const float2 prm = Gr->band_param[rr];
-    const int b0 = band_of(by0, prm.x, prm.y, nb), b1 = band_of(by1, prm.x, prm.y, nb);
-    // The first vertex's point-in-ring test rides along: its band is one of
-    // b0..b1, so the same scan classifies that band's edges for it (the FP32
-    // tier of ring_pip_fast).  When the box is isolated and every one of
-    // those edges was decided, the parity is ring_pip's answer; otherwise
-    // ring_pip runs as before.
-    const double2 v0 = Go->xy[Vo];
-    const float2 v032 = Go->xy32[Vo];
-    const bool v_in_rect = ring_rect_covers(*Gr, rr, v0, v032);
-    const int bv = band_of(v032.y, prm.x, prm.y, nb);
-    bool v_decided = true;
-    unsigned v_par = 0;
-    bool near = false;
-    for (int bb = b0; bb <= b1 && !near; bb++) {
-      const uint32_t e0 = Gr->band_off[B + bb], e1 = Gr->band_off[B + bb + 1];
-      const bool vband = v_in_rect && bb == bv;
-      for (uint32_t k = e0; k < e1; k++) {
-        const float4 sg = Gr->band_seg[k];
-        const float2 c = make_float2(sg.x, sg.y), d = make_float2(sg.z, sg.w);
-        // xmax descending: the rest of the band is strictly left of the box
-        // (bbox-separated) and of its first vertex (tg's ray cast: OUT)
-        if (fmax0f(c.x, d.x) < bx0) break;
-        if (vband) {
-          const int pc = pip_seg_f32(c, d, v032);
-          if (pc == kIn) v_par ^= 1u;
-          else if (pc != kOut) v_decided = false;
-        }
-        if (fmax0f(c.x, d.x) < bx0 || fmin0f(c.x, d.x) > bx1 || fmax0f(c.y, d.y) < by0 ||
-            fmin0f(c.y, d.y) > by1)
-          continue;  // bboxes strictly separated
-        // the smaller ring's box strictly on one side of the segment's line
-        // (all four corners, decided orientations): the segment misses the
-        // box, every segment test against it fails in tg, and its ray-cast
-        // decision for any vertex in the box is the exact side test
-        const int s0 = orient32(c, d, make_float2(bx0, by0));
-        if (s0 != 0 && orient32(c, d, make_float2(bx1, by0)) == s0 &&
-            orient32(c, d, make_float2(bx1, by1)) == s0 &&
-            orient32(c, d, make_float2(bx0, by1)) == s0)
-          continue;
-        near = true;
-        break;
-      }
-    }
-    if (!near) {
-      if (!v_in_rect) return 0;  // ring_pip's first test
-      if (v_decided) return v_par != 0;
-      return ring_pip<kFast>(*Gr, rr, v0, v032, true, esc).hit ? 1 : 0;
-    }
-    if (kCheap) {
+  {
+    const int iso = ring_isolation<kFast>(*Gr, rr, *Go, ro, esc);
+    if (iso >= 0) return iso;
+    if (kCheap && iso == kIsoNear) {
       // the vertex loop below starts with this test
-      if (ring_pip<kFast>(*Gr, rr, v0, v032, true, esc, false).hit) return 1;
+      if (ring_pip<kFast>(*Gr, rr, Go->xy[Vo], Go->xy32[Vo], true, esc, false).hit) return 1;
       return kDeferred;
     }
   }

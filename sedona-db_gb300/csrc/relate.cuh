@@ -234,6 +234,14 @@ __device__ __noinline__ bool ring_contains_ring(const GeomsView& GA, uint32_t ra
     // outside (2) a, and no edge of a meets b, whatever allow_on_edge says
     const int st = grid_rect_status(GA, ra, Bq, GB.ring_rect32[rb]);
     if (st != 0) return st == 1;
+    // no edge of a near b's box (ring_isolation): b lies strictly inside or
+    // strictly outside a.  Inside, every point of b is inside a and no
+    // segment of b meets an edge of a, so tg's point tests (convex a) and
+    // segment tests (tg_ring_contains_segment: both ends in, no edge met)
+    // all pass; outside, the first vertex's test fails.  allow_on_edge
+    // changes neither.
+    const int iso = ring_isolation<kFast>(GA, ra, GB, rb, esc);
+    if (iso >= 0) return iso == 1;
   }
   const uint32_t Vb = GB.ring_vtx[rb];
   if (ring_flags_of(GA, ra) & kRingConvex) {
