@@ -11,6 +11,7 @@
 // bytes go to HBM in one copy and every page is decompressed and decoded
 // there into the Arrow large_binary layout the WKB decode kernel reads.
 #pragma once
+#include <functional>
 #include <string>
 #include <utility>
 #include <vector>
@@ -98,6 +99,14 @@ static_assert(sizeof(PageInfo) == 56, "PageInfo layout");
 // pages that use it carry it); returns whether it had one.
 bool walk_pages(const uint8_t* buf, uint64_t begin, uint64_t end, int codec, int max_def,
                 int dict_index, uint64_t* row, std::vector<PageInfo>& pages);
+// The same walk with the bytes fetched on demand: bytes_at(pos) gives the
+// chunk's bytes from position pos on, at least the page header there (a
+// header cut short throws "truncated thrift structure").  header_pos, when
+// given, receives each page's header position.
+using HeaderBytes = std::function<std::pair<const uint8_t*, const uint8_t*>(uint64_t)>;
+bool walk_pages(const HeaderBytes& bytes_at, uint64_t begin, uint64_t end, int codec,
+                int max_def, int dict_index, uint64_t* row, std::vector<PageInfo>& pages,
+                std::vector<uint64_t>* header_pos);
 
 // Snappy block compression (the published format: a varint length, then
 // literal and copy elements); used by the writer.

@@ -565,6 +565,14 @@ uint64_t parse_footer(const uint8_t* tail, uint64_t tail_len, uint64_t file_len,
 
 bool walk_pages(const uint8_t* buf, uint64_t begin, uint64_t end, int codec, int max_def,
                 int dict_index, uint64_t* row, std::vector<PageInfo>& pages) {
+  return walk_pages(
+      [buf, end](uint64_t pos) { return std::make_pair(buf + pos, buf + end); }, begin, end,
+      codec, max_def, dict_index, row, pages, nullptr);
+}
+
+bool walk_pages(const HeaderBytes& bytes_at, uint64_t begin, uint64_t end, int codec,
+                int max_def, int dict_index, uint64_t* row, std::vector<PageInfo>& pages,
+                std::vector<uint64_t>* header_pos) {
   if (codec != kUncompressed && codec != kSnappy)
     throw Error("parquet: compression codec " + std::to_string(codec) +
                 " is not supported (UNCOMPRESSED and SNAPPY are)");
@@ -572,7 +580,8 @@ bool walk_pages(const uint8_t* buf, uint64_t begin, uint64_t end, int codec, int
   uint64_t pos = begin;
   bool has_dict = false, seen_data = false;
   while (pos < end) {
-    TIn in{buf + pos, buf + end};
+    const auto hb = bytes_at(pos);
+    TIn in{hb.first, hb.second};
     int type = -1;
     int32_t usize = -1, csize = -1;
     int32_t nvals = -1, enc = -1, def_enc = kRle, nnulls = 0, def_len = 0, rep_len = 0;
@@ -610,10 +619,11 @@ bool walk_pages(const uint8_t* buf, uint64_t begin, uint64_t end, int codec, int
       else return false;
       return true;
     });
-    const uint64_t hdr = (uint64_t)(in.p - (buf + pos));
+    const uint64_t hdr = (uint64_t)(in.p - hb.first);
     if (usize < 0 || csize < 0) throw Error("parquet: page header without sizes");
     const uint64_t src = pos + hdr;
     if (src + (uint64_t)csize > end) throw Error("parquet: page runs past its column chunk");
+    const uint64_t page_pos = pos;
     pos = src + (uint64_t)csize;
     if (type == kIndexPage) continue;
     if (type != kDataPage && type != kDataPageV2 && type != kDictionaryPage)
@@ -664,6 +674,7 @@ bool walk_pages(const uint8_t* buf, uint64_t begin, uint64_t end, int codec, int
     if (pg.in_src && pg.raw_size != pg.src_size)
       throw Error("parquet: stored page whose sizes differ");
     pages.push_back(pg);
+    if (header_pos) header_pos->push_back(page_pos);
   }
   if (pos != end) throw Error("parquet: column chunk size disagrees with its pages");
   return has_dict;

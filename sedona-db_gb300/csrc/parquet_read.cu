@@ -195,6 +195,8 @@ __device__ __forceinline__ uint32_t win_u32(const Win& w, uint32_t pos) {
 }
 
 constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
+constexpr uint64_t kHeaderWindow = 4096;   // bytes read per page header from the file
+constexpr uint64_t kReadGroup = 4ull << 20;  // bytes of whole pages per reader-thread read
 constexpr uint32_t kFragWin = 2048;        // per warp, k_snappy_frags (headers, literals)
 constexpr uint32_t kWalkWin = 8192;        // per warp, PLAIN walks
 enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
@@ -977,19 +979,45 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
       p->stage_h_cap = total + 16;
     }
     uint8_t* hb = p->stage_h.as<uint8_t>();
-    {
+    p->file_bytes = total;
+
+    // The page table, from the page headers read straight from the file
+    // (small reads), so that the reader threads can index the Snappy pages
+    // they have just read while the bytes are in cache.  A header longer than
+    // the read window (large statistics) falls back to reading the chunks
+    // first and walking the pages in memory.
+    std::vector<PageInfo> pages;
+    std::vector<uint64_t> hpos;  // staging position of each page's header
+    uint64_t row = 0;
+    int ndict = 0;
+    bool prewalked = true;
+    try {
+      std::vector<uint8_t> win;
+      for (auto& r : ranges) {
+        auto bytes_at = [&](uint64_t pos) {
+          const uint64_t want = std::min<uint64_t>(kHeaderWindow, r.at + r.len - pos);
+          win.resize(want);
+          p->read_at(r.off + (pos - r.at), want, win.data());
+          return std::make_pair((const uint8_t*)win.data(), (const uint8_t*)win.data() + want);
+        };
+        if (walk_pages(bytes_at, r.at, r.at + r.len, r.codec, leaf.max_def, ndict, &row, pages,
+                       &hpos))
+          ndict++;
+      }
+    } catch (const Error&) {
+      prewalked = false;
+    }
+    if (!prewalked) {
+      pages.clear();
+      hpos.clear();
+      row = 0;
+      ndict = 0;
       std::vector<SpjParquet::ReadPiece> rd;
       for (auto& r : ranges) rd.push_back({r.off, r.len, hb + r.at});
       p->read_parallel(rd);
+      for (auto& r : ranges)
+        if (walk_pages(hb, r.at, r.at + r.len, r.codec, leaf.max_def, ndict, &row, pages)) ndict++;
     }
-    p->file_bytes = total;
-
-    // page table
-    std::vector<PageInfo> pages;
-    uint64_t row = 0;
-    int ndict = 0;
-    for (auto& r : ranges)
-      if (walk_pages(hb, r.at, r.at + r.len, r.codec, leaf.max_def, ndict, &row, pages)) ndict++;
     SPJ_CHECK(row == rows_expected, "the pages hold " + std::to_string(row) +
                                         " values, the row groups " +
                                         std::to_string(rows_expected) + " rows");
@@ -1028,41 +1056,87 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
     frag_base[np] = nfrag;
     const uint32_t nwork = (uint32_t)work.size();
 
+    // the Snappy block index of every compressed page (host threads)
+    std::vector<uint8_t> mode(np + 1, kModeStored);
+    std::vector<uint32_t> frag_ip(nfrag + 1, 0);
+    auto index_page = [&](uint32_t i) {
+      const PageInfo& pg = pages[i];
+      if (pg.in_src) return;
+      mode[i] = pg.lvl_bytes < pg.src_size && pg.lvl_bytes <= pg.raw_size
+                    ? snappy_block_index(hb + pg.src + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
+                                         pg.raw_size - pg.lvl_bytes,
+                                         frag_ip.data() + frag_base[i])
+                    : (uint8_t)kModeBad;
+    };
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    if (prewalked) {
+      // the chunk bytes in groups of whole pages (kReadGroup bytes or so): a
+      // thread reads a group, then indexes its pages while they are in cache
+      struct Group {
+        uint64_t beg, end, file;
+        uint32_t p0, p1;
+      };
+      std::vector<Group> groups;
+      uint32_t i = 0;
+      for (auto& r : ranges) {
+        const uint64_t rend = r.at + r.len;
+        uint64_t beg = r.at;
+        uint32_t p0 = i;
+        while (i < np && hpos[i] < rend) {
+          const uint64_t pend = i + 1 < np && hpos[i + 1] < rend ? hpos[i + 1] : rend;
+          i++;
+          if (pend - beg >= kReadGroup || pend == rend) {
+            groups.push_back({beg, pend, r.off + (beg - r.at), p0, i});
+            beg = pend;
+            p0 = i;
+          }
+        }
+        if (beg < rend) groups.push_back({beg, rend, r.off + (beg - r.at), p0, i});
+      }
+      std::atomic<size_t> next{0};
+      const size_t nt = std::min<size_t>({16, hw, groups.size()});
+      std::vector<std::exception_ptr> err(std::max<size_t>(nt, 1));
+      auto run = [&](size_t t) {
+        try {
+          for (size_t g = next++; g < groups.size(); g = next++) {
+            const Group& gr = groups[g];
+            p->read_at(gr.file, gr.end - gr.beg, hb + gr.beg);
+            for (uint32_t k = gr.p0; k < gr.p1; k++) index_page(k);
+          }
+        } catch (...) {
+          err[t] = std::current_exception();
+        }
+      };
+      std::vector<std::thread> th;
+      for (size_t t = 1; t < nt; t++) th.emplace_back(run, t);
+      run(0);
+      for (auto& t : th) t.join();
+      for (auto& e : err)
+        if (e) std::rethrow_exception(e);
+    }
     SPJ_CUDA(cudaEventRecord(p->ev[0], s));
     p->stage.reserve(total + 16, s);
     SPJ_CUDA(cudaMemcpyAsync(p->stage.get(), hb, total, cudaMemcpyHostToDevice, s));
     SPJ_CUDA(cudaEventRecord(p->ev[1], s));
-    // while the chunk bytes travel: the Snappy block index of every compressed
-    // page, on host threads (before any copy from pageable memory, which
-    // would wait for the copy above)
-    std::vector<uint8_t> mode(np + 1, kModeStored);
-    std::vector<uint32_t> frag_ip(nfrag + 1, 0);
-    {
+    if (!prewalked) {
+      // while the chunk bytes travel (before any copy from pageable memory,
+      // which would wait for the copy above)
       std::vector<uint32_t> todo;
-      for (uint32_t i = 0; i < np; i++)
-        if (!pages[i].in_src) todo.push_back(i);
+      for (uint32_t k = 0; k < np; k++)
+        if (!pages[k].in_src) todo.push_back(k);
       auto run = [&](size_t t, size_t nt) {
-        for (size_t j = t; j < todo.size(); j += nt) {
-          const PageInfo& pg = pages[todo[j]];
-          mode[todo[j]] =
-              pg.lvl_bytes < pg.src_size && pg.lvl_bytes <= pg.raw_size
-                  ? snappy_block_index(hb + pg.src + pg.lvl_bytes, pg.src_size - pg.lvl_bytes,
-                                       pg.raw_size - pg.lvl_bytes,
-                                       frag_ip.data() + frag_base[todo[j]])
-                  : (uint8_t)kModeBad;
-        }
+        for (size_t j = t; j < todo.size(); j += nt) index_page(todo[j]);
       };
-      const size_t nt = std::min<size_t>({16, std::max(1u, std::thread::hardware_concurrency()),
-                                          (todo.size() + 3) / 4});
+      const size_t nt = std::min<size_t>({16, hw, (todo.size() + 3) / 4});
       std::vector<std::thread> th;
       for (size_t t = 1; t < nt; t++) th.emplace_back(run, t, nt);
       run(0, std::max<size_t>(nt, 1));
       for (auto& t : th) t.join();
-      for (uint32_t i = 0; i < np; i++)
-        if (mode[i] == kModeBad)
-          throw Error("parquet: malformed Snappy data in page " + std::to_string(i) +
-                      " of the read (" + std::to_string(np) + " pages)");
     }
+    for (uint32_t k = 0; k < np; k++)
+      if (mode[k] == kModeBad)
+        throw Error("parquet: malformed Snappy data in page " + std::to_string(k) +
+                    " of the read (" + std::to_string(np) + " pages)");
     // the small tables come from pageable vectors: the copies complete
     // before the stream synchronisation below, while the vectors live
     p->pages.reserve(sizeof(PageInfo) * (np + 1), s);
