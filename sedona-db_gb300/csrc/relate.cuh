@@ -98,18 +98,25 @@ __device__ __forceinline__ bool any_segment_near(const GeomsView& G, uint32_t r,
 // ask whether any segment meets a condition that starts with
 // tg_segment_intersects_segment(query, segment), so neither their visit
 // order nor their rect filter changes the answer.  ring_pip reports tg's ON
-// edge index (the last ON segment in index order).
+// edge index (the last ON segment in index order).  carry: on entry the
+// point-in-ring result of q.a when known (idx != kNoCarry), the previous
+// segment's end point; on return q.b's result when it was computed (the next
+// segment's start point), else kNoCarry.
+constexpr int kNoCarry = -0x7fffffff;
 template <bool kFast>
 __device__ __noinline__ bool ring_contains_segment(const GeomsView& G, uint32_t r, const Seg q,
-                                                   bool aoe, uint32_t& esc) {
+                                                   bool aoe, uint32_t& esc, RingHit* carry) {
+  const RingHit known = *carry;
+  carry->idx = kNoCarry;
   const Rect64 R = G.ring_rect[r];
   if (fmin0(q.a.x, q.b.x) < R.x || fmax0(q.a.x, q.b.x) > R.z || fmin0(q.a.y, q.b.y) < R.y ||
       fmax0(q.a.y, q.b.y) > R.w)
     return false;
-  const RingHit ha = ring_pip<kFast>(G, r, q.a, q.a32, aoe, esc);
+  const RingHit ha = known.idx != kNoCarry ? known : ring_pip<kFast>(G, r, q.a, q.a32, aoe, esc);
   if (!ha.hit) return false;
   if (pteq(q.b, q.a)) return true;
   const RingHit hb = ring_pip<kFast>(G, r, q.b, q.b32, aoe, esc);
+  *carry = hb;
   if (!hb.hit) return false;
   const uint8_t fl = ring_flags_of(G, r);
   if (fl & kRingConvex) return true;
@@ -251,8 +258,11 @@ __device__ __noinline__ bool ring_contains_ring(const GeomsView& GA, uint32_t ra
     return true;
   }
   const int ns = GB.ring_nsegs[rb];
+  // consecutive segments share a vertex: its point-in-ring result carries over
+  RingHit carry{false, kNoCarry};
   for (int i = 0; i < ns; i++)
-    if (!ring_contains_segment<kFast>(GA, ra, ring_segment(GB, rb, i), aoe, esc)) return false;
+    if (!ring_contains_segment<kFast>(GA, ra, ring_segment(GB, rb, i), aoe, esc, &carry))
+      return false;
   return true;
 }
 
