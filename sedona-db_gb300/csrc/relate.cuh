@@ -359,6 +359,15 @@ __device__ __noinline__ bool poly_touches_poly(const GeomsView& GA, uint32_t qa,
   const uint32_t a0 = GA.part_ring[qa], a1 = GA.part_ring[qa + 1];
   const uint32_t b0 = GB.part_ring[qb], b1 = GB.part_ring[qb + 1];
   if (!ring_rects_intersect<kFast>(GA, a0, GB, b0)) return false;
+  if (kFast && a1 - a0 == 1 && b1 - b0 == 1) {
+    // two single rings, no edge of one near the other's box (ring_isolation):
+    // the other lies strictly inside or strictly outside, so the boundaries
+    // do not meet.  Inside, its segments' ends are in the ring with and
+    // without allow_on_edge (the loop below returns false); outside, no
+    // segment of either ring meets the other ring (no touches counted).
+    if (ring_isolation<kFast>(GA, a0, GB, b0, esc) >= 0) return false;
+    if (ring_isolation<kFast>(GB, b0, GA, a0, esc) >= 0) return false;
+  }
   // one polygon inside a hole of the other, touching the hole's boundary
   for (int ii = 0; ii < 2; ii++) {
     const GeomsView& GP = ii == 0 ? GA : GB;
