@@ -754,7 +754,7 @@ def run_learned(args, world, rank, local, pg):
     """Workload 5: 100M GMM build points, 10M range boxes + 10M exact-point
     lookups (ST_Intersects).  Chosen form: the learned index (trained on the
     GPU).  Plain form: the LBVH join with the FP64 refine on the same inputs,
-    which is also the judge of the pair set."""
+    which is also the arbiter of the pair set."""
     import torch
     from sedona_gpuspatial import capi, datagen
 
@@ -874,7 +874,7 @@ def run_learned(args, world, rank, local, pg):
     li.set_trained(True)
     assert n_untrained == npairs
 
-    # plain form / judge: the LBVH join, FP64 refine, same inputs
+    # plain form / arbiter: the LBVH join, FP64 refine, same inputs
     # (leaf size 4: measured best for range boxes and lookups over points)
     jp = capi.SpatialJoin(rt, leaf_size=4, refine_form=0)
     jp.build_device(db_)
@@ -896,7 +896,7 @@ def run_learned(args, world, rank, local, pg):
     fast_ms = (time.perf_counter() - t0) * 1e3
     assert n_fast == npairs, (n_fast, npairs)
     # parity: the learned index's full pair set against the LBVH join with
-    # the FP64 refine (the judge), per probe column, compared on the device
+    # the FP64 refine (the arbiter), per probe column, compared on the device
     parity = None
     if args.parity:
         equal = True
@@ -907,7 +907,7 @@ def run_learned(args, world, rank, local, pg):
             del ka, kb
         parity = {"pairs_equal": equal, "pairs": int(npairs),
                   "kind": "full sorted pair sets, learned index vs the LBVH join with the "
-                          "FP64 refine (the judge; both probe columns)"}
+                          "FP64 refine (the arbiter; both probe columns)"}
     n_rows = len(boxes) + len(lookups)
     hbm_peak, peak_kind = load_peaks()
     # algorithmic bytes per step: probe WKB + offsets once, per lookup the
@@ -944,7 +944,7 @@ def run_learned(args, world, rank, local, pg):
                                         "mean_err": st_untrained["mean_err"],
                                         "search_steps_per_lookup": untrained_steps}},
         "plain_f64_form": {"pairs_per_s": npairs / (plain_ms * 1e-3), "ms_per_step": plain_ms,
-                           "form": "LBVH join, FP64 refine (also the pair-set judge)",
+                           "form": "LBVH join, FP64 refine (also the pair-set arbiter)",
                            "speedup_chosen_vs_plain": plain_ms / ms},
         "lbvh_fast_form": {"ms_per_step": fast_ms, "pairs_per_s": npairs / (fast_ms * 1e-3),
                            "form": "LBVH join, FP32-filtered refine, Morton-ordered probes",

@@ -224,7 +224,7 @@ void* SpjStreamCudaStream(SpjStream* stream);
  * key -> rank (a root line picks one of `leaves` per-leaf lines) trained on
  * the GPU, lookups searched within each leaf's measured error and verified
  * exactly; the LBVH over the same points is the fallback (leaves over the
- * window) and the judge.  No counterpart in the reference (which has no
+ * window) and the arbiter.  No counterpart in the reference (which has no
  * learned index); it serves point build sides of the join (probe points:
  * exact-point lookups; probe polygons such as range boxes: ST_Intersects /
  * ST_Within / ST_CoveredBy(build point, probe polygon)). */

@@ -7,7 +7,7 @@
 // error; the result is verified against the neighbouring keys, so a lookup
 // is exact whatever the model's quality.  The LBVH over the same points is
 // the fallback (leaves whose error exceeds the window, boxes covering too
-// many grid cells) and the judge of the pair set (the regular join path on
+// many grid cells) and the arbiter of the pair set (the regular join path on
 // the same inputs must give the same pairs).
 //
 // Training runs on the GPU: per leaf, a forward pass evaluates the residuals

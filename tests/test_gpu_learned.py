@@ -1,5 +1,5 @@
 """Learned point index (workload-5 shape at small sizes): exact pair sets
-against the oracle and the LBVH judge, GPU training gradients against a CPU
+against the oracle and the LBVH arbiter, GPU training gradients against a CPU
 (numpy, FP64) restatement, and what training gains over the untrained model."""
 import numpy as np
 import pytest
@@ -31,13 +31,13 @@ def _oracle_pairs(oracle, build, probe, pred):
 
 @pytest.mark.parametrize("probe,pred", [("boxes", "intersects"), ("lookups", "intersects"),
                                         ("boxes", "within"), ("lookups", "equals")])
-def test_learned_pairs_match_oracle_and_lbvh_judge(env, probe, pred):
+def test_learned_pairs_match_oracle_and_lbvh_arbiter(env, probe, pred):
     capi, oracle, li, dev, cols = env
     db, dp, n = li.query_device(dev[probe][0], pred)
     got = pairs(*device_pairs(db, dp, n))
     assert n > 200
     assert got == _oracle_pairs(oracle, cols["build"], cols[probe], pred)
-    # the LBVH path (the regular join) on the same inputs is the judge
+    # the LBVH path (the regular join) on the same inputs is the arbiter
     j = capi.SpatialJoin()
     j.build_device(dev["build"][0])
     jb, jp, jn = j.probe_device(dev[probe][0], pred)
