@@ -19,6 +19,7 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
+static_assert(kScanTile == 4096, "compact_tiles (prims.cuh) counts tiles of 4096 flags");
 
 template <class Tin, class Tout>
 __global__ void k_tile_reduce(const Tin* __restrict__ in, int64_t n, Tout* __restrict__ sums) {
