@@ -9,9 +9,11 @@ The files cover what pyarrow writes by default and its options: SNAPPY and
 stored pages, data page v1 and v2, dictionary pages with RLE_DICTIONARY data
 pages, a dictionary that falls back to PLAIN in the middle of a chunk, a
 REQUIRED large_binary column, nulls, several row groups and pages, and other
-columns around the geometry.  One more file is built by hand (checked by
-reading it with pyarrow): its Snappy page holds a copy that reaches back
-across a 64 KiB block, which the format allows and Snappy writers do not emit.
+columns around the geometry.  Two more files are built by hand (checked by
+reading them with pyarrow).  In one, a Snappy page holds a copy that reaches
+back across a 64 KiB block, which the format allows and Snappy writers do not
+emit.  The other has a data page header with 3,000-byte min / max statistics,
+longer than the device reader's window for page headers.
 The values are synthetic (seeded) WKB points and polygons.
 """
 import json
@@ -124,7 +126,10 @@ def _snappy_literal(data):
     return bytes([(59 + nb) << 2]) + n.to_bytes(nb, "little") + data
 
 
-def cross_block_file(path, rng):
+def cross_block_file(path, rng, stats_bytes=0):
+    """stats_bytes > 0: no cross-block copy, but a data page header that
+    carries min / max statistics of that many bytes each (a header longer
+    than the reader's window for page headers)."""
     vals = [rng.integers(0, 256, int(rng.integers(200, 500)), dtype=np.uint8).tobytes()
             for _ in range(300)]
     levels = _varint(len(vals) << 1) + b"\x01"  # one RLE run of definition level 1
@@ -134,19 +139,24 @@ def cross_block_file(path, rng):
         body += np.uint32(len(v)).tobytes()
         starts.append(len(body))
         body += v
-    # a destination inside a value of block 1 copies bytes from a value of block 0
-    d = next(s for s in starts if s > 65536 + 8) + 4
-    src = starts[3] + 2
-    L = 48
-    body[d:d + L] = body[src:src + L]
-    # the first literal ends exactly at the block end, so only the copy
-    # crosses blocks (the block-parallel pass finds it and hands the page
-    # to the per-page pass)
-    comp = (_varint(len(body)) + _snappy_literal(bytes(body[:65536])) +
-            _snappy_literal(bytes(body[65536:d])) +
-            bytes([2 | ((L - 1) << 2)]) + (d - src).to_bytes(2, "little") +
-            _snappy_literal(bytes(body[d + L:])))
-    assert d - src < 65536 and d - src > d - 65536
+    if stats_bytes:
+        # literals only, split at the block end
+        comp = (_varint(len(body)) + _snappy_literal(bytes(body[:65536])) +
+                _snappy_literal(bytes(body[65536:])))
+    else:
+        # a destination inside a value of block 1 copies bytes from a value of block 0
+        d = next(s for s in starts if s > 65536 + 8) + 4
+        src = starts[3] + 2
+        L = 48
+        body[d:d + L] = body[src:src + L]
+        # the first literal ends exactly at the block end, so only the copy
+        # crosses blocks (the block-parallel pass finds it and hands the page
+        # to the per-page pass)
+        comp = (_varint(len(body)) + _snappy_literal(bytes(body[:65536])) +
+                _snappy_literal(bytes(body[65536:d])) +
+                bytes([2 | ((L - 1) << 2)]) + (d - src).to_bytes(2, "little") +
+                _snappy_literal(bytes(body[d + L:])))
+        assert d - src < 65536 and d - src > d - 65536
     # the values as written, re-read from the body
     out, q = [], 4 + len(levels)
     for _ in vals:
@@ -162,6 +172,11 @@ def cross_block_file(path, rng):
     h.i32(2, 0)
     h.i32(3, 3)
     h.i32(4, 3)
+    if stats_bytes:
+        h.begin(5)  # Statistics: max_value (5), min_value (6)
+        h.string(5, rng.integers(0, 256, stats_bytes, dtype=np.uint8).tobytes())
+        h.string(6, rng.integers(0, 256, stats_bytes, dtype=np.uint8).tobytes())
+        h.end()
     h.end()
     h.b.append(0)
     chunk = bytes(h.b) + comp
@@ -266,6 +281,13 @@ def main():
         "geometry").to_pylist()
     assert got == vals, "pyarrow reads the hand-built file differently"
     keep("cross_block_snappy_v1", vals)
+
+    vals = cross_block_file(os.path.join(outdir, "big_header_snappy_v1.parquet"), rng,
+                            stats_bytes=3000)
+    got = pq.read_table(os.path.join(outdir, "big_header_snappy_v1.parquet")).column(
+        "geometry").to_pylist()
+    assert got == vals, "pyarrow reads the hand-built file differently"
+    keep("big_header_snappy_v1", vals)
 
     np.savez_compressed(os.path.join(HERE, "parquet_expected.npz"), **expected)
     for f in sorted(os.listdir(outdir)):
