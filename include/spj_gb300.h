@@ -98,9 +98,10 @@ int SpjJoinFinishBuild(SpjJoin* join);
  *   "order_tiles"       -1 (default: auto, tiles of 524,288 candidates),
  *                       0-16: build-major order within 2^n equal tiles of
  *                       the probes' Morton-ordered candidate list
- *   "refine_min_blocks" 0 (default: auto, 6 in build-major candidate order,
- *                       else 4), 4 or 6: FP32 refine built for that many
- *                       resident 256-thread blocks per SM (fewer registers)
+ *   "refine_min_blocks" 0 (default: auto, 6 for ST_Intersects / ST_Disjoint
+ *                       in build-major candidate order, else 4), 4 or 6:
+ *                       FP32 refine built for that many resident 256-thread
+ *                       blocks per SM (fewer registers)
  *   "refine_split"      2 (default: auto, on unless the candidates are in
  *                       build-major order), 1 on, 0 off: FP32 refine of
  *                       relation predicates in two passes (a cheap pass over

@@ -237,7 +237,8 @@ uint64_t JoinEngine::probe(Workspace& ws, const WkbDeviceColumn& col, int predic
   reset_status(ws.status, s);
   ws.flags.reserve(m + 1, s);
   uint32_t *rq = nullptr, *rqn = nullptr;
-  const int mb = refine_blocks(cfg_.refine_min_blocks, build_major);
+  const int mb = refine_blocks(cfg_.refine_min_blocks, build_major,
+                               predicate == kIntersects || predicate == kDisjoint);
   const bool split = cfg_.refine_split == 1 || cfg_.refine_split == 3 ||
                      (cfg_.refine_split == 2 && !build_major);
   if (split && cfg_.refine_form == kFastF32 && predicate != kPredDWithin) {

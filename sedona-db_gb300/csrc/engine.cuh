@@ -56,10 +56,12 @@ struct EngineConfig {
   // 40.9 with 256-1024)
   int order_tiles = -1;
   // FP32 refine compiled for this many resident 256-thread blocks per SM
-  // (4 or 6), or 0 auto: 6 in build-major candidate order (a warp's pairs
-  // share one build geometry, and more resident warps hide its load latency
-  // better than registers do: 2M x 50k polygons 58.5 vs 60.5 ms), else 4
-  // (10M points x 50k zones: 96.7 vs 99.4 ms with 6)
+  // (4 or 6), or 0 auto: 6 for ST_Intersects / ST_Disjoint in build-major
+  // candidate order (a warp's pairs share one build geometry, and more
+  // resident warps hide its load latency better than registers do: 2M x
+  // 50k polygons 41.0 vs 43.4 ms), else 4 (the containment and touch tests'
+  // deeper calls want the registers: ST_Contains on the same inputs 77.1 vs
+  // 78.3 ms; 10M points x 50k zones: 96.7 vs 99.4 ms with 6)
   int refine_min_blocks = 0;
   // per-ring cell grids on the build side (clean cells answer point-in-ring
   // tests in O(1)); set before the build
@@ -91,9 +93,10 @@ inline uint64_t order_tile_count(int configured, uint64_t m) {
   return m / kOrderTileCandidates > 1 ? m / kOrderTileCandidates : 1;
 }
 
-// refine_min_blocks as configured, with 0 (auto) resolved by the candidate order
-inline int refine_blocks(int configured, bool build_major) {
-  return configured ? configured : (build_major ? 6 : 4);
+// refine_min_blocks as configured, with 0 (auto) resolved by the candidate order and
+// the predicate (intersects: ST_Intersects or ST_Disjoint)
+inline int refine_blocks(int configured, bool build_major, bool intersects = true) {
+  return configured ? configured : (build_major && intersects ? 6 : 4);
 }
 constexpr uint64_t kMaxSlotBytes = 8ull << 30;  // cap of the fused ST_DWithin slot buffer
 
