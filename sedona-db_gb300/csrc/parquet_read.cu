@@ -2,11 +2,14 @@
 // the SpjParquet* entry points.
 //
 // One read (all on the handle's stream, one H2D copy of the chunk bytes):
-//   host           footer (parsed at open); chunk bytes -> page-locked
-//                  buffer; page headers -> page table; while the bytes are
-//                  copied, the Snappy block index of each compressed page
-//                  (snappy_block_index: a chain of element headers, walked
-//                  on host threads)
+//   host           footer (parsed at open); page headers read from the file
+//                  -> page table; chunk bytes -> page-locked buffer in
+//                  groups of whole pages on host threads, each of which
+//                  builds the Snappy block index of the pages it read
+//                  (snappy_block_index: a chain of element headers) while
+//                  they are in cache.  A header longer than the read
+//                  window: all chunk bytes first, the index while they are
+//                  copied
 //   k_snappy_frags warp per 64 KiB output block: each element's bytes moved
 //                  by the 32 lanes (a back-reference shorter than its length
 //                  repeats its pattern, so every lane's byte is known without
