@@ -9,7 +9,12 @@
 // the digit-major histogram table, (3) a stable block-local ranking of the
 // tile by digit (warp match + per-warp digit counters), a reorder in shared
 // memory, then a scatter whose runs of equal digits land on consecutive
-// addresses.
+// addresses.  With segments, the table is segment-major, so the same passes
+// sort each segment of consecutive tiles in place.
+//
+// Compaction of candidate pairs by 0/1 flags: per-tile counts and their
+// scan, then each tile gathers its survivors in shared memory and writes
+// them as one run (no per-element position array).
 #include "prims.cuh"
 
 namespace spj {
