@@ -461,7 +461,7 @@ int SpjParquetReadWkb(SpjParquet* file, const char* column, int32_t rg_begin, in
 int SpjParquetGetStats(SpjParquet* file, double* ms_device, uint64_t* file_bytes,
                        uint64_t* page_bytes, uint64_t* value_bytes);
 /* The last read's phases (ms, CUDA events): the H2D copy of the chunk bytes,
- * Snappy decompression (k_snappy_scan, k_snappy_frags), page decode
+ * Snappy decompression (k_snappy_frags, k_snappy_pages), page decode
  * (dictionary and data pages: levels, value locations), and the value copy
  * with offsets and validity (k_copy_values, k_offsets64, k_pack_valid). */
 int SpjParquetGetPhases(SpjParquet* file, double* ms_h2d, double* ms_decompress,

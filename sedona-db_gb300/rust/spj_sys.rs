@@ -278,3 +278,220 @@ impl Drop for SpjKnnHandle {
         unsafe { SpjKnnRelease(self.raw) }
     }
 }
+
+// ---------------------------------------------------------------------------
+// GeoParquet -> device, result materialisation and the partitioned join
+// (include/spj_gb300.h): the readers and operators of sedona-geoparquet and
+// sedona-spatial-join call these in place of their CPU paths.
+
+/// An Arrow binary / large_binary column whose buffers are in device memory.
+#[repr(C)]
+#[derive(Clone, Copy)]
+pub struct SpjDeviceWkb {
+    pub length: i64,
+    pub offsets: *const c_void,
+    pub offsets_are_64bit: i32,
+    pub data: *const u8,
+    pub data_length: u64,
+    pub validity: *const u8,
+    pub validity_offset: i64,
+}
+
+/// A WKB column (Arrow binary / large_binary layout) in host memory.
+#[repr(C)]
+pub struct SpjHostWkb {
+    pub length: i64,
+    pub offsets: *const c_void,
+    pub offsets_are_64bit: i32,
+    pub data: *const u8,
+    pub validity: *const u8,
+    pub validity_offset: i64,
+}
+
+#[repr(C)]
+pub struct SpjParquet {
+    _private: [u8; 0],
+}
+
+#[repr(C)]
+pub struct SpjParquetWriteOptions {
+    pub compression: i32,
+    pub page_version: i32,
+    pub row_group_rows: i64,
+    pub page_bytes: i64,
+}
+
+#[repr(C)]
+pub struct SpjPartitionOptions {
+    pub num_partitions: u32,
+    pub sample_rows: u32,
+    pub build_budget_bytes: u64,
+    pub seed: u64,
+    pub host_gather: i32,
+    pub record_layout: i32,
+}
+
+#[repr(C)]
+#[derive(Default)]
+pub struct SpjPartitionStats {
+    pub partitions: u32,
+    pub passes: u32,
+    pub build_rows_max: u64,
+    pub probe_rows_multi: u64,
+    pub probe_rows_none: u64,
+    pub probe_rows_probed: u64,
+    pub pairs: u64,
+    pub ms_boxes: f64,
+    pub ms_partition: f64,
+    pub ms_passes: f64,
+    pub direct_host_reads: i32,
+}
+
+pub const SPJ_NULL_INDEX: u32 = 0xFFFF_FFFF;
+
+extern "C" {
+    pub fn SpjJoinBuildDevice(join: *mut SpjJoin, column: *const SpjDeviceWkb) -> c_int;
+
+    pub fn SpjParquetOpen(path: *const c_char, out: *mut *mut SpjParquet) -> c_int;
+    pub fn SpjParquetRelease(file: *mut SpjParquet);
+    pub fn SpjParquetLastError(file: *mut SpjParquet) -> *const c_char;
+    pub fn SpjParquetInfo(
+        file: *mut SpjParquet,
+        num_rows: *mut i64,
+        num_row_groups: *mut i32,
+        num_columns: *mut i32,
+    ) -> c_int;
+    pub fn SpjParquetColumnName(file: *mut SpjParquet, i: i32, buf: *mut c_char, cap: u64) -> c_int;
+    pub fn SpjParquetRowGroupRows(file: *mut SpjParquet, row_group: i32, rows: *mut i64) -> c_int;
+    pub fn SpjParquetReadWkb(
+        file: *mut SpjParquet,
+        column: *const c_char,
+        rg_begin: i32,
+        rg_end: i32,
+        device: i32,
+        out: *mut SpjDeviceWkb,
+    ) -> c_int;
+    pub fn SpjParquetWriteWkb(
+        path: *const c_char,
+        column: *const c_char,
+        length: i64,
+        offsets: *const c_void,
+        offsets_are_64bit: i32,
+        data: *const u8,
+        validity: *const u8,
+        validity_offset: i64,
+        options: *const SpjParquetWriteOptions,
+    ) -> c_int;
+
+    pub fn SpjMaterializeLastError() -> *const c_char;
+    pub fn SpjGatherFixed(
+        d_values: *const c_void,
+        width: u32,
+        n_values: u64,
+        d_idx: *const u32,
+        n: u64,
+        d_out: *mut c_void,
+        stream: *mut c_void,
+    ) -> c_int;
+    pub fn SpjGatherValidity(
+        d_validity: *const u8,
+        validity_offset: i64,
+        n_values: u64,
+        d_idx: *const u32,
+        n: u64,
+        d_out_bitmap: *mut u8,
+        null_count: *mut u64,
+        stream: *mut c_void,
+    ) -> c_int;
+    pub fn SpjGatherBinary(
+        d_offsets: *const c_void,
+        offsets_are_64bit: i32,
+        d_data: *const u8,
+        n_values: u64,
+        d_idx: *const u32,
+        n: u64,
+        d_out_offsets: *mut i64,
+        d_out_data: *mut u8,
+        capacity: u64,
+        out_bytes: *mut u64,
+        stream: *mut c_void,
+    ) -> c_int;
+    pub fn SpjVisitedMark(
+        d_bitmap: *mut u32,
+        n_rows: u64,
+        d_idx: *const u32,
+        n: u64,
+        stream: *mut c_void,
+    ) -> c_int;
+    pub fn SpjVisitedCollect(
+        d_bitmap: *const u32,
+        n_rows: u64,
+        visited: i32,
+        d_out_idx: *mut u32,
+        capacity: u64,
+        count: *mut u64,
+        stream: *mut c_void,
+    ) -> c_int;
+
+    pub fn SpjJoinPartitioned(
+        join: *mut SpjJoin,
+        build: *const SpjHostWkb,
+        probe: *const SpjHostWkb,
+        predicate: i32,
+        distance: f64,
+        options: *const SpjPartitionOptions,
+        callback: PairCallback,
+        user_data: *mut c_void,
+        stats: *mut SpjPartitionStats,
+    ) -> c_int;
+}
+
+/// A GeoParquet file opened for device reads (sedona-geoparquet's
+/// file_opener.rs reads the geometry column through this instead of
+/// arrow-rs when the scan feeds a GPU join).
+pub struct SpjParquetFile {
+    raw: *mut SpjParquet,
+}
+
+impl SpjParquetFile {
+    pub fn open(path: &CStr) -> Result<Self, String> {
+        let mut raw = ptr::null_mut();
+        let rc = unsafe { SpjParquetOpen(path.as_ptr(), &mut raw) };
+        if rc != 0 {
+            return Err(format!("SpjParquetOpen: {}", message(unsafe { SpjParquetLastError(ptr::null_mut()) })));
+        }
+        Ok(Self { raw })
+    }
+
+    /// Row groups [rg_begin, rg_end) of a WKB column (None: the primary
+    /// geometry column) as a device column, valid until the next read.
+    pub fn read_wkb(
+        &mut self,
+        column: Option<&CStr>,
+        rg_begin: i32,
+        rg_end: i32,
+        device: i32,
+    ) -> Result<SpjDeviceWkb, String> {
+        let mut out = SpjDeviceWkb {
+            length: 0,
+            offsets: ptr::null(),
+            offsets_are_64bit: 1,
+            data: ptr::null(),
+            data_length: 0,
+            validity: ptr::null(),
+            validity_offset: 0,
+        };
+        let col = column.map_or(ptr::null(), |c| c.as_ptr());
+        let rc = unsafe { SpjParquetReadWkb(self.raw, col, rg_begin, rg_end, device, &mut out) };
+        if rc != 0 {
+            return Err(format!("SpjParquetReadWkb: {}", message(unsafe { SpjParquetLastError(self.raw) })));
+        }
+        Ok(out)
+    }
+}
+
+impl Drop for SpjParquetFile {
+    fn drop(&mut self) {
+        unsafe { SpjParquetRelease(self.raw) }
+    }
+}

@@ -103,3 +103,38 @@ def test_option_keys_documented():
     documented = set(re.findall(r'^ \*   "([a-z_]+)"', block, re.M))
     assert accepted, "no option keys found"
     assert accepted == documented, (accepted ^ documented)
+
+
+def test_rust_bindings_name_declared_functions(lib):
+    """Every function the Rust bindings (sedona-db_gb300/rust/spj_sys.rs)
+    declare is declared in include/spj_gb300.h and exported by the library,
+    and every #[repr(C)] struct they mirror has the header's field names in
+    the header's order."""
+    src = open(os.path.join(ROOT, "sedona-db_gb300", "rust", "spj_sys.rs")).read()
+    rust_fns = sorted(set(re.findall(r"pub fn (Spj\w+)\s*\(", src)))
+    assert len(rust_fns) > 20
+    declared = set(declared_functions())
+    missing = [f for f in rust_fns if f not in declared]
+    assert not missing, missing
+    for f in rust_fns:
+        getattr(lib, f)
+    hdr = open(os.path.join(ROOT, "include", "spj_gb300.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    for name, body in re.findall(
+            r"#\[repr\(C\)\]\n(?:#\[derive\([^)]*\)\]\n)?pub struct (Spj\w+) \{(.*?)\n\}", src,
+            flags=re.S):
+        if "_private" in body:
+            continue
+        rust_fields = re.findall(r"pub (\w+):", body)
+        m = re.search(r"struct " + name + r" \{(.*?)\};", hdr, flags=re.S)
+        assert m, name
+        c_fields = []
+        for decl in m.group(1).split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            # "uint32_t partitions, passes" declares two fields
+            head, *rest = [p.strip() for p in decl.split(",")]
+            c_fields.append(re.findall(r"\w+", head)[-1])
+            c_fields.extend(rest)
+        assert rust_fields == c_fields, (name, rust_fields, c_fields)
