@@ -201,7 +201,8 @@ constexpr uint32_t kFragBytes = 1u << 16;  // Snappy's compression block
 constexpr uint64_t kHeaderWindow = 4096;   // bytes read per page header from the file
 constexpr uint64_t kReadGroup = 4ull << 20;  // bytes of whole pages per reader-thread read
 constexpr uint32_t kFragWin = 2048;        // per warp, k_snappy_frags (headers, literals)
-constexpr uint32_t kWalkWin = 8192;        // per warp, PLAIN walks
+constexpr uint32_t kWalkWin = 16384;       // per warp, PLAIN walks
+constexpr int kWalkThreads = 128;          // 4 walking warps per block
 enum PageMode : uint8_t { kModeStored = 0, kModeFragments = 1, kModeSequential = 2, kModeBad = 3 };
 
 // One Snappy element header at position ip of the window's range: output
@@ -1192,22 +1193,24 @@ extern "C" int SpjParquetReadWkb(SpjParquet* p, const char* column, int32_t rg_b
           dpages, np, dsrc, dpb, p->mode.as<uint8_t>(), st);
     }
     SPJ_CUDA(cudaEventRecord(p->ev[2], s));
-    const int g = grid_for((int64_t)np * 32, 256, kNumSMs * 16);
-    const int walk_smem = 8 * (kWalkWin + 16);
+    // a walk restages its window when it runs past it: 16 KiB windows halve
+    // the restages, and 4 warps per block keep a block's windows at 64 KiB
+    const int g = grid_for((int64_t)np * 32, kWalkThreads, kNumSMs * 16);
+    const int walk_smem = (kWalkThreads / 32) * (kWalkWin + 16);
     if (np) {
       SPJ_CUDA(cudaFuncSetAttribute(k_dict_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     walk_smem));
       SPJ_CUDA(cudaFuncSetAttribute(k_data_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     walk_smem));
       if (ndict)
-        k_dict_pages<<<g, 256, walk_smem, s>>>(dpages, np, dsrc, dpb,
+        k_dict_pages<<<g, kWalkThreads, walk_smem, s>>>(dpages, np, dsrc, dpb,
                                                p->dict_base.as<uint64_t>(),
                                                p->dict_ptr.as<uint64_t>(),
                                                p->dict_len.as<uint32_t>(), st);
       RowArrays ra{p->valid.as<uint8_t>(),    p->tmp_ptr.as<uint64_t>(),
                    p->tmp_len.as<uint32_t>(), p->vptr.as<uint64_t>(),
                    p->vlen.as<uint32_t>(),    p->nulls.as<unsigned long long>()};
-      k_data_pages<<<g, 256, walk_smem, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
+      k_data_pages<<<g, kWalkThreads, walk_smem, s>>>(dpages, np, dsrc, dpb, p->dict_base.as<uint64_t>(),
                                      p->dict_n.as<uint32_t>(), p->dict_ptr.as<uint64_t>(),
                                      p->dict_len.as<uint32_t>(), ra, st);
       SPJ_CUDA(cudaGetLastError());
